@@ -1,0 +1,198 @@
+/*
+ * salsa_gb300.h -- C-ABI of the GB300 SALSA microphysics step.
+ *
+ * This library replaces the body of UCLALES-SALSA's per-grid-cell microphysics
+ * driver, src/src_salsa/mo_salsa_driver.f90:112-435 (SUBROUTINE run_SALSA), and
+ * everything it calls below it (mo_salsa.f90:45-153 SUBROUTINE salsa and the
+ * process modules).  The arrays keep run_SALSA's layout: every field is a
+ * column-major (Fortran order) array with z fastest,
+ *     index(kk, ii, jj, b) = kk + nzp*(ii + nxp*(jj + nyp*b))      (0-based)
+ * and a per-species mass array of a category with nb bins stores bin b of
+ * species s at last index s*nb + b  (util.f90:955-961 getMassIndex, 0-based).
+ * Only interior cells are touched: kk = 1..nzp-2, ii = 2..nxp-3, jj = 2..nyp-3
+ * (0-based; mo_salsa_driver.f90:180-182 loops jj=3..nyp-2, ii=3..nxp-2,
+ * kk=nzp-1..2 in 1-based indexing).
+ *
+ * Units at the boundary are those of the LES: numbers #/kg, masses kg/kg,
+ * pressure Pa, temperature K, mixing ratios kg/kg, air density kg/m3.
+ *
+ * Every pointer in salsa_fields_t may point to host memory or to device memory
+ * of the handle's GPU (all pointers of one call must be on the same side).  For
+ * host pointers the library copies the fields to the GPU and the results back
+ * inside the call.  The call is synchronous.
+ *
+ * Threading: a handle is not reentrant; distinct handles are independent (no
+ * global mutable state).  The reference module state (allSALSA, zcc**, rateDiag)
+ * lives per cell on the GPU.
+ */
+#ifndef SALSA_GB300_H
+#define SALSA_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Limits of the bin layout supported by one handle. */
+#define SALSA_MAXSPEC 7      /* dry species (classSpecies.f90 maxspec) */
+#define SALSA_MAXNSP 9       /* dry + H2O + rime */
+#define SALSA_MAXBINS 96     /* ntotal = nbins + ncld + nprc + nice */
+
+/* Diagnostic process-rate fields, in the order of mo_salsa_driver.f90:392-411. */
+enum {
+  SALSA_DIAG_AUTOC = 0,    /* s_m_autoc      */
+  SALSA_DIAG_AUTOC80,      /* s_m_autoc80    */
+  SALSA_DIAG_AUTOC50,      /* s_m_autoc50    */
+  SALSA_DIAG_ACCR,         /* s_m_accr       */
+  SALSA_DIAG_ACCR80,       /* s_m_accr80     */
+  SALSA_DIAG_ACCR50,       /* s_m_accr50     */
+  SALSA_DIAG_ACCOLL,       /* s_m_ACcoll_dry */
+  SALSA_DIAG_APCOLL,       /* s_m_APcoll_dry */
+  SALSA_DIAG_ACTIV,        /* s_n_activ      */
+  SALSA_DIAG_CONDA,        /* s_m_conda      */
+  SALSA_DIAG_CONDC,        /* s_m_condc      */
+  SALSA_DIAG_CONDP,        /* s_m_condp      */
+  SALSA_DIAG_AICOLL,       /* s_m_AIcoll_dry (level 5) */
+  SALSA_DIAG_ICEHOM,       /* s_n_icehom     (level 5) */
+  SALSA_DIAG_ICEDEP,       /* s_n_icedep     (level 5) */
+  SALSA_DIAG_ICEIMM,       /* s_n_iceimm     (level 5) */
+  SALSA_DIAG_CONDI,        /* s_m_condi      (level 5) */
+  SALSA_NDIAG
+};
+
+/* ProcessSwitch (classProcessSwitch.f90:5-14): state is derived per call. */
+typedef struct {
+  int sw;          /* %switch */
+  double delay;    /* %delay [s] */
+  int mode;        /* %mode */
+} salsa_switch_t;
+
+/* POD mirror of the &salsa NAMELIST (mo_salsa_init.f90:522-600) plus the
+ * arguments of define_salsa(level) and salsa_initialize(chargeTmax,
+ * chargeCollEnh) (mo_salsa_init.f90:465, 792).  Defaults: salsa_gb300_default_config. */
+typedef struct {
+  int level;                                  /* thermodynamic level, 4 or 5 */
+  salsa_switch_t lscoag, lscnd, lsauto, lsactiv, lsicenucl, lsicemelt, lssecice;
+  int lscgaa, lscgcc, lscgca, lscgpc, lscgpa, lscgpp, lscgia, lscgic, lscgii, lscgip;
+  double Eiagg_max, Eiagg_min;
+  double cgintvl;
+  int lscndgas, lscndh2oae, lscndh2ocl, lscndh2oic;
+  int lsicehom, lsiceimm, lsicedep;
+  int ice_theta_dist;
+  salsa_switch_t lsFreeTheta;
+  double initMinTheta;
+  double mean_theta_imm, sigma_theta_imm, mean_theta_dep, sigma_theta_dep;
+  double iceShapeAlpha, iceShapeBeta, iceShapeGamma, iceShapeSigma;
+  int lsdistupdate;
+  int lscheckarrays;
+  double fixinc;
+  salsa_switch_t lsfreeRH;
+  double rhlim;
+  double eddy_dis;
+  int nsnucl, nj3;
+  double act_coeff;
+  /* bin layout: aerosol regimes (mo_submctl.f90:208-212), precip and ice BinLayout */
+  int nbin[2];
+  double reglim[4];
+  int prc_nbins;  double prc_dlo, prc_vol_ratio;
+  int ice_nbins;  double ice_dlo, ice_vol_ratio;
+  /* species: nspec_dry names out of SO4 OC BC DU SS NO NH, in mass-array order */
+  int nspec_dry;
+  char listspec[SALSA_MAXSPEC][4];
+  /* salsa_initialize arguments */
+  double chargeTMax, chargeCollEnh;
+  /* ---- GB300 extensions (no counterpart in the reference) ---- */
+  int precision;     /* 0: FP64 (parity form); 1: FP32-mixed form */
+  int diagnostics;   /* 1: accumulate process-rate diagnostics; 0: skip them */
+} salsa_config_t;
+
+/* Array arguments of run_SALSA (mo_salsa_driver.f90:112-133) after the Diag/Prog
+ * getData lookups (:481-561).  "t" suffix = tendency (time level 2), in/out:
+ * the library ADDS (new-old)/tstep to it.  NULL is allowed for arrays that the
+ * configuration does not use (rsi/nice/mice/micet/indef at level 4, chargeTime
+ * without lcharge, gaerot without lscndgas, wp without cloud-base activation,
+ * any diag entry). */
+typedef struct {
+  const double *press, *temp, *rsl, *rsi, *dn;    /* (nzp,nxp,nyp) */
+  const double *rp;  double *rpt;                 /* water vapour mixing ratio and its tendency */
+  const double *wp;                               /* vertical velocity */
+  const double *naero, *ncloud, *nprecp, *nice;   /* (...,nbins|ncld|nprc|nice) #/kg */
+  double *naerot, *ncloudt, *nprecpt, *nicet;
+  const double *maero, *mcloud, *mprecp, *mice;   /* (...,nwet*nb | (nwet+1)*nice) kg/kg */
+  double *maerot, *mcloudt, *mprecpt, *micet;
+  double *indef;        /* (...,nliquid) in/out: IN nucleated fraction (level 5, ice_theta_dist) */
+  double *chargeTime;   /* (...,nliquid) in/out: charging time tracer (lcharge) */
+  const double *gaero;  double *gaerot;           /* (...,5) gases #/kg */
+  double *pa_nactd;     /* (...,ncld) out */
+  double *pa_vactd;     /* (...,ns*ncld) out */
+  double *diag[SALSA_NDIAG];                      /* (nzp,nxp,nyp) out */
+  /* GB300 extension: per-cell hygroscopicity override (NULL = species tables) */
+  const double *kappa;
+} salsa_fields_t;
+
+/* Per-call status.  The reference STOPs or prints in these situations; the
+ * library records them per cell, finishes the step and returns nonzero. */
+typedef struct {
+  int code;                       /* 0 ok, else SALSA_E_* */
+  long long n_cells;              /* interior cells processed */
+  long long n_equil_nonconv;      /* equilibration > 100 iterations (mo_salsa_properties.f90:242,356) */
+  long long n_distr_nonconv;      /* distr_update > 100 passes (mo_salsa_update.f90:138,231,329,424) */
+  long long n_distr_negfrac;      /* zvfrac < 0 (mo_salsa_update.f90:111,204,302,397) */
+  long long n_cond_substeps;      /* > 100 condensation substeps (mo_salsa_dynamics.f90:1051) */
+  long long n_negative;           /* numc < -1e-6 after coagulation (mo_salsa_dynamics.f90:192) */
+  long long n_nonfinite;          /* NaN/Inf in the new state */
+} salsa_status_t;
+
+enum {
+  SALSA_OK = 0,
+  SALSA_E_ARG = 1,          /* NULL pointer / bad dimension / bad config value */
+  SALSA_E_UNSUPPORTED = 2,  /* configuration outside what this build implements */
+  SALSA_E_CUDA = 3,         /* CUDA runtime error */
+  SALSA_E_NUMERIC = 4,      /* a per-cell condition above occurred */
+  SALSA_E_NODEV = 5         /* no usable GPU */
+};
+
+typedef struct salsa_handle salsa_handle_t;
+
+/* Fill *cfg with the reference defaults (mo_submctl.f90, mo_ice_shape.f90,
+ * classProcessSwitch.f90, mo_salsa_init.f90:687-695). */
+void salsa_gb300_default_config(salsa_config_t *cfg);
+
+/* Replaces define_salsa(level) + salsa_initialize(chargeTmax, chargeCollEnh)
+ * (mo_salsa_init.f90:465-637, 792-858): builds species and bin tables on the
+ * host and uploads them to the current CUDA device. */
+int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out);
+
+/* Replaces run_SALSA(Diag, Prog, nzp, nxp, nyp, ns, wp, pa_nactd, pa_vactd,
+ * tstep, time, istp, level, lcharge, initialize)  (mo_salsa_driver.f90:112-435). */
+int salsa_gb300_run(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
+                    double tstep, double time, int istp, int level, int lcharge,
+                    int initialize, const salsa_fields_t *f, salsa_status_t *st);
+
+/* Same as salsa_gb300_run but enqueued on the caller's CUDA stream (a
+ * cudaStream_t passed as void*); all field pointers must be device pointers.
+ * Status counters are written to st after the stream reaches the end of the
+ * step only if sync != 0. */
+int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
+                          double tstep, double time, int istp, int level, int lcharge,
+                          int initialize, const salsa_fields_t *f, void *stream,
+                          int sync, salsa_status_t *st);
+
+/* Bin layout queries (mo_submctl.f90 nbins/ncld/nprc/nice and the diameter
+ * limit tables aerobins/cloudbins/precpbins/icebins, mo_salsa_init.f90:236-239). */
+int salsa_gb300_layout(const salsa_handle_t *h, int *nbins, int *ncld, int *nprc,
+                       int *nice, int *nwet, double *lolim_diam /* ntotal or NULL */);
+
+/* Number of kernel launches the last run issued (for launch accounting). */
+int salsa_gb300_last_launches(const salsa_handle_t *h);
+
+/* Average device time in ms of the dominant (step) kernel over the last run. */
+double salsa_gb300_last_kernel_ms(const salsa_handle_t *h);
+
+void salsa_gb300_finalize(salsa_handle_t *h);
+
+const char *salsa_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

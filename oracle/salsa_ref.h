@@ -1,0 +1,61 @@
+/*
+ * salsa_ref.h -- CPU oracle of the SALSA microphysics step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C FP64 restatement of the
+ * reference Fortran path run_SALSA -> salsa (UCLALES-SALSA
+ * src/src_salsa/mo_salsa_driver.f90:112-435, mo_salsa.f90:45-153 and the
+ * process modules), used by the tests as the parity checker and by bench.py as
+ * the timed CPU baseline.  The product library never links or calls it.
+ *
+ * Parity status: the reference is Fortran and no Fortran compiler exists in
+ * this environment, and the reference ships no tests, golden vectors or
+ * fixtures for this path.  The restatement is therefore "parity unpinned"
+ * against the real Fortran; it is pinned instead by closed-form checks in
+ * tests/ (flux-matching limits, semi-implicit single-pair update, Koehler
+ * equilibrium, water conservation by construction) and by committed golden
+ * vectors of its own outputs (tests/golden/).
+ *
+ * Interface: same structs as the product C-ABI (include/salsa_gb300.h).
+ */
+#ifndef SALSA_REF_H
+#define SALSA_REF_H
+#include "../include/salsa_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct salsa_ref_ctx salsa_ref_ctx_t;
+
+int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out);
+void salsa_ref_destroy(salsa_ref_ctx_t *ctx);
+
+/* Same argument meaning as salsa_gb300_run; host pointers only.
+ * nthreads <= 0: use all OpenMP threads.  carry_over != 0 reproduces the
+ * reference's serial module-state carry-over between cells (allSALSA keeps the
+ * previous cell's derived diameters); 0 resets them per cell (the GPU
+ * semantics, every cell sees the post-initialisation module state). */
+int salsa_ref_run(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, int ns,
+                  double tstep, double time, int istp, int level, int lcharge,
+                  int initialize, const salsa_fields_t *f, salsa_status_t *st,
+                  int nthreads, int carry_over);
+
+int salsa_ref_layout(const salsa_ref_ctx_t *ctx, int *nbins, int *ncld, int *nprc,
+                     int *nice, int *nwet, double *lolim_diam);
+
+/* Work-unit counters accumulated over the last run: [0] coagc evaluations,
+ * [1] acth2o calls, [2] J_imm evaluations, [3] equilibration iterations,
+ * [4] condensation substeps. */
+void salsa_ref_counters(const salsa_ref_ctx_t *ctx, long long out[5]);
+
+/* Single-function probes used by the closed-form tests. */
+double salsa_ref_terminal_vel(double diam, double rhop, double rhoa, double visc,
+                              double beta, int flag);
+double salsa_ref_coagc_pair(const salsa_ref_ctx_t *ctx, int b1, int b2,
+                            double numc1, double dwet1, double numc2,
+                            double dwet2, double temp, double pres);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,73 @@
+"""ctypes access to the CPU oracle (oracle/salsa_ref.c) for the tests.
+
+The oracle is test infrastructure: it is loaded only by tests/, by
+__graft_entry__.smoke() and by bench.py's CPU-baseline leg.
+"""
+import ctypes as C
+import os
+import subprocess
+
+from uclales_salsa_gb300.capi import Config, Fields, Status, make_fields
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "oracle", "_build", "libsalsa_ref.so")
+_lib = None
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build_oracle()
+        L = C.CDLL(LIB)
+        L.salsa_ref_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_void_p)]
+        L.salsa_ref_create.restype = C.c_int
+        L.salsa_ref_destroy.argtypes = [C.c_void_p]
+        L.salsa_ref_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Fields), C.POINTER(Status),
+                                    C.c_int, C.c_int]
+        L.salsa_ref_run.restype = C.c_int
+        L.salsa_ref_layout.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 5 + [C.POINTER(C.c_double)]
+        L.salsa_ref_counters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong * 5)]
+        L.salsa_ref_terminal_vel.argtypes = [C.c_double] * 5 + [C.c_int]
+        L.salsa_ref_terminal_vel.restype = C.c_double
+        L.salsa_ref_coagc_pair.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 6
+        L.salsa_ref_coagc_pair.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    def __init__(self, cfg):
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        rc = lib().salsa_ref_create(C.byref(cfg), C.byref(self.h))
+        if rc != 0:
+            raise RuntimeError(f"salsa_ref_create failed: {rc}")
+
+    def run(self, inp, fields, outputs, time=1.0, istp=1, initialize=0, lcharge=0, nthreads=0, carry_over=0):
+        f = make_fields(fields, outputs)
+        st = Status()
+        rc = lib().salsa_ref_run(self.h, inp.nzp, inp.nxp, inp.nyp, inp.ns, inp.dt, time, istp, inp.level,
+                                 lcharge, initialize, C.byref(f), C.byref(st), nthreads, carry_over)
+        return rc, st
+
+    def layout(self):
+        v = [C.c_int() for _ in range(5)]
+        arr = (C.c_double * 96)()
+        lib().salsa_ref_layout(self.h, *[C.byref(x) for x in v], arr)
+        return [x.value for x in v], list(arr)
+
+    def counters(self):
+        a = (C.c_longlong * 5)()
+        lib().salsa_ref_counters(self.h, C.byref(a))
+        return list(a)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().salsa_ref_destroy(self.h)
+            self.h = None

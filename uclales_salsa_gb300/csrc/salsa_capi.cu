@@ -1,0 +1,634 @@
+// salsa_capi.cu -- host side of the C-ABI in include/salsa_gb300.h.
+//
+// salsa_gb300_init replaces define_salsa + salsa_initialize
+// (src/src_salsa/mo_salsa_init.f90:465-637, 792-858): it validates the &salsa
+// configuration, builds the species tables (src/src_shared/classSpecies.f90:167-341)
+// and the bin layout (mo_salsa_init.f90:148-450), and uploads the per-block tables,
+// the I/O row table and the collision-pair table to the GPU.
+// salsa_gb300_run replaces run_SALSA (mo_salsa_driver.f90:112-435): it resolves the
+// process-switch states (set_SALSA_runtime :445-474), stages host arrays when the
+// caller passes host memory, and launches the fused step kernel.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/salsa_gb300.h"
+#include "salsa_device.cuh"
+
+namespace salsa {
+cudaError_t launch_d0(const DevParams &, cudaStream_t, int);
+cudaError_t launch_d1(const DevParams &, cudaStream_t, int);
+cudaError_t launch_f0(const DevParams &, cudaStream_t, int);
+cudaError_t launch_f1(const DevParams &, cudaStream_t, int);
+int blocks_per_sm_d0(const DevParams &);
+int blocks_per_sm_d1(const DevParams &);
+int blocks_per_sm_f0(const DevParams &);
+int blocks_per_sm_f1(const DevParams &);
+}  // namespace salsa
+
+using salsa::DevParams;
+using salsa::Row;
+
+namespace {
+
+const double PI6 = 0.5235988;   // mo_submctl.f90:266
+const char *ALLNAMES[9] = {"SO4", "OC", "BC", "DU", "SS", "NO", "NH", "H2O", "rime"};
+const double ALLMM[9] = {98.08e-3, 150.e-3, 12.e-3, 100.e-3, 58.44e-3, 62.01e-3, 18.04e-3, 18.016e-3, 18.016e-3};
+const double ALLRHO[9] = {1830., 1400., 2000., 2650., 2165., 1479., 1530., 1000., 400.};
+const double ALLDISS[9] = {3., 1., 0., 0., 2., 1., 1., 1., 1.};
+
+bool name_eq(const char *a, const char *b) {
+  char x[5] = {0}, y[5] = {0};
+  strncpy(x, a, 4);
+  strncpy(y, b, 4);
+  for (int i = 3; i >= 0 && (x[i] == ' ' || x[i] == 0); i--) x[i] = 0;
+  for (int i = 3; i >= 0 && (y[i] == ' ' || y[i] == 0); i--) y[i] = 0;
+  return strcmp(x, y) == 0;
+}
+
+struct BinTab {
+  std::vector<double> vlo, vhi, vrlo, vrhi, dmid;
+};
+
+void set_bin(BinTab &t, int b, double vlo, double vhi) {
+  t.vlo[b] = vlo;
+  t.vhi[b] = vhi;
+  t.dmid[b] = std::pow((vhi + vlo) / (2. * PI6), 1. / 3.);
+  double v = PI6 * t.dmid[b] * t.dmid[b] * t.dmid[b];
+  t.vrhi[b] = vhi / v;
+  t.vrlo[b] = vlo / v;
+}
+
+double hcube(double x) { return x * x * x; }
+
+}  // namespace
+
+struct salsa_handle {
+  salsa_config_t cfg;
+  int device = 0, nsm = 0;
+  DevParams base;               // layout part of the kernel parameters
+  double *d_tables = nullptr;
+  Row *d_rows = nullptr;
+  int *d_pairs = nullptr;
+  unsigned long long *d_status = nullptr;
+  unsigned long long *h_status = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<double> lolim_diam;
+  // sticky switch states (set_SALSA_runtime)
+  int st[7] = {0, 0, 0, 0, 0, 0, 0};
+  int st_freeRH = 0, st_freeTheta = 0;
+  // staging buffers for host-pointer calls
+  void *stage = nullptr;
+  size_t stage_bytes = 0;
+  int last_launches = 0;
+  double last_kernel_ms = 0.;
+};
+
+extern "C" {
+
+const char *salsa_gb300_version(void) { return "salsa_gb300 1.0 (sm_103a)"; }
+
+void salsa_gb300_default_config(salsa_config_t *c) {
+  if (!c) return;
+  memset(c, 0, sizeof *c);
+  c->level = 5;
+  salsa_switch_t off = {0, 0., 1};
+  c->lscoag = c->lscnd = c->lsauto = c->lsactiv = c->lsicenucl = c->lsicemelt = c->lssecice = off;
+  c->lsFreeTheta = c->lsfreeRH = off;
+  c->lscgaa = c->lscgcc = c->lscgca = c->lscgpc = c->lscgpa = c->lscgpp = 1;
+  c->lscgia = c->lscgic = c->lscgii = c->lscgip = 1;
+  c->Eiagg_max = 0.3;
+  c->Eiagg_min = 0.05;
+  c->cgintvl = 10.;
+  c->lscndgas = 0;
+  c->lscndh2oae = c->lscndh2ocl = c->lscndh2oic = 1;
+  c->ice_theta_dist = 1;
+  c->mean_theta_imm = 132.;
+  c->sigma_theta_imm = 20.;
+  c->mean_theta_dep = 15.5;
+  c->sigma_theta_dep = 1.4;
+  c->iceShapeAlpha = 15.56999e-3;
+  c->iceShapeBeta = 2.02;
+  c->iceShapeGamma = 0.55;
+  c->iceShapeSigma = 1.97;
+  c->lsdistupdate = 1;
+  c->fixinc = -1.;
+  c->rhlim = 1.20;
+  c->eddy_dis = 0.001;
+  c->nj3 = 1;
+  c->act_coeff = 1.e-7;
+  c->nbin[0] = 3;
+  c->nbin[1] = 8;
+  c->reglim[0] = 3.e-9;
+  c->reglim[1] = 4.e-8;
+  c->reglim[2] = 7.e-7;
+  c->reglim[3] = 1.5e-5;
+  c->prc_nbins = 20;
+  c->prc_dlo = 20.e-6;
+  c->prc_vol_ratio = 2.;
+  c->ice_nbins = 20;
+  c->ice_dlo = 20.e-6;
+  c->ice_vol_ratio = 2.;
+  c->nspec_dry = 1;
+  strcpy(c->listspec[0], "SO4");
+  c->chargeTMax = 1000.;
+  c->chargeCollEnh = 0.;
+  c->precision = 0;
+  c->diagnostics = 1;
+}
+
+int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
+  if (!cfg || !out) return SALSA_E_ARG;
+  *out = nullptr;
+  const salsa_config_t &g = *cfg;
+  if (g.level != 4 && g.level != 5) return SALSA_E_ARG;
+  if (g.nbin[0] < 1 || g.nbin[1] < 4 || g.prc_nbins < 1 || g.ice_nbins < 1) return SALSA_E_ARG;
+  if (g.nspec_dry < 1 || g.nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
+  if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
+  if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
+  // processes outside this build (the init check mirrors the oracle's)
+  if (g.nsnucl != 0 || g.lscndgas || g.lssecice.sw || g.lscoag.mode == 2 || g.lsactiv.mode == 2)
+    return SALSA_E_UNSUPPORTED;
+  if (g.level == 5 && g.fixinc > 0. && !(g.lsicehom || g.lsiceimm || g.lsicedep)) return SALSA_E_UNSUPPORTED;
+  if (g.prc_nbins > 20) return SALSA_E_UNSUPPORTED;   // precipitation-formation accumulators
+  int nb1 = g.nbin[0], nb2 = g.nbin[1];
+  int nbins = nb1 + 2 * nb2, ncld = 2 * nb2, nprc = g.prc_nbins, nice = g.ice_nbins;
+  int ntotal = nbins + ncld + nprc + nice;
+  if (ntotal > SALSA_MAXNB || ntotal > 255) return SALSA_E_ARG;
+
+  // ---- species (classSpecies.f90:167-244, sortProperties :247-272, defineSubsets :275-341) ----
+  int allInd[9], used[9];
+  for (int i = 0; i < 9; i++) { allInd[i] = -1; used[i] = 0; }
+  for (int i = 0; i < g.nspec_dry; i++)
+    for (int k = 0; k < SALSA_MAXSPEC; k++)
+      if (name_eq(ALLNAMES[k], g.listspec[i])) { allInd[k] = i; used[k] = 1; }
+  int cnt = 0;
+  for (int k = 0; k < SALSA_MAXSPEC; k++) cnt += used[k];
+  if (cnt != g.nspec_dry) return SALSA_E_ARG;
+  int nlist = g.nspec_dry;
+  allInd[7] = nlist; used[7] = 1;
+  allInd[8] = nlist + 1; used[8] = 1;
+  DevParams B;
+  memset(&B, 0, sizeof B);
+  B.nused = nlist + 2; B.ndry = nlist; B.nwet = nlist + 1; B.iwa = nlist; B.irim = nlist + 1;
+  for (int k = 0; k < 9; k++) if (used[k]) {
+    int j = allInd[k];
+    B.rholiq[j] = ALLRHO[k];
+    B.rhoice[j] = (k == 7) ? 917. : ALLRHO[k];
+    B.MM[j] = ALLMM[k];
+    B.diss[j] = ALLDISS[k];
+  }
+  for (int j = 0; j < B.nused; j++)
+    for (int k = 0; k < 9; k++) if (used[k] && allInd[k] == j) {
+      if (k == 0 || k == 1 || k == 4 || k == 5 || k == 6) B.ind_soluble[B.nsoluble++] = j;
+      if (k == 2 || k == 3) B.ind_insoluble[B.ninsoluble++] = j;
+    }
+  B.ix_so4 = allInd[0]; B.ix_oc = allInd[1]; B.ix_bc = allInd[2]; B.ix_du = allInd[3];
+  B.ix_ss = allInd[4]; B.ix_no = allInd[5]; B.ix_nh = allInd[6];
+  if (g.level == 5 && g.ice_theta_dist && (g.lsicehom || g.lsiceimm || g.lsicedep) && B.ix_du < 0)
+    return SALSA_E_UNSUPPORTED;   // iceNucleation (mo_salsa_cloud_ice_SE.f90:439) indexes DU
+
+  // ---- bins (mo_salsa_init.f90:148-450, salsa_initialize :806-814) ----
+  B.in1a = 0; B.in2a = B.in1a + nb1; B.in2b = B.in2a + nb2;
+  B.fn1a = B.in2a - 1; B.fn2a = B.fn1a + nb2; B.fn2b = B.fn2a + nb2;
+  B.nbins = nbins; B.ncld = ncld; B.nprc = nprc; B.nice = nice; B.ntotal = ntotal;
+  B.nliquid = nbins + ncld + nprc;
+  B.ica_cur = 0; B.ica_par = B.in2a; B.fca_cur = nb2 - 1;
+  B.icb_cur = nb2; B.icb_par = B.in2b; B.fcb_cur = ncld - 1;
+  BinTab t;
+  t.vlo.assign(ntotal, 0.); t.vhi.assign(ntotal, 0.); t.vrlo.assign(ntotal, 0.); t.vrhi.assign(ntotal, 0.);
+  t.dmid.assign(ntotal, 0.);
+  {
+    const double *rl = g.reglim;
+    double ratio = rl[1] / rl[0];
+    for (int cc = B.in1a; cc <= B.fn1a; cc++)
+      set_bin(t, cc, PI6 * hcube(rl[0] * std::pow(ratio, (double)cc / nb1)),
+              PI6 * hcube(rl[0] * std::pow(ratio, (double)(cc + 1) / nb1)));
+    int nbin2 = 4, nbin3 = nb2 - nbin2;
+    ratio = rl[2] / rl[1];
+    for (int dd = B.in2a; dd <= B.in2a + nbin2 - 1; dd++) {
+      int cc = dd - B.in2a;
+      set_bin(t, dd, PI6 * hcube(rl[1] * std::pow(ratio, (double)cc / nbin2)),
+              PI6 * hcube(rl[1] * std::pow(ratio, (double)(cc + 1) / nbin2)));
+    }
+    ratio = rl[3] / rl[2];
+    for (int dd = B.in2a + nbin2; dd <= B.fn2a; dd++) {
+      int cc = dd - (B.fn2a - (nbin3 - 1));
+      set_bin(t, dd, PI6 * hcube(rl[2] * std::pow(ratio, (double)cc / nbin3)),
+              PI6 * hcube(rl[2] * std::pow(ratio, (double)(cc + 1) / nbin3)));
+    }
+    for (int i = 0; i < nb2; i++) {
+      int a = B.in2a + i, b = B.in2b + i;
+      t.vlo[b] = t.vlo[a]; t.vhi[b] = t.vhi[a]; t.dmid[b] = t.dmid[a]; t.vrlo[b] = t.vrlo[a]; t.vrhi[b] = t.vrhi[a];
+    }
+    // cloud bins parallel to 2a and 2b (set_cloudbins :311-324)
+    for (int i = 0; i < nb2; i++) {
+      for (int r = 0; r < 2; r++) {
+        int a = (r == 0 ? B.in2a : B.in2b) + i, c = nbins + r * nb2 + i;
+        t.vlo[c] = t.vlo[a]; t.vhi[c] = t.vhi[a]; t.dmid[c] = t.dmid[a]; t.vrlo[c] = t.vrlo[a]; t.vrhi[c] = t.vrhi[a];
+      }
+    }
+    // buildBinLimits :429-450
+    auto blo = [&](int n, double dlo, double vr, int off) {
+      double r = std::pow(vr, 1. / 3.);
+      double lo = dlo, hi = dlo * r;
+      for (int i = 0; i < n; i++) {
+        if (i > 0) { lo = lo * r; hi = lo * r; }
+        set_bin(t, off + i, PI6 * hcube(lo), PI6 * hcube(hi));
+      }
+    };
+    blo(nprc, g.prc_dlo, g.prc_vol_ratio, nbins + ncld);
+    blo(nice, g.ice_dlo, g.ice_vol_ratio, B.nliquid);
+  }
+  std::vector<double> precpbins(nprc);
+  for (int i = 0; i < nprc; i++) precpbins[i] = std::pow(t.vlo[nbins + ncld + i] / PI6, 1. / 3.);
+  B.cnt80 = B.cnt50 = 0;
+  for (int i = 0; i < nprc; i++) { B.cnt80 += precpbins[i] < 80.e-6; B.cnt50 += precpbins[i] < 50.e-6; }
+
+  // ---- per-block tables ----
+  int nbp = ntotal;
+  B.nb_pad = nbp;
+  std::vector<double> tab((size_t)salsa::TAB_N * nbp, 0.);
+  for (int b = 0; b < ntotal; b++) {
+    tab[salsa::TAB_VLO * nbp + b] = t.vlo[b];
+    tab[salsa::TAB_VHI * nbp + b] = t.vhi[b];
+    tab[salsa::TAB_VRLO * nbp + b] = t.vrlo[b];
+    tab[salsa::TAB_VRHI * nbp + b] = t.vrhi[b];
+    tab[salsa::TAB_DMID * nbp + b] = t.dmid[b];
+  }
+  for (int i = 0; i < nprc; i++) tab[salsa::TAB_PRECPBINS * nbp + i] = precpbins[i];
+  B.tab_doubles = (int)tab.size();
+
+  // ---- I/O rows: thermodynamics, numbers, masses, IN deficit, charge time, outputs ----
+  std::vector<Row> rows;
+  auto add = [&](int fin, int fout, int idx, int mode) {
+    Row r;
+    r.fin = (int16_t)fin; r.fout = (int16_t)fout; r.idx = (int16_t)idx; r.mode = (int16_t)mode;
+    rows.push_back(r);
+  };
+  add(salsa::FI_PRESS, -1, 0, salsa::ROW_IN);
+  add(salsa::FI_TEMP, -1, 0, salsa::ROW_IN);
+  add(salsa::FI_RSL, -1, 0, salsa::ROW_IN);
+  add(salsa::FI_RSI, -1, 0, salsa::ROW_IN);
+  add(salsa::FI_RP, salsa::FO_RPT, 0, salsa::ROW_TEND);
+  add(salsa::FI_DN, -1, 0, salsa::ROW_IN);
+  add(salsa::FI_WP, -1, 0, salsa::ROW_IN);
+  add(salsa::FI_KAPPA, -1, 0, salsa::ROW_IN);
+  int ncat = (g.level == 5) ? 4 : 3;
+  const int catnb[4] = {nbins, ncld, nprc, nice};
+  B.raw_num = (int)rows.size();
+  for (int c = 0; c < ncat; c++)
+    for (int b = 0; b < catnb[c]; b++) add(salsa::FI_NAERO + c, salsa::FO_NAEROT + c, b, salsa::ROW_TEND);
+  for (int c = 0; c < 4; c++) B.raw_mbase[c] = 0;
+  for (int c = 0; c < ncat; c++) {
+    B.raw_mbase[c] = (int)rows.size();
+    int nsp = (c == 3) ? B.nwet + 1 : B.nwet;
+    for (int s = 0; s < nsp; s++)
+      for (int b = 0; b < catnb[c]; b++) add(salsa::FI_MAERO + c, salsa::FO_MAEROT + c, s * catnb[c] + b, salsa::ROW_TEND);
+  }
+  B.raw_indef = -1;
+  if (g.level == 5 && g.ice_theta_dist) {
+    B.raw_indef = (int)rows.size();
+    for (int b = 0; b < B.nliquid; b++) add(salsa::FI_INDEF, salsa::FO_INDEF, b, salsa::ROW_INOUT);
+  }
+  B.raw_charge = (int)rows.size();
+  for (int b = 0; b < B.nliquid; b++) add(salsa::FI_CHARGE, salsa::FO_CHARGE, b, salsa::ROW_INOUT);
+  B.raw_nact = (int)rows.size();
+  for (int k = 0; k < ncld; k++) add(-1, salsa::FO_NACT, k, salsa::ROW_OUT);
+  B.raw_vact = (int)rows.size();
+  for (int s = 0; s < B.nwet; s++)
+    for (int k = 0; k < ncld; k++) add(-1, salsa::FO_VACT, s * ncld + k, salsa::ROW_OUT);
+  B.raw_diag = (int)rows.size();
+  int ndiag = (g.level == 5) ? SALSA_NDIAG : SALSA_DIAG_AICOLL;
+  for (int i = 0; i < ndiag; i++) add(-1, salsa::FO_DIAG0 + i, 0, salsa::ROW_OUT);
+  B.nrows = (int)rows.size();
+  B.nraw = B.nrows;
+
+  // ---- collision pairs i <= j of enabled category pairs (mo_salsa_coagulation_kernels.f90:24-90) ----
+  salsa_config_t e = g;
+  if (g.level == 4) { e.lscgia = e.lscgic = e.lscgii = e.lscgip = 0; }
+  auto cat_of = [&](int b) { return b < nbins ? 0 : (b < nbins + ncld ? 1 : (b < B.nliquid ? 2 : 3)); };
+  auto pair_on = [&](int ci, int cj) -> bool {
+    if (ci > cj) { int x = ci; ci = cj; cj = x; }
+    if (ci == 0 && cj == 0) return e.lscgaa;
+    if (ci == 1 && cj == 1) return e.lscgcc;
+    if (ci == 2 && cj == 2) return e.lscgpp;
+    if (ci == 3 && cj == 3) return e.lscgii;
+    if (ci == 0 && cj == 1) return e.lscgca;
+    if (ci == 0 && cj == 2) return e.lscgpa;
+    if (ci == 0 && cj == 3) return e.lscgia;
+    if (ci == 1 && cj == 2) return e.lscgpc;
+    if (ci == 1 && cj == 3) return e.lscgic;
+    return e.lscgip;
+  };
+  std::vector<int> pairs;
+  for (int i = 0; i < ntotal; i++)
+    for (int j = i; j < ntotal; j++)
+      if (pair_on(cat_of(i), cat_of(j))) pairs.push_back(i | (j << 8));
+  B.npairs = (int)pairs.size();
+
+  salsa_handle *h = new salsa_handle();
+  h->cfg = g;
+  if (cudaGetDevice(&h->device) != cudaSuccess) { delete h; return SALSA_E_NODEV; }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) { delete h; return SALSA_E_NODEV; }
+  h->nsm = prop.multiProcessorCount;
+  int kt_bytes = g.precision == 0 ? 8 : 4;
+  {
+    size_t tri_n = (size_t)nbp * (nbp + 1) / 2;
+    size_t kd = (tri_n * kt_bytes + 7) / 8;
+    size_t n = ((B.nraw + 1) & ~1) + nbp + SALSA_NSV * nbp + 7 * nbp + 13 * nbp + 336 + 32 + kd;
+    B.ws_doubles = (int)((n + 1) & ~(size_t)1);
+  }
+  size_t smem = sizeof(double) * ((size_t)B.tab_doubles + (size_t)SALSA_CPG * B.ws_doubles);
+  if (smem > (size_t)prop.sharedMemPerBlockOptin) { delete h; return SALSA_E_UNSUPPORTED; }
+  bool ok = cudaMalloc(&h->d_tables, tab.size() * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&h->d_rows, rows.size() * sizeof(Row)) == cudaSuccess &&
+            cudaMalloc(&h->d_pairs, (pairs.size() + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&h->d_status, salsa::ST_N * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMallocHost(&h->h_status, salsa::ST_N * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreate(&h->ev0) == cudaSuccess && cudaEventCreate(&h->ev1) == cudaSuccess;
+  if (ok)
+    ok = cudaMemcpy(h->d_tables, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(h->d_rows, rows.data(), rows.size() * sizeof(Row), cudaMemcpyHostToDevice) == cudaSuccess &&
+         (pairs.empty() ||
+          cudaMemcpy(h->d_pairs, pairs.data(), pairs.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess);
+  if (!ok) {
+    salsa_gb300_finalize(h);
+    return SALSA_E_CUDA;
+  }
+  B.tables = h->d_tables;
+  B.rows = h->d_rows;
+  B.pairs = h->d_pairs;
+  B.status = h->d_status;
+  B.Eiagg_max = g.Eiagg_max; B.Eiagg_min = g.Eiagg_min; B.eddy_dis = g.eddy_dis; B.rhlim = g.rhlim;
+  B.initMinTheta = g.initMinTheta; B.chargeTimeMax = g.chargeTMax; B.chargeCollEnh = g.chargeCollEnh;
+  B.mean_theta_imm = g.mean_theta_imm; B.sigma_theta_imm = g.sigma_theta_imm;
+  B.mean_theta_dep = g.mean_theta_dep; B.sigma_theta_dep = g.sigma_theta_dep;
+  B.iceShapeAlpha = g.iceShapeAlpha; B.iceShapeBeta = g.iceShapeBeta;
+  B.iceShapeGamma = g.iceShapeGamma; B.iceShapeSigma = g.iceShapeSigma;
+  B.level = g.level;
+  h->base = B;
+  h->lolim_diam.resize(ntotal);
+  for (int b = 0; b < ntotal; b++) h->lolim_diam[b] = std::pow(t.vlo[b] / PI6, 1. / 3.);
+  *out = h;
+  return SALSA_OK;
+}
+
+void salsa_gb300_finalize(salsa_handle_t *h) {
+  if (!h) return;
+  if (h->d_tables) cudaFree(h->d_tables);
+  if (h->d_rows) cudaFree(h->d_rows);
+  if (h->d_pairs) cudaFree(h->d_pairs);
+  if (h->d_status) cudaFree(h->d_status);
+  if (h->h_status) cudaFreeHost(h->h_status);
+  if (h->stage) cudaFree(h->stage);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int salsa_gb300_layout(const salsa_handle_t *h, int *nbins, int *ncld, int *nprc, int *nice, int *nwet,
+                       double *lolim) {
+  if (!h) return SALSA_E_ARG;
+  if (nbins) *nbins = h->base.nbins;
+  if (ncld) *ncld = h->base.ncld;
+  if (nprc) *nprc = h->base.nprc;
+  if (nice) *nice = h->base.nice;
+  if (nwet) *nwet = h->base.nwet;
+  if (lolim) for (int b = 0; b < h->base.ntotal; b++) lolim[b] = h->lolim_diam[b];
+  return SALSA_OK;
+}
+
+int salsa_gb300_last_launches(const salsa_handle_t *h) { return h ? h->last_launches : 0; }
+double salsa_gb300_last_kernel_ms(const salsa_handle_t *h) { return h ? h->last_kernel_ms : 0.; }
+
+}  // extern "C"
+
+namespace {
+
+// Field bookkeeping: (pointer slot in salsa_fields_t, role, number of planes)
+struct FieldRef {
+  const double **in;   // for inputs
+  double **inout;      // for tendencies / outputs
+  int planes;
+  int is_output;       // needs device->host copy back
+  int is_input;        // needs host->device copy
+};
+
+int resolve_side(const void *p, int *side) {
+  if (!p) return 0;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return SALSA_E_ARG;
+  }
+  int s = (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) ? 1 : 0;
+  if (*side < 0) *side = s;
+  else if (*side != s) return SALSA_E_ARG;
+  return 0;
+}
+
+int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep, double time, int istp, int level,
+             int lcharge, int initialize, const salsa_fields_t *f, cudaStream_t stream, int sync, salsa_status_t *st,
+             int allow_host) {
+  if (!h || !f) return SALSA_E_ARG;
+  const salsa_config_t &g = h->cfg;
+  if (level != g.level || nzp < 3 || nxp < 5 || nyp < 5 || !(tstep > 0.) || !(tstep <= 600.) || ns < h->base.nwet)
+    return SALSA_E_ARG;   // tstep <= 600 s keeps the 0.02 s condensation substep loop bounded
+  if (!f->press || !f->temp || !f->rsl || !f->dn || !f->rp || !f->rpt || !f->naero || !f->ncloud || !f->nprecp ||
+      !f->naerot || !f->ncloudt || !f->nprecpt || !f->maero || !f->mcloud || !f->mprecp || !f->maerot || !f->mcloudt ||
+      !f->mprecpt || !f->pa_nactd || !f->pa_vactd)
+    return SALSA_E_ARG;
+  if (level == 5 && (!f->rsi || !f->nice || !f->mice || !f->nicet || !f->micet)) return SALSA_E_ARG;
+  if (level == 5 && g.ice_theta_dist && !f->indef) return SALSA_E_ARG;
+  if (lcharge && !f->chargeTime) return SALSA_E_ARG;
+  if (cudaSetDevice(h->device) != cudaSuccess) return SALSA_E_NODEV;
+
+  // set_SALSA_runtime (mo_salsa_driver.f90:445-474): states switch on once and stay on
+  const salsa_switch_t *ms[7] = {&g.lscoag, &g.lscnd, &g.lsauto, &g.lsactiv, &g.lsicenucl, &g.lsicemelt, &g.lssecice};
+  for (int i = 0; i < 7; i++) {
+    int sw = ms[i]->sw;
+    if (level == 4 && i >= 4) sw = 0;   // define_salsa :615-635
+    if (sw && time >= ms[i]->delay) h->st[i] = 1;
+  }
+  if (g.lsfreeRH.sw && time > g.lsfreeRH.delay) h->st_freeRH = 1;
+  if (g.lsFreeTheta.sw && time > g.lsFreeTheta.delay) h->st_freeTheta = 1;
+  (void)istp;
+
+  DevParams P = h->base;
+  P.nzp = nzp; P.nxp = nxp; P.nyp = nyp;
+  P.nz_int = nzp - 2; P.nx_int = nxp - 4;
+  P.ncells = (long long)(nzp - 2) * (nxp - 4) * (nyp - 4);
+  P.plane = (long long)nzp * nxp * nyp;
+  P.ngroups = (P.ncells + SALSA_CPG - 1) / SALSA_CPG;
+  P.level = level; P.lcharge = lcharge; P.initialize = initialize;
+  P.dt = tstep;
+  P.st_coag = h->st[0]; P.st_cnd = h->st[1]; P.st_auto = h->st[2]; P.st_activ = h->st[3];
+  P.st_icenucl = h->st[4]; P.st_icemelt = h->st[5];
+  P.st_freeRH = h->st_freeRH; P.st_freeTheta = h->st_freeTheta;
+  P.coag_mode = g.lscoag.mode; P.auto_mode = g.lsauto.mode; P.activ_mode = g.lsactiv.mode;
+  P.icenucl_mode = (level == 4) ? 1 : g.lsicenucl.mode;
+  P.lscgaa = g.lscgaa; P.lscgcc = g.lscgcc; P.lscgca = g.lscgca; P.lscgpc = g.lscgpc; P.lscgpa = g.lscgpa;
+  P.lscgpp = g.lscgpp; P.lscgia = g.lscgia; P.lscgic = g.lscgic; P.lscgii = g.lscgii; P.lscgip = g.lscgip;
+  P.lscndh2oae = g.lscndh2oae; P.lscndh2ocl = g.lscndh2ocl; P.lscndh2oic = g.lscndh2oic;
+  P.lsicehom = g.lsicehom; P.lsiceimm = g.lsiceimm; P.lsicedep = g.lsicedep;
+  P.ice_theta_dist = g.ice_theta_dist; P.lsdistupdate = g.lsdistupdate;
+  if (level == 4) {
+    P.lscgia = P.lscgic = P.lscgii = P.lscgip = 0;
+    P.lscndh2oic = 0;
+    P.ice_theta_dist = 0;
+    P.lsicehom = P.lsiceimm = P.lsicedep = 0;
+  }
+  P.has_kappa = f->kappa != nullptr;
+  int nliq = h->base.nliquid;
+  const int nb[4] = {h->base.nbins, h->base.ncld, h->base.nprc, h->base.nice};
+  const int nw = h->base.nwet;
+  // field table: pointer, planes, direction
+  struct F { const double *src; double *dst; long long planes; int in, out, fi, fo; };
+  std::vector<F> fl;
+  auto fin = [&](const double *p, long long planes, int fi) { fl.push_back({p, nullptr, planes, 1, 0, fi, -1}); };
+  auto fio = [&](double *p, long long planes, int fo, int in) { fl.push_back({p, p, planes, in, 1, -1, fo}); };
+  fin(f->press, 1, salsa::FI_PRESS); fin(f->temp, 1, salsa::FI_TEMP); fin(f->rsl, 1, salsa::FI_RSL);
+  fin(level == 5 ? f->rsi : nullptr, 1, salsa::FI_RSI);
+  fin(f->rp, 1, salsa::FI_RP); fin(f->dn, 1, salsa::FI_DN); fin(f->wp, 1, salsa::FI_WP);
+  fin(f->kappa, 1, salsa::FI_KAPPA);
+  fin(f->naero, nb[0], salsa::FI_NAERO); fin(f->ncloud, nb[1], salsa::FI_NCLOUD); fin(f->nprecp, nb[2], salsa::FI_NPRECP);
+  fin(level == 5 ? f->nice : nullptr, nb[3], salsa::FI_NICE);
+  fin(f->maero, (long long)nw * nb[0], salsa::FI_MAERO); fin(f->mcloud, (long long)nw * nb[1], salsa::FI_MCLOUD);
+  fin(f->mprecp, (long long)nw * nb[2], salsa::FI_MPRECP);
+  fin(level == 5 ? f->mice : nullptr, (long long)(nw + 1) * nb[3], salsa::FI_MICE);
+  bool use_indef = level == 5 && g.ice_theta_dist;
+  fio(f->rpt, 1, salsa::FO_RPT, 1);
+  fio(f->naerot, nb[0], salsa::FO_NAEROT, 1); fio(f->ncloudt, nb[1], salsa::FO_NCLOUDT, 1);
+  fio(f->nprecpt, nb[2], salsa::FO_NPRECPT, 1);
+  fio(level == 5 ? f->nicet : nullptr, nb[3], salsa::FO_NICET, 1);
+  fio(f->maerot, (long long)nw * nb[0], salsa::FO_MAEROT, 1); fio(f->mcloudt, (long long)nw * nb[1], salsa::FO_MCLOUDT, 1);
+  fio(f->mprecpt, (long long)nw * nb[2], salsa::FO_MPRECPT, 1);
+  fio(level == 5 ? f->micet : nullptr, (long long)(nw + 1) * nb[3], salsa::FO_MICET, 1);
+  fio(use_indef ? f->indef : nullptr, nliq, salsa::FO_INDEF, 1);
+  fio(lcharge ? f->chargeTime : nullptr, nliq, salsa::FO_CHARGE, 1);
+  fio(f->pa_nactd, nb[1], salsa::FO_NACT, 0);
+  fio(f->pa_vactd, (long long)nw * nb[1], salsa::FO_VACT, 0);
+  int ndiag = (level == 5) ? SALSA_NDIAG : SALSA_DIAG_AICOLL;
+  for (int i = 0; i < ndiag; i++) fio(g.diagnostics ? f->diag[i] : nullptr, 1, salsa::FO_DIAG0 + i, 0);
+
+  int side = -1;
+  for (auto &x : fl) {
+    const void *p = x.src ? (const void *)x.src : (const void *)x.dst;
+    if (resolve_side(p, &side)) return SALSA_E_ARG;
+  }
+  bool host = side == 0;
+  if (host && !allow_host) return SALSA_E_ARG;
+  cudaStream_t s = stream ? stream : h->stream;
+  int launches = 0;
+  if (host) {
+    size_t need = 0;
+    for (auto &x : fl) {
+      const void *p = x.src ? (const void *)x.src : (const void *)x.dst;
+      if (p) need += (size_t)(x.planes * P.plane) * sizeof(double);
+    }
+    if (need > h->stage_bytes) {
+      if (h->stage) cudaFree(h->stage);
+      h->stage = nullptr;
+      h->stage_bytes = 0;
+      if (cudaMalloc(&h->stage, need) != cudaSuccess) return SALSA_E_CUDA;
+      h->stage_bytes = need;
+    }
+  }
+  for (int i = 0; i < salsa::FI_N; i++) P.fin[i] = nullptr;
+  for (int i = 0; i < salsa::FO_N; i++) P.fout[i] = nullptr;
+  size_t off = 0;
+  for (auto &x : fl) {
+    const double *hp = x.src ? x.src : x.dst;
+    if (!hp) continue;
+    double *dp;
+    size_t bytes = (size_t)(x.planes * P.plane) * sizeof(double);
+    if (host) {
+      dp = reinterpret_cast<double *>(static_cast<char *>(h->stage) + off);
+      off += bytes;
+      if (x.in && cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return SALSA_E_CUDA;
+    } else {
+      dp = const_cast<double *>(hp);
+    }
+    if (x.fi >= 0) P.fin[x.fi] = dp;
+    if (x.fo >= 0) {
+      P.fout[x.fo] = dp;
+      if (x.fo == salsa::FO_INDEF) P.fin[salsa::FI_INDEF] = dp;
+      if (x.fo == salsa::FO_CHARGE) P.fin[salsa::FI_CHARGE] = dp;
+    }
+  }
+  if (P.ncells > 0) {
+    if (cudaMemsetAsync(h->d_status, 0, salsa::ST_N * sizeof(unsigned long long), s) != cudaSuccess) return SALSA_E_CUDA;
+    int prec = g.precision, dg = g.diagnostics ? 1 : 0;
+    int bps = prec == 0 ? (dg ? salsa::blocks_per_sm_d1(P) : salsa::blocks_per_sm_d0(P))
+                        : (dg ? salsa::blocks_per_sm_f1(P) : salsa::blocks_per_sm_f0(P));
+    if (bps <= 0) return SALSA_E_CUDA;
+    long long grid = (long long)bps * h->nsm * 8;
+    if (grid > P.ngroups) grid = P.ngroups;
+    cudaEventRecord(h->ev0, s);
+    cudaError_t e = prec == 0 ? (dg ? salsa::launch_d1(P, s, (int)grid) : salsa::launch_d0(P, s, (int)grid))
+                              : (dg ? salsa::launch_f1(P, s, (int)grid) : salsa::launch_f0(P, s, (int)grid));
+    cudaEventRecord(h->ev1, s);
+    if (e != cudaSuccess) return SALSA_E_CUDA;
+    launches = 1;
+    if (cudaMemcpyAsync(h->h_status, h->d_status, salsa::ST_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) !=
+        cudaSuccess)
+      return SALSA_E_CUDA;
+  }
+  if (host) {
+    off = 0;
+    for (auto &x : fl) {
+      const double *hp = x.src ? x.src : x.dst;
+      if (!hp) continue;
+      size_t bytes = (size_t)(x.planes * P.plane) * sizeof(double);
+      double *dp = reinterpret_cast<double *>(static_cast<char *>(h->stage) + off);
+      off += bytes;
+      if (x.out && cudaMemcpyAsync(x.dst, dp, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return SALSA_E_CUDA;
+    }
+  }
+  h->last_launches = launches;
+  if (!sync && !host) {
+    if (st) memset(st, 0, sizeof *st);
+    return SALSA_OK;
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return SALSA_E_CUDA;
+  float kms = 0.f;
+  if (P.ncells > 0 && cudaEventElapsedTime(&kms, h->ev0, h->ev1) == cudaSuccess) h->last_kernel_ms = kms;
+  salsa_status_t loc;
+  memset(&loc, 0, sizeof loc);
+  if (P.ncells > 0) {
+    loc.n_cells = (long long)h->h_status[salsa::ST_CELLS];
+    loc.n_equil_nonconv = (long long)h->h_status[salsa::ST_EQUIL];
+    loc.n_distr_nonconv = (long long)h->h_status[salsa::ST_DISTR];
+    loc.n_distr_negfrac = (long long)h->h_status[salsa::ST_NEGFRAC];
+    loc.n_cond_substeps = (long long)h->h_status[salsa::ST_COND];
+    loc.n_negative = (long long)h->h_status[salsa::ST_NEG];
+    loc.n_nonfinite = (long long)h->h_status[salsa::ST_NONFINITE];
+  }
+  loc.code = (loc.n_equil_nonconv || loc.n_distr_nonconv || loc.n_distr_negfrac || loc.n_nonfinite) ? SALSA_E_NUMERIC
+                                                                                                      : SALSA_OK;
+  if (st) *st = loc;
+  return loc.code;
+}
+
+}  // namespace
+
+extern "C" int salsa_gb300_run(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep, double time,
+                               int istp, int level, int lcharge, int initialize, const salsa_fields_t *f,
+                               salsa_status_t *st) {
+  return run_impl(h, nzp, nxp, nyp, ns, tstep, time, istp, level, lcharge, initialize, f, nullptr, 1, st, 1);
+}
+
+extern "C" int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep, double time,
+                                     int istp, int level, int lcharge, int initialize, const salsa_fields_t *f,
+                                     void *stream, int sync, salsa_status_t *st) {
+  return run_impl(h, nzp, nxp, nyp, ns, tstep, time, istp, level, lcharge, initialize, f, (cudaStream_t)stream, sync,
+                  st, 0);
+}

@@ -1,0 +1,2235 @@
+// salsa_kernel_impl.cuh -- the fused SALSA microphysics step for sm_103a (templates;
+// instantiated by salsa_k_*.cu, one translation unit per precision/diagnostics form).
+//
+// One launch advances every interior grid cell by one SALSA call
+// (UCLALES-SALSA src/src_salsa/mo_salsa_driver.f90:180-427 -> mo_salsa.f90:45-153).
+//
+// Execution model
+//   * block = SALSA_CPG warps = SALSA_CPG consecutive interior cells ("group");
+//     the block stages the group's bin-major input rows into shared memory with
+//     sector-complete loads (SALSA_CPG consecutive doubles per row), every warp
+//     advances its own cell out of shared memory, and the block writes the
+//     tendency rows back with read-modify-write of SALSA_CPG-cell segments.
+//   * inside a cell, lanes split bins (diameters, condensation, activation,
+//     freezing) and bin pairs (collision kernels); the Gauss-Seidel bin sweep of
+//     the coagulation update stays ordered, each target bin's partner sums are
+//     lane-parallel and reduced with warp shuffles.
+//   * KT is the arithmetic type of the collision kernels and of the condensation
+//     mass-transfer coefficients: double for the parity form, float for the mixed
+//     form (partner sums then use compensated summation; denominators, the water
+//     budget and all state updates stay double).
+#pragma once
+#include "salsa_device.cuh"
+#include <cstdio>
+
+namespace salsa {
+namespace {   // internal linkage: every instantiation unit carries its own copy
+
+// ----------------------------------------------------------------------------------------
+// per-warp workspace
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+struct WS {
+  double *raw, *numc, *volc, *dwet, *ddry, *dins, *dnsp, *rhomean, *indef, *ctime, *scr, *misc;
+  KT *K;
+  int *pbuf;
+  int NB;
+  __device__ __forceinline__ double &v(int s, int b) const { return volc[s * NB + b]; }
+  __device__ __forceinline__ double *sc(int k) const { return scr + k * NB; }
+};
+
+// misc slots (doubles)
+enum {
+  M_DIAG = 0,              // 17 diagnostic accumulators
+  M_FLAGS = 17,            // F_* per-cell condition counters
+  M_RV = 24,               // water vapour mixing ratio of the cell
+  M_PF = 32,               // precipitation-formation accumulators (7 + 9 * nprc, nprc <= 23)
+  M_PFSLOT = M_PF + 216,   // 8 partner slots * 10
+  M_END = M_PFSLOT + 80
+};
+enum { F_NEG = 0, F_EQUIL, F_DISTR, F_NEGFRAC, F_COND };
+#define SALSA_MISC_DOUBLES 336
+#define SALSA_NSCR 13
+
+__device__ __forceinline__ int phase_of(const DevParams &P, int b) {
+  return b < P.nbins ? 1 : (b < P.nbins + P.ncld ? 2 : (b < P.nliquid ? 3 : 4));
+}
+__device__ __forceinline__ double nlim_of(int ph) { return ph <= 2 ? K_NLIM : K_PRLIM; }
+__device__ __forceinline__ double dlim_of(int ph) {
+  return ph == 1 ? 30.e-6 : (ph == 2 ? 100.e-6 : (ph == 3 ? 5.e-3 : 10.e-3));
+}
+__device__ __forceinline__ int tri(int i, int j, int NB) {  // i <= j
+  return i * NB - (i * (i - 1)) / 2 + (j - i);
+}
+template <typename KT>
+__device__ __forceinline__ KT kget(const WS<KT> &w, int i, int j) {
+  return i <= j ? w.K[tri(i, j, w.NB)] : w.K[tri(j, i, w.NB)];
+}
+
+// ----------------------------------------------------------------------------------------
+// classSection.f90:91-159 updateDiameter(limit=.TRUE., type="all") and :169-195 updateRhomean.
+// With limit set, dnsp = MIN(dwet, dlim) overwrites the non-spherical diameter (:149-150),
+// so getDiameter's value never survives a type="all" update and is not evaluated here.
+// ----------------------------------------------------------------------------------------
+__device__ void updateDiameterAll(const DevParams &P, const WS<double> *, double *numc, double *volc, double *dwet,
+                                  double *ddry, double *dins, double *dnsp, const double *dmid, int NB, int b) {
+  int ph = phase_of(P, b);
+  double n = numc[b];
+  double dw, dd, di;
+  if (n > nlim_of(ph)) {
+    double vs = 0., vd = 0., vi = 0.;
+    for (int s = 0; s < P.nused; s++) vs += volc[s * NB + b];
+    for (int s = 0; s < P.ndry; s++) vd += volc[s * NB + b];
+    for (int k = 0; k < P.ninsoluble; k++) vi += volc[P.ind_insoluble[k] * NB + b];
+    dw = cbrt(vs / n / K_PI6);
+    dd = cbrt(vd / n / K_PI6);
+    di = cbrt(vi / n / K_PI6);
+  } else {
+    dw = dd = di = dmid[b];
+  }
+  double dl = dlim_of(ph);
+  dw = fmin(dw, dl);
+  dwet[b] = dw;
+  dnsp[b] = dw;
+  ddry[b] = fmin(dd, dl);
+  dins[b] = fmin(di, dl);
+}
+
+__device__ __forceinline__ double rhomean_of(const DevParams &P, int ph, double n, double vw, double vr) {
+  if (ph > 3) {
+    if (n > nlim_of(ph)) {
+      double mp = K_RHOIC * vw, mr = K_RHORI * vr, mt = mp + mr;
+      double r = (mp * K_RHOIC + mr * K_RHORI) / fmax(mt, 7.e-25);
+      return fmin(r, K_RHOIC);
+    }
+    return K_RHOIC;
+  }
+  return K_RHOWA;
+}
+
+// classSection.f90:202-224 getRimeFraction
+__device__ __forceinline__ double rimefrac(const DevParams &P, double n, double vw, double vr, int ph) {
+  double r = 0.;
+  if (ph == 4 && vw > 1.e-23 && vr > 1.e-23 && n > nlim_of(ph)) r = vr * K_RHORI / (vw * K_RHOIC + vr * K_RHORI);
+  return r;
+}
+
+// ----------------------------------------------------------------------------------------
+// Terminal velocity: mo_particle_external_properties.f90:237-352 (+ ice shape
+// coefficients, mo_ice_shape.f90:145-191)
+// ----------------------------------------------------------------------------------------
+template <typename T>
+struct Shape { T alpha, beta, gamma, sigma; };
+
+template <typename T>
+__device__ __forceinline__ T t_exp(T x);
+template <> __device__ __forceinline__ double t_exp<double>(double x) { return exp(x); }
+template <> __device__ __forceinline__ float t_exp<float>(float x) { return expf(x); }
+template <typename T>
+__device__ __forceinline__ T t_log(T x);
+template <> __device__ __forceinline__ double t_log<double>(double x) { return log(x); }
+template <> __device__ __forceinline__ float t_log<float>(float x) { return logf(x); }
+template <typename T>
+__device__ __forceinline__ T t_sqrt(T x);
+template <> __device__ __forceinline__ double t_sqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float t_sqrt<float>(float x) { return sqrtf(x); }
+template <typename T>
+__device__ __forceinline__ T t_cbrt(T x);
+template <> __device__ __forceinline__ double t_cbrt<double>(double x) { return cbrt(x); }
+template <> __device__ __forceinline__ float t_cbrt<float>(float x) { return cbrtf(x); }
+template <typename T>
+__device__ __forceinline__ T t_pow(T x, T y);
+template <> __device__ __forceinline__ double t_pow<double>(double x, double y) { return pow(x, y); }
+template <> __device__ __forceinline__ float t_pow<float>(float x, float y) { return powf(x, y); }
+
+template <typename T>
+__device__ void shape_coeffs(const DevParams &P, Shape<T> &s, double mpri, double mrim, double numc) {
+  s.alpha = (T)(K_PI6 * K_RHOIC);
+  s.beta = (T)3.;
+  s.gamma = (T)(K_PI / 4.);
+  s.sigma = (T)2.;
+  if (numc < 1.e-6) return;
+  double Mtot = (mpri + mrim) / numc;
+  double Fr = fmax(fmin(mrim / (Mtot * numc), 0.9999), 0.0001);
+  double rho_b = Fr * K_RHORI + (1. - Fr) * K_RHOIC;
+  double Dth = pow(K_PI6 * K_RHOIC / P.iceShapeAlpha, 1. / (P.iceShapeBeta - 3.));
+  double Dgr = pow(P.iceShapeAlpha / (K_PI6 * rho_b), 1. / (3. - P.iceShapeBeta));
+  double Dcr = pow((1. / (1. - Fr)) * P.iceShapeAlpha / (K_PI6 * rho_b), 1. / (3. - P.iceShapeBeta));
+  double Mth = K_RHOIC * K_PI6 * cube(Dth), Mgr = rho_b * K_PI6 * cube(Dgr), Mcr = rho_b * K_PI6 * cube(Dcr);
+  if (Mtot >= Mth && Mtot < Mgr) {
+    s.alpha = (T)P.iceShapeAlpha; s.beta = (T)P.iceShapeBeta; s.gamma = (T)P.iceShapeGamma; s.sigma = (T)P.iceShapeSigma;
+  } else if (Mtot > Mcr) {
+    double hlp = 1. / (1. - Fr);
+    s.alpha = (T)(P.iceShapeAlpha * hlp);
+    s.beta = (T)P.iceShapeBeta;
+    s.gamma = (T)(P.iceShapeGamma * (1. - Fr) + K_PI / 4. * Fr);
+    s.sigma = (T)(P.iceShapeSigma * (1. - Fr) + 2. * Fr);
+  }
+}
+
+template <typename T>
+__device__ T terminal_vel(T diam, T rhop, T rhoa, T visc, T beta, int flag, const Shape<T> &sh, T dnsp) {
+  const T grav = (T)K_GRAV;
+  T tv = 0;
+  if (flag <= 3) {
+    if (diam <= (T)19E-6) {
+      tv = sq(diam) * (rhop - rhoa) * grav * beta / ((T)18. * visc);
+    } else if (diam < (T)1.07E-3) {
+      T NDa = (T)4. / (T)3. * cube(diam) * grav * (rhop - rhoa) * rhoa / sq(visc);
+      T X = t_log(NDa);
+      T X2 = sq(X);
+      T Y = (T)-0.318657E1 + (T)0.992696 * X - (T)0.153193E-2 * X2 - (T)0.987059E-3 * X2 * X -
+            (T)0.578878E-3 * sq(X2) + (T)0.855176E-4 * sq(X2) * X - (T)0.327815E-5 * cube(X2);
+      T Re2 = beta * t_exp(Y);
+      tv = visc / rhoa / diam * Re2;
+    } else {
+      T Np = cube((T)K_SURFW0) * sq(rhoa) / (sq(sq(visc)) * (rhop - rhoa) * grav);
+      T Bo = (T)4. / (T)3. * (rhop - rhoa) * grav / (T)K_SURFW0 * sq(diam);
+      T Np6 = t_sqrt(t_cbrt(Np));
+      T X3 = t_log(Bo * Np6);
+      T X32 = sq(X3);
+      T Y3 = (T)-0.500015E1 + (T)0.523778E1 * X3 - (T)0.204914E1 * X32 + (T)0.475294 * X32 * X3 -
+             (T)0.542819E-1 * sq(X32) + (T)0.238449E-2 * sq(X32) * X3;
+      T Re3 = Np6 * t_exp(Y3);
+      tv = fmin(visc / rhoa / diam * Re3, (T)9.2);
+    }
+  } else {
+    // Khvorostyanov and Curry 2002 (kc1213/kcbre/kcare/kcAv/kcBv/kcVt :297-352)
+    T Vb = (T)K_PI6 * cube(diam);
+    T Ap = sh.gamma * t_pow(dnsp, sh.sigma);
+    T X = ((T)2. * Vb * (rhop - rhoa) * grav * sq(dnsp)) / (Ap * rhoa * sq(visc));
+    const T c1 = (T)0.0902, delta0 = (T)9.06;
+    T k12 = t_sqrt((T)1. + c1 * t_sqrt(X));
+    T bre = (T)0.5 * c1 * t_sqrt(X);
+    bre = bre / (k12 - (T)1.);
+    bre = bre / k12;
+    T are = (T)0.25 * sq(delta0);
+    are = are * sq(k12 - (T)1.);
+    are = are / t_pow(X, bre);
+    T Av = are * t_pow(visc, (T)1. - (T)2. * bre);
+    Av = Av * t_pow(((T)2. * sh.alpha * grav) / (rhoa * sh.gamma), bre);
+    T Bv = bre * (sh.beta - sh.sigma + (T)2.) - (T)1.;
+    tv = Av * t_pow(dnsp, Bv);
+  }
+  return tv;
+}
+
+// per-cell constants of the collision kernel (mo_salsa_coagulation_kernels.f90:282-284, 343-345, 389-391)
+template <typename T>
+struct CoagCell { T T_, visc, mfp, zrhoa, vkin, shearA, turbB; };
+
+// per-bin collision properties (the particle-dependent part of coagc :263-364)
+template <typename T>
+struct BinProps { T diam, mass, beta, dfpart, mtvel, omega, termv, reyn, schm; };
+
+template <typename T>
+__device__ void bin_props(const CoagCell<T> &cc, int ph, T diam, T dsph, T mass, T rhomean, const Shape<T> &sh,
+                          BinProps<T> &o) {
+  o.diam = diam;
+  o.mass = mass;
+  T knud = (T)2. * cc.mfp / diam;
+  o.beta = (T)1. + knud * ((T)1.142 + (T)0.558 * t_exp((T)-0.999 / knud));
+  o.dfpart = o.beta * (T)K_BOLTZ * cc.T_ / ((T)3. * (T)K_PI * cc.visc * diam);
+  o.mtvel = t_sqrt(((T)8. * (T)K_BOLTZ * cc.T_) / ((T)K_PI * mass));
+  o.omega = (T)8. * o.dfpart / ((T)K_PI * o.mtvel);
+  if (ph < 4) o.termv = terminal_vel<T>(diam, rhomean, cc.zrhoa, cc.visc, o.beta, ph, sh, (T)0);
+  else o.termv = terminal_vel<T>(dsph, rhomean, cc.zrhoa, cc.visc, o.beta, ph, sh, diam);
+  o.reyn = diam * o.termv / cc.vkin;
+  o.schm = cc.vkin / o.dfpart;
+}
+
+// pair part of coagc (:298-416)
+template <typename T>
+__device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinProps<T> &b) {
+  T mdiam = (T)0.5 * (a.diam + b.diam);
+  T flux1 = (T)4. * (T)K_PI * mdiam * (a.dfpart + b.dfpart);
+  T flux2 = (T)K_PI * t_sqrt(sq(a.mtvel) + sq(b.mtvel)) * sq(mdiam);
+  T m2 = sq(mdiam);
+  T oa2 = m2 + sq(a.omega), ob2 = m2 + sq(b.omega);
+  T tva1 = (cube(mdiam + a.omega) - oa2 * t_sqrt(oa2)) / ((T)3. * mdiam * a.omega) - mdiam;
+  T tva2 = (cube(mdiam + b.omega) - ob2 * t_sqrt(ob2)) / ((T)3. * mdiam * b.omega) - mdiam;
+  T fmdist = t_sqrt(sq(tva1) + sq(tva2));
+  bool first_large = a.diam >= b.diam;
+  const BinProps<T> &L = first_large ? a : b;
+  const BinProps<T> &S = first_large ? b : a;
+  T dv = fabs(a.termv - b.termv);
+  T stok = (T)2. * S.termv * dv / (L.diam * (T)K_GRAV);
+  T zbrown = flux1 / (mdiam / (mdiam + fmdist) + flux1 / flux2);
+  T zbrconv;
+  if (L.reyn <= (T)1.) zbrconv = (T)0.45 * zbrown * t_cbrt(L.reyn * S.schm);
+  else zbrconv = (T)0.45 * zbrown * t_sqrt(L.reyn) * t_cbrt(S.schm);
+  T hd = (T)0.5 * (a.diam + b.diam);
+  T ztshear = cc.shearA * cube(hd);
+  T zturb = cc.turbB * sq(hd) * dv;
+  T zea = sq(stok) / sq(stok + (T)0.5);
+  T zev = 0;
+  if (stok > (T)1.214) {
+    zev = (T)0.75 * t_log((T)2. * stok) / (stok - (T)1.214);
+    zev = (T)1. / sq((T)1. + zev);
+  }
+  T zecoll = ((T)60. * zev + zea * L.reyn) / ((T)60. + L.reyn);
+  T zgrav = zecoll * (T)K_PI * sq(mdiam);
+  zgrav = zgrav * dv;
+  return zbrown + zbrconv + t_sqrt(sq(zgrav) + sq(ztshear) + sq(zturb));
+}
+
+template <typename KT>
+__device__ __forceinline__ void load_props(const KT *S, int NB, int b, BinProps<KT> &o) {
+  o.diam = S[0 * NB + b]; o.mass = S[1 * NB + b]; o.beta = S[2 * NB + b]; o.dfpart = S[3 * NB + b];
+  o.mtvel = S[4 * NB + b]; o.omega = S[5 * NB + b]; o.termv = S[6 * NB + b]; o.reyn = S[7 * NB + b];
+  o.schm = S[8 * NB + b];
+}
+
+template <typename KT>
+__device__ void eval_pairs(const DevParams &P, const WS<KT> &w, const CoagCell<KT> &cc, const KT *S,
+                           const double *dmid, const int *list, int n, int lane) {
+  const int NB = w.NB;
+  if (lane < n) {
+    int q = list[lane];
+    int i = q & 0xff, j = (q >> 8) & 0xff;
+    BinProps<KT> a, b;
+    load_props<KT>(S, NB, j, b);
+    if (fabs(dmid[i] - dmid[j]) / dmid[i] < 1.e-2) {
+      // self-coagulation offset (:273-276): particle 1 takes 1.1x the diameter and 1.33x the mass of particle 2
+      Shape<KT> sh;
+      sh.alpha = S[9 * NB + i]; sh.beta = S[10 * NB + i]; sh.gamma = S[11 * NB + i]; sh.sigma = S[12 * NB + i];
+      bin_props<KT>(cc, phase_of(P, i), (KT)1.1 * b.diam, (KT)w.dwet[i], (KT)1.33 * b.mass, (KT)w.rhomean[i], sh, a);
+    } else {
+      load_props<KT>(S, NB, i, a);
+    }
+    KT k = coag_pair<KT>(cc, a, b);
+    if (P.lcharge) {
+      // charging enhancement (:411-416)
+      double kd = (double)k;
+      kd = kd + kd * P.chargeCollEnh * 0.5 * (w.ctime[i] + w.ctime[j]) / P.chargeTimeMax;
+      k = (KT)kd;
+    }
+    w.K[tri(i, j, NB)] = k;
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// Collision kernels for all enabled bin pairs: mo_salsa_coagulation_kernels.f90:24-180
+// (buildKernelSelf/buildKernel: pairs whose partner has numc < nlim are zero).
+// Scratch: 0 diam 1 mass 2 beta 3 dfpart 4 mtvel 5 omega 6 termv 7 reyn 8 schm 9-12 shape
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+__device__ void build_kernels(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
+                              int lane) {
+  const int NB = w.NB;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  CoagCell<KT> cc;
+  {
+    double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+    double mfp = (1.656e-10 * T + 1.828e-8) * K_PSTAND / pres;
+    double zrhoa = pres / (K_RD * T);
+    double vkin = visc / zrhoa;
+    cc.T_ = (KT)T; cc.visc = (KT)visc; cc.mfp = (KT)mfp; cc.zrhoa = (KT)zrhoa; cc.vkin = (KT)vkin;
+    cc.shearA = (KT)sqrt(8. * K_PI * P.eddy_dis / (15. * vkin));
+    cc.turbB = (KT)(K_PI * pow(P.eddy_dis, 0.75) / (K_GRAV * sqrt(sqrt(vkin))));
+  }
+  KT *S = reinterpret_cast<KT *>(w.scr);   // KT-typed scratch, 13 * NB entries
+  for (int b = lane; b < P.ntotal; b += 32) {
+    int ph = phase_of(P, b);
+    Shape<KT> sh;
+    if (ph == 4) {
+      double mp = 0.;
+      for (int s = 0; s < P.nused - 1; s++) mp += w.v(s, b) * K_RHOIC;
+      shape_coeffs<KT>(P, sh, mp, w.v(P.nused - 1, b) * K_RHORI, w.numc[b]);
+    } else {
+      sh.alpha = sh.beta = sh.gamma = sh.sigma = 0;
+    }
+    double diam = w.dwet[b];   // dnsp == dwet after a limited "all" update
+    double mass = w.rhomean[b] * K_PI6 * cube(w.dwet[b]);
+    BinProps<KT> o;
+    bin_props<KT>(cc, ph, (KT)diam, (KT)w.dwet[b], (KT)mass, (KT)w.rhomean[b], sh, o);
+    S[0 * NB + b] = o.diam; S[1 * NB + b] = o.mass; S[2 * NB + b] = o.beta; S[3 * NB + b] = o.dfpart;
+    S[4 * NB + b] = o.mtvel; S[5 * NB + b] = o.omega; S[6 * NB + b] = o.termv; S[7 * NB + b] = o.reyn;
+    S[8 * NB + b] = o.schm;
+    S[9 * NB + b] = sh.alpha; S[10 * NB + b] = sh.beta; S[11 * NB + b] = sh.gamma; S[12 * NB + b] = sh.sigma;
+  }
+  __syncwarp();
+  // scan the pair table; compact the active pairs into pbuf and evaluate them 32 at a time
+  int nbuf = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < P.npairs; base += 32) {
+    bool act = false;
+    int pk = 0;
+    int t = base + lane;
+    if (t < P.npairs) {
+      pk = __ldg(P.pairs + t);
+      int i = pk & 0xff, j = (pk >> 8) & 0xff;
+      act = w.numc[i] >= nlim_of(phase_of(P, i)) && w.numc[j] >= nlim_of(phase_of(P, j));
+      if (!act) w.K[tri(i, j, NB)] = (KT)0;
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, act);
+    if (act) w.pbuf[nbuf + __popc(bal & lt)] = pk;
+    nbuf += __popc(bal);
+    __syncwarp();
+    if (nbuf >= 32) {
+      eval_pairs<KT>(P, w, cc, S, dmid, w.pbuf + nbuf - 32, 32, lane);
+      nbuf -= 32;
+      __syncwarp();
+    }
+  }
+  if (nbuf > 0) eval_pairs<KT>(P, w, cc, S, dmid, w.pbuf, nbuf, lane);
+  __syncwarp();
+}
+
+
+// ----------------------------------------------------------------------------------------
+// Semi-implicit coagulation update: mo_salsa_coagulation_processes.f90:24-702 and the
+// driver mo_salsa_dynamics.f90:92-202.  Target bins are visited in the reference order
+// (ice, precipitation, aerosol, cloud; ascending bins); every partner sum of one target
+// is accumulated lane-parallel and reduced once.  Only the diagnostics that reach the
+// output fields are accumulated (the number-only rate tallies of accumulateSink never do).
+// ----------------------------------------------------------------------------------------
+struct TAcc {
+  double sink, self;
+  double src[SALSA_NSV];
+  double dg[7];   // 0 autoc(abs) 1 autoc80 2 autoc50 3 accr 4 accr80 5 accr50 6 coll mass
+  __device__ __forceinline__ void zero() {
+    sink = self = 0.;
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = 0.;
+#pragma unroll
+    for (int d = 0; d < 7; d++) dg[d] = 0.;
+  }
+  __device__ __forceinline__ void reduce(bool diag) {
+    sink = warp_sum(sink);
+    self = warp_sum(self);
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = warp_sum(src[s]);
+    if (diag) {
+#pragma unroll
+      for (int d = 0; d < 7; d++) dg[d] = warp_sum(dg[d]);
+    }
+  }
+};
+
+template <typename KT>
+__device__ __forceinline__ void sink_range(const WS<KT> &w, int t, int g0, int istr, int iend, double xx, TAcc &a,
+                                           bool to_self, int lane) {
+  for (int ll = istr + lane; ll <= iend; ll += 32) {
+    int g = g0 + ll;
+    double d = xx * (double)kget(w, t, g) * w.numc[g];
+    if (to_self) a.self += d; else a.sink += d;
+  }
+}
+
+template <typename KT>
+__device__ __forceinline__ void source_range(const WS<KT> &w, int t, int g0, int istr, int iend, int nspec, TAcc &a,
+                                             int lane) {
+  for (int ll = istr + lane; ll <= iend; ll += 32) {
+    int g = g0 + ll;
+    double k = (double)kget(w, g, t);
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++)
+      if (s < nspec) a.src[s] += k * w.v(s, g);
+  }
+}
+
+// applyCoag (:539-559): lanes 0..nspec-1 update the volumes, then the number
+template <typename KT>
+__device__ __forceinline__ void apply_coag(const WS<KT> &w, int t, int nspec, double dt, const TAcc &a, int lane) {
+  double my = 0.;
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++)
+    if (lane == s) my = a.src[s];
+  double n = w.numc[t];
+  if (lane < nspec) w.v(lane, t) = (w.v(lane, t) + dt * my * n) / (1. + dt * a.sink);
+  __syncwarp();
+  if (lane == 0) w.numc[t] = n / (1. + dt * (a.sink + a.self));
+  __syncwarp();
+}
+
+template <typename KT>
+__device__ void coag_aero(const DevParams &P, const WS<KT> &w, double dt, int lane) {
+  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid;
+  for (int kk = P.in1a; kk <= P.fn2b; kk++) {
+    if (w.numc[kk] < K_NLIM) continue;
+    TAcc a;
+    a.zero();
+    int reg = kk <= P.fn1a ? 0 : (kk <= P.fn2a ? 1 : 2);
+    if (reg == 0) {
+      int icla = P.ica_cur + max(kk - P.ica_par, 0);
+      int iclb = P.icb_cur + (icla - P.ica_cur);
+      if (P.lscgaa) {
+        sink_range(w, kk, 0, kk + 1, P.fn2b, 1.0, a, false, lane);
+        sink_range(w, kk, 0, kk, kk, 0.5, a, true, lane);
+      }
+      if (P.lscgca) {
+        sink_range(w, kk, C0, icla, P.fca_cur, 1.0, a, false, lane);
+        sink_range(w, kk, C0, iclb, P.fcb_cur, 1.0, a, false, lane);
+      }
+      if (P.lscgpa) sink_range(w, kk, P0, 0, P.nprc - 1, 1.0, a, false, lane);
+      if (P.lscgia) sink_range(w, kk, I0, 0, P.nice - 1, 1.0, a, false, lane);
+      if (P.lscgaa && kk > P.in1a) source_range(w, kk, 0, P.in1a, kk - 1, nspec, a, lane);
+      if (P.lscgca) {
+        icla = P.ica_cur + (kk - P.ica_par) - 1;
+        iclb = P.icb_cur + (icla - P.ica_cur);
+        if (icla >= P.ica_cur) source_range(w, kk, C0, P.ica_cur, icla, nspec, a, lane);
+        if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
+      }
+    } else if (reg == 1) {
+      int index_b = P.in2b + (kk - P.in2a);
+      int icla = P.ica_cur + max(kk - P.ica_par, 0);
+      int iclb = P.icb_cur + max(kk - P.ica_par, 0);
+      if (P.lscgaa) {
+        if (kk < P.fn2a) {
+          sink_range(w, kk, 0, kk + 1, P.fn2a, 1.0, a, false, lane);
+          sink_range(w, kk, 0, index_b, P.fn2b, 1.0, a, false, lane);
+        }
+        sink_range(w, kk, 0, kk, kk, 0.5, a, true, lane);
+      }
+      if (P.lscgca) {
+        sink_range(w, kk, C0, icla, P.fca_cur, 1.0, a, false, lane);
+        sink_range(w, kk, C0, iclb, P.fcb_cur, 1.0, a, false, lane);
+      }
+      if (P.lscgpa) sink_range(w, kk, P0, 0, P.nprc - 1, 1.0, a, false, lane);
+      if (P.lscgia) sink_range(w, kk, I0, 0, P.nice - 1, 1.0, a, false, lane);
+      if (P.lscgaa) {
+        source_range(w, kk, 0, P.in1a, kk - 1, nspec, a, lane);
+        source_range(w, kk, 0, P.in2b, index_b, nspec, a, lane);
+      }
+      if (P.lscgca) {
+        icla = P.ica_cur + (kk - P.ica_par) - 1;
+        iclb = P.icb_cur + (icla - P.ica_cur);
+        if (icla >= P.ica_cur) source_range(w, kk, C0, P.ica_cur, icla, nspec, a, lane);
+        if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
+      }
+    } else {
+      int index_a = P.in2a + (kk - P.in2b);
+      int icla = P.ica_cur + max(kk - P.icb_par, 0);
+      int iclb = P.icb_cur + max(kk - P.icb_par, 0);
+      if (P.lscgaa) {
+        if (kk < P.fn2b) {
+          sink_range(w, kk, 0, kk + 1, P.fn2b, 1.0, a, false, lane);
+          sink_range(w, kk, 0, index_a, P.fn2a, 1.0, a, false, lane);
+        }
+        sink_range(w, kk, 0, kk, kk, 0.5, a, true, lane);
+      }
+      if (P.lscgca) {
+        sink_range(w, kk, C0, icla, P.fca_cur, 1.0, a, false, lane);
+        sink_range(w, kk, C0, iclb, P.fcb_cur, 1.0, a, false, lane);
+      }
+      if (P.lscgpa) sink_range(w, kk, P0, 0, P.nprc - 1, 1.0, a, false, lane);
+      if (P.lscgia) sink_range(w, kk, I0, 0, P.nice - 1, 1.0, a, false, lane);
+      if (P.lscgaa) {
+        source_range(w, kk, 0, P.in2b, kk - 1, nspec, a, lane);
+        source_range(w, kk, 0, P.in1a, index_a, nspec, a, lane);
+      }
+      if (P.lscgca) {
+        iclb = P.icb_cur + (kk - P.icb_par) - 1;
+        icla = P.ica_cur + (iclb - P.icb_cur);
+        if (icla >= P.ica_cur) source_range(w, kk, C0, P.ica_cur, icla, nspec, a, lane);
+        if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
+      }
+    }
+    a.reduce(false);
+    apply_coag(w, kk, nspec, dt, a, lane);
+  }
+}
+
+// accumulatePrecipFormation (:1457-1584) for the partners istr..iend (cloud-local) of
+// target t (cloud-local).  Per-partner contributions are staged in partner slots and
+// summed per precipitation bin in partner order, which keeps the result deterministic.
+template <typename KT>
+__device__ void precip_formation(const DevParams &P, const WS<KT> &w, const double *tb, int t, int istr, int iend,
+                                 double fix, bool selfcoll, TAcc &a, bool diag, int lane) {
+  const int C0 = P.nbins, nspec = P.nwet, nprc = P.nprc, iwa = P.iwa;
+  const double *pbins = tb + TAB_PRECPBINS * P.nb_pad;
+  double *pf = w.misc + M_PF;                // [0..6] volsink, then vol_prc[nprc][7], num_prc[nprc], INFnum[nprc]
+  double *vol_prc = pf + 7, *num_prc = pf + 7 + 7 * nprc, *inf_prc = num_prc + nprc;
+  double *slot = w.misc + M_PFSLOT;          // 8 slots x 10: tp, dvol[7], dnum, x*dnum
+  const int tg = C0 + t;
+  for (int c0 = istr; c0 <= iend; c0 += 8) {
+    int np = min(8, iend - c0 + 1);
+    if (lane < np) {
+      int ll = c0 + lane, lg = C0 + ll;
+      double dt3 = cube(w.dwet[tg]) + cube(w.dwet[lg]);
+      double D_new = cbrt(dt3);
+      int cnt = 0;
+      for (int i = 0; i < nprc; i++) cnt += (D_new > pbins[i]);
+      double klt = (double)kget(w, lg, tg);
+      double nt = w.numc[tg], nl = w.numc[lg];
+      double *sl = slot + lane * 10;
+      sl[0] = (double)(cnt - 1);
+      double dnum = 0.;
+      if (D_new > pbins[0]) {
+        double dvw = 0.;
+        if (selfcoll) {
+          for (int s = 0; s < nspec; s++) sl[1 + s] = w.v(s, lg) * nt * klt * fix;
+          dnum = (0.5 * klt * nl * nt) * fix;
+          sl[9] = w.indef[lg] * dnum;
+          a.self += 0.5 * klt * nt;
+        } else {
+          for (int s = 0; s < nspec; s++) sl[1 + s] = (w.v(s, lg) * nt + w.v(s, tg) * nl) * klt * fix;
+          dnum = (klt * nl * nt) * fix;
+          sl[9] = 0.5 * (w.indef[lg] + w.indef[tg]) * dnum;
+          a.sink += (double)kget(w, tg, lg) * nl;
+        }
+        dvw = sl[1 + iwa];
+        if (diag) {
+          a.dg[0] += dvw;
+          if (D_new > 50.e-6) a.dg[2] += dvw;
+          if (D_new > 80.e-6) a.dg[1] += dvw;
+        }
+      } else {
+        sl[0] = -1.;
+        if (selfcoll) a.self += 0.5 * (double)kget(w, tg, lg) * nl;
+        else
+          for (int s = 0; s < nspec; s++) a.src[s] += klt * w.v(s, lg);
+      }
+      sl[8] = dnum;
+    }
+    __syncwarp();
+    // sum the staged contributions per precipitation bin (partner order)
+    for (int e = lane; e < nprc * (nspec + 2); e += 32) {
+      int tp = e / (nspec + 2), q = e % (nspec + 2);
+      double acc = 0.;
+      bool any = false;
+      for (int j = 0; j < np; j++) {
+        const double *sl = slot + j * 10;
+        if ((int)sl[0] == tp) { acc += (q < nspec) ? sl[1 + q] : (q == nspec ? sl[8] : sl[9]); any = true; }
+      }
+      if (any) {
+        if (q < nspec) vol_prc[tp * 7 + q] += acc;
+        else if (q == nspec) num_prc[tp] += acc;
+        else inf_prc[tp] += acc;
+      }
+    }
+    if (selfcoll && lane < nspec) {
+      // volsink_slf: the single self partner's contribution (same expression as dvol)
+      const double *sl = slot;
+      if ((int)sl[0] >= 0) pf[lane] += sl[1 + lane];
+    }
+    __syncwarp();
+  }
+}
+
+template <typename KT>
+__device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb, double dt, bool diag, int lane) {
+  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid, nprc = P.nprc;
+  const bool autoc1 = P.st_auto && P.auto_mode == 1;
+  double *pf = w.misc + M_PF;
+  for (int reg = 0; reg < 2; reg++) {
+    int kfirst = reg == 0 ? P.ica_cur : P.icb_cur;
+    int klast = reg == 0 ? P.fca_cur : P.fcb_cur;
+    int o_first = reg == 0 ? P.icb_cur : P.ica_cur;
+    int o_last = reg == 0 ? P.fcb_cur : P.fca_cur;
+    for (int kk = kfirst; kk <= klast; kk++) {
+      int tg = C0 + kk;
+      if (w.numc[tg] < K_NLIM) continue;
+      TAcc a;
+      a.zero();
+      if (autoc1) {
+        for (int e = lane; e < 7 + nprc * 9; e += 32) pf[e] = 0.;
+        __syncwarp();
+      }
+      int other = o_first + (kk - kfirst);
+      int rel = kk - kfirst;
+      if (P.lscgca && kk < klast) {
+        int iaa = P.ica_par + rel + 1, iab = P.icb_par + rel + 1;
+        for (int ll = iaa + lane; ll <= P.fn2a; ll += 32) a.sink += (double)kget(w, ll, tg) * w.numc[ll];
+        for (int ll = iab + lane; ll <= P.fn2b; ll += 32) a.sink += (double)kget(w, ll, tg) * w.numc[ll];
+      }
+      if (P.lscgcc) {
+        if (kk < klast) {
+          sink_range(w, tg, C0, kk + 1, klast, 1.0, a, false, lane);
+          sink_range(w, tg, C0, other, o_last, 1.0, a, false, lane);
+        }
+        if (autoc1) {
+          double n = w.numc[tg];
+          double fix = fmax(1. - dt * (0.5 * (double)kget(w, tg, tg) * (n * n) / n), 0.1);
+          precip_formation(P, w, tb, kk, kk, kk, fix, true, a, diag, lane);
+        } else {
+          sink_range(w, tg, C0, kk, kk, 0.5, a, true, lane);
+        }
+      }
+      if (P.lscgpc) sink_range(w, tg, P0, 0, nprc - 1, 1.0, a, false, lane);
+      if (P.lscgic) sink_range(w, tg, I0, 0, P.nice - 1, 1.0, a, false, lane);
+      if (P.lscgca) {
+        int iaa = P.ica_par + rel, iab = P.icb_par + rel;
+        double cm = 0.;
+        for (int ll = P.in1a + lane; ll <= iaa; ll += 32) {
+          double k = (double)kget(w, ll, tg);
+          for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, ll);
+          if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.v(s, ll) * P.rholiq[s];
+        }
+        for (int ll = P.in2b + lane; ll <= iab; ll += 32) {
+          double k = (double)kget(w, ll, tg);
+          for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, ll);
+          if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.v(s, ll) * P.rholiq[s];
+        }
+        a.dg[6] += cm;
+      }
+      if (P.lscgcc && kk > kfirst) {
+        if (autoc1) {
+          double s1 = 0.;
+          for (int i = kfirst + lane; i <= klast; i += 32) s1 += (double)kget(w, tg, C0 + i) * w.numc[C0 + i];
+          s1 = warp_sum(s1);
+          double fix = fmax(1. - dt * s1, 0.1);
+          precip_formation(P, w, tb, kk, kfirst, kk - 1, fix, false, a, diag, lane);
+          double s2 = 0.;
+          for (int i = o_first + lane; i <= o_last; i += 32) s2 += (double)kget(w, tg, C0 + i) * w.numc[C0 + i];
+          s2 = warp_sum(s2);
+          fix = fmax(1. - dt * s2, 0.1);
+          precip_formation(P, w, tb, kk, o_first, other, fix, false, a, diag, lane);
+        } else {
+          source_range(w, tg, C0, kfirst, kk - 1, nspec, a, lane);
+          source_range(w, tg, C0, o_first, other, nspec, a, lane);
+        }
+      }
+      a.reduce(diag);
+      if (diag && lane == 0) {
+        double nt = w.numc[tg];
+        w.misc[M_DIAG + DG_ACCOLL] += a.dg[6] * nt;
+        w.misc[M_DIAG + DG_AUTOC] += a.dg[0];
+        w.misc[M_DIAG + DG_AUTOC80] += a.dg[1];
+        w.misc[M_DIAG + DG_AUTOC50] += a.dg[2];
+      }
+      apply_coag(w, tg, nspec, dt, a, lane);
+      if (autoc1) {
+        // applyCoagPrecipFormation (:654-702)
+        const double *vol_prc = pf + 7, *num_prc = pf + 7 + 7 * nprc, *inf_num = num_prc + nprc;
+        if (lane < nspec) w.v(lane, tg) = w.v(lane, tg) - dt * pf[lane];
+        for (int e = lane; e < nprc * nspec; e += 32) {
+          int cc = e / nspec, s = e % nspec;
+          w.v(s, P0 + cc) = w.v(s, P0 + cc) + dt * vol_prc[cc * 7 + s];
+        }
+        __syncwarp();
+        for (int cc = lane; cc < nprc; cc += 32) {
+          int g = P0 + cc;
+          double nrate = num_prc[cc];
+          double inf = nrate > 0. ? inf_num[cc] / nrate : 0.;
+          double n = w.numc[g] + dt * nrate;
+          w.numc[g] = n;
+          if (n > K_PRLIM) w.indef[g] = (w.indef[g] * (n - dt * nrate) + inf * dt * nrate) / n;
+        }
+        __syncwarp();
+      }
+    }
+  }
+}
+
+template <typename KT>
+__device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb, double dt, bool diag, int lane) {
+  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid, nprc = P.nprc, iwa = P.iwa;
+  const double *pbins = tb + TAB_PRECPBINS * P.nb_pad;
+  for (int kk = 0; kk < nprc; kk++) {
+    int tg = P0 + kk;
+    if (w.numc[tg] < K_PRLIM) continue;
+    TAcc a;
+    a.zero();
+    double num_slf = 0.;
+    if (P.lscgpp) {
+      if (kk < nprc - 1) sink_range(w, tg, P0, kk + 1, nprc - 1, 1.0, a, false, lane);
+      else sink_range(w, tg, P0, kk, kk, 0.5, a, true, lane);
+    }
+    if (P.lscgip) sink_range(w, tg, I0, 0, P.nice - 1, 1.0, a, false, lane);
+    const double D = w.dwet[tg];
+    if (P.lscgpa) {
+      double cm = 0.;
+      for (int ll = P.in1a + lane; ll <= P.fn2b; ll += 32) {
+        double k = (double)kget(w, ll, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, ll);
+        if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.v(s, ll) * P.rholiq[s];
+      }
+      a.dg[6] += cm;
+    }
+    if (P.lscgpc) {
+      // source from cloud; accretion and autoconversion diagnostics (:1086-1215, coll phase 2)
+      for (int ll = lane; ll < P.ncld; ll += 32) {
+        int g = C0 + ll;
+        double k = (double)kget(w, g, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, g);
+        if (diag) {
+          double kw = k * w.v(iwa, g);
+          a.dg[3] += kw;
+          double dd = cube(D) + cube(w.dwet[g]);
+          if (D > 0. && D < 80.e-6 && dd > cube(80.e-6)) a.dg[1] += kw;
+          if (D > 0. && D < 50.e-6 && dd > cube(50.e-6)) a.dg[2] += kw;
+          if (pbins[kk] > 80.e-6) a.dg[4] += kw;
+          if (pbins[kk] > 50.e-6) a.dg[5] += kw;
+        }
+      }
+    }
+    if (P.lscgpp && kk > 0) {
+      int ex80 = min(kk - 1, P.cnt80 - 1), ex50 = min(kk - 1, P.cnt50 - 1);
+      for (int ll = lane; ll <= kk - 1; ll += 32) {
+        int g = P0 + ll;
+        double k = (double)kget(w, g, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, g);
+        if (diag) {
+          double kw = k * w.v(iwa, g);
+          double dd = cube(D) + cube(w.dwet[g]);
+          if (ll <= ex80 && D > 0. && D < 80.e-6 && dd > cube(80.e-6)) a.dg[1] += kw;
+          if (ll <= ex50 && D > 0. && D < 50.e-6 && dd > cube(50.e-6)) a.dg[2] += kw;
+          if (ll <= ex80 && pbins[kk] > 80.e-6) a.dg[4] += kw;
+          if (ll <= ex50 && pbins[kk] > 50.e-6) a.dg[5] += kw;
+        }
+      }
+    }
+    a.reduce(diag);
+    if (diag && lane == 0) {
+      double nt = w.numc[tg];
+      w.misc[M_DIAG + DG_APCOLL] += a.dg[6] * nt;
+      w.misc[M_DIAG + DG_ACCR] += a.dg[3] * nt;
+      w.misc[M_DIAG + DG_AUTOC80] += a.dg[1] * nt;
+      w.misc[M_DIAG + DG_AUTOC50] += a.dg[2] * nt;
+      w.misc[M_DIAG + DG_ACCR80] += a.dg[4] * nt;
+      w.misc[M_DIAG + DG_ACCR50] += a.dg[5] * nt;
+    }
+    // precipSelfCoag (:1588-1611) with the pre-update state
+    double kself = (P.lscgpp && kk < nprc - 1) ? (double)kget(w, tg, tg) : 0.;
+    double nold = w.numc[tg];
+    double vs_my = (lane < nspec) ? w.v(lane, tg) * nold * kself : 0.;
+    num_slf = 0.5 * kself * nold * nold;
+    apply_coag(w, tg, nspec, dt, a, lane);
+    if (P.lscgpp && kk < nprc - 1) {
+      // applyCoagPrecp (:584-599): self-coagulation products go to the next bin
+      if (lane < nspec) {
+        w.v(lane, tg + 1) = w.v(lane, tg + 1) + dt * vs_my;
+        w.v(lane, tg) = w.v(lane, tg) - dt * vs_my;
+      }
+      if (lane == 0) {
+        w.numc[tg + 1] = w.numc[tg + 1] + dt * num_slf;
+        w.numc[tg] = w.numc[tg] - dt * num_slf;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+template <typename KT>
+__device__ void coag_ice(const DevParams &P, const WS<KT> &w, double dt, int lane) {
+  const int nspec = P.nused, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid, nice = P.nice;
+  const int iwa = P.iwa, irim = P.irim, ndry = P.ndry;
+  (void)C0; (void)P0;
+  for (int kk = 0; kk < nice; kk++) {
+    int tg = I0 + kk;
+    if (w.numc[tg] < K_PRLIM) continue;
+    TAcc a;
+    a.zero();
+    double rf_t = rimefrac(P, w.numc[tg], w.v(iwa, tg), w.v(irim, tg), 4);
+    if (P.lscgii) {
+      // Eagg from the larger rime fraction of the pair (:758-769)
+      for (int ll = kk + 1 + lane; ll <= nice - 1; ll += 32) {
+        int g = I0 + ll;
+        double rf = fmax(rimefrac(P, w.numc[g], w.v(iwa, g), w.v(irim, g), 4), rf_t);
+        double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
+        a.sink += E * 1.0 * (double)kget(w, tg, g) * w.numc[g];
+      }
+      if (lane == 0) {
+        double E = P.Eiagg_max - fmax(rf_t, rf_t) * (P.Eiagg_max - P.Eiagg_min);
+        a.self += E * 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
+      }
+    }
+    // accumulateSourcePhaseChange (:1244-1280)
+    if (P.lscgia)
+      for (int ll = P.in1a + lane; ll <= P.fn2b; ll += 32) {
+        double k = (double)kget(w, ll, tg);
+        for (int s = 0; s < ndry; s++) a.src[s] += k * w.v(s, ll);
+        a.src[iwa] += k * w.v(iwa, ll) * K_RHOWA / K_RHOIC;
+      }
+    if (P.lscgic)
+      for (int ll = lane; ll < P.ncld; ll += 32) {
+        int g = C0 + ll;
+        double k = (double)kget(w, g, tg);
+        for (int s = 0; s < ndry; s++) a.src[s] += k * w.v(s, g);
+        a.src[irim] += k * w.v(iwa, g) * K_RHOWA / K_RHORI;
+      }
+    if (P.lscgip)
+      for (int ll = lane; ll < P.nprc; ll += 32) {
+        int g = P0 + ll;
+        double k = (double)kget(w, g, tg);
+        for (int s = 0; s < ndry; s++) a.src[s] += k * w.v(s, g);
+        a.src[irim] += k * w.v(iwa, g) * K_RHOWA / K_RHORI;
+      }
+    // accumulateSourceIce (:1385-1427)
+    if (P.lscgii && kk > 0)
+      for (int ll = lane; ll <= kk - 1; ll += 32) {
+        int g = I0 + ll;
+        double rf = fmax(rimefrac(P, w.numc[g], w.v(iwa, g), w.v(irim, g), 4), rf_t);
+        double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
+        double k = (double)kget(w, g, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += E * k * w.v(s, g);
+      }
+    a.reduce(false);
+    // applyCoagIce (:605-651): every species slot with the same semi-implicit form
+    apply_coag(w, tg, nspec, dt, a, lane);
+    if (lane == 0) w.rhomean[tg] = rhomean_of(P, 4, w.numc[tg], w.v(iwa, tg), w.v(irim, tg));
+    __syncwarp();
+  }
+}
+
+template <typename KT>
+__device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *tb, double dt, double T, double pres,
+                            bool diag, int lane) {
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  // updateDiameter("all") on every bin (:146-152) and rhomean of the kernel categories
+  for (int b = lane; b < P.ntotal; b += 32) {
+    updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, b);
+    int ph = phase_of(P, b);
+    bool inker = (ph == 1 && (P.lscgaa || P.lscgca || P.lscgpa || P.lscgia)) ||
+                 (ph == 2 && (P.lscgcc || P.lscgca || P.lscgpc || P.lscgic)) ||
+                 (ph == 3 && (P.lscgpp || P.lscgpa || P.lscgpc || P.lscgip)) ||
+                 (ph == 4 && (P.lscgii || P.lscgia || P.lscgic || P.lscgip));
+    if (inker) w.rhomean[b] = rhomean_of(P, ph, w.numc[b], w.v(P.iwa, b), w.v(P.irim, b));
+  }
+  __syncwarp();
+  build_kernels<KT>(P, w, tb, T, pres, lane);
+  bool any_aero = P.lscgaa || P.lscgca || P.lscgpa || P.lscgia;
+  bool any_cloud = P.lscgcc || P.lscgca || P.lscgpc || P.lscgic;
+  bool any_precp = P.lscgpp || P.lscgpa || P.lscgpc || P.lscgip;
+  bool any_ice = P.lscgii || P.lscgia || P.lscgic || P.lscgip;
+  if (any_ice && T < 273.15) coag_ice<KT>(P, w, dt, lane);
+  if (any_precp) coag_precp<KT>(P, w, tb, dt, diag, lane);
+  if (any_aero) coag_aero<KT>(P, w, dt, lane);
+  if (any_cloud) coag_cloud<KT>(P, w, tb, dt, diag, lane);
+  bool neg = false;
+  for (int b = lane; b < P.ntotal; b += 32) {
+    if (w.numc[b] < -1.e-6) neg = true;
+    w.numc[b] = fmax(0., w.numc[b]);
+    for (int s = 0; s < P.nused; s++) w.v(s, b) = fmax(0., w.v(s, b));
+  }
+  if (warp_any(neg) && lane == 0) w.misc[M_FLAGS + F_NEG] = 1.;
+  __syncwarp();
+}
+
+
+// ----------------------------------------------------------------------------------------
+// Water uptake: mo_salsa_properties.f90:73-380 equilibration.
+// Regime 1a carries the Kelvin factor zke from bin to bin (:170, set once before
+// the bin loop), so its bins are visited in order; regime 2 (init) restarts zke per
+// bin and runs lane-parallel.
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+__device__ __forceinline__ double zvolc_of(const DevParams &P, const WS<KT> &w, int which, int b) {
+  const int ix[7] = {P.ix_so4, P.ix_oc, P.ix_bc, P.ix_du, P.ix_ss, P.ix_no, P.ix_nh};
+  int d = ix[which];
+  return (d >= 0 && which < 5) ? w.v(d, b) : 0.;   // only the first five are copied (:148)
+}
+
+template <typename KT>
+__device__ double equil_iterate(const DevParams &P, const WS<KT> &w, int b, double zrh, double T, double &zke,
+                                double tol, bool regime2, double &zdwet_out, double &zcore_out, int &nonconv) {
+  double numc = w.numc[b];
+  double zv0 = zvolc_of(P, w, 0, b), zv1 = zvolc_of(P, w, 1, b), zv4 = zvolc_of(P, w, 4, b);
+  double zvp[7];
+  for (int i = 0; i < 7; i++) zvp[i] = zvolc_of(P, w, i, b) / numc;
+  double zcore = regime2 ? (zvp[0] + zvp[1] + zvp[2] + zvp[3] + zvp[4]) : (zvp[0] + zvp[1]);
+  double zdwet = w.dwet[b];
+  double zdold = 1.;
+  double zlwc = 0.;
+  int count = 0;
+  const double rhosu_msu = 1830. / 98.08e-3, rhooc_moc = 1400. / 150.e-3, rhoss_mss = 2165. / 58.44e-3;
+  while (fabs(zdwet / zdold - 1.) > tol) {
+    zdold = fmax(zdwet, 1.e-20);
+    double zaw = zrh / zke;
+    double a2 = zaw * zaw, a3 = a2 * zaw, a4 = a2 * a2;
+    double bm1 = +1.1065495e+2 - 3.6759197e+2 * zaw + 5.0462934e+2 * a2 - 3.1543839e+2 * a3 + 6.770824e+1 * a4;
+    double bm2 = 1. / (zaw * K_MWA) - 1. / K_MWA;
+    // nitric acid molality only multiplies a zero NO volume (NO not copied, :148) -> its term is zero
+    zlwc = (zv0 * rhosu_msu) / bm1 + K_EPSOC * zv1 * rhooc_moc / bm2;
+    if (regime2) {
+      double bm5 = +5.875248e+1 - 1.8781997e+2 * zaw + 2.7211377e+2 * a2 - 1.8458287e+2 * a3 + 4.153689e+1 * a4;
+      zlwc += (zv4 * rhoss_mss) / bm5;
+    }
+    zdwet = cbrt(zlwc / numc / K_RHOWA / K_PI6 + (zvp[5] + zvp[6]) / K_PI6 + zcore / K_PI6);
+    zke = exp(2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T * zdwet));
+    count++;
+    if (count > 100) { nonconv = 1; break; }
+  }
+  zdwet_out = zdwet;
+  zcore_out = zcore;
+  return zlwc;
+}
+
+template <typename KT>
+__device__ void equilibration(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
+                              int lane) {
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  int nonconv = 0;
+  // regime 1a, in bin order (all lanes run it; lane 0 writes)
+  {
+    double zke = 1.001;
+    for (int kk = P.in1a; kk <= P.fn1a; kk++) {
+      if (w.numc[kk] > K_NLIM) {
+        double zrh = fmin(fmax(prh, 0.05), 0.98);
+        double zd, zc;
+        double zlwc = equil_iterate<KT>(P, w, kk, zrh, T, zke, 1.e-2, false, zd, zc, nonconv);
+        __syncwarp();
+        if (lane == 0) {
+          w.v(P.iwa, kk) = zlwc / K_RHOWA;
+          if (init) w.dwet[kk] = zd;
+        }
+      } else if (init && lane == 0) {
+        w.dwet[kk] = dmid[kk];
+      }
+      __syncwarp();
+    }
+  }
+  if (init) {
+    for (int kk = P.in2a + lane; kk <= P.fn2b; kk += 32) {
+      if (w.numc[kk] > K_NLIM) {
+        double zke = 1.02;
+        double zrh = fmin(fmax(prh, 0.37), 0.98);
+        double zd, zc;
+        double zlwc = equil_iterate<KT>(P, w, kk, zrh, T, zke, 1.e-12, true, zd, zc, nonconv);
+        w.v(P.iwa, kk) = zlwc / K_RHOWA;
+        w.dwet[kk] = zd;
+      } else {
+        w.dwet[kk] = dmid[kk];
+      }
+    }
+  }
+  if (warp_any(nonconv) && lane == 0) w.misc[M_FLAGS + F_EQUIL] = 1.;
+  __syncwarp();
+}
+
+// ----------------------------------------------------------------------------------------
+// Condensation of water: mo_salsa_dynamics.f90:691-1125 gpparth2o, :1127-1157 acth2o.
+// Scratch (per global bin): 0 kelvin 1 cwsurf 2 mt 3 wsat 4 cw (current) 5 zns (solute
+// moles in acth2o) 6 orgic 7 orgri
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+__device__ __forceinline__ double solute_moles(const DevParams &P, const WS<KT> &w, int b, double kappa) {
+  double zns = 0.;
+  if (P.has_kappa) {
+    double vs = 0.;
+    for (int nn = 0; nn < P.ndry; nn++) if (P.diss[nn] > 0.) vs += w.v(nn, b);
+    zns = kappa * vs * K_RHOWA / K_MWA;
+  } else {
+    for (int nn = 0; nn < P.ndry; nn++) zns = zns + P.diss[nn] * w.v(nn, b) * P.rholiq[nn] / P.MM[nn];
+  }
+  return zns;
+}
+__device__ __forceinline__ double acth2o_w(double znw, double zns) { return fmax(0.1, znw / fmax(K_EPS, (znw + zns))); }
+
+template <typename KT>
+__device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres, double prs,
+                          double prsi, double &prv, double dt, double kappa, bool diag, int lane) {
+  const int nbins = P.nbins, ncld = P.ncld, nprc = P.nprc, nice = P.nice, ntot = P.ntotal;
+  const int iwa = P.iwa, irim = P.irim, C0 = nbins, P0 = nbins + ncld, I0 = P.nliquid;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const double zrh = prv / prs;
+  // aerosol water before/after the equilibrium update
+  double l1 = 0.;
+  for (int b = lane; b <= P.fn2b; b += 32) l1 += w.v(iwa, b);
+  double zaelwc1 = warp_sum(l1) * K_RHOWA;
+  // The init-form call repeats the 1a update with identical inputs (dwet untouched by
+  // the first call, zke restarted at 1.001), so running it alone gives the same state.
+  if (zrh < 0.98 || !P.lscndh2oae) equilibration<KT>(P, w, tb, zrh, T, true, lane);
+  else equilibration<KT>(P, w, tb, zrh, T, false, lane);
+  double l2 = 0.;
+  for (int b = lane; b <= P.fn2b; b += 32) l2 += w.v(iwa, b);
+  double zaelwc2 = warp_sum(l2) * K_RHOWA;
+  prv = prv - (zaelwc2 - zaelwc1) / (pres * K_MAIR / (K_RG * T));
+
+  bool anycl = false, anypr = false, anyic = false, anyae = false;
+  for (int b = lane; b < ntot; b += 32) {
+    int ph = phase_of(P, b);
+    double n = w.numc[b];
+    if (ph == 1) anyae |= n > K_NLIM;
+    else if (ph == 2) anycl |= n > K_NLIM;
+    else if (ph == 3) anypr |= n > K_PRLIM;
+    else anyic |= n > K_PRLIM;
+  }
+  anyae = warp_any(anyae); anycl = warp_any(anycl); anypr = warp_any(anypr); anyic = warp_any(anyic);
+  if (!((anycl || (anypr && P.lscndh2ocl)) || (anyic && P.lscndh2oic) || (anyae && zrh > 0.98 && P.lscndh2oae)))
+    return;
+
+  const double rhoair = K_MAIR * pres / (K_RG * T);
+  double zdfh2o = (5. / (16. * K_AVOG * rhoair * 1.e-3 * sq(3.11e-8))) *
+                  sqrt(K_RG * 1.e7 * T * K_MAIR * 1.e3 * (K_MWA + K_MAIR) * 1.e3 / (2. * K_PI * K_MWA * 1.e3));
+  zdfh2o = zdfh2o * 1.e-4;
+  const double zmfph2o = 3. * zdfh2o * sqrt(K_PI * K_MWA / (8. * K_RG * T));
+  const double zthcond = 0.023807 + 7.1128e-5 * (T - 273.16);
+  const int NB = w.NB;
+  double *kel = w.sc(0), *surf = w.sc(1), *mt = w.sc(2), *wsat = w.sc(3), *cw = w.sc(4), *zns = w.sc(5),
+         *orgic = w.sc(6), *orgri = w.sc(7);
+  (void)NB;
+  // diameters and densities (:819-822), then per-bin coefficients (:826-955)
+  for (int b = lane; b < ntot; b += 32) {
+    updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, b);
+    int ph = phase_of(P, b);
+    w.rhomean[b] = rhomean_of(P, ph, w.numc[b], w.v(iwa, b), w.v(irim, b));
+    double n = w.numc[b];
+    double k_ = 1., sf = 0., m = 0., ws = 0.;
+    double ns_ = (ph <= 3) ? solute_moles(P, w, b, kappa) : 0.;
+    bool act;
+    if (ph == 1) act = n > K_NLIM && zrh > 0.98 && P.lscndh2oae;
+    else if (ph == 2) act = n > K_NLIM && P.lscndh2ocl;
+    else if (ph == 3) act = n > K_PRLIM && P.lscndh2ocl;
+    else act = n > K_PRLIM && P.lscndh2oic && T < 273.15;
+    if (act) {
+      if (ph <= 3) {
+        double dwet = w.dwet[b];
+        double znw = w.v(iwa, b) * P.rholiq[iwa] / P.MM[iwa];
+        double zact = acth2o_w(znw, ns_);
+        k_ = exp(4. * K_SURFW0 * K_MWA / (K_RG * T * K_RHOWA * dwet));
+        sf = prs * rhoair / K_MWA;
+        ws = zact * k_;
+        KT zknud = (KT)2. * (KT)zmfph2o / (KT)dwet;
+        KT zbeta = (zknud + (KT)1.) / ((KT)0.377 * zknud + (KT)1. + (KT)4. / ((KT)3. * (KT)1.) * (zknud + zknud * zknud));
+        KT h1 = (KT)n * (KT)2. * (KT)K_PI * (KT)dwet * (KT)zdfh2o * zbeta;
+        KT h2 = (KT)K_MWA * (KT)zdfh2o * (KT)K_ALV * (KT)ws * (KT)sf / ((KT)zthcond * (KT)T);
+        KT h3 = (((KT)K_ALV * (KT)K_MWA) / ((KT)K_RG * (KT)T)) - (KT)1.;
+        m = (double)(h1 / (h2 * h3 + (KT)1.));
+      } else {
+        double dwet = w.dnsp[b];
+        double cap = 0.5 * dwet;
+        k_ = exp(4. * K_SURFI0 * K_MWA / (K_RG * T * K_RHOWA * dwet));
+        sf = prsi * rhoair / K_MWA;
+        ws = 1.0 * k_;
+        KT zknud = (KT)2. * (KT)zmfph2o / (KT)dwet;
+        KT zbeta = (zknud + (KT)1.) / ((KT)0.377 * zknud + (KT)1. + (KT)4. / (KT)3. * (zknud + zknud * zknud));
+        KT h1 = (KT)n * (KT)4. * (KT)K_PI * (KT)cap * (KT)zdfh2o * zbeta;
+        KT h2 = (KT)K_MWA * (KT)zdfh2o * (KT)K_ALS * (KT)ws * (KT)sf / ((KT)zthcond * (KT)T);
+        KT h3 = (((KT)K_ALS * (KT)K_MWA) / ((KT)K_RG * (KT)T)) - (KT)1.;
+        m = (double)(h1 / (h2 * h3 + (KT)1.));
+      }
+    }
+    kel[b] = k_; surf[b] = sf; mt[b] = m; wsat[b] = ws; zns[b] = ns_;
+    if (ph <= 3) {
+      cw[b] = w.v(iwa, b) * K_RHOWA / K_MWA;
+      orgic[b] = orgri[b] = 0.;
+    } else {
+      double c1 = w.v(iwa, b) * K_RHOIC / K_MWA;
+      cw[b] = c1 + w.v(irim, b) * K_RHORI / K_MWA;
+      orgic[b] = w.v(iwa, b) * K_RHOIC / K_MWA;
+      orgri[b] = w.v(irim, b) * K_RHORI / K_MWA;
+    }
+  }
+  __syncwarp();
+  // categories updated inside the substep loop (:1002-1031)
+  bool upd_ae = false, upd_cl = false, upd_pr = false, upd_ic = false;
+  {
+    bool a = false, c = false, p = false, i = false;
+    for (int b = lane; b < ntot; b += 32) {
+      int ph = phase_of(P, b);
+      double n = w.numc[b];
+      if (ph == 1) a |= n > K_NLIM; else if (ph == 2) c |= n > K_NLIM; else if (ph == 3) p |= n > K_PRLIM; else i |= n > K_PRLIM;
+    }
+    upd_ae = warp_any(a) && zrh > 0.98; upd_cl = warp_any(c); upd_pr = warp_any(p); upd_ic = warp_any(i);
+  }
+  double zcwc = prv * rhoair / K_MWA;
+  double tsum = 0., msum = 0.;
+  for (int b = lane; b < ntot; b += 32) {
+    tsum += cw[b];
+    if (b >= P.in2a) msum += mt[b];   // the substep sums skip regime 1a (nstr = in2a)
+  }
+  const double zcwtot = zcwc + warp_sum(tsum);
+  const double mtot = warp_sum(msum);
+  double ttot = 0., zcwint = 0.;
+  int counter = 0;
+  while (ttot < dt) {
+    const double adt = 2.e-2;
+    double sp = 0.;
+    for (int b = P.in2a + lane; b < ntot; b += 32) sp += mt[b] * wsat[b] * surf[b];
+    double zhlp1 = zcwc + adt * warp_sum(sp);
+    double zhlp2 = 1. + adt * mtot;
+    zcwint = fmin(zhlp1 / zhlp2, zcwtot);
+    double cs = 0.;
+    for (int b = lane; b < ntot; b += 32) {
+      int ph = phase_of(P, b);
+      double c = cw[b];
+      bool upd = (ph == 1) ? (upd_ae && b >= P.in2a) : (ph == 2 ? upd_cl : (ph == 3 ? upd_pr : upd_ic));
+      if (upd) {
+        double ci = c + fmin(fmax(adt * mt[b] * (zcwint - wsat[b] * surf[b]), -1.e-1 * c), 1.e-1 * c);
+        wsat[b] = (ph <= 3) ? acth2o_w(ci, zns[b]) * kel[b] : kel[b];
+        c = fmax(ci, 0.);
+      }
+      cw[b] = c;
+      cs += c;
+    }
+    zcwint = zcwtot - warp_sum(cs);
+    zcwc = zcwint;
+    ttot = ttot + adt;
+    counter++;
+    if (counter >= 200000) break;   // the C-ABI bounds tstep, so this cap is never the exit path
+  }
+  if (counter > 100 && lane == 0) w.misc[M_FLAGS + F_COND] = 1.;
+  prv = zcwint * K_MWA / rhoair;
+  // Cond_i diagnostic (:1086-1112): vrate(irim) is only assigned on sublimation and keeps
+  // its previous value on later deposition bins; the sum follows the ice bins in order.
+  double dci = 0.;
+  if (diag && lane == 0) {
+    double vr_last = 0.;
+    for (int k = 0; k < nice; k++) {
+      int b = I0 + k;
+      double dvitot = cw[b] - (orgic[b] + orgri[b]);
+      if (dvitot > 0.) {
+        dci += dvitot * K_MWA / K_RHOIC * K_RHOIC + vr_last * K_RHORI;
+      } else if (dvitot < 0.) {
+        double f = (cw[b] / (orgic[b] + orgri[b])) - 1.;
+        vr_last = f * orgri[b] * K_MWA / K_RHORI;
+        dci += f * orgic[b] * K_MWA / K_RHOIC * K_RHOIC + vr_last * K_RHORI;
+      }
+    }
+  }
+  __syncwarp();
+  // write back and diagnostics (:1061-1117)
+  double dca = 0., dcc = 0., dcp = 0.;
+  for (int b = lane; b < ntot; b += 32) {
+    int ph = phase_of(P, b);
+    if (ph <= 3) {
+      double nv = fmax(0., cw[b] * K_MWA / K_RHOWA);
+      double d = nv - w.v(iwa, b);
+      if (ph == 1) dca += d; else if (ph == 2) dcc += d; else dcp += d;
+      w.v(iwa, b) = nv;
+    } else {
+      double dvitot = cw[b] - (orgic[b] + orgri[b]);
+      if (dvitot > 0.) {
+        double dv = dvitot * K_MWA / K_RHOIC;
+        w.v(iwa, b) = w.v(iwa, b) + dv;
+      } else if (dvitot < 0.) {
+        double f = (cw[b] / (orgic[b] + orgri[b])) - 1.;
+        double dvice = f * orgic[b], dvrime = f * orgri[b];
+        w.v(iwa, b) = w.v(iwa, b) + dvice * K_MWA / K_RHOIC;
+        w.v(irim, b) = w.v(irim, b) + dvrime * K_MWA / K_RHORI;
+      }
+    }
+    if (w.numc[b] > nlim_of(ph)) w.rhomean[b] = rhomean_of(P, ph, w.numc[b], w.v(iwa, b), w.v(irim, b));
+  }
+  if (diag) {
+    dca = warp_sum(dca); dcc = warp_sum(dcc); dcp = warp_sum(dcp);
+    if (lane == 0) {
+      w.misc[M_DIAG + DG_CONDA] += dca;
+      w.misc[M_DIAG + DG_CONDC] += dcc;
+      w.misc[M_DIAG + DG_CONDP] += dcp;
+      w.misc[M_DIAG + DG_CONDI] += dci;
+    }
+  }
+  __syncwarp();
+}
+
+// ----------------------------------------------------------------------------------------
+// Interstitial activation: mo_salsa_cloud.f90:859-1195 actInterst (+ intgN/intgV :1381-1398)
+// Lanes own cloud bins; the transfer touches only the parallel aerosol bin.
+// ----------------------------------------------------------------------------------------
+__device__ __forceinline__ double intgN(double k, double c, double lo, double hi) {
+  return 0.5 * k * fmax(hi * hi - lo * lo, 0.) + c * fmax(hi - lo, 0.);
+}
+__device__ __forceinline__ double intgV(double k, double c, double lo, double hi) {
+  return (1. / 3.) * k * fmax(cube(hi) - cube(lo), 0.) + 0.5 * c * fmax(hi * hi - lo * lo, 0.);
+}
+
+template <typename KT>
+__device__ void act_interst(const DevParams &P, const WS<KT> &w, const double *tb, double prv, double prs, double T,
+                            bool diag, int lane) {
+  if (prv / prs <= 1.000) return;
+  const int ndry = P.ndry, nwet = P.nwet, iwa = P.iwa, C0 = P.nbins;
+  const double *dmid = tb + TAB_DMID * P.nb_pad, *vrlo = tb + TAB_VRLO * P.nb_pad, *vrhi = tb + TAB_VRHI * P.nb_pad;
+  const double THvol = 1.e-28;
+  double zkelvin = 4. * K_MWA * K_SURFW0 / (K_RG * K_RHOWA * T);
+  double zdcstar = 2. * zkelvin / (3. * ((prv / prs) - 1.));
+  double zvcstar = K_PI6 * cube(zdcstar);
+  double *actn = w.sc(8);        // per cloud bin
+  double *actv = w.sc(0);        // [s * NB + cb] (reuses condensation scratch 0..nwet-1)
+  double nsum = 0.;
+  for (int cb = lane; cb < P.ncld; cb += 32) {
+    int ab = (cb <= P.fca_cur) ? P.ica_par + (cb - P.ica_cur) : P.icb_par + (cb - P.icb_cur);
+    double an = 0.;
+    double av[SALSA_NSV];
+    for (int s = 0; s < SALSA_NSV; s++) av[s] = 0.;
+    double vol_sol = 0.;
+    for (int i = 0; i < P.nsoluble; i++) vol_sol += w.v(P.ind_soluble[i], ab);
+    double Nmid = w.numc[ab];
+    bool go = !(Nmid < K_NLIM) && !(vol_sol < Nmid * THvol) && !(w.v(iwa, ab) < Nmid * THvol);
+    if (go) {
+      double Vwmid = 0., Vmid = 0.;
+      for (int s = 0; s < nwet; s++) Vwmid += w.v(s, ab);
+      Vwmid /= Nmid;
+      for (int s = 0; s < ndry; s++) Vmid += w.v(s, ab);
+      Vmid /= Nmid;
+      double Vlo = Vmid * vrlo[ab], Vhi = Vmid * vrhi[ab];
+      double Nim1, Vim1, Vlom1, Vhim1, Vwim1, Nip1, Vip1, Vlop1, Vhip1, Vwip1;
+      if (ab == P.in1a || ab == P.in2b) {
+        Nim1 = K_NLIM; Vim1 = Vlo / 2.; Vlom1 = 0.; Vhim1 = Vlo; Vwim1 = Vim1;
+      } else {
+        Nim1 = w.numc[ab - 1];
+        if (Nim1 > K_NLIM) {
+          double vd = 0., vw = 0.;
+          for (int s = 0; s < ndry; s++) vd += w.v(s, ab - 1);
+          for (int s = 0; s < nwet; s++) vw += w.v(s, ab - 1);
+          Vim1 = vd / Nim1; Vwim1 = vw / Nim1;
+        } else {
+          Vim1 = K_PI6 * cube(dmid[ab - 1]); Vwim1 = K_PI6 * cube(dmid[ab - 1]);
+        }
+        Vlom1 = Vim1 * vrlo[ab - 1]; Vhim1 = Vim1 * vrhi[ab - 1];
+      }
+      if (ab == P.fn2a || ab == P.fn2b) {
+        Nip1 = K_NLIM; Vip1 = Vhi + 0.5 * (Vhi - Vlo); Vlop1 = Vhi; Vhip1 = Vhi + (Vhi - Vlo); Vwip1 = Vip1;
+      } else {
+        Nip1 = w.numc[ab + 1];
+        if (Nip1 > K_NLIM) {
+          double vd = 0., vw = 0.;
+          for (int s = 0; s < ndry; s++) vd += w.v(s, ab + 1);
+          for (int s = 0; s < nwet; s++) vw += w.v(s, ab + 1);
+          Vip1 = vd / Nip1; Vwip1 = vw / Nip1;
+        } else {
+          Vip1 = K_PI6 * cube(dmid[ab + 1]); Vwip1 = K_PI6 * cube(dmid[ab + 1]);
+        }
+        Vlop1 = Vip1 * vrlo[ab + 1]; Vhip1 = Vip1 * vrhi[ab + 1];
+      }
+      Vip1 = fmax(Vhi, Vip1);
+      Vim1 = fmin(Vlo, Vim1);
+      double zs1 = (Vwmid - fmax(Vwim1, 0.)) / (Vmid - Vim1);
+      double zs2 = (fmax(Vwip1, 0.) - Vwmid) / (Vip1 - Vmid);
+      double V01 = Vwmid - zs1 * Vmid, V02 = Vwmid - zs2 * Vmid;
+      double Vwlo = fmax(V01 + zs1 * Vlo, Vlo), Vwhi = fmax(V02 + zs2 * Vhi, Vhi);
+      double vint1, vint2;
+      bool r1, r2, r3, r4;
+      if (zvcstar < Vwlo && zvcstar < Vwmid && zvcstar < Vwhi) {
+        vint1 = Vlo; vint2 = Vhi; r1 = r2 = r3 = r4 = true;
+      } else if (zvcstar > Vwlo && zvcstar > Vwmid && zvcstar > Vwhi) {
+        vint1 = 999.; vint2 = 999.; r1 = r2 = r3 = r4 = false;
+      } else {
+        double vcut = (zvcstar - V01) / zs1;
+        vint1 = (vcut < Vlo || vcut > Vmid) ? Vlo : vcut;
+        vcut = (zvcstar - V02) / zs2;
+        vint2 = (vcut < Vmid || vcut > Vhi) ? Vmid : vcut;
+        r1 = Vwlo > zvcstar; r2 = Vwmid > zvcstar; r3 = Vwmid > zvcstar; r4 = Vwhi > zvcstar;
+      }
+      double dNim1 = Nim1 / (Vhim1 - Vlom1), dNip1 = Nip1 / (Vhip1 - Vlop1), dNmid = Nmid / (Vhi - Vlo);
+      zs1 = (dNmid - dNim1) / (Vmid - Vim1);
+      zs2 = (dNip1 - dNmid) / (Vip1 - Vmid);
+      double N01 = dNmid - zs1 * Vmid, N02 = dNmid - zs2 * Vmid;
+      double Nnorm = intgN(zs1, N01, Vlo, Vmid) + intgN(zs2, N02, Vmid, Vhi);
+      double Vnorm = intgV(zs1, N01, Vlo, Vmid) + intgV(zs2, N02, Vmid, Vhi);
+      double zactvol = 0., Nact = 0.;
+      if (r1) { Nact += (Nmid / Nnorm) * intgN(zs1, N01, Vlo, vint1); zactvol += (Nmid * Vmid / Vnorm) * intgV(zs1, N01, Vlo, vint1); }
+      if (r2) { Nact += (Nmid / Nnorm) * intgN(zs1, N01, vint1, Vmid); zactvol += (Nmid * Vmid / Vnorm) * intgV(zs1, N01, vint1, Vmid); }
+      if (r3) { Nact += (Nmid / Nnorm) * intgN(zs2, N02, Vmid, vint2); zactvol += (Nmid * Vmid / Vnorm) * intgV(zs2, N02, Vmid, vint2); }
+      if (r4) { Nact += (Nmid / Nnorm) * intgN(zs2, N02, vint2, Vhi); zactvol += (Nmid * Vmid / Vnorm) * intgV(zs2, N02, vint2, Vhi); }
+      an = fmin(Nact, Nmid);
+      for (int s = 0; s < nwet; s++) av[s] = fmin(zactvol * (w.v(s, ab) / (Vmid * Nmid)), w.v(s, ab));
+    }
+    actn[cb] = an;
+    for (int s = 0; s < nwet; s++) actv[s * w.NB + cb] = av[s];
+    nsum += an;
+  }
+  __syncwarp();
+  if (diag) {
+    nsum = warp_sum(nsum);
+    if (lane == 0) w.misc[M_DIAG + DG_ACTIV] += nsum;
+  }
+  for (int cb = lane; cb < P.ncld; cb += 32) {
+    int ab = P.ica_par + cb, cg = C0 + cb;
+    double an = actn[cb];
+    if (an > 0.) w.ctime[cg] = (an * P.chargeTimeMax + w.numc[cg] * w.ctime[cg]) / (an + w.numc[cg]);
+    w.numc[ab] = fmax(0., w.numc[ab] - an);
+    double nc = w.numc[cg] + an;
+    w.numc[cg] = nc;
+    for (int s = 0; s < nwet; s++) {
+      double av = actv[s * w.NB + cb];
+      w.v(s, ab) = fmax(0., w.v(s, ab) - av);
+      w.v(s, cg) = w.v(s, cg) + av;
+    }
+    if (nc > 0.) w.indef[cg] = (w.indef[cg] * (nc - an) + w.indef[ab] * an) / nc;
+  }
+  __syncwarp();
+}
+
+// mo_salsa_cloud.f90:1401-1477 autoconv2 (cloud bins from the largest; all move to precip bin 1)
+template <typename KT>
+__device__ void autoconv2(const DevParams &P, const WS<KT> &w, double dt, int lane) {
+  if (lane == 0) {
+    const double zd0 = 50.e-6, sigmag = 1.2, max_rate_autoc = 1.0e10;
+    const int C0 = P.nbins, P0 = P.nbins + P.ncld;
+    for (int cc = P.ncld - 1; cc >= 0; cc--) {
+      int g = C0 + cc;
+      double tot = 0.;
+      double Ntot = w.numc[g], Vtot = 0.;
+      for (int s = 0; s < P.nwet; s++) Vtot += w.v(s, g);
+      if (Ntot > K_NLIM && Vtot > 0.) {
+        double ls = log(sigmag);
+        double dvg = cbrt(Vtot / Ntot / K_PI6) * exp((3. * ls * ls) / 2.);
+        double dg = dvg * exp(-3. * ls * ls);
+        double hlp2 = sqrt(2.) * ls;
+        double Vrem = Vtot * (1. - (0.5 + 0.5 * erf((log(zd0) - log(dvg)) / hlp2)));
+        double Nrem = Ntot * (1. - (0.5 + 0.5 * erf((log(zd0) - log(dg)) / hlp2)));
+        if (Vrem > 0. && Nrem > K_PRLIM) {
+          for (int s = 0; s < P.ndry; s++) {
+            w.v(s, P0) = w.v(s, P0) + w.v(s, g) * (Nrem / Ntot);
+            w.v(s, g) = w.v(s, g) * (1. - (Nrem / Ntot));
+          }
+          w.v(P.iwa, P0) = w.v(P.iwa, P0) + w.v(P.iwa, g) * (Vrem / Vtot);
+          w.v(P.iwa, g) = w.v(P.iwa, g) * (1. - (Vrem / Vtot));
+          w.numc[P0] = w.numc[P0] + Nrem;
+          w.numc[g] = w.numc[g] - Nrem;
+          tot = tot + Nrem;
+          if (tot > max_rate_autoc * dt) break;
+        }
+      }
+    }
+  }
+  __syncwarp();
+}
+
+
+// ----------------------------------------------------------------------------------------
+// Ice nucleation with contact-angle distributions: mo_salsa_cloud_ice_SE.f90:28-555.
+// Lanes own liquid bins; each lane stages what its bin hands to the ice bins, and the
+// ice bins then add the staged amounts in liquid-bin order (the reference order).
+// ----------------------------------------------------------------------------------------
+__device__ __constant__ double c_gl_x[10] = {-0.973908239224106, -0.865060566454542, -0.679410688379483,
+                                             -0.433395397408358, -0.148874339007507, 0.148874339007507,
+                                             0.433395397408358,  0.679410688379483,  0.865060566454542,
+                                             0.973908239224106};
+__device__ __constant__ double c_gl_w[10] = {0.066667031481273176, 0.14945422671662059, 0.21908574324601154,
+                                             0.26926671836765848,  0.29552422471242434, 0.29552422471242434,
+                                             0.26926671836765848,  0.21908574324601154, 0.14945422671662059,
+                                             0.066667031481273176};
+
+__device__ double erfm1(double x) {   // math_functions.f90:494-510
+  const double a = 0.140012;
+  double sgn = x < 0. ? -1. : 1.;
+  double xx = fmax(1.e-20, 1. - x * x);
+  double t1 = log(xx), t2 = 2. / (K_PI_FULL * a);
+  double t3 = t2 + 0.5 * t1, t4 = t1 / a, t5 = t2 + 0.5 * t1;
+  return sgn * sqrt(sqrt(t3 * t3 - t4) - t5);
+}
+__device__ __forceinline__ double f_gauss(double x, double sig, double mean) {   // :515-524
+  double a = sqrt(2. * K_PI_FULL) * sig;
+  double b = (x - mean) * (x - mean);
+  b = b / (sig * sig);
+  return (1. / a) * exp(-0.5 * b);
+}
+__device__ double het_sf(double x, double mis) {   // SE :375-390
+  if (x > 100.) return (cube(mis) - 3. * mis + 2.) / 4.;
+  double fii = sqrt(1. - 2. * mis * x + x * x);
+  double fpsi = (x - mis) / fii;
+  return 0.5 * (1. + cube((1. - mis * x) / fii) + (2. - 3. * fpsi + cube(fpsi)) * cube(x) + 3. * mis * (fpsi - 1.) * x * x);
+}
+
+// Temperature-only parts of J_imm (:210-278), evaluated once per cell and bin
+struct JimmPre { double act_energy, sigma_is, d_g; bool ok; };
+__device__ JimmPre jimm_pre(double Tk, double Seq) {
+  JimmPre r;
+  const double rho_ice = 900., T0 = 273.15;
+  double Tc = Tk - T0;
+  r.act_energy = K_RG * Tk * (347. / (Tk - 177.) - log(4.14 / 349.)) / K_AVOG;
+  r.sigma_is = 28.e-3 + 0.25e-3 * Tc;
+  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double GG = K_RG * Tk / K_MWA / Lefm;
+  double sg = pow(Seq, GG);
+  r.ok = !((T0 / Tk) * sg < 1.0001);
+  r.d_g = r.ok ? 4. * r.sigma_is / (rho_ice * Lefm * log((T0 / Tk) * sg) - 1.7e10 * 0.) : 0.;
+  if (r.d_g <= 1e-10) r.ok = false;
+  return r;
+}
+__device__ double J_imm(const JimmPre &q, double theta, double Tk, double Din) {
+  if (Din < 1e-10 || !q.ok) return 0.;
+  double costh = cos(theta * K_PI / 180.);
+  double sf = het_sf(Din / q.d_g, costh);
+  double crit = (K_PI / 3.) * q.sigma_is * (q.d_g * q.d_g) * sf - (1. / 4.) * 0.0 * (1. - costh) * Din * Din;
+  return (K_BOLTZ * Tk / K_PLANCK) * 1.e19 * K_PI * (Din * Din) * exp(-(q.act_energy + crit) / (K_BOLTZ * Tk));
+}
+__device__ double J_dep(double theta, double Tk, double Din, double Seq) {   // :282-331
+  if (Din < 1e-10 || Seq < 1.0001) return 0.;
+  double Tc = Tk - 273.15;
+  double sigma_iv = ((76.1 - 0.155 * Tc) + (28.5 + 0.25 * Tc)) * 1.e-3;
+  double d_g = 4. * sigma_iv / (K_RG * K_RHOIC / K_MWA * Tk * log(Seq) - 1.7e10 * 0.);
+  if (d_g <= 1e-10) return 0.;
+  double costh = cos(theta * K_PI / 180.);
+  double sf = het_sf(Din / d_g, costh);
+  double crit = (K_PI / 3.) * sigma_iv * (d_g * d_g) * sf;
+  return (1. / 4.) * 1.e30 * (Din * Din) * exp(-(0. + crit) / (K_BOLTZ * Tk));
+}
+__device__ double J_hf(double Tk, double Sw) {   // :335-371
+  const double Nc = 5.85e16, T0 = 273.15;
+  double Tc = Tk - T0;
+  double act = 0.694e-19 * (1. + 0.027 * (Tc + 30.));
+  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double GG = K_RG * Tk / Lefm / K_MWA;
+  double sg = pow(Sw, GG);
+  if ((T0 / Tk) * sg < 1.0001) return 0.;
+  double sigma_is = 28.e-3 + 0.25e-3 * Tc;
+  double d_g = 4. * sigma_is / (K_RHOIC * Lefm * log((T0 / Tk) * sg));
+  if (d_g <= 1e-10) return 0.;
+  double crit = (K_PI / 3.) * sigma_is * d_g * d_g;
+  return 2.0 * Nc * (K_RHOWA * K_BOLTZ * Tk / K_RHOIC / K_PLANCK) * sqrt(sigma_is / K_BOLTZ / Tk) *
+         exp(-(crit + act) / (K_BOLTZ * Tk));
+}
+
+// calcSweq (mo_particle_external_properties.f90:402-447)
+template <typename KT>
+__device__ double calc_sweq(const DevParams &P, const WS<KT> &w, int b, double T, double kappa) {
+  double n = w.numc[b];
+  if (n < nlim_of(phase_of(P, b))) return 0.;
+  double vs = 0.;
+  for (int s = 0; s < P.nused; s++) vs += w.v(s, b);
+  double dwet = cbrt(vs / n / K_PI6);
+  double znw = w.v(P.iwa, b) * K_RHOWA / K_MWA, zvw = w.v(P.iwa, b);
+  double zns = 0., zvs = 0., zvtot = 0.;
+  for (int i = 0; i < P.ndry; i++) {
+    zns = zns + P.diss[i] * w.v(i, b) * P.rholiq[i] / P.MM[i];
+    zvs = zvs + fmin(1., P.diss[i]) * w.v(i, b);
+    zvtot = zvtot + w.v(i, b);
+  }
+  if (P.has_kappa) zns = solute_moles(P, w, b, kappa);
+  double kel = exp(4. * K_SURFW0 * K_MWA / (K_RG * T * K_RHOWA * dwet));
+  if (zvw > 1.e-28 * n || zvs > 1.e-28 * n) return (znw / (zns + znw)) * kel;
+  if (zvtot - zvs > 1.e-28 * n) return kel;
+  return (znw / (K_EPS + zns + znw)) * kel;
+}
+
+__device__ __forceinline__ int ice_bin_of(const DevParams &P, const double *vlo, double dwet) {   // :542-555
+  double vol = K_PI6 * cube(dwet) * K_RHOWA / K_RHOIC;
+  int ii = 0;
+  for (int k = 0; k < P.nice; k++) ii += (vlo[P.nliquid + k] < vol);
+  return min(max(1, ii), P.nice) - 1;
+}
+__device__ __forceinline__ int precip_bin_of(const DevParams &P, const double *vlo, double dwet, double dens) {
+  double vol = K_PI6 * cube(dwet) * dens / K_RHOWA;   // :559-573
+  int ii = 0;
+  for (int k = 0; k < P.nprc; k++) ii += (vlo[P.nbins + P.ncld + k] < vol);
+  return min(max(1, ii), P.nprc) - 1;
+}
+
+// staged ice contribution of one liquid bin: [0] target ice bin (-1 none), [1..nused] volumes, [8] number
+template <typename KT>
+__device__ void ice_apply_staged(const DevParams &P, const WS<KT> &w, const double *stage, int nsrc, int lane) {
+  // one lane per ice bin and component, sources in order
+  const int ncomp = P.nused + 1;
+  for (int e = lane; e < P.nice * ncomp; e += 32) {
+    int ib = e / ncomp, q = e % ncomp, g = P.nliquid + ib;
+    double val = (q < P.nused) ? w.v(q, g) : w.numc[g];
+    for (int k = 0; k < nsrc; k++) {
+      const double *st = stage + k * 10;
+      if ((int)st[0] != ib) continue;
+      double add = (q < P.nused) ? st[1 + q] : st[8];
+      if (add != 0. || st[9] != 0.) val = fmax(0., val + add);
+    }
+    if (q < P.nused) w.v(q, g) = val; else w.numc[g] = val;
+  }
+  __syncwarp();
+}
+
+template <typename KT>
+__device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *tb, double T, double prv, double prs,
+                            double prsi, double dt, double kappa, bool diag, int lane) {
+  if (P.ninsoluble <= 0) return;
+  const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad;
+  const double dmin = 1.e-10, tmax_homog = 237.9, minVin = K_PI6 * cube(1.e-8);
+  const int nl = P.nliquid, ndry = P.ndry, iwa = P.iwa, irim = P.irim, idu = P.ix_du;
+  double *stage = w.scr;   // nl * 10 doubles
+  double dh = 0., dd = 0., di = 0.;
+  for (int kk = lane; kk < nl; kk += 32) {
+    double *st = stage + kk * 10;
+    for (int q = 0; q < 10; q++) st[q] = 0.;
+    st[0] = -1.;
+    double Seq = calc_sweq(P, w, kk, T, kappa);
+    double Si = prv / prsi;
+    updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, kk);
+    double dwet = w.dwet[kk], dins_ = w.ddry[kk];
+    double n = w.numc[kk];
+    int ph = phase_of(P, kk);
+    double f_hom = 0., f_imm = 0., f_dep = 0.;
+    if (dwet - dins_ > dmin && T < tmax_homog && P.lsicehom) {
+      double Jh = J_hf(T, Seq);
+      f_hom = 1. - exp(-Jh * K_PI6 * (cube(dwet) - cube(dins_)) * dt);
+    }
+    bool countable = !(T > 273.15) && !(n < nlim_of(ph));
+    if (P.lsiceimm) {
+      // low_theta (:394-417)
+      double th00 = P.mean_theta_imm + sqrt(2.) * P.sigma_theta_imm * erfm1(2. * w.indef[kk] - 1.);
+      th00 = fmin(fmax(th00, 0.), 180.);
+      if (!P.st_freeTheta) th00 = fmax(P.initMinTheta, th00);
+      bool mask = (ph == 2 || ph == 3) && (w.dins[kk] > dmin);
+      if (mask && countable) {
+        // gauss_legendre (:131-206), mode 1
+        double thmin = th00, thmax = 180., acc = 0.;
+        double din = w.ddry[kk];
+        JimmPre q = jimm_pre(T, Seq);
+        for (int i = 0; i < 10; i++) {
+          double th1 = 0.5 * (thmax - thmin) * c_gl_x[i] + 0.5 * (thmax + thmin);
+          double J = J_imm(q, th1, T, din);
+          double ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_imm, P.mean_theta_imm) : 0.;
+          acc = acc + ft * c_gl_w[i] * (1. - exp(-J * dt));
+        }
+        f_imm = 0.5 * (thmax - thmin) * acc;
+      }
+    }
+    if (P.lsicedep) {
+      double th00 = P.mean_theta_dep + sqrt(2.) * P.sigma_theta_dep * erfm1(2. * w.indef[kk] - 1.);
+      th00 = fmin(fmax(th00, 0.), 180.);
+      if (!P.st_freeTheta) th00 = fmax(P.initMinTheta, th00);
+      bool mask = (ph == 1 && prv / prs < 1.0) && (w.dwet[kk] - w.dins[kk] < dmin) && (w.dins[kk] > dmin);
+      if (mask && countable) {
+        double thmin = th00, thmax = 180., acc = 0.;
+        double din = w.ddry[kk];
+        for (int i = 0; i < 10; i++) {
+          double th1 = 0.5 * (thmax - thmin) * c_gl_x[i] + 0.5 * (thmax + thmin);
+          double J = J_dep(th1, T, din, Si);
+          double ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_dep, P.mean_theta_dep) : 0.;
+          acc = acc + ft * c_gl_w[i] * (1. - exp(-J * dt));
+        }
+        f_dep = 0.5 * (thmax - thmin) * acc;
+      }
+    }
+    dh += n * f_hom; dd += n * f_dep; di += n * f_imm;
+    double frac = fmax(0., fmin(0.99, f_imm + f_hom + f_dep - (f_imm + f_dep) * f_hom));
+    // iceNucleation (:421-538)
+    if (n < nlim_of(ph)) continue;
+    double vins = 0.;
+    for (int k = 0; k < P.ninsoluble; k++) vins += w.v(P.ind_insoluble[k], kk);
+    if (vins < minVin) continue;
+    int bb = ice_bin_of(P, vlo, dwet);
+    double vdry = 0.;
+    for (int s = 0; s < ndry; s++) vdry += w.v(s, kk);
+    double V_tot = frac * vdry;
+    double frac_DU = w.v(idu, kk) / vdry;
+    double frac2, ncur0;
+    if (frac_DU <= 0.1) { frac2 = frac * frac_DU; ncur0 = n * frac_DU; }
+    else { frac2 = frac; ncur0 = n; }
+    double nnuc = frac2 * n;
+    double f1 = nnuc + (ncur0 - nnuc) * w.indef[kk];
+    f1 = f1 / ncur0;
+    w.indef[kk] = fmin(fmax(f1, 0.), 1. - 1.e-20);
+    st[0] = (double)bb;
+    st[9] = 1.;
+    bool mk = P.st_icenucl;
+    if (frac_DU <= 0.1) {
+      if (mk) st[1 + idu] = V_tot * frac_DU;
+      w.v(idu, kk) = fmax(0., w.v(idu, kk) - V_tot * frac_DU);
+    } else {
+      for (int s = 0; s < ndry; s++) {
+        if (mk) st[1 + s] = w.v(s, kk) * frac2;
+        w.v(s, kk) = fmax(0., w.v(s, kk) * (1. - frac2));
+      }
+    }
+    if (ph == 1 || ph == 2) {
+      if (mk) st[1 + iwa] = w.v(iwa, kk) * frac2 * K_RHOWA / K_RHOIC;
+    } else {
+      if (mk) st[1 + irim] = w.v(iwa, kk) * frac2 * K_RHOWA / K_RHORI;
+    }
+    w.v(iwa, kk) = fmax(0., w.v(iwa, kk) * (1. - frac2));
+    if (mk) st[8] = n * frac2;
+    w.numc[kk] = fmax(0., n * (1. - frac2));
+    if (!mk) st[9] = 0.;
+  }
+  __syncwarp();
+  if (diag) {
+    dh = warp_sum(dh); dd = warp_sum(dd); di = warp_sum(di);
+    if (lane == 0) {
+      w.misc[M_DIAG + DG_ICEHOM] += dh;
+      w.misc[M_DIAG + DG_ICEDEP] += dd;
+      w.misc[M_DIAG + DG_ICEIMM] += di;
+    }
+  }
+  if (P.st_icenucl) ice_apply_staged(P, w, stage, nl, lane);
+}
+
+// classic ice nucleation (mo_salsa_cloud_ice.f90:26-140 with calc_Jhet/Jdep/Jhf :146-291)
+__device__ double calc_Jhet(double rn, double temp, double Sw) {
+  const double rho_ice = 900., c_1s = 1e32, T0 = 273.15, mis = 0.5;
+  if (rn < 1e-10) return 0.;
+  double Tc = temp - T0;
+  double act = K_RG * temp * (347. / (temp - 177.) - log(4.14 / 349.)) / K_AVOG;
+  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double GG = K_RG * temp / K_MWA / Lefm;
+  double sg = pow(Sw, GG);
+  if ((T0 / temp) * sg < 1.0001) return 0.;
+  double sigma_is = 28.e-3 + 0.25e-3 * Tc;
+  double r_g = 4. * sigma_is / (rho_ice * Lefm * log((T0 / temp) * sg) - 1.7e10 * 0.);
+  if (r_g <= 1e-10) return 0.;
+  double sf = het_sf(rn / r_g, mis);
+  double crit = (K_PI / 3.) * sigma_is * r_g * r_g * sf - (1. / 4.) * 0.0 * (1. - mis) * rn * rn;
+  return K_BOLTZ * temp / K_PLANCK * c_1s * K_PI * rn * rn * exp((-act - crit) / (K_BOLTZ * temp));
+}
+__device__ double calc_Jdep(double rn, double temp, double Si) {
+  const double rho_ice = 900., mis = 0.5;
+  if (rn < 1e-10 || Si < 1.0001) return 0.;
+  double Tc = temp - 273.15;
+  double sigma_iv = ((76.1 - 0.155 * Tc) + (28.5 + 0.25 * Tc)) * 1e-3;
+  double r_g = 4. * sigma_iv / (K_RG * rho_ice / K_MWA * temp * log(Si) - 1.7e10 * 0.);
+  if (r_g <= 1e-10) return 0.;
+  double sf = het_sf(rn / r_g, mis);
+  double crit = (K_PI / 3.) * sigma_iv * r_g * r_g * sf;
+  return (1. / 4.) * 1.e30 * rn * rn * exp((-0. - crit) / (K_BOLTZ * temp));
+}
+__device__ double calc_Jhf(double temp, double Sw) {
+  const double Nc = 5.85e16, rho_ice = 900., T0 = 273.15;
+  double Tc = temp - T0;
+  double act = 0.694e-19 * (1. + 0.027 * (Tc + 30.));
+  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double GG = K_RG * temp / Lefm / K_MWA;
+  double sg = pow(Sw, GG);
+  if ((T0 / temp) * sg < 1.0001) return 0.;
+  double sigma_is = 28.e-3 + 0.25e-3 * Tc;
+  double r_g = 2. * sigma_is / (rho_ice * Lefm * log((T0 / temp) * sg));
+  if (r_g <= 1e-10) return 0.;
+  double crit = 4. * K_PI / 3. * sigma_is * r_g * r_g;
+  return 2.0 * Nc * (K_RHOWA * K_BOLTZ * temp / rho_ice / K_PLANCK) * sqrt(sigma_is / K_BOLTZ / temp) *
+         exp((-crit - act) / (K_BOLTZ * temp));
+}
+
+template <typename KT>
+__device__ void ice_nucl_classic(const DevParams &P, const WS<KT> &w, const double *tb, double T, double prv,
+                                 double prs, double prsi, double dt, double kappa, bool diag, int lane) {
+  const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad;
+  const double tmax_homog = 237.9, dmin = 1.e-10;
+  const int nl = P.nliquid, ndry = P.ndry, iwa = P.iwa, irim = P.irim;
+  double *stage = w.scr;
+  double dh = 0., dd = 0., di = 0.;
+  for (int kk = lane; kk < nl; kk += 32) {
+    double *st = stage + kk * 10;
+    for (int q = 0; q < 10; q++) st[q] = 0.;
+    st[0] = -1.;
+    int ph = phase_of(P, kk);
+    if (T > 273.15 || w.numc[kk] < nlim_of(ph)) continue;
+    updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, kk);
+    double dins_ = w.dins[kk], dwet = w.dwet[kk];
+    double Sw = calc_sweq(P, w, kk, T, kappa);
+    double pf_imm = 0., pf_dep = 0., pf_hom = 0.;
+    if (dins_ > dmin && P.lsiceimm && (ph == 2 || ph == 3)) pf_imm = 1. - exp(-calc_Jhet(dins_, T, Sw) * dt);
+    if (dins_ > dmin && dwet - dins_ < dmin && prv / prs < 1.0 && ph == 1 && P.lsicedep)
+      pf_dep = 1. - exp(-calc_Jdep(dins_, T, prv / prsi) * dt);
+    if (dwet - dins_ > dmin && T < tmax_homog && P.lsicehom)
+      pf_hom = 1. - exp(-calc_Jhf(T, Sw) * K_PI6 * (cube(dwet) - cube(dins_)) * dt);
+    double frac = fmax(0., fmin(0.99, pf_imm + pf_hom + pf_dep - (pf_imm + pf_dep) * pf_hom));
+    int bb = ice_bin_of(P, vlo, dwet);
+    bool mk = P.st_icenucl;
+    st[0] = (double)bb;
+    st[9] = mk ? 1. : 0.;
+    for (int s = 0; s < ndry; s++) {
+      if (mk) st[1 + s] = w.v(s, kk) * frac;
+      w.v(s, kk) = fmax(0., w.v(s, kk) * (1. - frac));
+    }
+    if (ph == 1 || ph == 2) { if (mk) st[1 + iwa] = w.v(iwa, kk) * frac * K_RHOWA / K_RHOIC; }
+    else { if (mk) st[1 + irim] = w.v(iwa, kk) * frac * K_RHOWA / K_RHORI; }
+    w.v(iwa, kk) = fmax(0., w.v(iwa, kk) * (1. - frac));
+    if (mk) st[8] = w.numc[kk] * frac;
+    double nn = fmax(0., w.numc[kk] * (1. - frac));
+    w.numc[kk] = nn;
+    // iceDiagnostics is called after iceNucleation (:130-132): the reduced number
+    dh += nn * pf_hom; dd += nn * pf_dep; di += nn * pf_imm;
+  }
+  __syncwarp();
+  if (diag) {
+    dh = warp_sum(dh); dd = warp_sum(dd); di = warp_sum(di);
+    if (lane == 0) {
+      w.misc[M_DIAG + DG_ICEHOM] += dh;
+      w.misc[M_DIAG + DG_ICEDEP] += dd;
+      w.misc[M_DIAG + DG_ICEIMM] += di;
+    }
+  }
+  ice_apply_staged(P, w, stage, nl, lane);
+  for (int b = P.nliquid + lane; b < P.ntotal; b += 32)
+    w.rhomean[b] = rhomean_of(P, 4, w.numc[b], w.v(iwa, b), w.v(irim, b));
+  __syncwarp();
+}
+
+// ice_melt (mo_salsa_cloud_ice.f90:393-462): ice bins staged per lane, precip bins add in ice order
+template <typename KT>
+__device__ void ice_melt(const DevParams &P, const WS<KT> &w, const double *tb, double T, int lane) {
+  if (T < 273.15) return;
+  const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad;
+  const double maxfrac = 0.999;
+  const int ndry = P.ndry, iwa = P.iwa, irim = P.irim, I0 = P.nliquid, P0 = P.nbins + P.ncld;
+  double *stage = w.scr;   // nice * 10
+  for (int k = lane; k < P.nice; k += 32) {
+    int g = I0 + k;
+    double *st = stage + k * 10;
+    for (int q = 0; q < 10; q++) st[q] = 0.;
+    st[0] = -1.;
+    if (w.numc[g] < K_PRLIM) continue;
+    // updateDiameter(limit, "wet") and updateRhomean
+    double n = w.numc[g];
+    double dw;
+    if (n > K_PRLIM) {
+      double vs = 0.;
+      for (int s = 0; s < P.nused; s++) vs += w.v(s, g);
+      dw = cbrt(vs / n / K_PI6);
+    } else {
+      dw = dmid[g];
+    }
+    dw = fmin(dw, 10.e-3);
+    w.dwet[g] = dw;
+    double rm = rhomean_of(P, 4, n, w.v(iwa, g), w.v(irim, g));
+    w.rhomean[g] = rm;
+    int bb = precip_bin_of(P, vlo, dw, rm);
+    st[0] = (double)bb;
+    for (int s = 0; s < ndry; s++) {
+      st[1 + s] = maxfrac * w.v(s, g);
+      w.v(s, g) = (1. - maxfrac) * w.v(s, g);
+    }
+    double liqvol = (w.v(iwa, g) * K_RHOIC + w.v(irim, g) * K_RHORI) / K_RHOWA;
+    st[8] = maxfrac * n;
+    w.numc[g] = (1. - maxfrac) * n;
+    st[1 + iwa] = maxfrac * liqvol;
+    w.v(iwa, g) = (1. - maxfrac) * w.v(iwa, g);
+    w.v(irim, g) = (1. - maxfrac) * w.v(irim, g);
+  }
+  __syncwarp();
+  // precip bin gets dry species, number, water in ice-bin order
+  for (int e = lane; e < P.nprc * (P.nwet + 1); e += 32) {
+    int pb = e / (P.nwet + 1), q = e % (P.nwet + 1), g = P0 + pb;
+    double val = (q < P.nwet) ? w.v(q, g) : w.numc[g];
+    for (int k = 0; k < P.nice; k++) {
+      const double *st = stage + k * 10;
+      if ((int)st[0] != pb) continue;
+      val = val + ((q < P.nwet) ? st[1 + q] : st[8]);
+    }
+    if (q < P.nwet) w.v(q, g) = val; else w.numc[g] = val;
+  }
+  __syncwarp();
+}
+
+// ----------------------------------------------------------------------------------------
+// distr_update: mo_salsa_update.f90:21-433.  Each sweep moves content between
+// neighbouring bins in descending bin order and depends on the previous moves, so it
+// runs on lane 0.  The bin-limit flag is overwritten by every checked bin (:132, 224,
+// 322, 418): the last checked bin decides whether another sweep follows.
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+__device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *tb, int lane) {
+  if (lane == 0) {
+    const double *vlo = tb + TAB_VLO * P.nb_pad, *vhi = tb + TAB_VHI * P.nb_pad, *dmid = tb + TAB_DMID * P.nb_pad;
+    const int zndry = P.ndry, znwet = P.nwet, znnsp = P.nused;
+    int f_distr = 0, f_neg = 0;
+    // aerosols
+    {
+      bool within = false;
+      int count = 0;
+      while (!within) {
+        within = true;
+        for (int kk = P.fn2b - 1; kk >= P.in1a; kk--) {
+          if (w.numc[kk] > K_NLIM) {
+            if (kk == P.fn2a) continue;
+            double sd = 0.;
+            for (int s = 0; s < zndry; s++) sd += w.v(s, kk);
+            double zvpart = sd / w.numc[kk];
+            if (vlo[kk] > zvpart && kk == P.in1a) continue;
+            if (vlo[kk] > zvpart) {
+              int mm = (kk == P.in2b) ? P.fn1a : kk - 1;
+              w.numc[mm] = w.numc[mm] + w.numc[kk];
+              w.numc[kk] = 0.;
+              for (int s = 0; s < znwet; s++) { w.v(s, mm) = w.v(s, mm) + w.v(s, kk); w.v(s, kk) = 0.; }
+              continue;
+            }
+            if (zvpart <= K_PI6 * cube(dmid[kk])) continue;
+            double zVrat = vhi[kk] / vlo[kk];
+            double zVilo = 2. * zvpart / (1. + zVrat);
+            double zVihi = zVrat * zVilo;
+            double zVexc = 0.5 * (zVihi + vhi[kk]);
+            double znfrac = fmin(1., (zVihi - vhi[kk]) / (zVihi - zVilo));
+            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
+            if (zvfrac < 0.) f_neg = 1;
+            int mm = kk + 1;
+            double f = znfrac * w.numc[kk] * zVexc;
+            for (int s = 0; s < znwet; s++) {
+              double vk = w.v(s, kk);
+              double mv = f * vk / sd;
+              w.v(s, mm) = w.v(s, mm) + mv;
+              w.v(s, kk) = vk - mv;
+            }
+            w.numc[mm] = w.numc[mm] + znfrac * w.numc[kk];
+            w.numc[kk] = w.numc[kk] * (1. - znfrac);
+          }
+          if (w.numc[kk] > K_NLIM) {
+            double sd = 0.;
+            for (int s = 0; s < zndry; s++) sd += w.v(s, kk);
+            double zvpart = sd / w.numc[kk];
+            within = (vlo[kk] < zvpart && zvpart < vhi[kk]);
+          }
+        }
+        if (++count > 100) { f_distr = 1; break; }
+      }
+    }
+    // cloud droplets
+    {
+      const int C0 = P.nbins;
+      bool within = false;
+      int count = 0;
+      while (!within) {
+        within = true;
+        for (int kk = P.ncld - 1; kk >= P.ica_cur; kk--) {
+          int g = C0 + kk;
+          double sd = 0.;
+          for (int s = 0; s < zndry; s++) sd += w.v(s, g);
+          if (w.numc[g] > K_NLIM && sd > 1.e-30) {
+            double zvpart = sd / w.numc[g];
+            double zVrat = vhi[g] / vlo[g];
+            double zVilo = 2. * zvpart / (1. + zVrat);
+            double zVihi = zVrat * zVilo;
+            double zVexc, znfrac;
+            int mm;
+            if (zvpart < vlo[g] && (kk != P.ica_cur && kk != P.icb_cur)) {
+              zVexc = 0.5 * (zVilo + vlo[g]);
+              znfrac = fmin(1., (vlo[g] - zVilo) / (zVihi - zVilo));
+              mm = kk - 1;
+            } else if (zvpart > vhi[g] && (kk != P.fca_cur && kk != P.fcb_cur)) {
+              zVexc = 0.5 * (zVihi + vhi[g]);
+              znfrac = fmin(1., (zVihi - vhi[g]) / (zVihi - zVilo));
+              mm = kk + 1;
+            } else {
+              continue;
+            }
+            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
+            if (zvfrac < 0.) f_neg = 1;
+            int gm = C0 + mm;
+            for (int s = 0; s < znwet; s++) {
+              double vk = w.v(s, g);
+              w.v(s, gm) = w.v(s, gm) + zvfrac * vk;
+              w.v(s, g) = vk - zvfrac * vk;
+            }
+            double nk = w.numc[g];
+            w.numc[gm] = w.numc[gm] + znfrac * nk;
+            w.numc[g] = nk - znfrac * nk;
+          }
+          sd = 0.;
+          for (int s = 0; s < zndry; s++) sd += w.v(s, g);
+          if (w.numc[g] > K_NLIM && sd > 1.e-30) {
+            double zvpart = sd / w.numc[g];
+            within = (vlo[g] < zvpart && zvpart < vhi[g]);
+          }
+        }
+        if (++count > 100) { f_distr = 1; break; }
+      }
+    }
+    // precipitation (wet volume)
+    {
+      const int P0 = P.nbins + P.ncld;
+      bool within = false;
+      int count = 0;
+      while (!within) {
+        within = true;
+        for (int kk = P.nprc - 1; kk >= 0; kk--) {
+          int g = P0 + kk;
+          if (w.numc[g] > K_PRLIM) {
+            double sw = 0.;
+            for (int s = 0; s < znwet; s++) sw += w.v(s, g);
+            double zvpart = sw / w.numc[g];
+            double zVrat = vhi[g] / vlo[g];
+            double zVilo = 2. * zvpart / (1. + zVrat);
+            double zVihi = zVrat * zVilo;
+            double vm = K_PI6 * cube(dmid[g]);
+            double zvdec = vm - 0.2 * (vm - vlo[g]);
+            double zVexc, znfrac;
+            int mm;
+            if (zvpart < zvdec && kk != 0) {
+              zVexc = 0.5 * (zVilo + vlo[g]);
+              znfrac = fmin(1., (vlo[g] - zVilo) / (zVihi - zVilo));
+              mm = kk - 1;
+            } else if (zvpart > vm && kk != P.nprc - 1) {
+              zVexc = 0.5 * (zVihi + vhi[g]);
+              znfrac = fmin(.99, (zVihi - vhi[g]) / (zVihi - zVilo));
+              mm = kk + 1;
+            } else {
+              continue;
+            }
+            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
+            if (zvfrac < 0.) f_neg = 1;
+            int gm = P0 + mm;
+            for (int s = 0; s < znwet; s++) {
+              double vk = w.v(s, g);
+              w.v(s, gm) = w.v(s, gm) + zvfrac * vk;
+              w.v(s, g) = vk - zvfrac * vk;
+            }
+            double nk = w.numc[g];
+            w.numc[gm] = w.numc[gm] + znfrac * nk;
+            w.numc[g] = nk - znfrac * nk;
+          }
+          if (w.numc[g] > K_PRLIM) {
+            double sw = 0.;
+            for (int s = 0; s < znwet; s++) sw += w.v(s, g);
+            double zvpart = sw / w.numc[g];
+            within = (vlo[g] < zvpart && zvpart < vhi[g]);
+          }
+        }
+        if (++count > 100) { f_distr = 1; break; }
+      }
+    }
+    if (P.level >= 5) {
+      const int I0 = P.nliquid;
+      bool within = false;
+      int count = 0;
+      while (!within) {
+        within = true;
+        for (int kk = P.nice - 1; kk >= 0; kk--) {
+          int g = I0 + kk;
+          if (w.numc[g] > K_PRLIM) {
+            double st = 0.;
+            for (int s = 0; s < znnsp; s++) st += w.v(s, g);
+            double zvpart = st / w.numc[g];
+            double zVrat = vhi[g] / vlo[g];
+            double zVilo = 2. * zvpart / (1. + zVrat);
+            double zVihi = zVrat * zVilo;
+            double vm = K_PI6 * cube(dmid[g]);
+            double zvdec = vm - 0.2 * (vm - vlo[g]);
+            double zVexc, znfrac;
+            int mm;
+            if (zvpart < zvdec && kk != 0) {
+              zVexc = 0.5 * (zVilo + vlo[g]);
+              znfrac = fmin(1.0, (vlo[g] - zVilo) / (zVihi - zVilo));
+              mm = kk - 1;
+            } else if (zvpart > vm && kk != P.nice - 1) {
+              zVexc = 0.5 * (zVihi + vhi[g]);
+              znfrac = fmin(0.99, (zVihi - vhi[g]) / (zVihi - zVilo));
+              mm = kk + 1;
+            } else {
+              continue;
+            }
+            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
+            if (zvfrac < 0.) f_neg = 1;
+            int gm = I0 + mm;
+            for (int s = 0; s < znnsp; s++) {
+              double vk = w.v(s, g);
+              w.v(s, gm) = w.v(s, gm) + zvfrac * vk;
+              w.v(s, g) = vk - zvfrac * vk;
+            }
+            double nk = w.numc[g];
+            w.numc[gm] = w.numc[gm] + znfrac * nk;
+            w.numc[g] = nk - znfrac * nk;
+          }
+          double st = 0.;
+          for (int s = 0; s < znnsp; s++) st += w.v(s, g);
+          if (w.numc[g] > K_PRLIM && st > 1.e-30) {
+            double zvpart = st / w.numc[g];
+            within = (vlo[g] < zvpart && zvpart < vhi[g]);
+          }
+        }
+        if (++count > 100) { f_distr = 1; break; }
+      }
+    }
+    if (f_distr) w.misc[M_FLAGS + F_DISTR] = 1.;
+    if (f_neg) w.misc[M_FLAGS + F_NEGFRAC] = 1.;
+  }
+  __syncwarp();
+}
+
+
+// ----------------------------------------------------------------------------------------
+// One cell: the body of the run_SALSA cell loop (mo_salsa_driver.f90:185-419) around
+// salsa() (mo_salsa.f90:89-149).  Every cell starts from the post-initialisation module
+// state (bin templates), i.e. each cell sees allSALSA as the reference's first cell does.
+// ----------------------------------------------------------------------------------------
+template <typename KT, bool DIAG>
+__device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, int lane) {
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  double *raw = w.raw;
+  const double T = raw[RW_T], pres = raw[RW_P], rs = raw[RW_RS], rsi = raw[RW_RSI], dn = raw[RW_DN];
+  const double kappa = raw[RW_KAPPA];
+  const double dt = P.dt;
+  double rv = P.st_freeRH ? raw[RW_RV] : fmin(raw[RW_RV], rs * P.rhlim);
+  const double rv_old = rv;
+  const int nwet = P.nwet, irim = P.irim;
+  const int bstart[4] = {0, P.nbins, P.nbins + P.ncld, P.nliquid};
+  const int bnum[4] = {P.nbins, P.ncld, P.nprc, P.nice};
+  for (int b = lane; b < P.ntotal; b += 32) {
+    int icat = phase_of(P, b) - 1;
+    w.dwet[b] = dmid[b];
+    w.ddry[b] = w.dins[b] = w.dnsp[b] = 0.;
+    if (icat == 3 && P.level < 5) {
+      w.numc[b] = 0.;
+      for (int s = 0; s < SALSA_NSV; s++) w.v(s, b) = 0.;
+      w.rhomean[b] = 0.;
+      w.indef[b] = 0.;
+      w.ctime[b] = 0.;
+      continue;
+    }
+    int nbloc = b - bstart[icat], nbc = bnum[icat];
+    const double *rm = raw + P.raw_mbase[icat];
+    for (int s = 0; s < SALSA_NSV; s++) w.v(s, b) = 0.;
+    if (icat < 3) {
+      for (int s = 0; s < nwet; s++) w.v(s, b) = rm[s * nbc + nbloc] * dn / P.rholiq[s];
+    } else {
+      for (int s = 0; s < nwet; s++) w.v(s, b) = rm[s * nbc + nbloc] * dn / P.rhoice[s];
+      w.v(irim, b) = rm[irim * nbc + nbloc] * dn / K_RHORI;
+    }
+    w.numc[b] = raw[P.raw_num + b] * dn;
+    w.indef[b] = (icat < 3 && P.raw_indef >= 0) ? raw[P.raw_indef + b] : 0.;
+    w.ctime[b] = (icat < 3 && P.raw_charge >= 0) ? raw[P.raw_charge + b] : 0.;
+    w.rhomean[b] = rhomean_of(P, icat + 1, w.numc[b], w.v(P.iwa, b), w.v(irim, b));
+  }
+  for (int i = lane; i < M_PF; i += 32) w.misc[i] = 0.;
+  __syncwarp();
+  if (P.initialize) equilibration<KT>(P, w, tb, 0.3, T, true, lane);
+
+  // ---- salsa() ----
+  if (P.st_coag) coagulation<KT>(P, w, tb, dt, T, pres, DIAG, lane);
+  if (P.st_cnd && (P.lscndh2ocl || P.lscndh2oae || P.lscndh2oic))
+    gpparth2o<KT>(P, w, tb, T, pres, rs, rsi, rv, dt, kappa, DIAG, lane);
+  if (P.st_auto && P.auto_mode == 2) autoconv2<KT>(P, w, dt, lane);
+  if (P.st_activ && P.activ_mode == 1) act_interst<KT>(P, w, tb, rv, rs, T, DIAG, lane);
+  if ((P.st_icenucl || P.icenucl_mode == 2) && (P.lsicehom || P.lsiceimm || P.lsicedep)) {
+    if (P.ice_theta_dist) ice_nucl_SE<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
+    else ice_nucl_classic<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
+  }
+  if (P.st_icemelt) ice_melt<KT>(P, w, tb, T, lane);
+  if (P.lsdistupdate) distr_update<KT>(P, w, tb, lane);
+
+  // ---- tendencies and outputs (mo_salsa_driver.f90:310-419) into the raw slots ----
+  bool bad = false;
+  for (int b = lane; b < P.ntotal; b += 32) {
+    int icat = phase_of(P, b) - 1;
+    if (icat == 3 && P.level < 5) continue;
+    int nbloc = b - bstart[icat], nbc = bnum[icat];
+    double *rm = raw + P.raw_mbase[icat];
+    if (icat < 3) {
+      for (int s = 0; s < nwet; s++) {
+        double *o = rm + s * nbc + nbloc;
+        *o = ((w.v(s, b) * P.rholiq[s] / dn) - *o) / dt;
+      }
+      if (P.raw_indef >= 0) raw[P.raw_indef + b] = w.indef[b];
+      if (P.raw_charge >= 0) raw[P.raw_charge + b] = w.ctime[b];
+    } else {
+      for (int s = 0; s < nwet; s++) {
+        double *o = rm + s * nbc + nbloc;
+        *o = ((w.v(s, b) * P.rhoice[s] / dn) - *o) / dt;
+      }
+      double *o = rm + irim * nbc + nbloc;
+      *o = ((w.v(irim, b) * K_RHORI / dn) - *o) / dt;
+    }
+    double *on = raw + P.raw_num + b;
+    *on = ((w.numc[b] / dn) - *on) / dt;
+    bad |= !isfinite(w.numc[b]);
+  }
+  // interstitial activation leaves the activated-droplet outputs at zero (:879, local pactd)
+  for (int i = lane; i < P.ncld * (1 + nwet); i += 32) raw[P.raw_nact + i] = 0.;
+  if (lane == 0) raw[RW_RV] = (rv - rv_old) / dt;
+  if (DIAG && P.raw_diag >= 0 && lane == 0) {
+    const double *d = w.misc + M_DIAG;
+    double *o = raw + P.raw_diag;
+    o[DG_AUTOC] = d[DG_AUTOC] * K_RHOWA / dn;
+    o[DG_AUTOC80] = d[DG_AUTOC80] * K_RHOWA / dn;
+    o[DG_AUTOC50] = d[DG_AUTOC50] * K_RHOWA / dn;
+    o[DG_ACCR] = d[DG_ACCR] * K_RHOWA / dn;
+    o[DG_ACCR80] = d[DG_ACCR80] * K_RHOWA / dn;
+    o[DG_ACCR50] = d[DG_ACCR50] * K_RHOWA / dn;
+    o[DG_ACCOLL] = d[DG_ACCOLL] / dn;
+    o[DG_APCOLL] = d[DG_APCOLL] / dn;
+    o[DG_ACTIV] = d[DG_ACTIV] / dn;
+    o[DG_CONDA] = d[DG_CONDA] / dn;
+    o[DG_CONDC] = d[DG_CONDC] / dn;
+    o[DG_CONDP] = d[DG_CONDP] / dn;
+    if (P.level == 5) {
+      o[DG_AICOLL] = 0.;   // AIcoll%volc is never accumulated on this path (coag_ice uses the phase-change source)
+      o[DG_ICEHOM] = d[DG_ICEHOM] / dn;
+      o[DG_ICEDEP] = d[DG_ICEDEP] / dn;
+      o[DG_ICEIMM] = d[DG_ICEIMM] / dn;
+      o[DG_CONDI] = d[DG_CONDI] / dn;
+    }
+  }
+  bad = warp_any(bad);
+  if (lane == 0 && P.status) {
+    const double *f = w.misc + M_FLAGS;
+    if (f[F_EQUIL] != 0.) atomicAdd(P.status + ST_EQUIL, 1ull);
+    if (f[F_DISTR] != 0.) atomicAdd(P.status + ST_DISTR, 1ull);
+    if (f[F_NEGFRAC] != 0.) atomicAdd(P.status + ST_NEGFRAC, 1ull);
+    if (f[F_COND] != 0.) atomicAdd(P.status + ST_COND, 1ull);
+    if (f[F_NEG] != 0.) atomicAdd(P.status + ST_NEG, 1ull);
+    if (bad) atomicAdd(P.status + ST_NONFINITE, 1ull);
+  }
+  __syncwarp();
+}
+
+template <typename KT>
+__device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
+  WS<KT> w;
+  const int NB = P.nb_pad;
+  w.NB = NB;
+  double *p = base;
+  w.raw = p; p += (P.nraw + 1) & ~1;
+  w.numc = p; p += NB;
+  w.volc = p; p += SALSA_NSV * NB;
+  w.dwet = p; p += NB;
+  w.ddry = p; p += NB;
+  w.dins = p; p += NB;
+  w.dnsp = p; p += NB;
+  w.rhomean = p; p += NB;
+  w.indef = p; p += NB;
+  w.ctime = p; p += NB;
+  w.scr = p; p += SALSA_NSCR * NB;
+  w.misc = p; p += SALSA_MISC_DOUBLES;
+  w.pbuf = reinterpret_cast<int *>(p); p += 32;
+  w.K = reinterpret_cast<KT *>(p);
+  return w;
+}
+
+__device__ __forceinline__ long long cell_offset(const DevParams &P, long long q) {
+  long long kq = q % P.nz_int, r = q / P.nz_int;
+  long long iq = r % P.nx_int, jq = r / P.nx_int;
+  return (1 + kq) + (long long)P.nzp * ((2 + iq) + (long long)P.nxp * (2 + jq));
+}
+
+template <typename KT, bool DIAG>
+__global__ void __launch_bounds__(SALSA_THREADS) salsa_step_kernel(const DevParams P) {
+  extern __shared__ double smem[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  double *tb = smem;
+  for (int i = tid; i < P.tab_doubles; i += SALSA_THREADS) tb[i] = P.tables[i];
+  double *wsbase = smem + P.tab_doubles;
+  WS<KT> w = make_ws<KT>(P, wsbase + (size_t)warp * P.ws_doubles);
+  __syncthreads();
+  for (long long g = blockIdx.x; g < P.ngroups; g += gridDim.x) {
+    // stage the group's input rows: consecutive threads read consecutive cells of one row
+    for (int e = tid; e < P.nrows * SALSA_CPG; e += SALSA_THREADS) {
+      int r = e / SALSA_CPG, c = e % SALSA_CPG;
+      long long q = g * SALSA_CPG + c;
+      if (q >= P.ncells) continue;
+      Row row = P.rows[r];
+      double v = 0.;
+      if (row.fin >= 0) {
+        const double *f = P.fin[row.fin];
+        if (f) v = __ldg(f + cell_offset(P, q) + P.plane * row.idx);
+      }
+      wsbase[(size_t)c * P.ws_doubles + r] = v;
+    }
+    __syncthreads();
+    long long q = g * SALSA_CPG + warp;
+    if (q < P.ncells) cell_step<KT, DIAG>(P, w, tb, lane);
+    __syncthreads();
+    // write the group's output rows
+    for (int e = tid; e < P.nrows * SALSA_CPG; e += SALSA_THREADS) {
+      int r = e / SALSA_CPG, c = e % SALSA_CPG;
+      long long qq = g * SALSA_CPG + c;
+      if (qq >= P.ncells) continue;
+      Row row = P.rows[r];
+      if (row.fout < 0) continue;
+      double *f = P.fout[row.fout];
+      if (!f) continue;
+      double v = wsbase[(size_t)c * P.ws_doubles + r];
+      double *a = f + cell_offset(P, qq) + P.plane * row.idx;
+      if (row.mode == ROW_TEND) *a = *a + v;
+      else *a = v;
+    }
+    if (tid == 0 && P.status) atomicAdd(P.status + ST_CELLS, (unsigned long long)min((long long)SALSA_CPG, P.ncells - g * SALSA_CPG));
+    __syncthreads();
+  }
+}
+
+// Host-side launch helpers, instantiated per form in salsa_k_*.cu.
+inline size_t smem_bytes(const DevParams &P) {
+  return sizeof(double) * ((size_t)P.tab_doubles + (size_t)SALSA_CPG * P.ws_doubles);
+}
+
+template <typename KT, bool DIAG>
+cudaError_t launch_t(const DevParams &P, cudaStream_t st, int grid) {
+  size_t sm = smem_bytes(P);
+  cudaError_t e = cudaFuncSetAttribute(salsa_step_kernel<KT, DIAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  salsa_step_kernel<KT, DIAG><<<grid, SALSA_THREADS, sm, st>>>(P);
+  return cudaGetLastError();
+}
+
+template <typename KT, bool DIAG>
+int blocks_per_sm_t(const DevParams &P) {
+  size_t sm = smem_bytes(P);
+  if (cudaFuncSetAttribute(salsa_step_kernel<KT, DIAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+      cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, salsa_step_kernel<KT, DIAG>, SALSA_THREADS, sm) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+}  // namespace
+}  // namespace salsa
