@@ -1,0 +1,297 @@
+"""Benchmark of the GB300 SALSA step (one JSON line on rank 0).
+
+A step is one SALSA call over every interior cell of the workload
+(run_SALSA, src/src_salsa/mo_salsa_driver.f90:112-435).  Default workload: the
+256x256x128 grid (8,388,608 cells) with 30 % cloudy cells, level 5, dt = 1 s.
+
+  value  -- FP64 (parity) form, cell-steps/s, inputs resident in HBM, CUDA events on
+            the launch stream around exactly K steps (after W warm-up steps).
+  mixed  -- the FP32-mixed form on the same inputs.
+  e2e    -- FP64 form through the C-ABI with pinned HOST buffers: the host->device
+            copy of every input and tendency array and the device->host copy of the
+            results are inside the timed region.
+  roofline -- algorithmic bytes per cell-step (8 * (3S + T + G + I + A + D)) over the
+            measured HBM copy bandwidth; the step is FP64-pipe bound, so the fraction is
+            small and the ncu FP64 pipe figures are in profiles/.
+  cpu_baseline -- the FP64 CPU oracle (a C restatement of the reference path; the
+            Fortran cannot be built here) on a bounded sample, all host threads.
+
+--impl reference times that CPU implementation alone on bounded samples of the same
+workload.  With torchrun, every rank runs the workload on its own GPU (independent
+cells, no collective on the data path); value is the sum over ranks of the cells
+over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+# algorithmic doubles per cell-step: prog read + tendency RMW (3S), thermo + rv RMW (T),
+# gases (G), IN deficit R+W (I), activation outputs (A), diagnostics (D)
+ALG_DOUBLES = {4: 3 * 266 + 8 + 5 + 0 + 98 + 12, 5: 3 * 322 + 9 + 5 + 76 + 98 + 17}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def field_bytes(d):
+    return sum(v.numel() * v.element_size() for v in d.values())
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as tdist
+    from uclales_salsa_gb300.inputs import make_inputs, make_outputs
+    from uclales_salsa_gb300.api import SalsaStep
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        tdist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    inp = make_inputs(args.workload, dev, precision=0, diagnostics=1)
+    ncell = inp.ncells
+    level = inp.level
+    results = {}
+    stream = torch.cuda.Stream(device=dev)
+    for form in (0, 1):
+        inp.cfg.precision = form
+        step = SalsaStep(inp.cfg)
+        fields = {k: v.clone() for k, v in inp.fields.items()}
+        outs = make_outputs(inp)
+        for _ in range(args.warmup):
+            step.run(inp, fields, outs, time=1.0, stream=stream)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kms = []
+        sampler = ClockSampler(local) if form == 0 else None
+        if sampler:
+            sampler.__enter__()
+        barrier()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.steps):
+                step.run(inp, fields, outs, time=1.0, stream=stream)
+                kms.append(step.last_kernel_ms())
+            e1.record(stream)
+        barrier()
+        if sampler:
+            sampler.__exit__()
+            results["clocks"] = sampler.summary()
+        ms = e0.elapsed_time(e1)
+        t = torch.tensor([ms], device=dev)
+        if world > 1:
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        results[form] = dict(ms_total=float(t.item()), kernel_ms=sum(kms) / len(kms), launches=args.steps)
+        step.close()
+        del fields, outs
+        torch.cuda.empty_cache()
+
+    # end to end through the C-ABI with pinned host buffers (FP64 form)
+    inp.cfg.precision = 0
+    def pinned(v):
+        return torch.empty(v.shape, dtype=v.dtype, pin_memory=True).copy_(v)
+
+    host_in = {k: pinned(v) for k, v in inp.fields.items()}
+    host_out = {k: pinned(v) for k, v in make_outputs(inp, device="cpu").items()}
+    del inp.fields
+    torch.cuda.empty_cache()
+    step = SalsaStep(inp.cfg)
+    step.run(inp, host_in, host_out, time=1.0)        # allocates the staging buffers once
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step.run(inp, host_in, host_out, time=1.0)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device=dev)
+    if world > 1:
+        tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    inputs_b = sum(v.numel() * 8 for k, v in host_in.items() if k in (
+        "press", "temp", "rsl", "rsi", "rp", "dn", "wp", "naero", "ncloud", "nprecp", "nice", "maero", "mcloud",
+        "mprecp", "mice", "indef"))
+    tend_b = sum(v.numel() * 8 for k, v in host_out.items() if k.endswith("t"))
+    out_b = field_bytes(host_out)
+    h2d = inputs_b + tend_b
+    d2h = out_b + host_in["indef"].numel() * 8
+    step.close()
+
+    r0 = results[0]
+    value = world * ncell * args.steps / (r0["ms_total"] / 1e3)
+    mixed = world * ncell * args.steps / (results[1]["ms_total"] / 1e3)
+    e2e = world * ncell * args.steps / e2e_s
+    bytes_cell = 8 * ALG_DOUBLES[level]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = bytes_cell * ncell / (r0["kernel_ms"] / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp))[args.workload] * ncell
+        except Exception:
+            traffic = None
+    line = {
+        "metric": "cell-steps/s (FP64 SALSA step; FP32-mixed form in 'mixed')",
+        "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r0["ms_total"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, run_SALSA layout)",
+        "config": {"workload": args.workload, "cells": ncell, "level": level, "dt_s": inp.dt,
+                   "l2": "inputs larger than L2 (%.1f GB per step)" % ((h2d + d2h) / 1e9)},
+        "mixed": {"value": mixed, "unit": "cell-steps/s", "ms_per_step": results[1]["ms_total"] / args.steps,
+                  "speedup_vs_fp64": mixed / value, "dtype": "f32 kernels + f64 state"},
+        "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_cell": bytes_cell},
+        "gpu_launches": args.steps,
+        "clocks": results.get("clocks"),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample_cells)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        tdist.destroy_process_group()
+
+
+def oracle_sample(workload, cells):
+    """A cubic-ish sub-block of the workload with the same distributions."""
+    from uclales_salsa_gb300.inputs import WORKLOADS, make_inputs
+    spec = WORKLOADS[workload]
+    Z = min(spec["Z"], 32)
+    side = max(1, int(round((cells / Z) ** 0.5)))
+    return make_inputs(workload, "cpu", X=side, Y=side, Z=Z)
+
+
+def cpu_baseline(workload, cells):
+    import torch
+    from uclales_salsa_gb300.inputs import make_outputs
+    from oracle_ref import Oracle
+    inp = oracle_sample(workload, cells)
+    o = Oracle(inp.cfg)
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    out = make_outputs(inp)
+    t0 = time.perf_counter()
+    o.run(inp, f, out, time=1.0)
+    dt = time.perf_counter() - t0
+    ncores = os.cpu_count()
+    return {"value": inp.ncells / dt, "unit": "cell-steps/s", "cores": ncores, "kind": "port",
+            "sample": f"{inp.ncells} cells ({inp.nxp - 4}x{inp.nyp - 4}x{inp.nzp - 2}) of {workload}, FP64 oracle, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from uclales_salsa_gb300.inputs import make_outputs
+    from oracle_ref import Oracle
+    inp = oracle_sample(args.workload, args.cpu_sample_cells)
+    o = Oracle(inp.cfg)
+    times = []
+    for i in range(args.warmup + args.steps):
+        f = {k: v.clone() for k, v in inp.fields.items()}
+        out = make_outputs(inp)
+        t0 = time.perf_counter()
+        o.run(inp, f, out, time=1.0)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    value = inp.ncells * len(times) / sum(times)
+    sample = (f"{inp.ncells} cells ({inp.nxp - 4}x{inp.nyp - 4}x{inp.nzp - 2}) of {args.workload} per step; "
+              "FP64 C restatement of the reference path (the Fortran reference cannot be built: no Fortran compiler)")
+    line = {"impl": "reference", "metric": "cell-steps/s (FP64 SALSA step; FP32-mixed form in 'mixed')",
+            "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * inp.ncells / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, run_SALSA layout)",
+            "config": {"workload": args.workload, "cells_per_step": inp.ncells},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="grid256x256x128")
+    ap.add_argument("--cpu-sample-cells", type=int, default=524288)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

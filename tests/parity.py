@@ -14,10 +14,13 @@ def interior(t, nzp, nxp, nyp):
     return t[..., 2:nyp - 2, 2:nxp - 2, 1:nzp - 1]
 
 
-def state_errors(inp, fields, out_a, out_b):
+def state_errors(inp, fields, out_a, out_b, tol=1e-6):
     """Max relative error of the NEW state (old + tendency * dt) per output field.
 
-    Relative to max(|new_ref|, floor).  Returns {field: (max_rel, n_over_1e-6, n)}."""
+    The error of a bin value is measured relative to the scale of its update,
+    max(|new_ref|, |old|, floor): when a process empties a bin completely the
+    result is the difference of two equal magnitudes and its rounding is relative
+    to the old value.  Returns {field: (max_rel, n_over_tol, n)}."""
     res = {}
     dt = inp.dt
     for name, st in STATE_OF.items():
@@ -29,8 +32,10 @@ def state_errors(inp, fields, out_a, out_b):
         a = interior(a, inp.nzp, inp.nxp, inp.nyp)
         b = interior(b, inp.nzp, inp.nxp, inp.nyp)
         fl = FLOOR["rp"] if name == "rpt" else (FLOOR["n"] if name in NUMBER_FIELDS else FLOOR["m"])
-        rel = (a - b).abs() / torch.clamp(b.abs(), min=fl)
-        res[name] = (float(rel.max()), int((rel > 1e-6).sum()), rel.numel())
+        o = interior(old, inp.nzp, inp.nxp, inp.nyp)
+        scale = torch.maximum(b.abs(), o.abs()).clamp(min=fl)
+        rel = (a - b).abs() / scale
+        res[name] = (float(rel.max()), int((rel > tol).sum()), rel.numel())
     return res
 
 

@@ -1,0 +1,215 @@
+"""GPU parity tests: the CUDA step (through the C-ABI) against the CPU oracle.
+
+Criterion.  For every bin value of the new state x = x_old + tendency * dt:
+    |x_gpu - x_oracle| <= max(RTOL * max(|x_oracle|, |x_old|, floor), C_ENV * envelope)
+where `envelope` is the oracle's own response to one-ulp perturbations of its inputs
+(T, rv, aerosol masses).  The reference's explicit, clamped condensation substep
+loop amplifies ulp differences in a few Aitken-bin water masses by many orders of
+magnitude (tests/test_oracle.py), so no non-bit-identical implementation can meet
+RTOL there; everywhere else the bound is RTOL.
+FP64 form: RTOL = 1e-10.  FP32-mixed form: RTOL = 1e-6 with the envelope taken from
+float-sized (1e-7) perturbations.
+"""
+import pytest
+import torch
+
+from uclales_salsa_gb300.inputs import make_inputs, make_outputs
+from uclales_salsa_gb300.api import SalsaStep
+from uclales_salsa_gb300 import capi
+from oracle_ref import Oracle
+from parity import STATE_OF, NUMBER_FIELDS, FLOOR, interior, output_errors
+
+pytestmark = pytest.mark.gpu
+C_ENV = 10.0
+CASES = [("grid16x16x40", {}), ("grid256x256x128", dict(X=8, Y=8, Z=16)), ("grid384x384x160", dict(X=16, Y=16, Z=12))]
+
+
+def oracle_run(inp, fields=None, scale=None, pert_eps=0.0, pert_field=None):
+    f = {k: v.clone() for k, v in (fields or inp.fields).items()}
+    if pert_field:
+        f[pert_field] = f[pert_field] * (1 + pert_eps)
+    out = make_outputs(inp)
+    rc, st = Oracle(inp.cfg).run(inp, f, out, time=1.0)
+    assert rc == 0, st.as_dict()
+    return f, out
+
+
+def gpu_run(inp, fields=None, host=False, diag=True):
+    src = fields or inp.fields
+    if host:
+        f = {k: v.clone().pin_memory() for k, v in src.items()}
+        out = {k: v.pin_memory() for k, v in make_outputs(inp, with_diag=diag).items()}
+    else:
+        f = {k: v.clone().cuda() for k, v in src.items()}
+        out = {k: v.cuda() for k, v in make_outputs(inp, with_diag=diag).items()}
+    step = SalsaStep(inp.cfg)
+    rc, st = step.run(inp, f, out, time=1.0)
+    torch.cuda.synchronize()
+    assert rc == 0, st.as_dict()
+    assert st.n_cells == inp.ncells
+    step.close()
+    return f, {k: v.cpu() for k, v in out.items()}
+
+
+def envelope(inp, base, eps):
+    env = {k: torch.zeros_like(v) for k, v in base.items()}
+    for pf in ("temp", "rp", "maero"):
+        _, o = oracle_run(inp, pert_eps=eps, pert_field=pf)
+        for k in env:
+            env[k] = torch.maximum(env[k], (o[k] - base[k]).abs())
+    return env
+
+
+def check(inp, gpu, ref, env, rtol):
+    report = {}
+    for name, st in STATE_OF.items():
+        if name not in ref:
+            continue
+        dt = inp.dt
+        I = lambda t: interior(t, inp.nzp, inp.nxp, inp.nyp)
+        old = I(inp.fields[st])
+        a, b = old + I(gpu[name]) * dt, old + I(ref[name]) * dt
+        e = I(env[name]) * dt
+        fl = FLOOR["rp"] if name == "rpt" else (FLOOR["n"] if name in NUMBER_FIELDS else FLOOR["m"])
+        scale = torch.maximum(b.abs(), old.abs()).clamp(min=fl)
+        err = (a - b).abs()
+        bound = torch.maximum(rtol * scale, C_ENV * e)
+        rel = err / scale
+        report[name] = dict(max_rel=float(rel.max()), frac_within=float((rel <= rtol).double().mean()),
+                            violations=int((err > bound).sum()))
+    return report
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+def test_fp64_parity(name, kw):
+    inp = make_inputs(name, "cpu", precision=0, **kw)
+    _, ref = oracle_run(inp)
+    _, gpu = gpu_run(inp)
+    env = envelope(inp, ref, 2.2e-16)
+    rep = check(inp, gpu, ref, env, 1e-10)
+    print(name, rep)
+    for k, r in rep.items():
+        assert r["violations"] == 0, (k, r)
+        assert r["frac_within"] > 0.999, (k, r)
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+def test_fp32_mixed_error_bound(name, kw):
+    inp = make_inputs(name, "cpu", precision=1, **kw)
+    _, ref = oracle_run(inp)
+    _, gpu = gpu_run(inp)
+    env = envelope(inp, ref, 1e-7)
+    rep = check(inp, gpu, ref, env, 1e-6)
+    print(name, rep)
+    for k, r in rep.items():
+        assert r["violations"] == 0, (k, r)
+
+
+def test_diagnostics_and_outputs_match():
+    inp = make_inputs("grid384x384x160", "cpu", precision=0, X=12, Y=12, Z=8)
+    _, ref = oracle_run(inp)
+    _, gpu = gpu_run(inp)
+    errs = output_errors(inp, gpu, ref)
+    print(errs)
+    for k, v in errs.items():
+        assert v < 1e-6, (k, v)   # relative to the field's largest value
+    assert float(gpu["pa_nactd"].abs().max()) == 0.0   # interstitial activation leaves them zero
+
+
+def test_in_deficit_fraction_matches():
+    inp = make_inputs("grid384x384x160", "cpu", precision=0, X=12, Y=12, Z=8)
+    fr, _ = oracle_run(inp)
+    fg, _ = gpu_run(inp)
+    a, b = fg["indef"].cpu(), fr["indef"]
+    assert float((a - b).abs().max()) < 1e-9
+
+
+def test_host_and_device_pointers_agree():
+    inp = make_inputs("grid256x256x128", "cpu", precision=0, X=8, Y=8, Z=8)
+    fh, oh = gpu_run(inp, host=True)
+    fd, od = gpu_run(inp, host=False)
+    for k in oh:
+        assert torch.equal(oh[k], od[k]), k
+    assert torch.equal(fh["indef"].cpu(), fd["indef"].cpu())
+
+
+def test_deterministic_and_diagnostics_do_not_change_state():
+    inp = make_inputs("grid384x384x160", "cpu", precision=0, X=12, Y=12, Z=8)
+    _, a = gpu_run(inp)
+    _, b = gpu_run(inp)
+    for k in a:
+        assert torch.equal(a[k], b[k]), k
+    inp.cfg.diagnostics = 0
+    _, c = gpu_run(inp, diag=False)
+    for k in c:
+        assert torch.equal(a[k], c[k]), k
+
+
+def test_async_entry_on_caller_stream():
+    inp = make_inputs("grid384x384x160", "cuda", precision=1, X=8, Y=8, Z=8)
+    out = make_outputs(inp)
+    step = SalsaStep(inp.cfg)
+    s = torch.cuda.Stream()
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    rc, st = step.run(inp, f, out, stream=s)
+    s.synchronize()
+    assert rc == 0 and st.n_cells == inp.ncells
+    out2 = make_outputs(inp)
+    f2 = {k: v.clone() for k, v in inp.fields.items()}
+    step.run(inp, f2, out2)
+    for k in out:
+        assert torch.equal(out[k], out2[k]), k
+
+
+def test_error_codes():
+    import ctypes as C
+    from uclales_salsa_gb300 import api
+    inp = make_inputs("grid16x16x40", "cuda", X=4, Y=4, Z=4)
+    step = SalsaStep(inp.cfg)
+    out = make_outputs(inp)
+    f = capi.make_fields(inp.fields, out)
+    st = capi.Status()
+    L = api.library()
+    run = lambda *a: L.salsa_gb300_run(step.h, *a, C.byref(f), C.byref(st))
+    assert run(inp.nzp, inp.nxp, inp.nyp, inp.ns, 1.0, 1.0, 1, 5, 0, 0) == capi.SALSA_E_ARG    # level mismatch
+    assert run(inp.nzp, 4, inp.nyp, inp.ns, 1.0, 1.0, 1, 4, 0, 0) == capi.SALSA_E_ARG         # nxp < 5
+    assert run(inp.nzp, inp.nxp, inp.nyp, inp.ns, 1e4, 1.0, 1, 4, 0, 0) == capi.SALSA_E_ARG   # tstep bound
+    assert run(inp.nzp, inp.nxp, inp.nyp, 2, 1.0, 1.0, 1, 4, 0, 0) == capi.SALSA_E_ARG        # ns < nwet
+    assert run(inp.nzp, inp.nxp, inp.nyp, inp.ns, 1.0, 1.0, 1, 4, 1, 0) == capi.SALSA_E_ARG   # lcharge w/o array
+    f.press = capi.ptr_of(0)
+    assert run(inp.nzp, inp.nxp, inp.nyp, inp.ns, 1.0, 1.0, 1, 4, 0, 0) == capi.SALSA_E_ARG   # NULL input
+    cfg = inp.cfg
+    cfg.nsnucl = 1
+    h = C.c_void_p()
+    assert L.salsa_gb300_init(C.byref(cfg), C.byref(h)) == capi.SALSA_E_UNSUPPORTED
+
+
+def test_full_size_invariants():
+    """256x256x128 (8.4M cells): finite, non-negative state and a closed water budget
+    for condensation + activation (size-independent properties of the step)."""
+    inp = make_inputs("grid256x256x128", "cuda", precision=0, diagnostics=0)
+    inp.cfg.lscoag.sw = 0
+    inp.cfg.lsicenucl.sw = 0
+    out = make_outputs(inp, with_diag=False)
+    step = SalsaStep(inp.cfg)
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    rc, st = step.run(inp, f, out, time=1.0)
+    torch.cuda.synchronize()
+    assert rc == 0 and st.n_cells == inp.ncells and st.n_nonfinite == 0
+    lay, dt = inp.layout, inp.dt
+    I = lambda t: interior(t, inp.nzp, inp.nxp, inp.nyp)
+    for name, s in STATE_OF.items():
+        if name in out:
+            new = I(inp.fields[s]) + I(out[name]) * dt
+            assert bool(torch.isfinite(new).all()), name
+            assert float(new.min()) > -1e-12 * float(I(inp.fields[s]).abs().max() + 1e-30), name
+    dn, T, p = I(inp.fields["dn"]), I(inp.fields["temp"]), I(inp.fields["press"])
+    rhoair = 28.97e-3 * p / (8.314 * T)
+    iw = lay.nwet - 1
+    dm = torch.zeros_like(dn)
+    for t, nb in (("maerot", lay.nbins), ("mcloudt", lay.ncld), ("mprecpt", lay.nprc)):
+        dm += I(out[t])[iw * nb:(iw + 1) * nb].sum(0) * dn
+    dm += I(out["micet"])[iw * lay.nice:(iw + 2) * lay.nice].sum(0) * dn
+    dv = I(out["rpt"]) * rhoair
+    total = I(inp.fields["rp"]) * rhoair / dt
+    assert float(((dm + dv).abs() / total).max()) < 1e-9

@@ -1,0 +1,214 @@
+"""CPU tests of the oracle (the FP64 restatement of run_SALSA used as parity checker)."""
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from uclales_salsa_gb300.inputs import make_inputs, make_outputs
+from uclales_salsa_gb300.layout import build_layout, lolim_diameters, PI6
+from uclales_salsa_gb300.config import workload_config
+from oracle_ref import Oracle, lib
+from parity import state_errors, interior
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def run(name, tweak=None, nthreads=0, carry_over=0, time=1.0, **kw):
+    inp = make_inputs(name, "cpu", **kw)
+    if tweak:
+        tweak(inp.cfg)
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    out = make_outputs(inp)
+    o = Oracle(inp.cfg)
+    rc, st = o.run(inp, f, out, time=time, nthreads=nthreads, carry_over=carry_over)
+    return inp, f, out, rc, st, o
+
+
+def only(*keep):
+    procs = ("lscoag", "lscnd", "lsactiv", "lsdistupdate", "lsicenucl", "lsicemelt")
+
+    def f(c):
+        for p in procs:
+            if p in keep:
+                continue
+            if p == "lsdistupdate":
+                c.lsdistupdate = 0
+            else:
+                getattr(c, p).sw = 0
+    return f
+
+
+@pytest.mark.parametrize("tag", ["grid16x16x40_sub", "grid256x256x128_sub", "grid384x384x160_sub"])
+def test_golden_fixtures(tag):
+    """The oracle reproduces its committed outputs (tests/golden/make_golden.py)."""
+    import golden.make_golden as mg
+    inp, f, out, rc = mg.run_case(mg.CASES[tag])
+    assert rc == 0
+    ref = np.load(os.path.join(HERE, "golden", f"{tag}.npz"))
+    for k, v in out.items():
+        a, b = v.numpy(), ref[f"out_{k}"]
+        assert a.shape == b.shape
+        diff = np.abs(a - b)
+        # bitwise on the generating platform; other libm builds may move ulp-sensitive bins
+        frac = float((diff <= 1e-12 * np.maximum(np.abs(b), 1e-300)).mean())
+        assert frac > 0.995, (k, frac)
+
+
+def test_layout_matches_reference_construction():
+    cfg = workload_config(5)
+    lay = build_layout(cfg)
+    o = Oracle(cfg)
+    (nbins, ncld, nprc, nice, nwet), lolim = o.layout()
+    assert (nbins, ncld, nprc, nice, nwet) == (17, 14, 7, 7, 6)
+    ref = lolim_diameters(lay)
+    for a, b in zip(ref, lolim[:lay.ntotal]):
+        assert abs(a - b) <= 1e-14 * b
+    # 3 nm - 10 um aerosol range, precipitation 20 um - 2 mm (mo_salsa_init.f90:148-450)
+    assert abs(lolim[0] - 3e-9) < 1e-20
+    assert abs(lay.vhilim[lay.fn2a] - PI6 * 1e-5 ** 3) < 1e-12 * PI6 * 1e-15
+    assert abs(lolim[nbins + ncld] - 20e-6) < 1e-18
+    top = (lay.vhilim[nbins + ncld + nprc - 1] / PI6) ** (1 / 3)
+    assert abs(top - 2e-3) < 1e-12
+    # cloud bins are parallel to the 2a and 2b aerosol bins (mo_salsa_init.f90:270-284)
+    for i in range(7):
+        assert lay.dmid[nbins + i] == lay.dmid[lay.in2a + i]
+        assert lay.dmid[nbins + 7 + i] == lay.dmid[lay.in2b + i]
+
+
+def test_terminal_velocity_stokes_regime():
+    """Small drops follow Stokes' law with the Cunningham factor (:259-261)."""
+    visc, rhoa = 1.8e-5, 1.2
+    for d in (1e-7, 1e-6, 1e-5):
+        v = lib().salsa_ref_terminal_vel(d, 1000., rhoa, visc, 1.1, 2)
+        assert v == pytest.approx(d * d * (1000. - rhoa) * 9.81 * 1.1 / (18. * visc), rel=1e-14)
+    # Beard and raindrop regimes increase monotonically across the 19 um and 1.07 mm limits
+    vs = [lib().salsa_ref_terminal_vel(d, 1000., rhoa, visc, 1.0, 3) for d in (15e-6, 25e-6, 1e-4, 1e-3, 2e-3)]
+    assert all(b > a for a, b in zip(vs, vs[1:]))
+    assert vs[-1] <= 9.2
+
+
+def coagc_numpy(d1, m1, rho1, d2, m2, rho2, T, P, eddy=0.001):
+    """Independent restatement of mo_salsa_coagulation_kernels.f90:263-407 (liquid, no charge)."""
+    pi, boltz, grav, rd, pstand = 3.1415927, 1.3807e-23, 9.81, 287.04, 1.01325e5
+    visc = (7.44523e-3 * math.sqrt(T ** 3)) / (5093. * (T + 110.4))
+    mfp = (1.656e-10 * T + 1.828e-8) * pstand / P
+    diam, mp = [d1, d2], [m1, m2]
+    knud = [2 * mfp / d for d in diam]
+    beta = [1 + k * (1.142 + 0.558 * math.exp(-0.999 / k)) for k in knud]
+    df = [b * boltz * T / (3 * pi * visc * d) for b, d in zip(beta, diam)]
+    mt = [math.sqrt(8 * boltz * T / (pi * m)) for m in mp]
+    om = [8 * f / (pi * v) for f, v in zip(df, mt)]
+    md = 0.5 * (d1 + d2)
+    f1 = 4 * pi * md * (df[0] + df[1])
+    f2 = pi * math.sqrt(mt[0] ** 2 + mt[1] ** 2) * md ** 2
+    tva = [((md + o) ** 3 - (md ** 2 + o ** 2) ** 1.5) / (3 * md * o) - md for o in om]
+    fm = math.sqrt(tva[0] ** 2 + tva[1] ** 2)
+    rhoa = P / (rd * T)
+    vkin = visc / rhoa
+    tv = [d * d * (r - rhoa) * grav * b / (18 * visc) for d, r, b in zip(diam, (rho1, rho2), beta)]
+    lrg, sml = (0, 1) if d1 >= d2 else (1, 0)
+    re = [d * v / vkin for d, v in zip(diam, tv)]
+    sc = [vkin / f for f in df]
+    stok = 2 * tv[sml] * abs(tv[0] - tv[1]) / (diam[lrg] * grav)
+    zb = f1 / (md / (md + fm) + f1 / f2)
+    zc = 0.45 * zb * (re[lrg] * sc[sml]) ** (1 / 3) if re[lrg] <= 1 else 0.45 * zb * math.sqrt(re[lrg]) * sc[sml] ** (1 / 3)
+    ts = math.sqrt(8 * pi * eddy / (15 * vkin)) * (0.5 * (d1 + d2)) ** 3
+    ti = pi * eddy ** 0.75 / (grav * math.sqrt(math.sqrt(vkin))) * (0.5 * (d1 + d2)) ** 2 * abs(tv[0] - tv[1])
+    zea = stok ** 2 / (stok + 0.5) ** 2
+    zev = (1 + 0.75 * math.log(2 * stok) / (stok - 1.214)) ** -2 if stok > 1.214 else 0.
+    ze = (60 * zev + zea * re[lrg]) / (60 + re[lrg])
+    zg = ze * pi * md ** 2 * abs(tv[0] - tv[1])
+    return zb + zc + math.sqrt(zg ** 2 + ts ** 2 + ti ** 2)
+
+
+def test_coagc_matches_independent_restatement():
+    cfg = workload_config(4)
+    o = Oracle(cfg)
+    lay = build_layout(cfg)
+    T, P = 285., 95e3
+    for b1, b2, d1, d2 in [(1, 5, 8e-9, 80e-9), (4, 20, 60e-9, 12e-6), (20, 33, 12e-6, 150e-6), (2, 36, 10e-9, 800e-6)]:
+        k = lib().salsa_ref_coagc_pair(o.h, b1, b2, 1e6, d1, 1e6, d2, T, P)
+        m1 = 1000. * PI6 * d1 ** 3
+        m2 = 1000. * PI6 * d2 ** 3
+        if lay.phase[b2] == 3 and d2 > 19e-6:
+            continue
+        kn = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
+        assert k == pytest.approx(kn, rel=1e-12), (b1, b2)
+
+
+def test_condensation_conserves_water():
+    """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
+    inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
+    assert rc == 0
+    lay, dt = inp.layout, inp.dt
+    dn = interior(inp.fields["dn"], inp.nzp, inp.nxp, inp.nyp)
+    T = interior(inp.fields["temp"], inp.nzp, inp.nxp, inp.nyp)
+    p = interior(inp.fields["press"], inp.nzp, inp.nxp, inp.nyp)
+    rhoair = 28.97e-3 * p / (8.314 * T)
+    iw = lay.nwet - 1
+    dm = 0.
+    for t, nb in (("maerot", lay.nbins), ("mcloudt", lay.ncld), ("mprecpt", lay.nprc)):
+        w = interior(out[t], inp.nzp, inp.nxp, inp.nyp)[iw * nb:(iw + 1) * nb].sum(0)
+        dm = dm + w * dn
+    dv = interior(out["rpt"], inp.nzp, inp.nxp, inp.nyp) * rhoair
+    total = interior(inp.fields["rp"], inp.nzp, inp.nxp, inp.nyp) * rhoair / dt
+    assert float(((dm + dv).abs() / total).max()) < 1e-9
+
+
+def test_activation_and_redistribution_conserve():
+    for keep in (("lsactiv",), ("lsdistupdate",)):
+        inp, f, out, rc, st, _ = run("grid384x384x160", only(*keep), X=8, Y=8, Z=8)
+        assert rc == 0
+        lay = inp.layout
+        I = lambda t: interior(t, inp.nzp, inp.nxp, inp.nyp)
+        n_old = I(inp.fields["naero"]).sum(0) + I(inp.fields["ncloud"]).sum(0)
+        dn_tot = I(out["naerot"]).sum(0) + I(out["ncloudt"]).sum(0)
+        assert float((dn_tot.abs() * inp.dt / n_old).max()) < 1e-12
+        for s in range(lay.ndry):
+            m_old = I(inp.fields["maero"])[s * lay.nbins:(s + 1) * lay.nbins].sum(0) + \
+                I(inp.fields["mcloud"])[s * lay.ncld:(s + 1) * lay.ncld].sum(0)
+            dm = I(out["maerot"])[s * lay.nbins:(s + 1) * lay.nbins].sum(0) + \
+                I(out["mcloudt"])[s * lay.ncld:(s + 1) * lay.ncld].sum(0)
+            assert float((dm.abs() * inp.dt / m_old).max()) < 1e-12
+
+
+def test_threads_do_not_change_results():
+    inp1, _, o1, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, nthreads=1)
+    inp2, _, o2, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, nthreads=0)
+    for k in o1:
+        assert torch.equal(o1[k], o2[k]), k
+
+
+def test_per_cell_state_reset_equals_carry_over_when_coagulating():
+    """With coagulation on, every derived diameter is recomputed before use, so the
+    reference's cell-to-cell module carry-over does not change a time step."""
+    _, _, a, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, carry_over=1)
+    _, _, b, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, carry_over=0)
+    for k in a:
+        assert torch.equal(a[k], b[k]), k
+
+
+def test_reference_scheme_is_ill_conditioned_in_aitken_water():
+    """One-ulp input perturbations move the condensed water of some Aitken bins by far
+    more than 1e-10: parity there is bounded by the scheme's conditioning."""
+    inp, f, base, _, _, _ = run("grid16x16x40", X=8, Y=8, Z=16)
+    inp2 = make_inputs("grid16x16x40", "cpu", X=8, Y=8, Z=16)
+    f2 = {k: v.clone() for k, v in inp2.fields.items()}
+    f2["rp"] = f2["rp"] * (1 + 2.2e-16)
+    out2 = make_outputs(inp2)
+    Oracle(inp2.cfg).run(inp2, f2, out2, time=1.0)
+    e = state_errors(inp, inp.fields, out2, base, tol=1e-10)
+    assert e["maerot"][0] > 1e-8
+
+
+def test_unsupported_and_bad_configs():
+    import ctypes as C
+    from uclales_salsa_gb300.capi import Config
+    for mod, code in ((lambda c: setattr(c, "nsnucl", 2), 2), (lambda c: setattr(c.lssecice, "sw", 1), 2),
+                      (lambda c: setattr(c, "nspec_dry", 0), 1), (lambda c: c.set_species(["SO4", "XX"]), 1)):
+        cfg = workload_config(5)
+        mod(cfg)
+        h = C.c_void_p()
+        assert lib().salsa_ref_create(C.byref(cfg), C.byref(h)) == code

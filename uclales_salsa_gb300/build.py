@@ -16,6 +16,9 @@ LIB = os.path.join(BUILD, "libsalsa_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 UNITS = ["salsa_k_d0.cu", "salsa_k_d1.cu", "salsa_k_f0.cu", "salsa_k_f1.cu", "salsa_capi.cu"]
+# The FP64 (parity) form is compiled without multiply-add contraction so that its
+# arithmetic rounds like the reference's x86-64 SSE2 build; the mixed form keeps FMA.
+FP64_UNITS = ("salsa_k_d0.cu", "salsa_k_d1.cu")
 
 
 def nvcc():
@@ -45,7 +48,8 @@ def build(force=False, verbose=False):
 
     def compile_one(u):
         obj = os.path.join(BUILD, u.replace(".cu", ".o"))
-        cmd = [cc] + ARCH + FLAGS + ["-c", os.path.join(CSRC, u), "-o", obj]
+        extra = ["-fmad=false"] if u in FP64_UNITS else []
+        cmd = [cc] + ARCH + FLAGS + extra + ["-c", os.path.join(CSRC, u), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {u}:\n{r.stdout}\n{r.stderr}")

@@ -199,12 +199,22 @@ __device__ T terminal_vel(T diam, T rhop, T rhoa, T visc, T beta, int flag, cons
     T Ap = sh.gamma * t_pow(dnsp, sh.sigma);
     T X = ((T)2. * Vb * (rhop - rhoa) * grav * sq(dnsp)) / (Ap * rhoa * sq(visc));
     const T c1 = (T)0.0902, delta0 = (T)9.06;
-    T k12 = t_sqrt((T)1. + c1 * t_sqrt(X));
-    T bre = (T)0.5 * c1 * t_sqrt(X);
-    bre = bre / (k12 - (T)1.);
-    bre = bre / k12;
+    T k12, km1, bre;
+    if (sizeof(T) == 8) {
+      k12 = t_sqrt((T)1. + c1 * t_sqrt(X));
+      km1 = k12 - (T)1.;
+      bre = (T)0.5 * c1 * t_sqrt(X);
+      bre = bre / km1;
+      bre = bre / k12;
+    } else {
+      // float: sqrt(1+y)-1 = y/(sqrt(1+y)+1) and b_Re = (1 + 1/k12)/2, free of cancellation
+      T y = c1 * t_sqrt(X);
+      k12 = t_sqrt((T)1. + y);
+      km1 = y / (k12 + (T)1.);
+      bre = (T)0.5 * ((T)1. + (T)1. / k12);
+    }
     T are = (T)0.25 * sq(delta0);
-    are = are * sq(k12 - (T)1.);
+    are = are * sq(km1);
     are = are / t_pow(X, bre);
     T Av = are * t_pow(visc, (T)1. - (T)2. * bre);
     Av = Av * t_pow(((T)2. * sh.alpha * grav) / (rhoa * sh.gamma), bre);
@@ -238,16 +248,36 @@ __device__ void bin_props(const CoagCell<T> &cc, int ph, T diam, T dsph, T mass,
   o.schm = cc.vkin / o.dfpart;
 }
 
+// ((m+w)^3 - (m^2+w^2)^(3/2)) / (3 m w) - m without cancellation (float form of :305-313):
+// with u = min(m,w)/max(m,w) and E = (1+u^2)^(3/2) - 1 = expm1(1.5 log1p(u^2)),
+// w <= m: m (u + u^2/3 - E/(3u));  w > m: w (1 + u^2/3 - E/(3u)).
+__device__ __forceinline__ float flux_match_stable(float m, float w) {
+  bool small = w <= m;
+  float L = small ? m : w;
+  float u = small ? w / m : m / w;
+  float u2 = u * u;
+  float E = expm1f(1.5f * log1pf(u2));
+  float core = u2 * (1.f / 3.f) - E / (3.f * u);
+  return small ? m * (u + core) : w * (1.f + core);
+}
+__device__ __forceinline__ double flux_match_stable(double m, double w) { return 0.; }
+
 // pair part of coagc (:298-416)
 template <typename T>
 __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinProps<T> &b) {
   T mdiam = (T)0.5 * (a.diam + b.diam);
   T flux1 = (T)4. * (T)K_PI * mdiam * (a.dfpart + b.dfpart);
   T flux2 = (T)K_PI * t_sqrt(sq(a.mtvel) + sq(b.mtvel)) * sq(mdiam);
-  T m2 = sq(mdiam);
-  T oa2 = m2 + sq(a.omega), ob2 = m2 + sq(b.omega);
-  T tva1 = (cube(mdiam + a.omega) - oa2 * t_sqrt(oa2)) / ((T)3. * mdiam * a.omega) - mdiam;
-  T tva2 = (cube(mdiam + b.omega) - ob2 * t_sqrt(ob2)) / ((T)3. * mdiam * b.omega) - mdiam;
+  T tva1, tva2;
+  if (sizeof(T) == 8) {
+    T m2 = sq(mdiam);
+    T oa2 = m2 + sq(a.omega), ob2 = m2 + sq(b.omega);
+    tva1 = (cube(mdiam + a.omega) - oa2 * t_sqrt(oa2)) / ((T)3. * mdiam * a.omega) - mdiam;
+    tva2 = (cube(mdiam + b.omega) - ob2 * t_sqrt(ob2)) / ((T)3. * mdiam * b.omega) - mdiam;
+  } else {
+    tva1 = flux_match_stable(mdiam, a.omega);
+    tva2 = flux_match_stable(mdiam, b.omega);
+  }
   T fmdist = t_sqrt(sq(tva1) + sq(tva2));
   bool first_large = a.diam >= b.diam;
   const BinProps<T> &L = first_large ? a : b;
