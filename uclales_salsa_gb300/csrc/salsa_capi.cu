@@ -86,6 +86,7 @@ struct salsa_handle {
   size_t stage_bytes = 0;
   int last_launches = 0;
   double last_kernel_ms = 0.;
+  unsigned long long *d_stage = nullptr;   // instrumented builds only
 };
 
 extern "C" {
@@ -366,6 +367,11 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   B.rows = h->d_rows;
   B.pairs = h->d_pairs;
   B.status = h->d_status;
+#ifdef SALSA_STAGE_TIMERS
+  cudaMalloc(&h->d_stage, 16 * sizeof(unsigned long long));
+  cudaMemset(h->d_stage, 0, 16 * sizeof(unsigned long long));
+  B.stage_clocks = h->d_stage;
+#endif
   B.Eiagg_max = g.Eiagg_max; B.Eiagg_min = g.Eiagg_min; B.eddy_dis = g.eddy_dis; B.rhlim = g.rhlim;
   B.initMinTheta = g.initMinTheta; B.chargeTimeMax = g.chargeTMax; B.chargeCollEnh = g.chargeCollEnh;
   B.mean_theta_imm = g.mean_theta_imm; B.sigma_theta_imm = g.sigma_theta_imm;
@@ -619,6 +625,15 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
 }
 
 }  // namespace
+
+#ifdef SALSA_STAGE_TIMERS
+extern "C" int salsa_gb300_stage_clocks(salsa_handle_t *h, unsigned long long *out16) {
+  cudaDeviceSynchronize();
+  cudaMemcpy(out16, h->d_stage, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaMemset(h->d_stage, 0, 16 * sizeof(unsigned long long));
+  return 0;
+}
+#endif
 
 extern "C" int salsa_gb300_run(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep, double time,
                                int istp, int level, int lcharge, int initialize, const salsa_fields_t *f,

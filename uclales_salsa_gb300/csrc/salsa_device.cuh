@@ -110,6 +110,7 @@ struct DevParams {
   const double *tables;     // bin tables (see TAB_* offsets)
   const int *pairs;         // packed pair list (i | j << 8)
   unsigned long long *status;
+  unsigned long long *stage_clocks;   // per-stage clock sums (instrumented builds only)
 };
 
 // block table layout (per bin, padded to nb_pad): offsets in units of nb_pad

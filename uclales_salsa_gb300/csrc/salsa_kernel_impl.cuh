@@ -414,6 +414,32 @@ __device__ void build_kernels(const DevParams &P, const WS<KT> &w, const double 
 // is accumulated lane-parallel and reduced once.  Only the diagnostics that reach the
 // output fields are accumulated (the number-only rate tallies of accumulateSink never do).
 // ----------------------------------------------------------------------------------------
+// Sum eight per-lane values over the warp with 9 adds: each butterfly step keeps half of
+// the values and exchanges the other half, after which every lane receives all totals.
+__device__ __forceinline__ void warp_sum8(double (&v)[8], int lane) {
+  const unsigned F = 0xffffffffu;
+  const bool h = lane & 16, g = lane & 8, f = lane & 4;
+  double a[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    double send = h ? v[i] : v[i + 4];
+    double keep = h ? v[i + 4] : v[i];
+    a[i] = keep + __shfl_xor_sync(F, send, 16);
+  }
+  double b[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    double send = g ? a[i] : a[i + 2];
+    double keep = g ? a[i + 2] : a[i];
+    b[i] = keep + __shfl_xor_sync(F, send, 8);
+  }
+  double c = (f ? b[1] : b[0]) + __shfl_xor_sync(F, f ? b[0] : b[1], 4);
+  c += __shfl_xor_sync(F, c, 2);
+  c += __shfl_xor_sync(F, c, 1);
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __shfl_sync(F, c, ((i >> 2) << 4) | (((i >> 1) & 1) << 3) | ((i & 1) << 2));
+}
+
 struct TAcc {
   double sink, self;
   double src[SALSA_NSV];
@@ -425,14 +451,26 @@ struct TAcc {
 #pragma unroll
     for (int d = 0; d < 7; d++) dg[d] = 0.;
   }
-  __device__ __forceinline__ void reduce(bool diag) {
-    sink = warp_sum(sink);
-    self = warp_sum(self);
+  __device__ __forceinline__ void reduce(bool diag, int lane) {
+    double v[8];
 #pragma unroll
-    for (int s = 0; s < SALSA_NSV; s++) src[s] = warp_sum(src[s]);
+    for (int s = 0; s < 7; s++) v[s] = src[s];
+    v[7] = sink;
+    warp_sum8(v, lane);
+#pragma unroll
+    for (int s = 0; s < 7; s++) src[s] = v[s];
+    sink = v[7];
     if (diag) {
+      double u[8];
+      u[0] = self;
 #pragma unroll
-      for (int d = 0; d < 7; d++) dg[d] = warp_sum(dg[d]);
+      for (int d = 0; d < 7; d++) u[d + 1] = dg[d];
+      warp_sum8(u, lane);
+      self = u[0];
+#pragma unroll
+      for (int d = 0; d < 7; d++) dg[d] = u[d + 1];
+    } else {
+      self = warp_sum(self);
     }
   }
 };
@@ -556,7 +594,7 @@ __device__ void coag_aero(const DevParams &P, const WS<KT> &w, double dt, int la
         if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
       }
     }
-    a.reduce(false);
+    a.reduce(false, lane);
     apply_coag(w, kk, nspec, dt, a, lane);
   }
 }
@@ -711,7 +749,7 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
           source_range(w, tg, C0, o_first, other, nspec, a, lane);
         }
       }
-      a.reduce(diag);
+      a.reduce(diag, lane);
       if (diag && lane == 0) {
         double nt = w.numc[tg];
         w.misc[M_DIAG + DG_ACCOLL] += a.dg[6] * nt;
@@ -801,7 +839,7 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
         }
       }
     }
-    a.reduce(diag);
+    a.reduce(diag, lane);
     if (diag && lane == 0) {
       double nt = w.numc[tg];
       w.misc[M_DIAG + DG_APCOLL] += a.dg[6] * nt;
@@ -886,7 +924,7 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, double dt, int lan
         double k = (double)kget(w, g, tg);
         for (int s = 0; s < nspec; s++) a.src[s] += E * k * w.v(s, g);
       }
-    a.reduce(false);
+    a.reduce(false, lane);
     // applyCoagIce (:605-651): every species slot with the same semi-implicit form
     apply_coag(w, tg, nspec, dt, a, lane);
     if (lane == 0) w.rhomean[tg] = rhomean_of(P, 4, w.numc[tg], w.v(iwa, tg), w.v(irim, tg));
@@ -909,7 +947,13 @@ __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *t
     if (inker) w.rhomean[b] = rhomean_of(P, ph, w.numc[b], w.v(P.iwa, b), w.v(P.irim, b));
   }
   __syncwarp();
+#ifdef SALSA_STAGE_TIMERS
+  long long t_k0 = clock64();
+#endif
   build_kernels<KT>(P, w, tb, T, pres, lane);
+#ifdef SALSA_STAGE_TIMERS
+  if (lane == 0 && P.stage_clocks) atomicAdd(P.stage_clocks + 8, (unsigned long long)(clock64() - t_k0));
+#endif
   bool any_aero = P.lscgaa || P.lscgca || P.lscgpa || P.lscgia;
   bool any_cloud = P.lscgcc || P.lscgca || P.lscgpc || P.lscgic;
   bool any_precp = P.lscgpp || P.lscgpa || P.lscgpc || P.lscgip;
@@ -1051,8 +1095,14 @@ __device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb,
   double zaelwc1 = warp_sum(l1) * K_RHOWA;
   // The init-form call repeats the 1a update with identical inputs (dwet untouched by
   // the first call, zke restarted at 1.001), so running it alone gives the same state.
+#ifdef SALSA_STAGE_TIMERS
+  long long t_eq0 = clock64();
+#endif
   if (zrh < 0.98 || !P.lscndh2oae) equilibration<KT>(P, w, tb, zrh, T, true, lane);
   else equilibration<KT>(P, w, tb, zrh, T, false, lane);
+#ifdef SALSA_STAGE_TIMERS
+  if (lane == 0 && P.stage_clocks) atomicAdd(P.stage_clocks + 10, (unsigned long long)(clock64() - t_eq0));
+#endif
   double l2 = 0.;
   for (int b = lane; b <= P.fn2b; b += 32) l2 += w.v(iwa, b);
   double zaelwc2 = warp_sum(l2) * K_RHOWA;
@@ -1155,6 +1205,9 @@ __device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb,
   const double mtot = warp_sum(msum);
   double ttot = 0., zcwint = 0.;
   int counter = 0;
+#ifdef SALSA_STAGE_TIMERS
+  long long t_sub0 = clock64();
+#endif
   while (ttot < dt) {
     const double adt = 2.e-2;
     double sp = 0.;
@@ -1182,6 +1235,9 @@ __device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb,
     if (counter >= 200000) break;   // the C-ABI bounds tstep, so this cap is never the exit path
   }
   if (counter > 100 && lane == 0) w.misc[M_FLAGS + F_COND] = 1.;
+#ifdef SALSA_STAGE_TIMERS
+  if (lane == 0 && P.stage_clocks) atomicAdd(P.stage_clocks + 9, (unsigned long long)(clock64() - t_sub0));
+#endif
   prv = zcwint * K_MWA / rhoair;
   // Cond_i diagnostic (:1086-1112): vrate(irim) is only assigned on sublimation and keeps
   // its previous value on later deposition bins; the sum follows the ice bins in order.
@@ -1812,222 +1868,237 @@ __device__ void ice_melt(const DevParams &P, const WS<KT> &w, const double *tb, 
 }
 
 // ----------------------------------------------------------------------------------------
-// distr_update: mo_salsa_update.f90:21-433.  Each sweep moves content between
-// neighbouring bins in descending bin order and depends on the previous moves, so it
-// runs on lane 0.  The bin-limit flag is overwritten by every checked bin (:132, 224,
-// 322, 418): the last checked bin decides whether another sweep follows.
+// distr_update: mo_salsa_update.f90:21-433.  A sweep visits the bins of a category in
+// descending order; a bin's move depends on what it holds when the sweep reaches it.
+// Moves go to the next bin up (visited already) or to a lower bin (visited later), so
+// every bin from the top down to the highest downward move holds its sweep-start
+// content when visited.  Those bins are processed by one lane each with the same
+// arithmetic as the sequential sweep; the bins below that point follow sequentially on
+// lane 0.  The bin-limit flag is overwritten by every checked bin (:132, 224, 322, 418):
+// the last checked bin decides whether another sweep follows.
 // ----------------------------------------------------------------------------------------
+enum { DC_AERO = 0, DC_CLOUD, DC_PRECP, DC_ICE };
+
+struct DStep {
+  int dir;              // 0 stays, 1 moves up, -1 moves down
+  int target;           // global index of the receiving bin
+  bool check, within, neg;
+  double own_n, push_n;
+  double own[SALSA_NSV], push[SALSA_NSV];
+};
+
+// One bin of one sweep given its current content (n, v): kk is the index inside the
+// category, g the global bin index.  Aerosols :66-136, cloud :150-226, precipitation
+// :240-324 (wet volume), ice :338-420 (total volume).
+template <int CAT>
+__device__ __forceinline__ void distr_bin(const DevParams &P, const double *tb, int kk, int g, double n,
+                                          const double (&v)[SALSA_NSV], DStep &o) {
+  const double *vlo = tb + TAB_VLO * P.nb_pad, *vhi = tb + TAB_VHI * P.nb_pad, *dmid = tb + TAB_DMID * P.nb_pad;
+  const int nmove = (CAT == DC_ICE) ? P.nused : P.nwet;
+  const int nsum = (CAT <= DC_CLOUD) ? P.ndry : nmove;
+  o.dir = 0; o.target = g; o.check = false; o.within = true; o.neg = false;
+  o.own_n = n; o.push_n = 0.;
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++) { o.own[s] = v[s]; o.push[s] = 0.; }
+  double sd = 0.;
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++) if (s < nsum) sd += v[s];
+  if (CAT == DC_AERO) {
+    if (!(n > K_NLIM) || g == P.fn2a) return;
+    const double zvpart = sd / n;
+    if (vlo[g] > zvpart) {
+      if (g == P.in1a) return;
+      o.dir = -1; o.target = (g == P.in2b) ? P.fn1a : g - 1;
+      o.own_n = 0.; o.push_n = n;
+#pragma unroll
+      for (int s = 0; s < SALSA_NSV; s++) if (s < nmove) { o.own[s] = 0.; o.push[s] = v[s]; }
+      return;
+    }
+    if (zvpart <= K_PI6 * cube(dmid[g])) return;
+    const double zVrat = vhi[g] / vlo[g];
+    const double zVilo = 2. * zvpart / (1. + zVrat);
+    const double zVihi = zVrat * zVilo;
+    const double zVexc = 0.5 * (zVihi + vhi[g]);
+    const double znfrac = fmin(1., (zVihi - vhi[g]) / (zVihi - zVilo));
+    const double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
+    o.neg = zvfrac < 0.;
+    const double f = znfrac * n * zVexc;
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++)
+      if (s < nmove) { double mv = f * v[s] / sd; o.push[s] = mv; o.own[s] = v[s] - mv; }
+    o.dir = 1; o.target = g + 1;
+    o.push_n = znfrac * n;
+    o.own_n = n * (1. - znfrac);
+    if (o.own_n > K_NLIM) {
+      double s2 = 0.;
+#pragma unroll
+      for (int s = 0; s < SALSA_NSV; s++) if (s < nsum) s2 += o.own[s];
+      const double zp = s2 / o.own_n;
+      o.check = true; o.within = (vlo[g] < zp && zp < vhi[g]);
+    }
+    return;
+  }
+  const double lim = (CAT == DC_CLOUD) ? K_NLIM : K_PRLIM;
+  if (!(n > lim) || (CAT == DC_CLOUD && !(sd > 1.e-30))) return;
+  const double zvpart = sd / n;
+  const double zVrat = vhi[g] / vlo[g];
+  const double zVilo = 2. * zvpart / (1. + zVrat);
+  const double zVihi = zVrat * zVilo;
+  double zVexc, znfrac;
+  if (CAT == DC_CLOUD) {
+    if (zvpart < vlo[g] && (kk != P.ica_cur && kk != P.icb_cur)) {
+      zVexc = 0.5 * (zVilo + vlo[g]);
+      znfrac = fmin(1., (vlo[g] - zVilo) / (zVihi - zVilo));
+      o.dir = -1;
+    } else if (zvpart > vhi[g] && (kk != P.fca_cur && kk != P.fcb_cur)) {
+      zVexc = 0.5 * (zVihi + vhi[g]);
+      znfrac = fmin(1., (zVihi - vhi[g]) / (zVihi - zVilo));
+      o.dir = 1;
+    } else {
+      return;
+    }
+  } else {
+    const int ntop = (CAT == DC_PRECP) ? P.nprc - 1 : P.nice - 1;
+    const double vm = K_PI6 * cube(dmid[g]);
+    const double zvdec = vm - 0.2 * (vm - vlo[g]);
+    if (zvpart < zvdec && kk != 0) {
+      zVexc = 0.5 * (zVilo + vlo[g]);
+      znfrac = fmin(1., (vlo[g] - zVilo) / (zVihi - zVilo));
+      o.dir = -1;
+    } else if (zvpart > vm && kk != ntop) {
+      zVexc = 0.5 * (zVihi + vhi[g]);
+      znfrac = fmin(0.99, (zVihi - vhi[g]) / (zVihi - zVilo));
+      o.dir = 1;
+    } else {
+      return;
+    }
+  }
+  o.target = g + o.dir;
+  const double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
+  o.neg = zvfrac < 0.;
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++)
+    if (s < nmove) { o.push[s] = zvfrac * v[s]; o.own[s] = v[s] - zvfrac * v[s]; }
+  o.push_n = znfrac * n;
+  o.own_n = n - znfrac * n;
+  double s2 = 0.;
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++) if (s < nsum) s2 += o.own[s];
+  const bool chk = (CAT == DC_PRECP) ? (o.own_n > lim) : (o.own_n > lim && s2 > 1.e-30);
+  if (chk) {
+    const double zp = s2 / o.own_n;
+    o.check = true; o.within = (vlo[g] < zp && zp < vhi[g]);
+  }
+}
+
+// Sequential part of a sweep (one thread): bins kk = from .. lo in descending order.
+template <int CAT, typename KT>
+__device__ void distr_serial(const DevParams &P, const WS<KT> &w, const double *tb, int base, int from, int lo,
+                             bool &has_check, bool &within, bool &neg) {
+  const int nmove = (CAT == DC_ICE) ? P.nused : P.nwet;
+  for (int kk = from; kk >= lo; kk--) {
+    const int g = base + kk;
+    double v[SALSA_NSV];
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) v[s] = (s < nmove) ? w.v(s, g) : 0.;
+    DStep o;
+    distr_bin<CAT>(P, tb, kk, g, w.numc[g], v, o);
+    if (o.dir != 0) {
+#pragma unroll
+      for (int s = 0; s < SALSA_NSV; s++)
+        if (s < nmove) { w.v(s, o.target) = w.v(s, o.target) + o.push[s]; w.v(s, g) = o.own[s]; }
+      w.numc[o.target] = w.numc[o.target] + o.push_n;
+      w.numc[g] = o.own_n;
+    }
+    if (o.check) { has_check = true; within = o.within; }
+    neg = neg || o.neg;
+  }
+}
+
+// One sweep over bins lo..hi of a category (global index base + kk); hi_recv > hi when
+// the bin above the sweep range can receive particles.  Returns the bin-limit flag.
+template <int CAT, typename KT>
+__device__ bool distr_sweep(const DevParams &P, const WS<KT> &w, const double *tb, int lane, int base, int lo,
+                            int hi, int hi_recv, bool &neg_flag) {
+  const unsigned F = 0xffffffffu;
+  const int nmove = (CAT == DC_ICE) ? P.nused : P.nwet;
+  bool has_check = false, within = true, neg = false;
+  if (hi_recv >= 32) {
+    if (lane == 0) distr_serial<CAT>(P, w, tb, base, hi, lo, has_check, within, neg);
+  } else {
+    const int kk = lane, g = base + lane;
+    const bool inr = kk >= lo && kk <= hi_recv;
+    const bool dec = kk >= lo && kk <= hi;
+    double v[SALSA_NSV];
+    double n = 0.;
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) v[s] = (inr && s < nmove) ? w.v(s, g) : 0.;
+    if (inr) n = w.numc[g];
+    DStep o;
+    if (dec) {
+      distr_bin<CAT>(P, tb, kk, g, n, v, o);
+    } else {
+      o.dir = 0; o.target = g; o.check = false; o.within = true; o.neg = false;
+      o.own_n = n; o.push_n = 0.;
+#pragma unroll
+      for (int s = 0; s < SALSA_NSV; s++) { o.own[s] = v[s]; o.push[s] = 0.; }
+    }
+    const unsigned down = __ballot_sync(F, dec && o.dir < 0);
+    const int D = down ? 31 - __clz(down) : -1;
+    const bool par = inr && kk >= D;
+    const bool up = par && o.dir > 0;
+    const bool in_up = (__shfl_up_sync(F, up ? 1 : 0, 1) != 0) && lane > 0;
+    const double pn = __shfl_up_sync(F, o.push_n, 1);
+    double pv[SALSA_NSV];
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) pv[s] = __shfl_up_sync(F, o.push[s], 1);
+    if (par) {
+#pragma unroll
+      for (int s = 0; s < SALSA_NSV; s++)
+        if (s < nmove) w.v(s, g) = in_up ? o.own[s] + pv[s] : o.own[s];
+      w.numc[g] = in_up ? o.own_n + pn : o.own_n;
+      if (kk == D) {
+#pragma unroll
+        for (int s = 0; s < SALSA_NSV; s++)
+          if (s < nmove) w.v(s, o.target) = w.v(s, o.target) + o.push[s];
+        w.numc[o.target] = w.numc[o.target] + o.push_n;
+      }
+    }
+    const unsigned cm = __ballot_sync(F, par && o.check);
+    if (cm) within = __shfl_sync(F, o.within, __ffs(cm) - 1);
+    neg = __any_sync(F, par && o.neg);
+    __syncwarp();
+    if (lane == 0 && D > lo) {
+      bool hc = false, wi = true;
+      distr_serial<CAT>(P, w, tb, base, D - 1, lo, hc, wi, neg);
+      if (hc) within = wi;
+    }
+  }
+  __syncwarp();
+  within = __shfl_sync(F, within, 0);
+  neg_flag = neg_flag || __shfl_sync(F, neg, 0);
+  return within;
+}
+
 template <typename KT>
 __device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *tb, int lane) {
+  bool f_distr = false, f_neg = false;
+#pragma unroll 1
+  for (int c = 0; c < 4; c++) {
+    if (c == DC_ICE && P.level < 5) break;
+    bool within = false;
+    int count = 0;
+    while (!within) {
+      switch (c) {
+        case DC_AERO: within = distr_sweep<DC_AERO>(P, w, tb, lane, 0, P.in1a, P.fn2b - 1, P.fn2b, f_neg); break;
+        case DC_CLOUD: within = distr_sweep<DC_CLOUD>(P, w, tb, lane, P.nbins, P.ica_cur, P.ncld - 1, P.ncld - 1, f_neg); break;
+        case DC_PRECP: within = distr_sweep<DC_PRECP>(P, w, tb, lane, P.nbins + P.ncld, 0, P.nprc - 1, P.nprc - 1, f_neg); break;
+        default: within = distr_sweep<DC_ICE>(P, w, tb, lane, P.nliquid, 0, P.nice - 1, P.nice - 1, f_neg); break;
+      }
+      if (++count > 100) { f_distr = true; break; }
+    }
+  }
   if (lane == 0) {
-    const double *vlo = tb + TAB_VLO * P.nb_pad, *vhi = tb + TAB_VHI * P.nb_pad, *dmid = tb + TAB_DMID * P.nb_pad;
-    const int zndry = P.ndry, znwet = P.nwet, znnsp = P.nused;
-    int f_distr = 0, f_neg = 0;
-    // aerosols
-    {
-      bool within = false;
-      int count = 0;
-      while (!within) {
-        within = true;
-        for (int kk = P.fn2b - 1; kk >= P.in1a; kk--) {
-          if (w.numc[kk] > K_NLIM) {
-            if (kk == P.fn2a) continue;
-            double sd = 0.;
-            for (int s = 0; s < zndry; s++) sd += w.v(s, kk);
-            double zvpart = sd / w.numc[kk];
-            if (vlo[kk] > zvpart && kk == P.in1a) continue;
-            if (vlo[kk] > zvpart) {
-              int mm = (kk == P.in2b) ? P.fn1a : kk - 1;
-              w.numc[mm] = w.numc[mm] + w.numc[kk];
-              w.numc[kk] = 0.;
-              for (int s = 0; s < znwet; s++) { w.v(s, mm) = w.v(s, mm) + w.v(s, kk); w.v(s, kk) = 0.; }
-              continue;
-            }
-            if (zvpart <= K_PI6 * cube(dmid[kk])) continue;
-            double zVrat = vhi[kk] / vlo[kk];
-            double zVilo = 2. * zvpart / (1. + zVrat);
-            double zVihi = zVrat * zVilo;
-            double zVexc = 0.5 * (zVihi + vhi[kk]);
-            double znfrac = fmin(1., (zVihi - vhi[kk]) / (zVihi - zVilo));
-            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
-            if (zvfrac < 0.) f_neg = 1;
-            int mm = kk + 1;
-            double f = znfrac * w.numc[kk] * zVexc;
-            for (int s = 0; s < znwet; s++) {
-              double vk = w.v(s, kk);
-              double mv = f * vk / sd;
-              w.v(s, mm) = w.v(s, mm) + mv;
-              w.v(s, kk) = vk - mv;
-            }
-            w.numc[mm] = w.numc[mm] + znfrac * w.numc[kk];
-            w.numc[kk] = w.numc[kk] * (1. - znfrac);
-          }
-          if (w.numc[kk] > K_NLIM) {
-            double sd = 0.;
-            for (int s = 0; s < zndry; s++) sd += w.v(s, kk);
-            double zvpart = sd / w.numc[kk];
-            within = (vlo[kk] < zvpart && zvpart < vhi[kk]);
-          }
-        }
-        if (++count > 100) { f_distr = 1; break; }
-      }
-    }
-    // cloud droplets
-    {
-      const int C0 = P.nbins;
-      bool within = false;
-      int count = 0;
-      while (!within) {
-        within = true;
-        for (int kk = P.ncld - 1; kk >= P.ica_cur; kk--) {
-          int g = C0 + kk;
-          double sd = 0.;
-          for (int s = 0; s < zndry; s++) sd += w.v(s, g);
-          if (w.numc[g] > K_NLIM && sd > 1.e-30) {
-            double zvpart = sd / w.numc[g];
-            double zVrat = vhi[g] / vlo[g];
-            double zVilo = 2. * zvpart / (1. + zVrat);
-            double zVihi = zVrat * zVilo;
-            double zVexc, znfrac;
-            int mm;
-            if (zvpart < vlo[g] && (kk != P.ica_cur && kk != P.icb_cur)) {
-              zVexc = 0.5 * (zVilo + vlo[g]);
-              znfrac = fmin(1., (vlo[g] - zVilo) / (zVihi - zVilo));
-              mm = kk - 1;
-            } else if (zvpart > vhi[g] && (kk != P.fca_cur && kk != P.fcb_cur)) {
-              zVexc = 0.5 * (zVihi + vhi[g]);
-              znfrac = fmin(1., (zVihi - vhi[g]) / (zVihi - zVilo));
-              mm = kk + 1;
-            } else {
-              continue;
-            }
-            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
-            if (zvfrac < 0.) f_neg = 1;
-            int gm = C0 + mm;
-            for (int s = 0; s < znwet; s++) {
-              double vk = w.v(s, g);
-              w.v(s, gm) = w.v(s, gm) + zvfrac * vk;
-              w.v(s, g) = vk - zvfrac * vk;
-            }
-            double nk = w.numc[g];
-            w.numc[gm] = w.numc[gm] + znfrac * nk;
-            w.numc[g] = nk - znfrac * nk;
-          }
-          sd = 0.;
-          for (int s = 0; s < zndry; s++) sd += w.v(s, g);
-          if (w.numc[g] > K_NLIM && sd > 1.e-30) {
-            double zvpart = sd / w.numc[g];
-            within = (vlo[g] < zvpart && zvpart < vhi[g]);
-          }
-        }
-        if (++count > 100) { f_distr = 1; break; }
-      }
-    }
-    // precipitation (wet volume)
-    {
-      const int P0 = P.nbins + P.ncld;
-      bool within = false;
-      int count = 0;
-      while (!within) {
-        within = true;
-        for (int kk = P.nprc - 1; kk >= 0; kk--) {
-          int g = P0 + kk;
-          if (w.numc[g] > K_PRLIM) {
-            double sw = 0.;
-            for (int s = 0; s < znwet; s++) sw += w.v(s, g);
-            double zvpart = sw / w.numc[g];
-            double zVrat = vhi[g] / vlo[g];
-            double zVilo = 2. * zvpart / (1. + zVrat);
-            double zVihi = zVrat * zVilo;
-            double vm = K_PI6 * cube(dmid[g]);
-            double zvdec = vm - 0.2 * (vm - vlo[g]);
-            double zVexc, znfrac;
-            int mm;
-            if (zvpart < zvdec && kk != 0) {
-              zVexc = 0.5 * (zVilo + vlo[g]);
-              znfrac = fmin(1., (vlo[g] - zVilo) / (zVihi - zVilo));
-              mm = kk - 1;
-            } else if (zvpart > vm && kk != P.nprc - 1) {
-              zVexc = 0.5 * (zVihi + vhi[g]);
-              znfrac = fmin(.99, (zVihi - vhi[g]) / (zVihi - zVilo));
-              mm = kk + 1;
-            } else {
-              continue;
-            }
-            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
-            if (zvfrac < 0.) f_neg = 1;
-            int gm = P0 + mm;
-            for (int s = 0; s < znwet; s++) {
-              double vk = w.v(s, g);
-              w.v(s, gm) = w.v(s, gm) + zvfrac * vk;
-              w.v(s, g) = vk - zvfrac * vk;
-            }
-            double nk = w.numc[g];
-            w.numc[gm] = w.numc[gm] + znfrac * nk;
-            w.numc[g] = nk - znfrac * nk;
-          }
-          if (w.numc[g] > K_PRLIM) {
-            double sw = 0.;
-            for (int s = 0; s < znwet; s++) sw += w.v(s, g);
-            double zvpart = sw / w.numc[g];
-            within = (vlo[g] < zvpart && zvpart < vhi[g]);
-          }
-        }
-        if (++count > 100) { f_distr = 1; break; }
-      }
-    }
-    if (P.level >= 5) {
-      const int I0 = P.nliquid;
-      bool within = false;
-      int count = 0;
-      while (!within) {
-        within = true;
-        for (int kk = P.nice - 1; kk >= 0; kk--) {
-          int g = I0 + kk;
-          if (w.numc[g] > K_PRLIM) {
-            double st = 0.;
-            for (int s = 0; s < znnsp; s++) st += w.v(s, g);
-            double zvpart = st / w.numc[g];
-            double zVrat = vhi[g] / vlo[g];
-            double zVilo = 2. * zvpart / (1. + zVrat);
-            double zVihi = zVrat * zVilo;
-            double vm = K_PI6 * cube(dmid[g]);
-            double zvdec = vm - 0.2 * (vm - vlo[g]);
-            double zVexc, znfrac;
-            int mm;
-            if (zvpart < zvdec && kk != 0) {
-              zVexc = 0.5 * (zVilo + vlo[g]);
-              znfrac = fmin(1.0, (vlo[g] - zVilo) / (zVihi - zVilo));
-              mm = kk - 1;
-            } else if (zvpart > vm && kk != P.nice - 1) {
-              zVexc = 0.5 * (zVihi + vhi[g]);
-              znfrac = fmin(0.99, (zVihi - vhi[g]) / (zVihi - zVilo));
-              mm = kk + 1;
-            } else {
-              continue;
-            }
-            double zvfrac = fmin(0.99, znfrac * zVexc / zvpart);
-            if (zvfrac < 0.) f_neg = 1;
-            int gm = I0 + mm;
-            for (int s = 0; s < znnsp; s++) {
-              double vk = w.v(s, g);
-              w.v(s, gm) = w.v(s, gm) + zvfrac * vk;
-              w.v(s, g) = vk - zvfrac * vk;
-            }
-            double nk = w.numc[g];
-            w.numc[gm] = w.numc[gm] + znfrac * nk;
-            w.numc[g] = nk - znfrac * nk;
-          }
-          double st = 0.;
-          for (int s = 0; s < znnsp; s++) st += w.v(s, g);
-          if (w.numc[g] > K_PRLIM && st > 1.e-30) {
-            double zvpart = st / w.numc[g];
-            within = (vlo[g] < zvpart && zvpart < vhi[g]);
-          }
-        }
-        if (++count > 100) { f_distr = 1; break; }
-      }
-    }
     if (f_distr) w.misc[M_FLAGS + F_DISTR] = 1.;
     if (f_neg) w.misc[M_FLAGS + F_NEGFRAC] = 1.;
   }
@@ -2040,8 +2111,22 @@ __device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *
 // salsa() (mo_salsa.f90:89-149).  Every cell starts from the post-initialisation module
 // state (bin templates), i.e. each cell sees allSALSA as the reference's first cell does.
 // ----------------------------------------------------------------------------------------
+#ifdef SALSA_STAGE_TIMERS
+#define STAGE_MARK(k)                                                              \
+  do {                                                                             \
+    long long t_ = clock64();                                                      \
+    if (lane == 0 && P.stage_clocks) atomicAdd(P.stage_clocks + (k), (unsigned long long)(t_ - t_stage)); \
+    t_stage = t_;                                                                  \
+  } while (0)
+#else
+#define STAGE_MARK(k) do { } while (0)
+#endif
+
 template <typename KT, bool DIAG>
 __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, int lane) {
+#ifdef SALSA_STAGE_TIMERS
+  long long t_stage = clock64();
+#endif
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   double *raw = w.raw;
   const double T = raw[RW_T], pres = raw[RW_P], rs = raw[RW_RS], rsi = raw[RW_RSI], dn = raw[RW_DN];
@@ -2081,19 +2166,25 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   for (int i = lane; i < M_PF; i += 32) w.misc[i] = 0.;
   __syncwarp();
   if (P.initialize) equilibration<KT>(P, w, tb, 0.3, T, true, lane);
+  STAGE_MARK(0);
 
   // ---- salsa() ----
   if (P.st_coag) coagulation<KT>(P, w, tb, dt, T, pres, DIAG, lane);
+  STAGE_MARK(1);
   if (P.st_cnd && (P.lscndh2ocl || P.lscndh2oae || P.lscndh2oic))
     gpparth2o<KT>(P, w, tb, T, pres, rs, rsi, rv, dt, kappa, DIAG, lane);
+  STAGE_MARK(2);
   if (P.st_auto && P.auto_mode == 2) autoconv2<KT>(P, w, dt, lane);
   if (P.st_activ && P.activ_mode == 1) act_interst<KT>(P, w, tb, rv, rs, T, DIAG, lane);
+  STAGE_MARK(3);
   if ((P.st_icenucl || P.icenucl_mode == 2) && (P.lsicehom || P.lsiceimm || P.lsicedep)) {
     if (P.ice_theta_dist) ice_nucl_SE<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
     else ice_nucl_classic<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
   }
   if (P.st_icemelt) ice_melt<KT>(P, w, tb, T, lane);
+  STAGE_MARK(4);
   if (P.lsdistupdate) distr_update<KT>(P, w, tb, lane);
+  STAGE_MARK(5);
 
   // ---- tendencies and outputs (mo_salsa_driver.f90:310-419) into the raw slots ----
   bool bad = false;
@@ -2148,6 +2239,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
     }
   }
   bad = warp_any(bad);
+  STAGE_MARK(6);
   if (lane == 0 && P.status) {
     const double *f = w.misc + M_FLAGS;
     if (f[F_EQUIL] != 0.) atomicAdd(P.status + ST_EQUIL, 1ull);
