@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -326,11 +327,94 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
     if (ci == 1 && cj == 3) return e.lscgic;
     return e.lscgip;
   };
-  std::vector<int> pairs;
+  // pairs of (nearly) equal bin sizes take the self-coagulation offset of coagc
+  // (mo_salsa_coagulation_kernels.f90:273-276); they are listed after the others
+  std::vector<int> pairs, pairs_eq;
   for (int i = 0; i < ntotal; i++)
     for (int j = i; j < ntotal; j++)
-      if (pair_on(cat_of(i), cat_of(j))) pairs.push_back(i | (j << 8));
+      if (pair_on(cat_of(i), cat_of(j))) {
+        bool eq = std::fabs(t.dmid[i] - t.dmid[j]) / t.dmid[i] < 1.e-2;
+        (eq ? pairs_eq : pairs).push_back(i | (j << 8));
+      }
+  B.npairs_plain = (int)pairs.size();
+  pairs.insert(pairs.end(), pairs_eq.begin(), pairs_eq.end());
   B.npairs = (int)pairs.size();
+
+  // ---- per-target partner lists of the plain sink and source sums of the coagulation
+  // update (the partner ranges of mo_salsa_coagulation_processes.f90:24-430 for aerosol,
+  // cloud and precipitation targets; self terms and weighted sums stay in the kernel) ----
+  {
+    std::vector<int16_t> hdr(4 * (size_t)ntotal, 0), ent;
+    auto rng = [&](std::vector<int16_t> &v, int g0, int a, int b) {
+      for (int x = a; x <= b; x++) v.push_back((int16_t)(g0 + x));
+    };
+    const int C0 = nbins, P0 = nbins + ncld, I0 = B.nliquid;
+    for (int t = 0; t < ntotal; t++) {
+      std::vector<int16_t> sk, sr;
+      int cat = cat_of(t);
+      if (cat == 0) {
+        int kk = t;
+        int reg = kk <= B.fn1a ? 0 : (kk <= B.fn2a ? 1 : 2);
+        if (reg == 0) {
+          int icla = B.ica_cur + std::max(kk - B.ica_par, 0);
+          int iclb = B.icb_cur + (icla - B.ica_cur);
+          if (e.lscgaa) rng(sk, 0, kk + 1, B.fn2b);
+          if (e.lscgca) { rng(sk, C0, icla, B.fca_cur); rng(sk, C0, iclb, B.fcb_cur); }
+          if (e.lscgaa && kk > B.in1a) rng(sr, 0, B.in1a, kk - 1);
+        } else if (reg == 1) {
+          int index_b = B.in2b + (kk - B.in2a);
+          int icla = B.ica_cur + std::max(kk - B.ica_par, 0);
+          int iclb = B.icb_cur + std::max(kk - B.ica_par, 0);
+          if (e.lscgaa && kk < B.fn2a) { rng(sk, 0, kk + 1, B.fn2a); rng(sk, 0, index_b, B.fn2b); }
+          if (e.lscgca) { rng(sk, C0, icla, B.fca_cur); rng(sk, C0, iclb, B.fcb_cur); }
+          if (e.lscgaa) { rng(sr, 0, B.in1a, kk - 1); rng(sr, 0, B.in2b, index_b); }
+        } else {
+          int index_a = B.in2a + (kk - B.in2b);
+          int icla = B.ica_cur + std::max(kk - B.icb_par, 0);
+          int iclb = B.icb_cur + std::max(kk - B.icb_par, 0);
+          if (e.lscgaa && kk < B.fn2b) { rng(sk, 0, kk + 1, B.fn2b); rng(sk, 0, index_a, B.fn2a); }
+          if (e.lscgca) { rng(sk, C0, icla, B.fca_cur); rng(sk, C0, iclb, B.fcb_cur); }
+          if (e.lscgaa) { rng(sr, 0, B.in2b, kk - 1); rng(sr, 0, B.in1a, index_a); }
+        }
+        if (e.lscgpa) rng(sk, P0, 0, nprc - 1);
+        if (e.lscgia) rng(sk, I0, 0, nice - 1);
+        if (e.lscgca) {
+          int icla, iclb;
+          if (reg < 2) { icla = B.ica_cur + (kk - B.ica_par) - 1; iclb = B.icb_cur + (icla - B.ica_cur); }
+          else { iclb = B.icb_cur + (kk - B.icb_par) - 1; icla = B.ica_cur + (iclb - B.icb_cur); }
+          if (icla >= B.ica_cur) rng(sr, C0, B.ica_cur, icla);
+          if (iclb >= B.icb_cur) rng(sr, C0, B.icb_cur, iclb);
+        }
+      } else if (cat == 1) {
+        int kk = t - C0;
+        bool ra = kk <= B.fca_cur;
+        int kfirst = ra ? B.ica_cur : B.icb_cur, klast = ra ? B.fca_cur : B.fcb_cur;
+        int o_first = ra ? B.icb_cur : B.ica_cur, o_last = ra ? B.fcb_cur : B.fca_cur;
+        int rel = kk - kfirst, other = o_first + rel;
+        if (e.lscgca && kk < klast) { rng(sk, 0, B.ica_par + rel + 1, B.fn2a); rng(sk, 0, B.icb_par + rel + 1, B.fn2b); }
+        if (e.lscgcc && kk < klast) { rng(sk, C0, kk + 1, klast); rng(sk, C0, other, o_last); }
+        if (e.lscgpc) rng(sk, P0, 0, nprc - 1);
+        if (e.lscgic) rng(sk, I0, 0, nice - 1);
+      } else if (cat == 2) {
+        int kk = t - P0;
+        if (e.lscgpp && kk < nprc - 1) rng(sk, P0, kk + 1, nprc - 1);
+        if (e.lscgip) rng(sk, I0, 0, nice - 1);
+      }
+      hdr[4 * t] = (int16_t)(4 * ntotal + ent.size());
+      hdr[4 * t + 1] = (int16_t)sk.size();
+      ent.insert(ent.end(), sk.begin(), sk.end());
+      hdr[4 * t + 2] = (int16_t)(4 * ntotal + ent.size());
+      hdr[4 * t + 3] = (int16_t)sr.size();
+      ent.insert(ent.end(), sr.begin(), sr.end());
+    }
+    hdr.insert(hdr.end(), ent.begin(), ent.end());
+    while (hdr.size() % 4) hdr.push_back(0);
+    B.list_off = (int)tab.size();
+    size_t nd = hdr.size() / 4;
+    tab.resize(tab.size() + nd, 0.);
+    std::memcpy(tab.data() + B.list_off, hdr.data(), hdr.size() * sizeof(int16_t));
+    B.tab_doubles = (int)tab.size();
+  }
 
   salsa_handle *h = new salsa_handle();
   h->cfg = g;
@@ -341,8 +425,9 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   int kt_bytes = g.precision == 0 ? 8 : 4;
   {
     size_t tri_n = (size_t)nbp * (nbp + 1) / 2;
-    size_t kd = (tri_n * kt_bytes + 7) / 8;
-    size_t n = ((B.nraw + 1) & ~1) + nbp + SALSA_NSV * nbp + 7 * nbp + 13 * nbp + 336 + 32 + kd;
+    // the kernel triangle; after the coagulation the ice nucleation keeps 8 doubles per liquid bin there
+    size_t kd = std::max((tri_n * kt_bytes + 7) / 8, (size_t)8 * B.nliquid);
+    size_t n = ((B.nraw + 1) & ~1) + nbp + SALSA_NSV * nbp + 7 * nbp + 13 * nbp + 336 + 64 + kd;
     B.ws_doubles = (int)((n + 1) & ~(size_t)1);
   }
   size_t smem = sizeof(double) * ((size_t)B.tab_doubles + (size_t)SALSA_CPG * B.ws_doubles);

@@ -101,8 +101,10 @@ struct DevParams {
   int raw_num, raw_mbase[4], raw_indef, raw_charge, raw_nact, raw_vact, raw_diag, nraw;
   int nrows;           // rows in the row table
   int npairs;          // collision pairs in the pair table
+  int npairs_plain;    // pairs before the equal-size (self-coagulation offset) section
   int ws_doubles;      // per-warp workspace size
   int tab_doubles;     // per-block table size
+  int list_off;        // offset (doubles) of the int16 partner lists inside the block table
   // pointers
   const double *fin[FI_N];
   double *fout[FO_N];

@@ -310,20 +310,45 @@ __device__ __forceinline__ void load_props(const KT *S, int NB, int b, BinProps<
   o.schm = S[8 * NB + b];
 }
 
+// Per-bin properties are evaluated in FP64 in both forms and stored in the kernel type:
+// the float forms of exp/pow in the terminal velocities (Beard; Khvorostyanov-Curry for
+// ice) amplify the rounding of their exponents by |log(base)| to ~1e-5.
 template <typename KT>
-__device__ void eval_pairs(const DevParams &P, const WS<KT> &w, const CoagCell<KT> &cc, const KT *S,
-                           const double *dmid, const int *list, int n, int lane) {
+__device__ __forceinline__ void store_props(KT *S, int NB, int b, const BinProps<double> &o) {
+  S[0 * NB + b] = (KT)o.diam; S[1 * NB + b] = (KT)o.mass; S[2 * NB + b] = (KT)o.beta; S[3 * NB + b] = (KT)o.dfpart;
+  S[4 * NB + b] = (KT)o.mtvel; S[5 * NB + b] = (KT)o.omega; S[6 * NB + b] = (KT)o.termv; S[7 * NB + b] = (KT)o.reyn;
+  S[8 * NB + b] = (KT)o.schm;
+}
+template <typename KT>
+__device__ __forceinline__ void to_kt(const BinProps<double> &d, BinProps<KT> &o) {
+  o.diam = (KT)d.diam; o.mass = (KT)d.mass; o.beta = (KT)d.beta; o.dfpart = (KT)d.dfpart; o.mtvel = (KT)d.mtvel;
+  o.omega = (KT)d.omega; o.termv = (KT)d.termv; o.reyn = (KT)d.reyn; o.schm = (KT)d.schm;
+}
+// FP64 shape coefficients of bin b: they share the memory of S rows 9-12 in the FP64
+// form and sit behind the float rows in the mixed form.
+template <typename KT>
+__device__ __forceinline__ double *shape_rows(const WS<KT> &w) {
+  return sizeof(KT) == 8 ? w.scr + 9 * w.NB : w.scr + 7 * w.NB;
+}
+
+template <typename KT, bool OFFSET>
+__device__ void eval_pairs(const DevParams &P, const WS<KT> &w, const CoagCell<KT> &cc, const CoagCell<double> &cd,
+                           const KT *S, const int *list, int n, int lane) {
   const int NB = w.NB;
   if (lane < n) {
     int q = list[lane];
     int i = q & 0xff, j = (q >> 8) & 0xff;
     BinProps<KT> a, b;
     load_props<KT>(S, NB, j, b);
-    if (fabs(dmid[i] - dmid[j]) / dmid[i] < 1.e-2) {
+    if (OFFSET) {
       // self-coagulation offset (:273-276): particle 1 takes 1.1x the diameter and 1.33x the mass of particle 2
-      Shape<KT> sh;
-      sh.alpha = S[9 * NB + i]; sh.beta = S[10 * NB + i]; sh.gamma = S[11 * NB + i]; sh.sigma = S[12 * NB + i];
-      bin_props<KT>(cc, phase_of(P, i), (KT)1.1 * b.diam, (KT)w.dwet[i], (KT)1.33 * b.mass, (KT)w.rhomean[i], sh, a);
+      const double *SH = shape_rows(w);
+      Shape<double> sh;
+      sh.alpha = SH[0 * NB + i]; sh.beta = SH[1 * NB + i]; sh.gamma = SH[2 * NB + i]; sh.sigma = SH[3 * NB + i];
+      const double dj = w.dwet[j], mj = w.rhomean[j] * K_PI6 * cube(w.dwet[j]);
+      BinProps<double> ad;
+      bin_props<double>(cd, phase_of(P, i), 1.1 * dj, w.dwet[i], 1.33 * mj, w.rhomean[i], sh, ad);
+      to_kt<KT>(ad, a);
     } else {
       load_props<KT>(S, NB, i, a);
     }
@@ -341,69 +366,91 @@ __device__ void eval_pairs(const DevParams &P, const WS<KT> &w, const CoagCell<K
 // ----------------------------------------------------------------------------------------
 // Collision kernels for all enabled bin pairs: mo_salsa_coagulation_kernels.f90:24-180
 // (buildKernelSelf/buildKernel: pairs whose partner has numc < nlim are zero).
-// Scratch: 0 diam 1 mass 2 beta 3 dfpart 4 mtvel 5 omega 6 termv 7 reyn 8 schm 9-12 shape
+// Scratch: 0 diam 1 mass 2 beta 3 dfpart 4 mtvel 5 omega 6 termv 7 reyn 8 schm, then
+// the FP64 shape coefficients (shape_rows).
 // ----------------------------------------------------------------------------------------
 template <typename KT>
 __device__ void build_kernels(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
                               int lane) {
   const int NB = w.NB;
-  const double *dmid = tb + TAB_DMID * P.nb_pad;
-  CoagCell<KT> cc;
+  CoagCell<double> cd;
   {
     double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
     double mfp = (1.656e-10 * T + 1.828e-8) * K_PSTAND / pres;
     double zrhoa = pres / (K_RD * T);
     double vkin = visc / zrhoa;
-    cc.T_ = (KT)T; cc.visc = (KT)visc; cc.mfp = (KT)mfp; cc.zrhoa = (KT)zrhoa; cc.vkin = (KT)vkin;
-    cc.shearA = (KT)sqrt(8. * K_PI * P.eddy_dis / (15. * vkin));
-    cc.turbB = (KT)(K_PI * pow(P.eddy_dis, 0.75) / (K_GRAV * sqrt(sqrt(vkin))));
+    cd.T_ = T; cd.visc = visc; cd.mfp = mfp; cd.zrhoa = zrhoa; cd.vkin = vkin;
+    cd.shearA = sqrt(8. * K_PI * P.eddy_dis / (15. * vkin));
+    cd.turbB = K_PI * pow(P.eddy_dis, 0.75) / (K_GRAV * sqrt(sqrt(vkin)));
   }
-  KT *S = reinterpret_cast<KT *>(w.scr);   // KT-typed scratch, 13 * NB entries
-  for (int b = lane; b < P.ntotal; b += 32) {
+  CoagCell<KT> cc;
+  cc.T_ = (KT)cd.T_; cc.visc = (KT)cd.visc; cc.mfp = (KT)cd.mfp; cc.zrhoa = (KT)cd.zrhoa; cc.vkin = (KT)cd.vkin;
+  cc.shearA = (KT)cd.shearA; cc.turbB = (KT)cd.turbB;
+  KT *S = reinterpret_cast<KT *>(w.scr);   // KT-typed scratch, 9 * NB entries
+  double *SH = shape_rows(w);
+  // per-bin properties of the populated bins only (a pair with an empty bin has K = 0)
+  const unsigned lt = (1u << lane) - 1u;
+  int nact = 0;
+  for (int base = 0; base < P.ntotal; base += 32) {
+    int b = base + lane;
+    bool act = b < P.ntotal && w.numc[b] >= nlim_of(phase_of(P, b));
+    unsigned bal = __ballot_sync(0xffffffffu, act);
+    if (act) w.pbuf[nact + __popc(bal & lt)] = b;
+    nact += __popc(bal);
+  }
+  __syncwarp();
+  for (int e = lane; e < nact; e += 32) {
+    const int b = w.pbuf[e];
     int ph = phase_of(P, b);
-    Shape<KT> sh;
+    Shape<double> sh;
     if (ph == 4) {
       double mp = 0.;
       for (int s = 0; s < P.nused - 1; s++) mp += w.v(s, b) * K_RHOIC;
-      shape_coeffs<KT>(P, sh, mp, w.v(P.nused - 1, b) * K_RHORI, w.numc[b]);
+      shape_coeffs<double>(P, sh, mp, w.v(P.nused - 1, b) * K_RHORI, w.numc[b]);
     } else {
-      sh.alpha = sh.beta = sh.gamma = sh.sigma = 0;
+      sh.alpha = sh.beta = sh.gamma = sh.sigma = 0.;
     }
     double diam = w.dwet[b];   // dnsp == dwet after a limited "all" update
     double mass = w.rhomean[b] * K_PI6 * cube(w.dwet[b]);
-    BinProps<KT> o;
-    bin_props<KT>(cc, ph, (KT)diam, (KT)w.dwet[b], (KT)mass, (KT)w.rhomean[b], sh, o);
-    S[0 * NB + b] = o.diam; S[1 * NB + b] = o.mass; S[2 * NB + b] = o.beta; S[3 * NB + b] = o.dfpart;
-    S[4 * NB + b] = o.mtvel; S[5 * NB + b] = o.omega; S[6 * NB + b] = o.termv; S[7 * NB + b] = o.reyn;
-    S[8 * NB + b] = o.schm;
-    S[9 * NB + b] = sh.alpha; S[10 * NB + b] = sh.beta; S[11 * NB + b] = sh.gamma; S[12 * NB + b] = sh.sigma;
+    BinProps<double> o;
+    bin_props<double>(cd, ph, diam, w.dwet[b], mass, w.rhomean[b], sh, o);
+    store_props<KT>(S, NB, b, o);
+    SH[0 * NB + b] = sh.alpha; SH[1 * NB + b] = sh.beta; SH[2 * NB + b] = sh.gamma; SH[3 * NB + b] = sh.sigma;
   }
   __syncwarp();
-  // scan the pair table; compact the active pairs into pbuf and evaluate them 32 at a time
-  int nbuf = 0;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int base = 0; base < P.npairs; base += 32) {
-    bool act = false;
-    int pk = 0;
-    int t = base + lane;
-    if (t < P.npairs) {
-      pk = __ldg(P.pairs + t);
-      int i = pk & 0xff, j = (pk >> 8) & 0xff;
-      act = w.numc[i] >= nlim_of(phase_of(P, i)) && w.numc[j] >= nlim_of(phase_of(P, j));
-      if (!act) w.K[tri(i, j, NB)] = (KT)0;
-    }
-    unsigned bal = __ballot_sync(0xffffffffu, act);
-    if (act) w.pbuf[nbuf + __popc(bal & lt)] = pk;
-    nbuf += __popc(bal);
-    __syncwarp();
-    if (nbuf >= 32) {
-      eval_pairs<KT>(P, w, cc, S, dmid, w.pbuf + nbuf - 32, 32, lane);
-      nbuf -= 32;
+  // Scan the pair table, compact the active pairs into pbuf and evaluate them 32 at a
+  // time.  The table lists the pairs of equal-size bins (self-coagulation offset) last,
+  // so those evaluate in batches of their own.
+  for (int sec = 0; sec < 2; sec++) {
+    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
+    int nbuf = 0;
+    for (int base = p0; base < p1; base += 32) {
+      bool act = false;
+      int pk = 0;
+      int t = base + lane;
+      if (t < p1) {
+        pk = __ldg(P.pairs + t);
+        int i = pk & 0xff, j = (pk >> 8) & 0xff;
+        act = w.numc[i] >= nlim_of(phase_of(P, i)) && w.numc[j] >= nlim_of(phase_of(P, j));
+        if (!act) w.K[tri(i, j, NB)] = (KT)0;
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (act) w.pbuf[nbuf + __popc(bal & lt)] = pk;
+      nbuf += __popc(bal);
       __syncwarp();
+      if (nbuf >= 32) {
+        if (sec == 0) eval_pairs<KT, false>(P, w, cc, cd, S, w.pbuf + nbuf - 32, 32, lane);
+        else eval_pairs<KT, true>(P, w, cc, cd, S, w.pbuf + nbuf - 32, 32, lane);
+        nbuf -= 32;
+        __syncwarp();
+      }
     }
+    if (nbuf > 0) {
+      if (sec == 0) eval_pairs<KT, false>(P, w, cc, cd, S, w.pbuf, nbuf, lane);
+      else eval_pairs<KT, true>(P, w, cc, cd, S, w.pbuf, nbuf, lane);
+    }
+    __syncwarp();
   }
-  if (nbuf > 0) eval_pairs<KT>(P, w, cc, S, dmid, w.pbuf, nbuf, lane);
-  __syncwarp();
 }
 
 
@@ -470,20 +517,10 @@ struct TAcc {
 #pragma unroll
       for (int d = 0; d < 7; d++) dg[d] = u[d + 1];
     } else {
-      self = warp_sum(self);
+      self = __shfl_sync(0xffffffffu, self, 0);   // self terms are accumulated on lane 0 only
     }
   }
 };
-
-template <typename KT>
-__device__ __forceinline__ void sink_range(const WS<KT> &w, int t, int g0, int istr, int iend, double xx, TAcc &a,
-                                           bool to_self, int lane) {
-  for (int ll = istr + lane; ll <= iend; ll += 32) {
-    int g = g0 + ll;
-    double d = xx * (double)kget(w, t, g) * w.numc[g];
-    if (to_self) a.self += d; else a.sink += d;
-  }
-}
 
 template <typename KT>
 __device__ __forceinline__ void source_range(const WS<KT> &w, int t, int g0, int istr, int iend, int nspec, TAcc &a,
@@ -497,103 +534,64 @@ __device__ __forceinline__ void source_range(const WS<KT> &w, int t, int g0, int
   }
 }
 
-// applyCoag (:539-559): lanes 0..nspec-1 update the volumes, then the number
+// Partner lists of target bin t (built by the host from the partner ranges of the
+// reference's accumulateSink / accumulateSource calls): header [4 t .. 4 t + 3] =
+// sink offset, sink count, source offset, source count; entries are global bin indices.
+__device__ __forceinline__ const int16_t *partner_lists(const DevParams &P, const double *tb) {
+  return reinterpret_cast<const int16_t *>(tb + P.list_off);
+}
+
+template <typename KT>
+__device__ __forceinline__ void list_sinks(const WS<KT> &w, const int16_t *L, int t, TAcc &a, int lane) {
+  const int off = L[4 * t], n = L[4 * t + 1];
+  for (int e = lane; e < n; e += 32) {
+    const int g = L[off + e];
+    a.sink += (double)kget(w, t, g) * w.numc[g];
+  }
+}
+
+template <typename KT>
+__device__ __forceinline__ void list_sources(const WS<KT> &w, const int16_t *L, int t, int nspec, TAcc &a, int lane) {
+  const int off = L[4 * t + 2], n = L[4 * t + 3];
+  for (int e = lane; e < n; e += 32) {
+    const int g = L[off + e];
+    const double k = (double)kget(w, g, t);
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++)
+      if (s < nspec) a.src[s] += k * w.v(s, g);
+  }
+}
+
+// applyCoag (:539-559): lanes 0..nspec-1 update the volumes and lane nspec the number,
+// all in one division.
 template <typename KT>
 __device__ __forceinline__ void apply_coag(const WS<KT> &w, int t, int nspec, double dt, const TAcc &a, int lane) {
   double my = 0.;
 #pragma unroll
   for (int s = 0; s < SALSA_NSV; s++)
     if (lane == s) my = a.src[s];
-  double n = w.numc[t];
-  if (lane < nspec) w.v(lane, t) = (w.v(lane, t) + dt * my * n) / (1. + dt * a.sink);
+  const double n = w.numc[t];
+  const bool vol = lane < nspec;
+  const double num = vol ? w.v(lane, t) + dt * my * n : n;
+  const double den = vol ? 1. + dt * a.sink : 1. + dt * (a.sink + a.self);
+  const double q = num / den;
   __syncwarp();
-  if (lane == 0) w.numc[t] = n / (1. + dt * (a.sink + a.self));
+  if (vol) w.v(lane, t) = q;
+  else if (lane == nspec) w.numc[t] = q;
   __syncwarp();
 }
 
 template <typename KT>
-__device__ void coag_aero(const DevParams &P, const WS<KT> &w, double dt, int lane) {
-  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid;
+__device__ void coag_aero(const DevParams &P, const WS<KT> &w, const double *tb, double dt, int lane) {
+  const int nspec = P.nwet;
+  const int16_t *L = partner_lists(P, tb);
   for (int kk = P.in1a; kk <= P.fn2b; kk++) {
     if (w.numc[kk] < K_NLIM) continue;
     TAcc a;
     a.zero();
-    int reg = kk <= P.fn1a ? 0 : (kk <= P.fn2a ? 1 : 2);
-    if (reg == 0) {
-      int icla = P.ica_cur + max(kk - P.ica_par, 0);
-      int iclb = P.icb_cur + (icla - P.ica_cur);
-      if (P.lscgaa) {
-        sink_range(w, kk, 0, kk + 1, P.fn2b, 1.0, a, false, lane);
-        sink_range(w, kk, 0, kk, kk, 0.5, a, true, lane);
-      }
-      if (P.lscgca) {
-        sink_range(w, kk, C0, icla, P.fca_cur, 1.0, a, false, lane);
-        sink_range(w, kk, C0, iclb, P.fcb_cur, 1.0, a, false, lane);
-      }
-      if (P.lscgpa) sink_range(w, kk, P0, 0, P.nprc - 1, 1.0, a, false, lane);
-      if (P.lscgia) sink_range(w, kk, I0, 0, P.nice - 1, 1.0, a, false, lane);
-      if (P.lscgaa && kk > P.in1a) source_range(w, kk, 0, P.in1a, kk - 1, nspec, a, lane);
-      if (P.lscgca) {
-        icla = P.ica_cur + (kk - P.ica_par) - 1;
-        iclb = P.icb_cur + (icla - P.ica_cur);
-        if (icla >= P.ica_cur) source_range(w, kk, C0, P.ica_cur, icla, nspec, a, lane);
-        if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
-      }
-    } else if (reg == 1) {
-      int index_b = P.in2b + (kk - P.in2a);
-      int icla = P.ica_cur + max(kk - P.ica_par, 0);
-      int iclb = P.icb_cur + max(kk - P.ica_par, 0);
-      if (P.lscgaa) {
-        if (kk < P.fn2a) {
-          sink_range(w, kk, 0, kk + 1, P.fn2a, 1.0, a, false, lane);
-          sink_range(w, kk, 0, index_b, P.fn2b, 1.0, a, false, lane);
-        }
-        sink_range(w, kk, 0, kk, kk, 0.5, a, true, lane);
-      }
-      if (P.lscgca) {
-        sink_range(w, kk, C0, icla, P.fca_cur, 1.0, a, false, lane);
-        sink_range(w, kk, C0, iclb, P.fcb_cur, 1.0, a, false, lane);
-      }
-      if (P.lscgpa) sink_range(w, kk, P0, 0, P.nprc - 1, 1.0, a, false, lane);
-      if (P.lscgia) sink_range(w, kk, I0, 0, P.nice - 1, 1.0, a, false, lane);
-      if (P.lscgaa) {
-        source_range(w, kk, 0, P.in1a, kk - 1, nspec, a, lane);
-        source_range(w, kk, 0, P.in2b, index_b, nspec, a, lane);
-      }
-      if (P.lscgca) {
-        icla = P.ica_cur + (kk - P.ica_par) - 1;
-        iclb = P.icb_cur + (icla - P.ica_cur);
-        if (icla >= P.ica_cur) source_range(w, kk, C0, P.ica_cur, icla, nspec, a, lane);
-        if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
-      }
-    } else {
-      int index_a = P.in2a + (kk - P.in2b);
-      int icla = P.ica_cur + max(kk - P.icb_par, 0);
-      int iclb = P.icb_cur + max(kk - P.icb_par, 0);
-      if (P.lscgaa) {
-        if (kk < P.fn2b) {
-          sink_range(w, kk, 0, kk + 1, P.fn2b, 1.0, a, false, lane);
-          sink_range(w, kk, 0, index_a, P.fn2a, 1.0, a, false, lane);
-        }
-        sink_range(w, kk, 0, kk, kk, 0.5, a, true, lane);
-      }
-      if (P.lscgca) {
-        sink_range(w, kk, C0, icla, P.fca_cur, 1.0, a, false, lane);
-        sink_range(w, kk, C0, iclb, P.fcb_cur, 1.0, a, false, lane);
-      }
-      if (P.lscgpa) sink_range(w, kk, P0, 0, P.nprc - 1, 1.0, a, false, lane);
-      if (P.lscgia) sink_range(w, kk, I0, 0, P.nice - 1, 1.0, a, false, lane);
-      if (P.lscgaa) {
-        source_range(w, kk, 0, P.in2b, kk - 1, nspec, a, lane);
-        source_range(w, kk, 0, P.in1a, index_a, nspec, a, lane);
-      }
-      if (P.lscgca) {
-        iclb = P.icb_cur + (kk - P.icb_par) - 1;
-        icla = P.ica_cur + (iclb - P.icb_cur);
-        if (icla >= P.ica_cur) source_range(w, kk, C0, P.ica_cur, icla, nspec, a, lane);
-        if (iclb >= P.icb_cur) source_range(w, kk, C0, P.icb_cur, iclb, nspec, a, lane);
-      }
-    }
+    if (P.lscgaa && lane == 0) a.self = 0.5 * (double)kget(w, kk, kk) * w.numc[kk];
+    list_sinks(w, L, kk, a, lane);
+    list_sources(w, L, kk, nspec, a, lane);
     a.reduce(false, lane);
     apply_coag(w, kk, nspec, dt, a, lane);
   }
@@ -678,8 +676,9 @@ __device__ void precip_formation(const DevParams &P, const WS<KT> &w, const doub
 
 template <typename KT>
 __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb, double dt, bool diag, int lane) {
-  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid, nprc = P.nprc;
+  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, nprc = P.nprc;
   const bool autoc1 = P.st_auto && P.auto_mode == 1;
+  const int16_t *L = partner_lists(P, tb);
   double *pf = w.misc + M_PF;
   for (int reg = 0; reg < 2; reg++) {
     int kfirst = reg == 0 ? P.ica_cur : P.icb_cur;
@@ -697,26 +696,16 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
       }
       int other = o_first + (kk - kfirst);
       int rel = kk - kfirst;
-      if (P.lscgca && kk < klast) {
-        int iaa = P.ica_par + rel + 1, iab = P.icb_par + rel + 1;
-        for (int ll = iaa + lane; ll <= P.fn2a; ll += 32) a.sink += (double)kget(w, ll, tg) * w.numc[ll];
-        for (int ll = iab + lane; ll <= P.fn2b; ll += 32) a.sink += (double)kget(w, ll, tg) * w.numc[ll];
-      }
+      list_sinks(w, L, tg, a, lane);
       if (P.lscgcc) {
-        if (kk < klast) {
-          sink_range(w, tg, C0, kk + 1, klast, 1.0, a, false, lane);
-          sink_range(w, tg, C0, other, o_last, 1.0, a, false, lane);
-        }
         if (autoc1) {
           double n = w.numc[tg];
           double fix = fmax(1. - dt * (0.5 * (double)kget(w, tg, tg) * (n * n) / n), 0.1);
           precip_formation(P, w, tb, kk, kk, kk, fix, true, a, diag, lane);
-        } else {
-          sink_range(w, tg, C0, kk, kk, 0.5, a, true, lane);
+        } else if (lane == 0) {
+          a.self += 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
         }
       }
-      if (P.lscgpc) sink_range(w, tg, P0, 0, nprc - 1, 1.0, a, false, lane);
-      if (P.lscgic) sink_range(w, tg, I0, 0, P.nice - 1, 1.0, a, false, lane);
       if (P.lscgca) {
         int iaa = P.ica_par + rel, iab = P.icb_par + rel;
         double cm = 0.;
@@ -783,19 +772,17 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
 
 template <typename KT>
 __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb, double dt, bool diag, int lane) {
-  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid, nprc = P.nprc, iwa = P.iwa;
+  const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, nprc = P.nprc, iwa = P.iwa;
   const double *pbins = tb + TAB_PRECPBINS * P.nb_pad;
+  const int16_t *L = partner_lists(P, tb);
   for (int kk = 0; kk < nprc; kk++) {
     int tg = P0 + kk;
     if (w.numc[tg] < K_PRLIM) continue;
     TAcc a;
     a.zero();
     double num_slf = 0.;
-    if (P.lscgpp) {
-      if (kk < nprc - 1) sink_range(w, tg, P0, kk + 1, nprc - 1, 1.0, a, false, lane);
-      else sink_range(w, tg, P0, kk, kk, 0.5, a, true, lane);
-    }
-    if (P.lscgip) sink_range(w, tg, I0, 0, P.nice - 1, 1.0, a, false, lane);
+    list_sinks(w, L, tg, a, lane);
+    if (P.lscgpp && kk == nprc - 1 && lane == 0) a.self += 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
     const double D = w.dwet[tg];
     if (P.lscgpa) {
       double cm = 0.;
@@ -960,7 +947,7 @@ __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *t
   bool any_ice = P.lscgii || P.lscgia || P.lscgic || P.lscgip;
   if (any_ice && T < 273.15) coag_ice<KT>(P, w, dt, lane);
   if (any_precp) coag_precp<KT>(P, w, tb, dt, diag, lane);
-  if (any_aero) coag_aero<KT>(P, w, dt, lane);
+  if (any_aero) coag_aero<KT>(P, w, tb, dt, lane);
   if (any_cloud) coag_cloud<KT>(P, w, tb, dt, diag, lane);
   bool neg = false;
   for (int b = lane; b < P.ntotal; b += 32) {
@@ -1596,6 +1583,11 @@ __device__ void ice_apply_staged(const DevParams &P, const WS<KT> &w, const doub
   __syncwarp();
 }
 
+// SE ice nucleation (mo_salsa_SecondaryIce / iceNucleation, :394-538).  Pass A (lanes
+// over liquid bins) evaluates the per-bin quantities and decides which bins need the
+// Gauss-Legendre integral over contact angles; pass B evaluates the integrands with one
+// lane per (bin, node), three bins per warp pass, and sums each bin's ten terms in node
+// order; pass C (lanes over bins) applies the frozen fractions.
 template <typename KT>
 __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *tb, double T, double prv, double prs,
                             double prsi, double dt, double kappa, bool diag, int lane) {
@@ -1603,64 +1595,112 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
   const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad;
   const double dmin = 1.e-10, tmax_homog = 237.9, minVin = K_PI6 * cube(1.e-8);
   const int nl = P.nliquid, ndry = P.ndry, iwa = P.iwa, irim = P.irim, idu = P.ix_du;
+  const unsigned F = 0xffffffffu;
   double *stage = w.scr;   // nl * 10 doubles
-  double dh = 0., dd = 0., di = 0.;
+  // per-bin records in the (now unused) collision-kernel area: 8 doubles per bin
+  double *rec = reinterpret_cast<double *>(w.K);
+  enum { R_MODE = 0, R_THMIN, R_DIN, R_AE, R_SIG, R_DG, R_FHOM, R_FINT };
+  const double Si = prv / prsi;
+  // pass A
   for (int kk = lane; kk < nl; kk += 32) {
     double *st = stage + kk * 10;
     for (int q = 0; q < 10; q++) st[q] = 0.;
     st[0] = -1.;
-    double Seq = calc_sweq(P, w, kk, T, kappa);
-    double Si = prv / prsi;
+    double *r = rec + kk * 8;
     updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, kk);
-    double dwet = w.dwet[kk], dins_ = w.ddry[kk];
-    double n = w.numc[kk];
-    int ph = phase_of(P, kk);
-    double f_hom = 0., f_imm = 0., f_dep = 0.;
-    if (dwet - dins_ > dmin && T < tmax_homog && P.lsicehom) {
+    const double dwet = w.dwet[kk], dins_ = w.ddry[kk];
+    const double n = w.numc[kk];
+    const int ph = phase_of(P, kk);
+    const bool countable = !(T > 273.15) && !(n < nlim_of(ph));
+    const bool hom = dwet - dins_ > dmin && T < tmax_homog && P.lsicehom;
+    const bool imm = P.lsiceimm && (ph == 2 || ph == 3) && (w.dins[kk] > dmin) && countable;
+    const bool dep = P.lsicedep && (ph == 1 && prv / prs < 1.0) && (w.dwet[kk] - w.dins[kk] < dmin) &&
+                     (w.dins[kk] > dmin) && countable;
+    double Seq = 0.;
+    if (hom || imm) Seq = calc_sweq(P, w, kk, T, kappa);
+    double f_hom = 0.;
+    if (hom) {
       double Jh = J_hf(T, Seq);
       f_hom = 1. - exp(-Jh * K_PI6 * (cube(dwet) - cube(dins_)) * dt);
     }
-    bool countable = !(T > 273.15) && !(n < nlim_of(ph));
-    if (P.lsiceimm) {
+    r[R_FHOM] = f_hom;
+    r[R_MODE] = imm ? 1. : (dep ? 2. : 0.);
+    r[R_DIN] = w.ddry[kk];
+    if (imm) {
       // low_theta (:394-417)
       double th00 = P.mean_theta_imm + sqrt(2.) * P.sigma_theta_imm * erfm1(2. * w.indef[kk] - 1.);
       th00 = fmin(fmax(th00, 0.), 180.);
       if (!P.st_freeTheta) th00 = fmax(P.initMinTheta, th00);
-      bool mask = (ph == 2 || ph == 3) && (w.dins[kk] > dmin);
-      if (mask && countable) {
-        // gauss_legendre (:131-206), mode 1
-        double thmin = th00, thmax = 180., acc = 0.;
-        double din = w.ddry[kk];
-        JimmPre q = jimm_pre(T, Seq);
-        for (int i = 0; i < 10; i++) {
-          double th1 = 0.5 * (thmax - thmin) * c_gl_x[i] + 0.5 * (thmax + thmin);
-          double J = J_imm(q, th1, T, din);
-          double ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_imm, P.mean_theta_imm) : 0.;
-          acc = acc + ft * c_gl_w[i] * (1. - exp(-J * dt));
-        }
-        f_imm = 0.5 * (thmax - thmin) * acc;
-      }
-    }
-    if (P.lsicedep) {
+      JimmPre q = jimm_pre(T, Seq);
+      r[R_THMIN] = th00; r[R_AE] = q.act_energy; r[R_SIG] = q.sigma_is; r[R_DG] = q.ok ? q.d_g : -1.;
+    } else if (dep) {
       double th00 = P.mean_theta_dep + sqrt(2.) * P.sigma_theta_dep * erfm1(2. * w.indef[kk] - 1.);
       th00 = fmin(fmax(th00, 0.), 180.);
       if (!P.st_freeTheta) th00 = fmax(P.initMinTheta, th00);
-      bool mask = (ph == 1 && prv / prs < 1.0) && (w.dwet[kk] - w.dins[kk] < dmin) && (w.dins[kk] > dmin);
-      if (mask && countable) {
-        double thmin = th00, thmax = 180., acc = 0.;
-        double din = w.ddry[kk];
-        for (int i = 0; i < 10; i++) {
-          double th1 = 0.5 * (thmax - thmin) * c_gl_x[i] + 0.5 * (thmax + thmin);
-          double J = J_dep(th1, T, din, Si);
-          double ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_dep, P.mean_theta_dep) : 0.;
-          acc = acc + ft * c_gl_w[i] * (1. - exp(-J * dt));
+      r[R_THMIN] = th00;
+    }
+    r[R_FINT] = 0.;
+  }
+  __syncwarp();
+  // pass B: gauss_legendre (:131-206) for the bins that need it
+  {
+    const unsigned lt = (1u << lane) - 1u;
+    int nlist = 0;
+    int *list = w.pbuf;
+    for (int base = 0; base < nl; base += 32) {
+      int kk = base + lane;
+      bool need = kk < nl && rec[kk * 8 + R_MODE] != 0.;
+      unsigned bal = __ballot_sync(F, need);
+      if (need) list[nlist + __popc(bal & lt)] = kk;
+      nlist += __popc(bal);
+    }
+    __syncwarp();
+    const int grp = lane / 10, node = lane - grp * 10;
+    for (int b0 = 0; b0 < nlist; b0 += 3) {
+      const int slot = b0 + grp;
+      const bool on = grp < 3 && slot < nlist;
+      const int kk = on ? list[slot] : 0;
+      double term = 0.;
+      if (on) {
+        const double *r = rec + kk * 8;
+        const double thmin = r[R_THMIN], thmax = 180.;
+        const double th1 = 0.5 * (thmax - thmin) * c_gl_x[node] + 0.5 * (thmax + thmin);
+        double J, ft;
+        if (r[R_MODE] == 1.) {
+          JimmPre q;
+          q.act_energy = r[R_AE]; q.sigma_is = r[R_SIG]; q.d_g = r[R_DG]; q.ok = r[R_DG] >= 0.;
+          J = J_imm(q, th1, T, r[R_DIN]);
+          ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_imm, P.mean_theta_imm) : 0.;
+        } else {
+          J = J_dep(th1, T, r[R_DIN], Si);
+          ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_dep, P.mean_theta_dep) : 0.;
         }
-        f_dep = 0.5 * (thmax - thmin) * acc;
+        term = ft * c_gl_w[node] * (1. - exp(-J * dt));
+      }
+      double acc = 0.;
+      const int g10 = (grp < 3 ? grp : 0) * 10;
+#pragma unroll
+      for (int i = 0; i < 10; i++) acc = acc + __shfl_sync(F, term, g10 + i);
+      if (on && node == 0) {
+        double *r = rec + kk * 8;
+        r[R_FINT] = 0.5 * (180. - r[R_THMIN]) * acc;
       }
     }
+    __syncwarp();
+  }
+  // pass C: iceNucleation (:421-538)
+  double dh = 0., dd = 0., di = 0.;
+  for (int kk = lane; kk < nl; kk += 32) {
+    double *st = stage + kk * 10;
+    const double *r = rec + kk * 8;
+    const double dwet = w.dwet[kk];
+    const double n = w.numc[kk];
+    const int ph = phase_of(P, kk);
+    const double f_hom = r[R_FHOM];
+    const double f_imm = r[R_MODE] == 1. ? r[R_FINT] : 0.;
+    const double f_dep = r[R_MODE] == 2. ? r[R_FINT] : 0.;
     dh += n * f_hom; dd += n * f_dep; di += n * f_imm;
     double frac = fmax(0., fmin(0.99, f_imm + f_hom + f_dep - (f_imm + f_dep) * f_hom));
-    // iceNucleation (:421-538)
     if (n < nlim_of(ph)) continue;
     double vins = 0.;
     for (int k = 0; k < P.ninsoluble; k++) vins += w.v(P.ind_insoluble[k], kk);
@@ -2270,7 +2310,7 @@ __device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
   w.ctime = p; p += NB;
   w.scr = p; p += SALSA_NSCR * NB;
   w.misc = p; p += SALSA_MISC_DOUBLES;
-  w.pbuf = reinterpret_cast<int *>(p); p += 32;
+  w.pbuf = reinterpret_cast<int *>(p); p += 64;   // 128 ints: bin lists (<= 96) and pair batches (<= 63)
   w.K = reinterpret_cast<KT *>(p);
   return w;
 }
