@@ -1008,13 +1008,101 @@ __device__ double equil_iterate(const DevParams &P, const WS<KT> &w, int b, doub
   return zlwc;
 }
 
+// State of one fixed-point solve of equil_iterate, advanced one iteration at a time so
+// that the regime-1a chain (sequential: zke carries from bin to bin) runs on its own lane
+// next to the independent regime-2 solves.
+struct EqJob {
+  int kk, count;
+  bool r2;
+  double tol, zrh, zke, numc, zv0, zv1, zv4, zvp56, zcore, zdwet, zdold, zlwc;
+};
+
+template <typename KT>
+__device__ __forceinline__ void eq_load(const DevParams &P, const WS<KT> &w, int b, EqJob &j) {
+  j.kk = b;
+  j.count = 0;
+  j.numc = w.numc[b];
+  j.zv0 = zvolc_of(P, w, 0, b); j.zv1 = zvolc_of(P, w, 1, b); j.zv4 = zvolc_of(P, w, 4, b);
+  double zvp[7];
+  for (int i = 0; i < 7; i++) zvp[i] = zvolc_of(P, w, i, b) / j.numc;
+  j.zcore = j.r2 ? (zvp[0] + zvp[1] + zvp[2] + zvp[3] + zvp[4]) : (zvp[0] + zvp[1]);
+  j.zvp56 = zvp[5] + zvp[6];
+  j.zdwet = w.dwet[b];
+  j.zdold = 1.;
+  j.zlwc = 0.;
+}
+
+// one pass of the equil_iterate loop body (same operations in the same order)
+__device__ __forceinline__ void eq_step(EqJob &j, double T) {
+  const double rhosu_msu = 1830. / 98.08e-3, rhooc_moc = 1400. / 150.e-3, rhoss_mss = 2165. / 58.44e-3;
+  j.zdold = fmax(j.zdwet, 1.e-20);
+  double zaw = j.zrh / j.zke;
+  double a2 = zaw * zaw, a3 = a2 * zaw, a4 = a2 * a2;
+  double bm1 = +1.1065495e+2 - 3.6759197e+2 * zaw + 5.0462934e+2 * a2 - 3.1543839e+2 * a3 + 6.770824e+1 * a4;
+  double bm2 = 1. / (zaw * K_MWA) - 1. / K_MWA;
+  double zlwc = (j.zv0 * rhosu_msu) / bm1 + K_EPSOC * j.zv1 * rhooc_moc / bm2;
+  if (j.r2) {
+    double bm5 = +5.875248e+1 - 1.8781997e+2 * zaw + 2.7211377e+2 * a2 - 1.8458287e+2 * a3 + 4.153689e+1 * a4;
+    zlwc += (j.zv4 * rhoss_mss) / bm5;
+  }
+  j.zlwc = zlwc;
+  j.zdwet = cbrt(zlwc / j.numc / K_RHOWA / K_PI6 + j.zvp56 / K_PI6 + j.zcore / K_PI6);
+  j.zke = exp(2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T * j.zdwet));
+  j.count++;
+}
+
+// next regime-1a bin after b with numc > nlim; empty bins take dmid when initialising
+template <typename KT>
+__device__ __forceinline__ int eq_next_1a(const DevParams &P, const WS<KT> &w, const double *dmid, int b, bool init) {
+  for (int k = b + 1; k <= P.fn1a; k++) {
+    if (w.numc[k] > K_NLIM) return k;
+    if (init) w.dwet[k] = dmid[k];
+  }
+  return -1;
+}
+
 template <typename KT>
 __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
                               int lane) {
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   int nonconv = 0;
-  // regime 1a, in bin order (all lanes run it; lane 0 writes)
-  {
+  const int n2 = init ? P.fn2b - P.in2a + 1 : 0;
+  if (n2 <= 31) {
+    // lane 31: the regime-1a chain in bin order; lanes 0..n2-1: regime-2 bins
+    EqJob j;
+    j.kk = -1;
+    if (lane == 31) {
+      j.r2 = false; j.tol = 1.e-2; j.zrh = fmin(fmax(prh, 0.05), 0.98); j.zke = 1.001;
+      int k = eq_next_1a(P, w, dmid, P.in1a - 1, init);
+      if (k >= 0) eq_load(P, w, k, j);
+    } else if (lane < n2) {
+      int k = P.in2a + lane;
+      if (w.numc[k] > K_NLIM) {
+        j.r2 = true; j.tol = 1.e-12; j.zrh = fmin(fmax(prh, 0.37), 0.98); j.zke = 1.02;
+        eq_load(P, w, k, j);
+      } else {
+        w.dwet[k] = dmid[k];
+      }
+    }
+    while (__any_sync(0xffffffffu, j.kk >= 0)) {
+      if (j.kk >= 0) {
+        bool go = fabs(j.zdwet / j.zdold - 1.) > j.tol;
+        if (go) {
+          eq_step(j, T);
+          if (j.count > 100) { nonconv = 1; go = false; }
+        }
+        if (!go) {
+          w.v(P.iwa, j.kk) = j.zlwc / K_RHOWA;
+          if (init) w.dwet[j.kk] = j.zdwet;
+          int k = j.r2 ? -1 : eq_next_1a(P, w, dmid, j.kk, init);
+          if (k >= 0) eq_load(P, w, k, j);
+          else j.kk = -1;
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // regime 1a, in bin order (all lanes run it; lane 0 writes)
     double zke = 1.001;
     for (int kk = P.in1a; kk <= P.fn1a; kk++) {
       if (w.numc[kk] > K_NLIM) {
@@ -1031,8 +1119,6 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
       }
       __syncwarp();
     }
-  }
-  if (init) {
     for (int kk = P.in2a + lane; kk <= P.fn2b; kk += 32) {
       if (w.numc[kk] > K_NLIM) {
         double zke = 1.02;
@@ -2181,27 +2267,29 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
     int icat = phase_of(P, b) - 1;
     w.dwet[b] = dmid[b];
     w.ddry[b] = w.dins[b] = w.dnsp[b] = 0.;
-    if (icat == 3 && P.level < 5) {
-      w.numc[b] = 0.;
-      for (int s = 0; s < SALSA_NSV; s++) w.v(s, b) = 0.;
-      w.rhomean[b] = 0.;
-      w.indef[b] = 0.;
-      w.ctime[b] = 0.;
-      continue;
-    }
-    int nbloc = b - bstart[icat], nbc = bnum[icat];
-    const double *rm = raw + P.raw_mbase[icat];
     for (int s = 0; s < SALSA_NSV; s++) w.v(s, b) = 0.;
-    if (icat < 3) {
-      for (int s = 0; s < nwet; s++) w.v(s, b) = rm[s * nbc + nbloc] * dn / P.rholiq[s];
-    } else {
-      for (int s = 0; s < nwet; s++) w.v(s, b) = rm[s * nbc + nbloc] * dn / P.rhoice[s];
-      w.v(irim, b) = rm[irim * nbc + nbloc] * dn / K_RHORI;
-    }
-    w.numc[b] = raw[P.raw_num + b] * dn;
-    w.indef[b] = (icat < 3 && P.raw_indef >= 0) ? raw[P.raw_indef + b] : 0.;
-    w.ctime[b] = (icat < 3 && P.raw_charge >= 0) ? raw[P.raw_charge + b] : 0.;
-    w.rhomean[b] = rhomean_of(P, icat + 1, w.numc[b], w.v(P.iwa, b), w.v(irim, b));
+    const bool absent = icat == 3 && P.level < 5;
+    w.numc[b] = absent ? 0. : raw[P.raw_num + b] * dn;
+    w.indef[b] = (!absent && icat < 3 && P.raw_indef >= 0) ? raw[P.raw_indef + b] : 0.;
+    w.ctime[b] = (!absent && icat < 3 && P.raw_charge >= 0) ? raw[P.raw_charge + b] : 0.;
+  }
+  __syncwarp();
+  // mass rows of all categories, one lane per (category, species, bin) row
+  const int ncat = P.level == 5 ? 4 : 3;
+  const int m0 = P.raw_mbase[0];
+  const int nmrow = (ncat == 4 ? P.raw_mbase[3] + (nwet + 1) * P.nice : P.raw_mbase[2] + nwet * P.nprc) - m0;
+  for (int e = lane; e < nmrow; e += 32) {
+    const int r = m0 + e;
+    const int icat = (ncat == 4 && r >= P.raw_mbase[3]) ? 3 : (r >= P.raw_mbase[2] ? 2 : (r >= P.raw_mbase[1] ? 1 : 0));
+    const int loc = r - P.raw_mbase[icat], nbc = bnum[icat];
+    const int sp = loc / nbc, b = bstart[icat] + (loc - sp * nbc);
+    const double rho = icat < 3 ? P.rholiq[sp] : (sp < nwet ? P.rhoice[sp] : K_RHORI);
+    w.v(sp, b) = raw[r] * dn / rho;
+  }
+  __syncwarp();
+  for (int b = lane; b < P.ntotal; b += 32) {
+    int icat = phase_of(P, b) - 1;
+    w.rhomean[b] = (icat == 3 && P.level < 5) ? 0. : rhomean_of(P, icat + 1, w.numc[b], w.v(P.iwa, b), w.v(irim, b));
   }
   for (int i = lane; i < M_PF; i += 32) w.misc[i] = 0.;
   __syncwarp();
@@ -2228,25 +2316,20 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
 
   // ---- tendencies and outputs (mo_salsa_driver.f90:310-419) into the raw slots ----
   bool bad = false;
+  for (int e = lane; e < nmrow; e += 32) {
+    const int r = m0 + e;
+    const int icat = (ncat == 4 && r >= P.raw_mbase[3]) ? 3 : (r >= P.raw_mbase[2] ? 2 : (r >= P.raw_mbase[1] ? 1 : 0));
+    const int loc = r - P.raw_mbase[icat], nbc = bnum[icat];
+    const int sp = loc / nbc, b = bstart[icat] + (loc - sp * nbc);
+    const double rho = icat < 3 ? P.rholiq[sp] : (sp < nwet ? P.rhoice[sp] : K_RHORI);
+    raw[r] = ((w.v(sp, b) * rho / dn) - raw[r]) / dt;
+  }
   for (int b = lane; b < P.ntotal; b += 32) {
     int icat = phase_of(P, b) - 1;
     if (icat == 3 && P.level < 5) continue;
-    int nbloc = b - bstart[icat], nbc = bnum[icat];
-    double *rm = raw + P.raw_mbase[icat];
     if (icat < 3) {
-      for (int s = 0; s < nwet; s++) {
-        double *o = rm + s * nbc + nbloc;
-        *o = ((w.v(s, b) * P.rholiq[s] / dn) - *o) / dt;
-      }
       if (P.raw_indef >= 0) raw[P.raw_indef + b] = w.indef[b];
       if (P.raw_charge >= 0) raw[P.raw_charge + b] = w.ctime[b];
-    } else {
-      for (int s = 0; s < nwet; s++) {
-        double *o = rm + s * nbc + nbloc;
-        *o = ((w.v(s, b) * P.rhoice[s] / dn) - *o) / dt;
-      }
-      double *o = rm + irim * nbc + nbloc;
-      *o = ((w.v(irim, b) * K_RHORI / dn) - *o) / dt;
     }
     double *on = raw + P.raw_num + b;
     *on = ((w.numc[b] / dn) - *on) / dt;
@@ -2322,7 +2405,7 @@ __device__ __forceinline__ long long cell_offset(const DevParams &P, long long q
 }
 
 template <typename KT, bool DIAG>
-__global__ void __launch_bounds__(SALSA_THREADS) salsa_step_kernel(const DevParams P) {
+__global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevParams P) {
   extern __shared__ double smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   double *tb = smem;
