@@ -126,6 +126,7 @@ def run_gb300(args):
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         kms = []
+        nlaunch = 0
         sampler = ClockSampler(local) if form == 0 else None
         if sampler:
             sampler.__enter__()
@@ -135,6 +136,7 @@ def run_gb300(args):
             for _ in range(args.steps):
                 step.run(inp, fields, outs, time=1.0, stream=stream)
                 kms.append(step.last_kernel_ms())
+                nlaunch += step.last_launches()
             e1.record(stream)
         barrier()
         if sampler:
@@ -144,7 +146,7 @@ def run_gb300(args):
         t = torch.tensor([ms], device=dev)
         if world > 1:
             tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        results[form] = dict(ms_total=float(t.item()), kernel_ms=sum(kms) / len(kms), launches=args.steps)
+        results[form] = dict(ms_total=float(t.item()), kernel_ms=sum(kms) / len(kms), launches=nlaunch)
         step.close()
         del fields, outs
         torch.cuda.empty_cache()
@@ -210,7 +212,7 @@ def run_gb300(args):
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_cell": bytes_cell},
-        "gpu_launches": args.steps,
+        "gpu_launches": r0["launches"],
         "clocks": results.get("clocks"),
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -284,7 +286,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="grid256x256x128")
-    ap.add_argument("--cpu-sample-cells", type=int, default=524288)
+    ap.add_argument("--cpu-sample-cells", type=int, default=3145728)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

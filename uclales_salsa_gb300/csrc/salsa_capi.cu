@@ -33,6 +33,48 @@ int blocks_per_sm_f1(const DevParams &);
 using salsa::DevParams;
 using salsa::Row;
 
+// Cell order of one step: cells whose cloud, precipitation and ice bins are all below
+// the population limits fill the list from the front, the others from the back, so
+// that the four cells of a block (which meet at barriers) take the same code path.
+// Each warp claims its slots with one atomic per class; the order of the claims does
+// not affect any result, since every cell is computed independently.
+__global__ void salsa_order_kernel(const DevParams P, int *order) {
+  const unsigned F = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < P.ncells; base += stride) {
+    const long long q = base + threadIdx.x;
+    const bool act = q < P.ncells;
+    bool cloudy = false;
+    if (act) {
+      const long long off = salsa::cell_offset(P, q);
+      const double dn = __ldg(P.fin[salsa::FI_DN] + off);
+      const int cat[3] = {salsa::FI_NCLOUD, salsa::FI_NPRECP, salsa::FI_NICE};
+      const int nbc[3] = {P.ncld, P.nprc, P.level == 5 ? P.nice : 0};
+      const double lim[3] = {K_NLIM, K_PRLIM, K_PRLIM};
+      for (int c = 0; c < 3 && !cloudy; c++) {
+        const double *f = P.fin[cat[c]];
+        if (!f) continue;
+        for (int b = 0; b < nbc[c]; b++)
+          if (__ldg(f + off + P.plane * b) * dn >= lim[c]) { cloudy = true; break; }
+      }
+    }
+    const unsigned mc = __ballot_sync(F, act && cloudy), ma = __ballot_sync(F, act && !cloudy);
+    unsigned long long b0 = 0, b1 = 0;
+    if (lane == 0) {
+      if (ma) b0 = atomicAdd(P.status + salsa::ST_ORDER_CLEAR, (unsigned long long)__popc(ma));
+      if (mc) b1 = atomicAdd(P.status + salsa::ST_ORDER_CLOUDY, (unsigned long long)__popc(mc));
+    }
+    b0 = __shfl_sync(F, b0, 0);
+    b1 = __shfl_sync(F, b1, 0);
+    const unsigned lt = (1u << lane) - 1u;
+    if (act) {
+      if (cloudy) order[P.ncells - 1 - (long long)(b1 + __popc(mc & lt))] = (int)q;
+      else order[b0 + __popc(ma & lt)] = (int)q;
+    }
+  }
+}
+
 namespace {
 
 const double PI6 = 0.5235988;   // mo_submctl.f90:266
@@ -85,6 +127,8 @@ struct salsa_handle {
   // staging buffers for host-pointer calls
   void *stage = nullptr;
   size_t stage_bytes = 0;
+  int *d_order = nullptr;       // cell order list (salsa_order_kernel)
+  long long order_cap = 0;
   int last_launches = 0;
   double last_kernel_ms = 0.;
   unsigned long long *d_stage = nullptr;   // instrumented builds only
@@ -476,6 +520,7 @@ void salsa_gb300_finalize(salsa_handle_t *h) {
   if (h->d_tables) cudaFree(h->d_tables);
   if (h->d_rows) cudaFree(h->d_rows);
   if (h->d_pairs) cudaFree(h->d_pairs);
+  if (h->d_order) cudaFree(h->d_order);
   if (h->d_status) cudaFree(h->d_status);
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->stage) cudaFree(h->stage);
@@ -663,12 +708,31 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     if (bps <= 0) return SALSA_E_CUDA;
     long long grid = (long long)bps * h->nsm * 8;
     if (grid > P.ngroups) grid = P.ngroups;
+    if (P.ncells <= 0x7fffffffLL) {
+      if (P.ncells > h->order_cap) {
+        if (h->d_order) cudaFree(h->d_order);
+        h->d_order = nullptr;
+        h->order_cap = 0;
+        if (cudaMalloc(&h->d_order, (size_t)P.ncells * sizeof(int)) != cudaSuccess) return SALSA_E_CUDA;
+        h->order_cap = P.ncells;
+      }
+      P.order = h->d_order;
+    } else {
+      P.order = nullptr;
+    }
     cudaEventRecord(h->ev0, s);
+    if (P.order) {
+      long long og = (P.ncells + 255) / 256;
+      if (og > (long long)h->nsm * 16) og = (long long)h->nsm * 16;
+      salsa_order_kernel<<<(int)og, 256, 0, s>>>(P, h->d_order);
+      if (cudaGetLastError() != cudaSuccess) return SALSA_E_CUDA;
+      launches++;
+    }
     cudaError_t e = prec == 0 ? (dg ? salsa::launch_d1(P, s, (int)grid) : salsa::launch_d0(P, s, (int)grid))
                               : (dg ? salsa::launch_f1(P, s, (int)grid) : salsa::launch_f0(P, s, (int)grid));
     cudaEventRecord(h->ev1, s);
     if (e != cudaSuccess) return SALSA_E_CUDA;
-    launches = 1;
+    launches++;
     if (cudaMemcpyAsync(h->h_status, h->d_status, salsa::ST_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) !=
         cudaSuccess)
       return SALSA_E_CUDA;

@@ -65,7 +65,9 @@ enum {
 };
 
 // status counters
-enum { ST_CELLS = 0, ST_EQUIL, ST_DISTR, ST_NEGFRAC, ST_COND, ST_NEG, ST_NONFINITE, ST_N };
+enum { ST_CELLS = 0, ST_EQUIL, ST_DISTR, ST_NEGFRAC, ST_COND, ST_NEG, ST_NONFINITE,
+       ST_ORDER_CLEAR, ST_ORDER_CLOUDY,   // fill counters of the cell order list
+       ST_N };
 
 struct Row {
   int16_t fin;     // input field id or -1
@@ -112,6 +114,7 @@ struct DevParams {
   const double *tables;     // bin tables (see TAB_* offsets)
   const int *pairs;         // packed pair list (i | j << 8)
   unsigned long long *status;
+  const int *order;         // processing order of the cells (clear cells first), or null
   unsigned long long *stage_clocks;   // per-stage clock sums (instrumented builds only)
 };
 
@@ -134,5 +137,13 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 __device__ __forceinline__ int warp_any(bool b) { return __any_sync(0xffffffffu, b); }
+
+// offset of interior cell q (z fastest, then x, then y) inside a (nyp, nxp, nzp) plane
+__device__ __forceinline__ long long cell_offset(const DevParams &P, long long q) {
+  long long kq = q % P.nz_int, r = q / P.nz_int;
+  long long iq = r % P.nx_int, jq = r / P.nx_int;
+  return (1 + kq) + (long long)P.nzp * ((2 + iq) + (long long)P.nxp * (2 + jq));
+}
+__device__ __forceinline__ long long cell_at(const DevParams &P, long long i) { return P.order ? P.order[i] : i; }
 
 }  // namespace salsa

@@ -2398,11 +2398,6 @@ __device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
   return w;
 }
 
-__device__ __forceinline__ long long cell_offset(const DevParams &P, long long q) {
-  long long kq = q % P.nz_int, r = q / P.nz_int;
-  long long iq = r % P.nx_int, jq = r / P.nx_int;
-  return (1 + kq) + (long long)P.nzp * ((2 + iq) + (long long)P.nxp * (2 + jq));
-}
 
 template <typename KT, bool DIAG>
 __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevParams P) {
@@ -2414,37 +2409,37 @@ __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevP
   WS<KT> w = make_ws<KT>(P, wsbase + (size_t)warp * P.ws_doubles);
   __syncthreads();
   for (long long g = blockIdx.x; g < P.ngroups; g += gridDim.x) {
-    // stage the group's input rows: consecutive threads read consecutive cells of one row
-    for (int e = tid; e < P.nrows * SALSA_CPG; e += SALSA_THREADS) {
-      int r = e / SALSA_CPG, c = e % SALSA_CPG;
-      long long q = g * SALSA_CPG + c;
-      if (q >= P.ncells) continue;
-      Row row = P.rows[r];
-      double v = 0.;
-      if (row.fin >= 0) {
-        const double *f = P.fin[row.fin];
-        if (f) v = __ldg(f + cell_offset(P, q) + P.plane * row.idx);
+    // stage the group's input rows: consecutive threads read the group's cells of one row
+    const int c = tid % SALSA_CPG;
+    const long long qc = g * SALSA_CPG + c;
+    const bool okc = qc < P.ncells;
+    const long long offc = okc ? cell_offset(P, cell_at(P, qc)) : 0;
+    if (okc)
+      for (int r = tid / SALSA_CPG; r < P.nrows; r += SALSA_THREADS / SALSA_CPG) {
+        const Row row = P.rows[r];
+        double v = 0.;
+        if (row.fin >= 0) {
+          const double *f = P.fin[row.fin];
+          if (f) v = __ldg(f + offc + P.plane * row.idx);
+        }
+        wsbase[(size_t)c * P.ws_doubles + r] = v;
       }
-      wsbase[(size_t)c * P.ws_doubles + r] = v;
-    }
     __syncthreads();
     long long q = g * SALSA_CPG + warp;
     if (q < P.ncells) cell_step<KT, DIAG>(P, w, tb, lane);
     __syncthreads();
     // write the group's output rows
-    for (int e = tid; e < P.nrows * SALSA_CPG; e += SALSA_THREADS) {
-      int r = e / SALSA_CPG, c = e % SALSA_CPG;
-      long long qq = g * SALSA_CPG + c;
-      if (qq >= P.ncells) continue;
-      Row row = P.rows[r];
-      if (row.fout < 0) continue;
-      double *f = P.fout[row.fout];
-      if (!f) continue;
-      double v = wsbase[(size_t)c * P.ws_doubles + r];
-      double *a = f + cell_offset(P, qq) + P.plane * row.idx;
-      if (row.mode == ROW_TEND) *a = *a + v;
-      else *a = v;
-    }
+    if (okc)
+      for (int r = tid / SALSA_CPG; r < P.nrows; r += SALSA_THREADS / SALSA_CPG) {
+        const Row row = P.rows[r];
+        if (row.fout < 0) continue;
+        double *f = P.fout[row.fout];
+        if (!f) continue;
+        const double v = wsbase[(size_t)c * P.ws_doubles + r];
+        double *a = f + offc + P.plane * row.idx;
+        if (row.mode == ROW_TEND) *a = *a + v;
+        else *a = v;
+      }
     if (tid == 0 && P.status) atomicAdd(P.status + ST_CELLS, (unsigned long long)min((long long)SALSA_CPG, P.ncells - g * SALSA_CPG));
     __syncthreads();
   }
