@@ -193,11 +193,17 @@ def run_gb300(args):
     except Exception:
         peak, peak_src = 6800.0, "fallback"
     achieved = bytes_cell * ncell / (r0["kernel_ms"] / 1e3) / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    # DRAM bytes per cell from one ncu capture of the same kernel on a 131072-cell block of
+    # this workload (dram__bytes_read.sum + dram__bytes_write.sum / cells), scaled to the
+    # cells of one launch; the FP64 pipe figure is that capture's sm__pipe_fp64_cycles_active.
+    traffic, fp64_pipe = None, None
+    tp = os.path.join(ROOT, "profiles", "salsa_step_kernel_grid256.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp))[args.workload] * ncell
+            prof = json.load(open(tp))
+            if prof["workload"] == args.workload:
+                traffic = prof["dram_bytes_per_cell"]["fp64"] * ncell
+                fp64_pipe = prof["fp64_pipe_active_pct"]["fp64"]
         except Exception:
             traffic = None
     line = {
@@ -211,7 +217,9 @@ def run_gb300(args):
                   "speedup_vs_fp64": mixed / value, "dtype": "f32 kernels + f64 state"},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_cell": bytes_cell},
+                     "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_cell": bytes_cell,
+                     "note": "the step is bound by the FP64 pipe, not HBM",
+                     "fp64_pipe_active_pct_ncu": fp64_pipe},
         "gpu_launches": r0["launches"],
         "clocks": results.get("clocks"),
     }
