@@ -185,12 +185,53 @@ int salsa_gb300_layout(const salsa_handle_t *h, int *nbins, int *ncld, int *nprc
 /* Number of kernel launches the last run issued (for launch accounting). */
 int salsa_gb300_last_launches(const salsa_handle_t *h);
 
-/* Average device time in ms of the dominant (step) kernel over the last run. */
+/* Device time in ms of the last run's kernels (cell-order pre-pass and step kernel). */
 double salsa_gb300_last_kernel_ms(const salsa_handle_t *h);
 
 void salsa_gb300_finalize(salsa_handle_t *h);
 
 const char *salsa_gb300_version(void);
+
+/* ---- Gradient harness (no counterpart in the reference, which has no adjoint) ----
+ * A chain advances ncell independent warm cells (a level-4 handle) through nsub
+ * steps of length dt.  Each step is the coagulation (mo_salsa_dynamics.f90:92-202)
+ * followed by the water condensation (mo_salsa_dynamics.f90:691-1125 with the water
+ * uptake of mo_salsa_properties.f90:73-380); precipitation bins must stay empty
+ * (no autoconversion, activation or redistribution in the chain).  At the start of
+ * every step the vapour is imposed as rv = rs (1 + ssat), and the solute term of the
+ * water activity is kappa * V_soluble.
+ * The state of a cell is nstate = nliquid * (1 + nwet) doubles: the numbers of the
+ * liquid bins [#/kg], then the masses m[s][b] [kg/kg] (species-major, liquid bins
+ * fastest).  x arrays are [ncell][nstate]; all pointers are device pointers.
+ * Calls are synchronous on the library stream (or on `stream` when not NULL). */
+typedef struct {
+  int ncell;
+  int nsub;
+  double dt;                                      /* s, at most 1.2 */
+  const double *temp, *press, *rs, *dn;           /* [ncell]: K, Pa, kg/kg, kg/m3 */
+  const double *kappa;                            /* [ncell] solute hygroscopicity */
+  const double *ssat;                             /* [ncell] imposed supersaturation */
+} salsa_chain_t;
+
+/* nstate of the handle's layout (0 when the handle is not level 4). */
+int salsa_gb300_chain_state_size(const salsa_handle_t *h);
+
+/* xN = chain(x0).  ckpt (NULL or [ceil(nsub/ckpt_every)][ncell][nstate]) receives
+ * the states entering steps 0, ckpt_every, 2 ckpt_every, ... in SALSA units (#/m3,
+ * m3/m3), the form in which the adjoint restarts from them. */
+int salsa_gb300_chain_forward(salsa_handle_t *h, const salsa_chain_t *c, const double *x0, double *xN,
+                              double *ckpt, int ckpt_every, void *stream);
+
+/* Tangent-linear model: xN and dxN = J (dx0, dkappa, dssat); the d* inputs may be NULL (zero). */
+int salsa_gb300_chain_tlm(salsa_handle_t *h, const salsa_chain_t *c, const double *x0, const double *dx0,
+                          const double *dkappa, const double *dssat, double *xN, double *dxN, void *stream);
+
+/* Adjoint: xbar0 = J_x^T xbarN, kappabar = J_kappa^T xbarN, ssatbar = J_ssat^T xbarN.
+ * ckpt holds the states written by salsa_gb300_chain_forward with the same
+ * ckpt_every; the states between checkpoints are recomputed. */
+int salsa_gb300_chain_adjoint(salsa_handle_t *h, const salsa_chain_t *c, const double *ckpt, int ckpt_every,
+                              const double *xbarN, double *xbar0, double *kappabar, double *ssatbar,
+                              void *stream);
 
 #ifdef __cplusplus
 }

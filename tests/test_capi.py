@@ -9,6 +9,7 @@ import tempfile
 import pytest
 
 from uclales_salsa_gb300 import api, capi
+from uclales_salsa_gb300.chain import ChainDesc
 from uclales_salsa_gb300.config import reference_defaults
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -45,7 +46,7 @@ def _offsets_from_c(struct, fields):
 
 
 @pytest.mark.parametrize("struct,cls", [("salsa_config_t", capi.Config), ("salsa_fields_t", capi.Fields),
-                                        ("salsa_status_t", capi.Status)])
+                                        ("salsa_status_t", capi.Status), ("salsa_chain_t", ChainDesc)])
 def test_struct_layout_matches_ctypes(struct, cls):
     fields = [n for n, _ in cls._fields_]
     got = _offsets_from_c(struct, fields)

@@ -1,0 +1,185 @@
+"""GPU tests of the gradient harness: chains of coagulation + condensation steps.
+
+* the chain's forward step is the step kernel's coagulation + condensation;
+* the tangent-linear model agrees with FP64 central finite differences;
+* the adjoint passes the dot-product test against the tangent-linear model and
+  agrees with central finite differences (h = 1e-6 relative) component by component;
+* checkpoint intervals give the same adjoint; the torch.autograd.Function returns it.
+
+The finite-difference checks use short chains (3 steps).  Over longer chains the
+reference's explicit condensation substeps (adt = 0.02 s, +-10 % limiter) oscillate
+on the limiter for interstitial aerosol in supersaturated cells; there the exact
+derivative of the discrete scheme grows by orders of magnitude per step while the
+map stays smooth only on scales far below h, so central differences measure a
+different (smoothed) slope.  The dot-product test holds at any chain length.
+"""
+import pytest
+import torch
+
+from uclales_salsa_gb300.inputs import make_inputs, make_outputs
+from uclales_salsa_gb300.api import SalsaStep
+from uclales_salsa_gb300.chain import SalsaChain, chain_config, pack_state, chain_apply
+
+pytestmark = pytest.mark.gpu
+H = 1e-6
+
+
+def chain_case(ncell, seed=None):
+    inp = make_inputs("chain65536", "cuda", X=1, Y=1, Z=ncell, seed=seed)
+    inp.cfg = chain_config()
+    x, th, k, s = pack_state(inp)
+    return inp, x, th, k, s
+
+
+def cloud_slice(inp):
+    lay = inp.layout
+    nl = lay.nbins + lay.ncld + lay.nprc
+    idx = list(range(lay.nbins, lay.nbins + lay.ncld))
+    for sp in range(lay.nwet):
+        idx += [nl + sp * nl + b for b in range(lay.nbins, lay.nbins + lay.ncld)]
+    return torch.tensor(idx, device="cuda")
+
+
+def test_chain_step_is_the_step_kernel():
+    inp, x, th, k, s = chain_case(256)
+    f = {kk: v.clone() for kk, v in inp.fields.items()}
+    f["rp"][2:3, 2:3, 1:-1] = (th["rs"] * (1.0 + s)).reshape(1, 1, -1)
+    out = make_outputs(inp, with_diag=False)
+    st = SalsaStep(inp.cfg)
+    st.run(inp, f, out, time=1.0)
+    torch.cuda.synchronize()
+    new = {}
+    for kk, t in (("naero", "naerot"), ("ncloud", "ncloudt"), ("nprecp", "nprecpt"),
+                  ("maero", "maerot"), ("mcloud", "mcloudt"), ("mprecp", "mprecpt")):
+        new[kk] = f[kk] + out[t] * inp.dt
+    inp2 = type(inp)(**{**inp.__dict__, "fields": {**f, **new}})
+    ref, _, _, _ = pack_state(inp2)
+    ch = SalsaChain(inp.cfg)
+    xN, _ = ch.forward(x, th, k, s, nsub=1, dt=inp.dt, keep_checkpoints=False)
+    scale = torch.maximum(ref.abs(), x.abs()).clamp(min=1e-30)
+    rel = ((xN - ref).abs() / scale)
+    assert float(rel.max()) < 1e-12, float(rel.max())
+
+
+def _fd(ch, x, th, k, s, nsub, dt, ux=None, uk=None, us=None, h=H):
+    def run(sign):
+        xx = x + sign * h * ux if ux is not None else x
+        kk = k + sign * h * uk if uk is not None else k
+        ss = s + sign * h * us if us is not None else s
+        return ch.forward(xx.contiguous(), th, kk.contiguous(), ss.contiguous(), nsub, dt, keep_checkpoints=False)[0]
+    return (run(1.0) - run(-1.0)) / (2 * h)
+
+
+def _reliable(f1, f2):
+    """Cells whose central differences at h and 2h agree to 1e-7: the difference quotient
+    is then neither dominated by rounding nor crossing a branch of the scheme (the
+    limiter, the 1e-2 stop test of the aerosol water uptake, the population limits)."""
+    d = (f1 - f2).abs() if f1.dim() == 1 else (f1 - f2).norm(dim=1)
+    m = f1.abs() if f1.dim() == 1 else f1.norm(dim=1)
+    return d <= 1e-7 * m.clamp(min=1e-300)
+
+
+def test_tlm_matches_central_differences():
+    inp, x, th, k, s = chain_case(64)
+    ch = SalsaChain(inp.cfg)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    ux = x * torch.randn(x.shape, generator=g, device="cuda", dtype=torch.float64)
+    uk = k * torch.randn(k.shape, generator=g, device="cuda", dtype=torch.float64)
+    us = s * torch.randn(s.shape, generator=g, device="cuda", dtype=torch.float64)
+    nsub = 3
+    _, dxN = ch.tlm(x, th, k, s, nsub, inp.dt, ux, uk, us)
+    cs = cloud_slice(inp)
+    fd = _fd(ch, x, th, k, s, nsub, inp.dt, ux, uk, us)[:, cs]
+    fd2 = _fd(ch, x, th, k, s, nsub, inp.dt, ux, uk, us, h=2 * H)[:, cs]
+    ok = _reliable(fd, fd2)
+    a = dxN[:, cs]
+    err = (a - fd).norm(dim=1) / fd.norm(dim=1).clamp(min=1e-300)
+    print("tlm vs fd: reliable cells", float(ok.double().mean()), "median rel err", float(err[ok].median()),
+          "max", float(err[ok].max()))
+    assert float(ok.double().mean()) > 0.8
+    assert float(err[ok].median()) < 1e-7
+    assert float((err[ok] < 1e-6).double().mean()) > 0.98
+
+
+def test_adjoint_dot_product_and_checkpoint_intervals():
+    inp, x, th, k, s = chain_case(128)
+    ch = SalsaChain(inp.cfg)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    nsub = 8
+    ux = x * torch.randn(x.shape, generator=g, device="cuda", dtype=torch.float64)
+    uk = k * torch.randn(k.shape, generator=g, device="cuda", dtype=torch.float64)
+    us = s * torch.randn(s.shape, generator=g, device="cuda", dtype=torch.float64)
+    xN, dxN = ch.tlm(x, th, k, s, nsub, inp.dt, ux, uk, us)
+    cs = cloud_slice(inp)
+    yb = torch.zeros_like(xN)
+    yb[:, cs] = torch.randn((x.shape[0], cs.numel()), generator=g, device="cuda", dtype=torch.float64) / \
+        xN[:, cs].abs().clamp(min=1e-30)
+    xf, ck = ch.forward(x, th, k, s, nsub, inp.dt, ckpt_every=1)
+    assert torch.equal(xf, xN)
+    xb, kb, sb = ch.adjoint(ck, 1, th, k, s, nsub, inp.dt, yb)
+    lhs = (yb * dxN).sum(1)
+    rhs = (xb * ux).sum(1) + kb * uk + sb * us
+    rel = (lhs - rhs).abs() / torch.maximum(lhs.abs(), rhs.abs()).clamp(min=1e-300)
+    print("dot product test: median", float(rel.median()), "max", float(rel.max()))
+    assert float(rel.median()) < 1e-12
+    assert float(rel.max()) < 1e-10
+    # checkpoints every 3 steps: the states in between are recomputed
+    _, ck3 = ch.forward(x, th, k, s, nsub, inp.dt, ckpt_every=3)
+    xb3, kb3, sb3 = ch.adjoint(ck3, 3, th, k, s, nsub, inp.dt, yb)
+    assert torch.equal(xb3, xb) and torch.equal(kb3, kb) and torch.equal(sb3, sb)
+
+
+def test_adjoint_matches_central_differences():
+    inp, x, th, k, s = chain_case(64)
+    ch = SalsaChain(inp.cfg)
+    nsub = 3
+    lay = inp.layout
+    cs = cloud_slice(inp)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    w = torch.randn(cs.numel(), generator=g, device="cuda", dtype=torch.float64)
+    xN, ck = ch.forward(x, th, k, s, nsub, inp.dt)
+    yb = torch.zeros_like(xN)
+    yb[:, cs] = w / xN[:, cs].abs().clamp(min=1e-30)
+    xb, kb, sb = ch.adjoint(ck, 1, th, k, s, nsub, inp.dt, yb)
+    loss = lambda xx: (yb * xx).sum(1)
+    nl = lay.nbins + lay.ncld + lay.nprc
+    cases = []
+    for e in [lay.nbins + 3, lay.nbins + 9, nl + 0 * nl + 6, nl + 5 * nl + lay.nbins + 4, nl + 4 * nl + 12, 5]:
+        u = torch.zeros_like(x)
+        u[:, e] = x[:, e]
+        cases.append((f"x[{e}]", dict(ux=u), xb[:, e] * x[:, e]))
+    # the cloud state depends weakly on kappa: at h = 1e-6 the difference quotient is
+    # rounding-limited (its error scales as 1/h), so kappa takes h = 1e-4
+    cases.append(("kappa", dict(uk=k, h=1e-4), kb * k))
+    cases.append(("ssat", dict(us=s), sb * s))
+    nrel = 0
+    for name, kw, ad in cases:
+        h = kw.pop("h", H)
+        fd = loss(_fd(ch, x, th, k, s, nsub, inp.dt, h=h, **kw))
+        fd2 = loss(_fd(ch, x, th, k, s, nsub, inp.dt, h=2 * h, **kw))
+        ok = _reliable(fd, fd2)
+        rel = (fd - ad).abs() / fd.abs().clamp(min=1e-300)
+        med = float(rel[ok].median()) if bool(ok.any()) else float("nan")
+        print(name, "reliable", float(ok.double().mean()), "median rel", med)
+        if float(ok.double().mean()) >= 0.5:
+            nrel += 1
+            assert med < 1e-6, name
+            assert float((rel[ok] < 1e-6).double().mean()) > 0.9, name
+    assert nrel >= 4
+
+
+def test_autograd_function_returns_the_adjoint():
+    inp, x, th, k, s = chain_case(32)
+    ch = SalsaChain(inp.cfg)
+    x0 = x.clone().requires_grad_(True)
+    kk = k.clone().requires_grad_(True)
+    ss = s.clone().requires_grad_(True)
+    xN = chain_apply(ch, x0, kk, ss, th, 4, inp.dt)
+    cs = cloud_slice(inp)
+    loss = (xN[:, cs] / xN[:, cs].detach().abs().clamp(min=1e-30)).sum()
+    gx, gk, gs = torch.autograd.grad(loss, (x0, kk, ss))
+    yb = torch.zeros_like(x)
+    yb[:, cs] = 1.0 / xN[:, cs].detach().abs().clamp(min=1e-30)
+    _, ck = ch.forward(x, th, k, s, 4, inp.dt)
+    xb, kb, sb = ch.adjoint(ck, 1, th, k, s, 4, inp.dt, yb)
+    assert torch.equal(gx, xb) and torch.equal(gk, kb) and torch.equal(gs, sb)

@@ -18,6 +18,7 @@
 
 #include "../../include/salsa_gb300.h"
 #include "salsa_device.cuh"
+#include "salsa_internal.h"
 
 namespace salsa {
 cudaError_t launch_d0(const DevParams &, cudaStream_t, int);
@@ -129,6 +130,8 @@ struct salsa_handle {
   size_t stage_bytes = 0;
   int *d_order = nullptr;       // cell order list (salsa_order_kernel)
   long long order_cap = 0;
+  void *scratch[4] = {nullptr, nullptr, nullptr, nullptr};   // gradient-chain buffers
+  size_t scratch_bytes[4] = {0, 0, 0, 0};
   int last_launches = 0;
   double last_kernel_ms = 0.;
   unsigned long long *d_stage = nullptr;   // instrumented builds only
@@ -521,6 +524,8 @@ void salsa_gb300_finalize(salsa_handle_t *h) {
   if (h->d_rows) cudaFree(h->d_rows);
   if (h->d_pairs) cudaFree(h->d_pairs);
   if (h->d_order) cudaFree(h->d_order);
+  for (int i = 0; i < 4; i++)
+    if (h->scratch[i]) cudaFree(h->scratch[i]);
   if (h->d_status) cudaFree(h->d_status);
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->stage) cudaFree(h->stage);
@@ -711,6 +716,8 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     if (P.ncells <= 0x7fffffffLL) {
       if (P.ncells > h->order_cap) {
         if (h->d_order) cudaFree(h->d_order);
+  for (int i = 0; i < 4; i++)
+    if (h->scratch[i]) cudaFree(h->scratch[i]);
         h->d_order = nullptr;
         h->order_cap = 0;
         if (cudaMalloc(&h->d_order, (size_t)P.ncells * sizeof(int)) != cudaSuccess) return SALSA_E_CUDA;
@@ -796,3 +803,27 @@ extern "C" int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int ny
   return run_impl(h, nzp, nxp, nyp, ns, tstep, time, istp, level, lcharge, initialize, f, (cudaStream_t)stream, sync,
                   st, 0);
 }
+
+// ---- handle internals for the other translation units (C++ linkage, not part of the C-ABI) ----
+namespace salsa {
+bool handle_params(const salsa_handle_t *h, DevParams *base, cudaStream_t *stream, int *device, int *nsm) {
+  if (!h) return false;
+  *base = h->base;
+  *stream = h->stream;
+  *device = h->device;
+  *nsm = h->nsm;
+  return true;
+}
+const salsa_config_t *handle_config(const salsa_handle_t *h) { return h ? &h->cfg : nullptr; }
+void *handle_scratch(salsa_handle_t *h, int slot, size_t bytes) {
+  if (!h || slot < 0 || slot >= 4) return nullptr;
+  if (bytes > h->scratch_bytes[slot]) {
+    if (h->scratch[slot]) cudaFree(h->scratch[slot]);
+    h->scratch[slot] = nullptr;
+    h->scratch_bytes[slot] = 0;
+    if (cudaMalloc(&h->scratch[slot], bytes) != cudaSuccess) return nullptr;
+    h->scratch_bytes[slot] = bytes;
+  }
+  return h->scratch[slot];
+}
+}  // namespace salsa

@@ -1,0 +1,1369 @@
+// salsa_chain.cu -- gradient harness: chains of coagulation + condensation steps.
+//
+// A chain advances independent cells through nsub steps of length dt.  Each step is
+// the coagulation (mo_salsa_dynamics.f90:92-202 with the kernels and the update of
+// mo_salsa_coagulation_kernels.f90 / mo_salsa_coagulation_processes.f90) followed by
+// the water condensation (gpparth2o, mo_salsa_dynamics.f90:691-1125, with the
+// aerosol water uptake of mo_salsa_properties.f90:73-380), in warm (level 4) cells
+// whose precipitation bins stay empty, with no autoconversion, activation or bin
+// redistribution.  The water vapour is imposed at the start of every step,
+// rv = rs (1 + s), and the solute term of the water activity is kappa * V_soluble.
+//
+// Three kernels share one generic step, chain_step<R>:
+//   * chain_forward_kernel  (R = double): the chain, with optional checkpoints;
+//   * chain_tlm_kernel      (R = Dual<1>): the tangent-linear model of the chain;
+//   * chain_adjoint_kernel  (R = double): the hand-written reverse sweep.  For every
+//     step (last to first) it recomputes the step from a checkpoint while taping
+//     the intermediate states and the condensation substep history, then runs the
+//     adjoint of each stage in reverse order.  Local partial derivatives of the
+//     collision kernel, the mass-transfer coefficients and one water-uptake
+//     iteration come from dual-number evaluations of the same code.
+// One warp owns one cell; lanes split bins and bin pairs as in the step kernel.
+#include <cuda_runtime.h>
+#include "../../include/salsa_gb300.h"
+#include "salsa_kernel_impl.cuh"
+#include "salsa_dual.cuh"
+#include "salsa_internal.h"
+
+namespace salsa {
+namespace {
+
+// dual-number forms of the math templates used by bin_props / coag_pair / terminal_vel
+template <> __device__ __forceinline__ Dual<1> t_exp<Dual<1>>(Dual<1> x) { return d_exp(x); }
+template <> __device__ __forceinline__ Dual<1> t_log<Dual<1>>(Dual<1> x) { return d_log(x); }
+template <> __device__ __forceinline__ Dual<1> t_sqrt<Dual<1>>(Dual<1> x) { return d_sqrt(x); }
+template <> __device__ __forceinline__ Dual<1> t_cbrt<Dual<1>>(Dual<1> x) { return d_cbrt(x); }
+template <> __device__ __forceinline__ Dual<1> t_pow<Dual<1>>(Dual<1> x, Dual<1> y) { return d_pow(x, y); }
+template <> __device__ __forceinline__ Dual<2> t_exp<Dual<2>>(Dual<2> x) { return d_exp(x); }
+template <> __device__ __forceinline__ Dual<2> t_log<Dual<2>>(Dual<2> x) { return d_log(x); }
+template <> __device__ __forceinline__ Dual<2> t_sqrt<Dual<2>>(Dual<2> x) { return d_sqrt(x); }
+template <> __device__ __forceinline__ Dual<2> t_cbrt<Dual<2>>(Dual<2> x) { return d_cbrt(x); }
+template <> __device__ __forceinline__ Dual<2> t_pow<Dual<2>>(Dual<2> x, Dual<2> y) { return d_pow(x, y); }
+
+// generic math for the step (double or dual)
+__device__ __forceinline__ double g_cbrt(double x) { return cbrt(x); }
+__device__ __forceinline__ double g_exp(double x) { return exp(x); }
+template <int N> __device__ __forceinline__ Dual<N> g_cbrt(const Dual<N> &x) { return d_cbrt(x); }
+template <int N> __device__ __forceinline__ Dual<N> g_exp(const Dual<N> &x) { return d_exp(x); }
+template <typename R> __device__ __forceinline__ R g_wsum(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += shfl_xor(v, o);
+  return v;
+}
+template <typename R> __device__ __forceinline__ R g_acth2o(R znw, R zns) {   // acth2o_w
+  return fmax(R(0.1), znw / fmax(R(K_EPS), znw + zns));
+}
+
+// ---- per-cell constants of a chain ----
+template <typename R>
+struct ChainCell {
+  double T, pres, prs, dn, rhoair;
+  R kappa, prv0;     // solute hygroscopicity; imposed vapour rs (1 + s)
+};
+
+// ---- per-warp workspace (shared memory) of the generic step ----
+//   n[NL], v[NW][NL]  state in SALSA units (#/m3, m3/m3); bins 0..NL-1 are the liquid bins
+//   dw[NL]            diameters at the start of the coagulation
+//   K[NL (NL+1)/2]    collision kernels of the liquid bins (i <= j)
+//   S[9][NL]          per-bin collision properties
+//   kel, surf, mt, wsat, cw, zns [NL]  condensation coefficients and substep state
+template <typename R>
+struct CW {
+  R *n, *v, *dw, *K, *S, *kel, *surf, *mt, *wsat, *cw, *zns;
+  int *pbuf;
+  int NL;
+  __device__ __forceinline__ R &V(int s, int b) const { return v[s * NL + b]; }
+  __device__ __forceinline__ R &Kij(int i, int j) const { return i <= j ? K[tri(i, j, NL)] : K[tri(j, i, NL)]; }
+};
+
+__host__ __device__ __forceinline__ int chain_tri(int NL) { return NL * (NL + 1) / 2; }
+// R-typed entries of the workspace, then 64 ints of compaction buffer
+__host__ __device__ __forceinline__ int chain_ws_entries(int NL, int NW) {
+  return NL + NW * NL + NL + chain_tri(NL) + 9 * NL + 6 * NL;
+}
+
+template <typename R>
+__device__ __forceinline__ CW<R> make_cw(R *base, int NL, int NW) {
+  CW<R> w;
+  w.NL = NL;
+  R *p = base;
+  w.n = p; p += NL;
+  w.v = p; p += NW * NL;
+  w.dw = p; p += NL;
+  w.K = p; p += chain_tri(NL);
+  w.S = p; p += 9 * NL;
+  w.kel = p; p += NL;
+  w.surf = p; p += NL;
+  w.mt = p; p += NL;
+  w.wsat = p; p += NL;
+  w.cw = p; p += NL;
+  w.zns = p; p += NL;
+  w.pbuf = reinterpret_cast<int *>(p);
+  return w;
+}
+
+// ---- tape of one step (global memory, doubles, per warp) ----
+enum { TP_MAXIT = 64, TP_MAXEQ = 104 };
+struct TapeLayout {
+  int x_in, x_pre, x_mid, x_eq, eq, hist_zc, hist_c, hist_w, nit, total;
+};
+__host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n1a) {
+  TapeLayout t;
+  const int ns = NL * (1 + NW);
+  t.x_in = 0;
+  t.x_pre = t.x_in + ns;                    // after the coagulation sweep, before the clamp
+  t.x_mid = t.x_pre + ns;
+  t.x_eq = t.x_mid + ns;
+  t.eq = t.x_eq + ns;                       // per 1a bin: [count, zke_0 .. zke_count]
+  t.hist_zc = t.eq + n1a * TP_MAXEQ;        // per substep: zcwc entering it
+  t.hist_c = t.hist_zc + TP_MAXIT;          // per substep: c of every bin entering it
+  t.hist_w = t.hist_c + TP_MAXIT * NL;      // per substep: wsat of every bin entering it
+  t.nit = t.hist_w + TP_MAXIT * NL;         // number of substeps
+  t.total = t.nit + 2;
+  return t;
+}
+
+__device__ __forceinline__ void state_to_tape(double *dst, const double *n, const double *v, int NL, int NW, int lane) {
+  for (int e = lane; e < NL * (1 + NW); e += 32) dst[e] = e < NL ? n[e] : v[e - NL];
+}
+__device__ __forceinline__ void tape_to_state(const double *src, double *n, double *v, int NL, int NW, int lane) {
+  for (int e = lane; e < NL * (1 + NW); e += 32) {
+    if (e < NL) n[e] = src[e];
+    else v[e - NL] = src[e];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Generic step (R = double or Dual<1>).  Each stage restates the step kernel's code for
+// the liquid bins with the same operation order, so the R = double chain reproduces the
+// step kernel's coagulation + condensation bit for bit.
+// ---------------------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R liquid_dwet(const DevParams &P, const CW<R> &w, const double *dmid, int b) {
+  // updateDiameterAll, wet diameter of a liquid bin (classSection.f90:91-159)
+  const int ph = phase_of(P, b);
+  R dw;
+  if (val(w.n[b]) > nlim_of(ph)) {
+    R vs = R(0.);
+    for (int s = 0; s < P.nwet; s++) vs += w.V(s, b);
+    dw = g_cbrt(vs / w.n[b] / K_PI6);
+  } else {
+    dw = R(dmid[b]);
+  }
+  return fmin(dw, R(dlim_of(ph)));
+}
+
+template <typename R>
+__device__ __forceinline__ CoagCell<R> chain_coagcell(double T, double pres, const DevParams &P) {
+  const double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+  const double mfp = (1.656e-10 * T + 1.828e-8) * K_PSTAND / pres;
+  const double zrhoa = pres / (K_RD * T);
+  const double vkin = visc / zrhoa;
+  CoagCell<R> c;
+  c.T_ = R(T); c.visc = R(visc); c.mfp = R(mfp); c.zrhoa = R(zrhoa); c.vkin = R(vkin);
+  c.shearA = R(sqrt(8. * K_PI * P.eddy_dis / (15. * vkin)));
+  c.turbB = R(K_PI * pow(P.eddy_dis, 0.75) / (K_GRAV * sqrt(sqrt(vkin))));
+  return c;
+}
+
+template <typename R>
+__device__ __forceinline__ void chain_store_props(R *S, int NL, int b, const BinProps<R> &o) {
+  S[0 * NL + b] = o.diam; S[1 * NL + b] = o.mass; S[2 * NL + b] = o.beta; S[3 * NL + b] = o.dfpart;
+  S[4 * NL + b] = o.mtvel; S[5 * NL + b] = o.omega; S[6 * NL + b] = o.termv; S[7 * NL + b] = o.reyn;
+  S[8 * NL + b] = o.schm;
+}
+template <typename R>
+__device__ __forceinline__ void chain_load_props(const R *S, int NL, int b, BinProps<R> &o) {
+  o.diam = S[0 * NL + b]; o.mass = S[1 * NL + b]; o.beta = S[2 * NL + b]; o.dfpart = S[3 * NL + b];
+  o.mtvel = S[4 * NL + b]; o.omega = S[5 * NL + b]; o.termv = S[6 * NL + b]; o.reyn = S[7 * NL + b];
+  o.schm = S[8 * NL + b];
+}
+
+// diameters at the start of the coagulation, collision properties and kernels
+template <typename R>
+__device__ void chain_kernels(const DevParams &P, const CW<R> &w, const double *tb, double T, double pres, int lane) {
+  const int NL = w.NL;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const CoagCell<R> cc = chain_coagcell<R>(T, pres, P);
+  for (int b = lane; b < NL; b += 32) w.dw[b] = liquid_dwet(P, w, dmid, b);
+  __syncwarp();
+  for (int b = lane; b < NL; b += 32) {
+    const int ph = phase_of(P, b);
+    if (!(val(w.n[b]) >= nlim_of(ph))) continue;
+    Shape<R> sh;
+    sh.alpha = sh.beta = sh.gamma = sh.sigma = R(0.);
+    const R mass = R(K_RHOWA * K_PI6) * cube(w.dw[b]);
+    BinProps<R> o;
+    bin_props<R>(cc, ph, w.dw[b], w.dw[b], mass, R(K_RHOWA), sh, o);
+    chain_store_props<R>(w.S, NL, b, o);
+  }
+  __syncwarp();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int sec = 0; sec < 2; sec++) {
+    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
+    for (int base = p0; base < p1; base += 32) {
+      const int t = base + lane;
+      bool act = false;
+      int i = 0, j = 0;
+      if (t < p1) {
+        const int pk = __ldg(P.pairs + t);
+        i = pk & 0xff; j = (pk >> 8) & 0xff;
+        act = val(w.n[i]) >= nlim_of(phase_of(P, i)) && val(w.n[j]) >= nlim_of(phase_of(P, j));
+        if (!act) w.Kij(i, j) = R(0.);
+      }
+      (void)lt;
+      if (act) {
+        BinProps<R> a, bb;
+        chain_load_props<R>(w.S, NL, j, bb);
+        if (sec == 1) {
+          Shape<R> sh;
+          sh.alpha = sh.beta = sh.gamma = sh.sigma = R(0.);
+          const R dj = w.dw[j], mj = R(K_RHOWA * K_PI6) * cube(w.dw[j]);
+          bin_props<R>(cc, phase_of(P, i), R(1.1) * dj, w.dw[i], R(1.33) * mj, R(K_RHOWA), sh, a);
+        } else {
+          chain_load_props<R>(w.S, NL, i, a);
+        }
+        w.Kij(i, j) = coag_pair<R>(cc, a, bb);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// semi-implicit update of one target from its reduced sums (applyCoag, :539-559)
+template <typename R>
+__device__ __forceinline__ void chain_apply(const CW<R> &w, int t, int nspec, double dt, R (&src)[SALSA_NSV], R sink,
+                                            R self, int lane) {
+  R my = R(0.);
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++)
+    if (lane == s) my = src[s];
+  const R n = w.n[t];
+  const bool vol = lane < nspec;
+  const R num = vol ? w.V(lane, t) + dt * my * n : n;
+  const R den = vol ? 1. + dt * sink : 1. + dt * (sink + self);
+  const R q = num / den;
+  __syncwarp();
+  if (vol) w.V(lane, t) = q;
+  else if (lane == nspec) w.n[t] = q;
+  __syncwarp();
+}
+
+template <typename R>
+__device__ __forceinline__ void chain_reduce(R (&src)[SALSA_NSV], R &sink, R &self) {
+#pragma unroll
+  for (int s = 0; s < SALSA_NSV; s++) src[s] = g_wsum(src[s]);
+  sink = g_wsum(sink);
+  self = shfl_idx(self, 0);
+}
+
+// Sources of cloud target tg (coag_cloud, :320-420 without precipitation formation):
+// aerosol bins in1a..iaa and in2b..iab, then cloud bins kfirst..kk-1 and o_first..other.
+// f(g) is called for every partner g of this lane, in the step kernel's lane order.
+template <typename F>
+__device__ __forceinline__ void cloud_sources(const DevParams &P, int kk, int kfirst, int o_first, int lane, F f) {
+  const int C0 = P.nbins, rel = kk - kfirst, other = o_first + rel;
+  if (P.lscgca) {
+    const int iaa = P.ica_par + rel, iab = P.icb_par + rel;
+    for (int ll = P.in1a + lane; ll <= iaa; ll += 32) f(ll);
+    for (int ll = P.in2b + lane; ll <= iab; ll += 32) f(ll);
+  }
+  if (P.lscgcc && kk > kfirst) {
+    for (int ll = kfirst + lane; ll <= kk - 1; ll += 32) f(C0 + ll);
+    for (int ll = o_first + lane; ll <= other; ll += 32) f(C0 + ll);
+  }
+}
+
+// Gauss-Seidel coagulation update of the aerosol, then the cloud targets
+// (mo_salsa_dynamics.f90:160-186); chain_coag_clamp is the clamp of :188-197.
+template <typename R>
+__device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const double *tb, double dt, int lane) {
+  const int nspec = P.nwet;
+  const int16_t *L = partner_lists(P, tb);
+  for (int kk = P.in1a; kk <= P.fn2b; kk++) {
+    if (val(w.n[kk]) < K_NLIM) continue;
+    R src[SALSA_NSV], sink = R(0.), self = R(0.);
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = R(0.);
+    if (P.lscgaa && lane == 0) self = 0.5 * w.Kij(kk, kk) * w.n[kk];
+    {
+      const int off = L[4 * kk], n = L[4 * kk + 1];
+      for (int e = lane; e < n; e += 32) { const int g = L[off + e]; sink += w.Kij(kk, g) * w.n[g]; }
+    }
+    {
+      const int off = L[4 * kk + 2], n = L[4 * kk + 3];
+      for (int e = lane; e < n; e += 32) {
+        const int g = L[off + e];
+        const R k = w.Kij(g, kk);
+#pragma unroll
+        for (int s = 0; s < SALSA_NSV; s++)
+          if (s < nspec) src[s] += k * w.V(s, g);
+      }
+    }
+    chain_reduce(src, sink, self);
+    chain_apply(w, kk, nspec, dt, src, sink, self, lane);
+  }
+  const int C0 = P.nbins;
+  for (int reg = 0; reg < 2; reg++) {
+    const int kfirst = reg == 0 ? P.ica_cur : P.icb_cur, klast = reg == 0 ? P.fca_cur : P.fcb_cur;
+    const int o_first = reg == 0 ? P.icb_cur : P.ica_cur;
+    for (int kk = kfirst; kk <= klast; kk++) {
+      const int tg = C0 + kk;
+      if (val(w.n[tg]) < K_NLIM) continue;
+      R src[SALSA_NSV], sink = R(0.), self = R(0.);
+#pragma unroll
+      for (int s = 0; s < SALSA_NSV; s++) src[s] = R(0.);
+      {
+        const int off = L[4 * tg], n = L[4 * tg + 1];
+        for (int e = lane; e < n; e += 32) { const int g = L[off + e]; sink += w.Kij(tg, g) * w.n[g]; }
+      }
+      if (P.lscgcc && lane == 0) self += 0.5 * w.Kij(tg, tg) * w.n[tg];
+      cloud_sources(P, kk, kfirst, o_first, lane, [&](int g) {
+        const R k = w.Kij(g, tg);
+#pragma unroll
+        for (int s = 0; s < SALSA_NSV; s++)
+          if (s < nspec) src[s] += k * w.V(s, g);
+      });
+      chain_reduce(src, sink, self);
+      chain_apply(w, tg, nspec, dt, src, sink, self, lane);
+    }
+  }
+}
+
+template <typename R>
+__device__ void chain_coag_clamp(const DevParams &P, const CW<R> &w, int lane) {
+  for (int b = lane; b < w.NL; b += 32) {
+    w.n[b] = fmax(R(0.), w.n[b]);
+    for (int s = 0; s < P.nwet; s++) w.V(s, b) = fmax(R(0.), w.V(s, b));
+  }
+  __syncwarp();
+}
+
+// ---- condensation (gpparth2o) ----
+template <typename R>
+__device__ __forceinline__ R chain_zvolc(const DevParams &P, const CW<R> &w, int which, int b) {
+  const int ix[7] = {P.ix_so4, P.ix_oc, P.ix_bc, P.ix_du, P.ix_ss, P.ix_no, P.ix_nh};
+  const int d = ix[which];
+  return (d >= 0 && which < 5) ? w.V(d, b) : R(0.);
+}
+
+// one iteration of the regime-1a water uptake (equil_iterate / eq_step, :196-245):
+// zke -> (zlwc, zdwet, zke')
+template <typename R>
+__device__ __forceinline__ void eq1a_iter(R zrh, R &zke, R zv0, R zv1, R numc, R zvp56, R zcore, double T, R &zlwc,
+                                          R &zdwet) {
+  const double rhosu_msu = 1830. / 98.08e-3, rhooc_moc = 1400. / 150.e-3;
+  R zaw = zrh / zke;
+  R a2 = zaw * zaw, a3 = a2 * zaw, a4 = a2 * a2;
+  R bm1 = +1.1065495e+2 - 3.6759197e+2 * zaw + 5.0462934e+2 * a2 - 3.1543839e+2 * a3 + 6.770824e+1 * a4;
+  R bm2 = 1. / (zaw * K_MWA) - 1. / K_MWA;
+  zlwc = (zv0 * rhosu_msu) / bm1 + K_EPSOC * zv1 * rhooc_moc / bm2;
+  zdwet = g_cbrt(zlwc / numc / K_RHOWA / K_PI6 + zvp56 / K_PI6 + zcore / K_PI6);
+  zke = g_exp(2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T * zdwet));
+}
+
+// the regime-1a chain of the non-initialising equilibration (:160-250), on every lane
+template <typename R>
+__device__ void chain_equil_1a(const DevParams &P, const CW<R> &w, R prh, double T, double *tp_eq, int lane) {
+  R zke = R(1.001);
+  const R zrh = fmin(fmax(prh, R(0.05)), R(0.98));
+  for (int kk = P.in1a; kk <= P.fn1a; kk++) {
+    double *te = tp_eq ? tp_eq + (kk - P.in1a) * TP_MAXEQ : nullptr;
+    if (!(val(w.n[kk]) > K_NLIM)) {
+      if (te && lane == 0) te[0] = -1.;
+      continue;
+    }
+    const R numc = w.n[kk];
+    const R zv0 = chain_zvolc(P, w, 0, kk), zv1 = chain_zvolc(P, w, 1, kk);
+    R zvp[7];
+    for (int i = 0; i < 7; i++) zvp[i] = chain_zvolc(P, w, i, kk) / numc;
+    const R zcore = zvp[0] + zvp[1];
+    const R zvp56 = zvp[5] + zvp[6];
+    double zdwet = val(w.dw[kk]), zdold = 1.;
+    R zlwc = R(0.);
+    int count = 0;
+    if (te && lane == 0) te[1] = val(zke);
+    while (fabs(zdwet / zdold - 1.) > 1.e-2) {
+      zdold = fmax(zdwet, 1.e-20);
+      R zd;
+      eq1a_iter(zrh, zke, zv0, zv1, numc, zvp56, zcore, T, zlwc, zd);
+      zdwet = val(zd);
+      count++;
+      if (te && lane == 0 && count + 1 < TP_MAXEQ) te[count + 1] = val(zke);
+      if (count > 100) break;
+    }
+    if (te && lane == 0) te[0] = (double)count;
+    __syncwarp();
+    if (lane == 0) w.V(P.iwa, kk) = zlwc / K_RHOWA;
+    __syncwarp();
+  }
+}
+
+// per-bin condensation coefficients (:819-955) for the liquid bins
+template <typename R>
+__device__ __forceinline__ void cond_coeffs(R n, R dwet, R znw, R zns, double T, double prs, double rhoair, double zdfh2o,
+                                            double zmfph2o, double zthcond, R &k_, R &sf, R &ws, R &m) {
+  R zact = g_acth2o(znw, zns);
+  k_ = g_exp(4. * K_SURFW0 * K_MWA / (K_RG * T * K_RHOWA * dwet));
+  sf = R(prs * rhoair / K_MWA);
+  ws = zact * k_;
+  R zknud = 2. * zmfph2o / dwet;
+  R zbeta = (zknud + 1.) / (0.377 * zknud + 1. + 4. / (3. * 1.) * (zknud + zknud * zknud));
+  R h1 = n * 2. * K_PI * dwet * zdfh2o * zbeta;
+  R h2 = K_MWA * zdfh2o * K_ALV * ws * sf / (zthcond * T);
+  R h3 = R(((K_ALV * K_MWA) / (K_RG * T)) - 1.);
+  m = h1 / (h2 * h3 + 1.);
+}
+
+struct CondConst { double rhoair, zdfh2o, zmfph2o, zthcond; };
+__device__ __forceinline__ CondConst cond_const(double T, double pres) {
+  CondConst c;
+  c.rhoair = K_MAIR * pres / (K_RG * T);
+  double zdfh2o = (5. / (16. * K_AVOG * c.rhoair * 1.e-3 * sq(3.11e-8))) *
+                  sqrt(K_RG * 1.e7 * T * K_MAIR * 1.e3 * (K_MWA + K_MAIR) * 1.e3 / (2. * K_PI * K_MWA * 1.e3));
+  c.zdfh2o = zdfh2o * 1.e-4;
+  c.zmfph2o = 3. * c.zdfh2o * sqrt(K_PI * K_MWA / (8. * K_RG * T));
+  c.zthcond = 0.023807 + 7.1128e-5 * (T - 273.16);
+  return c;
+}
+
+template <typename R>
+__device__ __forceinline__ R chain_solute(const DevParams &P, const CW<R> &w, int b, R kappa) {
+  R vs = R(0.);
+  for (int nn = 0; nn < P.ndry; nn++)
+    if (P.diss[nn] > 0.) vs += w.V(nn, b);
+  return kappa * vs * K_RHOWA / K_MWA;
+}
+
+// gpparth2o for warm cells (level 4).  Returns the substep count.
+template <typename R>
+__device__ int chain_condensation(const DevParams &P, const CW<R> &w, const double *tb, const ChainCell<R> &c,
+                                  double dt, double *tp, const TapeLayout &tl, int lane) {
+  const int NL = w.NL, iwa = P.iwa;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const double T = c.T, pres = c.pres, prs = c.prs;
+  R prv = c.prv0;
+  const R zrh = prv / prs;
+  R l1 = R(0.);
+  for (int b = lane; b <= P.fn2b; b += 32) l1 += w.V(iwa, b);
+  const R zaelwc1 = g_wsum(l1) * K_RHOWA;
+  chain_equil_1a(P, w, zrh, T, tp ? tp + tl.eq : nullptr, lane);
+  if (tp) { state_to_tape(tp + tl.x_eq, (double *)w.n, (double *)w.v, NL, P.nwet, lane); }
+  R l2 = R(0.);
+  for (int b = lane; b <= P.fn2b; b += 32) l2 += w.V(iwa, b);
+  const R zaelwc2 = g_wsum(l2) * K_RHOWA;
+  prv = prv - (zaelwc2 - zaelwc1) / (pres * K_MAIR / (K_RG * T));
+
+  bool anycl = false, anypr = false, anyae = false;
+  for (int b = lane; b < NL; b += 32) {
+    const int ph = phase_of(P, b);
+    const double n = val(w.n[b]);
+    if (ph == 1) anyae |= n > K_NLIM;
+    else if (ph == 2) anycl |= n > K_NLIM;
+    else anypr |= n > K_PRLIM;
+  }
+  anyae = warp_any(anyae); anycl = warp_any(anycl); anypr = warp_any(anypr);
+  if (tp && lane == 0) tp[tl.nit] = -1.;
+  if (!((anycl || (anypr && P.lscndh2ocl)) || (anyae && val(zrh) > 0.98 && P.lscndh2oae))) return 0;
+
+  const CondConst cc = cond_const(T, pres);
+  for (int b = lane; b < NL; b += 32) {
+    const int ph = phase_of(P, b);
+    const R dwet = liquid_dwet(P, w, dmid, b);
+    const R n = w.n[b];
+    R k_ = R(1.), sf = R(0.), m = R(0.), ws = R(0.);
+    const R ns_ = chain_solute(P, w, b, c.kappa);
+    bool act;
+    if (ph == 1) act = val(n) > K_NLIM && val(zrh) > 0.98 && P.lscndh2oae;
+    else if (ph == 2) act = val(n) > K_NLIM && P.lscndh2ocl;
+    else act = val(n) > K_PRLIM && P.lscndh2ocl;
+    if (act) {
+      const R znw = w.V(iwa, b) * P.rholiq[iwa] / P.MM[iwa];
+      cond_coeffs(n, dwet, znw, ns_, T, prs, cc.rhoair, cc.zdfh2o, cc.zmfph2o, cc.zthcond, k_, sf, ws, m);
+    }
+    w.kel[b] = k_; w.surf[b] = sf; w.mt[b] = m; w.wsat[b] = ws; w.zns[b] = ns_;
+    w.cw[b] = w.V(iwa, b) * K_RHOWA / K_MWA;
+  }
+  __syncwarp();
+  bool a = false, cl = false, pr = false;
+  for (int b = lane; b < NL; b += 32) {
+    const int ph = phase_of(P, b);
+    const double n = val(w.n[b]);
+    if (ph == 1) a |= n > K_NLIM; else if (ph == 2) cl |= n > K_NLIM; else pr |= n > K_PRLIM;
+  }
+  const bool upd_ae = warp_any(a) && val(zrh) > 0.98, upd_cl = warp_any(cl), upd_pr = warp_any(pr);
+  R zcwc = prv * cc.rhoair / K_MWA;
+  R tsum = R(0.), msum = R(0.);
+  for (int b = lane; b < NL; b += 32) {
+    tsum += w.cw[b];
+    if (b >= P.in2a) msum += w.mt[b];
+  }
+  const R zcwtot = zcwc + g_wsum(tsum);
+  const R mtot = g_wsum(msum);
+  double ttot = 0.;
+  R zcwint = R(0.);
+  int counter = 0;
+  while (ttot < dt) {
+    const double adt = 2.e-2;
+    if (tp && counter < TP_MAXIT) {
+      if (lane == 0) tp[tl.hist_zc + counter] = val(zcwc);
+      for (int b = lane; b < NL; b += 32) {
+        tp[tl.hist_c + counter * NL + b] = val(w.cw[b]);
+        tp[tl.hist_w + counter * NL + b] = val(w.wsat[b]);
+      }
+    }
+    R sp = R(0.);
+    for (int b = P.in2a + lane; b < NL; b += 32) sp += w.mt[b] * w.wsat[b] * w.surf[b];
+    const R zhlp1 = zcwc + adt * g_wsum(sp);
+    const R zhlp2 = 1. + adt * mtot;
+    zcwint = fmin(zhlp1 / zhlp2, zcwtot);
+    R cs = R(0.);
+    for (int b = lane; b < NL; b += 32) {
+      const int ph = phase_of(P, b);
+      R cc_ = w.cw[b];
+      const bool upd = (ph == 1) ? (upd_ae && b >= P.in2a) : (ph == 2 ? upd_cl : upd_pr);
+      if (upd) {
+        const R ci = cc_ + fmin(fmax(adt * w.mt[b] * (zcwint - w.wsat[b] * w.surf[b]), -1.e-1 * cc_), 1.e-1 * cc_);
+        w.wsat[b] = g_acth2o(ci, w.zns[b]) * w.kel[b];
+        cc_ = fmax(ci, R(0.));
+      }
+      w.cw[b] = cc_;
+      cs += cc_;
+    }
+    zcwint = zcwtot - g_wsum(cs);
+    zcwc = zcwint;
+    ttot = ttot + adt;
+    counter++;
+    if (counter >= 200000) break;
+  }
+  if (tp) {
+    if (lane == 0) tp[tl.nit] = (double)counter;
+    if (counter < TP_MAXIT)
+      for (int b = lane; b < NL; b += 32) tp[tl.hist_c + counter * NL + b] = val(w.cw[b]);
+  }
+  __syncwarp();
+  for (int b = lane; b < NL; b += 32) w.V(iwa, b) = fmax(R(0.), w.cw[b] * K_MWA / K_RHOWA);
+  __syncwarp();
+  return counter;
+}
+
+// ---- one step of the chain ----
+template <typename R>
+__device__ int chain_step(const DevParams &P, const CW<R> &w, const double *tb, const ChainCell<R> &c, double dt,
+                          double *tp, const TapeLayout &tl, int lane) {
+  const int NL = w.NL, NW = P.nwet;
+  if (tp) state_to_tape(tp + tl.x_in, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
+  // the chain's domain: empty precipitation bins, vapour at or above 98 % of saturation
+  // (the non-initialising branch of the water uptake, mo_salsa_dynamics.f90:797-801)
+  bool pr = false;
+  for (int b = P.nbins + P.ncld + lane; b < NL; b += 32) pr |= val(w.n[b]) >= K_PRLIM;
+  if (warp_any(pr) || !(val(c.prv0) / c.prs >= 0.98)) return 1;
+  chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
+  chain_coag_update<R>(P, w, tb, dt, lane);
+  __syncwarp();
+  if (tp) state_to_tape(tp + tl.x_pre, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
+  chain_coag_clamp<R>(P, w, lane);
+  if (tp) state_to_tape(tp + tl.x_mid, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
+  __syncwarp();
+  chain_condensation<R>(P, w, tb, c, dt, tp, tl, lane);
+  return 0;
+}
+
+struct ChainArgs {
+  int ncell, nsub, every, NL, NW, nstate, ws_doubles, n1a;
+  double dt;
+  const double *temp, *press, *rs, *dn, *kappa, *ssat;
+  const double *x0;
+  double *xN, *ckpt;
+  const double *dx0, *dkappa, *dssat;
+  double *dxN;
+  const double *xbarN;
+  double *xbar0, *kappabar, *ssatbar;
+  double *seg, *tape;
+  unsigned long long *err;
+};
+
+__device__ __forceinline__ void set_tangent(double &, double) {}
+__device__ __forceinline__ void set_tangent(Dual<1> &x, double t) { x.d[0] = t; }
+__device__ __forceinline__ double tangent(double) { return 0.; }
+__device__ __forceinline__ double tangent(const Dual<1> &x) { return x.d[0]; }
+
+// boundary units (#/kg, kg/kg) <-> SALSA units (#/m3, m3/m3), as the step kernel's unpack
+template <typename R>
+__device__ void chain_load(const DevParams &P, const CW<R> &w, const double *x, const double *dx, double dn, int lane) {
+  const int NL = w.NL;
+  for (int e = lane; e < NL * (1 + P.nwet); e += 32) {
+    if (e < NL) {
+      w.n[e] = R(x[e] * dn);
+      if (dx) set_tangent(w.n[e], dx[e] * dn);
+    } else {
+      const int s = (e - NL) / NL, b = (e - NL) - s * NL;
+      w.V(s, b) = R(x[e] * dn / P.rholiq[s]);
+      if (dx) set_tangent(w.V(s, b), dx[e] * dn / P.rholiq[s]);
+    }
+  }
+  __syncwarp();
+}
+template <typename R>
+__device__ void chain_store(const DevParams &P, const CW<R> &w, double *x, double *dx, double dn, int lane) {
+  const int NL = w.NL;
+  __syncwarp();
+  for (int e = lane; e < NL * (1 + P.nwet); e += 32) {
+    if (e < NL) {
+      x[e] = val(w.n[e]) / dn;
+      if (dx) dx[e] = tangent(w.n[e]) / dn;
+    } else {
+      const int s = (e - NL) / NL, b = (e - NL) - s * NL;
+      x[e] = val(w.V(s, b)) * P.rholiq[s] / dn;
+      if (dx) dx[e] = tangent(w.V(s, b)) * P.rholiq[s] / dn;
+    }
+  }
+  __syncwarp();
+}
+
+template <typename R>
+__device__ __forceinline__ ChainCell<R> chain_cell(const ChainArgs &A, long long q, bool tlm) {
+  ChainCell<R> c;
+  c.T = A.temp[q]; c.pres = A.press[q]; c.prs = A.rs[q]; c.dn = A.dn[q];
+  c.rhoair = K_MAIR * c.pres / (K_RG * c.T);
+  c.kappa = R(A.kappa[q]);
+  c.prv0 = R(A.rs[q] * (1.0 + A.ssat[q]));
+  if (tlm) {
+    set_tangent(c.kappa, A.dkappa ? A.dkappa[q] : 0.);
+    set_tangent(c.prv0, A.dssat ? A.rs[q] * A.dssat[q] : 0.);
+  }
+  return c;
+}
+
+__device__ __forceinline__ void chain_tables(const DevParams &P, double *tb) {
+  for (int i = threadIdx.x; i < P.tab_doubles; i += blockDim.x) tb[i] = P.tables[i];
+  __syncthreads();
+}
+
+// forward chain (R = double) and tangent-linear chain (R = Dual<1>); one warp per cell
+template <typename R, bool TLM>
+__global__ void __launch_bounds__(128) chain_fwd_kernel(const DevParams P, const ChainArgs A) {
+  extern __shared__ double smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  double *tb = smem;
+  chain_tables(P, tb);
+  CW<R> w = make_cw<R>(reinterpret_cast<R *>(smem + P.tab_doubles + (size_t)warp * A.ws_doubles), A.NL, A.NW);
+  TapeLayout tl = tape_layout(A.NL, A.NW, A.n1a);
+  unsigned long long nerr = 0;
+  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
+    const ChainCell<R> c = chain_cell<R>(A, q, TLM);
+    chain_load<R>(P, w, A.x0 + q * A.nstate, TLM ? (A.dx0 ? A.dx0 + q * A.nstate : nullptr) : nullptr, c.dn, lane);
+    int bad = 0;
+    for (int k = 0; k < A.nsub && !bad; k++) {
+      if (!TLM && A.ckpt && k % A.every == 0) {
+        double *dst = A.ckpt + ((long long)(k / A.every) * A.ncell + q) * A.nstate;
+        for (int e = lane; e < A.nstate; e += 32) dst[e] = val(w.n[e]);   // n then v: SALSA units
+      }
+      bad = chain_step<R>(P, w, tb, c, A.dt, nullptr, tl, lane);
+    }
+    nerr += bad;
+    chain_store<R>(P, w, A.xN + q * A.nstate, TLM ? A.dxN + q * A.nstate : nullptr, c.dn, lane);
+  }
+  if (lane == 0 && nerr) atomicAdd(A.err, nerr);
+}
+
+
+// =======================================================================================
+// Adjoint (R = double).  Shared-memory adjoint workspace per warp:
+//   an[NL], av[NW][NL]   adjoint of the state (the "new" slot during the coagulation reverse)
+//   on[NL], ov[NW][NL]   adjoint of the state entering the coagulation sweep ("old" slot)
+//   Kb[tri], Pj[tri]     adjoint of K; then K-bar * dK/dd_i and K-bar * dK/dd_j per pair
+//   Sd[18][NL]           per-bin collision properties as Dual<1> in the bin's own diameter
+//   db, cb, wb, mtb, kelb, znsb [NL]   adjoints of diameters and condensation quantities
+// =======================================================================================
+struct AW {
+  double *an, *av, *on, *ov, *Kb, *Pj, *cb, *wb, *mtb, *kelb, *znsb;
+  int NL;
+  __device__ __forceinline__ double &AV(int s, int b) const { return av[s * NL + b]; }
+  __device__ __forceinline__ double &OV(int s, int b) const { return ov[s * NL + b]; }
+};
+__host__ __device__ __forceinline__ int adj_ws_doubles(int NL, int NW) {
+  return 2 * (NL + NW * NL) + 2 * chain_tri(NL) + 5 * NL;
+}
+__device__ __forceinline__ AW make_aw(double *p, int NL, int NW) {
+  AW a;
+  a.NL = NL;
+  a.an = p; p += NL;
+  a.av = p; p += NW * NL;
+  a.on = p; p += NL;
+  a.ov = p; p += NW * NL;
+  a.Kb = p; p += chain_tri(NL);
+  a.Pj = p; p += chain_tri(NL);
+  a.cb = p; p += NL;
+  a.wb = p; p += NL;
+  a.mtb = p; p += NL;
+  a.kelb = p; p += NL;
+  a.znsb = p; p += NL;
+  return a;
+}
+// Rows for the diameter derivatives of the nine collision properties during the kernel
+// reverse: the condensation scratch of both workspaces is free by then.  The property
+// values themselves are still in w.S from the taped step.
+__device__ __forceinline__ double *prop_drow(const CW<double> &w, const AW &a, int k) {
+  double *r[9] = {a.cb, a.wb, a.mtb, a.kelb, a.znsb, w.kel, w.surf, w.mt, w.wsat};
+  return r[k];
+}
+
+__device__ __forceinline__ double wsum(double v) { return g_wsum(v); }
+
+// ---- condensation reverse: adjoint of the state after condensation -> after the
+// coagulation (x_mid); adds to kbar (kappa) and pbar (imposed vapour) ----
+__device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &a, const double *tb,
+                             const ChainCell<double> &c, double dt, const double *tp, const TapeLayout &tl,
+                             double &kbar, double &pbar, int lane) {
+  const int NL = w.NL, NW = P.nwet, iwa = P.iwa;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const double T = c.T, pres = c.pres, prs = c.prs;
+  const double D = pres * K_MAIR / (K_RG * T);
+  const int nit = (int)tp[tl.nit];
+  // state after the water uptake (x_eq)
+  tape_to_state(tp + tl.x_eq, w.n, w.v, NL, NW, lane);
+  __syncwarp();
+  const double zrh = c.prv0 / prs;
+  double prv_adj_bar = 0.;
+  const CondConst cc = cond_const(T, pres);
+  if (nit >= 0) {
+    // recompute the coefficients of the substep loop
+    for (int b = lane; b < NL; b += 32) {
+      const int ph = phase_of(P, b);
+      const double dwet = liquid_dwet(P, w, dmid, b);
+      const double n = w.n[b];
+      double k_ = 1., sf = 0., m = 0., ws = 0.;
+      const double ns_ = chain_solute(P, w, b, c.kappa);
+      bool act;
+      if (ph == 1) act = n > K_NLIM && zrh > 0.98 && P.lscndh2oae;
+      else if (ph == 2) act = n > K_NLIM && P.lscndh2ocl;
+      else act = n > K_PRLIM && P.lscndh2ocl;
+      if (act) {
+        const double znw = w.V(iwa, b) * P.rholiq[iwa] / P.MM[iwa];
+        cond_coeffs(n, dwet, znw, ns_, T, prs, cc.rhoair, cc.zdfh2o, cc.zmfph2o, cc.zthcond, k_, sf, ws, m);
+      }
+      w.kel[b] = k_; w.surf[b] = sf; w.mt[b] = m; w.zns[b] = ns_;
+      a.cb[b] = 0.; a.wb[b] = 0.; a.mtb[b] = 0.; a.kelb[b] = 0.; a.znsb[b] = 0.;
+    }
+    __syncwarp();
+    bool ae = false, cl = false, pr = false;
+    for (int b = lane; b < NL; b += 32) {
+      const int ph = phase_of(P, b);
+      const double n = w.n[b];
+      if (ph == 1) ae |= n > K_NLIM; else if (ph == 2) cl |= n > K_NLIM; else pr |= n > K_PRLIM;
+    }
+    const bool upd_ae = warp_any(ae) && zrh > 0.98, upd_cl = warp_any(cl), upd_pr = warp_any(pr);
+    double tsum = 0., msum = 0.;
+    for (int b = lane; b < NL; b += 32) {
+      tsum += w.V(iwa, b) * K_RHOWA / K_MWA;
+      if (b >= P.in2a) msum += w.mt[b];
+    }
+    const double zcwtot = tp[tl.hist_zc] + wsum(tsum);
+    const double mtot = wsum(msum);
+    // write-back: V_w = max(0, c_final MWA / RHOWA)
+    for (int b = lane; b < NL; b += 32) {
+      const double cf = tp[tl.hist_c + nit * NL + b];
+      const double y = cf * K_MWA / K_RHOWA;
+      a.cb[b] = y > 0. ? a.AV(iwa, b) * K_MWA / K_RHOWA : 0.;
+      a.AV(iwa, b) = 0.;
+    }
+    __syncwarp();
+    double zcb = 0., zcwtotb = 0., mtotb = 0.;
+    const double adt = 2.e-2;
+    for (int it = nit - 1; it >= 0; it--) {
+      const double zc_in = tp[tl.hist_zc + it];
+      const double *cin = tp + tl.hist_c + it * NL, *win = tp + tl.hist_w + it * NL;
+      double sp = 0.;
+      for (int b = P.in2a + lane; b < NL; b += 32) sp += w.mt[b] * win[b] * w.surf[b];
+      const double zhlp1 = zc_in + adt * wsum(sp);
+      const double zhlp2 = 1. + adt * mtot;
+      const double q = zhlp1 / zhlp2;
+      const double zcwint = fmin(q, zcwtot);
+      // zcwc_out = zcwtot - sum c_out
+      zcwtotb += zcb;
+      double zib = 0.;   // adjoint of zcwint (this lane's share)
+      for (int b = lane; b < NL; b += 32) {
+        a.cb[b] -= zcb;
+        const int ph = phase_of(P, b);
+        const bool upd = (ph == 1) ? (upd_ae && b >= P.in2a) : (ph == 2 ? upd_cl : upd_pr);
+        if (!upd) continue;
+        const double c0 = cin[b], w0 = win[b], mt = w.mt[b], sf = w.surf[b], kel = w.kel[b], zns = w.zns[b];
+        const double arg = adt * mt * (zcwint - w0 * sf);
+        const double lo = -1.e-1 * c0, hi = 1.e-1 * c0;
+        const double a1 = fmax(arg, lo);
+        const double cl_ = fmin(a1, hi);
+        const double ci = c0 + cl_;
+        double cib = ci > 0. ? a.cb[b] : 0.;
+        // wsat_out = acth2o(ci, zns) * kel
+        const double gw = a.wb[b];
+        const double den = fmax(K_EPS, ci + zns);
+        const double r = ci / den;
+        const double act = fmax(0.1, r);
+        a.kelb[b] += gw * act;
+        const double ab = gw * kel;
+        if (r > 0.1) {
+          if (ci + zns > K_EPS) {
+            const double d2 = (ci + zns) * (ci + zns);
+            cib += ab * zns / d2;
+            a.znsb[b] += -ab * ci / d2;
+          } else {
+            cib += ab / K_EPS;
+          }
+        }
+        double c0b = cib, a1b = 0.;
+        if (hi < a1) c0b += 1.e-1 * cib; else a1b = cib;
+        double argb = 0.;
+        if (lo > arg) c0b += -1.e-1 * a1b; else argb = a1b;
+        a.mtb[b] += argb * adt * (zcwint - w0 * sf);
+        zib += argb * adt * mt;
+        a.cb[b] = c0b;
+        a.wb[b] = -argb * adt * mt * sf;
+      }
+      const double zcwintb = wsum(zib);
+      double qb = 0.;
+      if (zcwtot < q) zcwtotb += zcwintb; else qb = zcwintb;
+      const double zhlp1b = qb / zhlp2;
+      const double zhlp2b = -qb * q / zhlp2;
+      mtotb += zhlp2b * adt;
+      zcb = zhlp1b;
+      const double spb = zhlp1b * adt;
+      for (int b = P.in2a + lane; b < NL; b += 32) {
+        a.mtb[b] += spb * win[b] * w.surf[b];
+        a.wb[b] += spb * w.mt[b] * w.surf[b];
+      }
+      __syncwarp();
+    }
+    // loop set-up: mtot, zcwtot = zcwc0 + sum cw0, zcwc0 = prv_adj rhoair / MWA
+    for (int b = lane; b < NL; b += 32) {
+      if (b >= P.in2a) a.mtb[b] += mtotb;
+      a.cb[b] += zcwtotb;
+    }
+    zcb += zcwtotb;
+    prv_adj_bar = zcb * cc.rhoair / K_MWA;
+    __syncwarp();
+    // coefficients (x_eq state): cw0, zns, and kel/ws/mt through dual numbers
+    double kb_l = 0.;
+    for (int b = lane; b < NL; b += 32) {
+      const int ph = phase_of(P, b);
+      a.AV(iwa, b) += a.cb[b] * K_RHOWA / K_MWA;
+      const double n = w.n[b];
+      bool act;
+      if (ph == 1) act = n > K_NLIM && zrh > 0.98 && P.lscndh2oae;
+      else if (ph == 2) act = n > K_NLIM && P.lscndh2ocl;
+      else act = n > K_PRLIM && P.lscndh2ocl;
+      double znsb = a.znsb[b];
+      if (act) {
+        // inputs: 0 n, 1 dwet, 2 znw, 3 zns
+        Dual<4> dn_(n), dd(liquid_dwet(P, w, dmid, b)), dz(w.V(iwa, b) * P.rholiq[iwa] / P.MM[iwa]), ds(w.zns[b]);
+        dn_.d[0] = 1.; dd.d[1] = 1.; dz.d[2] = 1.; ds.d[3] = 1.;
+        Dual<4> k_, sf, ws, m;
+        cond_coeffs(dn_, dd, dz, ds, T, prs, cc.rhoair, cc.zdfh2o, cc.zmfph2o, cc.zthcond, k_, sf, ws, m);
+        double g[4];
+        for (int i = 0; i < 4; i++) g[i] = a.kelb[b] * k_.d[i] + a.wb[b] * ws.d[i] + a.mtb[b] * m.d[i];
+        a.an[b] += g[0];
+        a.AV(iwa, b) += g[2] * P.rholiq[iwa] / P.MM[iwa];
+        znsb += g[3];
+        // wet diameter of x_eq
+        if (n > nlim_of(ph)) {
+          double vs = 0.;
+          for (int s = 0; s < NW; s++) vs += w.V(s, b);
+          const double dw = cbrt(vs / n / K_PI6);
+          if (!(dlim_of(ph) < dw)) {
+            for (int s = 0; s < NW; s++) a.AV(s, b) += g[1] * dw / (3. * vs);
+            a.an[b] += -g[1] * dw / (3. * n);
+          }
+        }
+      }
+      // zns = kappa * V_soluble * RHOWA / MWA
+      double vsol = 0.;
+      for (int nn = 0; nn < P.ndry; nn++)
+        if (P.diss[nn] > 0.) vsol += w.V(nn, b);
+      kb_l += znsb * vsol * K_RHOWA / K_MWA;
+      for (int nn = 0; nn < P.ndry; nn++)
+        if (P.diss[nn] > 0.) a.AV(nn, b) += znsb * c.kappa * K_RHOWA / K_MWA;
+    }
+    kbar += wsum(kb_l);
+    __syncwarp();
+  }
+  // prv_adj = prv0 - (zaelwc2 - zaelwc1) / D
+  pbar += prv_adj_bar;
+  const double zael2b = -prv_adj_bar / D, zael1b = prv_adj_bar / D;
+  for (int b = lane; b <= P.fn2b; b += 32) a.AV(iwa, b) += zael2b * K_RHOWA;
+  __syncwarp();
+  // regime-1a water uptake reverse (bins in reverse order, zke chained)
+  if (lane == 0) {
+    double zkeb = 0.;
+    for (int kk = P.fn1a; kk >= P.in1a; kk--) {
+      const double *te = tp + tl.eq + (kk - P.in1a) * TP_MAXEQ;
+      if (te[0] < 0.) continue;
+      const int cnt = (int)te[0];
+      double zlwcb = a.AV(iwa, kk) / K_RHOWA;
+      a.AV(iwa, kk) = 0.;
+      if (cnt == 0) continue;
+      // x_mid values of the bin (the tape's x_mid)
+      const double *xm = tp + tl.x_mid;
+      const double numc = xm[kk];
+      const int ix_so4 = P.ix_so4, ix_oc = P.ix_oc;
+      const double zv0 = ix_so4 >= 0 ? xm[NL + ix_so4 * NL + kk] : 0.;
+      const double zv1 = ix_oc >= 0 ? xm[NL + ix_oc * NL + kk] : 0.;
+      const double zcore = zv0 / numc + zv1 / numc;
+      double zv0b = 0., zv1b = 0., numcb = 0., zcoreb = 0.;
+      const Dual<5> zrhd(fmin(fmax(zrh, 0.05), 0.98));
+      for (int i = cnt; i >= 1; i--) {
+        Dual<5> zke(te[1 + (i - 1)]), d0(zv0), d1(zv1), dnm(numc), dco(zcore);
+        zke.d[0] = 1.; d0.d[1] = 1.; d1.d[2] = 1.; dnm.d[3] = 1.; dco.d[4] = 1.;
+        Dual<5> zlwc, zd;
+        eq1a_iter(zrhd, zke, d0, d1, dnm, Dual<5>(0.), dco, T, zlwc, zd);   // zke is now zke_i
+        const double lb = (i == cnt) ? zlwcb : 0.;
+        double g[5];
+        for (int k = 0; k < 5; k++) g[k] = lb * zlwc.d[k] + zkeb * zke.d[k];
+        zkeb = g[0];
+        zv0b += g[1]; zv1b += g[2]; numcb += g[3]; zcoreb += g[4];
+      }
+      zv0b += zcoreb / numc;
+      zv1b += zcoreb / numc;
+      numcb += -zcoreb * zv0 / (numc * numc) - zcoreb * zv1 / (numc * numc);
+      if (ix_so4 >= 0) a.AV(ix_so4, kk) += zv0b;
+      if (ix_oc >= 0) a.AV(ix_oc, kk) += zv1b;
+      a.an[kk] += numcb;
+    }
+  }
+  __syncwarp();
+  for (int b = lane; b <= P.fn2b; b += 32) a.AV(iwa, b) += zael1b * K_RHOWA;
+  __syncwarp();
+}
+
+// ---- coagulation reverse: adjoint of x_mid (after the clamp) -> adjoint of x_in ----
+// Values a target saw: a partner updated earlier in the sweep (lower index, processed)
+// shows its new value (x_pre), any other its old value (x_in).
+__device__ void coag_reverse(const DevParams &P, const CW<double> &w, const AW &a, const double *tb, double dt,
+                             const double *tp, const TapeLayout &tl, int lane) {
+  const int NL = w.NL, NW = P.nwet, C0 = P.nbins;
+  const double *xin = tp + tl.x_in, *xpre = tp + tl.x_pre, *xmid = tp + tl.x_mid;
+  const int16_t *L = partner_lists(P, tb);
+  // clamp: pass where the clamped value is positive
+  for (int e = lane; e < NL * (1 + NW); e += 32) {
+    double *slot = e < NL ? a.an + e : a.av + (e - NL);
+    if (!(xmid[e] > 0.)) *slot = 0.;
+  }
+  for (int e = lane; e < NL * (1 + NW); e += 32) (e < NL ? a.on[e] : a.ov[e - NL]) = 0.;
+  for (int e = lane; e < chain_tri(NL); e += 32) a.Kb[e] = 0.;
+  __syncwarp();
+  auto processed = [&](int b) -> bool {
+    return ((b >= P.in1a && b <= P.fn2b) || (b >= C0 && b < C0 + P.ncld)) && xin[b] >= K_NLIM;
+  };
+  // value of partner g and its adjoint slot as seen by target t
+  auto nval = [&](int g, int t) -> double { return (processed(g) && g < t) ? xpre[g] : xin[g]; };
+  auto vval = [&](int s, int g, int t) -> double {
+    return (processed(g) && g < t) ? xpre[NL + s * NL + g] : xin[NL + s * NL + g];
+  };
+  auto nslot = [&](int g, int t) -> double & { return (processed(g) && g < t) ? a.an[g] : a.on[g]; };
+  auto vslot = [&](int s, int g, int t) -> double & { return (processed(g) && g < t) ? a.AV(s, g) : a.OV(s, g); };
+  // K at the step's start state lives in w.K (recomputed by the caller)
+  for (int t = C0 + P.ncld - 1; t >= P.in1a; t--) {
+    if (!processed(t)) continue;
+    const bool isc = t >= C0;
+    int kk = 0, kfirst = 0, o_first = 0;
+    if (isc) {
+      kk = t - C0;
+      const bool ra = kk <= P.fca_cur;
+      kfirst = ra ? P.ica_cur : P.icb_cur;
+      o_first = ra ? P.icb_cur : P.ica_cur;
+    }
+    // recompute the target's sums exactly as the forward sweep
+    double src[SALSA_NSV], sink = 0., self = 0.;
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = 0.;
+    const int soff = L[4 * t], sn = L[4 * t + 1];
+    for (int e = lane; e < sn; e += 32) { const int g = L[soff + e]; sink += w.Kij(t, g) * nval(g, t); }
+    const bool has_self = isc ? P.lscgcc : P.lscgaa;
+    if (has_self && lane == 0) self = 0.5 * w.Kij(t, t) * xin[t];
+    auto src_add = [&](int g) {
+      const double k = w.Kij(g, t);
+      for (int s = 0; s < SALSA_NSV; s++)
+        if (s < NW) src[s] += k * vval(s, g, t);
+    };
+    if (isc) {
+      cloud_sources(P, kk, kfirst, o_first, lane, src_add);
+    } else {
+      const int roff = L[4 * t + 2], rn = L[4 * t + 3];
+      for (int e = lane; e < rn; e += 32) src_add(L[roff + e]);
+    }
+    chain_reduce(src, sink, self);
+    const double nt = xin[t];
+    const double den1 = 1. + dt * sink, den2 = 1. + dt * (sink + self);
+    // adjoints of the outputs (new slot of t)
+    double vbar[SALSA_NSV];
+    for (int s = 0; s < SALSA_NSV; s++) vbar[s] = s < NW ? a.AV(s, t) : 0.;
+    const double nbar = a.an[t];
+    const double nnew = xpre[t];
+    double srcb[SALSA_NSV], ntb = nbar / den2, sinkb = -nbar * nnew * dt / den2;
+    const double selfb = -nbar * nnew * dt / den2;
+    for (int s = 0; s < SALSA_NSV; s++) {
+      srcb[s] = 0.;
+      if (s < NW) {
+        const double vn = xpre[NL + s * NL + t];
+        srcb[s] = vbar[s] * dt * nt / den1;
+        ntb += vbar[s] * dt * src[s] / den1;
+        sinkb += -vbar[s] * vn * dt / den1;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      for (int s = 0; s < NW; s++) { a.OV(s, t) += vbar[s] / den1; a.AV(s, t) = 0.; }
+      if (has_self) {
+        a.Kb[tri(t, t, NL)] += selfb * 0.5 * nt;
+        ntb += selfb * 0.5 * w.Kij(t, t);
+      }
+      a.on[t] += ntb;
+      a.an[t] = 0.;
+    }
+    __syncwarp();
+    // partners (distinct bins per lane)
+    for (int e = lane; e < sn; e += 32) {
+      const int g = L[soff + e];
+      a.Kb[g < t ? tri(g, t, NL) : tri(t, g, NL)] += sinkb * nval(g, t);
+      nslot(g, t) += sinkb * w.Kij(t, g);
+    }
+    __syncwarp();
+    auto src_rev = [&](int g) {
+      const double k = w.Kij(g, t);
+      double kb = 0.;
+      for (int s = 0; s < NW; s++) {
+        kb += srcb[s] * vval(s, g, t);
+        vslot(s, g, t) += srcb[s] * k;
+      }
+      a.Kb[g < t ? tri(g, t, NL) : tri(t, g, NL)] += kb;
+    };
+    if (isc) {
+      cloud_sources(P, kk, kfirst, o_first, lane, src_rev);
+    } else {
+      const int roff = L[4 * t + 2], rn = L[4 * t + 3];
+      for (int e = lane; e < rn; e += 32) src_rev(L[roff + e]);
+    }
+    __syncwarp();
+  }
+  // adjoint of x_in: old slot, plus the new slot of the bins the sweep did not update
+  for (int e = lane; e < NL * (1 + NW); e += 32) {
+    const int b = e < NL ? e : (e - NL) % NL;
+    double &nw_ = e < NL ? a.an[e] : a.av[e - NL];
+    const double o = e < NL ? a.on[e] : a.ov[e - NL];
+    nw_ = (processed(b) ? 0. : nw_) + o;
+  }
+  __syncwarp();
+}
+
+// ---- collision-kernel reverse: K-bar -> diameter adjoints -> x_in adjoint ----
+__device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW &a, const double *tb, double T,
+                               double pres, const double *xin, int lane) {
+  const int NL = w.NL, NW = P.nwet;
+  const CoagCell<Dual<2>> c2 = chain_coagcell<Dual<2>>(T, pres, P);
+  const CoagCell<Dual<1>> c1 = chain_coagcell<Dual<1>>(T, pres, P);
+  // diameter derivatives of the per-bin properties (values: w.S of the taped step)
+  for (int b = lane; b < NL; b += 32) {
+    const int ph = phase_of(P, b);
+    if (!(w.n[b] >= nlim_of(ph))) continue;
+    Dual<1> d(w.dw[b]);
+    d.d[0] = 1.;
+    Shape<Dual<1>> sh;
+    sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<1>(0.);
+    const Dual<1> mass = Dual<1>(K_RHOWA * K_PI6) * cube(d);
+    BinProps<Dual<1>> o;
+    bin_props<Dual<1>>(c1, ph, d, d, mass, Dual<1>(K_RHOWA), sh, o);
+    const Dual<1> *po = &o.diam;
+    for (int k = 0; k < 9; k++) prop_drow(w, a, k)[b] = po[k].d[0];
+  }
+  __syncwarp();
+  auto lift = [&](int b, int dir, BinProps<Dual<2>> &o) {
+    Dual<2> *po = &o.diam;
+    for (int k = 0; k < 9; k++) {
+      Dual<2> x(w.S[k * NL + b]);
+      x.d[dir] = prop_drow(w, a, k)[b];
+      po[k] = x;
+    }
+  };
+  for (int e = lane; e < chain_tri(NL); e += 32) a.Pj[e] = 0.;
+  __syncwarp();
+  for (int sec = 0; sec < 2; sec++) {
+    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
+    for (int t = p0 + lane; t < p1; t += 32) {
+      const int pk = __ldg(P.pairs + t);
+      const int i = pk & 0xff, j = (pk >> 8) & 0xff;
+      const int ti = tri(i, j, NL);
+      const bool act = w.n[i] >= nlim_of(phase_of(P, i)) && w.n[j] >= nlim_of(phase_of(P, j));
+      const double kb = a.Kb[ti];
+      if (!act || kb == 0.) { a.Kb[ti] = 0.; continue; }
+      BinProps<Dual<2>> A_, B_;
+      lift(j, 1, B_);
+      if (sec == 1) {
+        Shape<Dual<2>> sh;
+        sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<2>(0.);
+        Dual<2> dj(w.dw[j]), di(w.dw[i]);
+        dj.d[1] = 1.; di.d[0] = 1.;
+        const Dual<2> mj = Dual<2>(K_RHOWA * K_PI6) * cube(dj);
+        bin_props<Dual<2>>(c2, phase_of(P, i), Dual<2>(1.1) * dj, di, Dual<2>(1.33) * mj, Dual<2>(K_RHOWA), sh, A_);
+      } else {
+        lift(i, 0, A_);
+      }
+      const Dual<2> k = coag_pair<Dual<2>>(c2, A_, B_);
+      a.Kb[ti] = kb * k.d[0];   // d K / d d_i
+      a.Pj[ti] = kb * k.d[1];   // d K / d d_j
+    }
+  }
+  __syncwarp();
+  // gather per bin in a fixed order, then through the wet diameter of x_in
+  for (int b = lane; b < NL; b += 32) {
+    double g = 0.;
+    for (int j = b; j < NL; j++) g += a.Kb[tri(b, j, NL)];
+    for (int i = 0; i <= b; i++) g += a.Pj[tri(i, b, NL)];
+    const int ph = phase_of(P, b);
+    const double n = xin[b];
+    if (n > nlim_of(ph) && g != 0.) {
+      double vs = 0.;
+      for (int s = 0; s < NW; s++) vs += xin[NL + s * NL + b];
+      const double dw = cbrt(vs / n / K_PI6);
+      if (!(dlim_of(ph) < dw)) {
+        for (int s = 0; s < NW; s++) a.AV(s, b) += g * dw / (3. * vs);
+        a.an[b] += -g * dw / (3. * n);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// clock64 stage sums of the adjoint (instrumented builds): 10 segment recompute,
+// 11 taped step, 12 condensation reverse, 13 coagulation reverse, 14 kernel reverse
+#ifdef SALSA_STAGE_TIMERS
+#define ADJ_MARK(k)                                                                               \
+  do {                                                                                            \
+    long long t_ = clock64();                                                                     \
+    if (lane == 0 && P.stage_clocks && (k) > 10) atomicAdd(P.stage_clocks + (k) - 1, (unsigned long long)(t_ - t_adj)); \
+    if (lane == 0 && P.stage_clocks && (k) == 10) atomicAdd(P.stage_clocks + 15, (unsigned long long)(t_ - t_adj)); \
+    t_adj = t_;                                                                                   \
+  } while (0)
+#else
+#define ADJ_MARK(k) do { } while (0)
+#endif
+
+// ---- adjoint kernel: one warp per cell, steps in reverse, segments recomputed ----
+__global__ void __launch_bounds__(128) chain_adj_kernel(const DevParams P, const ChainArgs A) {
+  extern __shared__ double smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  double *tb = smem;
+  chain_tables(P, tb);
+  const int NL = A.NL, NW = A.NW, ns = A.nstate;
+  double *base = smem + P.tab_doubles + (size_t)warp * A.ws_doubles;
+  CW<double> w = make_cw<double>(base, NL, NW);
+  AW a = make_aw(base + chain_ws_entries(NL, NW) + 32, NL, NW);
+  const TapeLayout tl = tape_layout(NL, NW, A.n1a);
+  const long long gw = (long long)blockIdx.x * wpb + warp;
+  double *tp = A.tape + gw * tl.total;
+  double *seg = A.seg + gw * (long long)A.every * ns;
+  unsigned long long nerr = 0;
+#ifdef SALSA_STAGE_TIMERS
+  long long t_adj = clock64();
+#endif
+  for (long long q = gw; q < A.ncell; q += (long long)gridDim.x * wpb) {
+    const ChainCell<double> c = chain_cell<double>(A, q, false);
+    // adjoint of xN (boundary units) -> SALSA units
+    for (int e = lane; e < ns; e += 32) {
+      const double g = A.xbarN[q * ns + e];
+      if (e < NL) a.an[e] = g / c.dn;
+      else a.av[e - NL] = g * P.rholiq[(e - NL) / NL] / c.dn;
+    }
+    double kbar = 0., pbar = 0.;
+    int bad = 0;
+    const int nseg = (A.nsub + A.every - 1) / A.every;
+    for (int sg = nseg - 1; sg >= 0 && !bad; sg--) {
+      const int k0 = sg * A.every, k1 = min(A.nsub, k0 + A.every);
+      // states entering steps k0 .. k1-1
+      const double *ck = A.ckpt + ((long long)sg * A.ncell + q) * ns;
+      for (int e = lane; e < ns; e += 32) seg[e] = ck[e];
+      if (k1 - k0 > 1) {
+        tape_to_state(ck, w.n, w.v, NL, NW, lane);
+        __syncwarp();
+        for (int k = k0; k < k1 - 1 && !bad; k++) {
+          bad = chain_step<double>(P, w, tb, c, A.dt, nullptr, tl, lane);
+          __syncwarp();
+          for (int e = lane; e < ns; e += 32) seg[(long long)(k + 1 - k0) * ns + e] = w.n[e];
+        }
+      }
+      __syncwarp();
+      for (int k = k1 - 1; k >= k0 && !bad; k--) {
+        ADJ_MARK(10);
+        tape_to_state(seg + (long long)(k - k0) * ns, w.n, w.v, NL, NW, lane);
+        __syncwarp();
+        bad = chain_step<double>(P, w, tb, c, A.dt, tp, tl, lane);
+        __syncwarp();
+        if (bad) break;
+        ADJ_MARK(11);
+        double pb = 0.;
+        cond_reverse(P, w, a, tb, c, A.dt, tp, tl, kbar, pb, lane);
+        pbar += pb;
+        ADJ_MARK(12);
+        // the step's start state; K and the diameters of it are still in the workspace
+        // (the condensation does not touch them)
+        tape_to_state(tp + tl.x_in, w.n, w.v, NL, NW, lane);
+        __syncwarp();
+        coag_reverse(P, w, a, tb, A.dt, tp, tl, lane);
+        ADJ_MARK(13);
+        kernel_reverse(P, w, a, tb, c.T, c.pres, tp + tl.x_in, lane);
+        ADJ_MARK(14);
+      }
+    }
+    nerr += bad;
+    // SALSA units -> boundary units of x0
+    for (int e = lane; e < ns; e += 32) {
+      const double g = e < NL ? a.an[e] : a.av[e - NL];
+      A.xbar0[q * ns + e] = e < NL ? g * c.dn : g * c.dn / P.rholiq[(e - NL) / NL];
+    }
+    if (lane == 0) {
+      A.kappabar[q] = kbar;
+      A.ssatbar[q] = pbar * c.prs;
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && nerr) atomicAdd(A.err, nerr);
+}
+
+}  // namespace
+}  // namespace salsa
+
+// =======================================================================================
+// C-ABI entry points of the chain
+// =======================================================================================
+namespace {
+using salsa::DevParams;
+using salsa::ChainArgs;
+
+int chain_params(salsa_handle_t *h, const salsa_chain_t *c, DevParams *P, ChainArgs *A, cudaStream_t *st, void *stream,
+                 int *nsm) {
+  int dev = 0;
+  cudaStream_t hs;
+  if (!h || !c || !salsa::handle_params(h, P, &hs, &dev, nsm)) return SALSA_E_ARG;
+  const salsa_config_t *g = salsa::handle_config(h);
+  if (g->level != 4) return SALSA_E_UNSUPPORTED;
+  if (c->ncell <= 0 || c->nsub <= 0 || !(c->dt > 0.) || c->dt > 1.2) return SALSA_E_ARG;
+  if (!c->temp || !c->press || !c->rs || !c->dn || !c->kappa || !c->ssat) return SALSA_E_ARG;
+  if (cudaSetDevice(dev) != cudaSuccess) return SALSA_E_NODEV;
+  *st = stream ? (cudaStream_t)stream : hs;
+  P->level = 4; P->lcharge = 0; P->initialize = 0; P->dt = c->dt; P->has_kappa = 1;
+  P->lscgaa = g->lscgaa; P->lscgcc = g->lscgcc; P->lscgca = g->lscgca; P->lscgpc = g->lscgpc; P->lscgpa = g->lscgpa;
+  P->lscgpp = g->lscgpp; P->lscgia = P->lscgic = P->lscgii = P->lscgip = 0;
+  P->lscndh2oae = g->lscndh2oae; P->lscndh2ocl = g->lscndh2ocl; P->lscndh2oic = 0;
+  memset(A, 0, sizeof *A);
+  A->ncell = c->ncell; A->nsub = c->nsub; A->dt = c->dt;
+  A->NL = P->nliquid; A->NW = P->nwet; A->nstate = A->NL * (1 + A->NW); A->n1a = P->fn1a - P->in1a + 1;
+  A->temp = c->temp; A->press = c->press; A->rs = c->rs; A->dn = c->dn; A->kappa = c->kappa; A->ssat = c->ssat;
+  A->every = 1;
+  unsigned long long *err = (unsigned long long *)salsa::handle_scratch(h, 3, 64);
+  if (!err) return SALSA_E_CUDA;
+  A->err = err;
+  if (cudaMemsetAsync(err, 0, sizeof(unsigned long long), *st) != cudaSuccess) return SALSA_E_CUDA;
+  return SALSA_OK;
+}
+
+template <typename R>
+int ws_doubles(int NL, int NW) {
+  return (int)(((size_t)salsa::chain_ws_entries(NL, NW) * sizeof(R) + 7) / 8) + 32;
+}
+
+template <typename K>
+int launch_chain(K kernel, const DevParams &P, const ChainArgs &A, cudaStream_t st, int nsm, int wpb) {
+  size_t smem = sizeof(double) * ((size_t)P.tab_doubles + (size_t)wpb * A.ws_doubles);
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return SALSA_E_CUDA;
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, 32 * wpb, smem) != cudaSuccess || bps <= 0)
+    return SALSA_E_CUDA;
+  long long grid = (long long)bps * nsm * 4;
+  long long need = (A.ncell + wpb - 1) / wpb;
+  if (grid > need) grid = need;
+  kernel<<<(int)grid, 32 * wpb, smem, st>>>(P, A);
+  return cudaGetLastError() == cudaSuccess ? SALSA_OK : SALSA_E_CUDA;
+}
+
+int chain_finish(const ChainArgs &A, cudaStream_t st) {
+  unsigned long long nerr = 0;
+  if (cudaMemcpyAsync(&nerr, A.err, sizeof nerr, cudaMemcpyDeviceToHost, st) != cudaSuccess) return SALSA_E_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return SALSA_E_CUDA;
+  return nerr ? SALSA_E_NUMERIC : SALSA_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int salsa_gb300_chain_state_size(const salsa_handle_t *h) {
+  DevParams P;
+  cudaStream_t s;
+  int dev, nsm;
+  if (!salsa::handle_params(h, &P, &s, &dev, &nsm)) return 0;
+  return salsa::handle_config(h)->level == 4 ? P.nliquid * (1 + P.nwet) : 0;
+}
+
+int salsa_gb300_chain_forward(salsa_handle_t *h, const salsa_chain_t *c, const double *x0, double *xN, double *ckpt,
+                              int ckpt_every, void *stream) {
+  DevParams P;
+  ChainArgs A;
+  cudaStream_t st;
+  int nsm = 0;
+  int rc = chain_params(h, c, &P, &A, &st, stream, &nsm);
+  if (rc) return rc;
+  if (!x0 || !xN || (ckpt && ckpt_every <= 0)) return SALSA_E_ARG;
+  A.x0 = x0; A.xN = xN; A.ckpt = ckpt; A.every = ckpt ? ckpt_every : 1;
+  A.ws_doubles = ws_doubles<double>(A.NL, A.NW);
+  rc = launch_chain(salsa::chain_fwd_kernel<double, false>, P, A, st, nsm, 4);
+  if (rc) return rc;
+  return chain_finish(A, st);
+}
+
+int salsa_gb300_chain_tlm(salsa_handle_t *h, const salsa_chain_t *c, const double *x0, const double *dx0,
+                          const double *dkappa, const double *dssat, double *xN, double *dxN, void *stream) {
+  DevParams P;
+  ChainArgs A;
+  cudaStream_t st;
+  int nsm = 0;
+  int rc = chain_params(h, c, &P, &A, &st, stream, &nsm);
+  if (rc) return rc;
+  if (!x0 || !xN || !dxN) return SALSA_E_ARG;
+  A.x0 = x0; A.xN = xN; A.dx0 = dx0; A.dkappa = dkappa; A.dssat = dssat; A.dxN = dxN;
+  A.ws_doubles = ws_doubles<salsa::Dual<1>>(A.NL, A.NW);
+  rc = launch_chain(salsa::chain_fwd_kernel<salsa::Dual<1>, true>, P, A, st, nsm, 4);
+  if (rc) return rc;
+  return chain_finish(A, st);
+}
+
+int salsa_gb300_chain_adjoint(salsa_handle_t *h, const salsa_chain_t *c, const double *ckpt, int ckpt_every,
+                              const double *xbarN, double *xbar0, double *kappabar, double *ssatbar, void *stream) {
+  DevParams P;
+  ChainArgs A;
+  cudaStream_t st;
+  int nsm = 0;
+  int rc = chain_params(h, c, &P, &A, &st, stream, &nsm);
+  if (rc) return rc;
+  if (!ckpt || ckpt_every <= 0 || !xbarN || !xbar0 || !kappabar || !ssatbar) return SALSA_E_ARG;
+  A.ckpt = const_cast<double *>(ckpt); A.every = ckpt_every;
+  A.xbarN = xbarN; A.xbar0 = xbar0; A.kappabar = kappabar; A.ssatbar = ssatbar;
+  A.ws_doubles = salsa::chain_ws_entries(A.NL, A.NW) + 32 + salsa::adj_ws_doubles(A.NL, A.NW);
+  const int wpb = 2;
+  auto kernel = salsa::chain_adj_kernel;
+  size_t smem = sizeof(double) * ((size_t)P.tab_doubles + (size_t)wpb * A.ws_doubles);
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return SALSA_E_CUDA;
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, 32 * wpb, smem) != cudaSuccess || bps <= 0)
+    return SALSA_E_CUDA;
+  long long grid = (long long)bps * nsm;
+  long long need = (A.ncell + wpb - 1) / wpb;
+  if (grid > need) grid = need;
+  const salsa::TapeLayout tl = salsa::tape_layout(A.NL, A.NW, A.n1a);
+  const size_t nw = (size_t)grid * wpb;
+  A.tape = (double *)salsa::handle_scratch(h, 0, nw * tl.total * sizeof(double));
+  A.seg = (double *)salsa::handle_scratch(h, 1, nw * (size_t)ckpt_every * A.nstate * sizeof(double));
+  if (!A.tape || !A.seg) return SALSA_E_CUDA;
+  kernel<<<(int)grid, 32 * wpb, smem, st>>>(P, A);
+  if (cudaGetLastError() != cudaSuccess) return SALSA_E_CUDA;
+  return chain_finish(A, st);
+}
+
+}  // extern "C"

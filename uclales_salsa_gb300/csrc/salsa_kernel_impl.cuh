@@ -5,7 +5,7 @@
 // (UCLALES-SALSA src/src_salsa/mo_salsa_driver.f90:180-427 -> mo_salsa.f90:45-153).
 //
 // Execution model
-//   * block = SALSA_CPG warps = SALSA_CPG consecutive interior cells ("group");
+//   * block = SALSA_CPG warps = SALSA_CPG interior cells ("group");
 //     the block stages the group's bin-major input rows into shared memory with
 //     sector-complete loads (SALSA_CPG consecutive doubles per row), every warp
 //     advances its own cell out of shared memory, and the block writes the
@@ -16,8 +16,11 @@
 //     lane-parallel and reduced with warp shuffles.
 //   * KT is the arithmetic type of the collision kernels and of the condensation
 //     mass-transfer coefficients: double for the parity form, float for the mixed
-//     form (partner sums then use compensated summation; denominators, the water
-//     budget and all state updates stay double).
+//     form (the partner sums accumulate the float kernel values in double, which is
+//     tighter than compensated float sums; denominators, the water budget and all
+//     state updates stay double).
+//   * a pre-pass orders the cells so that the cells of one block share a class
+//     (all-clear or cloudy); a block's cells are then not always neighbours.
 #pragma once
 #include "salsa_device.cuh"
 #include <cstdio>
@@ -121,6 +124,11 @@ __device__ __forceinline__ double rimefrac(const DevParams &P, double n, double 
 template <typename T>
 struct Shape { T alpha, beta, gamma, sigma; };
 
+// float selects the cancellation-free single-precision forms; every other arithmetic
+// type (double, and the dual numbers of the gradient kernels) takes the FP64 forms
+template <typename T> struct is_f32 { static constexpr bool value = false; };
+template <> struct is_f32<float> { static constexpr bool value = true; };
+
 template <typename T>
 __device__ __forceinline__ T t_exp(T x);
 template <> __device__ __forceinline__ double t_exp<double>(double x) { return exp(x); }
@@ -200,7 +208,7 @@ __device__ T terminal_vel(T diam, T rhop, T rhoa, T visc, T beta, int flag, cons
     T X = ((T)2. * Vb * (rhop - rhoa) * grav * sq(dnsp)) / (Ap * rhoa * sq(visc));
     const T c1 = (T)0.0902, delta0 = (T)9.06;
     T k12, km1, bre;
-    if (sizeof(T) == 8) {
+    if (!is_f32<T>::value) {
       k12 = t_sqrt((T)1. + c1 * t_sqrt(X));
       km1 = k12 - (T)1.;
       bre = (T)0.5 * c1 * t_sqrt(X);
@@ -269,7 +277,7 @@ __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinPro
   T flux1 = (T)4. * (T)K_PI * mdiam * (a.dfpart + b.dfpart);
   T flux2 = (T)K_PI * t_sqrt(sq(a.mtvel) + sq(b.mtvel)) * sq(mdiam);
   T tva1, tva2;
-  if (sizeof(T) == 8) {
+  if (!is_f32<T>::value) {
     T m2 = sq(mdiam);
     T oa2 = m2 + sq(a.omega), ob2 = m2 + sq(b.omega);
     tva1 = (cube(mdiam + a.omega) - oa2 * t_sqrt(oa2)) / ((T)3. * mdiam * a.omega) - mdiam;

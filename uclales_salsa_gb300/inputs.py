@@ -41,6 +41,11 @@ WORKLOADS = {
     "batch65536": dict(X=1, Y=1, Z=65536, level=4, T=(280., 295.), p=(90.e3, 101.e3),
                        rh_clear=(1.0, 1.01), cloudy=0.0, pattern="none", ice=False, seed=3, dt=0.5,
                        kappa=(0.1, 1.2), supersat=(0.0, 0.01)),
+    # gradient workload: 65,536 independent warm cells, every cell holding the cloud
+    # droplet distribution (and no precipitation), kappa and an imposed supersaturation
+    "chain65536": dict(X=1, Y=1, Z=65536, level=4, T=(280., 295.), p=(90.e3, 101.e3),
+                       rh_clear=(1.0, 1.01), rh_cloud=(1.0, 1.01), cloudy=1.0, pattern="random", ice=False,
+                       precip=False, seed=5, dt=0.5, kappa=(0.1, 1.2), supersat=(0.0, 0.01)),
     # 384x384x160, level 5, 10 % cloudy as convective columns with ice, 90 % clear at RH 40-85 %
     "grid384x384x160": dict(X=384, Y=384, Z=160, level=5, T=(235., 270.), p=(90.e3, 101.e3),
                             rh_clear=(0.40, 0.85), rh_cloud=(1.0, 1.01), cloudy=0.10, pattern="columns",
@@ -214,7 +219,7 @@ def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnos
                 for k in range(ndry):
                     vcld[k, cb] = ncld_[cb] * vd * comp[k]
                 vcld[ndry, cb] = ncld_[cb] * vw
-        for j in range(npr):
+        for j in range(npr if spec.get("precip", True) else 0):
             nprc_[j] = 1000.0 / npr * cm
             dm = lay.dmid[lay.nbins + ncl + j]
             v = PI6 * dm ** 3
