@@ -177,6 +177,21 @@ int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
                           int initialize, const salsa_fields_t *f, void *stream,
                           int sync, salsa_status_t *st);
 
+/* No counterpart in the reference.  Same as salsa_gb300_run_async, but the call
+ * allocates nothing: the cell-order list and the status counters sit in module
+ * memory of the library (a static device array sized for SALSA_NOALLOC_MAXCELLS
+ * = 2,097,152 interior cells; larger grids return SALSA_E_ARG).  The call clears
+ * the status counters on the stream before the step.  The first call on a handle
+ * resolves the module scratch of the handle's device (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls on one device share the
+ * scratch: calls that overlap in time (other streams, other handles on the same
+ * device) race on it and must be serialised by the caller.  Device pointers only. */
+#define SALSA_NOALLOC_MAXCELLS 2097152
+int salsa_gb300_run_noalloc(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
+                            double tstep, double time, int istp, int level, int lcharge,
+                            int initialize, const salsa_fields_t *f, void *stream,
+                            int sync, salsa_status_t *st);
+
 /* Bin layout queries (mo_submctl.f90 nbins/ncld/nprc/nice and the diameter
  * limit tables aerobins/cloudbins/precpbins/icebins, mo_salsa_init.f90:236-239). */
 int salsa_gb300_layout(const salsa_handle_t *h, int *nbins, int *ncld, int *nprc,

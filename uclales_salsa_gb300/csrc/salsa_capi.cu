@@ -34,6 +34,12 @@ int blocks_per_sm_f1(const DevParams &);
 using salsa::DevParams;
 using salsa::Row;
 
+// Scratch of salsa_gb300_run_noalloc: the cell-order list and the status counters live
+// in module memory, so that entry point allocates nothing.  SALSA_NOALLOC_MAXCELLS
+// (header) bounds the interior cells of one call (8 MiB of order list).
+static __device__ __align__(256) int g_na_order[SALSA_NOALLOC_MAXCELLS];
+static __device__ __align__(256) unsigned long long g_na_status[salsa::ST_N];
+
 // Cell order of one step: cells whose cloud, precipitation and ice bins are all below
 // the population limits fill the list from the front, the others from the back, so
 // that the four cells of a block (which meet at barriers) take the same code path.
@@ -130,6 +136,8 @@ struct salsa_handle {
   size_t stage_bytes = 0;
   int *d_order = nullptr;       // cell order list (salsa_order_kernel)
   long long order_cap = 0;
+  int *na_order = nullptr;      // module scratch of salsa_gb300_run_noalloc on this handle's device
+  unsigned long long *na_status = nullptr;
   void *scratch[4] = {nullptr, nullptr, nullptr, nullptr};   // gradient-chain buffers
   size_t scratch_bytes[4] = {0, 0, 0, 0};
   int last_launches = 0;
@@ -578,7 +586,7 @@ int resolve_side(const void *p, int *side) {
 
 int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep, double time, int istp, int level,
              int lcharge, int initialize, const salsa_fields_t *f, cudaStream_t stream, int sync, salsa_status_t *st,
-             int allow_host) {
+             int allow_host, int noalloc = 0) {
   if (!h || !f) return SALSA_E_ARG;
   const salsa_config_t &g = h->cfg;
   if (level != g.level || nzp < 3 || nxp < 5 || nyp < 5 || !(tstep > 0.) || !(tstep <= 600.) || ns < h->base.nwet)
@@ -705,15 +713,20 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
       if (x.fo == salsa::FO_CHARGE) P.fin[salsa::FI_CHARGE] = dp;
     }
   }
+  if (noalloc && P.ncells > SALSA_NOALLOC_MAXCELLS) return SALSA_E_ARG;
+  unsigned long long *d_status = noalloc ? h->na_status : h->d_status;
+  P.status = d_status;
   if (P.ncells > 0) {
-    if (cudaMemsetAsync(h->d_status, 0, salsa::ST_N * sizeof(unsigned long long), s) != cudaSuccess) return SALSA_E_CUDA;
+    if (cudaMemsetAsync(d_status, 0, salsa::ST_N * sizeof(unsigned long long), s) != cudaSuccess) return SALSA_E_CUDA;
     int prec = g.precision, dg = g.diagnostics ? 1 : 0;
     int bps = prec == 0 ? (dg ? salsa::blocks_per_sm_d1(P) : salsa::blocks_per_sm_d0(P))
                         : (dg ? salsa::blocks_per_sm_f1(P) : salsa::blocks_per_sm_f0(P));
     if (bps <= 0) return SALSA_E_CUDA;
     long long grid = (long long)bps * h->nsm * 8;
     if (grid > P.ngroups) grid = P.ngroups;
-    if (P.ncells <= 0x7fffffffLL) {
+    if (noalloc) {
+      P.order = h->na_order;
+    } else if (P.ncells <= 0x7fffffffLL) {
       if (P.ncells > h->order_cap) {
         if (h->d_order) cudaFree(h->d_order);
   for (int i = 0; i < 4; i++)
@@ -731,7 +744,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     if (P.order) {
       long long og = (P.ncells + 255) / 256;
       if (og > (long long)h->nsm * 16) og = (long long)h->nsm * 16;
-      salsa_order_kernel<<<(int)og, 256, 0, s>>>(P, h->d_order);
+      salsa_order_kernel<<<(int)og, 256, 0, s>>>(P, const_cast<int *>(P.order));
       if (cudaGetLastError() != cudaSuccess) return SALSA_E_CUDA;
       launches++;
     }
@@ -740,7 +753,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     cudaEventRecord(h->ev1, s);
     if (e != cudaSuccess) return SALSA_E_CUDA;
     launches++;
-    if (cudaMemcpyAsync(h->h_status, h->d_status, salsa::ST_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) !=
+    if (cudaMemcpyAsync(h->h_status, d_status, salsa::ST_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) !=
         cudaSuccess)
       return SALSA_E_CUDA;
   }
@@ -802,6 +815,23 @@ extern "C" int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int ny
                                      void *stream, int sync, salsa_status_t *st) {
   return run_impl(h, nzp, nxp, nyp, ns, tstep, time, istp, level, lcharge, initialize, f, (cudaStream_t)stream, sync,
                   st, 0);
+}
+
+extern "C" int salsa_gb300_run_noalloc(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
+                                       double time, int istp, int level, int lcharge, int initialize,
+                                       const salsa_fields_t *f, void *stream, int sync, salsa_status_t *st) {
+  if (!h) return SALSA_E_ARG;
+  if (!h->na_order || !h->na_status) {
+    // first call on this handle: resolve the module scratch of the handle's device
+    if (cudaSetDevice(h->device) != cudaSuccess) return SALSA_E_NODEV;
+    void *po = nullptr, *ps = nullptr;
+    if (cudaGetSymbolAddress(&po, g_na_order) != cudaSuccess || cudaGetSymbolAddress(&ps, g_na_status) != cudaSuccess)
+      return SALSA_E_CUDA;
+    h->na_order = static_cast<int *>(po);
+    h->na_status = static_cast<unsigned long long *>(ps);
+  }
+  return run_impl(h, nzp, nxp, nyp, ns, tstep, time, istp, level, lcharge, initialize, f, (cudaStream_t)stream, sync,
+                  st, 0, 1);
 }
 
 // ---- handle internals for the other translation units (C++ linkage, not part of the C-ABI) ----
