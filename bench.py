@@ -15,6 +15,8 @@ A step is one SALSA call over every interior cell of the workload
             small and the ncu FP64 pipe figures are in profiles/.
   cpu_baseline -- the FP64 CPU oracle (a C restatement of the reference path; the
             Fortran cannot be built here) on a bounded sample, all host threads.
+  adjoint -- forward and adjoint time of the gradient harness (65,536 warm cells, 60
+            coagulation + condensation steps of 0.5 s, checkpoints every step).
 
 --impl reference times that CPU implementation alone on bounded samples of the same
 workload.  With torchrun, every rank runs the workload on its own GPU (independent
@@ -223,12 +225,48 @@ def run_gb300(args):
         "gpu_launches": r0["launches"],
         "clocks": results.get("clocks"),
     }
+    if rank == 0 and not args.no_adjoint:
+        line["adjoint"] = chain_bench(dev)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample_cells)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         tdist.destroy_process_group()
+
+
+def chain_bench(dev, nsub=60):
+    """Forward and adjoint time of the gradient harness on its workload: 65,536 warm
+    cells, nsub coagulation + condensation steps of 0.5 s, checkpoints every step."""
+    import torch
+    from uclales_salsa_gb300.inputs import make_inputs
+    from uclales_salsa_gb300.chain import SalsaChain, chain_config, pack_state
+    inp = make_inputs("chain65536", dev)
+    inp.cfg = chain_config()
+    x, th, k, s = pack_state(inp)
+    ch = SalsaChain(inp.cfg)
+    yb = torch.zeros_like(x)
+    lay = inp.layout
+    nl = lay.nbins + lay.ncld + lay.nprc
+    for b in range(lay.nbins, lay.nbins + lay.ncld):   # loss: final cloud numbers and masses
+        yb[:, b] = 1.0
+        for sp in range(lay.nwet):
+            yb[:, nl + sp * nl + b] = 1.0
+    xw, ckw = ch.forward(x, th, k, s, 2, inp.dt)          # warm-up (module load, allocation)
+    ch.adjoint(ckw, 1, th, k, s, 2, inp.dt, yb)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    ev[0].record()
+    xN, ck = ch.forward(x, th, k, s, nsub, inp.dt, ckpt_every=1)
+    ev[1].record()
+    xb, kb, sb = ch.adjoint(ck, 1, th, k, s, nsub, inp.dt, yb / xN.abs().clamp(min=1e-30))
+    ev[2].record()
+    torch.cuda.synchronize()
+    f_ms, a_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    ch.close()
+    return {"workload": f"chain65536 ({x.shape[0]} cells, {nsub} steps of {inp.dt} s, coagulation + condensation)",
+            "forward_ms": f_ms, "adjoint_ms": a_ms, "adjoint_over_forward": a_ms / f_ms, "checkpoint_every": 1,
+            "gradients_finite": bool(torch.isfinite(xb).all() and torch.isfinite(kb).all() and torch.isfinite(sb).all())}
 
 
 def oracle_sample(workload, cells):
@@ -296,6 +334,7 @@ def main():
     ap.add_argument("--workload", default="grid256x256x128")
     ap.add_argument("--cpu-sample-cells", type=int, default=3145728)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -105,7 +105,7 @@ __device__ __forceinline__ CW<R> make_cw(R *base, int NL, int NW) {
 // ---- tape of one step (global memory, doubles, per warp) ----
 enum { TP_MAXIT = 64, TP_MAXEQ = 104 };
 struct TapeLayout {
-  int x_in, x_pre, x_mid, x_eq, eq, hist_zc, hist_c, hist_w, nit, total;
+  int x_in, x_pre, x_mid, x_eq, sums, pj, eq, hist_zc, hist_c, hist_w, nit, total;
 };
 __host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n1a) {
   TapeLayout t;
@@ -114,7 +114,9 @@ __host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n
   t.x_pre = t.x_in + ns;                    // after the coagulation sweep, before the clamp
   t.x_mid = t.x_pre + ns;
   t.x_eq = t.x_mid + ns;
-  t.eq = t.x_eq + ns;                       // per 1a bin: [count, zke_0 .. zke_count]
+  t.sums = t.x_eq + ns;                     // per coagulation target: sink, self, src[NSV]
+  t.pj = t.sums + NL * (2 + SALSA_NSV);     // kernel reverse: K-bar * dK/dd_j per pair
+  t.eq = t.pj + chain_tri(NL);              // per 1a bin: [count, zke_0 .. zke_count]
   t.hist_zc = t.eq + n1a * TP_MAXEQ;        // per substep: zcwc entering it
   t.hist_c = t.hist_zc + TP_MAXIT;          // per substep: c of every bin entering it
   t.hist_w = t.hist_c + TP_MAXIT * NL;      // per substep: wsat of every bin entering it
@@ -277,7 +279,17 @@ __device__ __forceinline__ void cloud_sources(const DevParams &P, int kk, int kf
 // Gauss-Seidel coagulation update of the aerosol, then the cloud targets
 // (mo_salsa_dynamics.f90:160-186); chain_coag_clamp is the clamp of :188-197.
 template <typename R>
-__device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const double *tb, double dt, int lane) {
+__device__ __forceinline__ void tape_sums(double *ts, int t, const R (&src)[SALSA_NSV], R sink, R self, int lane) {
+  if (ts && lane == 0) {
+    double *o = ts + t * (2 + SALSA_NSV);
+    o[0] = val(sink); o[1] = val(self);
+    for (int s = 0; s < SALSA_NSV; s++) o[2 + s] = val(src[s]);
+  }
+}
+
+template <typename R>
+__device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const double *tb, double dt, int lane,
+                                  double *ts = nullptr) {
   const int nspec = P.nwet;
   const int16_t *L = partner_lists(P, tb);
   for (int kk = P.in1a; kk <= P.fn2b; kk++) {
@@ -301,6 +313,7 @@ __device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const doub
       }
     }
     chain_reduce(src, sink, self);
+    tape_sums(ts, kk, src, sink, self, lane);
     chain_apply(w, kk, nspec, dt, src, sink, self, lane);
   }
   const int C0 = P.nbins;
@@ -325,6 +338,7 @@ __device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const doub
           if (s < nspec) src[s] += k * w.V(s, g);
       });
       chain_reduce(src, sink, self);
+      tape_sums(ts, tg, src, sink, self, lane);
       chain_apply(w, tg, nspec, dt, src, sink, self, lane);
     }
   }
@@ -559,7 +573,7 @@ __device__ int chain_step(const DevParams &P, const CW<R> &w, const double *tb, 
   for (int b = P.nbins + P.ncld + lane; b < NL; b += 32) pr |= val(w.n[b]) >= K_PRLIM;
   if (warp_any(pr) || !(val(c.prv0) / c.prs >= 0.98)) return 1;
   chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
-  chain_coag_update<R>(P, w, tb, dt, lane);
+  chain_coag_update<R>(P, w, tb, dt, lane, tp ? tp + tl.sums : nullptr);
   __syncwarp();
   if (tp) state_to_tape(tp + tl.x_pre, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
   chain_coag_clamp<R>(P, w, lane);
@@ -672,18 +686,18 @@ __global__ void __launch_bounds__(128) chain_fwd_kernel(const DevParams P, const
 // Adjoint (R = double).  Shared-memory adjoint workspace per warp:
 //   an[NL], av[NW][NL]   adjoint of the state (the "new" slot during the coagulation reverse)
 //   on[NL], ov[NW][NL]   adjoint of the state entering the coagulation sweep ("old" slot)
-//   Kb[tri], Pj[tri]     adjoint of K; then K-bar * dK/dd_i and K-bar * dK/dd_j per pair
-//   Sd[18][NL]           per-bin collision properties as Dual<1> in the bin's own diameter
-//   db, cb, wb, mtb, kelb, znsb [NL]   adjoints of diameters and condensation quantities
+//   Kb[tri]              adjoint of K; then K-bar * dK/dd_i per pair (K-bar * dK/dd_j goes
+//                        to the tape's pj rows)
+//   cb, wb, mtb, kelb, znsb [NL]   adjoints of the condensation quantities
 // =======================================================================================
 struct AW {
-  double *an, *av, *on, *ov, *Kb, *Pj, *cb, *wb, *mtb, *kelb, *znsb;
+  double *an, *av, *on, *ov, *Kb, *cb, *wb, *mtb, *kelb, *znsb;
   int NL;
   __device__ __forceinline__ double &AV(int s, int b) const { return av[s * NL + b]; }
   __device__ __forceinline__ double &OV(int s, int b) const { return ov[s * NL + b]; }
 };
 __host__ __device__ __forceinline__ int adj_ws_doubles(int NL, int NW) {
-  return 2 * (NL + NW * NL) + 2 * chain_tri(NL) + 5 * NL;
+  return 2 * (NL + NW * NL) + chain_tri(NL) + 5 * NL;
 }
 __device__ __forceinline__ AW make_aw(double *p, int NL, int NW) {
   AW a;
@@ -693,7 +707,6 @@ __device__ __forceinline__ AW make_aw(double *p, int NL, int NW) {
   a.on = p; p += NL;
   a.ov = p; p += NW * NL;
   a.Kb = p; p += chain_tri(NL);
-  a.Pj = p; p += chain_tri(NL);
   a.cb = p; p += NL;
   a.wb = p; p += NL;
   a.mtb = p; p += NL;
@@ -971,25 +984,13 @@ __device__ void coag_reverse(const DevParams &P, const CW<double> &w, const AW &
       kfirst = ra ? P.ica_cur : P.icb_cur;
       o_first = ra ? P.icb_cur : P.ica_cur;
     }
-    // recompute the target's sums exactly as the forward sweep
-    double src[SALSA_NSV], sink = 0., self = 0.;
-    for (int s = 0; s < SALSA_NSV; s++) src[s] = 0.;
+    // the target's sums, taped by the forward sweep
+    const double *tsum = tp + tl.sums + t * (2 + SALSA_NSV);
+    double src[SALSA_NSV];
+    const double sink = tsum[0], self = tsum[1];
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = tsum[2 + s];
     const int soff = L[4 * t], sn = L[4 * t + 1];
-    for (int e = lane; e < sn; e += 32) { const int g = L[soff + e]; sink += w.Kij(t, g) * nval(g, t); }
     const bool has_self = isc ? P.lscgcc : P.lscgaa;
-    if (has_self && lane == 0) self = 0.5 * w.Kij(t, t) * xin[t];
-    auto src_add = [&](int g) {
-      const double k = w.Kij(g, t);
-      for (int s = 0; s < SALSA_NSV; s++)
-        if (s < NW) src[s] += k * vval(s, g, t);
-    };
-    if (isc) {
-      cloud_sources(P, kk, kfirst, o_first, lane, src_add);
-    } else {
-      const int roff = L[4 * t + 2], rn = L[4 * t + 3];
-      for (int e = lane; e < rn; e += 32) src_add(L[roff + e]);
-    }
-    chain_reduce(src, sink, self);
     const double nt = xin[t];
     const double den1 = 1. + dt * sink, den2 = 1. + dt * (sink + self);
     // adjoints of the outputs (new slot of t)
@@ -1055,7 +1056,7 @@ __device__ void coag_reverse(const DevParams &P, const CW<double> &w, const AW &
 
 // ---- collision-kernel reverse: K-bar -> diameter adjoints -> x_in adjoint ----
 __device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW &a, const double *tb, double T,
-                               double pres, const double *xin, int lane) {
+                               double pres, const double *xin, double *Pj, int lane) {
   const int NL = w.NL, NW = P.nwet;
   const CoagCell<Dual<2>> c2 = chain_coagcell<Dual<2>>(T, pres, P);
   const CoagCell<Dual<1>> c1 = chain_coagcell<Dual<1>>(T, pres, P);
@@ -1082,7 +1083,7 @@ __device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW
       po[k] = x;
     }
   };
-  for (int e = lane; e < chain_tri(NL); e += 32) a.Pj[e] = 0.;
+  for (int e = lane; e < chain_tri(NL); e += 32) Pj[e] = 0.;
   __syncwarp();
   for (int sec = 0; sec < 2; sec++) {
     const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
@@ -1107,7 +1108,7 @@ __device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW
       }
       const Dual<2> k = coag_pair<Dual<2>>(c2, A_, B_);
       a.Kb[ti] = kb * k.d[0];   // d K / d d_i
-      a.Pj[ti] = kb * k.d[1];   // d K / d d_j
+      Pj[ti] = kb * k.d[1];     // d K / d d_j
     }
   }
   __syncwarp();
@@ -1115,7 +1116,7 @@ __device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW
   for (int b = lane; b < NL; b += 32) {
     double g = 0.;
     for (int j = b; j < NL; j++) g += a.Kb[tri(b, j, NL)];
-    for (int i = 0; i <= b; i++) g += a.Pj[tri(i, b, NL)];
+    for (int i = 0; i <= b; i++) g += Pj[tri(i, b, NL)];
     const int ph = phase_of(P, b);
     const double n = xin[b];
     if (n > nlim_of(ph) && g != 0.) {
@@ -1207,7 +1208,7 @@ __global__ void __launch_bounds__(128) chain_adj_kernel(const DevParams P, const
         __syncwarp();
         coag_reverse(P, w, a, tb, A.dt, tp, tl, lane);
         ADJ_MARK(13);
-        kernel_reverse(P, w, a, tb, c.T, c.pres, tp + tl.x_in, lane);
+        kernel_reverse(P, w, a, tb, c.T, c.pres, tp + tl.x_in, tp + tl.pj, lane);
         ADJ_MARK(14);
       }
     }
@@ -1345,7 +1346,7 @@ int salsa_gb300_chain_adjoint(salsa_handle_t *h, const salsa_chain_t *c, const d
   A.ckpt = const_cast<double *>(ckpt); A.every = ckpt_every;
   A.xbarN = xbarN; A.xbar0 = xbar0; A.kappabar = kappabar; A.ssatbar = ssatbar;
   A.ws_doubles = salsa::chain_ws_entries(A.NL, A.NW) + 32 + salsa::adj_ws_doubles(A.NL, A.NW);
-  const int wpb = 2;
+  const int wpb = 4;
   auto kernel = salsa::chain_adj_kernel;
   size_t smem = sizeof(double) * ((size_t)P.tab_doubles + (size_t)wpb * A.ws_doubles);
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
