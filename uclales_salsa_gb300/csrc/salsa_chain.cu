@@ -12,14 +12,17 @@
 // Three kernels share one generic step, chain_step<R>:
 //   * chain_forward_kernel  (R = double): the chain, with optional checkpoints;
 //   * chain_tlm_kernel      (R = Dual<1>): the tangent-linear model of the chain;
-//   * chain_adjoint_kernel  (R = double): the hand-written reverse sweep.  For every
-//     step (last to first) it recomputes the step from a checkpoint while taping
-//     the intermediate states and the condensation substep history, then runs the
-//     adjoint of each stage in reverse order.  Local partial derivatives of the
+//   * the adjoint (R = double), hand-written, run step by step from the last step:
+//     chain_taped_kernel recomputes the step of every cell from its checkpoint (or
+//     from the states chain_seg_kernel recomputed inside a checkpoint segment) and
+//     tapes the intermediate states, the condensation substep history and the
+//     collision kernels with their diameter derivatives; chain_rev_kernel then runs
+//     the adjoint of each stage in reverse order.  Local partial derivatives of the
 //     collision kernel, the mass-transfer coefficients and one water-uptake
 //     iteration come from dual-number evaluations of the same code.
 // One warp owns one cell; lanes split bins and bin pairs as in the step kernel.
 #include <cuda_runtime.h>
+#include <type_traits>
 #include "../../include/salsa_gb300.h"
 #include "salsa_kernel_impl.cuh"
 #include "salsa_dual.cuh"
@@ -102,28 +105,34 @@ __device__ __forceinline__ CW<R> make_cw(R *base, int NL, int NW) {
   return w;
 }
 
-// ---- tape of one step (global memory, doubles, per warp) ----
-enum { TP_MAXIT = 64, TP_MAXEQ = 104 };
+// ---- tape of one step (global memory, doubles, per cell) ----
+enum { TP_MAXEQ = 104 };
 struct TapeLayout {
-  int x_in, x_pre, x_mid, x_eq, sums, pj, eq, hist_zc, hist_c, hist_w, nit, total;
+  int x_in, x_pre, x_mid, x_eq, sums, pj, K, dki, dkj, eq, hist_zc, hist_c, hist_w, nit, maxit, total;
 };
-__host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n1a) {
+// maxit: substep rows of the condensation history (the loop count plus the final row)
+__host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n1a, int maxit) {
   TapeLayout t;
-  const int ns = NL * (1 + NW);
+  const int ns = NL * (1 + NW), tr = NL * (NL + 1) / 2;
+  t.maxit = maxit;
   t.x_in = 0;
   t.x_pre = t.x_in + ns;                    // after the coagulation sweep, before the clamp
   t.x_mid = t.x_pre + ns;
   t.x_eq = t.x_mid + ns;
   t.sums = t.x_eq + ns;                     // per coagulation target: sink, self, src[NSV]
   t.pj = t.sums + NL * (2 + SALSA_NSV);     // kernel reverse: K-bar * dK/dd_j per pair
-  t.eq = t.pj + chain_tri(NL);              // per 1a bin: [count, zke_0 .. zke_count]
+  t.K = t.pj + tr;                          // collision kernels of the step
+  t.dki = t.K + tr;                         // dK/dd_i and dK/dd_j of every pair (i <= j)
+  t.dkj = t.dki + tr;
+  t.eq = t.dkj + tr;                        // per 1a bin: [count, zke_0 .. zke_count]
   t.hist_zc = t.eq + n1a * TP_MAXEQ;        // per substep: zcwc entering it
-  t.hist_c = t.hist_zc + TP_MAXIT;          // per substep: c of every bin entering it
-  t.hist_w = t.hist_c + TP_MAXIT * NL;      // per substep: wsat of every bin entering it
-  t.nit = t.hist_w + TP_MAXIT * NL;         // number of substeps
+  t.hist_c = t.hist_zc + maxit;             // per substep: c of every bin entering it
+  t.hist_w = t.hist_c + maxit * NL;         // per substep: wsat of every bin entering it
+  t.nit = t.hist_w + maxit * NL;            // number of substeps; then the cell's void flag
   t.total = t.nit + 2;
   return t;
 }
+__host__ __device__ __forceinline__ int tape_maxit(double dt) { return (int)(dt / 2.e-2) + 3; }
 
 __device__ __forceinline__ void state_to_tape(double *dst, const double *n, const double *v, int NL, int NW, int lane) {
   for (int e = lane; e < NL * (1 + NW); e += 32) dst[e] = e < NL ? n[e] : v[e - NL];
@@ -519,7 +528,7 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
   int counter = 0;
   while (ttot < dt) {
     const double adt = 2.e-2;
-    if (tp && counter < TP_MAXIT) {
+    if (tp && counter < tl.maxit) {
       if (lane == 0) tp[tl.hist_zc + counter] = val(zcwc);
       for (int b = lane; b < NL; b += 32) {
         tp[tl.hist_c + counter * NL + b] = val(w.cw[b]);
@@ -552,7 +561,7 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
   }
   if (tp) {
     if (lane == 0) tp[tl.nit] = (double)counter;
-    if (counter < TP_MAXIT)
+    if (counter < tl.maxit)
       for (int b = lane; b < NL; b += 32) tp[tl.hist_c + counter * NL + b] = val(w.cw[b]);
   }
   __syncwarp();
@@ -561,10 +570,76 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
   return counter;
 }
 
+// Collision kernels of a taped step (FP64): the values as chain_kernels<double>, plus
+// dK/dd_i and dK/dd_j of every pair from dual numbers.  drow (9 NL) receives the
+// diameter derivatives of the per-bin properties; the kernels and their derivatives
+// go to the tape (tri layout, zero for pairs that are not active).
+__device__ void chain_kernels_taped(const DevParams &P, const CW<double> &w, const double *tb, double T, double pres,
+                                    double *drow, double *Kt, double *dki, double *dkj, int lane) {
+  const int NL = w.NL;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const CoagCell<Dual<1>> c1 = chain_coagcell<Dual<1>>(T, pres, P);
+  const CoagCell<Dual<2>> c2 = chain_coagcell<Dual<2>>(T, pres, P);
+  for (int b = lane; b < NL; b += 32) w.dw[b] = liquid_dwet(P, w, dmid, b);
+  for (int e = lane; e < chain_tri(NL); e += 32) { dki[e] = 0.; dkj[e] = 0.; }
+  __syncwarp();
+  for (int b = lane; b < NL; b += 32) {
+    const int ph = phase_of(P, b);
+    if (!(w.n[b] >= nlim_of(ph))) continue;
+    Dual<1> d(w.dw[b]);
+    d.d[0] = 1.;
+    Shape<Dual<1>> sh;
+    sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<1>(0.);
+    const Dual<1> mass = Dual<1>(K_RHOWA * K_PI6) * cube(d);
+    BinProps<Dual<1>> o;
+    bin_props<Dual<1>>(c1, ph, d, d, mass, Dual<1>(K_RHOWA), sh, o);
+    const Dual<1> *po = &o.diam;
+    for (int k = 0; k < 9; k++) { w.S[k * NL + b] = po[k].v; drow[k * NL + b] = po[k].d[0]; }
+  }
+  __syncwarp();
+  auto lift = [&](int b, int dir, BinProps<Dual<2>> &o) {
+    Dual<2> *po = &o.diam;
+    for (int k = 0; k < 9; k++) {
+      Dual<2> x(w.S[k * NL + b]);
+      x.d[dir] = drow[k * NL + b];
+      po[k] = x;
+    }
+  };
+  for (int sec = 0; sec < 2; sec++) {
+    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
+    for (int t = p0 + lane; t < p1; t += 32) {
+      const int pk = __ldg(P.pairs + t);
+      const int i = pk & 0xff, j = (pk >> 8) & 0xff;
+      const int ti = tri(i, j, NL);
+      const bool act = w.n[i] >= nlim_of(phase_of(P, i)) && w.n[j] >= nlim_of(phase_of(P, j));
+      if (!act) { w.K[ti] = 0.; continue; }
+      BinProps<Dual<2>> A_, B_;
+      lift(j, 1, B_);
+      if (sec == 1) {
+        Shape<Dual<2>> sh;
+        sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<2>(0.);
+        Dual<2> dj(w.dw[j]), di(w.dw[i]);
+        dj.d[1] = 1.; di.d[0] = 1.;
+        const Dual<2> mj = Dual<2>(K_RHOWA * K_PI6) * cube(dj);
+        bin_props<Dual<2>>(c2, phase_of(P, i), Dual<2>(1.1) * dj, di, Dual<2>(1.33) * mj, Dual<2>(K_RHOWA), sh, A_);
+      } else {
+        lift(i, 0, A_);
+      }
+      const Dual<2> k = coag_pair<Dual<2>>(c2, A_, B_);
+      w.K[ti] = k.v;
+      dki[ti] = k.d[0];
+      dkj[ti] = k.d[1];
+    }
+  }
+  __syncwarp();
+  for (int e = lane; e < chain_tri(NL); e += 32) Kt[e] = w.K[e];
+  __syncwarp();
+}
+
 // ---- one step of the chain ----
 template <typename R>
 __device__ int chain_step(const DevParams &P, const CW<R> &w, const double *tb, const ChainCell<R> &c, double dt,
-                          double *tp, const TapeLayout &tl, int lane) {
+                          double *tp, const TapeLayout &tl, int lane, double *drow = nullptr) {
   const int NL = w.NL, NW = P.nwet;
   if (tp) state_to_tape(tp + tl.x_in, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
   // the chain's domain: empty precipitation bins, vapour at or above 98 % of saturation
@@ -572,7 +647,12 @@ __device__ int chain_step(const DevParams &P, const CW<R> &w, const double *tb, 
   bool pr = false;
   for (int b = P.nbins + P.ncld + lane; b < NL; b += 32) pr |= val(w.n[b]) >= K_PRLIM;
   if (warp_any(pr) || !(val(c.prv0) / c.prs >= 0.98)) return 1;
-  chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
+  if constexpr (std::is_same<R, double>::value) {
+    if (tp) chain_kernels_taped(P, w, tb, c.T, c.pres, drow, tp + tl.K, tp + tl.dki, tp + tl.dkj, lane);
+    else chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
+  } else {
+    chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
+  }
   chain_coag_update<R>(P, w, tb, dt, lane, tp ? tp + tl.sums : nullptr);
   __syncwarp();
   if (tp) state_to_tape(tp + tl.x_pre, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
@@ -656,13 +736,13 @@ __device__ __forceinline__ void chain_tables(const DevParams &P, double *tb) {
 
 // forward chain (R = double) and tangent-linear chain (R = Dual<1>); one warp per cell
 template <typename R, bool TLM>
-__global__ void __launch_bounds__(128) chain_fwd_kernel(const DevParams P, const ChainArgs A) {
+__global__ void __launch_bounds__(128, 2) chain_fwd_kernel(const DevParams P, const ChainArgs A) {
   extern __shared__ double smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double *tb = smem;
   chain_tables(P, tb);
   CW<R> w = make_cw<R>(reinterpret_cast<R *>(smem + P.tab_doubles + (size_t)warp * A.ws_doubles), A.NL, A.NW);
-  TapeLayout tl = tape_layout(A.NL, A.NW, A.n1a);
+  TapeLayout tl = tape_layout(A.NL, A.NW, A.n1a, tape_maxit(A.dt));
   unsigned long long nerr = 0;
   for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
     const ChainCell<R> c = chain_cell<R>(A, q, TLM);
@@ -713,13 +793,6 @@ __device__ __forceinline__ AW make_aw(double *p, int NL, int NW) {
   a.kelb = p; p += NL;
   a.znsb = p; p += NL;
   return a;
-}
-// Rows for the diameter derivatives of the nine collision properties during the kernel
-// reverse: the condensation scratch of both workspaces is free by then.  The property
-// values themselves are still in w.S from the taped step.
-__device__ __forceinline__ double *prop_drow(const CW<double> &w, const AW &a, int k) {
-  double *r[9] = {a.cb, a.wb, a.mtb, a.kelb, a.znsb, w.kel, w.surf, w.mt, w.wsat};
-  return r[k];
 }
 
 __device__ __forceinline__ double wsum(double v) { return g_wsum(v); }
@@ -1054,62 +1127,13 @@ __device__ void coag_reverse(const DevParams &P, const CW<double> &w, const AW &
   __syncwarp();
 }
 
-// ---- collision-kernel reverse: K-bar -> diameter adjoints -> x_in adjoint ----
-__device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW &a, const double *tb, double T,
-                               double pres, const double *xin, double *Pj, int lane) {
-  const int NL = w.NL, NW = P.nwet;
-  const CoagCell<Dual<2>> c2 = chain_coagcell<Dual<2>>(T, pres, P);
-  const CoagCell<Dual<1>> c1 = chain_coagcell<Dual<1>>(T, pres, P);
-  // diameter derivatives of the per-bin properties (values: w.S of the taped step)
-  for (int b = lane; b < NL; b += 32) {
-    const int ph = phase_of(P, b);
-    if (!(w.n[b] >= nlim_of(ph))) continue;
-    Dual<1> d(w.dw[b]);
-    d.d[0] = 1.;
-    Shape<Dual<1>> sh;
-    sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<1>(0.);
-    const Dual<1> mass = Dual<1>(K_RHOWA * K_PI6) * cube(d);
-    BinProps<Dual<1>> o;
-    bin_props<Dual<1>>(c1, ph, d, d, mass, Dual<1>(K_RHOWA), sh, o);
-    const Dual<1> *po = &o.diam;
-    for (int k = 0; k < 9; k++) prop_drow(w, a, k)[b] = po[k].d[0];
-  }
-  __syncwarp();
-  auto lift = [&](int b, int dir, BinProps<Dual<2>> &o) {
-    Dual<2> *po = &o.diam;
-    for (int k = 0; k < 9; k++) {
-      Dual<2> x(w.S[k * NL + b]);
-      x.d[dir] = prop_drow(w, a, k)[b];
-      po[k] = x;
-    }
-  };
-  for (int e = lane; e < chain_tri(NL); e += 32) Pj[e] = 0.;
-  __syncwarp();
-  for (int sec = 0; sec < 2; sec++) {
-    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
-    for (int t = p0 + lane; t < p1; t += 32) {
-      const int pk = __ldg(P.pairs + t);
-      const int i = pk & 0xff, j = (pk >> 8) & 0xff;
-      const int ti = tri(i, j, NL);
-      const bool act = w.n[i] >= nlim_of(phase_of(P, i)) && w.n[j] >= nlim_of(phase_of(P, j));
-      const double kb = a.Kb[ti];
-      if (!act || kb == 0.) { a.Kb[ti] = 0.; continue; }
-      BinProps<Dual<2>> A_, B_;
-      lift(j, 1, B_);
-      if (sec == 1) {
-        Shape<Dual<2>> sh;
-        sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<2>(0.);
-        Dual<2> dj(w.dw[j]), di(w.dw[i]);
-        dj.d[1] = 1.; di.d[0] = 1.;
-        const Dual<2> mj = Dual<2>(K_RHOWA * K_PI6) * cube(dj);
-        bin_props<Dual<2>>(c2, phase_of(P, i), Dual<2>(1.1) * dj, di, Dual<2>(1.33) * mj, Dual<2>(K_RHOWA), sh, A_);
-      } else {
-        lift(i, 0, A_);
-      }
-      const Dual<2> k = coag_pair<Dual<2>>(c2, A_, B_);
-      a.Kb[ti] = kb * k.d[0];   // d K / d d_i
-      Pj[ti] = kb * k.d[1];     // d K / d d_j
-    }
+// ---- collision-kernel reverse: K-bar and the taped dK/dd -> x_in adjoint ----
+__device__ void kernel_reverse(const DevParams &P, const AW &a, const double *xin, const double *dki,
+                               const double *dkj, double *Pj, int NL, int NW, int lane) {
+  for (int e = lane; e < chain_tri(NL); e += 32) {
+    const double kb = a.Kb[e];
+    a.Kb[e] = kb * dki[e];
+    Pj[e] = kb * dkj[e];
   }
   __syncwarp();
   // gather per bin in a fixed order, then through the wet diameter of x_in
@@ -1132,22 +1156,37 @@ __device__ void kernel_reverse(const DevParams &P, const CW<double> &w, const AW
   __syncwarp();
 }
 
-// clock64 stage sums of the adjoint (instrumented builds): 10 segment recompute,
-// 11 taped step, 12 condensation reverse, 13 coagulation reverse, 14 kernel reverse
-#ifdef SALSA_STAGE_TIMERS
-#define ADJ_MARK(k)                                                                               \
-  do {                                                                                            \
-    long long t_ = clock64();                                                                     \
-    if (lane == 0 && P.stage_clocks && (k) > 10) atomicAdd(P.stage_clocks + (k) - 1, (unsigned long long)(t_ - t_adj)); \
-    if (lane == 0 && P.stage_clocks && (k) == 10) atomicAdd(P.stage_clocks + 15, (unsigned long long)(t_ - t_adj)); \
-    t_adj = t_;                                                                                   \
-  } while (0)
-#else
-#define ADJ_MARK(k) do { } while (0)
-#endif
+// ---- adjoint kernels; the host runs them step by step, last step first ----
+// Segment recompute: the states entering steps k0+1 .. k1-1 of a checkpoint segment.
+__global__ void __launch_bounds__(128, 2) chain_seg_kernel(const DevParams P, const ChainArgs A, int sg) {
+  extern __shared__ double smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  double *tb = smem;
+  chain_tables(P, tb);
+  const int NL = A.NL, NW = A.NW, ns = A.nstate;
+  CW<double> w = make_cw<double>(smem + P.tab_doubles + (size_t)warp * A.ws_doubles, NL, NW);
+  const TapeLayout tl = tape_layout(NL, NW, A.n1a, tape_maxit(A.dt));
+  const int k0 = sg * A.every, k1 = min(A.nsub, k0 + A.every);
+  unsigned long long nerr = 0;
+  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
+    const ChainCell<double> c = chain_cell<double>(A, q, false);
+    tape_to_state(A.ckpt + ((long long)sg * A.ncell + q) * ns, w.n, w.v, NL, NW, lane);
+    __syncwarp();
+    int bad = 0;
+    for (int k = k0; k < k1 - 1 && !bad; k++) {
+      bad = chain_step<double>(P, w, tb, c, A.dt, nullptr, tl, lane);
+      __syncwarp();
+      double *dst = A.seg + ((long long)(k + 1 - k0) * A.ncell + q) * ns;
+      for (int e = lane; e < ns; e += 32) dst[e] = w.n[e];
+      __syncwarp();
+    }
+    nerr += bad;
+  }
+  if (lane == 0 && nerr) atomicAdd(A.err, nerr);
+}
 
-// ---- adjoint kernel: one warp per cell, steps in reverse, segments recomputed ----
-__global__ void __launch_bounds__(128) chain_adj_kernel(const DevParams P, const ChainArgs A) {
+// Taped step: recompute step k of every cell from the state entering it, taping.
+__global__ void __launch_bounds__(128, 2) chain_taped_kernel(const DevParams P, const ChainArgs A, const double *src) {
   extern __shared__ double smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double *tb = smem;
@@ -1155,76 +1194,78 @@ __global__ void __launch_bounds__(128) chain_adj_kernel(const DevParams P, const
   const int NL = A.NL, NW = A.NW, ns = A.nstate;
   double *base = smem + P.tab_doubles + (size_t)warp * A.ws_doubles;
   CW<double> w = make_cw<double>(base, NL, NW);
-  AW a = make_aw(base + chain_ws_entries(NL, NW) + 32, NL, NW);
-  const TapeLayout tl = tape_layout(NL, NW, A.n1a);
-  const long long gw = (long long)blockIdx.x * wpb + warp;
-  double *tp = A.tape + gw * tl.total;
-  double *seg = A.seg + gw * (long long)A.every * ns;
+  double *drow = base + chain_ws_entries(NL, NW) + 32;
+  const TapeLayout tl = tape_layout(NL, NW, A.n1a, tape_maxit(A.dt));
   unsigned long long nerr = 0;
-#ifdef SALSA_STAGE_TIMERS
-  long long t_adj = clock64();
-#endif
-  for (long long q = gw; q < A.ncell; q += (long long)gridDim.x * wpb) {
+  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
     const ChainCell<double> c = chain_cell<double>(A, q, false);
-    // adjoint of xN (boundary units) -> SALSA units
-    for (int e = lane; e < ns; e += 32) {
-      const double g = A.xbarN[q * ns + e];
-      if (e < NL) a.an[e] = g / c.dn;
-      else a.av[e - NL] = g * P.rholiq[(e - NL) / NL] / c.dn;
-    }
-    double kbar = 0., pbar = 0.;
-    int bad = 0;
-    const int nseg = (A.nsub + A.every - 1) / A.every;
-    for (int sg = nseg - 1; sg >= 0 && !bad; sg--) {
-      const int k0 = sg * A.every, k1 = min(A.nsub, k0 + A.every);
-      // states entering steps k0 .. k1-1
-      const double *ck = A.ckpt + ((long long)sg * A.ncell + q) * ns;
-      for (int e = lane; e < ns; e += 32) seg[e] = ck[e];
-      if (k1 - k0 > 1) {
-        tape_to_state(ck, w.n, w.v, NL, NW, lane);
-        __syncwarp();
-        for (int k = k0; k < k1 - 1 && !bad; k++) {
-          bad = chain_step<double>(P, w, tb, c, A.dt, nullptr, tl, lane);
-          __syncwarp();
-          for (int e = lane; e < ns; e += 32) seg[(long long)(k + 1 - k0) * ns + e] = w.n[e];
-        }
-      }
-      __syncwarp();
-      for (int k = k1 - 1; k >= k0 && !bad; k--) {
-        ADJ_MARK(10);
-        tape_to_state(seg + (long long)(k - k0) * ns, w.n, w.v, NL, NW, lane);
-        __syncwarp();
-        bad = chain_step<double>(P, w, tb, c, A.dt, tp, tl, lane);
-        __syncwarp();
-        if (bad) break;
-        ADJ_MARK(11);
-        double pb = 0.;
-        cond_reverse(P, w, a, tb, c, A.dt, tp, tl, kbar, pb, lane);
-        pbar += pb;
-        ADJ_MARK(12);
-        // the step's start state; K and the diameters of it are still in the workspace
-        // (the condensation does not touch them)
-        tape_to_state(tp + tl.x_in, w.n, w.v, NL, NW, lane);
-        __syncwarp();
-        coag_reverse(P, w, a, tb, A.dt, tp, tl, lane);
-        ADJ_MARK(13);
-        kernel_reverse(P, w, a, tb, c.T, c.pres, tp + tl.x_in, tp + tl.pj, lane);
-        ADJ_MARK(14);
-      }
-    }
+    tape_to_state(src + q * ns, w.n, w.v, NL, NW, lane);
+    __syncwarp();
+    double *tp = A.tape + q * (long long)tl.total;
+    const int bad = chain_step<double>(P, w, tb, c, A.dt, tp, tl, lane, drow);
     nerr += bad;
-    // SALSA units -> boundary units of x0
-    for (int e = lane; e < ns; e += 32) {
-      const double g = e < NL ? a.an[e] : a.av[e - NL];
-      A.xbar0[q * ns + e] = e < NL ? g * c.dn : g * c.dn / P.rholiq[(e - NL) / NL];
-    }
-    if (lane == 0) {
-      A.kappabar[q] = kbar;
-      A.ssatbar[q] = pbar * c.prs;
-    }
+    if (lane == 0) tp[tl.nit + 1] = bad ? 1. : 0.;   // 1: the cell's adjoint is void
     __syncwarp();
   }
   if (lane == 0 && nerr) atomicAdd(A.err, nerr);
+}
+
+// Reverse of step k of every cell; the running adjoint of the state (SALSA units) is
+// kept in xbar0, the kappa and supersaturation adjoints accumulate in place.
+__global__ void __launch_bounds__(128, 2) chain_rev_kernel(const DevParams P, const ChainArgs A) {
+  extern __shared__ double smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  double *tb = smem;
+  chain_tables(P, tb);
+  const int NL = A.NL, NW = A.NW, ns = A.nstate;
+  double *base = smem + P.tab_doubles + (size_t)warp * A.ws_doubles;
+  // condensation-reverse workspace: state and six per-bin rows; K lives in the tape
+  CW<double> w;
+  w.NL = NL;
+  w.n = base; w.v = base + NL;
+  w.kel = base + ns; w.surf = w.kel + NL; w.mt = w.surf + NL; w.wsat = w.mt + NL; w.cw = w.wsat + NL;
+  w.zns = w.cw + NL;
+  w.dw = nullptr; w.S = nullptr; w.pbuf = nullptr; w.K = nullptr;
+  AW a = make_aw(base + ns + 6 * NL, NL, NW);
+  const TapeLayout tl = tape_layout(NL, NW, A.n1a, tape_maxit(A.dt));
+  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
+    double *tp = A.tape + q * (long long)tl.total;
+    if (tp[tl.nit + 1] != 0.) continue;
+    const ChainCell<double> c = chain_cell<double>(A, q, false);
+    w.K = tp + tl.K;
+    double *xb = A.xbar0 + q * ns;
+    for (int e = lane; e < ns; e += 32) { if (e < NL) a.an[e] = xb[e]; else a.av[e - NL] = xb[e]; }
+    __syncwarp();
+    double kbar = 0., pbar = 0.;
+    cond_reverse(P, w, a, tb, c, A.dt, tp, tl, kbar, pbar, lane);
+    tape_to_state(tp + tl.x_in, w.n, w.v, NL, NW, lane);
+    __syncwarp();
+    coag_reverse(P, w, a, tb, A.dt, tp, tl, lane);
+    kernel_reverse(P, a, tp + tl.x_in, tp + tl.dki, tp + tl.dkj, tp + tl.pj, NL, NW, lane);
+    for (int e = lane; e < ns; e += 32) xb[e] = e < NL ? a.an[e] : a.av[e - NL];
+    if (lane == 0) {
+      A.kappabar[q] += kbar;
+      A.ssatbar[q] += pbar * c.prs;
+    }
+    __syncwarp();
+  }
+}
+
+// Unit conversions of the adjoint between the boundary (#/kg, kg/kg) and SALSA units.
+__global__ void chain_adj_units(const DevParams P, const ChainArgs A, int to_salsa) {
+  const long long n = (long long)A.ncell * A.nstate;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long q = i / A.nstate;
+    const int e = (int)(i - q * A.nstate);
+    const double dn = A.dn[q];
+    const double rho = e < A.NL ? 1. : P.rholiq[(e - A.NL) / A.NL];
+    if (to_salsa) {
+      A.xbar0[i] = A.xbarN[i] * rho / dn;
+      if (e == 0) { A.kappabar[q] = 0.; A.ssatbar[q] = 0.; }
+    } else {
+      A.xbar0[i] = A.xbar0[i] * dn / rho;
+    }
+  }
 }
 
 }  // namespace
@@ -1345,24 +1386,51 @@ int salsa_gb300_chain_adjoint(salsa_handle_t *h, const salsa_chain_t *c, const d
   if (!ckpt || ckpt_every <= 0 || !xbarN || !xbar0 || !kappabar || !ssatbar) return SALSA_E_ARG;
   A.ckpt = const_cast<double *>(ckpt); A.every = ckpt_every;
   A.xbarN = xbarN; A.xbar0 = xbar0; A.kappabar = kappabar; A.ssatbar = ssatbar;
-  A.ws_doubles = salsa::chain_ws_entries(A.NL, A.NW) + 32 + salsa::adj_ws_doubles(A.NL, A.NW);
-  const int wpb = 4;
-  auto kernel = salsa::chain_adj_kernel;
-  size_t smem = sizeof(double) * ((size_t)P.tab_doubles + (size_t)wpb * A.ws_doubles);
-  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  const int NL = A.NL, NW = A.NW, ns = A.nstate, wpb = 4;
+  const salsa::TapeLayout tl = salsa::tape_layout(NL, NW, A.n1a, salsa::tape_maxit(A.dt));
+  A.tape = (double *)salsa::handle_scratch(h, 0, (size_t)A.ncell * tl.total * sizeof(double));
+  A.seg = ckpt_every > 1
+              ? (double *)salsa::handle_scratch(h, 1, (size_t)ckpt_every * A.ncell * ns * sizeof(double))
+              : nullptr;
+  if (!A.tape || (ckpt_every > 1 && !A.seg)) return SALSA_E_CUDA;
+  // per-kernel shared memory (doubles per warp) and grids
+  const int ws_fwd = salsa::chain_ws_entries(NL, NW) + 32;
+  const int ws_tap = ws_fwd + 9 * NL;
+  const int ws_rev = ns + 6 * NL + salsa::adj_ws_doubles(NL, NW);
+  auto config = [&](auto kernel, int wsd, int *grid, size_t *smem) -> bool {
+    *smem = sizeof(double) * ((size_t)P.tab_doubles + (size_t)wpb * wsd);
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
+      return false;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, 32 * wpb, *smem) != cudaSuccess || bps <= 0)
+      return false;
+    long long g = (long long)bps * nsm, need = (A.ncell + wpb - 1) / wpb;
+    *grid = (int)(g < need ? g : need);
+    return true;
+  };
+  int g_seg = 0, g_tap = 0, g_rev = 0;
+  size_t s_seg = 0, s_tap = 0, s_rev = 0;
+  if (!config(salsa::chain_seg_kernel, ws_fwd, &g_seg, &s_seg) ||
+      !config(salsa::chain_taped_kernel, ws_tap, &g_tap, &s_tap) ||
+      !config(salsa::chain_rev_kernel, ws_rev, &g_rev, &s_rev))
     return SALSA_E_CUDA;
-  int bps = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, 32 * wpb, smem) != cudaSuccess || bps <= 0)
-    return SALSA_E_CUDA;
-  long long grid = (long long)bps * nsm;
-  long long need = (A.ncell + wpb - 1) / wpb;
-  if (grid > need) grid = need;
-  const salsa::TapeLayout tl = salsa::tape_layout(A.NL, A.NW, A.n1a);
-  const size_t nw = (size_t)grid * wpb;
-  A.tape = (double *)salsa::handle_scratch(h, 0, nw * tl.total * sizeof(double));
-  A.seg = (double *)salsa::handle_scratch(h, 1, nw * (size_t)ckpt_every * A.nstate * sizeof(double));
-  if (!A.tape || !A.seg) return SALSA_E_CUDA;
-  kernel<<<(int)grid, 32 * wpb, smem, st>>>(P, A);
+  salsa::chain_adj_units<<<4 * nsm, 256, 0, st>>>(P, A, 1);
+  const int nseg = (A.nsub + A.every - 1) / A.every;
+  for (int sg = nseg - 1; sg >= 0; sg--) {
+    const int k0 = sg * A.every, k1 = A.nsub < k0 + A.every ? A.nsub : k0 + A.every;
+    if (k1 - k0 > 1) {
+      A.ws_doubles = ws_fwd;
+      salsa::chain_seg_kernel<<<g_seg, 32 * wpb, s_seg, st>>>(P, A, sg);
+    }
+    for (int k = k1 - 1; k >= k0; k--) {
+      const double *src = k == k0 ? A.ckpt + (size_t)sg * A.ncell * ns : A.seg + (size_t)(k - k0) * A.ncell * ns;
+      A.ws_doubles = ws_tap;
+      salsa::chain_taped_kernel<<<g_tap, 32 * wpb, s_tap, st>>>(P, A, src);
+      A.ws_doubles = ws_rev;
+      salsa::chain_rev_kernel<<<g_rev, 32 * wpb, s_rev, st>>>(P, A);
+    }
+  }
+  salsa::chain_adj_units<<<4 * nsm, 256, 0, st>>>(P, A, 0);
   if (cudaGetLastError() != cudaSuccess) return SALSA_E_CUDA;
   return chain_finish(A, st);
 }
