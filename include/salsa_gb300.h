@@ -177,15 +177,21 @@ int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
                           int initialize, const salsa_fields_t *f, void *stream,
                           int sync, salsa_status_t *st);
 
-/* No counterpart in the reference.  Same as salsa_gb300_run_async, but the call
- * allocates nothing: the cell-order list and the status counters sit in module
- * memory of the library (a static device array sized for SALSA_NOALLOC_MAXCELLS
- * = 2,097,152 interior cells; larger grids return SALSA_E_ARG).  The call clears
- * the status counters on the stream before the step.  The first call on a handle
- * resolves the module scratch of the handle's device (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls on one device share the
- * scratch: calls that overlap in time (other streams, other handles on the same
- * device) race on it and must be serialised by the caller.  Device pointers only. */
+/* No counterpart in the reference.  The step for callers that must not allocate GPU
+ * memory: a model that gives all free device memory to its own pool at start-up (a
+ * later cudaMalloc then fails), or one whose time loop cannot afford the
+ * device-wide synchronisation that cudaMalloc and cudaFree imply.  Same arguments
+ * and results as salsa_gb300_run_async (device pointers only), but the scratch the
+ * step needs -- the cell-order list and the status counters -- sits in a static
+ * device array of the library: 8 MiB, enough for SALSA_NOALLOC_MAXCELLS =
+ * 2,097,152 interior cells (larger grids return SALSA_E_ARG).  Every GPU that loads
+ * the library holds that array until the process exits.  The array keeps the last
+ * call's contents; each call clears the status counters on its stream and rewrites
+ * the whole order list.  The first call on a handle looks up the array's device
+ * address on the handle's device (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls on one device share the array: calls that overlap
+ * on the GPU (other streams, other handles on that device) race on it, so the
+ * caller must serialise them. */
 #define SALSA_NOALLOC_MAXCELLS 2097152
 int salsa_gb300_run_noalloc(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
                             double tstep, double time, int istp, int level, int lcharge,

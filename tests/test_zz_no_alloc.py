@@ -1,9 +1,12 @@
-"""salsa_gb300_run_noalloc: the step with module scratch instead of allocations.
+"""salsa_gb300_run_noalloc: the step for callers that cannot allocate GPU memory.
 
-Two calls in a row on the same inputs must reproduce salsa_gb300_run_async bit for
-bit (outputs, in-place IN deficit and status counts); the second call checks that
-the counters and the order list are cleared between calls.  The file is collected
-last so that it also runs after every other GPU test in one session.
+An LES that hands its GPU memory to its own pool, or whose time loop cannot take
+the synchronisation of cudaMalloc, calls this entry point; it keeps its scratch in
+a static device array of the library instead of allocating.  Two calls in a row on
+the same inputs must reproduce salsa_gb300_run_async bit for bit (outputs,
+in-place IN deficit and status counts); the second call checks that the counters
+and the order list left by the first call do not leak into it.  The file is
+collected last so that it also runs after every other GPU test in one session.
 """
 import ctypes as C
 

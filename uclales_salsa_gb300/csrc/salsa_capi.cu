@@ -34,9 +34,12 @@ int blocks_per_sm_f1(const DevParams &);
 using salsa::DevParams;
 using salsa::Row;
 
-// Scratch of salsa_gb300_run_noalloc: the cell-order list and the status counters live
-// in module memory, so that entry point allocates nothing.  SALSA_NOALLOC_MAXCELLS
-// (header) bounds the interior cells of one call (8 MiB of order list).
+// Scratch of salsa_gb300_run_noalloc, the step for callers that cannot allocate GPU
+// memory (their own pool holds it, or cudaMalloc's device-wide synchronisation would
+// stall their time loop): the cell-order list and the status counters live in module
+// memory.  SALSA_NOALLOC_MAXCELLS (header) bounds the interior cells of one call.
+// Host code must not take these names as device addresses: it looks the addresses up
+// with cudaGetSymbolAddress on the handle's device.
 static __device__ __align__(256) int g_na_order[SALSA_NOALLOC_MAXCELLS];
 static __device__ __align__(256) unsigned long long g_na_status[salsa::ST_N];
 
