@@ -1023,6 +1023,7 @@ struct EqJob {
   int kk, count;
   bool r2;
   double tol, zrh, zke, numc, zv0, zv1, zv4, zvp56, zcore, zdwet, zdold, zlwc;
+  double q0, q1, q4, p56, pc;   // per-bin invariants of the iteration (same operations, computed once)
 };
 
 template <typename KT>
@@ -1035,27 +1036,35 @@ __device__ __forceinline__ void eq_load(const DevParams &P, const WS<KT> &w, int
   for (int i = 0; i < 7; i++) zvp[i] = zvolc_of(P, w, i, b) / j.numc;
   j.zcore = j.r2 ? (zvp[0] + zvp[1] + zvp[2] + zvp[3] + zvp[4]) : (zvp[0] + zvp[1]);
   j.zvp56 = zvp[5] + zvp[6];
+  {
+    const double rhosu_msu = 1830. / 98.08e-3, rhooc_moc = 1400. / 150.e-3, rhoss_mss = 2165. / 58.44e-3;
+    j.q0 = j.zv0 * rhosu_msu;
+    j.q1 = K_EPSOC * j.zv1 * rhooc_moc;
+    j.q4 = j.zv4 * rhoss_mss;
+    j.p56 = j.zvp56 / K_PI6;
+    j.pc = j.zcore / K_PI6;
+  }
   j.zdwet = w.dwet[b];
   j.zdold = 1.;
   j.zlwc = 0.;
 }
 
-// one pass of the equil_iterate loop body (same operations in the same order)
-__device__ __forceinline__ void eq_step(EqJob &j, double T) {
-  const double rhosu_msu = 1830. / 98.08e-3, rhooc_moc = 1400. / 150.e-3, rhoss_mss = 2165. / 58.44e-3;
+// one pass of the equil_iterate loop body (same operations in the same order; the
+// per-bin invariants q*, p* and kT = K_BOLTZ * T are computed once)
+__device__ __forceinline__ void eq_step(EqJob &j, double kT) {
   j.zdold = fmax(j.zdwet, 1.e-20);
   double zaw = j.zrh / j.zke;
   double a2 = zaw * zaw, a3 = a2 * zaw, a4 = a2 * a2;
   double bm1 = +1.1065495e+2 - 3.6759197e+2 * zaw + 5.0462934e+2 * a2 - 3.1543839e+2 * a3 + 6.770824e+1 * a4;
   double bm2 = 1. / (zaw * K_MWA) - 1. / K_MWA;
-  double zlwc = (j.zv0 * rhosu_msu) / bm1 + K_EPSOC * j.zv1 * rhooc_moc / bm2;
+  double zlwc = j.q0 / bm1 + j.q1 / bm2;
   if (j.r2) {
     double bm5 = +5.875248e+1 - 1.8781997e+2 * zaw + 2.7211377e+2 * a2 - 1.8458287e+2 * a3 + 4.153689e+1 * a4;
-    zlwc += (j.zv4 * rhoss_mss) / bm5;
+    zlwc += j.q4 / bm5;
   }
   j.zlwc = zlwc;
-  j.zdwet = cbrt(zlwc / j.numc / K_RHOWA / K_PI6 + j.zvp56 / K_PI6 + j.zcore / K_PI6);
-  j.zke = exp(2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T * j.zdwet));
+  j.zdwet = cbrt(zlwc / j.numc / K_RHOWA / K_PI6 + j.p56 + j.pc);
+  j.zke = exp(2. * K_SURFW0 * K_MVWA / (kT * j.zdwet));
   j.count++;
 }
 
@@ -1075,6 +1084,7 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   int nonconv = 0;
   const int n2 = init ? P.fn2b - P.in2a + 1 : 0;
+  const double kT = K_BOLTZ * T;
   if (n2 <= 31) {
     // lane 31: the regime-1a chain in bin order; lanes 0..n2-1: regime-2 bins
     EqJob j;
@@ -1096,7 +1106,7 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
       if (j.kk >= 0) {
         bool go = fabs(j.zdwet / j.zdold - 1.) > j.tol;
         if (go) {
-          eq_step(j, T);
+          eq_step(j, kT);
           if (j.count > 100) { nonconv = 1; go = false; }
         }
         if (!go) {
