@@ -1,0 +1,100 @@
+"""GPU parity of the step's less common paths (FP64 form against the oracle).
+
+Each case changes one part of the configuration or of the call on a small block of
+a workload: the classic ice nucleation (mo_salsa_cloud_ice.f90:26-140), every SE
+freezing mode, ice melting (mo_salsa_cloud_ice.f90:393-462), the second
+autoconversion mode (mo_salsa_cloud.f90 autoconv2), the charging enhancement of the
+collision kernels (mo_salsa_coagulation_kernels.f90:411-416), the initialising call
+(run_SALSA with initialize=.TRUE.) and a step without coagulation.  The criterion is
+the one of test_gpu_parity.py.
+"""
+import pytest
+import torch
+
+from uclales_salsa_gb300.inputs import make_inputs, make_outputs
+from uclales_salsa_gb300.api import SalsaStep
+from oracle_ref import Oracle
+from test_gpu_parity import check, VIOL_FRAC, FRAC_WITHIN, PERTURBED
+
+pytestmark = pytest.mark.gpu
+
+
+def _classic_ice(inp, f):
+    c = inp.cfg
+    c.ice_theta_dist = 0
+    c.lsicehom = c.lsiceimm = c.lsicedep = 1
+
+
+def _se_all_modes(inp, f):
+    c = inp.cfg
+    c.lsicehom = c.lsiceimm = c.lsicedep = 1
+
+
+def _melting(inp, f):
+    f["temp"] += 12.0          # part of the ice now sits above 273.15 K
+    inp.cfg.lsicemelt.sw = 1
+
+
+def _autoconv2(inp, f):
+    inp.cfg.lsauto.mode = 2
+
+
+def _no_coag(inp, f):
+    inp.cfg.lscoag.sw = 0
+
+
+def _charge(inp, f):
+    lay = inp.layout
+    g = torch.Generator().manual_seed(5)
+    shp = (lay.nbins + lay.ncld + lay.nprc,) + tuple(f["press"].shape)
+    f["chargeTime"] = torch.rand(shp, generator=g, dtype=torch.float64) * inp.cfg.chargeTMax
+    inp.cfg.chargeCollEnh = 2.0   # the default 0 would switch the enhancement off
+
+
+CASES = [
+    ("classic_ice", "grid384x384x160", dict(X=12, Y=12, Z=8), _classic_ice, {}),
+    ("se_all_modes", "grid384x384x160", dict(X=12, Y=12, Z=8), _se_all_modes, {}),
+    ("melting", "grid384x384x160", dict(X=12, Y=12, Z=8), _melting, {}),
+    ("autoconv2", "grid256x256x128", dict(X=8, Y=8, Z=16), _autoconv2, {}),
+    ("no_coagulation", "grid256x256x128", dict(X=8, Y=8, Z=16), _no_coag, {}),
+    ("charge", "grid256x256x128", dict(X=8, Y=8, Z=16), _charge, dict(lcharge=1)),
+    ("initialize", "grid16x16x40", dict(X=8, Y=8, Z=16), lambda inp, f: None, dict(initialize=1)),
+]
+
+
+def _oracle(inp, fields, kw, pf=None, eps=0.0):
+    f = {k: v.clone() for k, v in fields.items()}
+    if pf:
+        f[pf] = f[pf] * (1 + eps)
+    out = make_outputs(inp)
+    rc, st = Oracle(inp.cfg).run(inp, f, out, time=1.0, **kw)
+    assert rc == 0, st.as_dict()
+    return out
+
+
+@pytest.mark.parametrize("name,wl,kw,mod,call", CASES, ids=[c[0] for c in CASES])
+def test_variant_parity(name, wl, kw, mod, call):
+    inp = make_inputs(wl, "cpu", precision=0, **kw)
+    fields = {k: v.clone() for k, v in inp.fields.items()}
+    mod(inp, fields)
+    inp.fields = fields
+    ref = _oracle(inp, fields, call)
+    env = {k: torch.zeros_like(v) for k, v in ref.items()}
+    for pf in PERTURBED:
+        for sgn in (1.0, -1.0):
+            o = _oracle(inp, fields, call, pf, sgn * 2.2e-16)
+            for k in env:
+                env[k] = torch.maximum(env[k], (o[k] - ref[k]).abs())
+    f = {k: v.clone().cuda() for k, v in fields.items()}
+    out = {k: v.cuda() for k, v in make_outputs(inp).items()}
+    step = SalsaStep(inp.cfg)
+    rc, st = step.run(inp, f, out, time=1.0, **call)
+    torch.cuda.synchronize()
+    assert rc == 0, (name, st.as_dict())
+    gpu = {k: v.cpu() for k, v in out.items()}
+    step.close()
+    rep = check(inp, gpu, ref, env, 1e-10)
+    print(name, rep)
+    for k, r in rep.items():
+        assert r["violations"] <= VIOL_FRAC * r["n"], (name, k, r)
+        assert r["frac_within"] >= FRAC_WITHIN, (name, k, r)
