@@ -28,6 +28,21 @@
 #include "salsa_dual.cuh"
 #include "salsa_internal.h"
 
+// Sub-stage clocks of the instrumented build (stage_profile --chain): a warp adds the
+// clock64() delta since the previous mark to counter k.
+#ifdef SALSA_STAGE_TIMERS
+#define SUB_BEGIN() long long t_sub = clock64()
+#define SUB_MARK(k)                                                                               \
+  do {                                                                                            \
+    long long t_ = clock64();                                                                     \
+    if (lane == 0 && P.stage_clocks) atomicAdd(P.stage_clocks + (k), (unsigned long long)(t_ - t_sub)); \
+    t_sub = t_;                                                                                   \
+  } while (0)
+#else
+#define SUB_BEGIN() do { } while (0)
+#define SUB_MARK(k) do { } while (0)
+#endif
+
 namespace salsa {
 namespace {
 
@@ -108,7 +123,7 @@ __device__ __forceinline__ CW<R> make_cw(R *base, int NL, int NW) {
 // ---- tape of one step (global memory, doubles, per cell) ----
 enum { TP_MAXEQ = 104 };
 struct TapeLayout {
-  int x_in, x_pre, x_mid, x_eq, sums, pj, K, dki, dkj, eq, hist_zc, hist_c, hist_w, nit, maxit, total;
+  int x_in, x_pre, x_mid, x_eq, sums, K, dki, dkj, eq, hist_zc, hist_c, hist_w, nit, maxit, total;
 };
 // maxit: substep rows of the condensation history (the loop count plus the final row)
 __host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n1a, int maxit) {
@@ -120,8 +135,7 @@ __host__ __device__ __forceinline__ TapeLayout tape_layout(int NL, int NW, int n
   t.x_mid = t.x_pre + ns;
   t.x_eq = t.x_mid + ns;
   t.sums = t.x_eq + ns;                     // per coagulation target: sink, self, src[NSV]
-  t.pj = t.sums + NL * (2 + SALSA_NSV);     // kernel reverse: K-bar * dK/dd_j per pair
-  t.K = t.pj + tr;                          // collision kernels of the step
+  t.K = t.sums + NL * (2 + SALSA_NSV);      // collision kernels of the step
   t.dki = t.K + tr;                         // dK/dd_i and dK/dd_j of every pair (i <= j)
   t.dkj = t.dki + tr;
   t.eq = t.dkj + tr;                        // per 1a bin: [count, zke_0 .. zke_count]
@@ -190,6 +204,76 @@ __device__ __forceinline__ void chain_load_props(const R *S, int NL, int b, BinP
   o.schm = S[8 * NL + b];
 }
 
+// Populated bins (number at or above the bin's limit), compacted into pbuf in bin order;
+// returns their count.  Bins below the limit have no collision properties and every
+// pair with such a bin has K = 0 (the step kernel's build_kernels does the same).
+template <typename R>
+__device__ __forceinline__ int chain_active_bins(const DevParams &P, const CW<R> &w, int lane) {
+  const unsigned lt = (1u << lane) - 1u;
+  int nact = 0;
+  for (int base = 0; base < w.NL; base += 32) {
+    const int b = base + lane;
+    const bool act = b < w.NL && val(w.n[b]) >= nlim_of(phase_of(P, b));
+    const unsigned bal = __ballot_sync(0xffffffffu, act);
+    if (act) w.pbuf[nact + __popc(bal & lt)] = b;
+    nact += __popc(bal);
+  }
+  __syncwarp();
+  return nact;
+}
+
+// Scans the pair table section by section (pairs of unequal, then of equal bin sizes),
+// compacts the pairs of two populated bins into pbuf and calls f(sec, pair) for 32 of
+// them at a time, one per lane, then for the rest; zero(pair) is called for the pairs
+// with an empty bin.  Lanes never idle on an empty pair.
+template <typename R, typename F, typename Z>
+__device__ __forceinline__ void chain_pairs(const DevParams &P, const CW<R> &w, int lane, F f, Z zero) {
+  const unsigned lt = (1u << lane) - 1u;
+  for (int sec = 0; sec < 2; sec++) {
+    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
+    int nbuf = 0;
+    for (int base = p0; base < p1; base += 32) {
+      const int t = base + lane;
+      bool act = false;
+      int pk = 0;
+      if (t < p1) {
+        pk = __ldg(P.pairs + t);
+        const int i = pk & 0xff, j = (pk >> 8) & 0xff;
+        act = val(w.n[i]) >= nlim_of(phase_of(P, i)) && val(w.n[j]) >= nlim_of(phase_of(P, j));
+        if (!act) zero(pk);
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (act) w.pbuf[nbuf + __popc(bal & lt)] = pk;
+      nbuf += __popc(bal);
+      __syncwarp();
+      if (nbuf >= 32) {
+        f(sec, w.pbuf[nbuf - 32 + lane]);
+        nbuf -= 32;
+        __syncwarp();
+      }
+    }
+    if (lane < nbuf) f(sec, w.pbuf[lane]);
+    __syncwarp();
+  }
+}
+
+// Collision properties of populated bin b, and the kernel of its pairs of equal bin size
+// (coagc :273-276: the first particle of such a pair is taken 1.1 times larger and 1.33
+// times heavier).  For liquid bins that first particle's properties depend on bin j of
+// the pair alone: terminal_vel takes the same branch for every liquid phase and the
+// sphere-equivalent diameter enters only for ice.  So every equal-size pair (i, j) of the
+// chain's liquid bins has the kernel of bin j, evaluated once per bin here.
+template <typename R>
+__device__ __forceinline__ R chain_bin_props(const DevParams &P, const CoagCell<R> &cc, int b, R d, BinProps<R> &o) {
+  Shape<R> sh;
+  sh.alpha = sh.beta = sh.gamma = sh.sigma = R(0.);
+  const R mass = R(K_RHOWA * K_PI6) * cube(d);
+  bin_props<R>(cc, phase_of(P, b), d, d, mass, R(K_RHOWA), sh, o);
+  BinProps<R> big;
+  bin_props<R>(cc, phase_of(P, b), R(1.1) * d, d, R(1.33) * mass, R(K_RHOWA), sh, big);
+  return coag_pair<R>(cc, big, o);
+}
+
 // diameters at the start of the coagulation, collision properties and kernels
 template <typename R>
 __device__ void chain_kernels(const DevParams &P, const CW<R> &w, const double *tb, double T, double pres, int lane) {
@@ -198,46 +282,29 @@ __device__ void chain_kernels(const DevParams &P, const CW<R> &w, const double *
   const CoagCell<R> cc = chain_coagcell<R>(T, pres, P);
   for (int b = lane; b < NL; b += 32) w.dw[b] = liquid_dwet(P, w, dmid, b);
   __syncwarp();
-  for (int b = lane; b < NL; b += 32) {
-    const int ph = phase_of(P, b);
-    if (!(val(w.n[b]) >= nlim_of(ph))) continue;
-    Shape<R> sh;
-    sh.alpha = sh.beta = sh.gamma = sh.sigma = R(0.);
-    const R mass = R(K_RHOWA * K_PI6) * cube(w.dw[b]);
+  R *keq = w.kel;   // equal-size kernel per bin (the condensation rows are free here)
+  const int nact = chain_active_bins(P, w, lane);
+  for (int e = lane; e < nact; e += 32) {
+    const int b = w.pbuf[e];
     BinProps<R> o;
-    bin_props<R>(cc, ph, w.dw[b], w.dw[b], mass, R(K_RHOWA), sh, o);
+    keq[b] = chain_bin_props<R>(P, cc, b, w.dw[b], o);
     chain_store_props<R>(w.S, NL, b, o);
   }
   __syncwarp();
-  const unsigned lt = (1u << lane) - 1u;
-  for (int sec = 0; sec < 2; sec++) {
-    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
-    for (int base = p0; base < p1; base += 32) {
-      const int t = base + lane;
-      bool act = false;
-      int i = 0, j = 0;
-      if (t < p1) {
-        const int pk = __ldg(P.pairs + t);
-        i = pk & 0xff; j = (pk >> 8) & 0xff;
-        act = val(w.n[i]) >= nlim_of(phase_of(P, i)) && val(w.n[j]) >= nlim_of(phase_of(P, j));
-        if (!act) w.Kij(i, j) = R(0.);
-      }
-      (void)lt;
-      if (act) {
-        BinProps<R> a, bb;
-        chain_load_props<R>(w.S, NL, j, bb);
+  chain_pairs(
+      P, w, lane,
+      [&](int sec, int pk) {
+        const int i = pk & 0xff, j = (pk >> 8) & 0xff;
         if (sec == 1) {
-          Shape<R> sh;
-          sh.alpha = sh.beta = sh.gamma = sh.sigma = R(0.);
-          const R dj = w.dw[j], mj = R(K_RHOWA * K_PI6) * cube(w.dw[j]);
-          bin_props<R>(cc, phase_of(P, i), R(1.1) * dj, w.dw[i], R(1.33) * mj, R(K_RHOWA), sh, a);
-        } else {
-          chain_load_props<R>(w.S, NL, i, a);
+          w.K[tri(i, j, NL)] = keq[j];
+          return;
         }
-        w.Kij(i, j) = coag_pair<R>(cc, a, bb);
-      }
-    }
-  }
+        BinProps<R> a, bb;
+        chain_load_props<R>(w.S, NL, i, a);
+        chain_load_props<R>(w.S, NL, j, bb);
+        w.K[tri(i, j, NL)] = coag_pair<R>(cc, a, bb);
+      },
+      [&](int pk) { w.K[tri(pk & 0xff, (pk >> 8) & 0xff, NL)] = R(0.); });
   __syncwarp();
 }
 
@@ -260,11 +327,25 @@ __device__ __forceinline__ void chain_apply(const CW<R> &w, int t, int nspec, do
   __syncwarp();
 }
 
+// warp totals of the sums of one target; in FP64 the eight sums share one transposed
+// butterfly (warp_sum8: the same addition tree as g_wsum, so the same totals)
 template <typename R>
-__device__ __forceinline__ void chain_reduce(R (&src)[SALSA_NSV], R &sink, R &self) {
+__device__ __forceinline__ void chain_reduce(R (&src)[SALSA_NSV], R &sink, R &self, int lane) {
+  static_assert(SALSA_NSV == 7, "src and sink fill the eight slots of warp_sum8");
+  if constexpr (std::is_same<R, double>::value) {
+    double v[8];
 #pragma unroll
-  for (int s = 0; s < SALSA_NSV; s++) src[s] = g_wsum(src[s]);
-  sink = g_wsum(sink);
+    for (int s = 0; s < 7; s++) v[s] = src[s];
+    v[7] = sink;
+    warp_sum8(v, lane);
+#pragma unroll
+    for (int s = 0; s < 7; s++) src[s] = v[s];
+    sink = v[7];
+  } else {
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = g_wsum(src[s]);
+    sink = g_wsum(sink);
+  }
   self = shfl_idx(self, 0);
 }
 
@@ -321,7 +402,7 @@ __device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const doub
           if (s < nspec) src[s] += k * w.V(s, g);
       }
     }
-    chain_reduce(src, sink, self);
+    chain_reduce(src, sink, self, lane);
     tape_sums(ts, kk, src, sink, self, lane);
     chain_apply(w, kk, nspec, dt, src, sink, self, lane);
   }
@@ -346,7 +427,7 @@ __device__ void chain_coag_update(const DevParams &P, const CW<R> &w, const doub
         for (int s = 0; s < SALSA_NSV; s++)
           if (s < nspec) src[s] += k * w.V(s, g);
       });
-      chain_reduce(src, sink, self);
+      chain_reduce(src, sink, self, lane);
       tape_sums(ts, tg, src, sink, self, lane);
       chain_apply(w, tg, nspec, dt, src, sink, self, lane);
     }
@@ -465,6 +546,7 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
   const int NL = w.NL, iwa = P.iwa;
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   const double T = c.T, pres = c.pres, prs = c.prs;
+  SUB_BEGIN();
   R prv = c.prv0;
   const R zrh = prv / prs;
   R l1 = R(0.);
@@ -508,6 +590,7 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
     w.cw[b] = w.V(iwa, b) * K_RHOWA / K_MWA;
   }
   __syncwarp();
+  SUB_MARK(5);
   bool a = false, cl = false, pr = false;
   for (int b = lane; b < NL; b += 32) {
     const int ph = phase_of(P, b);
@@ -567,6 +650,7 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
   __syncwarp();
   for (int b = lane; b < NL; b += 32) w.V(iwa, b) = fmax(R(0.), w.cw[b] * K_MWA / K_RHOWA);
   __syncwarp();
+  SUB_MARK(6);
   return counter;
 }
 
@@ -583,16 +667,16 @@ __device__ void chain_kernels_taped(const DevParams &P, const CW<double> &w, con
   for (int b = lane; b < NL; b += 32) w.dw[b] = liquid_dwet(P, w, dmid, b);
   for (int e = lane; e < chain_tri(NL); e += 32) { dki[e] = 0.; dkj[e] = 0.; }
   __syncwarp();
-  for (int b = lane; b < NL; b += 32) {
-    const int ph = phase_of(P, b);
-    if (!(w.n[b] >= nlim_of(ph))) continue;
+  double *keq = w.kel, *dkeq = w.surf;   // equal-size kernel per bin and its d-derivative
+  const int nact = chain_active_bins(P, w, lane);
+  for (int e = lane; e < nact; e += 32) {
+    const int b = w.pbuf[e];
     Dual<1> d(w.dw[b]);
     d.d[0] = 1.;
-    Shape<Dual<1>> sh;
-    sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<1>(0.);
-    const Dual<1> mass = Dual<1>(K_RHOWA * K_PI6) * cube(d);
     BinProps<Dual<1>> o;
-    bin_props<Dual<1>>(c1, ph, d, d, mass, Dual<1>(K_RHOWA), sh, o);
+    const Dual<1> k = chain_bin_props<Dual<1>>(P, c1, b, d, o);
+    keq[b] = k.v;
+    dkeq[b] = k.d[0];
     const Dual<1> *po = &o.diam;
     for (int k = 0; k < 9; k++) { w.S[k * NL + b] = po[k].v; drow[k * NL + b] = po[k].d[0]; }
   }
@@ -605,32 +689,26 @@ __device__ void chain_kernels_taped(const DevParams &P, const CW<double> &w, con
       po[k] = x;
     }
   };
-  for (int sec = 0; sec < 2; sec++) {
-    const int p0 = sec == 0 ? 0 : P.npairs_plain, p1 = sec == 0 ? P.npairs_plain : P.npairs;
-    for (int t = p0 + lane; t < p1; t += 32) {
-      const int pk = __ldg(P.pairs + t);
-      const int i = pk & 0xff, j = (pk >> 8) & 0xff;
-      const int ti = tri(i, j, NL);
-      const bool act = w.n[i] >= nlim_of(phase_of(P, i)) && w.n[j] >= nlim_of(phase_of(P, j));
-      if (!act) { w.K[ti] = 0.; continue; }
-      BinProps<Dual<2>> A_, B_;
-      lift(j, 1, B_);
-      if (sec == 1) {
-        Shape<Dual<2>> sh;
-        sh.alpha = sh.beta = sh.gamma = sh.sigma = Dual<2>(0.);
-        Dual<2> dj(w.dw[j]), di(w.dw[i]);
-        dj.d[1] = 1.; di.d[0] = 1.;
-        const Dual<2> mj = Dual<2>(K_RHOWA * K_PI6) * cube(dj);
-        bin_props<Dual<2>>(c2, phase_of(P, i), Dual<2>(1.1) * dj, di, Dual<2>(1.33) * mj, Dual<2>(K_RHOWA), sh, A_);
-      } else {
+  chain_pairs(
+      P, w, lane,
+      [&](int sec, int pk) {
+        const int i = pk & 0xff, j = (pk >> 8) & 0xff;
+        const int ti = tri(i, j, NL);
+        if (sec == 1) {   // the equal-size kernel depends on bin j alone
+          w.K[ti] = keq[j];
+          dki[ti] = 0.;
+          dkj[ti] = dkeq[j];
+          return;
+        }
+        BinProps<Dual<2>> A_, B_;
         lift(i, 0, A_);
-      }
-      const Dual<2> k = coag_pair<Dual<2>>(c2, A_, B_);
-      w.K[ti] = k.v;
-      dki[ti] = k.d[0];
-      dkj[ti] = k.d[1];
-    }
-  }
+        lift(j, 1, B_);
+        const Dual<2> k = coag_pair<Dual<2>>(c2, A_, B_);
+        w.K[ti] = k.v;
+        dki[ti] = k.d[0];
+        dkj[ti] = k.d[1];
+      },
+      [&](int pk) { w.K[tri(pk & 0xff, (pk >> 8) & 0xff, NL)] = 0.; });
   __syncwarp();
   for (int e = lane; e < chain_tri(NL); e += 32) Kt[e] = w.K[e];
   __syncwarp();
@@ -647,19 +725,25 @@ __device__ int chain_step(const DevParams &P, const CW<R> &w, const double *tb, 
   bool pr = false;
   for (int b = P.nbins + P.ncld + lane; b < NL; b += 32) pr |= val(w.n[b]) >= K_PRLIM;
   if (warp_any(pr) || !(val(c.prv0) / c.prs >= 0.98)) return 1;
+#ifdef SALSA_STAGE_TIMERS
+  long long t_stage = clock64();
+#endif
   if constexpr (std::is_same<R, double>::value) {
     if (tp) chain_kernels_taped(P, w, tb, c.T, c.pres, drow, tp + tl.K, tp + tl.dki, tp + tl.dkj, lane);
     else chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
   } else {
     chain_kernels<R>(P, w, tb, c.T, c.pres, lane);
   }
+  STAGE_MARK(11);
   chain_coag_update<R>(P, w, tb, dt, lane, tp ? tp + tl.sums : nullptr);
   __syncwarp();
   if (tp) state_to_tape(tp + tl.x_pre, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
   chain_coag_clamp<R>(P, w, lane);
   if (tp) state_to_tape(tp + tl.x_mid, (const double *)w.n, nullptr, NL * (1 + NW), 0, lane);
   __syncwarp();
+  STAGE_MARK(12);
   chain_condensation<R>(P, w, tb, c, dt, tp, tl, lane);
+  STAGE_MARK(13);
   return 0;
 }
 
@@ -766,8 +850,7 @@ __global__ void __launch_bounds__(128, 2) chain_fwd_kernel(const DevParams P, co
 // Adjoint (R = double).  Shared-memory adjoint workspace per warp:
 //   an[NL], av[NW][NL]   adjoint of the state (the "new" slot during the coagulation reverse)
 //   on[NL], ov[NW][NL]   adjoint of the state entering the coagulation sweep ("old" slot)
-//   Kb[tri]              adjoint of K; then K-bar * dK/dd_i per pair (K-bar * dK/dd_j goes
-//                        to the tape's pj rows)
+//   Kb[tri]              adjoint of K; then K-bar * dK/dd_i per pair
 //   cb, wb, mtb, kelb, znsb [NL]   adjoints of the condensation quantities
 // =======================================================================================
 struct AW {
@@ -807,6 +890,7 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
   const double T = c.T, pres = c.pres, prs = c.prs;
   const double D = pres * K_MAIR / (K_RG * T);
   const int nit = (int)tp[tl.nit];
+  SUB_BEGIN();
   // state after the water uptake (x_eq)
   tape_to_state(tp + tl.x_eq, w.n, w.v, NL, NW, lane);
   __syncwarp();
@@ -857,6 +941,7 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
     __syncwarp();
     double zcb = 0., zcwtotb = 0., mtotb = 0.;
     const double adt = 2.e-2;
+    const double izh2 = 1. / (1. + adt * mtot);   // the substeps' constant denominator
     for (int it = nit - 1; it >= 0; it--) {
       const double zc_in = tp[tl.hist_zc + it];
       const double *cin = tp + tl.hist_c + it * NL, *win = tp + tl.hist_w + it * NL;
@@ -890,9 +975,9 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
         const double ab = gw * kel;
         if (r > 0.1) {
           if (ci + zns > K_EPS) {
-            const double d2 = (ci + zns) * (ci + zns);
-            cib += ab * zns / d2;
-            a.znsb[b] += -ab * ci / d2;
+            const double id = 1. / (ci + zns), q2 = ab * id * id;
+            cib += q2 * zns;
+            a.znsb[b] += -q2 * ci;
           } else {
             cib += ab / K_EPS;
           }
@@ -909,8 +994,8 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
       const double zcwintb = wsum(zib);
       double qb = 0.;
       if (zcwtot < q) zcwtotb += zcwintb; else qb = zcwintb;
-      const double zhlp1b = qb / zhlp2;
-      const double zhlp2b = -qb * q / zhlp2;
+      const double zhlp1b = qb * izh2;
+      const double zhlp2b = -qb * q * izh2;
       mtotb += zhlp2b * adt;
       zcb = zhlp1b;
       const double spb = zhlp1b * adt;
@@ -928,6 +1013,7 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
     zcb += zcwtotb;
     prv_adj_bar = zcb * cc.rhoair / K_MWA;
     __syncwarp();
+    SUB_MARK(0);
     // coefficients (x_eq state): cw0, zns, and kel/ws/mt through dual numbers
     double kb_l = 0.;
     for (int b = lane; b < NL; b += 32) {
@@ -971,62 +1057,110 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
     }
     kbar += wsum(kb_l);
     __syncwarp();
+    SUB_MARK(1);
   }
   // prv_adj = prv0 - (zaelwc2 - zaelwc1) / D
   pbar += prv_adj_bar;
   const double zael2b = -prv_adj_bar / D, zael1b = prv_adj_bar / D;
   for (int b = lane; b <= P.fn2b; b += 32) a.AV(iwa, b) += zael2b * K_RHOWA;
   __syncwarp();
-  // regime-1a water uptake reverse (bins in reverse order, zke chained)
-  if (lane == 0) {
+  // Regime-1a water uptake reverse.  The forward iterates zke_{i+1} = f(zke_i; bin) through
+  // the 1a bins in order, carrying zke from bin to bin; the tape holds every iterate.  The
+  // local partials of the iterations are independent of one another, so lanes evaluate
+  // them in parallel (Dual<5>, 32 iterations at a time, in reverse order: bins fn1a ..
+  // in1a, iterations cnt .. 1).  The adjoint of zke then runs through each chunk serially,
+  // and the input adjoints of every bin are warp sums of its iterations' terms.
+  {
+    const int n1a = P.fn1a - P.in1a + 1;
+    const double *xm = tp + tl.x_mid;
+    const Dual<5> zrhd(fmin(fmax(zrh, 0.05), 0.98));
+    auto eq_of = [&](int r) { return tp + tl.eq + (P.fn1a - r - P.in1a) * TP_MAXEQ; };
+    int total = 0;
+    for (int r = 0; r < n1a; r++) total += eq_of(r)[0] > 0. ? (int)eq_of(r)[0] : 0;
+    double tot[4] = {0., 0., 0., 0.};   // lane r < n1a: sums for bin fn1a - r (zv0, zv1, numc, zcore)
     double zkeb = 0.;
-    for (int kk = P.fn1a; kk >= P.in1a; kk--) {
-      const double *te = tp + tl.eq + (kk - P.in1a) * TP_MAXEQ;
-      if (te[0] < 0.) continue;
-      const int cnt = (int)te[0];
-      double zlwcb = a.AV(iwa, kk) / K_RHOWA;
-      a.AV(iwa, kk) = 0.;
-      if (cnt == 0) continue;
-      // x_mid values of the bin (the tape's x_mid)
-      const double *xm = tp + tl.x_mid;
-      const double numc = xm[kk];
-      const int ix_so4 = P.ix_so4, ix_oc = P.ix_oc;
-      const double zv0 = ix_so4 >= 0 ? xm[NL + ix_so4 * NL + kk] : 0.;
-      const double zv1 = ix_oc >= 0 ? xm[NL + ix_oc * NL + kk] : 0.;
-      const double zcore = zv0 / numc + zv1 / numc;
-      double zv0b = 0., zv1b = 0., numcb = 0., zcoreb = 0.;
-      const Dual<5> zrhd(fmin(fmax(zrh, 0.05), 0.98));
-      for (int i = cnt; i >= 1; i--) {
-        Dual<5> zke(te[1 + (i - 1)]), d0(zv0), d1(zv1), dnm(numc), dco(zcore);
+    for (int base = 0; base < total; base += 32) {
+      const int f = base + lane;
+      int r = -1;
+      double p[5] = {0., 0., 0., 0., 0.}, q[5] = {0., 0., 0., 0., 0.};
+      if (f < total) {
+        int rem = f, cnt = 0;
+        for (r = 0; r < n1a; r++) {
+          cnt = eq_of(r)[0] > 0. ? (int)eq_of(r)[0] : 0;
+          if (rem < cnt) break;
+          rem -= cnt;
+        }
+        const int i = cnt - rem, kk = P.fn1a - r;
+        const double *te = eq_of(r);
+        const double numc = xm[kk];
+        const double zv0 = P.ix_so4 >= 0 ? xm[NL + P.ix_so4 * NL + kk] : 0.;
+        const double zv1 = P.ix_oc >= 0 ? xm[NL + P.ix_oc * NL + kk] : 0.;
+        const double zcore = zv0 / numc + zv1 / numc;
+        Dual<5> zke(te[i]), d0(zv0), d1(zv1), dnm(numc), dco(zcore);
         zke.d[0] = 1.; d0.d[1] = 1.; d1.d[2] = 1.; dnm.d[3] = 1.; dco.d[4] = 1.;
         Dual<5> zlwc, zd;
         eq1a_iter(zrhd, zke, d0, d1, dnm, Dual<5>(0.), dco, T, zlwc, zd);   // zke is now zke_i
-        const double lb = (i == cnt) ? zlwcb : 0.;
-        double g[5];
-        for (int k = 0; k < 5; k++) g[k] = lb * zlwc.d[k] + zkeb * zke.d[k];
-        zkeb = g[0];
-        zv0b += g[1]; zv1b += g[2]; numcb += g[3]; zcoreb += g[4];
+        const double lb = (i == cnt) ? a.AV(iwa, kk) / K_RHOWA : 0.;
+        for (int k = 0; k < 5; k++) { p[k] = zke.d[k]; q[k] = lb * zlwc.d[k]; }
       }
-      zv0b += zcoreb / numc;
-      zv1b += zcoreb / numc;
-      numcb += -zcoreb * zv0 / (numc * numc) - zcoreb * zv1 / (numc * numc);
-      if (ix_so4 >= 0) a.AV(ix_so4, kk) += zv0b;
-      if (ix_oc >= 0) a.AV(ix_oc, kk) += zv1b;
-      a.an[kk] += numcb;
+      // the zke adjoint entering each iteration, serially through the chunk
+      const int n = min(32, total - base);
+      double myz = 0.;
+      for (int l = 0; l < n; l++) {
+        const double q0 = shfl_idx(q[0], l), p0 = shfl_idx(p[0], l);
+        if (lane == l) myz = zkeb;
+        zkeb = q0 + zkeb * p0;
+      }
+      double g[4];
+      for (int k = 0; k < 4; k++) g[k] = q[k + 1] + myz * p[k + 1];
+      // per-bin sums, two bins per transposed butterfly
+      for (int r0 = 0; r0 < n1a; r0 += 2) {
+        double v[8];
+        for (int k = 0; k < 4; k++) { v[k] = r == r0 ? g[k] : 0.; v[4 + k] = r == r0 + 1 ? g[k] : 0.; }
+        warp_sum8(v, lane);
+        for (int k = 0; k < 4; k++) {
+          if (lane == r0) tot[k] += v[k];
+          if (lane == r0 + 1) tot[k] += v[4 + k];
+        }
+      }
+    }
+    __syncwarp();
+    if (lane < n1a) {
+      const int kk = P.fn1a - lane;
+      const double *te = eq_of(lane);
+      if (te[0] >= 0.) {
+        a.AV(iwa, kk) = 0.;
+        if (te[0] > 0.) {
+          const double numc = xm[kk];
+          const double zv0 = P.ix_so4 >= 0 ? xm[NL + P.ix_so4 * NL + kk] : 0.;
+          const double zv1 = P.ix_oc >= 0 ? xm[NL + P.ix_oc * NL + kk] : 0.;
+          double zv0b = tot[0], zv1b = tot[1], numcb = tot[2];
+          const double zcoreb = tot[3];
+          zv0b += zcoreb / numc;
+          zv1b += zcoreb / numc;
+          numcb += -zcoreb * zv0 / (numc * numc) - zcoreb * zv1 / (numc * numc);
+          if (P.ix_so4 >= 0) a.AV(P.ix_so4, kk) += zv0b;
+          if (P.ix_oc >= 0) a.AV(P.ix_oc, kk) += zv1b;
+          a.an[kk] += numcb;
+        }
+      }
     }
   }
   __syncwarp();
   for (int b = lane; b <= P.fn2b; b += 32) a.AV(iwa, b) += zael1b * K_RHOWA;
   __syncwarp();
+  SUB_MARK(2);
 }
 
 // ---- coagulation reverse: adjoint of x_mid (after the clamp) -> adjoint of x_in ----
 // Values a target saw: a partner updated earlier in the sweep (lower index, processed)
 // shows its new value (x_pre), any other its old value (x_in).
+// w.n / w.v hold x_in, xpre the state after the sweep and w.K the step's kernels (shared
+// memory copies of the tape's rows).
 __device__ void coag_reverse(const DevParams &P, const CW<double> &w, const AW &a, const double *tb, double dt,
-                             const double *tp, const TapeLayout &tl, int lane) {
+                             const double *tp, const TapeLayout &tl, const double *xpre, int lane) {
   const int NL = w.NL, NW = P.nwet, C0 = P.nbins;
-  const double *xin = tp + tl.x_in, *xpre = tp + tl.x_pre, *xmid = tp + tl.x_mid;
+  const double *xin = w.n, *xmid = tp + tl.x_mid;
   const int16_t *L = partner_lists(P, tb);
   // clamp: pass where the clamped value is positive
   for (int e = lane; e < NL * (1 + NW); e += 32) {
@@ -1065,26 +1199,27 @@ __device__ void coag_reverse(const DevParams &P, const CW<double> &w, const AW &
     const int soff = L[4 * t], sn = L[4 * t + 1];
     const bool has_self = isc ? P.lscgcc : P.lscgaa;
     const double nt = xin[t];
-    const double den1 = 1. + dt * sink, den2 = 1. + dt * (sink + self);
+    // the two denominators of the update, as reciprocals (the partials divide by them)
+    const double r1 = 1. / (1. + dt * sink), r2 = 1. / (1. + dt * (sink + self));
     // adjoints of the outputs (new slot of t)
     double vbar[SALSA_NSV];
     for (int s = 0; s < SALSA_NSV; s++) vbar[s] = s < NW ? a.AV(s, t) : 0.;
     const double nbar = a.an[t];
     const double nnew = xpre[t];
-    double srcb[SALSA_NSV], ntb = nbar / den2, sinkb = -nbar * nnew * dt / den2;
-    const double selfb = -nbar * nnew * dt / den2;
+    double srcb[SALSA_NSV], ntb = nbar * r2, sinkb = -nbar * nnew * dt * r2;
+    const double selfb = sinkb;
     for (int s = 0; s < SALSA_NSV; s++) {
       srcb[s] = 0.;
       if (s < NW) {
-        const double vn = xpre[NL + s * NL + t];
-        srcb[s] = vbar[s] * dt * nt / den1;
-        ntb += vbar[s] * dt * src[s] / den1;
-        sinkb += -vbar[s] * vn * dt / den1;
+        const double vn = xpre[NL + s * NL + t], vr = vbar[s] * dt * r1;
+        srcb[s] = vr * nt;
+        ntb += vr * src[s];
+        sinkb += -vr * vn;
       }
     }
     __syncwarp();
     if (lane == 0) {
-      for (int s = 0; s < NW; s++) { a.OV(s, t) += vbar[s] / den1; a.AV(s, t) = 0.; }
+      for (int s = 0; s < NW; s++) { a.OV(s, t) += vbar[s] * r1; a.AV(s, t) = 0.; }
       if (has_self) {
         a.Kb[tri(t, t, NL)] += selfb * 0.5 * nt;
         ntb += selfb * 0.5 * w.Kij(t, t);
@@ -1157,8 +1292,17 @@ __device__ void kernel_reverse(const DevParams &P, const AW &a, const double *xi
 }
 
 // ---- adjoint kernels; the host runs them step by step, last step first ----
+// Cells are handed to warps one at a time from a counter of the launch (zero before it),
+// so that warps drawing cheap cells take more of them and the launch ends evenly.
+__device__ __forceinline__ long long next_cell(unsigned *ctr, int lane) {
+  unsigned q = 0;
+  if (lane == 0) q = atomicAdd(ctr, 1u);
+  return (long long)__shfl_sync(0xffffffffu, q, 0);
+}
+
 // Segment recompute: the states entering steps k0+1 .. k1-1 of a checkpoint segment.
-__global__ void __launch_bounds__(128, 2) chain_seg_kernel(const DevParams P, const ChainArgs A, int sg) {
+__global__ void __launch_bounds__(128, 2) chain_seg_kernel(const DevParams P, const ChainArgs A, int sg,
+                                                           unsigned *ctr) {
   extern __shared__ double smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double *tb = smem;
@@ -1168,7 +1312,7 @@ __global__ void __launch_bounds__(128, 2) chain_seg_kernel(const DevParams P, co
   const TapeLayout tl = tape_layout(NL, NW, A.n1a, tape_maxit(A.dt));
   const int k0 = sg * A.every, k1 = min(A.nsub, k0 + A.every);
   unsigned long long nerr = 0;
-  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
+  for (long long q = next_cell(ctr, lane); q < A.ncell; q = next_cell(ctr, lane)) {
     const ChainCell<double> c = chain_cell<double>(A, q, false);
     tape_to_state(A.ckpt + ((long long)sg * A.ncell + q) * ns, w.n, w.v, NL, NW, lane);
     __syncwarp();
@@ -1186,7 +1330,8 @@ __global__ void __launch_bounds__(128, 2) chain_seg_kernel(const DevParams P, co
 }
 
 // Taped step: recompute step k of every cell from the state entering it, taping.
-__global__ void __launch_bounds__(128, 2) chain_taped_kernel(const DevParams P, const ChainArgs A, const double *src) {
+__global__ void __launch_bounds__(128, 2) chain_taped_kernel(const DevParams P, const ChainArgs A, const double *src,
+                                                             unsigned *ctr) {
   extern __shared__ double smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double *tb = smem;
@@ -1197,7 +1342,7 @@ __global__ void __launch_bounds__(128, 2) chain_taped_kernel(const DevParams P, 
   double *drow = base + chain_ws_entries(NL, NW) + 32;
   const TapeLayout tl = tape_layout(NL, NW, A.n1a, tape_maxit(A.dt));
   unsigned long long nerr = 0;
-  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
+  for (long long q = next_cell(ctr, lane); q < A.ncell; q = next_cell(ctr, lane)) {
     const ChainCell<double> c = chain_cell<double>(A, q, false);
     tape_to_state(src + q * ns, w.n, w.v, NL, NW, lane);
     __syncwarp();
@@ -1212,14 +1357,16 @@ __global__ void __launch_bounds__(128, 2) chain_taped_kernel(const DevParams P, 
 
 // Reverse of step k of every cell; the running adjoint of the state (SALSA units) is
 // kept in xbar0, the kappa and supersaturation adjoints accumulate in place.
-__global__ void __launch_bounds__(128, 2) chain_rev_kernel(const DevParams P, const ChainArgs A) {
+__global__ void __launch_bounds__(128, 2) chain_rev_kernel(const DevParams P, const ChainArgs A, unsigned *ctr) {
   extern __shared__ double smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double *tb = smem;
   chain_tables(P, tb);
   const int NL = A.NL, NW = A.NW, ns = A.nstate;
   double *base = smem + P.tab_doubles + (size_t)warp * A.ws_doubles;
-  // condensation-reverse workspace: state and six per-bin rows; K lives in the tape
+  // condensation-reverse workspace: state and six per-bin rows; then the adjoint
+  // workspace, and copies of the tape's x_pre and K for the coagulation reverse (K's
+  // rows take K-bar * dK/dd_j in the kernel reverse)
   CW<double> w;
   w.NL = NL;
   w.n = base; w.v = base + NL;
@@ -1227,21 +1374,30 @@ __global__ void __launch_bounds__(128, 2) chain_rev_kernel(const DevParams P, co
   w.zns = w.cw + NL;
   w.dw = nullptr; w.S = nullptr; w.pbuf = nullptr; w.K = nullptr;
   AW a = make_aw(base + ns + 6 * NL, NL, NW);
+  double *xpre_s = base + ns + 6 * NL + adj_ws_doubles(NL, NW), *K_s = xpre_s + ns;
   const TapeLayout tl = tape_layout(NL, NW, A.n1a, tape_maxit(A.dt));
-  for (long long q = (long long)blockIdx.x * wpb + warp; q < A.ncell; q += (long long)gridDim.x * wpb) {
+  for (long long q = next_cell(ctr, lane); q < A.ncell; q = next_cell(ctr, lane)) {
     double *tp = A.tape + q * (long long)tl.total;
     if (tp[tl.nit + 1] != 0.) continue;
     const ChainCell<double> c = chain_cell<double>(A, q, false);
-    w.K = tp + tl.K;
     double *xb = A.xbar0 + q * ns;
     for (int e = lane; e < ns; e += 32) { if (e < NL) a.an[e] = xb[e]; else a.av[e - NL] = xb[e]; }
     __syncwarp();
     double kbar = 0., pbar = 0.;
+#ifdef SALSA_STAGE_TIMERS
+    long long t_stage = clock64();
+#endif
     cond_reverse(P, w, a, tb, c, A.dt, tp, tl, kbar, pbar, lane);
+    STAGE_MARK(14);
     tape_to_state(tp + tl.x_in, w.n, w.v, NL, NW, lane);
+    for (int e = lane; e < ns; e += 32) xpre_s[e] = tp[tl.x_pre + e];
+    for (int e = lane; e < chain_tri(NL); e += 32) K_s[e] = tp[tl.K + e];
+    w.K = K_s;
     __syncwarp();
-    coag_reverse(P, w, a, tb, A.dt, tp, tl, lane);
-    kernel_reverse(P, a, tp + tl.x_in, tp + tl.dki, tp + tl.dkj, tp + tl.pj, NL, NW, lane);
+    coag_reverse(P, w, a, tb, A.dt, tp, tl, xpre_s, lane);
+    STAGE_MARK(15);
+    kernel_reverse(P, a, w.n, tp + tl.dki, tp + tl.dkj, K_s, NL, NW, lane);
+    STAGE_MARK(3);
     for (int e = lane; e < ns; e += 32) xb[e] = e < NL ? a.an[e] : a.av[e - NL];
     if (lane == 0) {
       A.kappabar[q] += kbar;
@@ -1393,10 +1549,15 @@ int salsa_gb300_chain_adjoint(salsa_handle_t *h, const salsa_chain_t *c, const d
               ? (double *)salsa::handle_scratch(h, 1, (size_t)ckpt_every * A.ncell * ns * sizeof(double))
               : nullptr;
   if (!A.tape || (ckpt_every > 1 && !A.seg)) return SALSA_E_CUDA;
+  // one work counter per launch: segment recomputes, then a taped and a reverse step each
+  const int nseg = (A.nsub + A.every - 1) / A.every;
+  const size_t nctr = (size_t)nseg + 2 * (size_t)A.nsub;
+  unsigned *ctr = (unsigned *)salsa::handle_scratch(h, 2, nctr * sizeof(unsigned));
+  if (!ctr || cudaMemsetAsync(ctr, 0, nctr * sizeof(unsigned), st) != cudaSuccess) return SALSA_E_CUDA;
   // per-kernel shared memory (doubles per warp) and grids
   const int ws_fwd = salsa::chain_ws_entries(NL, NW) + 32;
   const int ws_tap = ws_fwd + 9 * NL;
-  const int ws_rev = ns + 6 * NL + salsa::adj_ws_doubles(NL, NW);
+  const int ws_rev = ns + 6 * NL + salsa::adj_ws_doubles(NL, NW) + ns + salsa::chain_tri(NL);
   auto config = [&](auto kernel, int wsd, int *grid, size_t *smem) -> bool {
     *smem = sizeof(double) * ((size_t)P.tab_doubles + (size_t)wpb * wsd);
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
@@ -1415,19 +1576,19 @@ int salsa_gb300_chain_adjoint(salsa_handle_t *h, const salsa_chain_t *c, const d
       !config(salsa::chain_rev_kernel, ws_rev, &g_rev, &s_rev))
     return SALSA_E_CUDA;
   salsa::chain_adj_units<<<4 * nsm, 256, 0, st>>>(P, A, 1);
-  const int nseg = (A.nsub + A.every - 1) / A.every;
   for (int sg = nseg - 1; sg >= 0; sg--) {
     const int k0 = sg * A.every, k1 = A.nsub < k0 + A.every ? A.nsub : k0 + A.every;
     if (k1 - k0 > 1) {
       A.ws_doubles = ws_fwd;
-      salsa::chain_seg_kernel<<<g_seg, 32 * wpb, s_seg, st>>>(P, A, sg);
+      salsa::chain_seg_kernel<<<g_seg, 32 * wpb, s_seg, st>>>(P, A, sg, ctr + sg);
     }
     for (int k = k1 - 1; k >= k0; k--) {
       const double *src = k == k0 ? A.ckpt + (size_t)sg * A.ncell * ns : A.seg + (size_t)(k - k0) * A.ncell * ns;
       A.ws_doubles = ws_tap;
-      salsa::chain_taped_kernel<<<g_tap, 32 * wpb, s_tap, st>>>(P, A, src);
+      unsigned *c_k = ctr + nseg + 2 * k;
+      salsa::chain_taped_kernel<<<g_tap, 32 * wpb, s_tap, st>>>(P, A, src, c_k);
       A.ws_doubles = ws_rev;
-      salsa::chain_rev_kernel<<<g_rev, 32 * wpb, s_rev, st>>>(P, A);
+      salsa::chain_rev_kernel<<<g_rev, 32 * wpb, s_rev, st>>>(P, A, c_k + 1);
     }
   }
   salsa::chain_adj_units<<<4 * nsm, 256, 0, st>>>(P, A, 0);

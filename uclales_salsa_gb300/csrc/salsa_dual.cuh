@@ -4,7 +4,9 @@
 // templates (bin_props, coag_pair, terminal_vel) instantiate with Dual<2> to give
 // dK/d(d_i) and dK/d(d_j) for the adjoint, and the chain step instantiates with
 // Dual<1> for the tangent-linear model.  Derivatives follow the elementary rules;
-// min/max/abs take the branch of the value (one-sided at ties).
+// min/max/abs take the branch of the value (one-sided at ties).  The value parts round
+// exactly as the plain FP64 code (no contraction); the tangent parts use fused
+// multiply-adds, which only changes their last bits.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -61,14 +63,14 @@ template <int N> __device__ __forceinline__ Dual<N> operator-(const Dual<N> &a) 
 template <int N> __device__ __forceinline__ Dual<N> operator*(const Dual<N> &a, const Dual<N> &b) {
   Dual<N> r; r.v = a.v * b.v;
 #pragma unroll
-  for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  for (int i = 0; i < N; i++) r.d[i] = __fma_rn(a.d[i], b.v, a.v * b.d[i]);
   return r;
 }
 template <int N> __device__ __forceinline__ Dual<N> operator/(const Dual<N> &a, const Dual<N> &b) {
   Dual<N> r; r.v = a.v / b.v;
   const double ib = 1. / b.v;
 #pragma unroll
-  for (int i = 0; i < N; i++) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  for (int i = 0; i < N; i++) r.d[i] = __fma_rn(-r.v, b.d[i], a.d[i]) * ib;
   return r;
 }
 template <int N> __device__ __forceinline__ Dual<N> operator+(const Dual<N> &a, double b) { return a + Dual<N>(b); }
@@ -121,9 +123,9 @@ template <int N> __device__ __forceinline__ Dual<N> d_pow(const Dual<N> &a, cons
   Dual<N> r;
   r.v = pow(a.v, b.v);
   const double la = a.v > 0. ? log(a.v) : 0.;
-  const double ga = a.v != 0. ? b.v * r.v / a.v : 0.;
+  const double ga = a.v != 0. ? b.v * r.v / a.v : 0., rl = r.v * la;
 #pragma unroll
-  for (int i = 0; i < N; i++) r.d[i] = ga * a.d[i] + r.v * la * b.d[i];
+  for (int i = 0; i < N; i++) r.d[i] = __fma_rn(ga, a.d[i], rl * b.d[i]);
   return r;
 }
 

@@ -261,7 +261,6 @@ __device__ void bin_props(const CoagCell<T> &cc, int ph, T diam, T dsph, T mass,
 // w <= m: m (u + u^2/3 - E/(3u));  w > m: w (1 + u^2/3 - E/(3u)).
 __device__ __forceinline__ float flux_match_stable(float m, float w) {
   bool small = w <= m;
-  float L = small ? m : w;
   float u = small ? w / m : m / w;
   float u2 = u * u;
   float E = expm1f(1.5f * log1pf(u2));
