@@ -18,6 +18,10 @@ A step is one SALSA call over every interior cell of the workload
   adjoint -- forward and adjoint time of the gradient harness (65,536 warm cells, 60
             coagulation + condensation steps of 0.5 s, checkpoints every step).
 
+--workload grid384x384x160 (23.6 M cells) holds about 158 GB of fields on the device;
+run it with --in-place (the steps read the workload's own fields instead of a copy)
+and --no-e2e (the end-to-end leg would pin as much host memory again).
+
 --impl reference times that CPU implementation alone on bounded samples of the same
 workload.  With torchrun, every rank runs the workload on its own GPU (independent
 cells, no collective on the data path); value is the sum over ranks of the cells
@@ -121,7 +125,7 @@ def run_gb300(args):
     for form in (0, 1):
         inp.cfg.precision = form
         step = SalsaStep(inp.cfg)
-        fields = {k: v.clone() for k, v in inp.fields.items()}
+        fields = inp.fields if args.in_place else {k: v.clone() for k, v in inp.fields.items()}
         outs = make_outputs(inp)
         for _ in range(args.warmup):
             step.run(inp, fields, outs, time=1.0, stream=stream)
@@ -153,40 +157,44 @@ def run_gb300(args):
         del fields, outs
         torch.cuda.empty_cache()
 
-    # end to end through the C-ABI with pinned host buffers (FP64 form)
+    # bytes a step moves across the boundary: every input and tendency array in, the
+    # results (and the IN deficit) out
     inp.cfg.precision = 0
-    def pinned(v):
-        return torch.empty(v.shape, dtype=v.dtype, pin_memory=True).copy_(v)
-
-    host_in = {k: pinned(v) for k, v in inp.fields.items()}
-    host_out = {k: pinned(v) for k, v in make_outputs(inp, device="cpu").items()}
-    del inp.fields
-    torch.cuda.empty_cache()
-    step = SalsaStep(inp.cfg)
-    step.run(inp, host_in, host_out, time=1.0)        # allocates the staging buffers once
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step.run(inp, host_in, host_out, time=1.0)
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], device=dev)
-    if world > 1:
-        tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
-    e2e_s = float(te.item())
-    inputs_b = sum(v.numel() * 8 for k, v in host_in.items() if k in (
+    outs_meta = make_outputs(inp, device="meta")
+    inputs_b = sum(v.numel() * 8 for k, v in inp.fields.items() if k in (
         "press", "temp", "rsl", "rsi", "rp", "dn", "wp", "naero", "ncloud", "nprecp", "nice", "maero", "mcloud",
         "mprecp", "mice", "indef"))
-    tend_b = sum(v.numel() * 8 for k, v in host_out.items() if k.endswith("t"))
-    out_b = field_bytes(host_out)
+    tend_b = sum(v.numel() * 8 for k, v in outs_meta.items() if k.endswith("t"))
     h2d = inputs_b + tend_b
-    d2h = out_b + host_in["indef"].numel() * 8
-    step.close()
+    d2h = field_bytes(outs_meta) + (inp.fields["indef"].numel() * 8 if "indef" in inp.fields else 0)
+    e2e_s = None
+    if not args.no_e2e:
+        # end to end through the C-ABI with pinned host buffers (FP64 form)
+        def pinned(v):
+            return torch.empty(v.shape, dtype=v.dtype, pin_memory=True).copy_(v)
+
+        host_in = {k: pinned(v) for k, v in inp.fields.items()}
+        host_out = {k: pinned(v) for k, v in make_outputs(inp, device="cpu").items()}
+        del inp.fields
+        torch.cuda.empty_cache()
+        step = SalsaStep(inp.cfg)
+        step.run(inp, host_in, host_out, time=1.0)        # allocates the staging buffers once
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step.run(inp, host_in, host_out, time=1.0)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        te = torch.tensor([e2e_s], device=dev)
+        if world > 1:
+            tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
+        e2e_s = float(te.item())
+        step.close()
 
     r0 = results[0]
     value = world * ncell * args.steps / (r0["ms_total"] / 1e3)
     mixed = world * ncell * args.steps / (results[1]["ms_total"] / 1e3)
-    e2e = world * ncell * args.steps / e2e_s
+    e2e = world * ncell * args.steps / e2e_s if e2e_s else None
     bytes_cell = 8 * ALG_DOUBLES[level]
     peaks = {}
     try:
@@ -217,7 +225,8 @@ def run_gb300(args):
                    "l2": "inputs larger than L2 (%.1f GB per step)" % ((h2d + d2h) / 1e9)},
         "mixed": {"value": mixed, "unit": "cell-steps/s", "ms_per_step": results[1]["ms_total"] / args.steps,
                   "speedup_vs_fp64": mixed / value, "dtype": "f32 kernels + f64 state"},
-        "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": ({"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+                if e2e is not None else {"value": None, "note": "not measured (--no-e2e)"}),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_cell": bytes_cell,
                      "note": "the step is bound by the FP64 pipe, not HBM",
@@ -335,6 +344,8 @@ def main():
     ap.add_argument("--cpu-sample-cells", type=int, default=3145728)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--in-place", action="store_true", help="steps read the workload's fields, not a copy")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg through host buffers")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
