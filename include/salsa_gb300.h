@@ -109,8 +109,10 @@ typedef struct {
  * getData lookups (:481-561).  "t" suffix = tendency (time level 2), in/out:
  * the library ADDS (new-old)/tstep to it.  NULL is allowed for arrays that the
  * configuration does not use (rsi/nice/mice/micet/indef at level 4, chargeTime
- * without lcharge, gaerot without lscndgas, wp without cloud-base activation,
- * any diag entry). */
+ * without lcharge, gaero/gaerot without lscndgas, wp without cloud-base activation,
+ * any diag entry).  With lscndgas, gaero holds the five gases in #/kg (SO4, HNO3,
+ * NH3, non-volatile OC, semi-volatile OC; mo_salsa_driver.f90:285-290) and gaerot
+ * receives their tendencies. */
 typedef struct {
   const double *press, *temp, *rsl, *rsi, *dn;    /* (nzp,nxp,nyp) */
   const double *rp;  double *rpt;                 /* water vapour mixing ratio and its tendency */

@@ -47,6 +47,15 @@
 #define MWA_C   18.016e-3
 #define RHOWA_C 1000.
 #define MVWA   (MWA_C/AVOG/RHOWA_C)
+/* condensing vapours (mo_submctl.f90:284-322) */
+#define MSU_C  98.08e-3
+#define MOC_C  150.e-3
+#define RHOSU_C 1830.
+#define RHOOC_C 1400.
+#define MVSU   (MSU_C/AVOG/RHOSU_C)
+#define MVOC   (MOC_C/AVOG/RHOOC_C)
+#define D_SA   5.539376964394570e-10
+#define N3     158.79
 /* math_functions.f90:7 uses full-precision pi */
 #define PI_FULL 3.14159265358979323846264338327
 
@@ -2159,16 +2168,126 @@ static void distr_update(Cell *w, int level) {
 }
 
 /* ======================================================================
+ * mo_salsa_dynamics.f90:348-685 condgas: H2SO4 and organic vapours onto every bin
+ * (Fuchs-Sutugin collision rates, implicit gas-phase update).  The nucleation terms of
+ * the smallest bin (Jacobson 16.73, 16.75) read condgas's own zj3n3 and zxocnv, which
+ * it declares locally and zeroes (:433-444), so they vanish whatever nucleation
+ * computed; zxsa (the H2SO4 fraction of the 3 nm clusters) only multiplies such a zero.
+ * ====================================================================== */
+static void condgas(Cell *w, double *pcsa, double *pcocnv, double *pcocsv, double zxsa, double ptemp, double ppres,
+                    double ptstep) {
+  const salsa_ref_ctx_t *c = w->c;
+  Section *ae = w->aero, *cl = w->cloud, *pr = w->precp, *ic = w->ice;
+  const int in1a = c->in1a, in2a = c->in2a, fn2b = c->fn2b, ncld = c->ncld, nprc = c->nprc, nice = c->nice;
+  const int ioc = c->idx_name[1], iso4 = c->idx_name[0];
+  const double zj3n3[2] = {0., 0.}, zxocnv = 0.;
+  double zdvolsa[MAXB], zdvoloc[MAXB], zn_vs_c = 0.;
+  for (int k = 0; k < MAXB; k++) zdvolsa[k] = zdvoloc[k] = 0.;
+  for (int bb = 0; bb < c->ntotal; bb++) updateDiameter(c, &w->all[bb], 1, T_WET);
+  /* 1) air and vapour properties */
+  const double zvisc = (7.44523e-3 * sqrt(cube(ptemp))) / (5093. * (ptemp + 110.4));
+  const double zdfvap = 5.1111e-10 * pow(ptemp, 1.75) * PSTAND / ppres;
+  const double zmfp = 3. * zdfvap * sqrt(PI * c->msu / (8. * RG * ptemp));
+  /* 2) Knudsen numbers and transition-regime corrections; 3) collision rates */
+  double zknud[MAXB], zbeta[MAXB], zcolrate[MAXB], zcolrateca[MAXB], zcolratepa[MAXB], zcolrateia[MAXB];
+  for (int k = in1a; k <= fn2b; k++) {
+    zknud[k] = k <= in1a + 1 ? 2. * zmfp / (ae[k].dwet + D_SA) : 2. * zmfp / ae[k].dwet;
+    zbeta[k] = (zknud[k] + 1.) / (0.377 * zknud[k] + 1. + 4. / (3. * c->massacc[k]) * (zknud[k] + sq(zknud[k])));
+  }
+  for (int k = in1a; k <= fn2b; k++) {
+    zcolrate[k] = 0.;
+    if (k <= in1a + 1) {
+      const double zdfpart = BOLTZ * ptemp * zbeta[k] / (3. * PI * zvisc * ae[k].dwet);
+      if (ae[k].numc > NLIM) zcolrate[k] = 2. * PI * (ae[k].dwet + D_SA) * (zdfvap + zdfpart) * zbeta[k] * ae[k].numc;
+    } else if (ae[k].numc > NLIM) {
+      zcolrate[k] = 2. * PI * ae[k].dwet * zdfvap * zbeta[k] * ae[k].numc;
+    }
+  }
+  /* hydrometeors: beta = 1 / (1 + Kn (1.33 + 0.71/Kn) / (1 + 1/Kn)) */
+  Section *hs[3] = {cl, pr, ic};
+  double *hr[3] = {zcolrateca, zcolratepa, zcolrateia};
+  const int hn[3] = {ncld, nprc, nice};
+  const double hl[3] = {NLIM, PRLIM, PRLIM};
+  for (int h = 0; h < 3; h++)
+    for (int k = 0; k < hn[h]; k++) {
+      const double kn = 2. * zmfp / hs[h][k].dwet;
+      double b = 1. + kn * (1.33 + (0.71 / kn)) / (1. + (1. / kn));
+      b = 1. / b;
+      hr[h][k] = hs[h][k].numc > hl[h] ? 2. * PI * hs[h][k].dwet * zdfvap * b * hs[h][k].numc : 0.;
+    }
+  /* 4) condensation sink (Fortran SUM: in order) */
+  double sa = 0., sca = 0., spa = 0., sia = 0., sa2 = 0.;
+  for (int k = in1a; k <= fn2b; k++) sa += zcolrate[k];
+  for (int k = 0; k < ncld; k++) sca += zcolrateca[k];
+  for (int k = 0; k < nprc; k++) spa += zcolratepa[k];
+  for (int k = 0; k < nice; k++) sia += zcolrateia[k];
+  for (int k = in2a; k <= fn2b; k++) sa2 += zcolrate[k];
+  const double zcs_tot = sa + sca + spa + sia;
+  /* 5.1.1) non-volatile organics onto every bin */
+  if (*pcocnv > 1.e-10 && zcs_tot > 1.e-30 && ioc >= 0) {
+    zn_vs_c = 0.;
+    if (zj3n3[1] > 1.) zn_vs_c = zj3n3[1] / (zj3n3[1] + *pcocnv * zcolrate[in1a]);
+    double zcolrate_ocnv[MAXB];
+    for (int k = in1a; k <= fn2b; k++) zcolrate_ocnv[k] = zcolrate[k];
+    zcolrate_ocnv[in1a] = zcolrate_ocnv[in1a] + zj3n3[1] / *pcocnv;
+    const double zcs_ocnv = zcs_tot + zj3n3[1] / *pcocnv;
+    const double zcvap_new2 = *pcocnv / (1. + ptstep * zcs_ocnv);
+    const double zdvap2 = *pcocnv - zcvap_new2;
+    *pcocnv = zcvap_new2;
+    for (int k = in1a; k <= fn2b; k++) zdvoloc[k] = zcolrate_ocnv[k] / zcs_ocnv * MVOC * zdvap2;
+    for (int k = in1a; k <= fn2b; k++) ae[k].volc[ioc] = ae[k].volc[ioc] + zdvoloc[k];
+    for (int k = 0; k < ncld; k++) cl[k].volc[ioc] = cl[k].volc[ioc] + zcolrateca[k] / zcs_ocnv * MVOC * zdvap2;
+    for (int k = 0; k < nprc; k++) pr[k].volc[ioc] = pr[k].volc[ioc] + zcolratepa[k] / zcs_ocnv * MVOC * zdvap2;
+    for (int k = 0; k < nice; k++) ic[k].volc[ioc] = ic[k].volc[ioc] + zcolrateia[k] / zcs_ocnv * MVOC * zdvap2;
+    if (zxocnv > 0.) ae[in1a].numc = ae[in1a].numc + zn_vs_c * zdvoloc[in1a] / MVOC / (N3 * zxocnv);
+  }
+  /* 5.1.2) semi-volatile organics onto regimes 2a/2b and the hydrometeors.  The aerosol
+     update adds all of zdvoloc, which still holds the non-volatile increments of 5.1.1. */
+  const double zcs_ocsv = sa2 + sca + spa + sia;
+  if (*pcocsv > 1.e-10 && zcs_ocsv > 1.e-30 && ioc >= 0) {
+    const double zcvap_new3 = *pcocsv / (1. + ptstep * zcs_ocsv);
+    const double zdvap3 = *pcocsv - zcvap_new3;
+    *pcocsv = zcvap_new3;
+    for (int k = in2a; k <= fn2b; k++) zdvoloc[k] = zdvoloc[k] + zcolrate[k] / zcs_ocsv * MVOC * zdvap3;
+    for (int k = in1a; k <= fn2b; k++) ae[k].volc[ioc] = ae[k].volc[ioc] + zdvoloc[k];
+    for (int k = 0; k < ncld; k++) cl[k].volc[ioc] = cl[k].volc[ioc] + zcolrateca[k] / zcs_ocsv * MVOC * zdvap3;
+    for (int k = 0; k < nprc; k++) pr[k].volc[ioc] = pr[k].volc[ioc] + zcolratepa[k] / zcs_ocsv * MVOC * zdvap3;
+    for (int k = 0; k < nice; k++) ic[k].volc[ioc] = ic[k].volc[ioc] + zcolrateia[k] / zcs_ocsv * MVOC * zdvap3;
+  }
+  /* 5.2) sulphuric acid onto every bin */
+  if (*pcsa > 1.e-10 && zcs_tot > 1.e-30 && iso4 >= 0) {
+    zn_vs_c = 0.;
+    if (zj3n3[0] > 1.) zn_vs_c = zj3n3[0] / (zj3n3[0] + *pcsa * zcolrate[in1a]);
+    zcolrate[in1a] = zcolrate[in1a] + zj3n3[0] / *pcsa;
+    const double zcs_su = zcs_tot + zj3n3[0] / *pcsa;
+    const double zcvap_new1 = *pcsa / (1. + ptstep * zcs_su);
+    const double zdvap1 = *pcsa - zcvap_new1;
+    *pcsa = zcvap_new1;
+    for (int k = in1a; k <= fn2b; k++) zdvolsa[k] = zcolrate[k] / zcs_su * MVSU * zdvap1;
+    for (int k = in1a; k <= fn2b; k++) ae[k].volc[iso4] = ae[k].volc[iso4] + zdvolsa[k];
+    for (int k = 0; k < ncld; k++) cl[k].volc[iso4] = cl[k].volc[iso4] + zcolrateca[k] / zcs_su * MVSU * zdvap1;
+    for (int k = 0; k < nprc; k++) pr[k].volc[iso4] = pr[k].volc[iso4] + zcolratepa[k] / zcs_su * MVSU * zdvap1;
+    for (int k = 0; k < nice; k++) ic[k].volc[iso4] = ic[k].volc[iso4] + zcolrateia[k] / zcs_su * MVSU * zdvap1;
+    if (zxsa > 0.) ae[in1a].numc = ae[in1a].numc + zn_vs_c * zdvolsa[in1a] / MVSU / (N3 * zxsa);
+  }
+}
+
+/* ======================================================================
  * mo_salsa.f90:45-153 salsa
  * ====================================================================== */
 static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double prsi, double ptemp, double ptstep,
-                       double pw, int level, double *actd_n, double *actd_v) {
+                       double pw, int level, double *actd_n, double *actd_v, double *zg) {
   const salsa_ref_ctx_t *c = w->c;
   const salsa_config_t *g = &c->cfg;
   (void)pw;
   if (c->st_coag) coagulation(w, ptstep, ptemp, ppres);
   if (c->st_cnd) {
-    /* condensation :276-342: nucleation and condgas are rejected at init (nsnucl == 0, lscndgas off) */
+    /* condensation :276-342.  nucleation (mo_salsa_nucleation.f90:72-625) only returns the
+       3 nm formation rates, which condgas does not read (see condgas), and the H2SO4
+       fraction of the clusters: 1 for the H2SO4 schemes nsnucl = 1-3; for the mixed
+       schemes 5-9 it only multiplies condgas's vanishing nucleation term, and 1 stands in. */
+    const double zxsa = g->nsnucl > 0 ? 1. : 0.;
+    if (g->lscndgas) condgas(w, &zg[0], &zg[3], &zg[4], zxsa, ptemp, ppres, ptstep);
     if (g->lscndh2ocl || g->lscndh2oae || g->lscndh2oic) gpparth2o(w, ptemp, ppres, prs, prsi, prv, ptstep);
   }
   if (c->st_auto && g->lsauto.mode == 2) autoconv2(w, ptstep);
@@ -2221,7 +2340,10 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (!cfg || !out) return SALSA_E_ARG;
   if (cfg->nbin[0] < 1 || cfg->nbin[1] < 4 || cfg->prc_nbins < 1 || cfg->ice_nbins < 1) return SALSA_E_ARG;
   if (cfg->nspec_dry < 1 || cfg->nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
-  if (cfg->nsnucl != 0 || cfg->lscndgas || cfg->lssecice.sw || cfg->lscoag.mode == 2 || cfg->lsactiv.mode == 2)
+  if (cfg->lssecice.sw || cfg->lscoag.mode == 2 || cfg->lsactiv.mode == 2) return SALSA_E_UNSUPPORTED;
+  /* nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
+     nj3 outside 1-3 STOPs once a cell nucleates (:600-602) */
+  if (cfg->nsnucl == 4 || cfg->nsnucl < 0 || (cfg->nsnucl > 0 && (cfg->nj3 < 1 || cfg->nj3 > 3)))
     return SALSA_E_UNSUPPORTED;
   if (cfg->level == 5 && cfg->fixinc > 0. && !(cfg->lsicehom || cfg->lsiceimm || cfg->lsicedep))
     return SALSA_E_UNSUPPORTED;   /* ice_fixed_NC: marked broken in the reference (mo_salsa_cloud_ice.f90:321) */
@@ -2379,6 +2501,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
   if (level == 5 && (!f->rsi || !f->nice || !f->mice || !f->nicet || !f->micet)) return SALSA_E_ARG;
   if (level == 5 && g->ice_theta_dist && !f->indef) return SALSA_E_ARG;
   if (lcharge && !f->chargeTime) return SALSA_E_ARG;
+  if (g->lscndgas && (!f->gaero || !f->gaerot)) return SALSA_E_ARG;
   /* set_SALSA_runtime (sticky states) */
   const salsa_switch_t *ms[7] = {&g->lscoag, &g->lscnd, &g->lsauto, &g->lsactiv, &g->lsicenucl, &g->lsicemelt,
                                  &g->lssecice};
@@ -2480,8 +2603,12 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
         }
       }
       if (initialize) equilibration(w, 0.3, in_t, 1);
+      /* gases in #/m3 (mo_salsa_driver.f90:285-290): SO4, HNO3, NH3, OC non-volatile, OC semi-volatile */
+      double zg[5] = {0., 0., 0., 0., 0.};
+      if (f->gaero)
+        for (int i = 0; i < 5; i++) zg[i] = f->gaero[p + plane * i] * dn;
       for (int k = 0; k < ncld; k++) { actd_n[k] = 0.; for (int s2 = 0; s2 < NSP; s2++) actd_v[k * NSP + s2] = 0.; }
-      salsa_cell(w, in_p, &in_rv, in_rs, in_rsi, in_t, tstep, in_w, level, actd_n, actd_v);
+      salsa_cell(w, in_p, &in_rv, in_rs, in_rsi, in_t, tstep, in_w, level, actd_n, actd_v, zg);
       for (int nb = 0; nb < c->ntotal; nb++) {
         Section *s = &w->all[nb];
         int icat = s->phase - 1;
@@ -2510,6 +2637,9 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
         for (int k = 0; k < ncld; k++)
           f->pa_vactd[p + plane * (nc * ncld + k)] = actd_v[k * NSP + nc] * c->rholiq[nc] / dn;
       f->rpt[p] = f->rpt[p] + (in_rv - rv_old) / tstep;
+      if (g->lscndgas)   /* :369-384 */
+        for (int i = 0; i < 5; i++)
+          f->gaerot[p + plane * i] = f->gaerot[p + plane * i] + ((zg[i] / dn) - f->gaero[p + plane * i]) / tstep;
       if (g->diagnostics) {
         double d[SALSA_NDIAG];
         const Rate *R = w->rate;

@@ -4,9 +4,19 @@ import torch
 NUMBER_FIELDS = ["naerot", "ncloudt", "nprecpt", "nicet"]
 MASS_FIELDS = ["maerot", "mcloudt", "mprecpt", "micet"]
 STATE_OF = {"naerot": "naero", "ncloudt": "ncloud", "nprecpt": "nprecp", "nicet": "nice",
-            "maerot": "maero", "mcloudt": "mcloud", "mprecpt": "mprecp", "micet": "mice", "rpt": "rp"}
-# absolute floors below which a bin value is physically empty: numbers in #/kg, masses in kg/kg
-FLOOR = {"n": 1.e-3, "m": 1.e-24, "rp": 1.e-12}
+            "maerot": "maero", "mcloudt": "mcloud", "mprecpt": "mprecp", "micet": "mice", "rpt": "rp",
+            "gaerot": "gaero"}
+# absolute floors below which a value is physically empty: numbers in #/kg, masses in kg/kg,
+# gas molecules in #/kg
+FLOOR = {"n": 1.e-3, "m": 1.e-24, "rp": 1.e-12, "g": 1.0}
+
+
+def floor_of(name):
+    if name == "rpt":
+        return FLOOR["rp"]
+    if name == "gaerot":
+        return FLOOR["g"]
+    return FLOOR["n"] if name in NUMBER_FIELDS else FLOOR["m"]
 
 
 def interior(t, nzp, nxp, nyp):
@@ -31,7 +41,7 @@ def state_errors(inp, fields, out_a, out_b, tol=1e-6):
         b = old + out_b[name].double().cpu() * dt
         a = interior(a, inp.nzp, inp.nxp, inp.nyp)
         b = interior(b, inp.nzp, inp.nxp, inp.nyp)
-        fl = FLOOR["rp"] if name == "rpt" else (FLOOR["n"] if name in NUMBER_FIELDS else FLOOR["m"])
+        fl = floor_of(name)
         o = interior(old, inp.nzp, inp.nxp, inp.nyp)
         scale = torch.maximum(b.abs(), o.abs()).clamp(min=fl)
         rel = (a - b).abs() / scale

@@ -20,7 +20,7 @@ from uclales_salsa_gb300.inputs import make_inputs, make_outputs
 from uclales_salsa_gb300.api import SalsaStep
 from uclales_salsa_gb300 import capi
 from oracle_ref import Oracle
-from parity import STATE_OF, NUMBER_FIELDS, FLOOR, interior, output_errors
+from parity import STATE_OF, NUMBER_FIELDS, FLOOR, floor_of, interior, output_errors
 
 pytestmark = pytest.mark.gpu
 C_ENV = 10.0
@@ -77,7 +77,7 @@ def check(inp, gpu, ref, env, rtol):
         old = I(inp.fields[st])
         a, b = old + I(gpu[name]) * dt, old + I(ref[name]) * dt
         e = I(env[name]) * dt
-        fl = FLOOR["rp"] if name == "rpt" else (FLOOR["n"] if name in NUMBER_FIELDS else FLOOR["m"])
+        fl = floor_of(name)
         scale = torch.maximum(b.abs(), old.abs()).clamp(min=fl)
         err = (a - b).abs()
         bound = torch.maximum(rtol * scale, C_ENV * e)
@@ -187,9 +187,17 @@ def test_error_codes():
     f.press = capi.ptr_of(0)
     assert run(inp.nzp, inp.nxp, inp.nyp, inp.ns, 1.0, 1.0, 1, 4, 0, 0) == capi.SALSA_E_ARG   # NULL input
     cfg = inp.cfg
-    cfg.nsnucl = 1
+    cfg.nsnucl = 4          # ternary nucleation STOPs in the reference
     h = C.c_void_p()
     assert L.salsa_gb300_init(C.byref(cfg), C.byref(h)) == capi.SALSA_E_UNSUPPORTED
+    cfg.nsnucl = 0
+    cfg.lscndgas = 1        # gas condensation needs the gas tendency array
+    f.press = capi.ptr_of(inp.fields["press"].data_ptr())
+    f.gaerot = capi.ptr_of(0)
+    g = SalsaStep(cfg)
+    assert L.salsa_gb300_run(g.h, inp.nzp, inp.nxp, inp.nyp, inp.ns, 1.0, 1.0, 1, 4, 0, 0, C.byref(f),
+                             C.byref(st)) == capi.SALSA_E_ARG
+    g.close()
 
 
 def test_full_size_invariants():
@@ -210,7 +218,7 @@ def test_full_size_invariants():
         if name in out:
             new = I(inp.fields[s]) + I(out[name]) * dt
             assert bool(torch.isfinite(new).all()), name
-            fl = FLOOR["rp"] if name == "rpt" else (FLOOR["n"] if name in NUMBER_FIELDS else FLOOR["m"])
+            fl = floor_of(name)
             assert float(new.min()) > -1e-12 * (float(I(inp.fields[s]).abs().max()) + fl), name
     dn, T, p = I(inp.fields["dn"]), I(inp.fields["temp"]), I(inp.fields["press"])
     rhoair = 28.97e-3 * p / (8.314 * T)

@@ -5,7 +5,8 @@ a workload: the classic ice nucleation (mo_salsa_cloud_ice.f90:26-140), every SE
 freezing mode, ice melting (mo_salsa_cloud_ice.f90:393-462), the second
 autoconversion mode (mo_salsa_cloud.f90 autoconv2), the charging enhancement of the
 collision kernels (mo_salsa_coagulation_kernels.f90:411-416), the initialising call
-(run_SALSA with initialize=.TRUE.) and a step without coagulation.  The criterion is
+(run_SALSA with initialize=.TRUE.), a step without coagulation, and gas condensation
+with nucleation switched on (mo_salsa_dynamics.f90:276-685) at levels 5 and 4.  The criterion is
 the one of test_gpu_parity.py.
 """
 import pytest
@@ -43,6 +44,10 @@ def _no_coag(inp, f):
     inp.cfg.lscoag.sw = 0
 
 
+def _nucleation(inp, f):
+    inp.cfg.nsnucl = 1     # binary nucleation; gas condensation comes with the gas fields
+
+
 def _charge(inp, f):
     lay = inp.layout
     g = torch.Generator().manual_seed(5)
@@ -59,6 +64,8 @@ CASES = [
     ("no_coagulation", "grid256x256x128", dict(X=8, Y=8, Z=16), _no_coag, {}),
     ("charge", "grid256x256x128", dict(X=8, Y=8, Z=16), _charge, dict(lcharge=1)),
     ("initialize", "grid16x16x40", dict(X=8, Y=8, Z=16), lambda inp, f: None, dict(initialize=1)),
+    ("gas_condensation", "grid256x256x128", dict(X=8, Y=8, Z=16, gases=True), _nucleation, {}),
+    ("gas_condensation_level4", "grid16x16x40", dict(X=8, Y=8, Z=16, gases=True), _nucleation, {}),
 ]
 
 

@@ -211,8 +211,10 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
   if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
   // processes outside this build (the init check mirrors the oracle's)
-  if (g.nsnucl != 0 || g.lscndgas || g.lssecice.sw || g.lscoag.mode == 2 || g.lsactiv.mode == 2)
-    return SALSA_E_UNSUPPORTED;
+  if (g.lssecice.sw || g.lscoag.mode == 2 || g.lsactiv.mode == 2) return SALSA_E_UNSUPPORTED;
+  // nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
+  // nj3 outside 1-3 STOPs once a cell nucleates (:600-602)
+  if (g.nsnucl == 4 || g.nsnucl < 0 || (g.nsnucl > 0 && (g.nj3 < 1 || g.nj3 > 3))) return SALSA_E_UNSUPPORTED;
   if (g.level == 5 && g.fixinc > 0. && !(g.lsicehom || g.lsiceimm || g.lsicedep)) return SALSA_E_UNSUPPORTED;
   if (g.prc_nbins > 20) return SALSA_E_UNSUPPORTED;   // precipitation-formation accumulators
   int nb1 = g.nbin[0], nb2 = g.nbin[1];
@@ -338,6 +340,14 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   add(salsa::FI_DN, -1, 0, salsa::ROW_IN);
   add(salsa::FI_WP, -1, 0, salsa::ROW_IN);
   add(salsa::FI_KAPPA, -1, 0, salsa::ROW_IN);
+  // gases (mo_salsa_driver.f90:285-290, tendencies :369-384) only with gas condensation
+  B.raw_gas = -1;
+  if (g.lscndgas) {
+    B.raw_gas = (int)rows.size();
+    for (int i = 0; i < 5; i++) add(salsa::FI_GAERO, salsa::FO_GAEROT, i, salsa::ROW_TEND);
+  }
+  B.lscndgas = g.lscndgas;
+  B.nsnucl = g.nsnucl;
   int ncat = (g.level == 5) ? 4 : 3;
   const int catnb[4] = {nbins, ncld, nprc, nice};
   B.raw_num = (int)rows.size();
@@ -601,6 +611,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   if (level == 5 && (!f->rsi || !f->nice || !f->mice || !f->nicet || !f->micet)) return SALSA_E_ARG;
   if (level == 5 && g.ice_theta_dist && !f->indef) return SALSA_E_ARG;
   if (lcharge && !f->chargeTime) return SALSA_E_ARG;
+  if (g.lscndgas && (!f->gaero || !f->gaerot)) return SALSA_E_ARG;
   if (cudaSetDevice(h->device) != cudaSuccess) return SALSA_E_NODEV;
 
   // set_SALSA_runtime (mo_salsa_driver.f90:445-474): states switch on once and stay on
@@ -656,6 +667,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   fin(f->maero, (long long)nw * nb[0], salsa::FI_MAERO); fin(f->mcloud, (long long)nw * nb[1], salsa::FI_MCLOUD);
   fin(f->mprecp, (long long)nw * nb[2], salsa::FI_MPRECP);
   fin(level == 5 ? f->mice : nullptr, (long long)(nw + 1) * nb[3], salsa::FI_MICE);
+  fin(g.lscndgas ? f->gaero : nullptr, 5, salsa::FI_GAERO);
   bool use_indef = level == 5 && g.ice_theta_dist;
   fio(f->rpt, 1, salsa::FO_RPT, 1);
   fio(f->naerot, nb[0], salsa::FO_NAEROT, 1); fio(f->ncloudt, nb[1], salsa::FO_NCLOUDT, 1);
@@ -668,6 +680,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   fio(lcharge ? f->chargeTime : nullptr, nliq, salsa::FO_CHARGE, 1);
   fio(f->pa_nactd, nb[1], salsa::FO_NACT, 0);
   fio(f->pa_vactd, (long long)nw * nb[1], salsa::FO_VACT, 0);
+  fio(g.lscndgas ? f->gaerot : nullptr, 5, salsa::FO_GAEROT, 1);
   int ndiag = (level == 5) ? SALSA_NDIAG : SALSA_DIAG_AICOLL;
   for (int i = 0; i < ndiag; i++) fio(g.diagnostics ? f->diag[i] : nullptr, 1, salsa::FO_DIAG0 + i, 0);
 

@@ -38,6 +38,13 @@
 #define K_RHORI 400.
 #define K_MVWA (K_MWA / K_AVOG / K_RHOWA)
 #define K_PI_FULL 3.14159265358979323846
+// condensing vapours (mo_submctl.f90:284-322): molar masses, densities, molecular volumes
+#define K_MSU 98.08e-3
+#define K_MVSU (98.08e-3 / K_AVOG / 1830.)
+#define K_MVOC (150.e-3 / K_AVOG / 1400.)
+#define K_DSA 5.539376964394570e-10
+#define K_N3 158.79
+#define K_MASSACC 1.   // mass accommodation coefficient of every aerosol bin (mo_salsa_init.f90:818-820)
 
 namespace salsa {
 
@@ -45,12 +52,12 @@ namespace salsa {
 enum {
   FI_PRESS = 0, FI_TEMP, FI_RSL, FI_RSI, FI_RP, FI_DN, FI_WP, FI_KAPPA,
   FI_NAERO, FI_NCLOUD, FI_NPRECP, FI_NICE, FI_MAERO, FI_MCLOUD, FI_MPRECP, FI_MICE,
-  FI_INDEF, FI_CHARGE, FI_N
+  FI_INDEF, FI_CHARGE, FI_GAERO, FI_N
 };
 // output field ids (index into DevParams::fout)
 enum {
   FO_RPT = 0, FO_NAEROT, FO_NCLOUDT, FO_NPRECPT, FO_NICET, FO_MAEROT, FO_MCLOUDT, FO_MPRECPT, FO_MICET,
-  FO_INDEF, FO_CHARGE, FO_NACT, FO_VACT, FO_DIAG0, FO_N = FO_DIAG0 + 17
+  FO_INDEF, FO_CHARGE, FO_NACT, FO_VACT, FO_GAEROT, FO_DIAG0, FO_N = FO_DIAG0 + 17
 };
 // row modes
 enum { ROW_IN = 0, ROW_TEND = 1, ROW_INOUT = 2, ROW_OUT = 3 };
@@ -96,11 +103,13 @@ struct DevParams {
   int lscgaa, lscgcc, lscgca, lscgpc, lscgpa, lscgpp, lscgia, lscgic, lscgii, lscgip;
   int lscndh2oae, lscndh2ocl, lscndh2oic, lsicehom, lsiceimm, lsicedep, ice_theta_dist, lsdistupdate;
   int has_kappa;
+  int lscndgas, nsnucl;   // gas condensation; nucleation scheme (0: off)
   double Eiagg_max, Eiagg_min, eddy_dis, rhlim, initMinTheta, chargeTimeMax, chargeCollEnh;
   double mean_theta_imm, sigma_theta_imm, mean_theta_dep, sigma_theta_dep;
   double iceShapeAlpha, iceShapeBeta, iceShapeGamma, iceShapeSigma;
   // workspace layout (doubles)
   int raw_num, raw_mbase[4], raw_indef, raw_charge, raw_nact, raw_vact, raw_diag, nraw;
+  int raw_gas;         // first of the five gas rows (SO4, HNO3, NH3, OC non-volatile, OC semi-volatile), or -1
   int nrows;           // rows in the row table
   int npairs;          // collision pairs in the pair table
   int npairs_plain;    // pairs before the equal-size (self-coagulation offset) section

@@ -1172,6 +1172,115 @@ __device__ __forceinline__ double solute_moles(const DevParams &P, const WS<KT> 
 }
 __device__ __forceinline__ double acth2o_w(double znw, double zns) { return fmax(0.1, znw / fmax(K_EPS, (znw + zns))); }
 
+// ----------------------------------------------------------------------------------------
+// Gas condensation: mo_salsa_dynamics.f90:348-685 (condgas).  H2SO4 and the non- and
+// semi-volatile organic vapours condense onto every bin in proportion to its
+// Fuchs-Sutugin collision rate; the gas phase takes one implicit step.  zg holds the
+// five gases in #/m3 (SO4, HNO3, NH3, OC non-volatile, OC semi-volatile) on every lane.
+// The smallest-bin nucleation terms (Jacobson 16.73, 16.75) read condgas's own zj3n3
+// and zxocnv, which it declares locally and zeroes (:433-444): zn_vs_c stays 0, the
+// collision rate of the smallest bin and the sinks gain 0/c.  zxsa, the H2SO4 fraction of
+// the 3 nm clusters from nucleation, only multiplies that zero.  Collision rates go to
+// scratch row 0, the non-volatile organic increments of the aerosol bins to row 1.
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+__device__ void condgas(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres, double dt,
+                        double (&zg)[5], double zxsa, int lane) {
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const int ntot = P.ntotal, in1a = P.in1a, in2a = P.in2a, fn2b = P.fn2b;
+  const int C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid;
+  const int ioc = P.ix_oc, iso4 = P.ix_so4;
+  double *cr = w.scr, *dvoc = w.scr + w.NB;
+  const double zvisc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+  const double zdfvap = 5.1111e-10 * pow(T, 1.75) * K_PSTAND / pres;
+  const double zmfp = 3. * zdfvap * sqrt(K_PI * K_MSU / (8. * K_RG * T));
+  for (int b = lane; b < ntot; b += 32) {
+    // updateDiameter(limit=.TRUE., type="wet") (:446-448)
+    const int ph = phase_of(P, b);
+    const double n = w.numc[b];
+    double dw = dmid[b];
+    if (n > nlim_of(ph)) {
+      double vs = 0.;
+      for (int sp = 0; sp < P.nused; sp++) vs += w.v(sp, b);
+      dw = cbrt(vs / n / K_PI6);
+    }
+    dw = fmin(dw, dlim_of(ph));
+    w.dwet[b] = dw;
+    // collision rate of the vapour molecules with the bin's particles [1/s] (:461-541)
+    double r = 0.;
+    if (ph == 1) {
+      const bool small = b <= in1a + 1;   // molecule size and particle diffusion count below 20 nm
+      const double kn = small ? 2. * zmfp / (dw + K_DSA) : 2. * zmfp / dw;
+      const double beta = (kn + 1.) / (0.377 * kn + 1. + 4. / (3. * K_MASSACC) * (kn + sq(kn)));
+      if (small) {
+        const double zdfpart = K_BOLTZ * T * beta / (3. * K_PI * zvisc * dw);
+        if (n > K_NLIM) r = 2. * K_PI * (dw + K_DSA) * (zdfvap + zdfpart) * beta * n;
+      } else if (n > K_NLIM) {
+        r = 2. * K_PI * dw * zdfvap * beta * n;
+      }
+      dvoc[b] = 0.;
+    } else {
+      const double kn = 2. * zmfp / dw;
+      double beta = 1. + kn * (1.33 + (0.71 / kn)) / (1. + (1. / kn));
+      beta = 1. / beta;
+      if (n > (ph == 2 ? K_NLIM : K_PRLIM)) r = 2. * K_PI * dw * zdfvap * beta * n;
+    }
+    cr[b] = r;
+  }
+  __syncwarp();
+  // condensation sinks, summed in bin order as Fortran's SUM (:545, :603-606)
+  double sa = 0., sca = 0., spa = 0., sia = 0., sa2 = 0.;
+  for (int k = in1a; k <= fn2b; k++) sa += cr[k];
+  for (int k = 0; k < P.ncld; k++) sca += cr[C0 + k];
+  for (int k = 0; k < P.nprc; k++) spa += cr[P0 + k];
+  for (int k = 0; k < P.nice; k++) sia += cr[I0 + k];
+  for (int k = in2a; k <= fn2b; k++) sa2 += cr[k];
+  const double zcs_tot = sa + sca + spa + sia;
+  const double zn_vs_c = 0.;
+  // non-volatile organics onto every bin (:552-598)
+  if (zg[3] > 1.e-10 && zcs_tot > 1.e-30 && ioc >= 0) {
+    const double zcs = zcs_tot;
+    const double cnew = zg[3] / (1. + dt * zcs);
+    const double dv = zg[3] - cnew;
+    zg[3] = cnew;
+    for (int b = lane; b < ntot; b += 32) {
+      const double inc = cr[b] / zcs * K_MVOC * dv;
+      if (b <= fn2b) dvoc[b] = inc;
+      w.v(ioc, b) = w.v(ioc, b) + inc;
+    }
+  }
+  // semi-volatile organics onto regimes 2a/2b and the hydrometeors (:603-632); the aerosol
+  // update adds the whole increment row, which still holds the non-volatile increments
+  const double zcs_ocsv = sa2 + sca + spa + sia;
+  if (zg[4] > 1.e-10 && zcs_ocsv > 1.e-30 && ioc >= 0) {
+    const double cnew = zg[4] / (1. + dt * zcs_ocsv);
+    const double dv = zg[4] - cnew;
+    zg[4] = cnew;
+    for (int b = lane; b < ntot; b += 32) {
+      if (b <= fn2b) {
+        double d = dvoc[b];
+        if (b >= in2a) d = d + cr[b] / zcs_ocsv * K_MVOC * dv;
+        w.v(ioc, b) = w.v(ioc, b) + d;
+      } else {
+        w.v(ioc, b) = w.v(ioc, b) + cr[b] / zcs_ocsv * K_MVOC * dv;
+      }
+    }
+  }
+  // sulphuric acid onto every bin (:636-679)
+  if (zg[0] > 1.e-10 && zcs_tot > 1.e-30 && iso4 >= 0) {
+    const double zcs = zcs_tot;
+    const double cnew = zg[0] / (1. + dt * zcs);
+    const double dv = zg[0] - cnew;
+    zg[0] = cnew;
+    for (int b = lane; b < ntot; b += 32) {
+      const double inc = cr[b] / zcs * K_MVSU * dv;
+      w.v(iso4, b) = w.v(iso4, b) + inc;
+      if (b == in1a && zxsa > 0.) w.numc[b] = w.numc[b] + zn_vs_c * inc / K_MVSU / (K_N3 * zxsa);
+    }
+  }
+  __syncwarp();
+}
+
 template <typename KT>
 __device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres, double prs,
                           double prsi, double &prv, double dt, double kappa, bool diag, int lane) {
@@ -2311,13 +2420,23 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   for (int i = lane; i < M_PF; i += 32) w.misc[i] = 0.;
   __syncwarp();
   if (P.initialize) equilibration<KT>(P, w, tb, 0.3, T, true, lane);
+  // gases in #/m3 (mo_salsa_driver.f90:285-290)
+  double zg[5] = {0., 0., 0., 0., 0.};
+  if (P.raw_gas >= 0)
+    for (int i = 0; i < 5; i++) zg[i] = raw[P.raw_gas + i] * dn;
   STAGE_MARK(0);
 
   // ---- salsa() ----
   if (P.st_coag) coagulation<KT>(P, w, tb, dt, T, pres, DIAG, lane);
   STAGE_MARK(1);
-  if (P.st_cnd && (P.lscndh2ocl || P.lscndh2oae || P.lscndh2oic))
-    gpparth2o<KT>(P, w, tb, T, pres, rs, rsi, rv, dt, kappa, DIAG, lane);
+  if (P.st_cnd) {
+    // condensation (mo_salsa_dynamics.f90:276-342): nucleation returns only the 3 nm
+    // formation rates, which condgas does not read, and the H2SO4 fraction of the
+    // clusters: 1 for nsnucl = 1-3; for the mixed schemes it only multiplies condgas's
+    // vanishing nucleation term, and 1 stands in
+    if (P.lscndgas) condgas<KT>(P, w, tb, T, pres, dt, zg, P.nsnucl > 0 ? 1. : 0., lane);
+    if (P.lscndh2ocl || P.lscndh2oae || P.lscndh2oic) gpparth2o<KT>(P, w, tb, T, pres, rs, rsi, rv, dt, kappa, DIAG, lane);
+  }
   STAGE_MARK(2);
   if (P.st_auto && P.auto_mode == 2) autoconv2<KT>(P, w, dt, lane);
   if (P.st_activ && P.activ_mode == 1) act_interst<KT>(P, w, tb, rv, rs, T, DIAG, lane);
@@ -2355,6 +2474,8 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   // interstitial activation leaves the activated-droplet outputs at zero (:879, local pactd)
   for (int i = lane; i < P.ncld * (1 + nwet); i += 32) raw[P.raw_nact + i] = 0.;
   if (lane == 0) raw[RW_RV] = (rv - rv_old) / dt;
+  if (P.raw_gas >= 0 && lane == 0)   // :369-384
+    for (int i = 0; i < 5; i++) raw[P.raw_gas + i] = ((zg[i] / dn) - raw[P.raw_gas + i]) / dt;
   if (DIAG && P.raw_diag >= 0 && lane == 0) {
     const double *d = w.misc + M_DIAG;
     double *o = raw + P.raw_diag;

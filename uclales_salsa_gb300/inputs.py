@@ -122,8 +122,12 @@ def _cloud_mask(spec, gen, X, Y, Z, device):
     return m.reshape(-1)
 
 
-def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnostics=1, seed=None):
-    """Build the fields of workload `name` (optionally with a smaller interior)."""
+def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnostics=1, seed=None, gases=False):
+    """Build the fields of workload `name` (optionally with a smaller interior).
+
+    gases: seeded condensing-vapour concentrations in gaero (H2SO4 and non-volatile
+    organics 1e5-1e7 /cm3, semi-volatile organics 1e6-1e8 /cm3, HNO3 and NH3 1e8-1e9
+    /cm3, log-uniform) and gas condensation switched on; otherwise gaero is zero."""
     spec = dict(WORKLOADS[name])
     if X is not None:
         spec["X"], spec["Y"], spec["Z"] = X, Y, Z
@@ -264,6 +268,13 @@ def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnos
         fields["indef"] = pad(_u(gen, lay.nliquid * ncell, 0.0, 0.05, dev).reshape(lay.nliquid, ncell), lay.nliquid)
     if "kappa" in spec:
         fields["kappa"] = pad(_u(gen, ncell, *spec["kappa"], dev)[None], 1)[0]
+    if gases:
+        lo = torch.tensor([1.e5, 1.e8, 1.e8, 1.e5, 1.e6], **f64).log()
+        hi = torch.tensor([1.e7, 1.e9, 1.e9, 1.e7, 1.e8], **f64).log()
+        u = torch.rand((5, ncell), generator=gen, **f64)
+        conc = torch.exp(lo[:, None] + (hi - lo)[:, None] * u) * 1.e6     # #/m3
+        fields["gaero"] = pad(conc / dn, 5)
+        cfg.lscndgas = 1
     return SalsaInputs(name=name, cfg=cfg, layout=lay, nzp=nzp, nxp=nxp, nyp=nyp, ns=nwet, dt=spec["dt"],
                        level=level, fields=fields)
 
@@ -286,4 +297,6 @@ def make_outputs(inp, device=None, with_diag=True):
     if with_diag:
         nd = 17 if inp.level == 5 else 12
         out["diag"] = z(nd)
+    if inp.cfg.lscndgas:
+        out["gaerot"] = z(5)
     return out
