@@ -31,6 +31,7 @@
 #define PI     3.1415927
 #define PI6    0.5235988
 #define MAIR   28.97e-3
+#define CPA    1005.
 #define EPSR   DBL_EPSILON
 #define RD     287.04
 #define ALV    2.5e6
@@ -1414,6 +1415,188 @@ static double intgV(double ikk, double icc, double ilow, double ihigh) {   /* :1
   return (1. / 3.) * ikk * fmaxd(cube(ihigh) - cube(ilow), 0.) + 0.5 * icc * fmaxd(sq(ihigh) - sq(ilow), 0.);
 }
 
+/* :116-157 getSolute: moles of dissolved solute per particle of each aerosol bin */
+static void getSolute(const Cell *w, double *pns) {
+  const salsa_ref_ctx_t *c = w->c;
+  for (int kk = 0; kk <= c->fn2b; kk++) {
+    pns[kk] = 0.;
+    const Section *a = &w->aero[kk];
+    if (a->numc > a->nlim) {
+      for (int nn = 0; nn < c->ndry; nn++) pns[kk] = pns[kk] + c->diss[nn] * a->volc[nn] * c->rholiq[nn] / c->MM[nn];
+      pns[kk] = pns[kk] / a->numc;
+    }
+  }
+}
+
+/* :1199-1378 activate3: number and volume of the activated droplets of every cloud bin,
+   from piecewise-linear number densities in dry volume integrated above the critical
+   volume.  The state is not changed; only pactd (actd_n, actd_v) is. */
+static void activate3(Cell *w, int bcrita, const double *pdcrit, const double *pdcrlo, const double *pdcrhi,
+                      double pdcstar, double *actd_n, double *actd_v) {
+  const salsa_ref_ctx_t *c = w->c;
+  const Section *ae = w->aero;
+  const int ndry = c->ndry, nwet = c->nwet, iwa = c->iwa;
+  int all_small = 1;
+  for (int k = 0; k <= c->fn2b; k++) if (!(pdcrit[k] < EPSR)) all_small = 0;
+  if (all_small) return;
+  double zvcstar = 0., Vmid, Vhi, Vlo, zhlp;
+  const Section *bc = &ae[bcrita];
+  if (bc->numc < bc->nlim) {
+    Vmid = PI6 * cube(bc->dmid);
+  } else {
+    double sd = 0.;
+    for (int i = 0; i < ndry; i++) sd += bc->volc[i];
+    Vmid = sd / fmaxd(bc->nlim, bc->numc);
+  }
+  Vhi = bc->vhilim;
+  Vlo = bc->vlolim;
+  if (pdcstar >= pdcrit[bcrita]) {
+    zhlp = (PI6 * cube(pdcstar) - PI6 * cube(pdcrit[bcrita])) /
+           fmaxd(EPSR, PI6 * cube(pdcrhi[bcrita]) - PI6 * cube(pdcrit[bcrita]));
+    zvcstar = Vmid + zhlp * (Vhi - Vmid);
+  } else if (pdcstar < pdcrit[bcrita]) {
+    zhlp = (PI6 * cube(pdcrit[bcrita]) - PI6 * cube(pdcstar)) /
+           fmaxd(EPSR, PI6 * cube(pdcrit[bcrita]) - PI6 * cube(pdcrlo[bcrita]));
+    zvcstar = Vmid - zhlp * (Vmid - Vlo);
+  }
+  zvcstar = fmaxd(zvcstar, bc->vlolim);
+  zvcstar = fmind(zvcstar, bc->vhilim);
+  for (int cb = c->ica_cur; cb <= c->fcb_cur; cb++) {
+    const int ab = cb <= c->fca_cur ? c->ica_par + (cb - c->ica_cur) : c->icb_par + (cb - c->icb_cur);
+    const Section *a = &ae[ab];
+    if (a->numc < a->nlim) continue;
+    double Nmid = fmaxd(a->numc, a->nlim), sd = 0.;
+    for (int i = 0; i < ndry; i++) sd += a->volc[i];
+    Vmid = sd / Nmid;
+    Vlo = a->vlolim;
+    Vhi = a->vhilim;
+    double Nim1, Vim1, Vlom1, Vhim1, Nip1, Vip1, Vlop1, Vhip1;
+    if (ab == c->in1a || ab == c->in2b) {
+      Nim1 = a->nlim;
+      Vim1 = Vlo / 2.;
+      Vlom1 = 0.;
+      Vhim1 = Vlo;
+    } else {
+      const Section *m = &ae[ab - 1];
+      Nim1 = fmaxd(m->numc, m->nlim);
+      if (Nim1 > m->nlim) {
+        double v = 0.;
+        for (int i = 0; i < ndry; i++) v += m->volc[i];
+        Vim1 = v / Nim1;
+      } else {
+        Vim1 = PI6 * cube(m->dmid);
+      }
+      Vlom1 = m->vlolim;
+      Vhim1 = m->vhilim;
+    }
+    if (ab == c->fn2a || ab == c->fn2b) {
+      Nip1 = a->nlim;
+      Vip1 = Vhi + 0.5 * (Vhi - Vlo);
+      Vlop1 = Vhi;
+      Vhip1 = Vhi + (Vhi - Vlo);
+    } else {
+      const Section *q = &ae[ab + 1];
+      Nip1 = fmaxd(q->numc, q->nlim);
+      if (Nip1 > q->nlim) {
+        double v = 0.;
+        for (int i = 0; i < ndry; i++) v += q->volc[i];
+        Vip1 = v / Nip1;
+      } else {
+        Vip1 = PI6 * cube(q->dmid);
+      }
+      Vlop1 = q->vlolim;
+      Vhip1 = q->vhilim;
+    }
+    Vip1 = fmaxd(Vlop1, fmind(Vip1, Vhip1));
+    Vim1 = fmaxd(Vlom1, fmind(Vim1, Vhim1));
+    const double dNim1 = Nim1 / (Vhim1 - Vlom1), dNip1 = Nip1 / (Vhip1 - Vlop1), dNmid = Nmid / (Vhi - Vlo);
+    const double zs1 = (dNmid - dNim1) / (Vmid - Vim1), zs2 = (dNip1 - dNmid) / (Vip1 - Vmid);
+    const double N01 = dNmid - zs1 * Vmid, N02 = dNip1 - zs2 * Vip1;
+    const double Nnorm = intgN(zs1, N01, Vlo, Vmid) + intgN(zs2, N02, Vmid, Vhi);
+    const double Vnorm = intgV(zs1, N01, Vlo, Vmid) + intgV(zs2, N02, Vmid, Vhi);
+    double nact = 0., zactvol = 0.;
+    int set = 0;
+    if (zvcstar < Vmid) {
+      const double zvcint = fmaxd(zvcstar, Vlo);
+      nact = (Nmid / Nnorm) * (intgN(zs1, N01, zvcint, Vmid) + intgN(zs2, N02, Vmid, Vhi));
+      zactvol = (Nmid * Vmid / Vnorm) * (intgV(zs1, N01, zvcint, Vmid) + intgV(zs2, N02, Vmid, Vhi));
+      set = 1;
+    } else if (zvcstar >= Vmid) {
+      const double zvcint = fmind(zvcstar, Vhi);
+      nact = (Nmid / Nnorm) * (intgN(zs2, N02, zvcint, Vhi));
+      zactvol = (Nmid * Vmid / Vnorm) * (intgV(zs2, N02, zvcint, Vhi));
+      set = 1;
+    }
+    double *av = actd_v + cb * NSP;
+    if (set) {
+      actd_n[cb] = nact;
+      for (int ss = 0; ss < nwet; ss++) av[ss] = zactvol * (a->volc[ss] / (Vmid * Nmid));
+    }
+    actd_n[cb] = fmaxd(0., actd_n[cb]);
+    for (int ss = 0; ss < nwet; ss++) av[ss] = fmaxd(0., av[ss]);
+    av[iwa] = actd_n[cb] * PI6 * cube(pdcrit[ab]) * fmind(2., sq(3.e-6 / fmaxd(EPSR, pdcrit[ab])));
+  }
+}
+
+/* :161-375 ActCloudBase (Abdul-Razzak & Ghan 2002, sectional form): maximum parcel
+   supersaturation at cloud base from the updraft, critical diameters per bin, then
+   activate3 */
+static void ActCloudBase(Cell *w, double pres, double temp, double wvel, double *actd_n, double *actd_v) {
+  const salsa_ref_ctx_t *c = w->c;
+  const Section *ae = w->aero;
+  const int in1a = c->in1a, fn2a = c->fn2a, in2b = c->in2b, fn2b = c->fn2b;
+  const double mwa = c->mwa, rhowa = c->rhowa;
+  const double bb = 6. * mwa / (PI * rhowa);
+  double ns[MAXB], scrit[MAXB], frac[MAXB], zdcrit[MAXB], zdcrlo[MAXB], zdcrhi[MAXB];
+  for (int k = 0; k < MAXB; k++) frac[k] = zdcrit[k] = zdcrlo[k] = zdcrhi[k] = 0.;
+  int bcrita = fn2a, bcritb = fn2b;
+  double zdcstar = 0.;
+  getSolute(w, ns);
+  if (wvel > 0.) {
+    const double aa = 4. * mwa * SURFW0 / (RG * rhowa * temp);
+    const double x = 4. * cube(aa) / (27. * bb);
+    for (int k = in1a; k <= fn2b; k++) scrit[k] = exp(sqrt(x / fmaxd(EPSR, ns[k]))) - 1.;
+    double ntot = 0., sum1 = 0.;
+    for (int k = in1a; k <= fn2b; k++) ntot += ae[k].numc;
+    for (int k = in1a; k <= fn2b; k++) sum1 += ae[k].numc / pow(scrit[k], 2. / 3.);
+    if (!(ntot < ae[0].nlim)) {
+      const double V = wvel;
+      const double L = 2.501e6 - 2370. * (temp - 273.15);
+      const double a1 = 1. - (373.15 / temp);
+      const double ps = 101325. * exp(13.3185 * a1 - 1.976 * sq(a1) - 0.6445 * cube(a1) - 0.1299 * sq(sq(a1)));
+      const double alpha = GRAV * mwa * L / (CPA * RG * sq(temp)) - GRAV * MAIR / (RG * temp);
+      const double gamma = RG * temp / (ps * mwa) + mwa * sq(L) / (CPA * pres * MAIR * temp);
+      const double x1 = pres / 101325.;
+      const double dv1 = 1.e-4 * (0.211 / x1) * pow(temp / 273., 1.94);
+      const double ka1 = 1.e-3 * (4.39 + 0.071 * temp);
+      const double Gc = 1. / (rhowa * RG * temp / (ps * dv1 * mwa) + L * rhowa / (ka1 * temp) * (L * mwa / (temp * RG) - 1.));
+      const double s_eff = sqrt(cube(ntot / sum1));
+      const double theta = (sqrt(cube(alpha * V / Gc))) / (2. * PI * rhowa * gamma * ntot);
+      const double khi = (2. / 3.) * aa * sqrt(alpha * V / Gc);
+      const double s_max = s_eff / sqrt(0.5 * sqrt(cube(khi / theta)) + pow(sq(s_eff) / (theta + 3. * khi), 0.75));
+      zdcstar = 2. * aa / (3. * s_max);
+      for (int kk = in1a; kk <= fn2b; kk++) {
+        if (ae[kk].numc < ae[kk].nlim) continue;
+        const double nshi = ns[kk] * ae[kk].vratiohi;
+        const double sil = exp(sqrt(x / nshi)) - 1.;
+        if (s_max < sil) continue;
+        const double nslo = ns[kk] * ae[kk].vratiolo;
+        const double siu = exp(sqrt(x / nslo)) - 1.;
+        frac[kk] = fmind(1., log(s_max / sil) / log(siu / sil));
+        zdcrlo[kk] = 2. * sqrt(3. * nslo * bb / aa);
+        zdcrhi[kk] = 2. * sqrt(3. * nshi * bb / aa);
+        zdcrit[kk] = 2. * sqrt(3. * ns[kk] * bb / aa);
+      }
+      for (int kk = in1a; kk <= fn2a; kk++)
+        if (frac[kk] < 1. && frac[kk] > 0.) { bcrita = kk; break; }
+      for (int kk = in2b; kk <= fn2b; kk++)
+        if (frac[kk] < 1. && frac[kk] > 0.) { bcritb = kk; break; }
+    }
+  }
+  (void)bcritb;   /* computed by the reference, never read by activate3 */
+  activate3(w, bcrita, zdcrit, zdcrlo, zdcrhi, zdcstar, actd_n, actd_v);
+}
+
 /* :859-1195 actInterst */
 static void actInterst(Cell *w, double prv, double prs, double temp) {
   const salsa_ref_ctx_t *c = w->c;
@@ -2279,7 +2462,6 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
                        double pw, int level, double *actd_n, double *actd_v, double *zg) {
   const salsa_ref_ctx_t *c = w->c;
   const salsa_config_t *g = &c->cfg;
-  (void)pw;
   if (c->st_coag) coagulation(w, ptstep, ptemp, ppres);
   if (c->st_cnd) {
     /* condensation :276-342.  nucleation (mo_salsa_nucleation.f90:72-625) only returns the
@@ -2294,6 +2476,7 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
   if (c->st_activ) {
     for (int k = 0; k < c->ncld; k++) { actd_n[k] = 0.; for (int s = 0; s < NSP; s++) actd_v[k * NSP + s] = 0.; }
     if (g->lsactiv.mode == 1) actInterst(w, *prv, prs, ptemp);
+    if (g->lsactiv.mode == 2) ActCloudBase(w, ppres, ptemp, pw, actd_n, actd_v);
   }
   if (c->st_icenucl || g->lsicenucl.mode == 2) {
     if (g->lsicehom || g->lsiceimm || g->lsicedep) {
@@ -2340,7 +2523,7 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (!cfg || !out) return SALSA_E_ARG;
   if (cfg->nbin[0] < 1 || cfg->nbin[1] < 4 || cfg->prc_nbins < 1 || cfg->ice_nbins < 1) return SALSA_E_ARG;
   if (cfg->nspec_dry < 1 || cfg->nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
-  if (cfg->lssecice.sw || cfg->lscoag.mode == 2 || cfg->lsactiv.mode == 2) return SALSA_E_UNSUPPORTED;
+  if (cfg->lssecice.sw || cfg->lscoag.mode == 2) return SALSA_E_UNSUPPORTED;
   /* nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
      nj3 outside 1-3 STOPs once a cell nucleates (:600-602) */
   if (cfg->nsnucl == 4 || cfg->nsnucl < 0 || (cfg->nsnucl > 0 && (cfg->nj3 < 1 || cfg->nj3 > 3)))
@@ -2502,6 +2685,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
   if (level == 5 && g->ice_theta_dist && !f->indef) return SALSA_E_ARG;
   if (lcharge && !f->chargeTime) return SALSA_E_ARG;
   if (g->lscndgas && (!f->gaero || !f->gaerot)) return SALSA_E_ARG;
+  if (g->lsactiv.sw && g->lsactiv.mode == 2 && !f->wp) return SALSA_E_ARG;
   /* set_SALSA_runtime (sticky states) */
   const salsa_switch_t *ms[7] = {&g->lscoag, &g->lscnd, &g->lsauto, &g->lsactiv, &g->lsicenucl, &g->lsicemelt,
                                  &g->lssecice};

@@ -5,8 +5,10 @@ a workload: the classic ice nucleation (mo_salsa_cloud_ice.f90:26-140), every SE
 freezing mode, ice melting (mo_salsa_cloud_ice.f90:393-462), the second
 autoconversion mode (mo_salsa_cloud.f90 autoconv2), the charging enhancement of the
 collision kernels (mo_salsa_coagulation_kernels.f90:411-416), the initialising call
-(run_SALSA with initialize=.TRUE.), a step without coagulation, and gas condensation
-with nucleation switched on (mo_salsa_dynamics.f90:276-685) at levels 5 and 4.  The criterion is
+(run_SALSA with initialize=.TRUE.), a step without coagulation, gas condensation with
+nucleation switched on (mo_salsa_dynamics.f90:276-685) and cloud-base activation
+(mo_salsa_cloud.f90:161-375, 1199-1378), the last two at levels 5 and 4.  The
+activated-droplet outputs are checked as well.  The criterion is
 the one of test_gpu_parity.py.
 """
 import pytest
@@ -16,6 +18,7 @@ from uclales_salsa_gb300.inputs import make_inputs, make_outputs
 from uclales_salsa_gb300.api import SalsaStep
 from oracle_ref import Oracle
 from test_gpu_parity import check, VIOL_FRAC, FRAC_WITHIN, PERTURBED
+from parity import FLOOR, interior
 
 pytestmark = pytest.mark.gpu
 
@@ -48,6 +51,10 @@ def _nucleation(inp, f):
     inp.cfg.nsnucl = 1     # binary nucleation; gas condensation comes with the gas fields
 
 
+def _cloudbase(inp, f):
+    inp.cfg.lsactiv.mode = 2
+
+
 def _charge(inp, f):
     lay = inp.layout
     g = torch.Generator().manual_seed(5)
@@ -66,7 +73,23 @@ CASES = [
     ("initialize", "grid16x16x40", dict(X=8, Y=8, Z=16), lambda inp, f: None, dict(initialize=1)),
     ("gas_condensation", "grid256x256x128", dict(X=8, Y=8, Z=16, gases=True), _nucleation, {}),
     ("gas_condensation_level4", "grid16x16x40", dict(X=8, Y=8, Z=16, gases=True), _nucleation, {}),
+    ("cloudbase_activation", "grid384x384x160", dict(X=12, Y=12, Z=8), _cloudbase, {}),
+    ("cloudbase_activation_level4", "grid16x16x40", dict(X=8, Y=8, Z=16), _cloudbase, {}),
 ]
+
+
+def check_activation(inp, gpu, ref, env, rtol):
+    """The activated-droplet outputs (per kg of air) under the criterion of check()."""
+    rep = {}
+    I = lambda t: interior(t, inp.nzp, inp.nxp, inp.nyp)
+    for k, fl in (("pa_nactd", FLOOR["n"]), ("pa_vactd", FLOOR["m"])):
+        a, b, e = I(gpu[k]), I(ref[k]), I(env[k])
+        scale = b.abs().clamp(min=fl)
+        err = (a - b).abs()
+        rel = err / scale
+        rep[k] = dict(max_rel=float(rel.max()), frac_within=float((rel <= rtol).double().mean()),
+                      violations=int((err > torch.maximum(rtol * scale, 10.0 * e)).sum()), n=rel.numel())
+    return rep
 
 
 def _oracle(inp, fields, kw, pf=None, eps=0.0):
@@ -101,6 +124,7 @@ def test_variant_parity(name, wl, kw, mod, call):
     gpu = {k: v.cpu() for k, v in out.items()}
     step.close()
     rep = check(inp, gpu, ref, env, 1e-10)
+    rep.update(check_activation(inp, gpu, ref, env, 1e-10))
     print(name, rep)
     for k, r in rep.items():
         assert r["violations"] <= VIOL_FRAC * r["n"], (name, k, r)

@@ -247,6 +247,37 @@ def test_nucleation_does_not_change_the_step():
             assert torch.equal(out[k], base[k]), (nsnucl, k)
 
 
+def test_cloud_base_activation():
+    """lsactiv%mode = 2 (mo_salsa_cloud.f90:161-375, 1199-1378): only updraft cells
+    activate, the state is unchanged (the activated droplets are outputs only), and a
+    stronger updraft activates more droplets in total."""
+    def tw(c):
+        c.lsactiv.mode = 2
+    inp, f, out, rc, st, _ = run("grid384x384x160", tw, X=8, Y=8, Z=8)
+    assert rc == 0
+    I = lambda t: interior(t, inp.nzp, inp.nxp, inp.nyp)
+    na, w = I(out["pa_nactd"]).sum(0), I(inp.fields["wp"])
+    assert bool(torch.isfinite(out["pa_vactd"]).all()) and float(I(out["pa_vactd"]).min()) >= 0
+    assert float(na[w <= 0].abs().max()) == 0 and float((na[w > 0] > 0).double().mean()) > 0.95
+    assert float((na[w > 0] / I(inp.fields["naero"]).sum(0)[w > 0]).max()) < 1
+    # the same step with mode 1 changes the state; mode 2 leaves it to the other processes
+    def off(c):
+        only("lsactiv")(c)
+        c.lsactiv.mode = 2
+    inp0, _, out0, rc0, _, _ = run("grid384x384x160", off, X=8, Y=8, Z=8)
+    assert rc0 == 0
+    for k in ("naerot", "ncloudt", "maerot", "mcloudt"):   # the unit round trip's rounding only
+        old = I(inp0.fields[k[:-1]])
+        assert float((I(out0[k]).abs() * inp0.dt - 4.5e-16 * old.abs()).max()) <= 0, k
+    inp2 = make_inputs("grid384x384x160", "cpu", X=8, Y=8, Z=8)
+    tw(inp2.cfg)
+    f2 = {k: v.clone() for k, v in inp2.fields.items()}
+    f2["wp"] = f2["wp"] * 4
+    out2 = make_outputs(inp2)
+    assert Oracle(inp2.cfg).run(inp2, f2, out2, time=1.0)[0] == 0
+    assert float(I(out2["pa_nactd"]).sum()) > float(na.sum())
+
+
 def test_threads_do_not_change_results():
     inp1, _, o1, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, nthreads=1)
     inp2, _, o2, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, nthreads=0)

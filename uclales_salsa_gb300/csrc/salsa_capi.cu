@@ -211,7 +211,7 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
   if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
   // processes outside this build (the init check mirrors the oracle's)
-  if (g.lssecice.sw || g.lscoag.mode == 2 || g.lsactiv.mode == 2) return SALSA_E_UNSUPPORTED;
+  if (g.lssecice.sw || g.lscoag.mode == 2) return SALSA_E_UNSUPPORTED;
   // nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
   // nj3 outside 1-3 STOPs once a cell nucleates (:600-602)
   if (g.nsnucl == 4 || g.nsnucl < 0 || (g.nsnucl > 0 && (g.nj3 < 1 || g.nj3 > 3))) return SALSA_E_UNSUPPORTED;
@@ -612,6 +612,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   if (level == 5 && g.ice_theta_dist && !f->indef) return SALSA_E_ARG;
   if (lcharge && !f->chargeTime) return SALSA_E_ARG;
   if (g.lscndgas && (!f->gaero || !f->gaerot)) return SALSA_E_ARG;
+  if (g.lsactiv.sw && g.lsactiv.mode == 2 && !f->wp) return SALSA_E_ARG;
   if (cudaSetDevice(h->device) != cudaSuccess) return SALSA_E_NODEV;
 
   // set_SALSA_runtime (mo_salsa_driver.f90:445-474): states switch on once and stay on

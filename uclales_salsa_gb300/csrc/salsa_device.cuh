@@ -23,6 +23,7 @@
 #define K_PI 3.1415927
 #define K_PI6 0.5235988
 #define K_MAIR 28.97e-3
+#define K_CPA 1005.
 #define K_EPS 2.220446049250313e-16
 #define K_RD 287.04
 #define K_ALV 2.5e6

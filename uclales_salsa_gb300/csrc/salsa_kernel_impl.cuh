@@ -1502,6 +1502,173 @@ __device__ __forceinline__ double intgV(double k, double c, double lo, double hi
   return (1. / 3.) * k * fmax(cube(hi) - cube(lo), 0.) + 0.5 * c * fmax(hi * hi - lo * lo, 0.);
 }
 
+// ----------------------------------------------------------------------------------------
+// Cloud-base activation: mo_salsa_cloud.f90:161-375 (ActCloudBase: Abdul-Razzak & Ghan,
+// sectional form) and :1199-1378 (activate3).  The updraft sets the parcel's maximum
+// supersaturation, which gives a critical diameter per bin; the activated number and
+// volume of each cloud bin are integrals of piecewise-linear number densities in dry
+// volume above the critical volume.  The state does not change: the results go to the
+// activated-droplet outputs (raw rows, per kg of air).  One lane per aerosol bin, then
+// one lane per cloud bin; sums run in bin order on every lane.
+// ----------------------------------------------------------------------------------------
+template <typename KT>
+__device__ void act_cloudbase(const DevParams &P, const WS<KT> &w, const double *tb, double pres, double T,
+                              double wvel, double dn, double *raw, int lane) {
+  const int in1a = P.in1a, fn2a = P.fn2a, in2b = P.in2b, fn2b = P.fn2b, ndry = P.ndry, nwet = P.nwet;
+  const int iwa = P.iwa, ncld = P.ncld;
+  const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad, *vhi = tb + TAB_VHI * P.nb_pad;
+  const double *vrlo = tb + TAB_VRLO * P.nb_pad, *vrhi = tb + TAB_VRHI * P.nb_pad;
+  double *ns = w.sc(0), *zdcrit = w.sc(1), *zdcrlo = w.sc(2), *zdcrhi = w.sc(3), *frac = w.sc(4), *term = w.sc(5);
+  const double bb = 6. * K_MWA / (K_PI * K_RHOWA);   // Raoult term per mole of solute [m3]
+  // getSolute (:116-157): moles of dissolved solute per particle
+  for (int k = lane; k <= fn2b; k += 32) {
+    double n_ = 0.;
+    if (w.numc[k] > K_NLIM) {
+      for (int nn = 0; nn < ndry; nn++) n_ = n_ + P.diss[nn] * w.v(nn, k) * P.rholiq[nn] / P.MM[nn];
+      n_ = n_ / w.numc[k];
+    }
+    ns[k] = n_;
+    frac[k] = zdcrit[k] = zdcrlo[k] = zdcrhi[k] = 0.;
+  }
+  __syncwarp();
+  int bcrita = fn2a;
+  double zdcstar = 0.;
+  if (wvel > 0.) {
+    const double aa = 4. * K_MWA * K_SURFW0 / (K_RG * K_RHOWA * T);   // Kelvin term [m]
+    const double x = 4. * cube(aa) / (27. * bb);
+    for (int k = in1a + lane; k <= fn2b; k += 32) {
+      const double scrit = exp(sqrt(x / fmax(K_EPS, ns[k]))) - 1.;
+      term[k] = w.numc[k] / pow(scrit, 2. / 3.);
+    }
+    __syncwarp();
+    double ntot = 0., sum1 = 0.;   // part 3, eq. (8)
+    for (int k = in1a; k <= fn2b; k++) ntot += w.numc[k];
+    for (int k = in1a; k <= fn2b; k++) sum1 += term[k];
+    if (!(ntot < K_NLIM)) {
+      const double V = wvel;
+      const double L = 2.501e6 - 2370. * (T - 273.15);
+      const double a1 = 1. - (373.15 / T);
+      const double ps = 101325. * exp(13.3185 * a1 - 1.976 * sq(a1) - 0.6445 * cube(a1) - 0.1299 * sq(sq(a1)));
+      const double alpha = K_GRAV * K_MWA * L / (K_CPA * K_RG * sq(T)) - K_GRAV * K_MAIR / (K_RG * T);
+      const double gamma = K_RG * T / (ps * K_MWA) + K_MWA * sq(L) / (K_CPA * pres * K_MAIR * T);
+      const double x1 = pres / 101325.;
+      const double dv1 = 1.e-4 * (0.211 / x1) * pow(T / 273., 1.94);
+      const double ka1 = 1.e-3 * (4.39 + 0.071 * T);
+      const double Gc = 1. / (K_RHOWA * K_RG * T / (ps * dv1 * K_MWA) +
+                              L * K_RHOWA / (ka1 * T) * (L * K_MWA / (T * K_RG) - 1.));
+      const double s_eff = sqrt(cube(ntot / sum1));
+      const double theta = (sqrt(cube(alpha * V / Gc))) / (2. * K_PI * K_RHOWA * gamma * ntot);
+      const double khi = (2. / 3.) * aa * sqrt(alpha * V / Gc);
+      const double s_max = s_eff / sqrt(0.5 * sqrt(cube(khi / theta)) + pow(sq(s_eff) / (theta + 3. * khi), 0.75));
+      zdcstar = 2. * aa / (3. * s_max);
+      for (int kk = in1a + lane; kk <= fn2b; kk += 32) {
+        if (w.numc[kk] < K_NLIM) continue;
+        const double nshi = ns[kk] * vrhi[kk];
+        const double sil = exp(sqrt(x / nshi)) - 1.;
+        if (s_max < sil) continue;
+        const double nslo = ns[kk] * vrlo[kk];
+        const double siu = exp(sqrt(x / nslo)) - 1.;
+        frac[kk] = fmin(1., log(s_max / sil) / log(siu / sil));
+        zdcrlo[kk] = 2. * sqrt(3. * nslo * bb / aa);
+        zdcrhi[kk] = 2. * sqrt(3. * nshi * bb / aa);
+        zdcrit[kk] = 2. * sqrt(3. * ns[kk] * bb / aa);
+      }
+      __syncwarp();
+      for (int kk = in1a; kk <= fn2a; kk++)   // the critical bin of regime a
+        if (frac[kk] < 1. && frac[kk] > 0.) { bcrita = kk; break; }
+    }
+  }
+  // activate3: nothing activates when no bin has a critical diameter
+  bool big = false;
+  for (int k = lane; k <= fn2b; k += 32) big |= !(zdcrit[k] < K_EPS);
+  if (!warp_any(big)) return;
+  double Vmid, Vlo, Vhi;
+  if (w.numc[bcrita] < K_NLIM) {
+    Vmid = K_PI6 * cube(dmid[bcrita]);
+  } else {
+    double sd = 0.;
+    for (int i = 0; i < ndry; i++) sd += w.v(i, bcrita);
+    Vmid = sd / fmax(K_NLIM, w.numc[bcrita]);
+  }
+  Vhi = vhi[bcrita];
+  Vlo = vlo[bcrita];
+  double zvcstar = 0.;
+  const double dc = zdcrit[bcrita];
+  if (zdcstar >= dc) {
+    const double zhlp = (K_PI6 * cube(zdcstar) - K_PI6 * cube(dc)) / fmax(K_EPS, K_PI6 * cube(zdcrhi[bcrita]) - K_PI6 * cube(dc));
+    zvcstar = Vmid + zhlp * (Vhi - Vmid);
+  } else if (zdcstar < dc) {
+    const double zhlp = (K_PI6 * cube(dc) - K_PI6 * cube(zdcstar)) / fmax(K_EPS, K_PI6 * cube(dc) - K_PI6 * cube(zdcrlo[bcrita]));
+    zvcstar = Vmid - zhlp * (Vmid - Vlo);
+  }
+  zvcstar = fmax(zvcstar, vlo[bcrita]);
+  zvcstar = fmin(zvcstar, vhi[bcrita]);
+  for (int cb = lane; cb < ncld; cb += 32) {
+    const int ab = (cb <= P.fca_cur) ? P.ica_par + (cb - P.ica_cur) : P.icb_par + (cb - P.icb_cur);
+    if (w.numc[ab] < K_NLIM) continue;
+    const double Nmid = fmax(w.numc[ab], K_NLIM);
+    double sd = 0.;
+    for (int i = 0; i < ndry; i++) sd += w.v(i, ab);
+    const double Vm = sd / Nmid, Vl = vlo[ab], Vh = vhi[ab];
+    double Nim1, Vim1, Vlom1, Vhim1, Nip1, Vip1, Vlop1, Vhip1;
+    if (ab == in1a || ab == in2b) {
+      Nim1 = K_NLIM; Vim1 = Vl / 2.; Vlom1 = 0.; Vhim1 = Vl;
+    } else {
+      Nim1 = fmax(w.numc[ab - 1], K_NLIM);
+      if (Nim1 > K_NLIM) {
+        double v = 0.;
+        for (int i = 0; i < ndry; i++) v += w.v(i, ab - 1);
+        Vim1 = v / Nim1;
+      } else {
+        Vim1 = K_PI6 * cube(dmid[ab - 1]);
+      }
+      Vlom1 = vlo[ab - 1]; Vhim1 = vhi[ab - 1];
+    }
+    if (ab == fn2a || ab == fn2b) {
+      Nip1 = K_NLIM; Vip1 = Vh + 0.5 * (Vh - Vl); Vlop1 = Vh; Vhip1 = Vh + (Vh - Vl);
+    } else {
+      Nip1 = fmax(w.numc[ab + 1], K_NLIM);
+      if (Nip1 > K_NLIM) {
+        double v = 0.;
+        for (int i = 0; i < ndry; i++) v += w.v(i, ab + 1);
+        Vip1 = v / Nip1;
+      } else {
+        Vip1 = K_PI6 * cube(dmid[ab + 1]);
+      }
+      Vlop1 = vlo[ab + 1]; Vhip1 = vhi[ab + 1];
+    }
+    Vip1 = fmax(Vlop1, fmin(Vip1, Vhip1));
+    Vim1 = fmax(Vlom1, fmin(Vim1, Vhim1));
+    const double dNim1 = Nim1 / (Vhim1 - Vlom1), dNip1 = Nip1 / (Vhip1 - Vlop1), dNmid = Nmid / (Vh - Vl);
+    const double zs1 = (dNmid - dNim1) / (Vm - Vim1), zs2 = (dNip1 - dNmid) / (Vip1 - Vm);
+    const double N01 = dNmid - zs1 * Vm, N02 = dNip1 - zs2 * Vip1;
+    const double Nnorm = intgN(zs1, N01, Vl, Vm) + intgN(zs2, N02, Vm, Vh);
+    const double Vnorm = intgV(zs1, N01, Vl, Vm) + intgV(zs2, N02, Vm, Vh);
+    double nact = 0., zactvol = 0.;
+    bool set = false;
+    if (zvcstar < Vm) {
+      const double zvcint = fmax(zvcstar, Vl);
+      nact = (Nmid / Nnorm) * (intgN(zs1, N01, zvcint, Vm) + intgN(zs2, N02, Vm, Vh));
+      zactvol = (Nmid * Vm / Vnorm) * (intgV(zs1, N01, zvcint, Vm) + intgV(zs2, N02, Vm, Vh));
+      set = true;
+    } else if (zvcstar >= Vm) {
+      const double zvcint = fmin(zvcstar, Vh);
+      nact = (Nmid / Nnorm) * (intgN(zs2, N02, zvcint, Vh));
+      zactvol = (Nmid * Vm / Vnorm) * (intgV(zs2, N02, zvcint, Vh));
+      set = true;
+    }
+    nact = fmax(0., set ? nact : 0.);
+    for (int ss = 0; ss < nwet; ss++) {
+      double v = set ? zactvol * (w.v(ss, ab) / (Vm * Nmid)) : 0.;
+      v = fmax(0., v);
+      if (ss == iwa)   // the activated droplets' water (:1366-1367)
+        v = nact * K_PI6 * cube(zdcrit[ab]) * fmin(2., sq(3.e-6 / fmax(K_EPS, zdcrit[ab])));
+      raw[P.raw_vact + ss * ncld + cb] = v * P.rholiq[ss] / dn;
+    }
+    raw[P.raw_nact + cb] = nact / dn;
+  }
+}
+
 template <typename KT>
 __device__ void act_interst(const DevParams &P, const WS<KT> &w, const double *tb, double prv, double prs, double T,
                             bool diag, int lane) {
@@ -2440,6 +2607,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   STAGE_MARK(2);
   if (P.st_auto && P.auto_mode == 2) autoconv2<KT>(P, w, dt, lane);
   if (P.st_activ && P.activ_mode == 1) act_interst<KT>(P, w, tb, rv, rs, T, DIAG, lane);
+  if (P.st_activ && P.activ_mode == 2) act_cloudbase<KT>(P, w, tb, pres, T, raw[RW_W], dn, raw, lane);
   STAGE_MARK(3);
   if ((P.st_icenucl || P.icenucl_mode == 2) && (P.lsicehom || P.lsiceimm || P.lsicedep)) {
     if (P.ice_theta_dist) ice_nucl_SE<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
@@ -2471,8 +2639,10 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
     *on = ((w.numc[b] / dn) - *on) / dt;
     bad |= !isfinite(w.numc[b]);
   }
-  // interstitial activation leaves the activated-droplet outputs at zero (:879, local pactd)
-  for (int i = lane; i < P.ncld * (1 + nwet); i += 32) raw[P.raw_nact + i] = 0.;
+  // interstitial activation leaves the activated-droplet outputs at zero (:879, local pactd);
+  // cloud-base activation has written them
+  if (!(P.st_activ && P.activ_mode == 2))
+    for (int i = lane; i < P.ncld * (1 + nwet); i += 32) raw[P.raw_nact + i] = 0.;
   if (lane == 0) raw[RW_RV] = (rv - rv_old) / dt;
   if (P.raw_gas >= 0 && lane == 0)   // :369-384
     for (int i = 0; i < 5; i++) raw[P.raw_gas + i] = ((zg[i] / dn) - raw[P.raw_gas + i]) / dt;
