@@ -746,8 +746,6 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     } else if (P.ncells <= 0x7fffffffLL) {
       if (P.ncells > h->order_cap) {
         if (h->d_order) cudaFree(h->d_order);
-  for (int i = 0; i < 4; i++)
-    if (h->scratch[i]) cudaFree(h->scratch[i]);
         h->d_order = nullptr;
         h->order_cap = 0;
         if (cudaMalloc(&h->d_order, (size_t)P.ncells * sizeof(int)) != cudaSuccess) return SALSA_E_CUDA;
