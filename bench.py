@@ -8,8 +8,9 @@ A step is one SALSA call over every interior cell of the workload
             the launch stream around exactly K steps (after W warm-up steps).
   mixed  -- the FP32-mixed form on the same inputs.
   e2e    -- FP64 form through the C-ABI with pinned HOST buffers: the host->device
-            copy of every input and tendency array and the device->host copy of the
-            results are inside the timed region.
+            copy of every array and the device->host copy of the results are inside
+            the timed region (the C-ABI moves them in y-slabs that overlap the
+            computation).
   roofline -- algorithmic bytes per cell-step (8 * (3S + T + G + I + A + D)) over the
             measured HBM copy bandwidth; the step is FP64-pipe bound, so the fraction is
             small and the ncu FP64 pipe figures are in profiles/.
@@ -157,16 +158,19 @@ def run_gb300(args):
         del fields, outs
         torch.cuda.empty_cache()
 
-    # bytes a step moves across the boundary: every input and tendency array in, the
-    # results (and the IN deficit) out
+    # bytes a step moves across the boundary: the C-ABI copies the interior y rows
+    # (nyp - 4 of nyp) of every array it uses in, outputs included (so that their
+    # values outside the interior cells come back unchanged), and of the tendencies,
+    # outputs and IN deficit back out
     inp.cfg.precision = 0
     outs_meta = make_outputs(inp, device="meta")
+    rows = (inp.nyp - 4) / inp.nyp
     inputs_b = sum(v.numel() * 8 for k, v in inp.fields.items() if k in (
         "press", "temp", "rsl", "rsi", "rp", "dn", "wp", "naero", "ncloud", "nprecp", "nice", "maero", "mcloud",
         "mprecp", "mice", "indef"))
-    tend_b = sum(v.numel() * 8 for k, v in outs_meta.items() if k.endswith("t"))
-    h2d = inputs_b + tend_b
-    d2h = field_bytes(outs_meta) + (inp.fields["indef"].numel() * 8 if "indef" in inp.fields else 0)
+    indef_b = inp.fields["indef"].numel() * 8 if "indef" in inp.fields else 0
+    h2d = int(round((inputs_b + field_bytes(outs_meta)) * rows))
+    d2h = int(round((field_bytes(outs_meta) + indef_b) * rows))
     e2e_s = None
     if not args.no_e2e:
         # end to end through the C-ABI with pinned host buffers (FP64 form)

@@ -133,12 +133,33 @@ def test_in_deficit_fraction_matches():
 
 
 def test_host_and_device_pointers_agree():
-    inp = make_inputs("grid256x256x128", "cpu", precision=0, X=8, Y=8, Z=8)
+    """Host arrays go through the slab pipeline (ragged last slab, more slabs than
+    staging slots); the results equal the device-pointer call's, and values outside the
+    interior cells (halo columns, levels 1 and nzp, halo rows) come back unchanged in
+    every output, the outputs that are only written included."""
+    inp = make_inputs("grid256x256x128", "cpu", precision=0, X=8, Y=21, Z=8)
     fh, oh = gpu_run(inp, host=True)
     fd, od = gpu_run(inp, host=False)
     for k in oh:
         assert torch.equal(oh[k], od[k]), k
     assert torch.equal(fh["indef"].cpu(), fd["indef"].cpu())
+    g = torch.Generator().manual_seed(11)
+    pre = {k: torch.rand(v.shape, generator=g, dtype=torch.float64) for k, v in make_outputs(inp).items()}
+    res = {}
+    for host in (True, False):
+        f = {k: (v.clone().pin_memory() if host else v.clone().cuda()) for k, v in inp.fields.items()}
+        out = {k: (v.clone().pin_memory() if host else v.clone().cuda()) for k, v in pre.items()}
+        step = SalsaStep(inp.cfg)
+        rc, st = step.run(inp, f, out, time=1.0)
+        torch.cuda.synchronize()
+        step.close()
+        assert rc == 0
+        res[host] = {k: v.cpu() for k, v in out.items()}
+    for k in pre:
+        assert torch.equal(res[True][k], res[False][k]), k
+        m = torch.ones_like(pre[k], dtype=torch.bool)
+        interior(m, inp.nzp, inp.nxp, inp.nyp).fill_(False)
+        assert torch.equal(res[True][k][m], pre[k][m]), k
 
 
 def test_deterministic_and_diagnostics_do_not_change_state():

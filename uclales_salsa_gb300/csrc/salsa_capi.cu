@@ -119,6 +119,10 @@ double hcube(double x) { return x * x * x; }
 
 }  // namespace
 
+// host-buffer pipeline: staging slots and the number of y-slabs a grid is cut into
+#define SALSA_PIPE_SLOTS 3
+#define SALSA_PIPE_SLABS 16
+
 struct salsa_handle {
   salsa_config_t cfg;
   int device = 0, nsm = 0;
@@ -137,6 +141,8 @@ struct salsa_handle {
   // staging buffers for host-pointer calls
   void *stage = nullptr;
   size_t stage_bytes = 0;
+  cudaStream_t s_in = nullptr, s_out = nullptr;     // copy streams of the host-buffer pipeline
+  cudaEvent_t pev[3 * SALSA_PIPE_SLOTS + 2] = {};   // its slot and start/end events
   int *d_order = nullptr;       // cell order list (salsa_order_kernel)
   long long order_cap = 0;
   int *na_order = nullptr;      // module scratch of salsa_gb300_run_noalloc on this handle's device
@@ -550,6 +556,10 @@ void salsa_gb300_finalize(salsa_handle_t *h) {
   if (h->d_status) cudaFree(h->d_status);
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->stage) cudaFree(h->stage);
+  for (auto e : h->pev)
+    if (e) cudaEventDestroy(e);
+  if (h->s_in) cudaStreamDestroy(h->s_in);
+  if (h->s_out) cudaStreamDestroy(h->s_out);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -694,95 +704,157 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   if (host && !allow_host) return SALSA_E_ARG;
   cudaStream_t s = stream ? stream : h->stream;
   int launches = 0;
-  if (host) {
-    size_t need = 0;
-    for (auto &x : fl) {
-      const void *p = x.src ? (const void *)x.src : (const void *)x.dst;
-      if (p) need += (size_t)(x.planes * P.plane) * sizeof(double);
-    }
-    if (need > h->stage_bytes) {
-      if (h->stage) cudaFree(h->stage);
-      h->stage = nullptr;
-      h->stage_bytes = 0;
-      if (cudaMalloc(&h->stage, need) != cudaSuccess) return SALSA_E_CUDA;
-      h->stage_bytes = need;
-    }
-  }
   for (int i = 0; i < salsa::FI_N; i++) P.fin[i] = nullptr;
   for (int i = 0; i < salsa::FO_N; i++) P.fout[i] = nullptr;
-  size_t off = 0;
-  for (auto &x : fl) {
-    const double *hp = x.src ? x.src : x.dst;
-    if (!hp) continue;
-    double *dp;
-    size_t bytes = (size_t)(x.planes * P.plane) * sizeof(double);
-    if (host) {
-      dp = reinterpret_cast<double *>(static_cast<char *>(h->stage) + off);
-      off += bytes;
-      if (x.in && cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return SALSA_E_CUDA;
-    } else {
-      dp = const_cast<double *>(hp);
-    }
-    if (x.fi >= 0) P.fin[x.fi] = dp;
-    if (x.fo >= 0) {
-      P.fout[x.fo] = dp;
-      if (x.fo == salsa::FO_INDEF) P.fin[salsa::FI_INDEF] = dp;
-      if (x.fo == salsa::FO_CHARGE) P.fin[salsa::FI_CHARGE] = dp;
-    }
-  }
   if (noalloc && P.ncells > SALSA_NOALLOC_MAXCELLS) return SALSA_E_ARG;
   unsigned long long *d_status = noalloc ? h->na_status : h->d_status;
   P.status = d_status;
-  if (P.ncells > 0) {
-    if (cudaMemsetAsync(d_status, 0, salsa::ST_N * sizeof(unsigned long long), s) != cudaSuccess) return SALSA_E_CUDA;
-    int prec = g.precision, dg = g.diagnostics ? 1 : 0;
-    int bps = prec == 0 ? (dg ? salsa::blocks_per_sm_d1(P) : salsa::blocks_per_sm_d0(P))
-                        : (dg ? salsa::blocks_per_sm_f1(P) : salsa::blocks_per_sm_f0(P));
+  const int prec = g.precision, dg = g.diagnostics ? 1 : 0;
+  auto bind = [&](DevParams &Q, const F &x, double *dp) {
+    if (x.fi >= 0) Q.fin[x.fi] = dp;
+    if (x.fo >= 0) {
+      Q.fout[x.fo] = dp;
+      if (x.fo == salsa::FO_INDEF) Q.fin[salsa::FI_INDEF] = dp;
+      if (x.fo == salsa::FO_CHARGE) Q.fin[salsa::FI_CHARGE] = dp;
+    }
+  };
+  // order pre-pass and step kernel over the cells of Q, on stream s
+  auto launch = [&](DevParams &Q, int *order) -> int {
+    int bps = prec == 0 ? (dg ? salsa::blocks_per_sm_d1(Q) : salsa::blocks_per_sm_d0(Q))
+                        : (dg ? salsa::blocks_per_sm_f1(Q) : salsa::blocks_per_sm_f0(Q));
     if (bps <= 0) return SALSA_E_CUDA;
     long long grid = (long long)bps * h->nsm * 8;
-    if (grid > P.ngroups) grid = P.ngroups;
-    if (noalloc) {
-      P.order = h->na_order;
-    } else if (P.ncells <= 0x7fffffffLL) {
-      if (P.ncells > h->order_cap) {
-        if (h->d_order) cudaFree(h->d_order);
-        h->d_order = nullptr;
-        h->order_cap = 0;
-        if (cudaMalloc(&h->d_order, (size_t)P.ncells * sizeof(int)) != cudaSuccess) return SALSA_E_CUDA;
-        h->order_cap = P.ncells;
-      }
-      P.order = h->d_order;
-    } else {
-      P.order = nullptr;
-    }
-    cudaEventRecord(h->ev0, s);
-    if (P.order) {
-      long long og = (P.ncells + 255) / 256;
+    if (grid > Q.ngroups) grid = Q.ngroups;
+    Q.order = order;
+    if (order) {
+      // the order list's fill counters start at zero for every launch (a call may launch
+      // several, one per slab)
+      if (cudaMemsetAsync(Q.status + salsa::ST_ORDER_CLEAR, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
+        return SALSA_E_CUDA;
+      long long og = (Q.ncells + 255) / 256;
       if (og > (long long)h->nsm * 16) og = (long long)h->nsm * 16;
-      salsa_order_kernel<<<(int)og, 256, 0, s>>>(P, const_cast<int *>(P.order));
+      salsa_order_kernel<<<(int)og, 256, 0, s>>>(Q, order);
       if (cudaGetLastError() != cudaSuccess) return SALSA_E_CUDA;
       launches++;
     }
-    cudaError_t e = prec == 0 ? (dg ? salsa::launch_d1(P, s, (int)grid) : salsa::launch_d0(P, s, (int)grid))
-                              : (dg ? salsa::launch_f1(P, s, (int)grid) : salsa::launch_f0(P, s, (int)grid));
-    cudaEventRecord(h->ev1, s);
+    cudaError_t e = prec == 0 ? (dg ? salsa::launch_d1(Q, s, (int)grid) : salsa::launch_d0(Q, s, (int)grid))
+                              : (dg ? salsa::launch_f1(Q, s, (int)grid) : salsa::launch_f0(Q, s, (int)grid));
     if (e != cudaSuccess) return SALSA_E_CUDA;
     launches++;
-    if (cudaMemcpyAsync(h->h_status, d_status, salsa::ST_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) !=
-        cudaSuccess)
-      return SALSA_E_CUDA;
-  }
-  if (host) {
-    off = 0;
+    return SALSA_OK;
+  };
+  // the cell order list (clear cells first) for up to n cells
+  auto order_for = [&](long long n) -> int * {
+    if (noalloc) return h->na_order;
+    if (n > 0x7fffffffLL) return nullptr;
+    if (n > h->order_cap) {
+      if (h->d_order) cudaFree(h->d_order);
+      h->d_order = nullptr;
+      h->order_cap = 0;
+      if (cudaMalloc(&h->d_order, (size_t)n * sizeof(int)) != cudaSuccess) return nullptr;
+      h->order_cap = n;
+    }
+    return h->d_order;
+  };
+  if (P.ncells > 0 && cudaMemsetAsync(d_status, 0, salsa::ST_N * sizeof(unsigned long long), s) != cudaSuccess)
+    return SALSA_E_CUDA;
+  if (!host) {
     for (auto &x : fl) {
       const double *hp = x.src ? x.src : x.dst;
-      if (!hp) continue;
-      size_t bytes = (size_t)(x.planes * P.plane) * sizeof(double);
-      double *dp = reinterpret_cast<double *>(static_cast<char *>(h->stage) + off);
-      off += bytes;
-      if (x.out && cudaMemcpyAsync(x.dst, dp, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return SALSA_E_CUDA;
+      if (hp) bind(P, x, const_cast<double *>(hp));
     }
+    if (P.ncells > 0) {
+      int *order = order_for(P.ncells);
+      if (!order && P.ncells <= 0x7fffffffLL) return SALSA_E_CUDA;
+      cudaEventRecord(h->ev0, s);
+      int rc = launch(P, order);
+      cudaEventRecord(h->ev1, s);
+      if (rc) return rc;
+    }
+  } else if (P.ncells > 0) {
+    // Host arrays: the interior y rows travel in slabs through a ring of staging slots.
+    // Slab k is copied in on h->s_in, computed on s and copied out on h->s_out, so the
+    // copies of neighbouring slabs overlap the computation; a slot is refilled once the
+    // slab it held has been copied out.  Every array is copied in, outputs included, so
+    // the values outside the interior cells come back unchanged.
+    const int NS = SALSA_PIPE_SLOTS;
+    const long long nyi = nyp - 4, rowd = (long long)nxp * nzp;
+    const long long R = (nyi + SALSA_PIPE_SLABS - 1) / SALSA_PIPE_SLABS;
+    const int nslab = (int)((nyi + R - 1) / R);
+    const long long plane_s = (R + 4) * rowd;
+    size_t per_slot = 0;
+    for (auto &x : fl)
+      if (x.src || x.dst) per_slot += (size_t)(x.planes * plane_s) * sizeof(double);
+    if ((size_t)NS * per_slot > h->stage_bytes) {
+      if (h->stage) cudaFree(h->stage);
+      h->stage = nullptr;
+      h->stage_bytes = 0;
+      if (cudaMalloc(&h->stage, (size_t)NS * per_slot) != cudaSuccess) return SALSA_E_CUDA;
+      h->stage_bytes = (size_t)NS * per_slot;
+    }
+    if (!h->s_in) {
+      if (cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking) != cudaSuccess)
+        return SALSA_E_CUDA;
+      for (int i = 0; i < 3 * NS + 2; i++)
+        if (cudaEventCreateWithFlags(&h->pev[i], cudaEventDisableTiming) != cudaSuccess) return SALSA_E_CUDA;
+    }
+    cudaEvent_t *ev_in = h->pev, *ev_k = h->pev + NS, *ev_out = h->pev + 2 * NS;
+    cudaEvent_t ev_start = h->pev[3 * NS], ev_end = h->pev[3 * NS + 1];
+    int *order = order_for((long long)R * P.nz_int * P.nx_int);
+    if (!order) return SALSA_E_CUDA;
+    if (cudaEventRecord(ev_start, s) != cudaSuccess || cudaStreamWaitEvent(h->s_in, ev_start, 0) != cudaSuccess)
+      return SALSA_E_CUDA;
+    const size_t prow = (size_t)P.plane * sizeof(double), srow = (size_t)plane_s * sizeof(double);
+    for (int k = 0; k < nslab; k++) {
+      const int slot = k % NS;
+      char *base = static_cast<char *>(h->stage) + (size_t)slot * per_slot;
+      const long long j0 = 2 + (long long)k * R, rs = std::min(R, nyi - (long long)k * R);
+      const size_t width = (size_t)(rs * rowd) * sizeof(double);
+      if (k >= NS && cudaStreamWaitEvent(h->s_in, ev_out[slot], 0) != cudaSuccess) return SALSA_E_CUDA;
+      DevParams Q = P;
+      Q.nyp = (int)(rs + 4);
+      Q.plane = plane_s;
+      Q.ncells = (long long)P.nz_int * P.nx_int * rs;
+      Q.ngroups = (Q.ncells + SALSA_CPG - 1) / SALSA_CPG;
+      size_t off = 0;
+      for (auto &x : fl) {
+        const double *hp = x.src ? x.src : x.dst;
+        if (!hp) continue;
+        double *dp = reinterpret_cast<double *>(base + off);
+        off += (size_t)(x.planes * plane_s) * sizeof(double);
+        bind(Q, x, dp);
+        if (cudaMemcpy2DAsync(dp + 2 * rowd, srow, hp + j0 * rowd, prow, width, (size_t)x.planes,
+                              cudaMemcpyHostToDevice, h->s_in) != cudaSuccess)
+          return SALSA_E_CUDA;
+      }
+      if (cudaEventRecord(ev_in[slot], h->s_in) != cudaSuccess || cudaStreamWaitEvent(s, ev_in[slot], 0) != cudaSuccess)
+        return SALSA_E_CUDA;
+      if (k == 0) cudaEventRecord(h->ev0, s);
+      int rc = launch(Q, order);
+      if (rc) return rc;
+      if (k == nslab - 1) cudaEventRecord(h->ev1, s);
+      if (cudaEventRecord(ev_k[slot], s) != cudaSuccess || cudaStreamWaitEvent(h->s_out, ev_k[slot], 0) != cudaSuccess)
+        return SALSA_E_CUDA;
+      off = 0;
+      for (auto &x : fl) {
+        const double *hp = x.src ? x.src : x.dst;
+        if (!hp) continue;
+        double *dp = reinterpret_cast<double *>(base + off);
+        off += (size_t)(x.planes * plane_s) * sizeof(double);
+        if (x.out && cudaMemcpy2DAsync(x.dst + j0 * rowd, prow, dp + 2 * rowd, srow, width, (size_t)x.planes,
+                                       cudaMemcpyDeviceToHost, h->s_out) != cudaSuccess)
+          return SALSA_E_CUDA;
+      }
+      if (cudaEventRecord(ev_out[slot], h->s_out) != cudaSuccess) return SALSA_E_CUDA;
+    }
+    if (cudaEventRecord(ev_end, h->s_out) != cudaSuccess || cudaStreamWaitEvent(s, ev_end, 0) != cudaSuccess)
+      return SALSA_E_CUDA;
   }
+  if (P.ncells > 0 &&
+      cudaMemcpyAsync(h->h_status, d_status, salsa::ST_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess)
+    return SALSA_E_CUDA;
   h->last_launches = launches;
   if (!sync && !host) {
     if (st) memset(st, 0, sizeof *st);

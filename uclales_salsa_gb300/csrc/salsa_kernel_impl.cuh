@@ -48,7 +48,8 @@ enum {
   M_RV = 24,               // water vapour mixing ratio of the cell
   M_PF = 32,               // precipitation-formation accumulators (7 + 9 * nprc, nprc <= 23)
   M_PFSLOT = M_PF + 216,   // 8 partner slots * 10
-  M_END = M_PFSLOT + 80
+  M_GAS = M_PFSLOT + 80,   // the cell's five gases [#/m3] (gas condensation only)
+  M_END = M_GAS + 8
 };
 enum { F_NEG = 0, F_EQUIL, F_DISTR, F_NEGFRAC, F_COND };
 #define SALSA_MISC_DOUBLES 336
@@ -1176,16 +1177,19 @@ __device__ __forceinline__ double acth2o_w(double znw, double zns) { return fmax
 // Gas condensation: mo_salsa_dynamics.f90:348-685 (condgas).  H2SO4 and the non- and
 // semi-volatile organic vapours condense onto every bin in proportion to its
 // Fuchs-Sutugin collision rate; the gas phase takes one implicit step.  zg holds the
-// five gases in #/m3 (SO4, HNO3, NH3, OC non-volatile, OC semi-volatile) on every lane.
+// five gases in #/m3 (SO4, HNO3, NH3, OC non-volatile, OC semi-volatile) in shared memory.
 // The smallest-bin nucleation terms (Jacobson 16.73, 16.75) read condgas's own zj3n3
 // and zxocnv, which it declares locally and zeroes (:433-444): zn_vs_c stays 0, the
 // collision rate of the smallest bin and the sinks gain 0/c.  zxsa, the H2SO4 fraction of
 // the 3 nm clusters from nucleation, only multiplies that zero.  Collision rates go to
 // scratch row 0, the non-volatile organic increments of the aerosol bins to row 1.
 // ----------------------------------------------------------------------------------------
+// Kept out of line: the step's other paths do not carry its registers.
 template <typename KT>
-__device__ void condgas(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres, double dt,
-                        double (&zg)[5], double zxsa, int lane) {
+__device__ __noinline__ void condgas(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
+                                     double dt, double *gas, double zxsa, int lane) {
+  double zg[5];
+  for (int i = 0; i < 5; i++) zg[i] = gas[i];
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   const int ntot = P.ntotal, in1a = P.in1a, in2a = P.in2a, fn2b = P.fn2b;
   const int C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid;
@@ -1278,6 +1282,8 @@ __device__ void condgas(const DevParams &P, const WS<KT> &w, const double *tb, d
       if (b == in1a && zxsa > 0.) w.numc[b] = w.numc[b] + zn_vs_c * inc / K_MVSU / (K_N3 * zxsa);
     }
   }
+  __syncwarp();
+  if (lane < 5) gas[lane] = zg[lane];
   __syncwarp();
 }
 
@@ -1511,9 +1517,10 @@ __device__ __forceinline__ double intgV(double k, double c, double lo, double hi
 // activated-droplet outputs (raw rows, per kg of air).  One lane per aerosol bin, then
 // one lane per cloud bin; sums run in bin order on every lane.
 // ----------------------------------------------------------------------------------------
+// Kept out of line: the step's other paths do not carry its registers.
 template <typename KT>
-__device__ void act_cloudbase(const DevParams &P, const WS<KT> &w, const double *tb, double pres, double T,
-                              double wvel, double dn, double *raw, int lane) {
+__device__ __noinline__ void act_cloudbase(const DevParams &P, const WS<KT> &w, const double *tb, double pres,
+                                           double T, double wvel, double dn, double *raw, int lane) {
   const int in1a = P.in1a, fn2a = P.fn2a, in2b = P.in2b, fn2b = P.fn2b, ndry = P.ndry, nwet = P.nwet;
   const int iwa = P.iwa, ncld = P.ncld;
   const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad, *vhi = tb + TAB_VHI * P.nb_pad;
@@ -2588,9 +2595,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   __syncwarp();
   if (P.initialize) equilibration<KT>(P, w, tb, 0.3, T, true, lane);
   // gases in #/m3 (mo_salsa_driver.f90:285-290)
-  double zg[5] = {0., 0., 0., 0., 0.};
-  if (P.raw_gas >= 0)
-    for (int i = 0; i < 5; i++) zg[i] = raw[P.raw_gas + i] * dn;
+  if (P.raw_gas >= 0 && lane < 5) w.misc[M_GAS + lane] = raw[P.raw_gas + lane] * dn;
   STAGE_MARK(0);
 
   // ---- salsa() ----
@@ -2601,7 +2606,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
     // formation rates, which condgas does not read, and the H2SO4 fraction of the
     // clusters: 1 for nsnucl = 1-3; for the mixed schemes it only multiplies condgas's
     // vanishing nucleation term, and 1 stands in
-    if (P.lscndgas) condgas<KT>(P, w, tb, T, pres, dt, zg, P.nsnucl > 0 ? 1. : 0., lane);
+    if (P.lscndgas) condgas<KT>(P, w, tb, T, pres, dt, w.misc + M_GAS, P.nsnucl > 0 ? 1. : 0., lane);
     if (P.lscndh2ocl || P.lscndh2oae || P.lscndh2oic) gpparth2o<KT>(P, w, tb, T, pres, rs, rsi, rv, dt, kappa, DIAG, lane);
   }
   STAGE_MARK(2);
@@ -2644,8 +2649,8 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   if (!(P.st_activ && P.activ_mode == 2))
     for (int i = lane; i < P.ncld * (1 + nwet); i += 32) raw[P.raw_nact + i] = 0.;
   if (lane == 0) raw[RW_RV] = (rv - rv_old) / dt;
-  if (P.raw_gas >= 0 && lane == 0)   // :369-384
-    for (int i = 0; i < 5; i++) raw[P.raw_gas + i] = ((zg[i] / dn) - raw[P.raw_gas + i]) / dt;
+  if (P.raw_gas >= 0 && lane < 5)   // :369-384
+    raw[P.raw_gas + lane] = ((w.misc[M_GAS + lane] / dn) - raw[P.raw_gas + lane]) / dt;
   if (DIAG && P.raw_diag >= 0 && lane == 0) {
     const double *d = w.misc + M_DIAG;
     double *o = raw + P.raw_diag;
