@@ -149,6 +149,8 @@ def run_gb300(args):
         if sampler:
             sampler.__exit__()
             results["clocks"] = sampler.summary()
+        if form == 0 and not args.no_post and not args.in_place:   # the post step changes the fields
+            results["post"] = post_bench(step, inp, fields, outs, stream, peak_gbs())
         ms = e0.elapsed_time(e1)
         t = torch.tensor([ms], device=dev)
         if world > 1:
@@ -200,12 +202,7 @@ def run_gb300(args):
     mixed = world * ncell * args.steps / (results[1]["ms_total"] / 1e3)
     e2e = world * ncell * args.steps / e2e_s if e2e_s else None
     bytes_cell = 8 * ALG_DOUBLES[level]
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
-    except Exception:
-        peak, peak_src = 6800.0, "fallback"
+    peak, peak_src = peak_gbs()
     achieved = bytes_cell * ncell / (r0["kernel_ms"] / 1e3) / 1e9
     # DRAM bytes per cell from one ncu capture of the same kernel on a 131072-cell block of
     # this workload (dram__bytes_read.sum + dram__bytes_write.sum / cells), scaled to the
@@ -238,6 +235,8 @@ def run_gb300(args):
         "gpu_launches": r0["launches"],
         "clocks": results.get("clocks"),
     }
+    if "post" in results:
+        line["post_step"] = results["post"]
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = chain_bench(dev)
     if rank == 0 and not args.no_cpu_baseline:
@@ -246,6 +245,31 @@ def run_gb300(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         tdist.destroy_process_group()
+
+
+def peak_gbs():
+    """HBM copy bandwidth: the measured peak, else the fallback figure."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def post_bench(step, inp, fields, outs, stream, peak, reps=3):
+    """tend_constrain2 + SALSA_diagnostics over the whole grid after the timed steps
+    (fields and tendencies resident): device time per call and HBM roofline fraction of
+    the bytes each call must read or write."""
+    from uclales_salsa_gb300.post_case import post_arrays, post_bytes, time_post
+    a = post_arrays(inp, fields, outs)
+    tc_ms, dg_ms = time_post(step, inp, a, stream, reps)
+    tcb, dgb = post_bytes(a, inp.level)
+    del a
+    return {"what": "tend_constrain2 + SALSA_diagnostics (constrain_SALSA.f90) over the grid, fields in HBM",
+            "tend_constrain_ms": tc_ms, "diagnostics_ms": dg_ms,
+            "tend_constrain": {"bytes": tcb, "achieved_gbs": tcb / tc_ms / 1e6,
+                               "frac": tcb / tc_ms / 1e6 / peak[0]},
+            "diagnostics": {"bytes": dgb, "achieved_gbs": dgb / dg_ms / 1e6, "frac": dgb / dg_ms / 1e6 / peak[0]},
+            "peak_gbs": peak[0], "peak_source": peak[1]}
 
 
 def chain_bench(dev, nsub=60):
@@ -348,6 +372,7 @@ def main():
     ap.add_argument("--cpu-sample-cells", type=int, default=3145728)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-post", action="store_true", help="skip the tend_constrain2 / SALSA_diagnostics timing")
     ap.add_argument("--in-place", action="store_true", help="steps read the workload's fields, not a copy")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg through host buffers")
     args = ap.parse_args()

@@ -215,6 +215,46 @@ void salsa_gb300_finalize(salsa_handle_t *h);
 
 const char *salsa_gb300_version(void);
 
+/* ---- LES-side constraints after the step (src/src_LES/constrain_SALSA.f90) ----
+ * t_step (step.f90:330-334) follows run_SALSA with tend_constrain2, the scalar
+ * update, tend0 and SALSA_diagnostics; the two SALSA routines are here, on the same
+ * arrays as run_SALSA.  Value arrays (time level 1) and tendencies (level 2) of the
+ * SALSA_4d tracers (mo_progn_state.f90:165-333: naero, maero, ncloud, mcloud, nprecp,
+ * mprecp, gaero, nice, mice), the IN deficit and the charge time are in/out; rh and
+ * rhi (relative humidities over water and ice), temp and rp are the thermodynamic
+ * diagnostics SALSA_diagnostics reads, and rc, srp, snrp, rtot, ri, riri the
+ * diagnostic mixing ratios it writes (mo_diag_state.f90).  Arrays the level or
+ * configuration does not use may be NULL.  Device pointers only: these routines serve
+ * an LES whose fields live on the GPU.  Calls are asynchronous on `stream` (the
+ * library stream when NULL). */
+typedef struct {
+  double *naero, *ncloud, *nprecp, *nice;           /* (nzp,nxp,nyp,nb) #/kg */
+  double *maero, *mcloud, *mprecp, *mice;           /* (...,nspec*nb) kg/kg */
+  double *gaero;                                    /* (...,5) #/kg */
+  double *indef;                                    /* (...,nliquid) */
+  double *chargeTime;                               /* (...,nliquid) */
+  double *naerot, *ncloudt, *nprecpt, *nicet;       /* tendencies of the above */
+  double *maerot, *mcloudt, *mprecpt, *micet, *gaerot;
+  const double *rh, *rhi, *temp, *rp;               /* (nzp,nxp,nyp) */
+  double *rc, *srp, *snrp, *rtot, *ri, *riri;       /* (nzp,nxp,nyp) */
+} salsa_post_fields_t;
+
+/* tend_constrain2 (constrain_SALSA.f90:18-35): every tendency element of the SALSA_4d
+ * tracers becomes at least (-1 + 1e-8) * value / dtlt, so that one step of length dtlt
+ * leaves a value above zero; with ice_theta_dist at level 5 the IN deficit is
+ * clipped to [0, 1]. */
+int salsa_gb300_tend_constrain(salsa_handle_t *h, int nzp, int nxp, int nyp, double dtlt,
+                               const salsa_post_fields_t *f, void *stream);
+
+/* SALSA_diagnostics (constrain_SALSA.f90:52-370, findDry4Wet :376-463): negative
+ * values to zero; unless only_diag, particles with number but no mass are removed,
+ * evaporating cloud droplets, drops and ice return their number and mass to the
+ * aerosol bins, and aerosol bins below 0.1 nm dry diameter are emptied (their
+ * volatile species to the gases when gas condensation is on); then the water
+ * diagnostics rc, srp, snrp, rtot (and ri, riri at level 5) are recomputed. */
+int salsa_gb300_diagnostics(salsa_handle_t *h, int nzp, int nxp, int nyp, int only_diag, int lcharge,
+                            const salsa_post_fields_t *f, void *stream);
+
 /* ---- Gradient harness (no counterpart in the reference, which has no adjoint) ----
  * A chain advances ncell independent warm cells (a level-4 handle) through nsub
  * steps of length dt.  Each step is the coagulation (mo_salsa_dynamics.f90:92-202)

@@ -2869,3 +2869,274 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
   if (st) *st = loc;
   return loc.code;
 }
+
+/* ======================================================================
+ * LES-side constraints after the step: src/src_LES/constrain_SALSA.f90
+ * ====================================================================== */
+
+/* tend_constrain2 (:18-35) over every element of the SALSA_4d tracers (halos included) */
+int salsa_ref_tend_constrain(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, double dtlt,
+                             const salsa_post_fields_t *f) {
+  if (!c || !f || nzp < 3 || nxp < 5 || nyp < 5 || !(dtlt > 0.)) return SALSA_E_ARG;
+  const salsa_config_t *g = &c->cfg;
+  const long long plane = (long long)nzp * nxp * nyp;
+  const int nw = c->nwet, lvl5 = g->level == 5;
+  double *vp[9] = {f->naero, f->maero, f->ncloud, f->mcloud, f->nprecp, f->mprecp, f->gaero,
+                   lvl5 ? f->nice : NULL, lvl5 ? f->mice : NULL};
+  double *vt[9] = {f->naerot, f->maerot, f->ncloudt, f->mcloudt, f->nprecpt, f->mprecpt, f->gaerot,
+                   lvl5 ? f->nicet : NULL, lvl5 ? f->micet : NULL};
+  const long long np[9] = {c->nbins, (long long)nw * c->nbins, c->ncld, (long long)nw * c->ncld, c->nprc,
+                           (long long)nw * c->nprc, 5, c->nice, (long long)(nw + 1) * c->nice};
+  for (int a = 0; a < 9; a++) {
+    if (!vp[a] || !vt[a]) continue;
+    const long long n = np[a] * plane;
+    for (long long e = 0; e < n; e++) vt[a][e] = fmaxd((-1. + 1.e-8) * vp[a][e] / dtlt, vt[a][e]);
+  }
+  if (g->ice_theta_dist && g->level > 4 && f->indef) {
+    const long long n = (long long)c->nliquid * plane;
+    for (long long e = 0; e < n; e++) f->indef[e] = fmind(fmaxd(f->indef[e], 0.), 1.);
+  }
+  return SALSA_OK;
+}
+
+/* util.f90:1005-1024 calc_correlation, as written: sxy keeps only the last product */
+static double calc_correlation(const double *x, const double *y, int n) {
+  const double eps = EPSR;
+  double sx = 0., sy = 0., sx2 = 0., sy2 = 0., sxy = 0.;
+  for (int i = 0; i < n; i++) {
+    sx = sx + x[i];
+    sy = sy + y[i];
+    sx2 = sx2 + sq(x[i]);
+    sy2 = sy2 + sq(y[i]);
+    sxy = x[i] * y[i];
+  }
+  if (sx2 * n - sq(sx) < eps || sy2 * n - sq(sy) < eps) return 0.;
+  return (sxy * n - sx * sy) / (sqrt(sx2 * n - sq(sx)) * sqrt(sy2 * n - sq(sy)));
+}
+
+/* :376-463 findDry4Wet: the aerosol bin for evaporating drops or ice of bin ib at point p
+   (mevap species-major with nb bins).  The b bin is taken as fn2a + (ba - in2a), as the
+   reference writes it. */
+static int findDry4Wet(const salsa_ref_ctx_t *c, const double *aetot, const double *nevap, const double *mevap,
+                       int nb, int ib, long long p, long long plane, const double *naero, const double *maero) {
+  const int ndry = c->ndry, nbins = c->nbins, in2a = c->in2a, fn2a = c->fn2a;
+  double cd = 0.;
+  for (int s = 0; s < ndry; s++) cd += mevap[p + plane * ((long long)s * nb + ib)] / c->rholiq[s];
+  cd = cd / nevap[p + plane * ib];
+  cd = pow(cd / PI6, 1. / 3.);
+  int cnt = 0;
+  for (int b = in2a; b <= fn2a; b++) cnt += cd > aetot[b];
+  int ba = in2a + cnt - 1;
+  if (ba < in2a) ba = in2a;
+  if (ba > fn2a) ba = fn2a;
+  const int bb = fn2a + (ba - in2a);
+  if (naero[p + plane * bb] <= NLIM) return ba;
+  if (naero[p + plane * ba] <= NLIM) return bb;
+  double xa[NSP], xb[NSP], y[NSP];
+  for (int s = 0; s < ndry; s++) {
+    xa[s] = maero[p + plane * ((long long)s * nbins + ba)];
+    xb[s] = maero[p + plane * ((long long)s * nbins + bb)];
+    y[s] = mevap[p + plane * ((long long)s * nb + ib)];
+  }
+  const double ra = calc_correlation(xa, y, ndry), rb = calc_correlation(xb, y, ndry);
+  return ra < rb ? bb : ba;
+}
+
+/* :52-370 SALSA_diagnostics */
+int salsa_ref_diagnostics(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int only_diag, int lcharge,
+                          const salsa_post_fields_t *f) {
+  if (!c || !f || nzp < 3 || nxp < 5 || nyp < 5) return SALSA_E_ARG;
+  const salsa_config_t *g = &c->cfg;
+  const int lvl5 = g->level == 5;
+  if (!f->naero || !f->ncloud || !f->nprecp || !f->maero || !f->mcloud || !f->mprecp || !f->rp || !f->rc ||
+      !f->srp || !f->snrp || !f->rtot)
+    return SALSA_E_ARG;
+  if (lvl5 && (!f->nice || !f->mice || !f->ri || !f->riri)) return SALSA_E_ARG;
+  if (!only_diag && (!f->rh || !f->temp || (lvl5 && !f->rhi) || (lcharge && !f->chargeTime) ||
+                     (g->lscndgas && !f->gaero)))
+    return SALSA_E_ARG;
+  const long long plane = (long long)nzp * nxp * nyp;
+  const int nbins = c->nbins, ncld = c->ncld, nprc = c->nprc, nice = c->nice, nspec = c->nwet, ndry = c->ndry;
+  const int iwa = c->iwa, irim = c->irim;
+  const double massTH = 1.e-25;
+  double aetot[MAXB];
+  for (int b = 0; b < nbins; b++) aetot[b] = pow(c->tmpl[b].vlolim / PI6, 1. / 3.);   /* aerobins */
+  double *na = f->naero, *nc = f->ncloud, *np = f->nprecp, *ni = f->nice;
+  double *ma = f->maero, *mc = f->mcloud, *mp = f->mprecp, *mi = f->mice;
+#define AT(arr, nb, s, b) (arr)[p + plane * ((long long)(s) * (nb) + (b))]
+  /* remove negative values */
+  {
+    double *arr[8] = {na, nc, np, ma, mc, mp, lvl5 ? ni : NULL, lvl5 ? mi : NULL};
+    const long long n[8] = {nbins, ncld, nprc, (long long)nspec * nbins, (long long)nspec * ncld,
+                            (long long)nspec * nprc, nice, (long long)(nspec + 1) * nice};
+    for (int a = 0; a < 8; a++)
+      if (arr[a])
+        for (long long e = 0; e < n[a] * plane; e++) arr[a][e] = fmaxd(0., arr[a][e]);
+  }
+  if (!only_diag) {
+    for (int j = 2; j <= nyp - 3; j++)
+      for (int i = 2; i <= nxp - 3; i++)
+        for (int k = 0; k < nzp; k++) {
+          const long long p = k + (long long)nzp * (i + (long long)nxp * j);
+          /* particles with number but no mass */
+          for (int bc = 0; bc < nbins; bc++) {
+            double sm = 0.;
+            for (int s = 0; s < nspec; s++) sm += AT(ma, nbins, s, bc);
+            if (na[p + plane * bc] > 0. && sm <= 0.) {
+              na[p + plane * bc] = 0.;
+              for (int s = 0; s < nspec; s++) AT(ma, nbins, s, bc) = 0.;
+              if (lcharge) f->chargeTime[p + plane * bc] = 0.;
+            }
+          }
+          for (int bc = 0; bc < ncld; bc++) {
+            double sm = 0.;
+            for (int s = 0; s < nspec; s++) sm += AT(mc, ncld, s, bc);
+            if (nc[p + plane * bc] > 0. && sm <= 0.) {
+              nc[p + plane * bc] = 0.;
+              for (int s = 0; s < nspec; s++) AT(mc, ncld, s, bc) = 0.;
+              if (lcharge) f->chargeTime[p + plane * (nbins + bc)] = 0.;
+            }
+          }
+          for (int bc = 0; bc < nprc; bc++) {
+            if (np[p + plane * bc] > 0. && AT(mp, nprc, iwa, bc) <= 0.) {
+              np[p + plane * bc] = 0.;
+              for (int s = 0; s < nspec; s++) AT(mp, nprc, s, bc) = 0.;
+              if (lcharge) f->chargeTime[p + plane * (nbins + ncld + bc)] = 0.;
+            }
+          }
+          if (lvl5)
+            for (int bc = 0; bc < nice; bc++) {
+              const double mt = AT(mi, nice, iwa, bc) + AT(mi, nice, irim, bc);
+              if (ni[p + plane * bc] > 0. && mt < massTH) {
+                ni[p + plane * bc] = 0.;
+                for (int s = 0; s < nspec + 1; s++) AT(mi, nice, s, bc) = 0.;
+              }
+            }
+          const double T = f->temp[p], rh = f->rh[p];
+          /* evaporating cloud droplets */
+          for (int bc = c->ica_cur; bc <= c->fcb_cur; bc++) {
+            const double n_ = nc[p + plane * bc];
+            if (n_ > NLIM && rh < 0.999 && AT(mc, ncld, iwa, bc) < 1.e-5) {
+              double ns = 0.;
+              for (int s = 0; s < nspec - 1; s++) ns += c->diss[s] * AT(mc, ncld, s, bc) / c->MM[s];
+              ns = ns / n_;
+              const double zbb = 6. * c->mwa * ns / (PI * c->rhowa);
+              const double zaa = 4. * c->mwa * SURFW0 / (RG * c->rhowa * T);
+              const double cdcld = sqrt(3. * zbb / zaa);
+              double zvol = 0.;
+              for (int s = 0; s < nspec; s++) zvol += AT(mc, ncld, s, bc) / c->rholiq[s];
+              zvol = zvol / n_;
+              const double zdh2o = pow(zvol / PI6, 1. / 3.);
+              if (zdh2o < fmind(0.7 * cdcld, 1.3e-5) || AT(mc, ncld, iwa, bc) < massTH * n_) {
+                const int ba = bc <= c->fca_cur ? c->ica_par + (bc - c->ica_cur) : c->icb_par + (bc - c->icb_cur);
+                na[p + plane * ba] = na[p + plane * ba] + n_;
+                nc[p + plane * bc] = 0.;
+                for (int s = 0; s < nspec; s++) {
+                  AT(ma, nbins, s, ba) = AT(ma, nbins, s, ba) + AT(mc, ncld, s, bc);
+                  AT(mc, ncld, s, bc) = 0.;
+                }
+                if (lcharge) f->chargeTime[p + plane * (nbins + bc)] = 0.;
+              }
+            }
+          }
+          /* evaporating drops */
+          for (int bc = 0; bc < nprc; bc++) {
+            const double n_ = np[p + plane * bc];
+            if (n_ > PRLIM && rh < 0.999 && AT(mp, nprc, iwa, bc) < 1.e-6) {
+              double ns = 0.;
+              for (int s = 0; s < nspec - 1; s++) ns += c->diss[s] * AT(mp, nprc, s, bc) / c->MM[s];
+              ns = ns / n_;
+              const double zbb = 6. * c->mwa * ns / (PI * c->rhowa);
+              const double zaa = 4. * c->mwa * SURFW0 / (RG * c->rhowa * T);
+              const double cdprc = sqrt(3. * zbb / zaa);
+              double zvol = 0.;
+              for (int s = 0; s < nspec; s++) zvol += AT(mp, nprc, s, bc) / c->rholiq[s];
+              zvol = zvol / n_;
+              const double zdh2o = pow(zvol / PI6, 1. / 3.);
+              if (zdh2o < fmind(0.2 * cdprc, 10.e-6) || AT(mp, nprc, iwa, bc) < massTH * n_) {
+                const int ba = findDry4Wet(c, aetot, np, mp, nprc, bc, p, plane, na, ma);
+                na[p + plane * ba] = na[p + plane * ba] + n_;
+                np[p + plane * bc] = 0.;
+                for (int s = 0; s < nspec; s++) {
+                  AT(ma, nbins, s, ba) = AT(ma, nbins, s, ba) + AT(mp, nprc, s, bc);
+                  AT(mp, nprc, s, bc) = 0.;
+                }
+                if (lcharge) f->chargeTime[p + plane * (nbins + ncld + bc)] = 0.;
+              }
+            }
+          }
+          /* evaporating ice */
+          if (lvl5)
+            for (int bc = 0; bc < nice; bc++) {
+              const double mt = AT(mi, nice, iwa, bc) + AT(mi, nice, irim, bc);
+              double vt = 0.;
+              for (int s = 0; s < nspec + 1; s++) vt += AT(mi, nice, s, bc) / c->rhoice[s];
+              const double n_ = ni[p + plane * bc];
+              if (n_ > PRLIM && f->rhi[p] < 0.999 && mt < 1.e-15) {
+                double cdice = vt / n_;
+                cdice = pow(cdice / PI6, 1. / 3.);
+                double zdrms = 0., zwams = 0.;
+                for (int s = 0; s < ndry; s++) zdrms += AT(mi, nice, s, bc);
+                for (int s = 0; s < nspec + 1; s++) zwams += AT(mi, nice, s, bc);
+                const double zvol = zdrms / zwams;
+                if (zvol > 0.5 || cdice < 2.e-6) {
+                  const int ba = findDry4Wet(c, aetot, ni, mi, nice, bc, p, plane, na, ma);
+                  na[p + plane * ba] = na[p + plane * ba] + n_;
+                  ni[p + plane * bc] = 0.;
+                  for (int s = 0; s < nspec; s++) {
+                    AT(ma, nbins, s, ba) = AT(ma, nbins, s, ba) + AT(mi, nice, s, bc);
+                    AT(mi, nice, s, bc) = 0.;
+                  }
+                  AT(ma, nbins, iwa, ba) = AT(ma, nbins, iwa, ba) + AT(mi, nice, irim, bc);
+                  AT(mi, nice, irim, bc) = 0.;
+                }
+              }
+            }
+          /* aerosol bins below 0.1 nm dry diameter */
+          for (int ba = 0; ba < nbins; ba++) {
+            const double n_ = na[p + plane * ba];
+            if (n_ > NLIM) {
+              double zvol = 0.;
+              for (int s = 0; s < nspec - 1; s++) zvol += AT(ma, nbins, s, ba) / c->rholiq[s];
+              zvol = zvol / n_;
+              if (zvol < PI6 * cube(1.e-10)) {
+                if (g->lscndgas) {
+                  const int ix[4] = {c->idx_name[0], c->idx_name[1], c->idx_name[5], c->idx_name[6]};
+                  const int gi[4] = {0, 4, 1, 2};   /* SO4 -> 1, OC -> 5, NO -> 2, NH -> 3 */
+                  for (int q = 0; q < 4; q++)
+                    if (ix[q] >= 0)
+                      f->gaero[p + plane * gi[q]] = f->gaero[p + plane * gi[q]] + AT(ma, nbins, ix[q], ba) / c->MM[ix[q]] * AVOG;
+                }
+                for (int s = 0; s < nspec; s++) AT(ma, nbins, s, ba) = 0.;
+                na[p + plane * ba] = 0.;
+              }
+            }
+          }
+        }
+  }
+  /* water diagnostics, every point */
+  for (long long p = 0; p < plane; p++) {
+    double rc = 0., srp = 0., snrp = 0.;
+    for (int b = c->in1a; b <= c->fn2b; b++) rc += AT(ma, nbins, iwa, b);
+    double rcc = 0.;
+    for (int b = c->ica_cur; b <= c->fcb_cur; b++) rcc += AT(mc, ncld, iwa, b);
+    rc = rc + rcc;
+    for (int b = 0; b < nprc; b++) srp += AT(mp, nprc, iwa, b);
+    for (int b = 0; b < nprc; b++) snrp += np[p + plane * b];
+    f->rc[p] = rc;
+    f->srp[p] = srp;
+    f->snrp[p] = snrp;
+    double rt = rc + srp + f->rp[p];
+    if (lvl5) {
+      double ri = 0., riri = 0.;
+      for (int b = 0; b < nice; b++) ri += AT(mi, nice, iwa, b);
+      for (int b = 0; b < nice; b++) riri += AT(mi, nice, irim, b);
+      f->ri[p] = ri;
+      f->riri[p] = riri;
+      rt = rt + ri + riri;
+    }
+    f->rtot[p] = rt;
+  }
+#undef AT
+  return SALSA_OK;
+}

@@ -35,6 +35,13 @@ void salsa_ref_destroy(salsa_ref_ctx_t *ctx);
  * reference's serial module-state carry-over between cells (allSALSA keeps the
  * previous cell's derived diameters); 0 resets them per cell (the GPU
  * semantics, every cell sees the post-initialisation module state). */
+/* tend_constrain2 and SALSA_diagnostics (src/src_LES/constrain_SALSA.f90), same
+ * arguments as salsa_gb300_tend_constrain / salsa_gb300_diagnostics; host pointers. */
+int salsa_ref_tend_constrain(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, double dtlt,
+                             const salsa_post_fields_t *f);
+int salsa_ref_diagnostics(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, int only_diag, int lcharge,
+                          const salsa_post_fields_t *f);
+
 int salsa_ref_run(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, int ns,
                   double tstep, double time, int istp, int level, int lcharge,
                   int initialize, const salsa_fields_t *f, salsa_status_t *st,

@@ -7,7 +7,7 @@ import ctypes as C
 import os
 import subprocess
 
-from uclales_salsa_gb300.capi import Config, Fields, Status, make_fields
+from uclales_salsa_gb300.capi import Config, Fields, PostFields, Status, make_fields, make_post_fields
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB = os.path.join(ROOT, "oracle", "_build", "libsalsa_ref.so")
@@ -37,6 +37,12 @@ def lib():
         L.salsa_ref_terminal_vel.restype = C.c_double
         L.salsa_ref_coagc_pair.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 6
         L.salsa_ref_coagc_pair.restype = C.c_double
+        L.salsa_ref_tend_constrain.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                               C.POINTER(PostFields)]
+        L.salsa_ref_tend_constrain.restype = C.c_int
+        L.salsa_ref_diagnostics.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            C.POINTER(PostFields)]
+        L.salsa_ref_diagnostics.restype = C.c_int
         _lib = L
     return _lib
 
@@ -55,6 +61,14 @@ class Oracle:
         rc = lib().salsa_ref_run(self.h, inp.nzp, inp.nxp, inp.nyp, inp.ns, inp.dt, time, istp, inp.level,
                                  lcharge, initialize, C.byref(f), C.byref(st), nthreads, carry_over)
         return rc, st
+
+    def tend_constrain(self, nzp, nxp, nyp, dtlt, arrays):
+        f = make_post_fields(arrays)
+        return lib().salsa_ref_tend_constrain(self.h, nzp, nxp, nyp, dtlt, C.byref(f))
+
+    def diagnostics(self, nzp, nxp, nyp, arrays, only_diag=0, lcharge=0):
+        f = make_post_fields(arrays)
+        return lib().salsa_ref_diagnostics(self.h, nzp, nxp, nyp, only_diag, lcharge, C.byref(f))
 
     def layout(self):
         v = [C.c_int() for _ in range(5)]

@@ -10,7 +10,7 @@ layout.  The CUDA library is required: there is no CPU path.
 import ctypes as C
 import os
 
-from .capi import Config, Fields, Status, make_fields, ERROR_NAMES
+from .capi import Config, Fields, PostFields, Status, make_fields, make_post_fields, ERROR_NAMES
 
 _lib = None
 
@@ -46,6 +46,12 @@ def library():
     L.salsa_gb300_last_launches.restype = C.c_int
     L.salsa_gb300_last_kernel_ms.argtypes = [C.c_void_p]
     L.salsa_gb300_last_kernel_ms.restype = C.c_double
+    L.salsa_gb300_tend_constrain.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                             C.POINTER(PostFields), C.c_void_p]
+    L.salsa_gb300_tend_constrain.restype = C.c_int
+    L.salsa_gb300_diagnostics.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(PostFields), C.c_void_p]
+    L.salsa_gb300_diagnostics.restype = C.c_int
     L.salsa_gb300_finalize.argtypes = [C.c_void_p]
     L.salsa_gb300_version.restype = C.c_char_p
     _lib = L
@@ -55,7 +61,8 @@ def library():
 EXPORTED = ["salsa_gb300_default_config", "salsa_gb300_init", "salsa_gb300_run", "salsa_gb300_run_async",
             "salsa_gb300_layout", "salsa_gb300_last_launches", "salsa_gb300_last_kernel_ms",
             "salsa_gb300_finalize", "salsa_gb300_version", "salsa_gb300_run_noalloc", "salsa_gb300_chain_state_size",
-            "salsa_gb300_chain_forward", "salsa_gb300_chain_tlm", "salsa_gb300_chain_adjoint"]
+            "salsa_gb300_chain_forward", "salsa_gb300_chain_tlm", "salsa_gb300_chain_adjoint",
+            "salsa_gb300_tend_constrain", "salsa_gb300_diagnostics"]
 
 
 class SalsaStep:
@@ -90,6 +97,23 @@ class SalsaStep:
         arr = (C.c_double * 96)()
         library().salsa_gb300_layout(self.h, *[C.byref(x) for x in v], arr)
         return [x.value for x in v], list(arr)
+
+    def tend_constrain(self, nzp, nxp, nyp, dtlt, arrays, stream=None):
+        """tend_constrain2 (src/src_LES/constrain_SALSA.f90:18-35) on CUDA tensors:
+        `arrays` maps PostFields names (values and tendencies) to tensors."""
+        f = make_post_fields(arrays)
+        rc = library().salsa_gb300_tend_constrain(self.h, nzp, nxp, nyp, dtlt, C.byref(f),
+                                                  C.c_void_p(stream.cuda_stream if stream else 0))
+        if rc != 0:
+            raise SalsaError(rc, "salsa_gb300_tend_constrain")
+
+    def diagnostics(self, nzp, nxp, nyp, arrays, only_diag=0, lcharge=0, stream=None):
+        """SALSA_diagnostics (src/src_LES/constrain_SALSA.f90:52-370) on CUDA tensors."""
+        f = make_post_fields(arrays)
+        rc = library().salsa_gb300_diagnostics(self.h, nzp, nxp, nyp, only_diag, lcharge, C.byref(f),
+                                               C.c_void_p(stream.cuda_stream if stream else 0))
+        if rc != 0:
+            raise SalsaError(rc, "salsa_gb300_diagnostics")
 
     def last_launches(self):
         return library().salsa_gb300_last_launches(self.h)

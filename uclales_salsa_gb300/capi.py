@@ -98,6 +98,27 @@ class Fields(C.Structure):
     ]
 
 
+class PostFields(C.Structure):
+    """salsa_post_fields_t: the arrays of tend_constrain2 and SALSA_diagnostics."""
+    _fields_ = [(n, _PD) for n in (
+        "naero", "ncloud", "nprecp", "nice", "maero", "mcloud", "mprecp", "mice", "gaero", "indef", "chargeTime",
+        "naerot", "ncloudt", "nprecpt", "nicet", "maerot", "mcloudt", "mprecpt", "micet", "gaerot",
+        "rh", "rhi", "temp", "rp", "rc", "srp", "snrp", "rtot", "ri", "riri")]
+
+
+def make_post_fields(arrays):
+    """PostFields with the data pointers of the tensors in `arrays` (name -> tensor)."""
+    f = PostFields()
+    names = {n for n, _ in PostFields._fields_}
+    for name, t in arrays.items():
+        if name not in names or t is None:
+            continue
+        if not t.is_contiguous() or t.dtype.itemsize != 8:
+            raise ValueError(f"field {name} must be a contiguous float64 tensor")
+        setattr(f, name, ptr_of(t.data_ptr()))
+    return f
+
+
 class Status(C.Structure):
     _fields_ = [
         ("code", C.c_int),
