@@ -108,6 +108,10 @@ struct salsa_ref_ctx {
   long long counters[5];
   Section carry[MAXB];
   int carry_valid;
+  /* kernel storage of lscoag%mode = 2 (mo_salsa_driver.f90:52-55, 601-697): per interior
+     cell the ten kernel arrays, zero until first stored */
+  double *kcache;
+  long long kcache_cells;
 };
 
 /* Per-cell working state: the module arrays allSALSA, zcc**, rateDiag. */
@@ -126,6 +130,7 @@ typedef struct {
   long long cnt[5];
   const double *kappa;   /* NULL or per-cell kappa override */
   double kappa_cell;
+  long long cell;        /* interior cell index (kernel storage) */
 } Cell;
 
 static void rate_acc_n(Rate *r, double n) { r->numc += n; }
@@ -1009,12 +1014,33 @@ static void coag_ice(Cell *w, int nspec, double dt) {
   }
 }
 
+/* the ten kernel arrays of a cell in the storage of lscoag%mode = 2, in the order aa cc pp
+   ii ca pa ia pc ic ip (store_coag / fetch_coag, mo_salsa_driver.f90:655-697) */
+static long long kc_cell_doubles(const salsa_ref_ctx_t *c) {
+  const long long a = c->nbins, k = c->ncld, p = c->nprc, i = c->nice;
+  return a * a + k * k + p * p + i * i + a * k + a * p + a * i + k * p + k * i + p * i;
+}
+static void kc_copy(Cell *w, int store) {
+  const salsa_ref_ctx_t *c = w->c;
+  const int a = c->nbins, k = c->ncld, p = c->nprc, i = c->nice;
+  double *arr[10] = {w->zccaa, w->zcccc, w->zccpp, w->zccii, w->zccca, w->zccpa, w->zccia, w->zccpc, w->zccic,
+                     w->zccip};
+  const int n[10] = {a * a, k * k, p * p, i * i, a * k, a * p, a * i, k * p, k * i, p * i};
+  double *sto = c->kcache + w->cell * kc_cell_doubles(c);
+  for (int q = 0; q < 10; q++) {
+    if (store) memcpy(sto, arr[q], sizeof(double) * n[q]);
+    else memcpy(arr[q], sto, sizeof(double) * n[q]);
+    sto += n[q];
+  }
+}
+
 /* mo_salsa_dynamics.f90:92-202 coagulation */
 static void coagulation(Cell *w, double dt, double T, double P) {
   const salsa_ref_ctx_t *c = w->c;
   const salsa_config_t *g = &c->cfg;
   for (int bb = 0; bb < c->ntotal; bb++) updateDiameter(c, &w->all[bb], 1, T_ALL);
   if (g->lscoag.mode == 1 || c->lcgupdt) update_coagulation_kernels(w, P, T);
+  else if (g->lscoag.mode == 2) kc_copy(w, 0);   /* fetch_coag (mo_salsa_driver.f90:297-298) */
   int any_aero = g->lscgaa || g->lscgca || g->lscgpa || g->lscgia;
   int any_cloud = g->lscgcc || g->lscgca || g->lscgpc || g->lscgic;
   int any_precp = g->lscgpp || g->lscgpa || g->lscgpc || g->lscgip;
@@ -2523,7 +2549,7 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (!cfg || !out) return SALSA_E_ARG;
   if (cfg->nbin[0] < 1 || cfg->nbin[1] < 4 || cfg->prc_nbins < 1 || cfg->ice_nbins < 1) return SALSA_E_ARG;
   if (cfg->nspec_dry < 1 || cfg->nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
-  if (cfg->lssecice.sw || cfg->lscoag.mode == 2) return SALSA_E_UNSUPPORTED;
+  if (cfg->lssecice.sw) return SALSA_E_UNSUPPORTED;
   /* nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
      nj3 outside 1-3 STOPs once a cell nucleates (:600-602) */
   if (cfg->nsnucl == 4 || cfg->nsnucl < 0 || (cfg->nsnucl > 0 && (cfg->nj3 < 1 || cfg->nj3 > 3)))
@@ -2648,7 +2674,10 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   return SALSA_OK;
 }
 
-void salsa_ref_destroy(salsa_ref_ctx_t *ctx) { free(ctx); }
+void salsa_ref_destroy(salsa_ref_ctx_t *ctx) {
+  if (ctx) free(ctx->kcache);
+  free(ctx);
+}
 
 int salsa_ref_layout(const salsa_ref_ctx_t *c, int *nbins, int *ncld, int *nprc, int *nice, int *nwet,
                      double *lolim) {
@@ -2731,6 +2760,14 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
   int bstart[4] = {0, nbins, nbins + ncld, nbins + ncld + nprc};
   int bnum[4] = {nbins, ncld, nprc, nice};
   if (!carry_over) c->carry_valid = 0;
+  /* initialize_coagstorage (mo_salsa_driver.f90:601-650): zero storage for the grid */
+  if (g->lscoag.mode == 2 && (!c->kcache || c->kcache_cells != ncells)) {
+    free(c->kcache);
+    c->kcache = (double *)calloc((size_t)(ncells * kc_cell_doubles(c)), sizeof(double));
+    c->kcache_cells = c->kcache ? ncells : 0;
+    if (!c->kcache) return SALSA_E_ARG;
+  }
+  if (lvl4) { cl4.kcache = c->kcache; cl4.kcache_cells = c->kcache_cells; }
 
 #pragma omp parallel num_threads(nt) reduction(+ : s_eq, s_di, s_nf, s_co, s_ng, s_nan, ncell, cnt[:5])
   {
@@ -2755,6 +2792,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
       w->ice = &w->all[nbins + ncld + nprc]; w->liquid = &w->all[0];
       w->kappa = f->kappa;
       if (f->kappa) w->kappa_cell = f->kappa[p];
+      w->cell = q;
       double in_p = f->press[p], in_t = f->temp[p], in_rs = f->rsl[p];
       double in_rsi = (level == 5) ? f->rsi[p] : 0.;
       double in_w = f->wp ? f->wp[p] : 0.;
@@ -2793,6 +2831,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
         for (int i = 0; i < 5; i++) zg[i] = f->gaero[p + plane * i] * dn;
       for (int k = 0; k < ncld; k++) { actd_n[k] = 0.; for (int s2 = 0; s2 < NSP; s2++) actd_v[k * NSP + s2] = 0.; }
       salsa_cell(w, in_p, &in_rv, in_rs, in_rsi, in_t, tstep, in_w, level, actd_n, actd_v, zg);
+      if (g->lscoag.mode == 2 && c->lcgupdt) kc_copy(w, 1);   /* store_coag (:421-423) */
       for (int nb = 0; nb < c->ntotal; nb++) {
         Section *s = &w->all[nb];
         int icat = s->phase - 1;

@@ -129,3 +129,52 @@ def test_variant_parity(name, wl, kw, mod, call):
     for k, r in rep.items():
         assert r["violations"] <= VIOL_FRAC * r["n"], (name, k, r)
         assert r["frac_within"] >= FRAC_WITHIN, (name, k, r)
+
+
+@pytest.mark.parametrize("host", [False, True])
+def test_low_frequency_kernels(host):
+    """lscoag%mode = 2 over three steps (update, fetch with a changed state, update at a
+    multiple of cgintvl) against the oracle; with host arrays the slabs address the
+    storage by their first cell."""
+    inp = make_inputs("grid256x256x128", "cpu", precision=0, X=8, Y=8, Z=16)
+    inp.cfg.lscoag.mode, inp.cfg.cgintvl = 2, 10.
+    o = Oracle(inp.cfg)
+    step = SalsaStep(inp.cfg)
+    fields = {k: v.clone() for k, v in inp.fields.items()}
+    fields0 = {k: v.clone() for k, v in inp.fields.items()}    # the state the first (update) step stores
+    for time, istp in ((1.0, 1), (2.0, 2), (10.0, 10)):
+        ref = make_outputs(inp)
+        rc, _ = o.run(inp, {k: v.clone() for k, v in fields.items()}, ref, time=time, istp=istp)
+        assert rc == 0
+        env = {k: torch.zeros_like(v) for k, v in ref.items()}
+        for pf in PERTURBED:
+            for sgn in (1.0, -1.0):
+                f2 = {k: v.clone() for k, v in fields.items()}
+                f2[pf] = f2[pf] * (1 + sgn * 2.2e-16)
+                o2 = Oracle(inp.cfg)       # same storage state: replay the update step first
+                if istp > 1:
+                    warm = make_outputs(inp)
+                    o2.run(inp, {k: v.clone() for k, v in fields0.items()}, warm, time=1.0, istp=1)
+                out2 = make_outputs(inp)
+                o2.run(inp, f2, out2, time=time, istp=istp)
+                for k in env:
+                    env[k] = torch.maximum(env[k], (out2[k] - ref[k]).abs())
+        if host:
+            f = {k: v.clone().pin_memory() for k, v in fields.items()}
+            out = {k: v.pin_memory() for k, v in make_outputs(inp).items()}
+        else:
+            f = {k: v.clone().cuda() for k, v in fields.items()}
+            out = {k: v.cuda() for k, v in make_outputs(inp).items()}
+        rc, st = step.run(inp, f, out, time=time, istp=istp)
+        torch.cuda.synchronize()
+        assert rc == 0
+        inp.fields = fields
+        rep = check(inp, {k: v.cpu() for k, v in out.items()}, ref, env, 1e-10)
+        for k, r in rep.items():
+            assert r["violations"] <= VIOL_FRAC * r["n"], (time, k, r)
+            assert r["frac_within"] >= FRAC_WITHIN, (time, k, r)
+        # the next step starts from the new state
+        for t, v in (("naerot", "naero"), ("ncloudt", "ncloud"), ("nprecpt", "nprecp"), ("nicet", "nice"),
+                     ("maerot", "maero"), ("mcloudt", "mcloud"), ("mprecpt", "mprecp"), ("micet", "mice")):
+            fields[v] = (fields[v] + ref[t] * inp.dt).clamp(min=0)
+    step.close()

@@ -278,6 +278,34 @@ def test_cloud_base_activation():
     assert float(I(out2["pa_nactd"]).sum()) > float(na.sum())
 
 
+def test_low_frequency_kernel_storage():
+    """lscoag%mode = 2 (mo_salsa_driver.f90:297-298, 421-423, 469-470, 601-697): kernels are
+    computed and stored on update steps (istp <= 1 or time within one step of a multiple
+    of cgintvl) and fetched on the others; the storage starts at zero."""
+    base = make_inputs("grid256x256x128", "cpu", X=6, Y=6, Z=6)
+
+    def step(o, time, istp, fields=None):
+        out = make_outputs(base)
+        rc, _ = o.run(base, {k: v.clone() for k, v in (fields or base.fields).items()}, out, time=time, istp=istp)
+        assert rc == 0
+        return out
+    ref = step(Oracle(base.cfg), 1.0, 1)
+    cfg = make_inputs("grid256x256x128", "cpu", X=6, Y=6, Z=6).cfg
+    cfg.lscoag.mode, cfg.cgintvl = 2, 10.
+    o = Oracle(cfg)
+    first = step(o, 1.0, 1)
+    assert all(torch.equal(first[k], ref[k]) for k in ref)          # update step = mode 1
+    again = step(o, 2.0, 2)
+    assert all(torch.equal(again[k], ref[k]) for k in ref)          # fetched kernels of the same state
+    moved = {k: v.clone() for k, v in base.fields.items()}
+    moved["ncloud"] = moved["ncloud"] * 1.5
+    fetched = step(o, 3.0, 3, moved)
+    fresh = step(Oracle(base.cfg), 3.0, 3, moved)
+    assert not all(torch.equal(fetched[k], fresh[k]) for k in ref)  # stale kernels differ from new ones
+    empty = step(Oracle(cfg), 2.0, 2)
+    assert not all(torch.equal(empty[k], ref[k]) for k in ref)      # zero storage: no coagulation
+
+
 def test_threads_do_not_change_results():
     inp1, _, o1, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, nthreads=1)
     inp2, _, o2, _, _, _ = run("grid384x384x160", X=6, Y=6, Z=6, nthreads=0)

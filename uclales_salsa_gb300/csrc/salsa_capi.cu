@@ -141,6 +141,8 @@ struct salsa_handle {
   // staging buffers for host-pointer calls
   void *stage = nullptr;
   size_t stage_bytes = 0;
+  void *kcache = nullptr;       // kernel storage of lscoag%mode = 2
+  size_t kcache_bytes = 0;
   cudaStream_t s_in = nullptr, s_out = nullptr;     // copy streams of the host-buffer pipeline
   cudaEvent_t pev[3 * SALSA_PIPE_SLOTS + 2] = {};   // its slot and start/end events
   int *d_order = nullptr;       // cell order list (salsa_order_kernel)
@@ -217,7 +219,8 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
   if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
   // processes outside this build (the init check mirrors the oracle's)
-  if (g.lssecice.sw || g.lscoag.mode == 2) return SALSA_E_UNSUPPORTED;
+  if (g.lssecice.sw) return SALSA_E_UNSUPPORTED;
+  if (g.lscoag.mode == 2 && !(g.cgintvl > 0.)) return SALSA_E_ARG;
   // nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
   // nj3 outside 1-3 STOPs once a cell nucleates (:600-602)
   if (g.nsnucl == 4 || g.nsnucl < 0 || (g.nsnucl > 0 && (g.nj3 < 1 || g.nj3 > 3))) return SALSA_E_UNSUPPORTED;
@@ -354,6 +357,10 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   }
   B.lscndgas = g.lscndgas;
   B.nsnucl = g.nsnucl;
+  B.kc_mode = 0;
+  B.kc_stride = 0;
+  B.kc_base = 0;
+  B.kcache = nullptr;
   int ncat = (g.level == 5) ? 4 : 3;
   const int catnb[4] = {nbins, ncld, nprc, nice};
   B.raw_num = (int)rows.size();
@@ -556,6 +563,7 @@ void salsa_gb300_finalize(salsa_handle_t *h) {
   if (h->d_status) cudaFree(h->d_status);
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->stage) cudaFree(h->stage);
+  if (h->kcache) cudaFree(h->kcache);
   for (auto e : h->pev)
     if (e) cudaEventDestroy(e);
   if (h->s_in) cudaStreamDestroy(h->s_in);
@@ -661,6 +669,25 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     P.lsicehom = P.lsiceimm = P.lsicedep = 0;
   }
   P.has_kappa = f->kappa != nullptr;
+  // low-frequency kernel update (lscoag%mode = 2, set_SALSA_runtime :469-470): kernels are
+  // computed and stored on update steps and fetched from the storage on the others; the
+  // storage starts at zero (initialize_coagstorage :601-650)
+  if (g.lscoag.mode == 2 && P.st_coag && P.ncells > 0) {
+    if (noalloc) return SALSA_E_UNSUPPORTED;
+    const bool upd = std::fmod(time, g.cgintvl) < tstep || istp <= 1;
+    P.kc_mode = upd ? 1 : 2;
+    P.kc_stride = h->base.nb_pad * (h->base.nb_pad + 1) / 2;
+    const size_t bytes = (size_t)P.ncells * P.kc_stride * (g.precision == 0 ? 8 : 4);
+    if (bytes != h->kcache_bytes) {
+      if (h->kcache) cudaFree(h->kcache);
+      h->kcache = nullptr;
+      h->kcache_bytes = 0;
+      if (cudaMalloc(&h->kcache, bytes) != cudaSuccess) return SALSA_E_CUDA;
+      if (cudaMemset(h->kcache, 0, bytes) != cudaSuccess) return SALSA_E_CUDA;
+      h->kcache_bytes = bytes;
+    }
+    P.kcache = h->kcache;
+  }
   int nliq = h->base.nliquid;
   const int nb[4] = {h->base.nbins, h->base.ncld, h->base.nprc, h->base.nice};
   const int nw = h->base.nwet;
@@ -817,6 +844,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
       Q.plane = plane_s;
       Q.ncells = (long long)P.nz_int * P.nx_int * rs;
       Q.ngroups = (Q.ncells + SALSA_CPG - 1) / SALSA_CPG;
+      Q.kc_base = (long long)k * R * P.nz_int * P.nx_int;
       size_t off = 0;
       for (auto &x : fl) {
         const double *hp = x.src ? x.src : x.dst;

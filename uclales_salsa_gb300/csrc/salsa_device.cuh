@@ -105,6 +105,10 @@ struct DevParams {
   int lscndh2oae, lscndh2ocl, lscndh2oic, lsicehom, lsiceimm, lsicedep, ice_theta_dist, lsdistupdate;
   int has_kappa;
   int lscndgas, nsnucl;   // gas condensation; nucleation scheme (0: off)
+  // kernel storage of lscoag%mode = 2: 0 compute, 1 compute and store, 2 fetch
+  int kc_mode, kc_stride;  // kc_stride: kernel-type entries per cell (the kernel triangle)
+  long long kc_base;       // storage index of the call's first cell (host-buffer slabs)
+  void *kcache;
   double Eiagg_max, Eiagg_min, eddy_dis, rhlim, initMinTheta, chargeTimeMax, chargeCollEnh;
   double mean_theta_imm, sigma_theta_imm, mean_theta_dep, sigma_theta_dep;
   double iceShapeAlpha, iceShapeBeta, iceShapeGamma, iceShapeSigma;

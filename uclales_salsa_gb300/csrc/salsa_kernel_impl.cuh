@@ -929,7 +929,7 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, double dt, int lan
 
 template <typename KT>
 __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *tb, double dt, double T, double pres,
-                            bool diag, int lane) {
+                            bool diag, long long cell, int lane) {
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   // updateDiameter("all") on every bin (:146-152) and rhomean of the kernel categories
   for (int b = lane; b < P.ntotal; b += 32) {
@@ -945,7 +945,19 @@ __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *t
 #ifdef SALSA_STAGE_TIMERS
   long long t_k0 = clock64();
 #endif
-  build_kernels<KT>(P, w, tb, T, pres, lane);
+  if (P.kc_mode == 2) {
+    // fetch_coag (mo_salsa_driver.f90:297-298, 676-697): the kernels stored at the last
+    // update step of the low-frequency kernel mode
+    const KT *src = static_cast<const KT *>(P.kcache) + (P.kc_base + cell) * (long long)P.kc_stride;
+    for (int e = lane; e < P.kc_stride; e += 32) w.K[e] = src[e];
+    __syncwarp();
+  } else {
+    build_kernels<KT>(P, w, tb, T, pres, lane);
+    if (P.kc_mode == 1) {   // store_coag (:421-423, 655-674); the kernels do not change later in the step
+      KT *dst = static_cast<KT *>(P.kcache) + (P.kc_base + cell) * (long long)P.kc_stride;
+      for (int e = lane; e < P.kc_stride; e += 32) dst[e] = w.K[e];
+    }
+  }
 #ifdef SALSA_STAGE_TIMERS
   if (lane == 0 && P.stage_clocks) atomicAdd(P.stage_clocks + 8, (unsigned long long)(clock64() - t_k0));
 #endif
@@ -2549,7 +2561,7 @@ __device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *
 #endif
 
 template <typename KT, bool DIAG>
-__device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, int lane) {
+__device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, long long cell, int lane) {
 #ifdef SALSA_STAGE_TIMERS
   long long t_stage = clock64();
 #endif
@@ -2599,7 +2611,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   STAGE_MARK(0);
 
   // ---- salsa() ----
-  if (P.st_coag) coagulation<KT>(P, w, tb, dt, T, pres, DIAG, lane);
+  if (P.st_coag) coagulation<KT>(P, w, tb, dt, T, pres, DIAG, cell, lane);
   STAGE_MARK(1);
   if (P.st_cnd) {
     // condensation (mo_salsa_dynamics.f90:276-342): nucleation returns only the 3 nm
@@ -2739,7 +2751,7 @@ __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevP
       }
     __syncthreads();
     long long q = g * SALSA_CPG + warp;
-    if (q < P.ncells) cell_step<KT, DIAG>(P, w, tb, lane);
+    if (q < P.ncells) cell_step<KT, DIAG>(P, w, tb, cell_at(P, q), lane);
     __syncthreads();
     // write the group's output rows
     if (okc)
