@@ -255,6 +255,36 @@ int salsa_gb300_tend_constrain(salsa_handle_t *h, int nzp, int nxp, int nyp, dou
 int salsa_gb300_diagnostics(salsa_handle_t *h, int nzp, int nxp, int nyp, int only_diag, int lcharge,
                             const salsa_post_fields_t *f, void *stream);
 
+/* ---- Sedimentation and deposition of the bins (src/src_LES/mcrp.f90:745-1275) ----
+ * sedim_SALSA, called by micro after the step (step.f90:342): DepositionSlow for the
+ * aerosol and cloud bins (flux divergence of the fall speed, dry deposition on the
+ * lowest level) and DepositionFast for precipitation and ice (each parcel falls the
+ * distance of one time step, which may cross several levels).  Values are read; the
+ * tendencies, the liquid water potential temperature tendency tlt, the precipitation
+ * and ice fluxes rrate/irate (nzp,nxp,nyp) and sfcrrate/sfcirate (nxp,nyp) and the
+ * terminal velocities VtPrc/VtIce (nzp,nxp,nyp,nprc|nice) are written (the rates and
+ * velocities are overwritten, the tendencies and tlt added to).  tk, th and adn are the
+ * absolute and potential temperature and the air density; ustar (nxp,nyp) is the
+ * friction velocity and dzt (nzp) the inverse level thickness.  sed[0..3] switch the
+ * aerosol, cloud, precipitation and ice parts (sed_aero .. sed_ice); ice only at level
+ * 5.  Device pointers; asynchronous on `stream` (the library stream when NULL). */
+typedef struct {
+  const double *naero, *ncloud, *nprecp, *nice;       /* (nzp,nxp,nyp,nb) #/kg */
+  const double *maero, *mcloud, *mprecp, *mice;       /* (...,nspec*nb) kg/kg */
+  double *naerot, *ncloudt, *nprecpt, *nicet;         /* tendencies, added to */
+  double *maerot, *mcloudt, *mprecpt, *micet;
+  const double *tk, *th, *adn;                        /* (nzp,nxp,nyp) */
+  const double *ustar;                                /* (nxp,nyp) */
+  const double *dzt;                                  /* (nzp) */
+  double *tlt;                                        /* (nzp,nxp,nyp), added to */
+  double *rrate, *irate;                              /* (nzp,nxp,nyp) W/m2 */
+  double *sfcrrate, *sfcirate;                        /* (nxp,nyp) W/m2 */
+  double *VtPrc, *VtIce;                              /* (nzp,nxp,nyp,nprc|nice) m/s */
+} salsa_sedim_fields_t;
+
+int salsa_gb300_sedimentation(salsa_handle_t *h, int nzp, int nxp, int nyp, double dtlt, const int sed[4],
+                              const salsa_sedim_fields_t *f, void *stream);
+
 /* ---- Gradient harness (no counterpart in the reference, which has no adjoint) ----
  * A chain advances ncell independent warm cells (a level-4 handle) through nsub
  * steps of length dt.  Each step is the coagulation (mo_salsa_dynamics.f90:92-202)

@@ -3179,3 +3179,265 @@ int salsa_ref_diagnostics(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int onl
 #undef AT
   return SALSA_OK;
 }
+
+/* ======================================================================
+ * Sedimentation: src/src_LES/mcrp.f90:745-1275 (sedim_SALSA, DepositionSlow,
+ * DepositionFast).  Indices below are 0-based: level kc is the reference's k = kc + 1.
+ * The LES constants of defs.f90 (full-precision pi among them) sit beside the SALSA
+ * ones (pi6 of mo_submctl) as in the reference.
+ * ====================================================================== */
+#define LES_ALVL 2.5e+06
+#define LES_ALVI 2.834e+06
+#define LES_CP   1005.
+#define LES_G    9.81
+#define LES_KB   1.3807e-23
+#define SED_M    4.8096e-26
+#define SED_A    1.249
+#define SED_B    0.42
+#define SED_C    0.87
+
+/* calcDiamLES (mo_particle_external_properties.f90:169-201), spherical */
+static double calc_diam_les(const salsa_ref_ctx_t *c, int ns, double numc, const double *mass, int flag) {
+  if (numc < 1.e-15) return 0.;
+  double v = 0.;
+  for (int s = 0; s < ns; s++) v += mass[s] / (flag == 4 ? c->rhoice[s] : c->rholiq[s]);
+  return pow(v / numc / PI6, 1. / 3.);
+}
+
+/* per-level air properties (atm modelling eq. 4.54) */
+static void sed_air(double T, double adn, double *avis, double *kvis, double *lambda) {
+  *avis = 1.8325e-5 * (416.16 / (T + 120.0)) * pow(T / 296.16, 1.5);
+  *kvis = *avis / adn;
+  const double va = sqrt(8. * LES_KB * T / (PI_FULL * SED_M));
+  *lambda = 2. * *avis / (adn * va);
+}
+
+/* DepositionSlow (:926-1069) for nb bins of ns species; tendencies, tlt and the rates
+   are updated as sedim_SALSA does after the call (:790-835) */
+static void dep_slow(const salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, double dtlt, int nb, int ns, int flag,
+                     const double *numc, const double *mass, double *tn, double *tm, const salsa_sedim_fields_t *f) {
+  const long long plane = (long long)nzp * nxp * nyp;
+  const double clim = (flag == 3 || flag == 4) ? PRLIM : NLIM;
+  const int iw = ns - 1;   /* water: the last of the wet species */
+  double *rflm = (double *)calloc((size_t)nzp * nb * ns, sizeof(double));
+  double *rfln = (double *)calloc((size_t)nzp * nb, sizeof(double));
+  double *divm = (double *)calloc((size_t)nzp * nb * ns, sizeof(double));
+  double *divn = (double *)calloc((size_t)nzp * nb, sizeof(double));
+  double pmass[NSP];
+  for (int j = 2; j <= nyp - 3; j++)
+    for (int i = 2; i <= nxp - 3; i++) {
+      memset(rflm, 0, sizeof(double) * nzp * nb * ns);
+      memset(rfln, 0, sizeof(double) * nzp * nb);
+      memset(divm, 0, sizeof(double) * nzp * nb * ns);
+      memset(divn, 0, sizeof(double) * nzp * nb);
+      const long long col = (long long)nzp * (i + (long long)nxp * j);
+      for (int kc = nzp - 2; kc >= 1; kc--) {
+        const long long p = col + kc;
+        const int kp1 = kc + 1;
+        const double T = f->tk[p], ad = f->adn[p];
+        double avis, kvis, lambda;
+        sed_air(T, ad, &avis, &kvis, &lambda);
+        for (int bin = 0; bin < nb; bin++) {
+          const double n = numc[p + plane * bin];
+          if (n < clim) continue;
+          for (int s = 0; s < ns; s++) pmass[s] = mass[p + plane * ((long long)s * nb + bin)];
+          const double dwet = calc_diam_les(c, ns, n, pmass, flag);
+          double sm = 0.;
+          for (int s = 0; s < ns; s++) sm += pmass[s];
+          const double zdn = sm / n / (PI6 * cube(dwet));
+          const double Kn = 2. * lambda / dwet;
+          const double GG = 1. + Kn * (SED_A + SED_B * exp(-SED_C / Kn));
+          double vc = terminal_vel(dwet, zdn, ad, avis, GG, flag, NULL, 0.);
+          vc = fmind(vc, fmind(0.5 * (1. / f->dzt[kc]) / dtlt, 2.0));
+          if (kc == 1) {   /* the level just above the surface */
+            const double mdiff = (LES_KB * T * GG) / (3.0 * PI_FULL * avis * dwet);
+            const double Sc = kvis / mdiff;
+            double St = vc * pow(f->ustar[i + (long long)nxp * j], 2.0) / LES_G * kvis;
+            if (St < 0.01) St = 0.01;
+            const double rt = 1.0 / fmaxd(EPSR, (f->ustar[i + (long long)nxp * j] *
+                                                 (pow(Sc, -2.0 / 3.0) + pow(10., -3.0 / St))));
+            vc = (1. / rt) + vc;
+          }
+          for (int s = 0; s < ns; s++) rflm[(long long)kc * nb * ns + s * nb + bin] = -pmass[s] * vc;
+          rfln[kc * nb + bin] = -n * vc;
+        }
+        const double adp = f->adn[p + 1];
+        for (int e = 0; e < nb * ns; e++)
+          divm[(long long)kc * nb * ns + e] = (rflm[(long long)kp1 * nb * ns + e] * adp - rflm[(long long)kc * nb * ns + e] * ad) *
+                                              f->dzt[kc] / ad;
+        for (int e = 0; e < nb; e++)
+          divn[kc * nb + e] = (rfln[kp1 * nb + e] * adp - rfln[kc * nb + e] * ad) * f->dzt[kc] / ad;
+        double sw = 0.;   /* SUM(rflm(k,(ns-1)*nb:ns*nb)), 1-based as written */
+        for (int e = iw * nb - 1; e <= ns * nb - 1; e++) sw += rflm[(long long)kc * nb * ns + e];
+        f->rrate[p] = f->rrate[p] - sw * ad * LES_ALVL;
+      }
+      {
+        double sw = 0.;
+        for (int e = iw * nb - 1; e <= ns * nb - 1; e++) sw += rflm[(long long)1 * nb * ns + e];
+        const long long q = i + (long long)nxp * j;
+        f->sfcrrate[q] = f->sfcrrate[q] - sw * f->adn[col + 1] * LES_ALVL;
+      }
+      for (int kc = 1; kc <= nzp - 2; kc++) {
+        const long long p = col + kc;
+        for (int b = 0; b < nb; b++) tn[p + plane * b] = tn[p + plane * b] - divn[kc * nb + b];
+        for (int e = 0; e < nb * ns; e++) tm[p + plane * e] = tm[p + plane * e] - divm[(long long)kc * nb * ns + e];
+      }
+      for (int kc = 1; kc <= nzp - 1; kc++) {   /* k = 2 .. nzp */
+        const long long p = col + kc;
+        double sw = 0.;
+        for (int b = 0; b < nb; b++) sw += divm[(long long)kc * nb * ns + iw * nb + b];
+        f->tlt[p] = f->tlt[p] + sw * (LES_ALVL / LES_CP) * f->th[p] / f->tk[p];
+      }
+    }
+  free(rflm); free(rfln); free(divm); free(divn);
+}
+
+/* DepositionFast (:1073-1275) for nb bins of ns species, then sedim_SALSA's updates
+   (:840-905): tendencies += change / dtlt over the whole arrays, tlt */
+static void dep_fast(const salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, double dtlt, int nb, int ns, int flag,
+                     const double *numc, const double *mass, double *tn, double *tm, double *rate, double *srate,
+                     double *Vt, const salsa_sedim_fields_t *f) {
+  const long long plane = (long long)nzp * nxp * nyp;
+  const double clim = (flag == 3 || flag == 4) ? PRLIM : NLIM;
+  double *prnt = (double *)calloc((size_t)(plane * nb), sizeof(double));
+  double *prvt = (double *)calloc((size_t)(plane * nb * ns), sizeof(double));
+  double *prnchg = (double *)calloc((size_t)nzp * nb, sizeof(double));
+  double *prvchg = (double *)calloc((size_t)nzp * nb * ns, sizeof(double));
+  double *remprc = (double *)calloc((size_t)nb * ns, sizeof(double));
+  double pmass[NSP];
+  for (long long e = 0; e < plane * nb; e++) Vt[e] = 0.;
+  for (int j = 2; j <= nyp - 3; j++)
+    for (int i = 2; i <= nxp - 3; i++) {
+      memset(prnchg, 0, sizeof(double) * nzp * nb);
+      memset(prvchg, 0, sizeof(double) * nzp * nb * ns);
+      memset(remprc, 0, sizeof(double) * nb * ns);
+      const long long col = (long long)nzp * (i + (long long)nxp * j);
+      for (int kc = nzp - 2; kc >= 1; kc--) {
+        const long long p = col + kc;
+        const double T = f->tk[p], ad = f->adn[p];
+        double avis, kvis, lambda;
+        sed_air(T, ad, &avis, &kvis, &lambda);
+        (void)kvis;
+        for (int bin = 0; bin < nb; bin++) {
+          const double n = numc[p + plane * bin];
+          if (n < clim) continue;
+          for (int s = 0; s < ns; s++) pmass[s] = mass[p + plane * ((long long)s * nb + bin)];
+          const double dwet = calc_diam_les(c, ns, n, pmass, flag);
+          double dnsp = 0.;
+          Shape shape;
+          if (flag == 4) {
+            double mp = 0.;
+            for (int s = 0; s < ns - 1; s++) mp += pmass[s];
+            dnsp = getDiameter(c, mp, pmass[ns - 1], n);   /* calcDiamLES(sph=.FALSE.) */
+            getShapeCoefficients(c, &shape, mp, pmass[ns - 1], n);
+          }
+          double sm = 0.;
+          for (int s = 0; s < ns; s++) sm += pmass[s];
+          const double zdn = sm / n / (PI6 * cube(dwet));
+          const double Kn = 2. * lambda / dwet;
+          const double GG = 1. + Kn * (SED_A + SED_B * exp(-SED_C / Kn));
+          const double vc = flag < 4 ? terminal_vel(dwet, zdn, ad, avis, GG, flag, NULL, 0.)
+                                     : terminal_vel(dwet, zdn, ad, avis, GG, flag, &shape, dnsp);
+          Vt[p + plane * bin] = vc;
+          const double fdmax = dtlt * vc;
+          double fd = 0.;
+          int fi = 0, prcdep = 0;
+          while (fd < fdmax) {
+            fd = fd + (1. / f->dzt[kc - fi]);
+            fi = fi + 1;
+            if (kc - fi <= 0) { prcdep = 1; break; }
+          }
+          fi = fi - 1;
+          const int kf = kc - fi;
+          fd = fd - (1. / f->dzt[kf]);
+          const double fdos = fmind(fmaxd(fdmax - fd, 0.), 1. / f->dzt[kf]);
+          const double prnumc = n;
+          prnchg[kc * nb + bin] = prnchg[kc * nb + bin] - prnumc;
+          for (int ni = 0; ni < ns; ni++) {
+            pmass[ni] = mass[p + plane * ((long long)ni * nb + bin)];
+            prvchg[((long long)kc * nb + bin) * ns + ni] = prvchg[((long long)kc * nb + bin) * ns + ni] - pmass[ni];
+          }
+          if (prcdep)
+            for (int ni = 0; ni < ns; ni++) remprc[ni * nb + bin] = remprc[ni * nb + bin] + pmass[ni] * ad * vc;
+          if (flag == 4)
+            rate[p] = rate[p] + (mass[p + plane * ((long long)(ns - 2) * nb + bin)] +
+                                 mass[p + plane * ((long long)(ns - 1) * nb + bin)]) * ad * vc * LES_ALVI;
+          else
+            rate[p] = rate[p] + mass[p + plane * ((long long)(ns - 1) * nb + bin)] * ad * vc * LES_ALVL;
+          if (fdos * f->dzt[kf] > 0.5) {
+            prnchg[(kf - 1) * nb + bin] = prnchg[(kf - 1) * nb + bin] + prnumc * f->dzt[kf - 1] / f->dzt[kc];
+            for (int ni = 0; ni < ns; ni++) {
+              double *q = &prvchg[((long long)(kf - 1) * nb + bin) * ns + ni];
+              *q = *q + pmass[ni] * f->dzt[kf - 1] / f->dzt[kc];
+            }
+          } else {
+            prnchg[(kf - 1) * nb + bin] = prnchg[(kf - 1) * nb + bin] + (fdos * f->dzt[kf]) * prnumc * f->dzt[kf - 1] / f->dzt[kf];
+            prnchg[kf * nb + bin] = prnchg[kf * nb + bin] + (1. - fdos * f->dzt[kf]) * prnumc;
+            for (int ni = 0; ni < ns; ni++) {
+              double *q1 = &prvchg[((long long)(kf - 1) * nb + bin) * ns + ni];
+              double *q0 = &prvchg[((long long)kf * nb + bin) * ns + ni];
+              *q1 = *q1 + (fdos * f->dzt[kf]) * pmass[ni] * f->dzt[kf - 1] / f->dzt[kf];
+              *q0 = *q0 + (1. - fdos * f->dzt[kf]) * pmass[ni];
+            }
+          }
+        }
+      }
+      {
+        const long long q = i + (long long)nxp * j;
+        double sw = 0.;
+        const int e0 = (flag == 4 ? (ns - 2) * nb : (ns - 1) * nb) - 1;
+        for (int e = e0; e <= ns * nb - 1; e++) sw += remprc[e];
+        srate[q] = srate[q] + sw * (flag == 4 ? LES_ALVI : LES_ALVL);
+      }
+      for (int kc = 0; kc < nzp; kc++) {
+        const long long p = col + kc;
+        for (int b = 0; b < nb; b++) prnt[p + plane * b] = prnt[p + plane * b] + prnchg[kc * nb + b];
+        for (int ni = 0; ni < ns; ni++)
+          for (int b = 0; b < nb; b++)
+            prvt[p + plane * ((long long)ni * nb + b)] = prvt[p + plane * ((long long)ni * nb + b)] +
+                                                          prvchg[((long long)kc * nb + b) * ns + ni];
+      }
+    }
+  for (long long e = 0; e < plane * nb; e++) tn[e] = tn[e] + prnt[e] / dtlt;
+  for (long long e = 0; e < plane * nb * ns; e++) tm[e] = tm[e] + prvt[e] / dtlt;
+  const int w0 = (flag == 4 ? ns - 2 : ns - 1) * nb, w1 = ns * nb;   /* water (and rime) bins */
+  const double lat = flag == 4 ? LES_ALVI : LES_ALVL;
+  for (int j = 2; j <= nyp - 3; j++)
+    for (int i = 2; i <= nxp - 3; i++)
+      for (int kc = 0; kc <= nzp - 2; kc++) {
+        const long long p = kc + (long long)nzp * (i + (long long)nxp * j);
+        double sw = 0.;
+        for (int e = w0; e < w1; e++) sw += prvt[p + plane * e];
+        f->tlt[p] = f->tlt[p] - (sw / dtlt) * (lat / LES_CP) * f->th[p] / f->tk[p];
+      }
+  free(prnt); free(prvt); free(prnchg); free(prvchg); free(remprc);
+}
+
+int salsa_ref_sedimentation(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, double dtlt, const int sed[4],
+                            const salsa_sedim_fields_t *f) {
+  if (!c || !f || !sed || nzp < 3 || nxp < 5 || nyp < 5 || !(dtlt > 0.)) return SALSA_E_ARG;
+  const int lvl5 = c->cfg.level == 5, nspec = c->nwet;
+  if (!f->tk || !f->th || !f->adn || !f->ustar || !f->dzt || !f->tlt || !f->rrate || !f->sfcrrate) return SALSA_E_ARG;
+  if ((sed[0] && (!f->naero || !f->maero || !f->naerot || !f->maerot)) ||
+      (sed[1] && (!f->ncloud || !f->mcloud || !f->ncloudt || !f->mcloudt)) ||
+      (sed[2] && (!f->nprecp || !f->mprecp || !f->nprecpt || !f->mprecpt || !f->VtPrc)) ||
+      (sed[3] && lvl5 && (!f->nice || !f->mice || !f->nicet || !f->micet || !f->VtIce)))
+    return SALSA_E_ARG;
+  const long long plane = (long long)nzp * nxp * nyp, area = (long long)nxp * nyp;
+  for (long long e = 0; e < plane; e++) f->rrate[e] = 0.;
+  for (long long e = 0; e < area; e++) f->sfcrrate[e] = 0.;
+  if (lvl5) {
+    if (!f->irate || !f->sfcirate) return SALSA_E_ARG;
+    for (long long e = 0; e < plane; e++) f->irate[e] = 0.;
+    for (long long e = 0; e < area; e++) f->sfcirate[e] = 0.;
+  }
+  if (sed[0]) dep_slow(c, nzp, nxp, nyp, dtlt, c->nbins, nspec, 1, f->naero, f->maero, f->naerot, f->maerot, f);
+  if (sed[1]) dep_slow(c, nzp, nxp, nyp, dtlt, c->ncld, nspec, 2, f->ncloud, f->mcloud, f->ncloudt, f->mcloudt, f);
+  if (sed[2])
+    dep_fast(c, nzp, nxp, nyp, dtlt, c->nprc, nspec, 3, f->nprecp, f->mprecp, f->nprecpt, f->mprecpt, f->rrate,
+             f->sfcrrate, f->VtPrc, f);
+  if (sed[3] && lvl5)
+    dep_fast(c, nzp, nxp, nyp, dtlt, c->nice, nspec + 1, 4, f->nice, f->mice, f->nicet, f->micet, f->irate,
+             f->sfcirate, f->VtIce, f);
+  return SALSA_OK;
+}

@@ -42,6 +42,10 @@ int salsa_ref_tend_constrain(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, do
 int salsa_ref_diagnostics(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, int only_diag, int lcharge,
                           const salsa_post_fields_t *f);
 
+/* sedim_SALSA (src/src_LES/mcrp.f90:745-1275); arguments as salsa_gb300_sedimentation. */
+int salsa_ref_sedimentation(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, double dtlt, const int sed[4],
+                            const salsa_sedim_fields_t *f);
+
 int salsa_ref_run(salsa_ref_ctx_t *ctx, int nzp, int nxp, int nyp, int ns,
                   double tstep, double time, int istp, int level, int lcharge,
                   int initialize, const salsa_fields_t *f, salsa_status_t *st,

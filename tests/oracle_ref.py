@@ -7,7 +7,8 @@ import ctypes as C
 import os
 import subprocess
 
-from uclales_salsa_gb300.capi import Config, Fields, PostFields, Status, make_fields, make_post_fields
+from uclales_salsa_gb300.capi import (Config, Fields, PostFields, SedimFields, Status, make_fields,
+                                     make_post_fields, make_sedim_fields)
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB = os.path.join(ROOT, "oracle", "_build", "libsalsa_ref.so")
@@ -43,6 +44,9 @@ def lib():
         L.salsa_ref_diagnostics.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                             C.POINTER(PostFields)]
         L.salsa_ref_diagnostics.restype = C.c_int
+        L.salsa_ref_sedimentation.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                              C.POINTER(C.c_int * 4), C.POINTER(SedimFields)]
+        L.salsa_ref_sedimentation.restype = C.c_int
         _lib = L
     return _lib
 
@@ -69,6 +73,11 @@ class Oracle:
     def diagnostics(self, nzp, nxp, nyp, arrays, only_diag=0, lcharge=0):
         f = make_post_fields(arrays)
         return lib().salsa_ref_diagnostics(self.h, nzp, nxp, nyp, only_diag, lcharge, C.byref(f))
+
+    def sedimentation(self, nzp, nxp, nyp, dtlt, sed, arrays):
+        f = make_sedim_fields(arrays)
+        sw = (C.c_int * 4)(*[int(bool(x)) for x in sed])
+        return lib().salsa_ref_sedimentation(self.h, nzp, nxp, nyp, dtlt, C.byref(sw), C.byref(f))
 
     def layout(self):
         v = [C.c_int() for _ in range(5)]

@@ -1,0 +1,67 @@
+"""sedim_SALSA on the GPU (salsa_gb300_sedimentation) against the oracle on the same
+states.  The kernel takes the reference's operations in the reference's order; the
+wet diameter (pow(x, 1/3) against cbrt), the viscosity's (T/296.16)**1.5 and the fall
+speed's exp/log come from other libraries, so values agree to a few ulps, and the
+tests hold every output to 1e-10 of its change."""
+import pytest
+import torch
+
+from uclales_salsa_gb300.api import SalsaStep
+from oracle_ref import Oracle
+from sedim_cases import sedim_state, FILL
+
+pytestmark = pytest.mark.gpu
+CASES = [
+    ("grid16x16x40", dict(X=8, Y=8, Z=40), 1.0, (1, 1, 1, 1)),          # two rounds of 32 levels
+    ("grid16x16x40", dict(X=6, Y=5, Z=32), 0.7, (1, 1, 1, 1)),          # level 32 opens the second round
+    ("grid256x256x128", dict(X=6, Y=6, Z=128), 4.0, (1, 1, 1, 1)),      # five rounds; falls over many levels
+    ("grid384x384x160", dict(X=8, Y=8, Z=20), 1.0, (1, 0, 1, 1)),
+    ("grid384x384x160", dict(X=5, Y=7, Z=24), 2.5, (0, 1, 0, 1)),
+]
+RTOL = 1e-10
+
+
+def _check(name, base, ref, dev):
+    """Changes (ref - base, dev - base) agree to RTOL of the change, or to 1e-11 of the
+    largest change of the array for entries far below it (a parcel's removal and its
+    partial re-deposit at the same level cancel, and the ice fall speed's
+    sqrt(1 + c1 sqrt(X)) - 1 magnifies ulp differences for small crystals); at most
+    1e-6 of the entries may miss."""
+    dr = ref - base
+    dd = dev.cpu() - base
+    scale = float(dr.abs().max())
+    err = (dd - dr).abs()
+    bad = err > RTOL * dr.abs() + 1e-11 * scale
+    nbad = int(bad.sum())
+    assert nbad <= 1e-6 * dr.numel(), (name, nbad, float(err.max()), scale)
+    return scale
+
+
+@pytest.mark.parametrize("wl,kw,dtlt,sed", CASES, ids=[f"{c[0]}-dt{c[2]}-{''.join(map(str, c[3]))}" for c in CASES])
+def test_sedimentation_matches_oracle(wl, kw, dtlt, sed):
+    inp, a = sedim_state(wl, **kw)
+    ref = {k: v.clone() for k, v in a.items()}
+    assert Oracle(inp.cfg).sedimentation(inp.nzp, inp.nxp, inp.nyp, dtlt, sed, ref) == 0
+    dev = {k: v.clone().cuda() for k, v in a.items()}
+    step = SalsaStep(inp.cfg)
+    step.sedimentation(inp.nzp, inp.nxp, inp.nyp, dtlt, sed, dev)
+    torch.cuda.synchronize()
+    step.close()
+    moved = 0
+    for k in ref:
+        base = a[k] if not torch.all(a[k] == FILL) else torch.zeros_like(a[k])
+        moved += _check(k, base, ref[k], dev[k]) > 0
+    assert moved >= 6
+
+
+def test_sedimentation_arguments():
+    inp, a = sedim_state("grid16x16x40", X=4, Y=4, Z=8)
+    step = SalsaStep(inp.cfg)
+    with pytest.raises(Exception):   # host arrays are refused
+        step.sedimentation(inp.nzp, inp.nxp, inp.nyp, 1.0, (1, 1, 1, 1), a)
+    dev = {k: v.clone().cuda() for k, v in a.items() if k != "mprecpt"}
+    with pytest.raises(Exception):   # a switched-on part without its tendency
+        step.sedimentation(inp.nzp, inp.nxp, inp.nyp, 1.0, (0, 0, 1, 0), dev)
+    step.sedimentation(inp.nzp, inp.nxp, inp.nyp, 1.0, (1, 1, 0, 0), dev)   # fine without it when off
+    torch.cuda.synchronize()
+    step.close()

@@ -10,7 +10,8 @@ layout.  The CUDA library is required: there is no CPU path.
 import ctypes as C
 import os
 
-from .capi import Config, Fields, PostFields, Status, make_fields, make_post_fields, ERROR_NAMES
+from .capi import (Config, Fields, PostFields, SedimFields, Status, make_fields, make_post_fields,
+                   make_sedim_fields, ERROR_NAMES)
 
 _lib = None
 
@@ -52,6 +53,9 @@ def library():
     L.salsa_gb300_diagnostics.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.POINTER(PostFields), C.c_void_p]
     L.salsa_gb300_diagnostics.restype = C.c_int
+    L.salsa_gb300_sedimentation.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                            C.POINTER(C.c_int * 4), C.POINTER(SedimFields), C.c_void_p]
+    L.salsa_gb300_sedimentation.restype = C.c_int
     L.salsa_gb300_finalize.argtypes = [C.c_void_p]
     L.salsa_gb300_version.restype = C.c_char_p
     _lib = L
@@ -62,7 +66,7 @@ EXPORTED = ["salsa_gb300_default_config", "salsa_gb300_init", "salsa_gb300_run",
             "salsa_gb300_layout", "salsa_gb300_last_launches", "salsa_gb300_last_kernel_ms",
             "salsa_gb300_finalize", "salsa_gb300_version", "salsa_gb300_run_noalloc", "salsa_gb300_chain_state_size",
             "salsa_gb300_chain_forward", "salsa_gb300_chain_tlm", "salsa_gb300_chain_adjoint",
-            "salsa_gb300_tend_constrain", "salsa_gb300_diagnostics"]
+            "salsa_gb300_tend_constrain", "salsa_gb300_diagnostics", "salsa_gb300_sedimentation"]
 
 
 class SalsaStep:
@@ -114,6 +118,16 @@ class SalsaStep:
                                                C.c_void_p(stream.cuda_stream if stream else 0))
         if rc != 0:
             raise SalsaError(rc, "salsa_gb300_diagnostics")
+
+    def sedimentation(self, nzp, nxp, nyp, dtlt, sed, arrays, stream=None):
+        """sedim_SALSA (src/src_LES/mcrp.f90:745-905) on CUDA tensors: `arrays` maps
+        SedimFields names to tensors; sed = (aero, cloud, precp, ice) switches."""
+        f = make_sedim_fields(arrays)
+        sw = (C.c_int * 4)(*[int(bool(x)) for x in sed])
+        rc = library().salsa_gb300_sedimentation(self.h, nzp, nxp, nyp, dtlt, C.byref(sw), C.byref(f),
+                                                 C.c_void_p(stream.cuda_stream if stream else 0))
+        if rc != 0:
+            raise SalsaError(rc, "salsa_gb300_sedimentation")
 
     def last_launches(self):
         return library().salsa_gb300_last_launches(self.h)

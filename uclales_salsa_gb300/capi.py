@@ -98,6 +98,11 @@ class Fields(C.Structure):
     ]
 
 
+SEDIM_NAMES = ("naero", "ncloud", "nprecp", "nice", "maero", "mcloud", "mprecp", "mice",
+               "naerot", "ncloudt", "nprecpt", "nicet", "maerot", "mcloudt", "mprecpt", "micet",
+               "tk", "th", "adn", "ustar", "dzt", "tlt", "rrate", "irate", "sfcrrate", "sfcirate", "VtPrc", "VtIce")
+
+
 class PostFields(C.Structure):
     """salsa_post_fields_t: the arrays of tend_constrain2 and SALSA_diagnostics."""
     _fields_ = [(n, _PD) for n in (
@@ -112,6 +117,23 @@ def make_post_fields(arrays):
     names = {n for n, _ in PostFields._fields_}
     for name, t in arrays.items():
         if name not in names or t is None:
+            continue
+        if not t.is_contiguous() or t.dtype.itemsize != 8:
+            raise ValueError(f"field {name} must be a contiguous float64 tensor")
+        setattr(f, name, ptr_of(t.data_ptr()))
+    return f
+
+
+class SedimFields(C.Structure):
+    """salsa_sedim_fields_t: the arrays of sedim_SALSA (src/src_LES/mcrp.f90:745-905)."""
+    _fields_ = [(n, _PD) for n in SEDIM_NAMES]
+
+
+def make_sedim_fields(arrays):
+    """SedimFields with the data pointers of the tensors in `arrays` (name -> tensor)."""
+    f = SedimFields()
+    for name, t in arrays.items():
+        if name not in SEDIM_NAMES or t is None:
             continue
         if not t.is_contiguous() or t.dtype.itemsize != 8:
             raise ValueError(f"field {name} must be a contiguous float64 tensor")

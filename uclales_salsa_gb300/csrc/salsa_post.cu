@@ -16,11 +16,15 @@
 // order of their bits as integers), or an exponent bound that settles all but the cases
 // near the threshold, which then take the FP64 comparison.  FP64 arithmetic remains
 // where a value is produced.
+//
+// sedim_SALSA (src/src_LES/mcrp.f90:745-1275) runs one warp per column with the lanes
+// over the levels; see the comment above sedimentation_kernel.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 #include "../../include/salsa_gb300.h"
-#include "salsa_device.cuh"
+#include "salsa_kernel_impl.cuh"
 #include "salsa_internal.h"
 
 namespace salsa {
@@ -363,6 +367,368 @@ __global__ void __launch_bounds__(128) diagnostics_kernel(const PostArgs A) {
   }
 }
 
+// ---- sedim_SALSA (src/src_LES/mcrp.f90:745-1275) ----
+// One warp per column, lane l on levels l, l+32, ... (0-based: level kc is the
+// reference's k = kc + 1).  Per column, in the reference's order:
+//   DepositionSlow (:926-1069) for the aerosol and then the cloud bins: the flux of
+//     level kc+1 comes from the next lane by a shuffle (from the round above through a
+//     shared carry at a round boundary), and the divergence is subtracted from the
+//     tendency in place;
+//   DepositionFast (:1073-1275) for precipitation and then ice: pass A gives each source
+//     level its fall speed and the level kf that its parcel reaches; pass B gathers, for
+//     every target level, the contributions of the sources above it in the order the
+//     reference adds them (sources from the top down, the removal of the level's own
+//     parcel before its own re-deposit), so each change is the reference's sum.
+// The sums over bins (rrate, tlt, the surface rates) are taken in the reference's index
+// order, including the range (ns-1)*nb:ns*nb of its water sums, which starts at the
+// last bin of the species before water.  Halo columns only get their rates and fall
+// speeds zeroed, as the reference's whole-array assignments do; the reference also adds
+// a zero change to their precipitation and ice tendencies, which leaves every value as
+// it is apart from the sign of a negative zero, and that is not repeated here.
+constexpr double LES_ALVL = 2.5e+06, LES_ALVI = 2.834e+06, LES_CP = 1005., LES_G = 9.81, LES_KB = 1.3807e-23;
+constexpr double LES_PI = 3.14159265358979323846;   // defs.f90 pi (the SALSA pi6 stays truncated)
+constexpr double SED_M = 4.8096e-26, SED_A = 1.249, SED_B = 0.42, SED_C = 0.87;
+constexpr double EPS_REAL = 2.220446049250313e-16;   // epsilon(1.0) of the 8-byte default real
+constexpr int SED_KF = 0xffff, SED_BR = 1 << 16, SED_DEP = 1 << 17;   // pass-A code: kf | branch | deposited
+constexpr int SED_NS = SALSA_MAXSPEC + 2;   // species slots of a bin (wet species and rime)
+
+struct SedArgs {
+  DevParams P;                    // densities and ice shape parameters
+  long long plane;
+  int nzp, nxp, nyp, nspec, lvl5;
+  int sed[4];
+  int off_carry, off_vc, off_f1, off_kf, off_ws, off_rime, off_rem, off_sr;   // shared layout (doubles)
+  int warp_doubles;
+  double dtlt;
+  salsa_sedim_fields_t f;
+};
+
+struct SedAir { double avis, kvis, lambda; };
+
+// atm modelling eq. 4.54 (:986-989)
+__device__ __forceinline__ SedAir sed_air(double T, double ad) {
+  SedAir a;
+  const double x = T / 296.16;
+  a.avis = 1.8325e-5 * (416.16 / (T + 120.0)) * (x * sqrt(x));
+  a.kvis = a.avis / ad;
+  const double va = sqrt(8. * LES_KB * T / (LES_PI * SED_M));
+  a.lambda = 2. * a.avis / (ad * va);
+  return a;
+}
+
+// mo_ice_shape.f90:46-91 getDiameter (the maximum dimension of a non-spherical crystal)
+__device__ double ice_diameter(const DevParams &P, double mpri, double mrim, double numc) {
+  double res = 1.e-9;
+  if (numc < 1.e-6) return res;
+  const double Mtot = (mpri + mrim) / numc;
+  const double Fr = fmax(fmin(mrim / (Mtot * numc), 0.9999), 0.0001);
+  const double rho_b = Fr * K_RHORI + (1. - Fr) * K_RHOIC;
+  const double Dth = pow(K_PI6 * K_RHOIC / P.iceShapeAlpha, 1. / (P.iceShapeBeta - 3.));
+  const double Dgr = pow(P.iceShapeAlpha / (K_PI6 * rho_b), 1. / (3. - P.iceShapeBeta));
+  const double Dcr = pow((1. / (1. - Fr)) * P.iceShapeAlpha / (K_PI6 * rho_b), 1. / (3. - P.iceShapeBeta));
+  const double Mth = K_RHOIC * K_PI6 * cube(Dth), Mgr = rho_b * K_PI6 * cube(Dgr), Mcr = rho_b * K_PI6 * cube(Dcr);
+  if (Mtot < Mth) res = cbrt(Mtot / (K_PI6 * K_RHOIC));
+  else if (Mtot >= Mth && Mtot < Mgr) res = pow(Mtot / P.iceShapeAlpha, 1. / P.iceShapeBeta);
+  else if (Mtot >= Mgr && Mtot < Mcr) res = cbrt(Mtot / (K_PI6 * rho_b));
+  else if (Mtot >= Mcr) res = pow(Mtot / ((1. / (1. - Fr)) * P.iceShapeAlpha), 1. / P.iceShapeBeta);
+  return res;
+}
+
+// fall speed of one bin (:999-1011 and :1148-1173): the wet diameter, the particle
+// density, the slip correction GG and terminal_vel; m holds the bin's ns masses
+__device__ __forceinline__ double sed_speed(const SedArgs &A, int flag, int ns, double n, const double (&m)[SED_NS],
+                                            double ad, const SedAir &air, double &dwet, double &GG) {
+  double v = 0., sm = 0.;
+#pragma unroll
+  for (int s = 0; s < SED_NS; s++)
+    if (s < ns) {
+      v += m[s] / (flag == 4 ? A.P.rhoice[s] : A.P.rholiq[s]);
+      sm += m[s];
+    }
+  dwet = n < 1.e-15 ? 0. : cbrt(v / n / K_PI6);   // calcDiamLES, spherical
+  Shape<double> sh{0., 0., 0., 0.};
+  double dnsp = 0.;
+  if (flag == 4) {
+    double mp = 0., mr = 0.;
+#pragma unroll
+    for (int s = 0; s < SED_NS; s++) {
+      if (s < ns - 1) mp += m[s];
+      if (s == ns - 1) mr = m[s];
+    }
+    dnsp = n < 1.e-15 ? 0. : ice_diameter(A.P, mp, mr, n);   // calcDiamLES, non-spherical
+    shape_coeffs<double>(A.P, sh, mp, mr, n);
+  }
+  const double zdn = sm / n / (K_PI6 * cube(dwet));
+  const double Kn = 2. * air.lambda / dwet;
+  GG = 1. + Kn * (SED_A + SED_B * exp(-SED_C / Kn));
+  return terminal_vel<double>(dwet, zdn, ad, air.avis, GG, flag, sh, dnsp);
+}
+
+// DepositionSlow for one part of one column, with sedim_SALSA's tendency and tlt
+// updates (:799-843)
+__device__ void sed_slow(const SedArgs &A, double *sm, long long col, long long c2, int nb, int flag,
+                         const double *numc, const double *mass, double *tn, double *tm, int lane) {
+  const int nzp = A.nzp, ns = A.nspec, R = (nzp + 31) >> 5, cw = (ns + 1) * nb;
+  const long long pl = A.plane;
+  double *tlt_s = sm, *rr_s = sm + nzp, *carry = sm + A.off_carry, *sr_s = sm + A.off_sr;
+  for (int e = lane; e < 2 * cw; e += 32) carry[e] = 0.;
+  __syncwarp();
+  for (int r = R - 1; r >= 0; r--) {
+    const int kc = r * 32 + lane;
+    const bool inr = kc >= 1 && kc <= nzp - 2;
+    const long long p = col + kc;
+    double ad = 1., adp = 1., dz = 0., T = 0.;
+    SedAir air{0., 0., 0.};
+    if (inr) {
+      T = A.f.tk[p];
+      ad = A.f.adn[p];
+      adp = A.f.adn[p + 1];
+      dz = A.f.dzt[kc];
+      air = sed_air(T, ad);
+    }
+    const double *cin = carry + ((r + 1) & 1) * cw;
+    double *cout = carry + (r & 1) * cw;
+    double rsum = 0., tsum = 0., wl_r = 0., wl_d = 0.;
+    for (int bi = 0; bi < nb; bi++) {
+      const int b = bi == 0 ? nb - 1 : bi - 1;   // the last bin first: it opens the water sum
+      const double n = inr ? numc[p + pl * b] : 0.;
+      const bool act = inr && n >= K_NLIM;
+      double m[SED_NS];
+#pragma unroll
+      for (int s = 0; s < SED_NS; s++) m[s] = (act && s < ns) ? mass[p + pl * ((long long)s * nb + b)] : 0.;
+      double vc = 0.;
+      if (act) {
+        double dwet, GG;
+        vc = sed_speed(A, flag, ns, n, m, ad, air, dwet, GG);
+        vc = fmin(vc, fmin(0.5 * (1. / dz) / A.dtlt, 2.0));
+        if (kc == 1) {   // the level just above the surface (:1020-1028)
+          const double us = A.f.ustar[c2];
+          const double mdiff = (LES_KB * T * GG) / (3.0 * LES_PI * air.avis * dwet);
+          const double Sc = air.kvis / mdiff;
+          double St = vc * (us * us) / LES_G * air.kvis;
+          if (St < 0.01) St = 0.01;
+          const double rt = 1.0 / fmax(EPS_REAL, (us * (pow(Sc, -2.0 / 3.0) + pow(10., -3.0 / St))));
+          vc = (1. / rt) + vc;
+        }
+      }
+      // number flux, then the species in mass-index order
+#pragma unroll
+      for (int s = -1; s < SED_NS; s++) {
+        if (s >= ns) continue;
+        const double q = s < 0 ? n : m[s < 0 ? 0 : s];
+        const double rf = act ? -q * vc : 0.;
+        double up = __shfl_down_sync(0xffffffffu, rf, 1);
+        const int ci = b * (ns + 1) + (s + 1);
+        if (lane == 31) up = cin[ci];
+        if (lane == 0) cout[ci] = rf;
+        const double d = inr ? (up * adp - rf * ad) * dz / ad : 0.;
+        if (inr) {
+          double *t = s < 0 ? tn + p + pl * b : tm + p + pl * ((long long)s * nb + b);
+          *t = *t - d;
+        }
+        if (s == ns - 2 && bi == 0) rsum = 0. + rf;   // rflm(k,(ns-1)*nb) opens the sum
+        if (s == ns - 1) {
+          if (bi == 0) { wl_r = rf; wl_d = d; }
+          else { rsum += rf; tsum += d; }
+        }
+      }
+    }
+    rsum += wl_r;
+    tsum += wl_d;
+    if (inr) {
+      rr_s[kc] = rr_s[kc] - rsum * ad * LES_ALVL;
+      if (kc == 1) sr_s[0] = sr_s[0] - rsum * ad * LES_ALVL;
+    }
+    if (kc >= 1 && kc <= nzp - 1) tlt_s[kc] = tlt_s[kc] + tsum * (LES_ALVL / LES_CP) * A.f.th[p] / A.f.tk[p];
+    __syncwarp();
+  }
+}
+
+// DepositionFast for one part of one column, with sedim_SALSA's tendency and tlt
+// updates (:847-905)
+__device__ void sed_fast(const SedArgs &A, double *sm, long long col, int nb, int ns, int flag, const double *numc,
+                         const double *mass, double *tn, double *tm, double *Vt, double *rate_s, double *srate_s,
+                         int lane) {
+  const int nzp = A.nzp, R = (nzp + 31) >> 5;
+  const long long pl = A.plane;
+  const double alv = flag == 4 ? LES_ALVI : LES_ALVL;
+  const int iw = flag == 4 ? ns - 2 : ns - 1;   // water; for ice the rime follows it
+  double *tlt_s = sm, *vc_s = sm + A.off_vc, *f1_s = sm + A.off_f1, *ws_s = sm + A.off_ws, *rime_s = sm + A.off_rime,
+         *rem_s = sm + A.off_rem;
+  int *kf_s = (int *)(sm + A.off_kf);
+  const double *dzt = A.f.dzt;
+  for (int e = lane; e < nzp; e += 32) ws_s[e] = 0.;
+  for (int b = 0; b < nb; b++) {
+    // pass A: fall speed and destination of each source level (:1140-1216)
+    int span = -1;
+    for (int r = 0; r < R; r++) {
+      const int kc = r * 32 + lane;
+      const bool inr = kc >= 1 && kc <= nzp - 2;
+      const long long p = col + kc;
+      const double n = inr ? numc[p + pl * b] : 0.;
+      const bool act = inr && n >= K_PRLIM;
+      double vc = 0.;
+      int code = -1;
+      if (act) {
+        double m[SED_NS];
+#pragma unroll
+        for (int s = 0; s < SED_NS; s++) m[s] = s < ns ? mass[p + pl * ((long long)s * nb + b)] : 0.;
+        const double ad = A.f.adn[p];
+        const SedAir air = sed_air(A.f.tk[p], ad);
+        double dwet, GG;
+        vc = sed_speed(A, flag, ns, n, m, ad, air, dwet, GG);
+        const double fdmax = A.dtlt * vc;
+        double fd = 0.;
+        int fi = 0;
+        bool dep = false;
+        while (fd < fdmax) {   // at most kc passes
+          fd = fd + (1. / dzt[kc - fi]);
+          fi = fi + 1;
+          if (kc - fi <= 0) { dep = true; break; }
+        }
+        fi = fi - 1;
+        const int kf = kc - fi;
+        fd = fd - (1. / dzt[kf]);
+        const double fdos = fmin(fmax(fdmax - fd, 0.), 1. / dzt[kf]);
+        const double f1 = fdos * dzt[kf];
+        code = kf | (f1 > 0.5 ? SED_BR : 0) | (dep ? SED_DEP : 0);
+        vc_s[kc] = vc;
+        f1_s[kc] = f1;
+        span = max(span, kc - kf);
+        double mw = 0.;
+#pragma unroll
+        for (int s = 0; s < SED_NS; s++) if (s == iw) mw = m[s];
+        if (flag == 4) {
+          double mr = 0.;
+#pragma unroll
+          for (int s = 0; s < SED_NS; s++) if (s == ns - 1) mr = m[s];
+          mw = mw + mr;
+        }
+        rate_s[kc] = rate_s[kc] + mw * ad * vc * alv;
+      }
+      if (kc < nzp) {
+        kf_s[kc] = code;
+        Vt[p + pl * b] = vc;
+      }
+    }
+    const int F = __reduce_max_sync(0xffffffffu, span);
+    __syncwarp();
+    // removal statistics of the parcels that reach the surface (:1197-1202): the
+    // elements that the surface rate sums
+    if (lane < 3) {
+      int s = -1, pos = 0;
+      if (lane == 0 && b == nb - 1) { s = iw - 1; pos = 0; }
+      if (lane == 1) { s = iw; pos = 1 + b; }
+      if (lane == 2 && flag == 4) { s = ns - 1; pos = 1 + nb + b; }
+      if (s >= 0) {
+        double acc = 0.;
+        for (int kc = nzp - 2; kc >= 1; kc--) {
+          const int code = kf_s[kc];
+          if (code >= 0 && (code & SED_DEP)) acc = acc + mass[col + kc + pl * ((long long)s * nb + b)] * A.f.adn[col + kc] * vc_s[kc];
+        }
+        rem_s[pos] = acc;
+      }
+    }
+    // pass B: each target level gathers its change (:1218-1250), number then species
+    for (int s = -1; s < ns; s++) {
+      const double *src = s < 0 ? numc + col + pl * b : mass + col + pl * ((long long)s * nb + b);
+      double *dst = s < 0 ? tn + col + pl * b : tm + col + pl * ((long long)s * nb + b);
+      for (int r = 0; r < R; r++) {
+        const int L = r * 32 + lane;
+        if (L >= nzp) continue;
+        double acc = 0.;
+        const int k0 = min(nzp - 2, L + 1 + F), k1 = max(1, L - 1);
+        for (int k = k0; k >= k1; k--) {
+          const int code = kf_s[k];
+          if (code < 0) continue;
+          const int kf = code & SED_KF;
+          if (k != L && kf - 1 != L && kf != L) continue;
+          const double v = src[k];
+          if (k == L) acc = acc - v;
+          if (kf - 1 == L) {
+            if (code & SED_BR) acc = acc + v * dzt[kf - 1] / dzt[k];
+            else acc = acc + (f1_s[k] * v) * dzt[kf - 1] / dzt[kf];
+          } else if (kf == L && !(code & SED_BR)) {
+            acc = acc + (1. - f1_s[k]) * v;
+          }
+        }
+        const double val = 0. + acc;
+        dst[L] = dst[L] + val / A.dtlt;
+        if (s == iw) ws_s[L] += val;
+        if (flag == 4 && s == ns - 1) rime_s[L * nb + b] = val;
+      }
+    }
+    __syncwarp();
+  }
+  // surface rate (:1252-1257) and tlt (:867-876, :893-902)
+  if (lane == 0) {
+    double S = 0.;
+    const int npos = flag == 4 ? 1 + 2 * nb : 1 + nb;
+    for (int e = 0; e < npos; e++) S += rem_s[e];
+    srate_s[0] = srate_s[0] + S * alv;
+  }
+  for (int r = 0; r < R; r++) {
+    const int L = r * 32 + lane;
+    if (L > nzp - 2) continue;
+    double S = ws_s[L];
+    if (flag == 4)
+      for (int b = 0; b < nb; b++) S += rime_s[L * nb + b];
+    const long long p = col + L;
+    tlt_s[L] = tlt_s[L] - (S / A.dtlt) * (alv / LES_CP) * A.f.th[p] / A.f.tk[p];
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(128) sedimentation_kernel(const SedArgs A) {
+  extern __shared__ double sed_smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long c2 = (long long)blockIdx.x * (blockDim.x >> 5) + wib;   // column i + nxp*j
+  if (c2 >= (long long)A.nxp * A.nyp) return;
+  const int i = (int)(c2 % A.nxp), j = (int)(c2 / A.nxp), nzp = A.nzp;
+  const long long col = (long long)nzp * c2, pl = A.plane;
+  const bool fprc = A.sed[2], fice = A.sed[3] && A.lvl5;
+  if (i < 2 || i > A.nxp - 3 || j < 2 || j > A.nyp - 3) {   // halo: the whole-array zeroing only
+    for (int k = lane; k < nzp; k += 32) {
+      A.f.rrate[col + k] = 0.;
+      if (A.lvl5) A.f.irate[col + k] = 0.;
+      if (fprc) for (int b = 0; b < A.P.nprc; b++) A.f.VtPrc[col + k + pl * b] = 0.;
+      if (fice) for (int b = 0; b < A.P.nice; b++) A.f.VtIce[col + k + pl * b] = 0.;
+    }
+    if (lane == 0) {
+      A.f.sfcrrate[c2] = 0.;
+      if (A.lvl5) A.f.sfcirate[c2] = 0.;
+    }
+    return;
+  }
+  double *sm = sed_smem + (size_t)wib * A.warp_doubles;
+  double *tlt_s = sm, *rr_s = sm + nzp, *ir_s = sm + 2 * nzp, *sr_s = sm + A.off_sr;
+  for (int k = lane; k < nzp; k += 32) {
+    tlt_s[k] = A.f.tlt[col + k];
+    rr_s[k] = 0.;
+    ir_s[k] = 0.;
+  }
+  if (lane == 0) sr_s[0] = sr_s[1] = 0.;
+  __syncwarp();
+  if (A.sed[0]) sed_slow(A, sm, col, c2, A.P.nbins, 1, A.f.naero, A.f.maero, A.f.naerot, A.f.maerot, lane);
+  if (A.sed[1]) sed_slow(A, sm, col, c2, A.P.ncld, 2, A.f.ncloud, A.f.mcloud, A.f.ncloudt, A.f.mcloudt, lane);
+  if (fprc)
+    sed_fast(A, sm, col, A.P.nprc, A.nspec, 3, A.f.nprecp, A.f.mprecp, A.f.nprecpt, A.f.mprecpt, A.f.VtPrc, rr_s,
+             sr_s, lane);
+  if (fice)
+    sed_fast(A, sm, col, A.P.nice, A.nspec + 1, 4, A.f.nice, A.f.mice, A.f.nicet, A.f.micet, A.f.VtIce, ir_s,
+             sr_s + 1, lane);
+  __syncwarp();
+  for (int k = lane; k < nzp; k += 32) {
+    A.f.tlt[col + k] = tlt_s[k];
+    A.f.rrate[col + k] = rr_s[k];
+    if (A.lvl5) A.f.irate[col + k] = ir_s[k];
+  }
+  if (lane == 0) {
+    A.f.sfcrrate[c2] = sr_s[0];
+    if (A.lvl5) A.f.sfcirate[c2] = sr_s[1];
+  }
+}
+
 // every non-NULL pointer must be device (or managed) memory
 bool device_ptrs(std::initializer_list<const void *> ps) {
   for (const void *p : ps) {
@@ -459,6 +825,65 @@ int salsa_gb300_diagnostics(salsa_handle_t *h, int nzp, int nxp, int nyp, int on
   long long grid = (A.plane + 127) / 128;
   if (grid > (long long)nsm * 16) grid = (long long)nsm * 16;
   salsa::diagnostics_kernel<<<(int)grid, 128, 0, s>>>(A);
+  return cudaGetLastError() == cudaSuccess ? SALSA_OK : SALSA_E_CUDA;
+}
+
+int salsa_gb300_sedimentation(salsa_handle_t *h, int nzp, int nxp, int nyp, double dtlt, const int sed[4],
+                              const salsa_sedim_fields_t *f, void *stream) {
+  salsa::DevParams P;
+  cudaStream_t hs;
+  int dev = 0, nsm = 0;
+  if (!f || !sed || !salsa::handle_params(h, &P, &hs, &dev, &nsm)) return SALSA_E_ARG;
+  if (nzp < 3 || nxp < 5 || nyp < 5 || !(dtlt > 0.)) return SALSA_E_ARG;
+  const salsa_config_t *g = salsa::handle_config(h);
+  const bool lvl5 = g->level == 5;
+  const int s0 = sed[0] != 0, s1 = sed[1] != 0, s2 = sed[2] != 0, s3 = sed[3] != 0 && lvl5;
+  if (!f->tk || !f->th || !f->adn || !f->ustar || !f->dzt || !f->tlt || !f->rrate || !f->sfcrrate) return SALSA_E_ARG;
+  if (lvl5 && (!f->irate || !f->sfcirate)) return SALSA_E_ARG;
+  if ((s0 && (!f->naero || !f->maero || !f->naerot || !f->maerot)) ||
+      (s1 && (!f->ncloud || !f->mcloud || !f->ncloudt || !f->mcloudt)) ||
+      (s2 && (!f->nprecp || !f->mprecp || !f->nprecpt || !f->mprecpt || !f->VtPrc)) ||
+      (s3 && (!f->nice || !f->mice || !f->nicet || !f->micet || !f->VtIce)))
+    return SALSA_E_ARG;
+  if (!salsa::device_ptrs({f->naero, f->ncloud, f->nprecp, f->nice, f->maero, f->mcloud, f->mprecp, f->mice,
+                           f->naerot, f->ncloudt, f->nprecpt, f->nicet, f->maerot, f->mcloudt, f->mprecpt, f->micet,
+                           f->tk, f->th, f->adn, f->ustar, f->dzt, f->tlt, f->rrate, f->irate, f->sfcrrate,
+                           f->sfcirate, f->VtPrc, f->VtIce}))
+    return SALSA_E_ARG;
+  if (nzp > salsa::SED_KF || P.nwet < 2) return SALSA_E_UNSUPPORTED;
+  salsa::SedArgs A;
+  A.P = P;
+  A.plane = (long long)nzp * nxp * nyp;
+  A.nzp = nzp; A.nxp = nxp; A.nyp = nyp; A.nspec = P.nwet; A.lvl5 = lvl5;
+  A.sed[0] = s0; A.sed[1] = s1; A.sed[2] = s2; A.sed[3] = s3;
+  A.dtlt = dtlt;
+  A.f = *f;
+  // per-warp shared layout: tlt, rrate, irate columns, the slow carry (two rounds), the
+  // fast per-level arrays, the ice rime changes, the surface removal elements, two rates
+  const int nb_slow = std::max(s0 ? P.nbins : 0, s1 ? P.ncld : 0);
+  const int nb_fast = std::max(s2 ? P.nprc : 0, s3 ? P.nice : 0);
+  A.off_carry = 3 * nzp;
+  A.off_vc = A.off_carry + 2 * (P.nwet + 1) * nb_slow;
+  A.off_f1 = A.off_vc + nzp;
+  A.off_kf = A.off_f1 + nzp;
+  A.off_ws = A.off_kf + (nzp + 1) / 2;
+  A.off_rime = A.off_ws + nzp;
+  A.off_rem = A.off_rime + (s3 ? nzp * P.nice : 0);
+  A.off_sr = A.off_rem + 1 + 2 * nb_fast;
+  A.warp_doubles = A.off_sr + 2;
+  const size_t wbytes = (size_t)A.warp_doubles * sizeof(double);
+  int warps = 4;
+  while (warps > 1 && warps * wbytes > 160u * 1024u) warps >>= 1;
+  if (warps * wbytes > 200u * 1024u) return SALSA_E_UNSUPPORTED;
+  if (cudaSetDevice(dev) != cudaSuccess) return SALSA_E_NODEV;
+  const size_t smem = warps * wbytes;
+  if (smem > 48u * 1024u &&
+      cudaFuncSetAttribute(salsa::sedimentation_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return SALSA_E_CUDA;
+  cudaStream_t s = stream ? (cudaStream_t)stream : hs;
+  const long long cols = (long long)nxp * nyp, grid = (cols + warps - 1) / warps;
+  salsa::sedimentation_kernel<<<(unsigned)grid, 32 * warps, smem, s>>>(A);
   return cudaGetLastError() == cudaSuccess ? SALSA_OK : SALSA_E_CUDA;
 }
 

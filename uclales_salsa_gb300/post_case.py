@@ -1,11 +1,14 @@
-"""The LES-side constraints after a step (tend_constrain2 + SALSA_diagnostics) on a
-block of a workload, resident on the GPU (for timing and profiling).
+"""The LES-side routines around a step (tend_constrain2, SALSA_diagnostics and the
+bin sedimentation sedim_SALSA) on a block of a workload, resident on the GPU (for
+timing and profiling).
 
     python -m uclales_salsa_gb300.post_case --workload grid256x256x128 --X 128 --Y 128 --Z 64 --reps 3
 
 Runs one SALSA step to obtain tendencies, then times `reps` calls of each routine with
 CUDA events on one stream and prints their device times and the bytes each call reads
-and writes at least once (the values and tendencies it must inspect).
+and writes at least once (the values and tendencies it must inspect).  The
+sedimentation runs with all four parts on, level thickness 20 m, friction velocity
+0.3 m/s and dtlt = the step length.
 """
 import argparse
 import json
@@ -46,6 +49,60 @@ def post_bytes(a, level):
     return tc, dg
 
 
+SEDIM_PARTS = [("naero", "maero", "naerot", "maerot"), ("ncloud", "mcloud", "ncloudt", "mcloudt"),
+               ("nprecp", "mprecp", "nprecpt", "mprecpt"), ("nice", "mice", "nicet", "micet")]
+
+
+def sedim_arrays(inp, fields, outs, dz=20.0, ustar=0.3):
+    """SedimFields arrays from the fields and tendencies of a step (device tensors)."""
+    a = {}
+    for n, m, nt, mt in SEDIM_PARTS:
+        if n in fields and nt in outs:
+            a[n], a[m], a[nt], a[mt] = fields[n], fields[m], outs[nt], outs[mt]
+    t, p = fields["temp"], fields["press"]
+    tk = torch.where(t > 0, t, torch.full_like(t, 280.0))
+    pr = torch.where(p > 0, p, torch.full_like(p, 9.0e4))
+    a["tk"] = tk
+    a["adn"] = pr / (287.04 * tk)
+    a["th"] = tk * (1.0e5 / pr) ** (287.04 / 1005.0)
+    a["ustar"] = torch.full((inp.nyp, inp.nxp), ustar, dtype=torch.float64, device=t.device)
+    a["dzt"] = torch.full((inp.nzp,), 1.0 / dz, dtype=torch.float64, device=t.device)
+    a["tlt"] = torch.zeros_like(t)
+    for k in ("rrate", "irate"):
+        a[k] = torch.zeros_like(t)
+    for k in ("sfcrrate", "sfcirate"):
+        a[k] = torch.zeros_like(a["ustar"])
+    lay = inp.layout
+    a["VtPrc"] = torch.zeros((lay.nprc,) + tuple(t.shape), dtype=torch.float64, device=t.device)
+    if inp.level == 5:
+        a["VtIce"] = torch.zeros((lay.nice,) + tuple(t.shape), dtype=torch.float64, device=t.device)
+    return a
+
+
+def sedim_bytes(a):
+    """Bytes sedim_SALSA reads or writes at least once per call: the bin values, the
+    tendencies (read and written), tk, th, adn, tlt (read and written), the rates and
+    the fall speeds."""
+    b = lambda k: a[k].numel() * 8 if k in a else 0
+    tot = 0
+    for n, m, nt, mt in SEDIM_PARTS:
+        tot += b(n) + b(m) + 2 * (b(nt) + b(mt))
+    tot += b("tk") + b("th") + b("adn") + 2 * b("tlt") + b("rrate") + b("irate") + b("VtPrc") + b("VtIce")
+    return tot
+
+
+def time_sedim(step, inp, a, stream, reps, sed=(1, 1, 1, 1)):
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    with torch.cuda.stream(stream):
+        step.sedimentation(inp.nzp, inp.nxp, inp.nyp, inp.dt, sed, a, stream=stream)     # warm-up
+        ev[0].record(stream)
+        for _ in range(reps):
+            step.sedimentation(inp.nzp, inp.nxp, inp.nyp, inp.dt, sed, a, stream=stream)
+        ev[1].record(stream)
+    torch.cuda.synchronize()
+    return ev[0].elapsed_time(ev[1]) / reps
+
+
 def time_post(step, inp, a, stream, reps):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     with torch.cuda.stream(stream):
@@ -79,9 +136,13 @@ def main():
     s = torch.cuda.Stream()
     tc_ms, dg_ms = time_post(step, inp, a, s, a_.reps)
     tcb, dgb = post_bytes(a, inp.level)
+    sa = sedim_arrays(inp, fields, outs)
+    sd_ms = time_sedim(step, inp, sa, s, a_.reps)
+    sdb = sedim_bytes(sa)
     print(json.dumps({"workload": a_.workload, "points": inp.nzp * inp.nxp * inp.nyp,
-                      "tend_constrain_ms": tc_ms, "diagnostics_ms": dg_ms,
-                      "tend_constrain_gbs": tcb / tc_ms / 1e6, "diagnostics_gbs": dgb / dg_ms / 1e6}))
+                      "tend_constrain_ms": tc_ms, "diagnostics_ms": dg_ms, "sedimentation_ms": sd_ms,
+                      "tend_constrain_gbs": tcb / tc_ms / 1e6, "diagnostics_gbs": dgb / dg_ms / 1e6,
+                      "sedimentation_gbs": sdb / sd_ms / 1e6}))
     step.close()
 
 
