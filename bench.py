@@ -256,19 +256,29 @@ def peak_gbs():
 
 
 def post_bench(step, inp, fields, outs, stream, peak, reps=3):
-    """tend_constrain2 + SALSA_diagnostics over the whole grid after the timed steps
-    (fields and tendencies resident): device time per call and HBM roofline fraction of
-    the bytes each call must read or write."""
-    from uclales_salsa_gb300.post_case import post_arrays, post_bytes, time_post
+    """tend_constrain2, SALSA_diagnostics and sedim_SALSA over the whole grid after the
+    timed steps (fields and tendencies resident): device time per call and HBM roofline
+    fraction of the bytes each call must read or write.  The sedimentation is bound by
+    the FP64 pipe (fall speeds), not by HBM."""
+    from uclales_salsa_gb300.post_case import (post_arrays, post_bytes, time_post, sedim_arrays, sedim_bytes,
+                                               time_sedim)
     a = post_arrays(inp, fields, outs)
     tc_ms, dg_ms = time_post(step, inp, a, stream, reps)
     tcb, dgb = post_bytes(a, inp.level)
     del a
-    return {"what": "tend_constrain2 + SALSA_diagnostics (constrain_SALSA.f90) over the grid, fields in HBM",
-            "tend_constrain_ms": tc_ms, "diagnostics_ms": dg_ms,
+    sa = sedim_arrays(inp, fields, outs)
+    sd_ms = time_sedim(step, inp, sa, stream, reps)
+    sdb = sedim_bytes(sa)
+    del sa
+    return {"what": "tend_constrain2 + SALSA_diagnostics (constrain_SALSA.f90) and sedim_SALSA (mcrp.f90) over "
+                    "the grid, fields in HBM",
+            "tend_constrain_ms": tc_ms, "diagnostics_ms": dg_ms, "sedimentation_ms": sd_ms,
             "tend_constrain": {"bytes": tcb, "achieved_gbs": tcb / tc_ms / 1e6,
                                "frac": tcb / tc_ms / 1e6 / peak[0]},
             "diagnostics": {"bytes": dgb, "achieved_gbs": dgb / dg_ms / 1e6, "frac": dgb / dg_ms / 1e6 / peak[0]},
+            "sedimentation": {"bytes": sdb, "achieved_gbs": sdb / sd_ms / 1e6, "frac": sdb / sd_ms / 1e6 / peak[0],
+                              "bound": "fp64",
+                              "setup": "all four parts, 20 m levels, ustar 0.3 m/s, dtlt = step"},
             "peak_gbs": peak[0], "peak_source": peak[1]}
 
 

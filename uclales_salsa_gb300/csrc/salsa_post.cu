@@ -368,53 +368,48 @@ __global__ void __launch_bounds__(128) diagnostics_kernel(const PostArgs A) {
 }
 
 // ---- sedim_SALSA (src/src_LES/mcrp.f90:745-1275) ----
-// One warp per column, lane l on levels l, l+32, ... (0-based: level kc is the
-// reference's k = kc + 1).  Per column, in the reference's order:
-//   DepositionSlow (:926-1069) for the aerosol and then the cloud bins: the flux of
-//     level kc+1 comes from the next lane by a shuffle (from the round above through a
-//     shared carry at a round boundary), and the divergence is subtracted from the
-//     tendency in place;
-//   DepositionFast (:1073-1275) for precipitation and then ice: pass A gives each source
-//     level its fall speed and the level kf that its parcel reaches; pass B gathers, for
-//     every target level, the contributions of the sources above it in the order the
-//     reference adds them (sources from the top down, the removal of the level's own
-//     parcel before its own re-deposit), so each change is the reference's sum.
-// The sums over bins (rrate, tlt, the surface rates) are taken in the reference's index
-// order, including the range (ns-1)*nb:ns*nb of its water sums, which starts at the
-// last bin of the species before water.  Halo columns only get their rates and fall
-// speeds zeroed, as the reference's whole-array assignments do; the reference also adds
-// a zero change to their precipitation and ice tendencies, which leaves every value as
-// it is apart from the sign of a negative zero, and that is not repeated here.
+// One warp per column (0-based level kc is the reference's k = kc + 1).  The air
+// properties of every level are computed once per column into shared memory; then,
+// in the reference's order:
+//   DepositionSlow (:926-1069) for the aerosol and then the cloud bins.  Per bin, a
+//     ballot pass lists the levels whose number reaches the limit; the lanes take
+//     those levels for the fall speed (so a sparse bin costs only its populated
+//     levels), then the levels whose own or upper flux is non-zero for the flux
+//     divergence, which is subtracted from the tendency in place;
+//   DepositionFast (:1073-1275) for precipitation and then ice.  Per bin, pass A gives
+//     each populated source level its fall speed and the level kf its parcel reaches
+//     and marks the levels it changes; pass B gathers, for every marked level, the
+//     contributions of the sources in the order the reference adds them (sources from
+//     the top down, a level's removal of its own parcel before its re-deposit).
+// Levels and bins that the reference visits only to add a zero are skipped.  The sums
+// over bins (rrate, tlt, the surface rates) run in the reference's index order,
+// including the range (ns-1)*nb:ns*nb of its water sums, which starts at the last bin
+// of the species before water; the ice tlt sum adds the rime changes as one partial
+// sum after the water changes (the reference adds them one by one).  Quotients by a
+// density, by the number, by the diameter, by the level's air density and by dtlt are
+// taken as products with a reciprocal, which moves results by an ulp or so.  Halo
+// columns only get their rates and fall speeds zeroed, as the reference's whole-array
+// assignments do (its zero change to their tendencies is not repeated).
 constexpr double LES_ALVL = 2.5e+06, LES_ALVI = 2.834e+06, LES_CP = 1005., LES_G = 9.81, LES_KB = 1.3807e-23;
 constexpr double LES_PI = 3.14159265358979323846;   // defs.f90 pi (the SALSA pi6 stays truncated)
 constexpr double SED_M = 4.8096e-26, SED_A = 1.249, SED_B = 0.42, SED_C = 0.87;
 constexpr double EPS_REAL = 2.220446049250313e-16;   // epsilon(1.0) of the 8-byte default real
+constexpr double R_PI6 = 1. / K_PI6;
 constexpr int SED_KF = 0xffff, SED_BR = 1 << 16, SED_DEP = 1 << 17;   // pass-A code: kf | branch | deposited
 constexpr int SED_NS = SALSA_MAXSPEC + 2;   // species slots of a bin (wet species and rime)
+// per-warp shared arrays of nzp doubles
+enum { W_AD = 0, W_AVIS, W_LAM, W_ILAM, W_TLT, W_RR, W_IR, W_VC, W_P0, W_P1, W_P2, W_P3, W_N };
 
 struct SedArgs {
   DevParams P;                    // densities and ice shape parameters
   long long plane;
   int nzp, nxp, nyp, nspec, lvl5;
   int sed[4];
-  int off_carry, off_vc, off_f1, off_kf, off_ws, off_rime, off_rem, off_sr;   // shared layout (doubles)
-  int warp_doubles;
-  double dtlt;
+  int off_int, off_rem, off_sr, warp_doubles;   // per-warp shared layout (doubles)
+  double dtlt, rdtlt;
+  double rrholiq[9], rrhoice[9];  // reciprocal densities
   salsa_sedim_fields_t f;
 };
-
-struct SedAir { double avis, kvis, lambda; };
-
-// atm modelling eq. 4.54 (:986-989)
-__device__ __forceinline__ SedAir sed_air(double T, double ad) {
-  SedAir a;
-  const double x = T / 296.16;
-  a.avis = 1.8325e-5 * (416.16 / (T + 120.0)) * (x * sqrt(x));
-  a.kvis = a.avis / ad;
-  const double va = sqrt(8. * LES_KB * T / (LES_PI * SED_M));
-  a.lambda = 2. * a.avis / (ad * va);
-  return a;
-}
 
 // mo_ice_shape.f90:46-91 getDiameter (the maximum dimension of a non-spherical crystal)
 __device__ double ice_diameter(const DevParams &P, double mpri, double mrim, double numc) {
@@ -434,18 +429,20 @@ __device__ double ice_diameter(const DevParams &P, double mpri, double mrim, dou
   return res;
 }
 
-// fall speed of one bin (:999-1011 and :1148-1173): the wet diameter, the particle
-// density, the slip correction GG and terminal_vel; m holds the bin's ns masses
-__device__ __forceinline__ double sed_speed(const SedArgs &A, int flag, int ns, double n, const double (&m)[SED_NS],
-                                            double ad, const SedAir &air, double &dwet, double &GG) {
+// fall speed of one bin at one level (:999-1011, :1148-1173): wet diameter
+// (calcDiamLES), particle density, slip correction GG and terminal_vel
+__device__ __forceinline__ double sed_vel(const SedArgs &A, int flag, int ns, double n, const double (&m)[SED_NS],
+                                          double ad, double avis, double lam, double ilam, double &dwet, double &GG) {
   double v = 0., sm = 0.;
 #pragma unroll
   for (int s = 0; s < SED_NS; s++)
     if (s < ns) {
-      v += m[s] / (flag == 4 ? A.P.rhoice[s] : A.P.rholiq[s]);
+      v += m[s] * (flag == 4 ? A.rrhoice[s] : A.rrholiq[s]);
       sm += m[s];
     }
-  dwet = n < 1.e-15 ? 0. : cbrt(v / n / K_PI6);   // calcDiamLES, spherical
+  const double rn = 1. / n;
+  dwet = n < 1.e-15 ? 0. : cbrt(v * rn * R_PI6);
+  const double rd = 1. / dwet;
   Shape<double> sh{0., 0., 0., 0.};
   double dnsp = 0.;
   if (flag == 4) {
@@ -458,162 +455,201 @@ __device__ __forceinline__ double sed_speed(const SedArgs &A, int flag, int ns, 
     dnsp = n < 1.e-15 ? 0. : ice_diameter(A.P, mp, mr, n);   // calcDiamLES, non-spherical
     shape_coeffs<double>(A.P, sh, mp, mr, n);
   }
-  const double zdn = sm / n / (K_PI6 * cube(dwet));
-  const double Kn = 2. * air.lambda / dwet;
-  GG = 1. + Kn * (SED_A + SED_B * exp(-SED_C / Kn));
-  return terminal_vel<double>(dwet, zdn, ad, air.avis, GG, flag, sh, dnsp);
+  const double zdn = sm * rn * (rd * rd * rd) * R_PI6;
+  const double Kn = 2. * lam * rd;                            // 2 lambda / dwet
+  GG = 1. + Kn * (SED_A + SED_B * exp(-SED_C * 0.5 * dwet * ilam));
+  return terminal_vel<double>(dwet, zdn, ad, avis, GG, flag, sh, dnsp);
+}
+
+__device__ __forceinline__ bool act_bit(const unsigned *w, int k) { return (w[k >> 5] >> (k & 31)) & 1u; }
+__device__ __forceinline__ unsigned lanes_below(int lane) { return (1u << lane) - 1u; }
+
+// one bin: activity bits of the levels 1..nzp-2 (a number that is not below the limit)
+// and the ascending list of the active levels; zeroes the fall speed of the others
+__device__ int sed_activity(int nzp, const double *ncol, double clim, unsigned *actw, int *la, double *vt, int lane) {
+  const int R = (nzp + 31) >> 5;
+  int cnt = 0;
+  for (int r = 0; r < R; r++) {
+    const int kc = r * 32 + lane;
+    const bool inr = kc >= 1 && kc <= nzp - 2;
+    const bool act = inr && !(ncol[kc] < clim);
+    const unsigned w = __ballot_sync(0xffffffffu, act);
+    if (lane == 0) actw[r] = w;
+    if (act) la[cnt + __popc(w & lanes_below(lane))] = kc;
+    if (vt && !act && kc < nzp) vt[kc] = 0.;
+    cnt += __popc(w);
+  }
+  __syncwarp();
+  return cnt;
 }
 
 // DepositionSlow for one part of one column, with sedim_SALSA's tendency and tlt
 // updates (:799-843)
-__device__ void sed_slow(const SedArgs &A, double *sm, long long col, long long c2, int nb, int flag,
-                         const double *numc, const double *mass, double *tn, double *tm, int lane) {
-  const int nzp = A.nzp, ns = A.nspec, R = (nzp + 31) >> 5, cw = (ns + 1) * nb;
-  const long long pl = A.plane;
-  double *tlt_s = sm, *rr_s = sm + nzp, *carry = sm + A.off_carry, *sr_s = sm + A.off_sr;
-  for (int e = lane; e < 2 * cw; e += 32) carry[e] = 0.;
-  __syncwarp();
-  for (int r = R - 1; r >= 0; r--) {
-    const int kc = r * 32 + lane;
-    const bool inr = kc >= 1 && kc <= nzp - 2;
-    const long long p = col + kc;
-    double ad = 1., adp = 1., dz = 0., T = 0.;
-    SedAir air{0., 0., 0.};
-    if (inr) {
-      T = A.f.tk[p];
-      ad = A.f.adn[p];
-      adp = A.f.adn[p + 1];
-      dz = A.f.dzt[kc];
-      air = sed_air(T, ad);
-    }
-    const double *cin = carry + ((r + 1) & 1) * cw;
-    double *cout = carry + (r & 1) * cw;
-    double rsum = 0., tsum = 0., wl_r = 0., wl_d = 0.;
-    for (int bi = 0; bi < nb; bi++) {
-      const int b = bi == 0 ? nb - 1 : bi - 1;   // the last bin first: it opens the water sum
-      const double n = inr ? numc[p + pl * b] : 0.;
-      const bool act = inr && n >= K_NLIM;
+__device__ void sed_slow(const SedArgs &A, double *sm, const double *blk, long long col, long long c2, int nb,
+                         int flag, const double *numc, const double *mass, double *tn, double *tm, int lane) {
+  const int nzp = A.nzp, ns = A.nspec, R = (nzp + 31) >> 5;
+  const long long pl = A.plane, ps = pl * nb;
+  const double *ad_s = sm + W_AD * nzp, *avis_s = sm + W_AVIS * nzp, *lam_s = sm + W_LAM * nzp,
+               *ilam_s = sm + W_ILAM * nzp;
+  double *tlt_s = sm + W_TLT * nzp, *rr_s = sm + W_RR * nzp, *vc_s = sm + W_VC * nzp;
+  double *rs_s = sm + W_P0 * nzp, *ts_s = sm + W_P1 * nzp, *wr_s = sm + W_P2 * nzp, *wd_s = sm + W_P3 * nzp;
+  int *la = (int *)(sm + A.off_int), *lf = la + nzp;
+  unsigned *actw = (unsigned *)(lf + nzp);
+  double *sr_s = sm + A.off_sr;
+  const double *dzt_b = blk, *vmax_b = blk + 2 * nzp;
+  for (int e = lane; e < nzp; e += 32) rs_s[e] = ts_s[e] = wr_s[e] = wd_s[e] = 0.;
+  for (int bi = 0; bi < nb; bi++) {
+    const int b = bi == 0 ? nb - 1 : bi - 1;   // the last bin first: it opens the water sum
+    const double *ncol = numc + col + pl * b, *mcol = mass + col + pl * b;
+    const int na = sed_activity(nzp, ncol, K_NLIM, actw, la, nullptr, lane);
+    if (na == 0) continue;   // no flux anywhere in the column
+    // fall speeds of the populated levels (:990-1028)
+    for (int i = lane; i < ((na + 31) & ~31); i += 32) {
+      if (i >= na) continue;
+      const int k = la[i];
+      const double n = ncol[k];
       double m[SED_NS];
 #pragma unroll
-      for (int s = 0; s < SED_NS; s++) m[s] = (act && s < ns) ? mass[p + pl * ((long long)s * nb + b)] : 0.;
-      double vc = 0.;
-      if (act) {
-        double dwet, GG;
-        vc = sed_speed(A, flag, ns, n, m, ad, air, dwet, GG);
-        vc = fmin(vc, fmin(0.5 * (1. / dz) / A.dtlt, 2.0));
-        if (kc == 1) {   // the level just above the surface (:1020-1028)
-          const double us = A.f.ustar[c2];
-          const double mdiff = (LES_KB * T * GG) / (3.0 * LES_PI * air.avis * dwet);
-          const double Sc = air.kvis / mdiff;
-          double St = vc * (us * us) / LES_G * air.kvis;
-          if (St < 0.01) St = 0.01;
-          const double rt = 1.0 / fmax(EPS_REAL, (us * (pow(Sc, -2.0 / 3.0) + pow(10., -3.0 / St))));
-          vc = (1. / rt) + vc;
-        }
+      for (int s = 0; s < SED_NS; s++) m[s] = s < ns ? mcol[k + ps * s] : 0.;
+      double dwet, GG;
+      double vc = sed_vel(A, flag, ns, n, m, ad_s[k], avis_s[k], lam_s[k], ilam_s[k], dwet, GG);
+      vc = fmin(vc, vmax_b[k]);
+      if (k == 1) {   // the level just above the surface (:1020-1028)
+        const double T = A.f.tk[col + 1], us = A.f.ustar[c2], avis = avis_s[1];
+        const double kvis = avis / ad_s[1];
+        const double mdiff = (LES_KB * T * GG) / (3.0 * LES_PI * avis * dwet);
+        const double Sc = kvis / mdiff;
+        double St = vc * (us * us) / LES_G * kvis;
+        if (St < 0.01) St = 0.01;
+        const double rt = 1.0 / fmax(EPS_REAL, (us * (pow(Sc, -2.0 / 3.0) + pow(10., -3.0 / St))));
+        vc = (1. / rt) + vc;
       }
-      // number flux, then the species in mass-index order
+      vc_s[k] = vc;
+    }
+    // the levels with a non-zero divergence: own or upper level populated
+    int nf = 0;
+    for (int r = 0; r < R; r++) {
+      const int kc = r * 32 + lane;
+      const bool f = kc >= 1 && kc <= nzp - 2 && (act_bit(actw, kc) || act_bit(actw, kc + 1));
+      const unsigned w = __ballot_sync(0xffffffffu, f);
+      if (f) lf[nf + __popc(w & lanes_below(lane))] = kc;
+      nf += __popc(w);
+    }
+    __syncwarp();
+    // flux divergence (:1040-1048), number then the species in mass-index order
+    for (int i = lane; i < ((nf + 31) & ~31); i += 32) {
+      if (i >= nf) continue;
+      const int k = lf[i];
+      const bool a0 = act_bit(actw, k), a1 = act_bit(actw, k + 1);
+      const double v0 = a0 ? vc_s[k] : 0., v1 = a1 ? vc_s[k + 1] : 0.;
+      const double ad = ad_s[k], adp = ad_s[k + 1], q = dzt_b[k] / ad;
 #pragma unroll
       for (int s = -1; s < SED_NS; s++) {
         if (s >= ns) continue;
-        const double q = s < 0 ? n : m[s < 0 ? 0 : s];
-        const double rf = act ? -q * vc : 0.;
-        double up = __shfl_down_sync(0xffffffffu, rf, 1);
-        const int ci = b * (ns + 1) + (s + 1);
-        if (lane == 31) up = cin[ci];
-        if (lane == 0) cout[ci] = rf;
-        const double d = inr ? (up * adp - rf * ad) * dz / ad : 0.;
-        if (inr) {
-          double *t = s < 0 ? tn + p + pl * b : tm + p + pl * ((long long)s * nb + b);
-          *t = *t - d;
-        }
-        if (s == ns - 2 && bi == 0) rsum = 0. + rf;   // rflm(k,(ns-1)*nb) opens the sum
+        const double *src = s < 0 ? ncol : mcol + ps * s;
+        const double rf0 = a0 ? -src[k] * v0 : 0., rf1 = a1 ? -src[k + 1] * v1 : 0.;
+        const double d = (rf1 * adp - rf0 * ad) * q;
+        double *t = s < 0 ? tn + col + pl * b + k : tm + col + pl * b + ps * s + k;
+        *t = *t - d;
+        if (s == ns - 2 && bi == 0) rs_s[k] = 0. + rf0;   // rflm(k,(ns-1)*nb) opens the sum
         if (s == ns - 1) {
-          if (bi == 0) { wl_r = rf; wl_d = d; }
-          else { rsum += rf; tsum += d; }
+          if (bi == 0) { wr_s[k] = rf0; wd_s[k] = d; }
+          else { rs_s[k] += rf0; ts_s[k] += d; }
         }
       }
     }
-    rsum += wl_r;
-    tsum += wl_d;
-    if (inr) {
-      rr_s[kc] = rr_s[kc] - rsum * ad * LES_ALVL;
-      if (kc == 1) sr_s[0] = sr_s[0] - rsum * ad * LES_ALVL;
-    }
-    if (kc >= 1 && kc <= nzp - 1) tlt_s[kc] = tlt_s[kc] + tsum * (LES_ALVL / LES_CP) * A.f.th[p] / A.f.tk[p];
     __syncwarp();
   }
+  for (int r = 0; r < R; r++) {
+    const int kc = r * 32 + lane;
+    if (kc < 1 || kc > nzp - 1) continue;
+    if (kc <= nzp - 2) {
+      const double rsum = rs_s[kc] + wr_s[kc];
+      rr_s[kc] = rr_s[kc] - rsum * ad_s[kc] * LES_ALVL;
+      if (kc == 1) sr_s[0] = sr_s[0] - rsum * ad_s[kc] * LES_ALVL;
+    }
+    const double tsum = ts_s[kc] + wd_s[kc];
+    tlt_s[kc] = tlt_s[kc] + tsum * (LES_ALVL / LES_CP) * A.f.th[col + kc] / A.f.tk[col + kc];
+  }
+  __syncwarp();
 }
 
 // DepositionFast for one part of one column, with sedim_SALSA's tendency and tlt
 // updates (:847-905)
-__device__ void sed_fast(const SedArgs &A, double *sm, long long col, int nb, int ns, int flag, const double *numc,
-                         const double *mass, double *tn, double *tm, double *Vt, double *rate_s, double *srate_s,
-                         int lane) {
+__device__ void sed_fast(const SedArgs &A, double *sm, const double *blk, long long col, int nb, int ns, int flag,
+                         const double *numc, const double *mass, double *tn, double *tm, double *Vt, double *rate_s,
+                         double *srate_s, int lane) {
   const int nzp = A.nzp, R = (nzp + 31) >> 5;
-  const long long pl = A.plane;
+  const long long pl = A.plane, ps = pl * nb;
   const double alv = flag == 4 ? LES_ALVI : LES_ALVL;
   const int iw = flag == 4 ? ns - 2 : ns - 1;   // water; for ice the rime follows it
-  double *tlt_s = sm, *vc_s = sm + A.off_vc, *f1_s = sm + A.off_f1, *ws_s = sm + A.off_ws, *rime_s = sm + A.off_rime,
-         *rem_s = sm + A.off_rem;
-  int *kf_s = (int *)(sm + A.off_kf);
-  const double *dzt = A.f.dzt;
-  for (int e = lane; e < nzp; e += 32) ws_s[e] = 0.;
+  const double *ad_s = sm + W_AD * nzp, *avis_s = sm + W_AVIS * nzp, *lam_s = sm + W_LAM * nzp,
+               *ilam_s = sm + W_ILAM * nzp;
+  double *tlt_s = sm + W_TLT * nzp, *vc_s = sm + W_VC * nzp, *f1_s = sm + W_P0 * nzp, *ws_s = sm + W_P2 * nzp,
+         *wq_s = sm + W_P3 * nzp;
+  int *kf_s = (int *)(sm + W_P1 * nzp), *tg_s = kf_s + nzp;
+  int *la = (int *)(sm + A.off_int), *lt = la + nzp;
+  unsigned *actw = (unsigned *)(lt + nzp);
+  double *rem_s = sm + A.off_rem;
+  const double *dzt_b = blk, *dzl_b = blk + nzp;
+  for (int e = lane; e < nzp; e += 32) ws_s[e] = wq_s[e] = 0.;
+  for (int e = lane; e < 1 + 2 * nb; e += 32) rem_s[e] = 0.;
   for (int b = 0; b < nb; b++) {
-    // pass A: fall speed and destination of each source level (:1140-1216)
+    const double *ncol = numc + col + pl * b, *mcol = mass + col + pl * b;
+    double *vt = Vt + col + pl * b;
+    const int na = sed_activity(nzp, ncol, K_PRLIM, actw, la, vt, lane);
+    if (na == 0) continue;
+    for (int e = lane; e < nzp; e += 32) tg_s[e] = 0;
+    __syncwarp();
+    // pass A: fall speed and destination of each populated source level (:1140-1216)
     int span = -1;
-    for (int r = 0; r < R; r++) {
-      const int kc = r * 32 + lane;
-      const bool inr = kc >= 1 && kc <= nzp - 2;
-      const long long p = col + kc;
-      const double n = inr ? numc[p + pl * b] : 0.;
-      const bool act = inr && n >= K_PRLIM;
-      double vc = 0.;
-      int code = -1;
-      if (act) {
-        double m[SED_NS];
+    for (int i = lane; i < ((na + 31) & ~31); i += 32) {
+      if (i >= na) continue;
+      const int kc = la[i];
+      const double n = ncol[kc];
+      double m[SED_NS];
 #pragma unroll
-        for (int s = 0; s < SED_NS; s++) m[s] = s < ns ? mass[p + pl * ((long long)s * nb + b)] : 0.;
-        const double ad = A.f.adn[p];
-        const SedAir air = sed_air(A.f.tk[p], ad);
-        double dwet, GG;
-        vc = sed_speed(A, flag, ns, n, m, ad, air, dwet, GG);
-        const double fdmax = A.dtlt * vc;
-        double fd = 0.;
-        int fi = 0;
-        bool dep = false;
-        while (fd < fdmax) {   // at most kc passes
-          fd = fd + (1. / dzt[kc - fi]);
-          fi = fi + 1;
-          if (kc - fi <= 0) { dep = true; break; }
-        }
-        fi = fi - 1;
-        const int kf = kc - fi;
-        fd = fd - (1. / dzt[kf]);
-        const double fdos = fmin(fmax(fdmax - fd, 0.), 1. / dzt[kf]);
-        const double f1 = fdos * dzt[kf];
-        code = kf | (f1 > 0.5 ? SED_BR : 0) | (dep ? SED_DEP : 0);
-        vc_s[kc] = vc;
-        f1_s[kc] = f1;
-        span = max(span, kc - kf);
-        double mw = 0.;
-#pragma unroll
-        for (int s = 0; s < SED_NS; s++) if (s == iw) mw = m[s];
-        if (flag == 4) {
-          double mr = 0.;
-#pragma unroll
-          for (int s = 0; s < SED_NS; s++) if (s == ns - 1) mr = m[s];
-          mw = mw + mr;
-        }
-        rate_s[kc] = rate_s[kc] + mw * ad * vc * alv;
+      for (int s = 0; s < SED_NS; s++) m[s] = s < ns ? mcol[kc + ps * s] : 0.;
+      const double ad = ad_s[kc];
+      double dwet, GG;
+      const double vc = sed_vel(A, flag, ns, n, m, ad, avis_s[kc], lam_s[kc], ilam_s[kc], dwet, GG);
+      vt[kc] = vc;
+      const double fdmax = A.dtlt * vc;
+      double fd = 0.;
+      int fi = 0;
+      bool dep = false;
+      while (fd < fdmax) {   // at most kc passes
+        fd = fd + dzl_b[kc - fi];
+        fi = fi + 1;
+        if (kc - fi <= 0) { dep = true; break; }
       }
-      if (kc < nzp) {
-        kf_s[kc] = code;
-        Vt[p + pl * b] = vc;
+      fi = fi - 1;
+      const int kf = kc - fi;
+      fd = fd - dzl_b[kf];
+      const double fdos = fmin(fmax(fdmax - fd, 0.), dzl_b[kf]);
+      const double f1 = fdos * dzt_b[kf];
+      const bool br = f1 > 0.5;
+      kf_s[kc] = kf | (br ? SED_BR : 0) | (dep ? SED_DEP : 0);
+      f1_s[kc] = f1;
+      vc_s[kc] = vc;
+      tg_s[kc] = 1;
+      tg_s[kf - 1] = 1;
+      if (!br) tg_s[kf] = 1;
+      span = max(span, kc - kf);
+      double mw = 0.;
+#pragma unroll
+      for (int s = 0; s < SED_NS; s++) if (s == iw) mw = m[s];
+      if (flag == 4) {
+        double mr = 0.;
+#pragma unroll
+        for (int s = 0; s < SED_NS; s++) if (s == ns - 1) mr = m[s];
+        mw = mw + mr;
       }
+      rate_s[kc] = rate_s[kc] + mw * ad * vc * alv;
     }
     const int F = __reduce_max_sync(0xffffffffu, span);
     __syncwarp();
-    // removal statistics of the parcels that reach the surface (:1197-1202): the
+    // removal statistics of the parcels that reach the surface (:1197-1202), for the
     // elements that the surface rate sums
     if (lane < 3) {
       int s = -1, pos = 0;
@@ -622,40 +658,51 @@ __device__ void sed_fast(const SedArgs &A, double *sm, long long col, int nb, in
       if (lane == 2 && flag == 4) { s = ns - 1; pos = 1 + nb + b; }
       if (s >= 0) {
         double acc = 0.;
-        for (int kc = nzp - 2; kc >= 1; kc--) {
-          const int code = kf_s[kc];
-          if (code >= 0 && (code & SED_DEP)) acc = acc + mass[col + kc + pl * ((long long)s * nb + b)] * A.f.adn[col + kc] * vc_s[kc];
+        for (int i = na - 1; i >= 0; i--) {
+          const int kc = la[i];
+          if (kf_s[kc] & SED_DEP) acc = acc + mcol[kc + ps * s] * ad_s[kc] * vc_s[kc];
         }
         rem_s[pos] = acc;
       }
     }
-    // pass B: each target level gathers its change (:1218-1250), number then species
-    for (int s = -1; s < ns; s++) {
-      const double *src = s < 0 ? numc + col + pl * b : mass + col + pl * ((long long)s * nb + b);
-      double *dst = s < 0 ? tn + col + pl * b : tm + col + pl * ((long long)s * nb + b);
-      for (int r = 0; r < R; r++) {
-        const int L = r * 32 + lane;
-        if (L >= nzp) continue;
+    // the levels that change
+    int nt = 0;
+    for (int r = 0; r < R; r++) {
+      const int L = r * 32 + lane;
+      const bool t = L < nzp && tg_s[L];
+      const unsigned w = __ballot_sync(0xffffffffu, t);
+      if (t) lt[nt + __popc(w & lanes_below(lane))] = L;
+      nt += __popc(w);
+    }
+    __syncwarp();
+    // pass B: each changed level gathers its change (:1218-1250), number then species
+    for (int i = lane; i < ((nt + 31) & ~31); i += 32) {
+      if (i >= nt) continue;
+      const int L = lt[i];
+      const int k0 = min(nzp - 2, L + 1 + F), k1 = max(1, L - 1);
+#pragma unroll 1
+      for (int s = -1; s < ns; s++) {
+        const double *src = s < 0 ? ncol : mcol + ps * s;
         double acc = 0.;
-        const int k0 = min(nzp - 2, L + 1 + F), k1 = max(1, L - 1);
         for (int k = k0; k >= k1; k--) {
+          if (!act_bit(actw, k)) continue;
           const int code = kf_s[k];
-          if (code < 0) continue;
           const int kf = code & SED_KF;
           if (k != L && kf - 1 != L && kf != L) continue;
           const double v = src[k];
           if (k == L) acc = acc - v;
           if (kf - 1 == L) {
-            if (code & SED_BR) acc = acc + v * dzt[kf - 1] / dzt[k];
-            else acc = acc + (f1_s[k] * v) * dzt[kf - 1] / dzt[kf];
+            if (code & SED_BR) acc = acc + v * dzt_b[kf - 1] / dzt_b[k];
+            else acc = acc + (f1_s[k] * v) * dzt_b[kf - 1] / dzt_b[kf];
           } else if (kf == L && !(code & SED_BR)) {
             acc = acc + (1. - f1_s[k]) * v;
           }
         }
         const double val = 0. + acc;
-        dst[L] = dst[L] + val / A.dtlt;
+        double *t = s < 0 ? tn + col + pl * b + L : tm + col + pl * b + ps * s + L;
+        *t = *t + val * A.rdtlt;
         if (s == iw) ws_s[L] += val;
-        if (flag == 4 && s == ns - 1) rime_s[L * nb + b] = val;
+        if (flag == 4 && s == ns - 1) wq_s[L] += val;
       }
     }
     __syncwarp();
@@ -670,21 +717,27 @@ __device__ void sed_fast(const SedArgs &A, double *sm, long long col, int nb, in
   for (int r = 0; r < R; r++) {
     const int L = r * 32 + lane;
     if (L > nzp - 2) continue;
-    double S = ws_s[L];
-    if (flag == 4)
-      for (int b = 0; b < nb; b++) S += rime_s[L * nb + b];
-    const long long p = col + L;
-    tlt_s[L] = tlt_s[L] - (S / A.dtlt) * (alv / LES_CP) * A.f.th[p] / A.f.tk[p];
+    const double S = flag == 4 ? ws_s[L] + wq_s[L] : ws_s[L];
+    tlt_s[L] = tlt_s[L] - (S * A.rdtlt) * (alv / LES_CP) * A.f.th[col + L] / A.f.tk[col + L];
   }
   __syncwarp();
 }
 
 __global__ void __launch_bounds__(128) sedimentation_kernel(const SedArgs A) {
   extern __shared__ double sed_smem[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nzp = A.nzp;
+  // per block: dzt, 1/dzt and the slow fall-speed cap 0.5*(1/dzt)/dtlt (at most 2 m/s)
+  double *blk = sed_smem;
+  for (int k = threadIdx.x; k < nzp; k += blockDim.x) {
+    const double dz = A.f.dzt[k], dzl = 1. / dz;
+    blk[k] = dz;
+    blk[nzp + k] = dzl;
+    blk[2 * nzp + k] = fmin(0.5 * dzl / A.dtlt, 2.0);
+  }
+  __syncthreads();
   const long long c2 = (long long)blockIdx.x * (blockDim.x >> 5) + wib;   // column i + nxp*j
   if (c2 >= (long long)A.nxp * A.nyp) return;
-  const int i = (int)(c2 % A.nxp), j = (int)(c2 / A.nxp), nzp = A.nzp;
+  const int i = (int)(c2 % A.nxp), j = (int)(c2 / A.nxp);
   const long long col = (long long)nzp * c2, pl = A.plane;
   const bool fprc = A.sed[2], fice = A.sed[3] && A.lvl5;
   if (i < 2 || i > A.nxp - 3 || j < 2 || j > A.nyp - 3) {   // halo: the whole-array zeroing only
@@ -700,24 +753,39 @@ __global__ void __launch_bounds__(128) sedimentation_kernel(const SedArgs A) {
     }
     return;
   }
-  double *sm = sed_smem + (size_t)wib * A.warp_doubles;
-  double *tlt_s = sm, *rr_s = sm + nzp, *ir_s = sm + 2 * nzp, *sr_s = sm + A.off_sr;
+  double *sm = sed_smem + 3 * nzp + (size_t)wib * A.warp_doubles;
+  double *ad_s = sm + W_AD * nzp, *avis_s = sm + W_AVIS * nzp, *lam_s = sm + W_LAM * nzp, *ilam_s = sm + W_ILAM * nzp;
+  double *tlt_s = sm + W_TLT * nzp, *rr_s = sm + W_RR * nzp, *ir_s = sm + W_IR * nzp, *sr_s = sm + A.off_sr;
+  // air properties per level, atm modelling eq. 4.54 (:986-989)
   for (int k = lane; k < nzp; k += 32) {
-    tlt_s[k] = A.f.tlt[col + k];
+    const long long p = col + k;
+    const double ad = A.f.adn[p];
+    ad_s[k] = ad;
+    double avis = 0., lam = 0., ilam = 0.;
+    if (k >= 1 && k <= nzp - 2) {
+      const double T = A.f.tk[p], x = T / 296.16;
+      avis = 1.8325e-5 * (416.16 / (T + 120.0)) * (x * sqrt(x));
+      const double va = sqrt(8. * LES_KB * T / (LES_PI * SED_M));
+      lam = 2. * avis / (ad * va);
+      ilam = 1. / lam;
+    }
+    avis_s[k] = avis;
+    lam_s[k] = lam;
+    ilam_s[k] = ilam;
+    tlt_s[k] = A.f.tlt[p];
     rr_s[k] = 0.;
     ir_s[k] = 0.;
   }
   if (lane == 0) sr_s[0] = sr_s[1] = 0.;
   __syncwarp();
-  if (A.sed[0]) sed_slow(A, sm, col, c2, A.P.nbins, 1, A.f.naero, A.f.maero, A.f.naerot, A.f.maerot, lane);
-  if (A.sed[1]) sed_slow(A, sm, col, c2, A.P.ncld, 2, A.f.ncloud, A.f.mcloud, A.f.ncloudt, A.f.mcloudt, lane);
+  if (A.sed[0]) sed_slow(A, sm, blk, col, c2, A.P.nbins, 1, A.f.naero, A.f.maero, A.f.naerot, A.f.maerot, lane);
+  if (A.sed[1]) sed_slow(A, sm, blk, col, c2, A.P.ncld, 2, A.f.ncloud, A.f.mcloud, A.f.ncloudt, A.f.mcloudt, lane);
   if (fprc)
-    sed_fast(A, sm, col, A.P.nprc, A.nspec, 3, A.f.nprecp, A.f.mprecp, A.f.nprecpt, A.f.mprecpt, A.f.VtPrc, rr_s,
-             sr_s, lane);
+    sed_fast(A, sm, blk, col, A.P.nprc, A.nspec, 3, A.f.nprecp, A.f.mprecp, A.f.nprecpt, A.f.mprecpt, A.f.VtPrc,
+             rr_s, sr_s, lane);
   if (fice)
-    sed_fast(A, sm, col, A.P.nice, A.nspec + 1, 4, A.f.nice, A.f.mice, A.f.nicet, A.f.micet, A.f.VtIce, ir_s,
+    sed_fast(A, sm, blk, col, A.P.nice, A.nspec + 1, 4, A.f.nice, A.f.mice, A.f.nicet, A.f.micet, A.f.VtIce, ir_s,
              sr_s + 1, lane);
-  __syncwarp();
   for (int k = lane; k < nzp; k += 32) {
     A.f.tlt[col + k] = tlt_s[k];
     A.f.rrate[col + k] = rr_s[k];
@@ -857,26 +925,27 @@ int salsa_gb300_sedimentation(salsa_handle_t *h, int nzp, int nxp, int nyp, doub
   A.nzp = nzp; A.nxp = nxp; A.nyp = nyp; A.nspec = P.nwet; A.lvl5 = lvl5;
   A.sed[0] = s0; A.sed[1] = s1; A.sed[2] = s2; A.sed[3] = s3;
   A.dtlt = dtlt;
+  A.rdtlt = 1. / dtlt;
+  for (int s = 0; s < 9; s++) {
+    A.rrholiq[s] = P.rholiq[s] > 0. ? 1. / P.rholiq[s] : 0.;
+    A.rrhoice[s] = P.rhoice[s] > 0. ? 1. / P.rhoice[s] : 0.;
+  }
   A.f = *f;
-  // per-warp shared layout: tlt, rrate, irate columns, the slow carry (two rounds), the
-  // fast per-level arrays, the ice rime changes, the surface removal elements, two rates
-  const int nb_slow = std::max(s0 ? P.nbins : 0, s1 ? P.ncld : 0);
+  // shared layout: per block dzt, 1/dzt and the slow cap (3 nzp doubles); per warp the
+  // per-level arrays (W_N nzp doubles), three int arrays (two level lists of nzp and
+  // the activity words), the surface removal elements and the two surface rates
   const int nb_fast = std::max(s2 ? P.nprc : 0, s3 ? P.nice : 0);
-  A.off_carry = 3 * nzp;
-  A.off_vc = A.off_carry + 2 * (P.nwet + 1) * nb_slow;
-  A.off_f1 = A.off_vc + nzp;
-  A.off_kf = A.off_f1 + nzp;
-  A.off_ws = A.off_kf + (nzp + 1) / 2;
-  A.off_rime = A.off_ws + nzp;
-  A.off_rem = A.off_rime + (s3 ? nzp * P.nice : 0);
+  const int R = (nzp + 31) / 32;
+  A.off_int = salsa::W_N * nzp;
+  A.off_rem = A.off_int + (2 * nzp + R + 1) / 2;
   A.off_sr = A.off_rem + 1 + 2 * nb_fast;
   A.warp_doubles = A.off_sr + 2;
-  const size_t wbytes = (size_t)A.warp_doubles * sizeof(double);
+  const size_t wbytes = (size_t)A.warp_doubles * sizeof(double), bbytes = (size_t)3 * nzp * sizeof(double);
   int warps = 4;
-  while (warps > 1 && warps * wbytes > 160u * 1024u) warps >>= 1;
-  if (warps * wbytes > 200u * 1024u) return SALSA_E_UNSUPPORTED;
+  while (warps > 1 && bbytes + warps * wbytes > 100u * 1024u) warps >>= 1;
+  const size_t smem = bbytes + warps * wbytes;
+  if (smem > 200u * 1024u) return SALSA_E_UNSUPPORTED;
   if (cudaSetDevice(dev) != cudaSuccess) return SALSA_E_NODEV;
-  const size_t smem = warps * wbytes;
   if (smem > 48u * 1024u &&
       cudaFuncSetAttribute(salsa::sedimentation_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
