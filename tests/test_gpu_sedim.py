@@ -1,8 +1,8 @@
 """sedim_SALSA on the GPU (salsa_gb300_sedimentation) against the oracle on the same
-states.  The kernel takes the reference's operations in the reference's order; the
-wet diameter (pow(x, 1/3) against cbrt), the viscosity's (T/296.16)**1.5 and the fall
-speed's exp/log come from other libraries, so values agree to a few ulps, and the
-tests hold every output to 1e-10 of its change."""
+states.  The kernel follows the reference's steps and summation orders; it takes some
+quotients as products with reciprocals, contracts products and sums to fused
+multiply-adds and uses cbrt and the device exp/log/pow, so values agree to a few ulps,
+and the tests hold every output to 1e-10 of its change."""
 import pytest
 import torch
 
