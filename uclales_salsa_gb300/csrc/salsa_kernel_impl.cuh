@@ -1856,13 +1856,20 @@ __device__ __constant__ double c_gl_w[10] = {0.066667031481273176, 0.14945422671
                                              0.26926671836765848,  0.21908574324601154, 0.14945422671662059,
                                              0.066667031481273176};
 
+// Products that must not fuse with a following add: the freezing rates below take
+// exp(-crit/kT) of terms that cancel (het_sf), so a fused rounding there moves the
+// frozen fraction far more than any input rounding does.  The rest of the FP64 form
+// contracts multiply-adds.
+__device__ __forceinline__ double mrn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double cube_rn(double x) { return __dmul_rn(__dmul_rn(x, x), x); }
+
 __device__ double erfm1(double x) {   // math_functions.f90:494-510
   const double a = 0.140012;
   double sgn = x < 0. ? -1. : 1.;
   double xx = fmax(1.e-20, 1. - x * x);
   double t1 = log(xx), t2 = 2. / (K_PI_FULL * a);
-  double t3 = t2 + 0.5 * t1, t4 = t1 / a, t5 = t2 + 0.5 * t1;
-  return sgn * sqrt(sqrt(t3 * t3 - t4) - t5);
+  double t3 = t2 + mrn(0.5, t1), t4 = t1 / a, t5 = t2 + mrn(0.5, t1);
+  return sgn * sqrt(sqrt(mrn(t3, t3) - t4) - t5);
 }
 __device__ __forceinline__ double f_gauss(double x, double sig, double mean) {   // :515-524
   double a = sqrt(2. * K_PI_FULL) * sig;
@@ -1871,10 +1878,11 @@ __device__ __forceinline__ double f_gauss(double x, double sig, double mean) {  
   return (1. / a) * exp(-0.5 * b);
 }
 __device__ double het_sf(double x, double mis) {   // SE :375-390
-  if (x > 100.) return (cube(mis) - 3. * mis + 2.) / 4.;
-  double fii = sqrt(1. - 2. * mis * x + x * x);
+  if (x > 100.) return (cube_rn(mis) - mrn(3., mis) + 2.) / 4.;
+  double fii = sqrt(1. - mrn(mrn(2., mis), x) + mrn(x, x));
   double fpsi = (x - mis) / fii;
-  return 0.5 * (1. + cube((1. - mis * x) / fii) + (2. - 3. * fpsi + cube(fpsi)) * cube(x) + 3. * mis * (fpsi - 1.) * x * x);
+  return 0.5 * (1. + cube_rn((1. - mrn(mis, x)) / fii) + mrn(2. - mrn(3., fpsi) + cube_rn(fpsi), cube_rn(x)) +
+                mrn(mrn(mrn(mrn(3., mis), fpsi - 1.), x), x));
 }
 
 // Temperature-only parts of J_imm (:210-278), evaluated once per cell and bin
@@ -1884,12 +1892,12 @@ __device__ JimmPre jimm_pre(double Tk, double Seq) {
   const double rho_ice = 900., T0 = 273.15;
   double Tc = Tk - T0;
   r.act_energy = K_RG * Tk * (347. / (Tk - 177.) - log(4.14 / 349.)) / K_AVOG;
-  r.sigma_is = 28.e-3 + 0.25e-3 * Tc;
-  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  r.sigma_is = 28.e-3 + mrn(0.25e-3, Tc);
+  double Lefm = (79.7 + mrn(0.708, Tc) - mrn(mrn(2.5e-3, Tc), Tc)) * 4.1868e3;
   double GG = K_RG * Tk / K_MWA / Lefm;
   double sg = pow(Seq, GG);
   r.ok = !((T0 / Tk) * sg < 1.0001);
-  r.d_g = r.ok ? 4. * r.sigma_is / (rho_ice * Lefm * log((T0 / Tk) * sg) - 1.7e10 * 0.) : 0.;
+  r.d_g = r.ok ? 4. * r.sigma_is / (mrn(mrn(rho_ice, Lefm), log((T0 / Tk) * sg)) - 1.7e10 * 0.) : 0.;
   if (r.d_g <= 1e-10) r.ok = false;
   return r;
 }
@@ -1897,14 +1905,15 @@ __device__ double J_imm(const JimmPre &q, double theta, double Tk, double Din) {
   if (Din < 1e-10 || !q.ok) return 0.;
   double costh = cos(theta * K_PI / 180.);
   double sf = het_sf(Din / q.d_g, costh);
-  double crit = (K_PI / 3.) * q.sigma_is * (q.d_g * q.d_g) * sf - (1. / 4.) * 0.0 * (1. - costh) * Din * Din;
+  double crit = mrn(mrn(mrn((K_PI / 3.), q.sigma_is), mrn(q.d_g, q.d_g)), sf) -
+                mrn(mrn(mrn((1. / 4.) * 0.0, (1. - costh)), Din), Din);
   return (K_BOLTZ * Tk / K_PLANCK) * 1.e19 * K_PI * (Din * Din) * exp(-(q.act_energy + crit) / (K_BOLTZ * Tk));
 }
 __device__ double J_dep(double theta, double Tk, double Din, double Seq) {   // :282-331
   if (Din < 1e-10 || Seq < 1.0001) return 0.;
   double Tc = Tk - 273.15;
-  double sigma_iv = ((76.1 - 0.155 * Tc) + (28.5 + 0.25 * Tc)) * 1.e-3;
-  double d_g = 4. * sigma_iv / (K_RG * K_RHOIC / K_MWA * Tk * log(Seq) - 1.7e10 * 0.);
+  double sigma_iv = ((76.1 - mrn(0.155, Tc)) + (28.5 + mrn(0.25, Tc))) * 1.e-3;
+  double d_g = 4. * sigma_iv / (mrn(K_RG * K_RHOIC / K_MWA * Tk, log(Seq)) - 1.7e10 * 0.);
   if (d_g <= 1e-10) return 0.;
   double costh = cos(theta * K_PI / 180.);
   double sf = het_sf(Din / d_g, costh);
@@ -1914,12 +1923,12 @@ __device__ double J_dep(double theta, double Tk, double Din, double Seq) {   // 
 __device__ double J_hf(double Tk, double Sw) {   // :335-371
   const double Nc = 5.85e16, T0 = 273.15;
   double Tc = Tk - T0;
-  double act = 0.694e-19 * (1. + 0.027 * (Tc + 30.));
-  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double act = 0.694e-19 * (1. + mrn(0.027, (Tc + 30.)));
+  double Lefm = (79.7 + mrn(0.708, Tc) - mrn(mrn(2.5e-3, Tc), Tc)) * 4.1868e3;
   double GG = K_RG * Tk / Lefm / K_MWA;
   double sg = pow(Sw, GG);
   if ((T0 / Tk) * sg < 1.0001) return 0.;
-  double sigma_is = 28.e-3 + 0.25e-3 * Tc;
+  double sigma_is = 28.e-3 + mrn(0.25e-3, Tc);
   double d_g = 4. * sigma_is / (K_RHOIC * Lefm * log((T0 / Tk) * sg));
   if (d_g <= 1e-10) return 0.;
   double crit = (K_PI / 3.) * sigma_is * d_g * d_g;
@@ -1939,7 +1948,7 @@ __device__ double calc_sweq(const DevParams &P, const WS<KT> &w, int b, double T
   double zns = 0., zvs = 0., zvtot = 0.;
   for (int i = 0; i < P.ndry; i++) {
     zns = zns + P.diss[i] * w.v(i, b) * P.rholiq[i] / P.MM[i];
-    zvs = zvs + fmin(1., P.diss[i]) * w.v(i, b);
+    zvs = zvs + mrn(fmin(1., P.diss[i]), w.v(i, b));
     zvtot = zvtot + w.v(i, b);
   }
   if (P.has_kappa) zns = solute_moles(P, w, b, kappa);
@@ -2019,20 +2028,20 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
     double f_hom = 0.;
     if (hom) {
       double Jh = J_hf(T, Seq);
-      f_hom = 1. - exp(-Jh * K_PI6 * (cube(dwet) - cube(dins_)) * dt);
+      f_hom = 1. - exp(-Jh * K_PI6 * (cube_rn(dwet) - cube_rn(dins_)) * dt);
     }
     r[R_FHOM] = f_hom;
     r[R_MODE] = imm ? 1. : (dep ? 2. : 0.);
     r[R_DIN] = w.ddry[kk];
     if (imm) {
       // low_theta (:394-417)
-      double th00 = P.mean_theta_imm + sqrt(2.) * P.sigma_theta_imm * erfm1(2. * w.indef[kk] - 1.);
+      double th00 = P.mean_theta_imm + mrn(sqrt(2.) * P.sigma_theta_imm, erfm1(mrn(2., w.indef[kk]) - 1.));
       th00 = fmin(fmax(th00, 0.), 180.);
       if (!P.st_freeTheta) th00 = fmax(P.initMinTheta, th00);
       JimmPre q = jimm_pre(T, Seq);
       r[R_THMIN] = th00; r[R_AE] = q.act_energy; r[R_SIG] = q.sigma_is; r[R_DG] = q.ok ? q.d_g : -1.;
     } else if (dep) {
-      double th00 = P.mean_theta_dep + sqrt(2.) * P.sigma_theta_dep * erfm1(2. * w.indef[kk] - 1.);
+      double th00 = P.mean_theta_dep + mrn(sqrt(2.) * P.sigma_theta_dep, erfm1(mrn(2., w.indef[kk]) - 1.));
       th00 = fmin(fmax(th00, 0.), 180.);
       if (!P.st_freeTheta) th00 = fmax(P.initMinTheta, th00);
       r[R_THMIN] = th00;
@@ -2062,7 +2071,7 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
       if (on) {
         const double *r = rec + kk * 8;
         const double thmin = r[R_THMIN], thmax = 180.;
-        const double th1 = 0.5 * (thmax - thmin) * c_gl_x[node] + 0.5 * (thmax + thmin);
+        const double th1 = mrn(0.5 * (thmax - thmin), c_gl_x[node]) + 0.5 * (thmax + thmin);
         double J, ft;
         if (r[R_MODE] == 1.) {
           JimmPre q;
@@ -2097,8 +2106,8 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
     const double f_hom = r[R_FHOM];
     const double f_imm = r[R_MODE] == 1. ? r[R_FINT] : 0.;
     const double f_dep = r[R_MODE] == 2. ? r[R_FINT] : 0.;
-    dh += n * f_hom; dd += n * f_dep; di += n * f_imm;
-    double frac = fmax(0., fmin(0.99, f_imm + f_hom + f_dep - (f_imm + f_dep) * f_hom));
+    dh += mrn(n, f_hom); dd += mrn(n, f_dep); di += mrn(n, f_imm);
+    double frac = fmax(0., fmin(0.99, f_imm + f_hom + f_dep - mrn((f_imm + f_dep), f_hom)));
     if (n < nlim_of(ph)) continue;
     double vins = 0.;
     for (int k = 0; k < P.ninsoluble; k++) vins += w.v(P.ind_insoluble[k], kk);
@@ -2112,7 +2121,7 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
     if (frac_DU <= 0.1) { frac2 = frac * frac_DU; ncur0 = n * frac_DU; }
     else { frac2 = frac; ncur0 = n; }
     double nnuc = frac2 * n;
-    double f1 = nnuc + (ncur0 - nnuc) * w.indef[kk];
+    double f1 = nnuc + mrn((ncur0 - nnuc), w.indef[kk]);
     f1 = f1 / ncur0;
     w.indef[kk] = fmin(fmax(f1, 0.), 1. - 1.e-20);
     st[0] = (double)bb;
@@ -2120,7 +2129,7 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
     bool mk = P.st_icenucl;
     if (frac_DU <= 0.1) {
       if (mk) st[1 + idu] = V_tot * frac_DU;
-      w.v(idu, kk) = fmax(0., w.v(idu, kk) - V_tot * frac_DU);
+      w.v(idu, kk) = fmax(0., w.v(idu, kk) - mrn(V_tot, frac_DU));
     } else {
       for (int s = 0; s < ndry; s++) {
         if (mk) st[1 + s] = w.v(s, kk) * frac2;
@@ -2155,23 +2164,24 @@ __device__ double calc_Jhet(double rn, double temp, double Sw) {
   if (rn < 1e-10) return 0.;
   double Tc = temp - T0;
   double act = K_RG * temp * (347. / (temp - 177.) - log(4.14 / 349.)) / K_AVOG;
-  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double Lefm = (79.7 + mrn(0.708, Tc) - mrn(mrn(2.5e-3, Tc), Tc)) * 4.1868e3;
   double GG = K_RG * temp / K_MWA / Lefm;
   double sg = pow(Sw, GG);
   if ((T0 / temp) * sg < 1.0001) return 0.;
-  double sigma_is = 28.e-3 + 0.25e-3 * Tc;
-  double r_g = 4. * sigma_is / (rho_ice * Lefm * log((T0 / temp) * sg) - 1.7e10 * 0.);
+  double sigma_is = 28.e-3 + mrn(0.25e-3, Tc);
+  double r_g = 4. * sigma_is / (mrn(mrn(rho_ice, Lefm), log((T0 / temp) * sg)) - 1.7e10 * 0.);
   if (r_g <= 1e-10) return 0.;
   double sf = het_sf(rn / r_g, mis);
-  double crit = (K_PI / 3.) * sigma_is * r_g * r_g * sf - (1. / 4.) * 0.0 * (1. - mis) * rn * rn;
+  double crit = mrn(mrn(mrn(mrn((K_PI / 3.), sigma_is), r_g), r_g), sf) -
+                mrn(mrn(mrn((1. / 4.) * 0.0, (1. - mis)), rn), rn);
   return K_BOLTZ * temp / K_PLANCK * c_1s * K_PI * rn * rn * exp((-act - crit) / (K_BOLTZ * temp));
 }
 __device__ double calc_Jdep(double rn, double temp, double Si) {
   const double rho_ice = 900., mis = 0.5;
   if (rn < 1e-10 || Si < 1.0001) return 0.;
   double Tc = temp - 273.15;
-  double sigma_iv = ((76.1 - 0.155 * Tc) + (28.5 + 0.25 * Tc)) * 1e-3;
-  double r_g = 4. * sigma_iv / (K_RG * rho_ice / K_MWA * temp * log(Si) - 1.7e10 * 0.);
+  double sigma_iv = ((76.1 - mrn(0.155, Tc)) + (28.5 + mrn(0.25, Tc))) * 1e-3;
+  double r_g = 4. * sigma_iv / (mrn(K_RG * rho_ice / K_MWA * temp, log(Si)) - 1.7e10 * 0.);
   if (r_g <= 1e-10) return 0.;
   double sf = het_sf(rn / r_g, mis);
   double crit = (K_PI / 3.) * sigma_iv * r_g * r_g * sf;
@@ -2180,12 +2190,12 @@ __device__ double calc_Jdep(double rn, double temp, double Si) {
 __device__ double calc_Jhf(double temp, double Sw) {
   const double Nc = 5.85e16, rho_ice = 900., T0 = 273.15;
   double Tc = temp - T0;
-  double act = 0.694e-19 * (1. + 0.027 * (Tc + 30.));
-  double Lefm = (79.7 + 0.708 * Tc - 2.5e-3 * Tc * Tc) * 4.1868e3;
+  double act = 0.694e-19 * (1. + mrn(0.027, (Tc + 30.)));
+  double Lefm = (79.7 + mrn(0.708, Tc) - mrn(mrn(2.5e-3, Tc), Tc)) * 4.1868e3;
   double GG = K_RG * temp / Lefm / K_MWA;
   double sg = pow(Sw, GG);
   if ((T0 / temp) * sg < 1.0001) return 0.;
-  double sigma_is = 28.e-3 + 0.25e-3 * Tc;
+  double sigma_is = 28.e-3 + mrn(0.25e-3, Tc);
   double r_g = 2. * sigma_is / (rho_ice * Lefm * log((T0 / temp) * sg));
   if (r_g <= 1e-10) return 0.;
   double crit = 4. * K_PI / 3. * sigma_is * r_g * r_g;
@@ -2215,8 +2225,8 @@ __device__ void ice_nucl_classic(const DevParams &P, const WS<KT> &w, const doub
     if (dins_ > dmin && dwet - dins_ < dmin && prv / prs < 1.0 && ph == 1 && P.lsicedep)
       pf_dep = 1. - exp(-calc_Jdep(dins_, T, prv / prsi) * dt);
     if (dwet - dins_ > dmin && T < tmax_homog && P.lsicehom)
-      pf_hom = 1. - exp(-calc_Jhf(T, Sw) * K_PI6 * (cube(dwet) - cube(dins_)) * dt);
-    double frac = fmax(0., fmin(0.99, pf_imm + pf_hom + pf_dep - (pf_imm + pf_dep) * pf_hom));
+      pf_hom = 1. - exp(-calc_Jhf(T, Sw) * K_PI6 * (cube_rn(dwet) - cube_rn(dins_)) * dt);
+    double frac = fmax(0., fmin(0.99, pf_imm + pf_hom + pf_dep - mrn((pf_imm + pf_dep), pf_hom)));
     int bb = ice_bin_of(P, vlo, dwet);
     bool mk = P.st_icenucl;
     st[0] = (double)bb;
