@@ -63,6 +63,16 @@ __device__ __forceinline__ double g_cbrt(double x) { return cbrt(x); }
 __device__ __forceinline__ double g_exp(double x) { return exp(x); }
 template <int N> __device__ __forceinline__ Dual<N> g_cbrt(const Dual<N> &x) { return d_cbrt(x); }
 template <int N> __device__ __forceinline__ Dual<N> g_exp(const Dual<N> &x) { return d_exp(x); }
+__device__ __forceinline__ double g_fma(double a, double b, double c) { return fma(a, b, c); }
+// the value rounds once, as fma(double) does, so a dual run's values equal the plain run's
+template <int N>
+__device__ __forceinline__ Dual<N> g_fma(const Dual<N> &a, const Dual<N> &b, const Dual<N> &c) {
+  Dual<N> r;
+  r.v = fma(a.v, b.v, c.v);
+#pragma unroll
+  for (int i = 0; i < N; i++) r.d[i] = fma(a.d[i], b.v, fma(a.v, b.d[i], c.d[i]));
+  return r;
+}
 template <typename R> __device__ __forceinline__ R g_wsum(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += shfl_xor(v, o);
@@ -451,25 +461,28 @@ __device__ __forceinline__ R chain_zvolc(const DevParams &P, const CW<R> &w, int
   return (d >= 0 && which < 5) ? w.V(d, b) : R(0.);
 }
 
-// one iteration of the regime-1a water uptake (equil_iterate / eq_step, :196-245):
-// zke -> (zlwc, zdwet, zke')
+// one iteration of the regime-1a water uptake (equil_iterate, :196-245) in the form of
+// the step kernel's eq_step, operation for operation: izke = 1/zke -> (zlwc, zdwet, izke')
 template <typename R>
-__device__ __forceinline__ void eq1a_iter(R zrh, R &zke, R zv0, R zv1, R numc, R zvp56, R zcore, double T, R &zlwc,
+__device__ __forceinline__ void eq1a_iter(R zrh, R &izke, R zv0, R zv1, R numc, R zvp56, R zcore, double T, R &zlwc,
                                           R &zdwet) {
   const double rhosu_msu = 1830. / 98.08e-3, rhooc_moc = 1400. / 150.e-3;
-  R zaw = zrh / zke;
+  const double ckt = 2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T);
+  R zaw = zrh * izke;
   R a2 = zaw * zaw, a3 = a2 * zaw, a4 = a2 * a2;
   R bm1 = +1.1065495e+2 - 3.6759197e+2 * zaw + 5.0462934e+2 * a2 - 3.1543839e+2 * a3 + 6.770824e+1 * a4;
   R bm2 = 1. / (zaw * K_MWA) - 1. / K_MWA;
-  zlwc = (zv0 * rhosu_msu) / bm1 + K_EPSOC * zv1 * rhooc_moc / bm2;
-  zdwet = g_cbrt(zlwc / numc / K_RHOWA / K_PI6 + zvp56 / K_PI6 + zcore / K_PI6);
-  zke = g_exp(2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T * zdwet));
+  R q0 = zv0 * rhosu_msu, q1 = K_EPSOC * zv1 * rhooc_moc;
+  zlwc = g_fma(q1, bm1, q0 * bm2) / (bm1 * bm2);
+  R rinv = 1. / (numc * (K_RHOWA * K_PI6));
+  zdwet = g_cbrt(g_fma(zlwc, rinv, zvp56 / K_PI6) + zcore / K_PI6);
+  izke = g_exp(-(ckt / zdwet));
 }
 
 // the regime-1a chain of the non-initialising equilibration (:160-250), on every lane
 template <typename R>
 __device__ void chain_equil_1a(const DevParams &P, const CW<R> &w, R prh, double T, double *tp_eq, int lane) {
-  R zke = R(1.001);
+  R izke = R(1. / 1.001);   // 1/zke, carried from bin to bin
   const R zrh = fmin(fmax(prh, R(0.05)), R(0.98));
   for (int kk = P.in1a; kk <= P.fn1a; kk++) {
     double *te = tp_eq ? tp_eq + (kk - P.in1a) * TP_MAXEQ : nullptr;
@@ -486,14 +499,14 @@ __device__ void chain_equil_1a(const DevParams &P, const CW<R> &w, R prh, double
     double zdwet = val(w.dw[kk]), zdold = 1.;
     R zlwc = R(0.);
     int count = 0;
-    if (te && lane == 0) te[1] = val(zke);
-    while (fabs(zdwet / zdold - 1.) > 1.e-2) {
+    if (te && lane == 0) te[1] = val(izke);
+    while (fabs(zdwet - zdold) > 1.e-2 * zdold) {   // |zdwet/zdold - 1| > 1e-2, zdold > 0
       zdold = fmax(zdwet, 1.e-20);
       R zd;
-      eq1a_iter(zrh, zke, zv0, zv1, numc, zvp56, zcore, T, zlwc, zd);
+      eq1a_iter(zrh, izke, zv0, zv1, numc, zvp56, zcore, T, zlwc, zd);
       zdwet = val(zd);
       count++;
-      if (te && lane == 0 && count + 1 < TP_MAXEQ) te[count + 1] = val(zke);
+      if (te && lane == 0 && count + 1 < TP_MAXEQ) te[count + 1] = val(izke);
       if (count > 100) break;
     }
     if (te && lane == 0) te[0] = (double)count;
@@ -1096,12 +1109,12 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
         const double zv0 = P.ix_so4 >= 0 ? xm[NL + P.ix_so4 * NL + kk] : 0.;
         const double zv1 = P.ix_oc >= 0 ? xm[NL + P.ix_oc * NL + kk] : 0.;
         const double zcore = zv0 / numc + zv1 / numc;
-        Dual<5> zke(te[i]), d0(zv0), d1(zv1), dnm(numc), dco(zcore);
-        zke.d[0] = 1.; d0.d[1] = 1.; d1.d[2] = 1.; dnm.d[3] = 1.; dco.d[4] = 1.;
+        Dual<5> izke(te[i]), d0(zv0), d1(zv1), dnm(numc), dco(zcore);
+        izke.d[0] = 1.; d0.d[1] = 1.; d1.d[2] = 1.; dnm.d[3] = 1.; dco.d[4] = 1.;
         Dual<5> zlwc, zd;
-        eq1a_iter(zrhd, zke, d0, d1, dnm, Dual<5>(0.), dco, T, zlwc, zd);   // zke is now zke_i
+        eq1a_iter(zrhd, izke, d0, d1, dnm, Dual<5>(0.), dco, T, zlwc, zd);   // izke is now 1/zke_i
         const double lb = (i == cnt) ? a.AV(iwa, kk) / K_RHOWA : 0.;
-        for (int k = 0; k < 5; k++) { p[k] = zke.d[k]; q[k] = lb * zlwc.d[k]; }
+        for (int k = 0; k < 5; k++) { p[k] = izke.d[k]; q[k] = lb * zlwc.d[k]; }
       }
       // the zke adjoint entering each iteration, serially through the chunk
       const int n = min(32, total - base);

@@ -1030,12 +1030,13 @@ __device__ double equil_iterate(const DevParams &P, const WS<KT> &w, int b, doub
 
 // State of one fixed-point solve of equil_iterate, advanced one iteration at a time so
 // that the regime-1a chain (sequential: zke carries from bin to bin) runs on its own lane
-// next to the independent regime-2 solves.
+// next to the independent regime-2 solves.  The iteration carries 1/zke = exp(-c/dwet)
+// rather than zke, so that zaw = zrh/zke is a product.
 struct EqJob {
   int kk, count;
   bool r2;
-  double tol, zrh, zke, numc, zv0, zv1, zv4, zvp56, zcore, zdwet, zdold, zlwc;
-  double q0, q1, q4, p56, pc;   // per-bin invariants of the iteration (same operations, computed once)
+  double tol, zrh, izke, numc, zv0, zv1, zv4, zvp56, zcore, zdwet, zdold, zlwc;
+  double q0, q1, q4, p56, pc, rinv;   // per-bin invariants of the iteration, computed once
 };
 
 template <typename KT>
@@ -1055,28 +1056,34 @@ __device__ __forceinline__ void eq_load(const DevParams &P, const WS<KT> &w, int
     j.q4 = j.zv4 * rhoss_mss;
     j.p56 = j.zvp56 / K_PI6;
     j.pc = j.zcore / K_PI6;
+    j.rinv = 1. / (j.numc * (K_RHOWA * K_PI6));   // zlwc / numc / rhowa / pi6 as one product
   }
   j.zdwet = w.dwet[b];
   j.zdold = 1.;
   j.zlwc = 0.;
 }
 
-// one pass of the equil_iterate loop body (same operations in the same order; the
-// per-bin invariants q*, p* and kT = K_BOLTZ * T are computed once)
-__device__ __forceinline__ void eq_step(EqJob &j, double kT) {
+// one pass of the equil_iterate loop body (mo_salsa_properties.f90:196-230, :305-340).
+// FP64 divisions are the scarce resource here, so the pass takes three instead of ten:
+// the molality quotients share one denominator, the per-bin factor 1/(numc rhowa pi6)
+// and c = 2 sigma v_w / kT are computed once, and 1/zke = exp(-c/dwet) is carried.
+// The values move by an ulp or so against the reference's operation order.
+__device__ __forceinline__ void eq_step(EqJob &j, double ckt) {
   j.zdold = fmax(j.zdwet, 1.e-20);
-  double zaw = j.zrh / j.zke;
+  double zaw = j.zrh * j.izke;
   double a2 = zaw * zaw, a3 = a2 * zaw, a4 = a2 * a2;
   double bm1 = +1.1065495e+2 - 3.6759197e+2 * zaw + 5.0462934e+2 * a2 - 3.1543839e+2 * a3 + 6.770824e+1 * a4;
   double bm2 = 1. / (zaw * K_MWA) - 1. / K_MWA;
-  double zlwc = j.q0 / bm1 + j.q1 / bm2;
-  if (j.r2) {
-    double bm5 = +5.875248e+1 - 1.8781997e+2 * zaw + 2.7211377e+2 * a2 - 1.8458287e+2 * a3 + 4.153689e+1 * a4;
-    zlwc += j.q4 / bm5;
-  }
+  // regime 1a is the same sum with bm5 = 1 and no sea salt term (one code path for the
+  // 1a lane and the regime-2 lanes; explicit fmas so the gradient harness's copy of the
+  // 1a iteration rounds the same)
+  double bm5 = +5.875248e+1 - 1.8781997e+2 * zaw + 2.7211377e+2 * a2 - 1.8458287e+2 * a3 + 4.153689e+1 * a4;
+  bm5 = j.r2 ? bm5 : 1.;
+  const double q4 = j.r2 ? j.q4 : 0.;
+  const double zlwc = fma(q4, bm1 * bm2, fma(j.q1, bm1 * bm5, j.q0 * (bm2 * bm5))) / (bm1 * bm2 * bm5);
   j.zlwc = zlwc;
-  j.zdwet = cbrt(zlwc / j.numc / K_RHOWA / K_PI6 + j.p56 + j.pc);
-  j.zke = exp(2. * K_SURFW0 * K_MVWA / (kT * j.zdwet));
+  j.zdwet = cbrt(fma(zlwc, j.rinv, j.p56) + j.pc);
+  j.izke = exp(-(ckt / j.zdwet));
   j.count++;
 }
 
@@ -1096,19 +1103,19 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   int nonconv = 0;
   const int n2 = init ? P.fn2b - P.in2a + 1 : 0;
-  const double kT = K_BOLTZ * T;
+  const double ckt = 2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T);
   if (n2 <= 31) {
     // lane 31: the regime-1a chain in bin order; lanes 0..n2-1: regime-2 bins
     EqJob j;
     j.kk = -1;
     if (lane == 31) {
-      j.r2 = false; j.tol = 1.e-2; j.zrh = fmin(fmax(prh, 0.05), 0.98); j.zke = 1.001;
+      j.r2 = false; j.tol = 1.e-2; j.zrh = fmin(fmax(prh, 0.05), 0.98); j.izke = 1. / 1.001;
       int k = eq_next_1a(P, w, dmid, P.in1a - 1, init);
       if (k >= 0) eq_load(P, w, k, j);
     } else if (lane < n2) {
       int k = P.in2a + lane;
       if (w.numc[k] > K_NLIM) {
-        j.r2 = true; j.tol = 1.e-12; j.zrh = fmin(fmax(prh, 0.37), 0.98); j.zke = 1.02;
+        j.r2 = true; j.tol = 1.e-12; j.zrh = fmin(fmax(prh, 0.37), 0.98); j.izke = 1. / 1.02;
         eq_load(P, w, k, j);
       } else {
         w.dwet[k] = dmid[k];
@@ -1116,9 +1123,9 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
     }
     while (__any_sync(0xffffffffu, j.kk >= 0)) {
       if (j.kk >= 0) {
-        bool go = fabs(j.zdwet / j.zdold - 1.) > j.tol;
+        bool go = fabs(j.zdwet - j.zdold) > j.tol * j.zdold;   // |zdwet/zdold - 1| > tol, zdold > 0
         if (go) {
-          eq_step(j, kT);
+          eq_step(j, ckt);
           if (j.count > 100) { nonconv = 1; go = false; }
         }
         if (!go) {
