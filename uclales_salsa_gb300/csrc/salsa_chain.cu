@@ -622,8 +622,18 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
   double ttot = 0.;
   R zcwint = R(0.);
   int counter = 0;
+  // the step kernel's form of the substeps (gpparth2o): the sum of mt*wsat*surf that
+  // opens a substep is formed at the end of the previous one, with the same lane
+  // partial sums (lane l: bins l, l+32)
+  const double adt = 2.e-2;
+  R spsum;
+  {
+    R sp = R(0.);
+    for (int b = lane; b < NL; b += 32)
+      if (b >= P.in2a) sp += w.mt[b] * w.wsat[b] * w.surf[b];
+    spsum = g_wsum(sp);
+  }
   while (ttot < dt) {
-    const double adt = 2.e-2;
     if (tp && counter < tl.maxit) {
       if (lane == 0) tp[tl.hist_zc + counter] = val(zcwc);
       for (int b = lane; b < NL; b += 32) {
@@ -631,12 +641,10 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
         tp[tl.hist_w + counter * NL + b] = val(w.wsat[b]);
       }
     }
-    R sp = R(0.);
-    for (int b = P.in2a + lane; b < NL; b += 32) sp += w.mt[b] * w.wsat[b] * w.surf[b];
-    const R zhlp1 = zcwc + adt * g_wsum(sp);
+    const R zhlp1 = zcwc + adt * spsum;
     const R zhlp2 = 1. + adt * mtot;
     zcwint = fmin(zhlp1 / zhlp2, zcwtot);
-    R cs = R(0.);
+    R cs = R(0.), sp = R(0.);
     for (int b = lane; b < NL; b += 32) {
       const int ph = phase_of(P, b);
       R cc_ = w.cw[b];
@@ -648,8 +656,10 @@ __device__ int chain_condensation(const DevParams &P, const CW<R> &w, const doub
       }
       w.cw[b] = cc_;
       cs += cc_;
+      if (b >= P.in2a) sp += w.mt[b] * w.wsat[b] * w.surf[b];
     }
     zcwint = zcwtot - g_wsum(cs);
+    spsum = g_wsum(sp);
     zcwc = zcwint;
     ttot = ttot + adt;
     counter++;
@@ -959,7 +969,8 @@ __device__ void cond_reverse(const DevParams &P, const CW<double> &w, const AW &
       const double zc_in = tp[tl.hist_zc + it];
       const double *cin = tp + tl.hist_c + it * NL, *win = tp + tl.hist_w + it * NL;
       double sp = 0.;
-      for (int b = P.in2a + lane; b < NL; b += 32) sp += w.mt[b] * win[b] * w.surf[b];
+      for (int b = lane; b < NL; b += 32)
+        if (b >= P.in2a) sp += w.mt[b] * win[b] * w.surf[b];
       const double zhlp1 = zc_in + adt * wsum(sp);
       const double zhlp2 = 1. + adt * mtot;
       const double q = zhlp1 / zhlp2;

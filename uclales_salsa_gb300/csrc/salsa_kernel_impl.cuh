@@ -1432,14 +1432,23 @@ __device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb,
 #ifdef SALSA_STAGE_TIMERS
   long long t_sub0 = clock64();
 #endif
-  while (ttot < dt) {
-    const double adt = 2.e-2;
+  // The sum of mt*wsat*surf that opens a substep is formed at the end of the previous
+  // one and reduced together with its vapour sum: one paired butterfly of 5 adds
+  // instead of two of 5.  Lane l holds bins l, l+32 (the same partial sums for both),
+  // so the totals are those of two separate butterflies over those partial sums.
+  const double adt = 2.e-2;
+  double spsum;
+  {
     double sp = 0.;
-    for (int b = P.in2a + lane; b < ntot; b += 32) sp += mt[b] * wsat[b] * surf[b];
-    double zhlp1 = zcwc + adt * warp_sum(sp);
+    for (int b = lane; b < ntot; b += 32)
+      if (b >= P.in2a) sp += mt[b] * wsat[b] * surf[b];
+    spsum = warp_sum(sp);
+  }
+  while (ttot < dt) {
+    double zhlp1 = zcwc + adt * spsum;
     double zhlp2 = 1. + adt * mtot;
     zcwint = fmin(zhlp1 / zhlp2, zcwtot);
-    double cs = 0.;
+    double cs = 0., sp = 0.;
     for (int b = lane; b < ntot; b += 32) {
       int ph = phase_of(P, b);
       double c = cw[b];
@@ -1451,8 +1460,19 @@ __device__ void gpparth2o(const DevParams &P, const WS<KT> &w, const double *tb,
       }
       cw[b] = c;
       cs += c;
+      if (b >= P.in2a) sp += mt[b] * wsat[b] * surf[b];
     }
-    zcwint = zcwtot - warp_sum(cs);
+    {
+      // lanes 0-15 reduce cs, lanes 16-31 reduce sp
+      const bool hi = lane & 16;
+      double v = (hi ? sp : cs) + __shfl_xor_sync(0xffffffffu, hi ? cs : sp, 16);
+      v += __shfl_xor_sync(0xffffffffu, v, 8);
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      zcwint = zcwtot - __shfl_sync(0xffffffffu, v, 0);
+      spsum = __shfl_sync(0xffffffffu, v, 16);
+    }
     zcwc = zcwint;
     ttot = ttot + adt;
     counter++;
