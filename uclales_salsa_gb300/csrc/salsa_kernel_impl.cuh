@@ -292,7 +292,15 @@ __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinPro
   const BinProps<T> &S = first_large ? b : a;
   T dv = fabs(a.termv - b.termv);
   T stok = (T)2. * S.termv * dv / (L.diam * (T)K_GRAV);
-  T zbrown = flux1 / (mdiam / (mdiam + fmdist) + flux1 / flux2);
+  // flux1 / (mdiam/(mdiam+fmdist) + flux1/flux2) as one quotient in FP64; the float form
+  // keeps the reference's shape (the products would leave float's range)
+  T zbrown;
+  if (!is_f32<T>::value) {
+    const T mf = mdiam + fmdist;
+    zbrown = flux1 * flux2 * mf / (mdiam * flux2 + flux1 * mf);
+  } else {
+    zbrown = flux1 / (mdiam / (mdiam + fmdist) + flux1 / flux2);
+  }
   T zbrconv;
   if (L.reyn <= (T)1.) zbrconv = (T)0.45 * zbrown * t_cbrt(L.reyn * S.schm);
   else zbrconv = (T)0.45 * zbrown * t_sqrt(L.reyn) * t_cbrt(S.schm);
@@ -1898,11 +1906,20 @@ __device__ double erfm1(double x) {   // math_functions.f90:494-510
   double t3 = t2 + mrn(0.5, t1), t4 = t1 / a, t5 = t2 + mrn(0.5, t1);
   return sgn * sqrt(sqrt(mrn(t3, t3) - t4) - t5);
 }
-__device__ __forceinline__ double f_gauss(double x, double sig, double mean) {   // :515-524
-  double a = sqrt(2. * K_PI_FULL) * sig;
-  double b = (x - mean) * (x - mean);
-  b = b / (sig * sig);
-  return (1. / a) * exp(-0.5 * b);
+// f_gauss (:515-524) with its per-configuration factors 1/(sqrt(2 pi) sig) and 1/sig^2
+// taken once per cell
+struct GaussC { double ra, rs2, mean; };
+__device__ __forceinline__ GaussC gauss_c(double sig, double mean) {
+  GaussC g;
+  g.ra = 1. / (sqrt(2. * K_PI_FULL) * sig);
+  g.rs2 = 1. / (sig * sig);
+  g.mean = mean;
+  return g;
+}
+__device__ __forceinline__ double f_gauss(double x, const GaussC &g) {
+  double b = (x - g.mean) * (x - g.mean);
+  b = b * g.rs2;
+  return g.ra * exp(-0.5 * b);
 }
 __device__ double het_sf(double x, double mis) {   // SE :375-390
   if (x > 100.) return (cube_rn(mis) - mrn(3., mis) + 2.) / 4.;
@@ -1928,13 +1945,14 @@ __device__ JimmPre jimm_pre(double Tk, double Seq) {
   if (r.d_g <= 1e-10) r.ok = false;
   return r;
 }
-__device__ double J_imm(const JimmPre &q, double theta, double Tk, double Din) {
+// kth = K_BOLTZ * Tk / K_PLANCK, taken once per cell
+__device__ double J_imm(const JimmPre &q, double theta, double Tk, double Din, double kth) {
   if (Din < 1e-10 || !q.ok) return 0.;
   double costh = cos(theta * K_PI / 180.);
   double sf = het_sf(Din / q.d_g, costh);
   double crit = mrn(mrn(mrn((K_PI / 3.), q.sigma_is), mrn(q.d_g, q.d_g)), sf) -
                 mrn(mrn(mrn((1. / 4.) * 0.0, (1. - costh)), Din), Din);
-  return (K_BOLTZ * Tk / K_PLANCK) * 1.e19 * K_PI * (Din * Din) * exp(-(q.act_energy + crit) / (K_BOLTZ * Tk));
+  return kth * 1.e19 * K_PI * (Din * Din) * exp(-(q.act_energy + crit) / (K_BOLTZ * Tk));
 }
 __device__ double J_dep(double theta, double Tk, double Din, double Seq) {   // :282-331
   if (Din < 1e-10 || Seq < 1.0001) return 0.;
@@ -2090,6 +2108,9 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
     }
     __syncwarp();
     const int grp = lane / 10, node = lane - grp * 10;
+    const GaussC g_imm = gauss_c(P.sigma_theta_imm, P.mean_theta_imm);
+    const GaussC g_dep = gauss_c(P.sigma_theta_dep, P.mean_theta_dep);
+    const double kth = K_BOLTZ * T / K_PLANCK;
     for (int b0 = 0; b0 < nlist; b0 += 3) {
       const int slot = b0 + grp;
       const bool on = grp < 3 && slot < nlist;
@@ -2103,11 +2124,11 @@ __device__ void ice_nucl_SE(const DevParams &P, const WS<KT> &w, const double *t
         if (r[R_MODE] == 1.) {
           JimmPre q;
           q.act_energy = r[R_AE]; q.sigma_is = r[R_SIG]; q.d_g = r[R_DG]; q.ok = r[R_DG] >= 0.;
-          J = J_imm(q, th1, T, r[R_DIN]);
-          ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_imm, P.mean_theta_imm) : 0.;
+          J = J_imm(q, th1, T, r[R_DIN], kth);
+          ft = th1 > thmin ? f_gauss(th1, g_imm) : 0.;
         } else {
           J = J_dep(th1, T, r[R_DIN], Si);
-          ft = th1 > thmin ? f_gauss(th1, P.sigma_theta_dep, P.mean_theta_dep) : 0.;
+          ft = th1 > thmin ? f_gauss(th1, g_dep) : 0.;
         }
         term = ft * c_gl_w[node] * (1. - exp(-J * dt));
       }
