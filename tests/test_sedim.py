@@ -98,3 +98,44 @@ def test_switches_and_arguments():
     c = {k: v.clone() for k, v in a.items() if k != "mcloudt"}
     assert Oracle(inp.cfg).sedimentation(inp.nzp, inp.nxp, inp.nyp, 1.0, (0, 1, 0, 0), c) == 1
     assert Oracle(inp.cfg).sedimentation(inp.nzp, inp.nxp, inp.nyp, 0.0, (1, 1, 1, 1), a) == 1
+
+
+def test_long_step_deposits_every_drop():
+    """With dtlt = 1e5 s every populated precipitation parcel falls through the column:
+    it leaves its level and lands on the lowest one (one level thickness, so without
+    rescaling), and the surface rate is the water flux of all those parcels."""
+    inp, a = sedim_state("grid256x256x128", X=4, Y=4, Z=12, dz=5.0)
+    lay = inp.layout
+    dtlt = 1.0e5   # 20 um drops fall ~1 cm/s: 1 km in that time, the column is 60 m
+    b = _run(inp, a, dtlt, (0, 0, 1, 0))
+    n = a["nprecp"]
+    act = n >= 1e-6
+    d = (b["nprecpt"] - a["nprecpt"]) * dtlt
+    cols = _cols(d, inp)
+    nc = _cols(n * act, inp)
+    assert int(act.sum()) > 10
+    # levels 1..nzp-2 lose their parcel; level 0 gains the column's total
+    assert torch.allclose(cols[..., 1:-1], -nc[..., 1:-1], rtol=1e-12, atol=0)
+    assert torch.allclose(cols[..., 0], nc[..., 1:-1].sum(-1), rtol=1e-12, atol=0)
+    # surface rate: sum over the reference's range (last bin of the species before
+    # water, then the water bins) of m * adn * Vt over the column, times alvl
+    nw, nb = lay.nwet, lay.nprc
+    m = a["mprecp"].view(nw, nb, *n.shape[1:])
+    vt = b["VtPrc"]
+    terms = [m[nw - 2, nb - 1] * a["adn"] * vt[nb - 1]] + [m[nw - 1, k] * a["adn"] * vt[k] for k in range(nb)]
+    sfc = sum(_cols(t, inp)[..., 1:-1].sum(-1) for t in terms) * ALVL
+    got = b["sfcrrate"][2:inp.nyp - 2, 2:inp.nxp - 2]
+    assert float(got.max()) > 0
+    assert torch.allclose(got, sfc, rtol=1e-12, atol=0)
+
+
+def test_nothing_to_sediment():
+    """Empty bins everywhere: tendencies and tlt unchanged, rates and fall speeds zero."""
+    inp, a = sedim_state("grid16x16x40", X=3, Y=3, Z=6)
+    for k in ("naero", "ncloud", "nprecp", "maero", "mcloud", "mprecp"):
+        a[k] = torch.zeros_like(a[k])
+    b = _run(inp, a, 1.0, (1, 1, 1, 1))
+    for k in ("naerot", "maerot", "ncloudt", "mcloudt", "nprecpt", "mprecpt", "tlt"):
+        assert torch.equal(b[k], a[k]), k
+    for k in ("rrate", "sfcrrate", "VtPrc"):
+        assert float(b[k].abs().max()) == 0, k
