@@ -960,6 +960,15 @@ bool handle_params(const salsa_handle_t *h, DevParams *base, cudaStream_t *strea
   return true;
 }
 const salsa_config_t *handle_config(const salsa_handle_t *h) { return h ? &h->cfg : nullptr; }
+bool device_ptrs(std::initializer_list<const void *> ps) {
+  for (const void *p : ps) {
+    if (!p) continue;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return false;
+  }
+  return true;
+}
 void *handle_scratch(salsa_handle_t *h, int slot, size_t bytes) {
   if (!h || slot < 0 || slot >= 4) return nullptr;
   if (bytes > h->scratch_bytes[slot]) {

@@ -363,17 +363,6 @@ __global__ void __launch_bounds__(128) diagnostics_kernel(const PostArgs A) {
   }
 }
 
-// every non-NULL pointer must be device (or managed) memory
-bool device_ptrs(std::initializer_list<const void *> ps) {
-  for (const void *p : ps) {
-    if (!p) continue;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return false;
-  }
-  return true;
-}
-
 }  // namespace
 }  // namespace salsa
 

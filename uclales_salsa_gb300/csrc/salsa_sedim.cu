@@ -450,17 +450,6 @@ __global__ void __launch_bounds__(128) sedimentation_kernel(const SedArgs A) {
   }
 }
 
-// every non-NULL pointer must be device (or managed) memory
-bool sed_device_ptrs(std::initializer_list<const void *> ps) {
-  for (const void *p : ps) {
-    if (!p) continue;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return false;
-  }
-  return true;
-}
-
 }  // namespace
 }  // namespace salsa
 
@@ -483,7 +472,7 @@ int salsa_gb300_sedimentation(salsa_handle_t *h, int nzp, int nxp, int nyp, doub
       (s2 && (!f->nprecp || !f->mprecp || !f->nprecpt || !f->mprecpt || !f->VtPrc)) ||
       (s3 && (!f->nice || !f->mice || !f->nicet || !f->micet || !f->VtIce)))
     return SALSA_E_ARG;
-  if (!salsa::sed_device_ptrs({f->naero, f->ncloud, f->nprecp, f->nice, f->maero, f->mcloud, f->mprecp, f->mice,
+  if (!salsa::device_ptrs({f->naero, f->ncloud, f->nprecp, f->nice, f->maero, f->mcloud, f->mprecp, f->mice,
                            f->naerot, f->ncloudt, f->nprecpt, f->nicet, f->maerot, f->mcloudt, f->mprecpt, f->micet,
                            f->tk, f->th, f->adn, f->ustar, f->dzt, f->tlt, f->rrate, f->irate, f->sfcrrate,
                            f->sfcirate, f->VtPrc, f->VtIce}))
