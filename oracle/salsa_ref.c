@@ -13,6 +13,7 @@
  */
 #include <math.h>
 #include <float.h>
+#include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
 #include <stdio.h>
@@ -1032,6 +1033,19 @@ static void kc_copy(Cell *w, int store) {
     else memcpy(arr[q], sto, sizeof(double) * n[q]);
     sto += n[q];
   }
+}
+
+/* Per-cell reset of the working state.  The kernel arrays are cleared over the bins
+   of the layout only, as the reference's kernel arrays of those sizes are: clearing
+   their full MAXB x MAXB extent would cost more than the rest of a cell's work. */
+static void cell_clear(Cell *w, const salsa_ref_ctx_t *c) {
+  memset(w, 0, offsetof(Cell, zccaa));
+  memset(w->rate, 0, sizeof(Cell) - offsetof(Cell, rate));
+  const int a = c->nbins, k = c->ncld, p = c->nprc, i = c->nice;
+  double *arr[10] = {w->zccaa, w->zcccc, w->zccpp, w->zccii, w->zccca, w->zccpa, w->zccia, w->zccpc, w->zccic,
+                     w->zccip};
+  const int n[10] = {a * a, k * k, p * p, i * i, a * k, a * p, a * i, k * p, k * i, p * i};
+  for (int q = 0; q < 10; q++) memset(arr[q], 0, sizeof(double) * n[q]);
 }
 
 /* mo_salsa_dynamics.f90:92-202 coagulation */
@@ -2782,7 +2796,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
       int jq = (int)r;
       int kk = nzp - 2 - kq, ii = 2 + iq, jj = 2 + jq;
       long long p = kk + (long long)nzp * (ii + (long long)nxp * jj);
-      memset(w, 0, sizeof *w);
+      cell_clear(w, cc);
       w->c = cc;
       w->lcharge = lcharge;
       w->level = level;
