@@ -100,6 +100,8 @@ typedef struct {
   char listspec[SALSA_MAXSPEC][4];
   /* salsa_initialize arguments */
   double chargeTMax, chargeCollEnh;
+  /* secondary-ice subprocess switches (lssub, mo_salsa_init.f90:493-494, 675-677) */
+  salsa_switch_t lssiprimespln, lssipdropfrac, lssipicecollbreak;
   /* ---- GB300 extensions (no counterpart in the reference) ---- */
   int precision;     /* 0: FP64 (parity form); 1: FP32-mixed form */
   int diagnostics;   /* 1: accumulate process-rate diagnostics; 0: skip them */

@@ -62,6 +62,8 @@
 #define PI_FULL 3.14159265358979323846264338327
 
 #define MAXB SALSA_MAXBINS
+#define DLLIQ_RS 24.0e-6   /* mo_salsa_SIP_RS.f90:17: smallest drop that splinters on riming */
+#define DSPLINT 10.e-6     /* :21: splinter diameter */
 #define NSP  SALSA_MAXNSP
 
 static inline double sq(double x) { return x * x; }
@@ -101,11 +103,12 @@ struct salsa_ref_ctx {
   int in1a, fn1a, in2a, fn2a, in2b, fn2b;
   int ica_cur, ica_par, fca_cur, fca_par, icb_cur, icb_par, fcb_cur, fcb_par;
   Section tmpl[MAXB];
-  double precpbins[MAXB];
+  double precpbins[MAXB], icebins[MAXB];
   double massacc[MAXB];
   /* sticky switch states (mo_salsa_driver.f90:445-474) */
   int st_coag, st_cnd, st_auto, st_activ, st_icenucl, st_icemelt, st_secice, st_freeRH,
       st_freeTheta, lcgupdt;
+  int st_siprs;   /* lssiprimespln state (lssub, mo_salsa_driver.f90:458-461) */
   long long counters[5];
   Section carry[MAXB];
   int carry_valid;
@@ -124,6 +127,9 @@ typedef struct {
   double zccaa[MAXB * MAXB], zcccc[MAXB * MAXB], zccpp[MAXB * MAXB], zccii[MAXB * MAXB];
   double zccca[MAXB * MAXB], zccpa[MAXB * MAXB], zccia[MAXB * MAXB];
   double zccpc[MAXB * MAXB], zccic[MAXB * MAXB], zccip[MAXB * MAXB];
+  /* rime-splintering tallies nfrzn_rs / mfrzn_rs (mo_salsa_SIP_RS.f90:14), (nprc, nice):
+     number and mass of drops frozen onto each ice bin; cleared per cell */
+  double nfrzn_rs[MAXB * MAXB], mfrzn_rs[MAXB * MAXB];
   Rate rate[R_N];
   int lcharge, level;
   /* status flags */
@@ -538,7 +544,21 @@ static void accumulateSink(Cell *w, int nbcoll, int itrgt, int istr, int iend, c
           nrate_au50 += Eagg[ll] * xx * KIDX(zcc, nbcoll, itrgt, ll) * coll[ll].numc;
     }
   }
-  /* secondary-ice tallies (:869-977) are not built: secondary ice is out of scope */
+  /* secondary-ice tallies (:863-977) with ice collectors; of them rime splintering's
+     frozen-drop numbers (:950-975), per (precipitation bin, ice bin); drops collected from
+     cloud bins all count in row 1 */
+  if (coll[0].phase == 4 && c->st_secice) {
+    double sum = 0.;
+    for (int l = 0; l < c->nice; l++) sum += KIDX(zcc, nbcoll, itrgt, l) * coll[l].numc;
+    const double fix_coag = fmaxd(1. - sum, 0.1);
+    if (c->st_siprs && (trgtphase == 3 || trgtphase == 2)) {
+      const Section *t = trgtphase == 3 ? &w->precp[itrgt] : &w->cloud[itrgt];
+      const int row = trgtphase == 3 ? itrgt : 0;
+      for (int ll = istr; ll <= iend; ll++)
+        if (coll[ll].dwet >= t->dwet && t->dwet > DLLIQ_RS && t->numc > t->nlim && coll[ll].numc > coll[ll].nlim)
+          w->nfrzn_rs[row * c->nice + ll] += Eagg[ll] * KIDX(zcc, nbcoll, itrgt, ll) * coll[ll].numc * t->numc * fix_coag;
+    }
+  }
   if (trgtphase == 2) {
     double n = w->cloud[itrgt].numc;
     rate_acc_n(&w->rate[R_ACCR80], nrate80 * n);
@@ -657,11 +677,36 @@ static void accumulateSourceReverse(int nbcoll, int nspec, int itrgt, int istr, 
 static void accumulateSourcePhaseChange(Cell *w, int nbtrgt, int iice, int iwa, int itrgt, int istr, int iend,
                                         double rhotrgt, double rhocoll, const double *zcc, const Section *coll,
                                         double *source) {
-  int ndry = w->c->ndry;
+  const salsa_ref_ctx_t *c = w->c;
+  int ndry = c->ndry;
   for (int ll = istr; ll <= iend; ll++) {
     double k = KIDX(zcc, nbtrgt, ll, itrgt);
     for (int s = 0; s < ndry; s++) source[s] += k * coll[ll].volc[s];
     source[iice] += k * coll[ll].volc[iwa] * rhocoll / rhotrgt;
+  }
+  /* secondary-ice tallies (:1285-1378).  With lssecice on, the ice target's diameters are
+     updated here (:1291-1308), whichever scheme runs; of the tallies, rime splintering's
+     frozen-drop masses (:1354-1375), where drops collected from cloud bins use the kernel
+     of cloud bin 1 (ix = 1), as written */
+  if (c->st_secice) {
+    double fix_coag = 1.;
+    const int nb = coll[0].phase == 2 ? c->ncld : (coll[0].phase == 3 ? c->nprc : (coll[0].phase == 4 ? c->nice : 0));
+    if (nb > 0) {
+      double sum = 0.;
+      for (int l = 0; l < nb; l++) sum += KIDX(zcc, nbtrgt, l, itrgt) * coll[l].numc;
+      fix_coag = fmaxd(1. - sum, 0.1);
+      updateDiameter(c, &w->ice[itrgt], 1, T_ALL);
+    }
+    if (c->st_siprs)
+      for (int ll = istr; ll <= iend; ll++) {
+        const int ph = coll[ll].phase;
+        if (ph != 2 && ph != 3) continue;
+        if (coll[ll].dwet >= DLLIQ_RS && coll[ll].dwet < w->ice[itrgt].dnsp) {
+          const int ix = ph == 3 ? ll : 0;
+          w->mfrzn_rs[ix * c->nice + itrgt] +=
+              KIDX(zcc, nbtrgt, ix, itrgt) * coll[ll].volc[iwa] * w->ice[itrgt].numc * rhocoll * fix_coag;
+        }
+      }
   }
 }
 
@@ -1046,6 +1091,8 @@ static void cell_clear(Cell *w, const salsa_ref_ctx_t *c) {
                      w->zccip};
   const int n[10] = {a * a, k * k, p * p, i * i, a * k, a * p, a * i, k * p, k * i, p * i};
   for (int q = 0; q < 10; q++) memset(arr[q], 0, sizeof(double) * n[q]);
+  memset(w->nfrzn_rs, 0, sizeof(double) * p * i);
+  memset(w->mfrzn_rs, 0, sizeof(double) * p * i);
 }
 
 /* mo_salsa_dynamics.f90:92-202 coagulation */
@@ -2496,6 +2543,80 @@ static void condgas(Cell *w, double *pcsa, double *pcocnv, double *pcocsv, doubl
 }
 
 /* ======================================================================
+ * Secondary ice: mo_salsa_secondary_ice.f90:6-40 -> rime splintering,
+ * mo_salsa_SIP_RS.f90:28-215 (Hallett and Mossop 1974; Mossop 1976)
+ * ====================================================================== */
+/* :247-270 rs_halletmossop (splinters per kg of rime) and :276-299 rs_mossop (per frozen
+   drop), with dltemp_rs = 5: no temperature dependence */
+static double rs_splinters(int mode, double mfrzn, double nfrzn) {
+  return mode == 1 ? 3.5E8 * mfrzn : 4.0E-3 * nfrzn;
+}
+
+static void rimesplintering(Cell *w, double ptemp, double ptstep) {
+  const salsa_ref_ctx_t *c = w->c;
+  const int nprc = c->nprc, nice = c->nice, nspec = c->nused, mode = c->cfg.lssiprimespln.mode;
+  const double tmin = 238.15, tmax = 273.15;
+  const double v_i = 3.405365461487051e-16;   /* a 10 um hexagonal column of bulk ice */
+  Section *ice = w->ice;
+  int splbin = 0;                             /* :72, 1-based */
+  for (int bb = 0; bb < nice; bb++) splbin += c->icebins[bb] < DSPLINT;
+  if (splbin < 1) splbin = 1;
+  for (int e = 0; e < nprc * nice; e++) {
+    w->mfrzn_rs[e] = w->mfrzn_rs[e] * ptstep;
+    w->nfrzn_rs[e] = w->nfrzn_rs[e] * ptstep;
+  }
+  double fragvolc[MAXB][NSP], sinkvolc[MAXB][NSP], fragnumc[MAXB], sinknumc[MAXB], sinkv[NSP];
+  memset(fragvolc, 0, sizeof fragvolc); memset(sinkvolc, 0, sizeof sinkvolc);
+  memset(fragnumc, 0, sizeof fragnumc); memset(sinknumc, 0, sizeof sinknumc);
+  for (int bb = 0; bb < nice; bb++) {
+    double vall = 0.;
+    for (int s = 0; s < NSP; s++) vall += ice[bb].volc[s];
+    for (int cc = 0; cc < nprc; cc++) {
+      const double nf = w->nfrzn_rs[cc * nice + bb], mf = w->mfrzn_rs[cc * nice + bb];
+      if (ptemp < tmin || ptemp > tmax || nf < 1.e-12 || vall < 1.e-15 || ice[bb].numc < ice[bb].nlim ||
+          bb + 1 < splbin + 2)
+        continue;
+      const double ddmean = pow(mf / nf / c->rhowa / PI6, 1. / 3.);
+      if (ddmean < DLLIQ_RS) continue;
+      const double dN = rs_splinters(mode, mf, nf);
+      const double dV = dN * v_i;
+      fragnumc[splbin - 1] = fragnumc[splbin - 1] + dN;
+      double sv = 0.;
+      for (int s = 0; s < nspec; s++) sv += ice[bb].volc[s];
+      for (int s = 0; s < nspec; s++)
+        fragvolc[splbin - 1][s] = fragvolc[splbin - 1][s] + ice[bb].volc[s] * fmind(dV / sv, 1.);
+      for (int s = 0; s < nspec; s++) sinkv[s] = ice[bb].volc[s] * fmind(dV / sv, 1.0);
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = sinkvolc[bb][s] + sinkv[s];
+      double ss = 0.;
+      for (int s = 0; s < nspec; s++) ss += sinkv[s];
+      sinknumc[bb] = sinknumc[bb] + ss / (PI6 * pow(ddmean, 3.0));
+    }
+    if (ice[bb].numc < sinknumc[bb]) {                       /* :152-158 */
+      sinknumc[bb] = ice[bb].numc;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = ice[bb].volc[s];
+    }
+    double ssk = 0., sv = 0.;                                /* :160-168: the fragments keep their volume */
+    for (int s = 0; s < nspec; s++) { ssk += sinkvolc[bb][s]; sv += ice[bb].volc[s]; }
+    if (ssk > sv) {
+      const double frconst = 0.99 * sv / ssk;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = sinkvolc[bb][s] * frconst;
+      sinknumc[bb] = sinknumc[bb] * frconst;
+      sinknumc[bb] = fmind(sinknumc[bb], 0.99 * ice[bb].numc);
+    }
+  }
+  for (int bb = 0; bb < nice; bb++) {                        /* :194-201 */
+    ice[bb].numc = ice[bb].numc + fragnumc[bb];
+    ice[bb].numc = ice[bb].numc - sinknumc[bb];
+    ice[bb].numc = fmaxd(0., ice[bb].numc);
+    for (int s = 0; s < nspec; s++) {
+      ice[bb].volc[s] = ice[bb].volc[s] + fragvolc[bb][s];
+      ice[bb].volc[s] = ice[bb].volc[s] - sinkvolc[bb][s];
+      ice[bb].volc[s] = fmaxd(0., ice[bb].volc[s]);
+    }
+  }
+}
+
+/* ======================================================================
  * mo_salsa.f90:45-153 salsa
  * ====================================================================== */
 static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double prsi, double ptemp, double ptstep,
@@ -2503,6 +2624,7 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
   const salsa_ref_ctx_t *c = w->c;
   const salsa_config_t *g = &c->cfg;
   if (c->st_coag) coagulation(w, ptstep, ptemp, ppres);
+  if (c->st_secice && c->st_siprs) rimesplintering(w, ptemp, ptstep);   /* :98-99 */
   if (c->st_cnd) {
     /* condensation :276-342.  nucleation (mo_salsa_nucleation.f90:72-625) only returns the
        3 nm formation rates, which condgas does not read (see condgas), and the H2SO4
@@ -2563,7 +2685,12 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (!cfg || !out) return SALSA_E_ARG;
   if (cfg->nbin[0] < 1 || cfg->nbin[1] < 4 || cfg->prc_nbins < 1 || cfg->ice_nbins < 1) return SALSA_E_ARG;
   if (cfg->nspec_dry < 1 || cfg->nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
-  if (cfg->lssecice.sw) return SALSA_E_UNSUPPORTED;
+  /* secondary ice (mo_salsa_secondary_ice.f90:6-40): rime splintering (mo_salsa_SIP_RS.f90)
+     in its two modes; drop fracturing and ice-ice breakup are not restated */
+  if (cfg->lssecice.sw && cfg->level == 5 &&
+      (cfg->lssipdropfrac.sw || cfg->lssipicecollbreak.sw ||
+       (cfg->lssiprimespln.sw && cfg->lssiprimespln.mode != 1 && cfg->lssiprimespln.mode != 2)))
+    return SALSA_E_UNSUPPORTED;
   /* nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
      nj3 outside 1-3 STOPs once a cell nucleates (:600-602) */
   if (cfg->nsnucl == 4 || cfg->nsnucl < 0 || (cfg->nsnucl > 0 && (cfg->nj3 < 1 || cfg->nj3 > 3)))
@@ -2683,6 +2810,7 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
     }
   }
   for (int i = 0; i < c->nprc; i++) c->precpbins[i] = pow(pr[i].vlolim / PI6, 1. / 3.);
+  for (int i = 0; i < c->nice; i++) c->icebins[i] = pow(ic[i].vlolim / PI6, 1. / 3.);   /* set_icebins :420-423 */
   for (int i = 0; i < c->nbins; i++) c->massacc[i] = 1.;
   *out = c;
   return SALSA_OK;
@@ -2739,6 +2867,8 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
     if (lvl4 && (i == 4 || i == 5 || i == 6)) sw = 0;    /* define_salsa :615-635 */
     if (sw && time >= ms[i]->delay) *sts[i] = 1;
   }
+  /* subprocess switches; define_salsa switches them off at level 4 (:631-633) */
+  if (!lvl4 && g->lssiprimespln.sw && time >= g->lssiprimespln.delay) c->st_siprs = 1;
   if (g->lsfreeRH.sw && time > g->lsfreeRH.delay) c->st_freeRH = 1;
   if (g->lsFreeTheta.sw && time > g->lsFreeTheta.delay) c->st_freeTheta = 1;
   c->lcgupdt = (c->st_coag && g->lscoag.mode == 2 && (fmod(time, g->cgintvl) < tstep || istp <= 1));

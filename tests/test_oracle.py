@@ -338,9 +338,19 @@ def test_reference_scheme_is_ill_conditioned_in_aitken_water():
 def test_unsupported_and_bad_configs():
     import ctypes as C
     from uclales_salsa_gb300.capi import Config
-    for mod, code in ((lambda c: setattr(c, "nsnucl", 4), 2), (lambda c: setattr(c.lssecice, "sw", 1), 2),
+    def sip(sub, mode=1):
+        def m(c):
+            c.lssecice.sw = 1
+            getattr(c, sub).sw, getattr(c, sub).mode = 1, mode
+        return m
+    # secondary ice: rime splintering (modes 1, 2) is restated; drop fracturing and
+    # ice-ice breakup are not
+    for mod, code in ((lambda c: setattr(c, "nsnucl", 4), 2), (sip("lssipdropfrac"), 2),
+                      (sip("lssipicecollbreak"), 2), (sip("lssiprimespln", 3), 2), (sip("lssiprimespln", 1), 0),
                       (lambda c: setattr(c, "nspec_dry", 0), 1), (lambda c: c.set_species(["SO4", "XX"]), 1)):
         cfg = workload_config(5)
         mod(cfg)
         h = C.c_void_p()
         assert lib().salsa_ref_create(C.byref(cfg), C.byref(h)) == code
+        if code == 0:
+            lib().salsa_ref_destroy(h)

@@ -1,0 +1,62 @@
+"""Rime splintering (mo_salsa_SIP_RS.f90, through mo_salsa_secondary_ice.f90) in the
+oracle: the properties of the reference's scheme.  Secondary ice is not built on the
+GPU (salsa_gb300_init refuses lssecice); these tests pin the oracle's restatement."""
+import pytest
+import torch
+
+from uclales_salsa_gb300.inputs import make_outputs
+from oracle_ref import Oracle
+from parity import interior
+from sip_cases import sip_state
+
+
+def _step(inp):
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    out = make_outputs(inp)
+    rc, st = Oracle(inp.cfg).run(inp, f, out, time=1.0)
+    assert rc == 0, st.as_dict()
+    I = lambda t: interior(t, inp.nzp, inp.nxp, inp.nyp)
+    new = {k: I(f[k] + out[t] * inp.dt) for k, t in (("nice", "nicet"), ("mice", "micet"), ("nprecp", "nprecpt"),
+                                                    ("ncloud", "ncloudt"))}
+    return new, I(inp.fields["temp"])
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_splinters_conserve_ice_volume_and_add_crystals(mode):
+    """With coagulation alone, the scheme moves rime-ice volume from the riming bins to
+    the splinter bin (ice volume per species conserved) and adds crystals."""
+    a, T = _step(sip_state(mode, splinter=False))
+    b, _ = _step(sip_state(mode, splinter=True))
+    inp = sip_state(mode)
+    lay = inp.layout
+    nw1, nic = lay.nwet + 1, lay.nice
+    ma = a["mice"].view(nw1, nic, *a["mice"].shape[1:]).sum(1)
+    mb = b["mice"].view(nw1, nic, *b["mice"].shape[1:]).sum(1)
+    scale = ma.abs().amax(0).clamp(min=1e-30)
+    assert float(((mb - ma).abs() / scale).max()) < 1e-12
+    dn = b["nice"].sum(0) - a["nice"].sum(0)
+    assert float(dn.min()) >= -1e-12 * float(a["nice"].sum(0).max())
+    assert int((dn > 0).sum()) > 5
+    # the splinters land in the first ice bin (10 um is below every bin's lower limit)
+    assert float((b["nice"][0] - a["nice"][0]).max()) > 0
+    # the other categories are untouched by the scheme itself
+    assert torch.equal(a["nprecp"], b["nprecp"]) and torch.equal(a["ncloud"], b["ncloud"])
+
+
+def test_no_splinters_outside_the_temperature_range():
+    """Rime splintering acts between 238.15 K and 273.15 K only (:64-66)."""
+    a, T = _step(sip_state(1, splinter=False))
+    b, _ = _step(sip_state(1, splinter=True))
+    out = (T < 238.15) | (T > 273.15)
+    assert int(out.sum()) > 0
+    for k in ("nice", "mice"):
+        assert torch.equal(a[k][:, out], b[k][:, out]), k
+
+
+def test_hallett_mossop_counts_rime_mass_and_mossop_counts_drops():
+    """Mode 1 makes 3.5e8 splinters per kg of rime, mode 2 one per 250 frozen drops:
+    for the same collisions mode 1 gives far more splinters here (drops of ~1e-9 kg)."""
+    a, _ = _step(sip_state(1, splinter=False))
+    d1 = _step(sip_state(1))[0]["nice"].sum(0) - a["nice"].sum(0)
+    d2 = _step(sip_state(2))[0]["nice"].sum(0) - a["nice"].sum(0)
+    assert float(d1.sum()) > 100 * float(d2.sum()) > 0

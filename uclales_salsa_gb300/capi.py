@@ -62,6 +62,7 @@ class Config(C.Structure):
         ("nspec_dry", C.c_int),
         ("listspec", (C.c_char * 4) * MAXSPEC),
         ("chargeTMax", C.c_double), ("chargeCollEnh", C.c_double),
+        ("lssiprimespln", Switch), ("lssipdropfrac", Switch), ("lssipicecollbreak", Switch),
         ("precision", C.c_int),
         ("diagnostics", C.c_int),
     ]

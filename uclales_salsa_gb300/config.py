@@ -23,7 +23,7 @@ def reference_defaults(level=5):
     c = Config()
     c.level = level
     for name in ("lscoag", "lscnd", "lsauto", "lsactiv", "lsicenucl", "lsicemelt", "lssecice",
-                 "lsFreeTheta", "lsfreeRH"):
+                 "lsFreeTheta", "lsfreeRH", "lssiprimespln", "lssipdropfrac", "lssipicecollbreak"):
         _sw(getattr(c, name), False)
     for name in ("lscgaa", "lscgcc", "lscgca", "lscgpc", "lscgpa", "lscgpp", "lscgia", "lscgic",
                  "lscgii", "lscgip"):

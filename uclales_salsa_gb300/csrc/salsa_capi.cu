@@ -167,6 +167,7 @@ void salsa_gb300_default_config(salsa_config_t *c) {
   salsa_switch_t off = {0, 0., 1};
   c->lscoag = c->lscnd = c->lsauto = c->lsactiv = c->lsicenucl = c->lsicemelt = c->lssecice = off;
   c->lsFreeTheta = c->lsfreeRH = off;
+  c->lssiprimespln = c->lssipdropfrac = c->lssipicecollbreak = off;
   c->lscgaa = c->lscgcc = c->lscgca = c->lscgpc = c->lscgpa = c->lscgpp = 1;
   c->lscgia = c->lscgic = c->lscgii = c->lscgip = 1;
   c->Eiagg_max = 0.3;
