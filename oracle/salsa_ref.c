@@ -64,6 +64,7 @@
 #define MAXB SALSA_MAXBINS
 #define DLLIQ_RS 24.0e-6   /* mo_salsa_SIP_RS.f90:17: smallest drop that splinters on riming */
 #define DSPLINT 10.e-6     /* :21: splinter diameter */
+#define DLLIQ_DF 100.e-6   /* mo_salsa_SIP_DF.f90:18: smallest drop that fractures on freezing */
 #define NSP  SALSA_MAXNSP
 
 static inline double sq(double x) { return x * x; }
@@ -108,7 +109,7 @@ struct salsa_ref_ctx {
   /* sticky switch states (mo_salsa_driver.f90:445-474) */
   int st_coag, st_cnd, st_auto, st_activ, st_icenucl, st_icemelt, st_secice, st_freeRH,
       st_freeTheta, lcgupdt;
-  int st_siprs;   /* lssiprimespln state (lssub, mo_salsa_driver.f90:458-461) */
+  int st_siprs, st_sipdf;   /* lssiprimespln, lssipdropfrac states (lssub, mo_salsa_driver.f90:458-461) */
   long long counters[5];
   Section carry[MAXB];
   int carry_valid;
@@ -130,6 +131,7 @@ typedef struct {
   /* rime-splintering tallies nfrzn_rs / mfrzn_rs (mo_salsa_SIP_RS.f90:14), (nprc, nice):
      number and mass of drops frozen onto each ice bin; cleared per cell */
   double nfrzn_rs[MAXB * MAXB], mfrzn_rs[MAXB * MAXB];
+  double nfrzn_df[MAXB * MAXB], mfrzn_df[MAXB * MAXB];   /* drop fracturing's (mo_salsa_SIP_DF.f90:15) */
   Rate rate[R_N];
   int lcharge, level;
   /* status flags */
@@ -544,13 +546,23 @@ static void accumulateSink(Cell *w, int nbcoll, int itrgt, int istr, int iend, c
           nrate_au50 += Eagg[ll] * xx * KIDX(zcc, nbcoll, itrgt, ll) * coll[ll].numc;
     }
   }
-  /* secondary-ice tallies (:863-977) with ice collectors; of them rime splintering's
-     frozen-drop numbers (:950-975), per (precipitation bin, ice bin); drops collected from
-     cloud bins all count in row 1 */
+  /* secondary-ice tallies (:863-977) with ice collectors; of them drop fracturing's and
+     rime splintering's frozen-drop numbers, per (precipitation bin, ice bin); drops
+     collected from cloud bins all count in row 1 */
   if (coll[0].phase == 4 && c->st_secice) {
     double sum = 0.;
     for (int l = 0; l < c->nice; l++) sum += KIDX(zcc, nbcoll, itrgt, l) * coll[l].numc;
     const double fix_coag = fmaxd(1. - sum, 0.1);
+    /* drop fracturing (:899-944): drops larger than the collecting crystal (mode 4 would
+       count the others too); the drop bin's own numbers are tested twice, as written */
+    if (c->st_sipdf && (trgtphase == 3 || trgtphase == 2)) {
+      const Section *t = trgtphase == 3 ? &w->precp[itrgt] : &w->cloud[itrgt];
+      const int row = trgtphase == 3 ? itrgt : 0;
+      for (int ll = istr; ll <= iend; ll++)
+        if (coll[ll].numc > coll[ll].nlim && coll[ll].dwet < t->dwet && t->dwet > DLLIQ_DF && t->numc > t->nlim &&
+            coll[ll].numc > coll[ll].nlim)
+          w->nfrzn_df[row * c->nice + ll] += Eagg[ll] * KIDX(zcc, nbcoll, itrgt, ll) * coll[ll].numc * t->numc * fix_coag;
+    }
     if (c->st_siprs && (trgtphase == 3 || trgtphase == 2)) {
       const Section *t = trgtphase == 3 ? &w->precp[itrgt] : &w->cloud[itrgt];
       const int row = trgtphase == 3 ? itrgt : 0;
@@ -697,6 +709,17 @@ static void accumulateSourcePhaseChange(Cell *w, int nbtrgt, int iice, int iwa, 
       fix_coag = fmaxd(1. - sum, 0.1);
       updateDiameter(c, &w->ice[itrgt], 1, T_ALL);
     }
+    if (c->st_sipdf)   /* :1312-1346: drops larger than the crystal */
+      for (int ll = istr; ll <= iend; ll++) {
+        const int ph = coll[ll].phase;
+        if (ph != 2 && ph != 3) continue;
+        if (w->ice[itrgt].dnsp < coll[ll].dwet && coll[ll].dwet > DLLIQ_DF && w->ice[itrgt].numc > w->ice[itrgt].nlim &&
+            coll[ll].numc > coll[ll].nlim) {
+          const int ix = ph == 3 ? ll : 0;
+          w->mfrzn_df[ix * c->nice + itrgt] +=
+              KIDX(zcc, nbtrgt, ix, itrgt) * coll[ll].volc[iwa] * w->ice[itrgt].numc * rhocoll * fix_coag;
+        }
+      }
     if (c->st_siprs)
       for (int ll = istr; ll <= iend; ll++) {
         const int ph = coll[ll].phase;
@@ -1093,6 +1116,8 @@ static void cell_clear(Cell *w, const salsa_ref_ctx_t *c) {
   for (int q = 0; q < 10; q++) memset(arr[q], 0, sizeof(double) * n[q]);
   memset(w->nfrzn_rs, 0, sizeof(double) * p * i);
   memset(w->mfrzn_rs, 0, sizeof(double) * p * i);
+  memset(w->nfrzn_df, 0, sizeof(double) * p * i);
+  memset(w->mfrzn_df, 0, sizeof(double) * p * i);
 }
 
 /* mo_salsa_dynamics.f90:92-202 coagulation */
@@ -2616,6 +2641,107 @@ static void rimesplintering(Cell *w, double ptemp, double ptstep) {
   }
 }
 
+/* mo_salsa_SIP_DF.f90:370-398 df_lawson (mode 1), df_sullivan (mode 2), df_phillips_simple
+   (mode 3): fragments from nfrzn frozen drops of mean diameter ddmean */
+static double df_fragments(int mode, double T, double nfrzn, double ddmean) {
+  if (mode == 1) return nfrzn * 2.5e-11 * pow(fmind(ddmean, 3.e-3) * 1.e6, 4.);
+  if (mode == 2) {
+    const double hT = f_gauss(T, 10., 258.) / f_gauss(258., 10., 258.);
+    return nfrzn * 0.2 * hT * 2.5e-11 * pow(fmind(ddmean, 3.e-3) * 1.e6, 4.);
+  }
+  const double tl[5] = {-24. + 273.15, -20. + 273.15, -16. + 273.15, -10. + 273.15, -6. + 273.15};
+  const double hv[5] = {0.6, 0.24, 2.6, 0.43, 0.35};
+  double hT = 0.;
+  if (T >= tl[0] && T < tl[1]) hT = (hv[1] - hv[0]) * ((T - tl[0]) / 4.) + hv[0];
+  else if (T >= tl[1] && T < tl[2]) hT = (hv[2] - hv[1]) * ((T - tl[2]) / 4.) + hv[2];
+  else if (T >= tl[2] && T < tl[3]) hT = (hv[3] - hv[2]) * ((T - tl[3]) / 6.) + hv[3];
+  else if (T >= tl[3] && T < tl[4]) hT = (hv[4] - hv[3]) * ((T - tl[4]) / 4.) + hv[4];
+  return nfrzn * ((4. / 9.) * 1.e4 * hT * ddmean);
+}
+
+/* mo_salsa_SIP_DF.f90:29-260 dropfracturing (per cell): the fragments of each frozen
+   drop size go to the ice bins below it with a d^-3 number distribution */
+static void dropfracturing(Cell *w, double ptemp, double ptstep) {
+  const salsa_ref_ctx_t *c = w->c;
+  const int nprc = c->nprc, nice = c->nice, nspec = c->nused, mode = c->cfg.lssipdropfrac.mode;
+  const double tmin = 248.15, tmax = 271.15;
+  Section *ice = w->ice;
+  double icediams[MAXB], icebw[MAXB];
+  for (int bb = 0; bb < nice; bb++) {
+    icediams[bb] = ice[bb].dmid;
+    icebw[bb] = pow(ice[bb].vhilim / PI6, 1. / 3) - pow(ice[bb].vlolim / PI6, 1. / 3);
+  }
+  for (int e = 0; e < nprc * nice; e++) {
+    w->mfrzn_df[e] = w->mfrzn_df[e] * ptstep;
+    w->nfrzn_df[e] = w->nfrzn_df[e] * ptstep;
+  }
+  double fragvolc[MAXB][NSP], sinkvolc[MAXB][NSP], fragnumc[MAXB], sinknumc[MAXB];
+  double fragv_loc[MAXB][NSP], fragn_loc[MAXB], sinkv[NSP], dNb[MAXB], dVb[MAXB];
+  memset(fragvolc, 0, sizeof fragvolc); memset(sinkvolc, 0, sizeof sinkvolc);
+  memset(fragnumc, 0, sizeof fragnumc); memset(sinknumc, 0, sizeof sinknumc);
+  for (int bb = 0; bb < nice; bb++) {
+    memset(fragv_loc, 0, sizeof fragv_loc); memset(fragn_loc, 0, sizeof fragn_loc);
+    double vall = 0.;
+    for (int s = 0; s < NSP; s++) vall += ice[bb].volc[s];
+    for (int cc = 0; cc < nprc; cc++) {
+      const double nf = w->nfrzn_df[cc * nice + bb], mf = w->mfrzn_df[cc * nice + bb];
+      if (ptemp < tmin || ptemp > tmax || nf < 1.e-12 || vall < 1.e-15 || ice[bb].numc < ice[bb].nlim) continue;
+      const double ddmean = pow(mf / nf / c->rhowa / PI6, 1. / 3.);
+      if (ddmean < DLLIQ_DF) continue;
+      int npmax = 0;                                        /* :122, 1-based count */
+      for (int k = 0; k < nice; k++) npmax += icediams[k] <= ddmean;
+      npmax = npmax - 1 > 1 ? npmax - 1 : 1;
+      if (npmax <= 2) continue;
+      const double dN = df_fragments(mode, ptemp, nf, ddmean);
+      for (int k = 0; k < nice; k++) dNb[k] = dVb[k] = 0.;
+      double Nnorm = 0.;
+      for (int k = 0; k < npmax; k++) dNb[k] = 1. / cube(icediams[k]);
+      for (int k = 0; k < npmax; k++) Nnorm += dNb[k] * icebw[k];
+      for (int k = 0; k < npmax; k++) dNb[k] = dN * dNb[k] * icebw[k] / Nnorm;
+      for (int k = 0; k < npmax; k++) dVb[k] = dNb[k] * PI6 * cube(icediams[k]);
+      double sv = 0., sdv = 0.;
+      for (int s = 0; s < nspec; s++) sv += ice[bb].volc[s];
+      for (int k = 0; k < npmax; k++) sdv += dVb[k];
+      for (int k = 0; k < npmax; k++) {
+        fragn_loc[k] = fragn_loc[k] + dNb[k];
+        for (int s = 0; s < nspec; s++) fragv_loc[k][s] = fragv_loc[k][s] + ice[bb].volc[s] * (dVb[k] / sv);
+      }
+      for (int s = 0; s < nspec; s++) sinkv[s] = ice[bb].volc[s] * sdv / sv;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = sinkvolc[bb][s] + sinkv[s];
+      const double v_i = mf / nf / c->rhowa;
+      double ss = 0.;
+      for (int s = 0; s < nspec; s++) ss += sinkv[s];
+      sinknumc[bb] = sinknumc[bb] + ss / v_i;
+    }
+    for (int k = 0; k < nice; k++) {                        /* :175-176, before the safeguard */
+      fragnumc[k] = fragnumc[k] + fragn_loc[k];
+      for (int s = 0; s < NSP; s++) fragvolc[k][s] = fragvolc[k][s] + fragv_loc[k][s];
+    }
+    if (ice[bb].numc < sinknumc[bb]) {                      /* :183-189 */
+      sinknumc[bb] = ice[bb].numc;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = ice[bb].volc[s];
+    }
+    double ssk = 0., sv = 0.;                               /* :191-199: fragments already added */
+    for (int s = 0; s < nspec; s++) { ssk += sinkvolc[bb][s]; sv += ice[bb].volc[s]; }
+    if (ssk > sv) {
+      const double frconst = 0.99 * sv / ssk;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = sinkvolc[bb][s] * frconst;
+      sinknumc[bb] = sinknumc[bb] * frconst;
+      sinknumc[bb] = fmind(sinknumc[bb], 0.99 * ice[bb].numc);
+    }
+  }
+  for (int bb = 0; bb < nice; bb++) {                       /* :230-237 */
+    ice[bb].numc = ice[bb].numc + fragnumc[bb];
+    ice[bb].numc = ice[bb].numc - sinknumc[bb];
+    ice[bb].numc = fmaxd(0., ice[bb].numc);
+    for (int s = 0; s < nspec; s++) {
+      ice[bb].volc[s] = ice[bb].volc[s] + fragvolc[bb][s];
+      ice[bb].volc[s] = ice[bb].volc[s] - sinkvolc[bb][s];
+      ice[bb].volc[s] = fmaxd(0., ice[bb].volc[s]);
+    }
+  }
+}
+
 /* ======================================================================
  * mo_salsa.f90:45-153 salsa
  * ====================================================================== */
@@ -2624,7 +2750,10 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
   const salsa_ref_ctx_t *c = w->c;
   const salsa_config_t *g = &c->cfg;
   if (c->st_coag) coagulation(w, ptstep, ptemp, ppres);
-  if (c->st_secice && c->st_siprs) rimesplintering(w, ptemp, ptstep);   /* :98-99 */
+  if (c->st_secice) {                                                   /* :98-99 */
+    if (c->st_siprs) rimesplintering(w, ptemp, ptstep);
+    if (c->st_sipdf) dropfracturing(w, ptemp, ptstep);
+  }
   if (c->st_cnd) {
     /* condensation :276-342.  nucleation (mo_salsa_nucleation.f90:72-625) only returns the
        3 nm formation rates, which condgas does not read (see condgas), and the H2SO4
@@ -2686,10 +2815,12 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (cfg->nbin[0] < 1 || cfg->nbin[1] < 4 || cfg->prc_nbins < 1 || cfg->ice_nbins < 1) return SALSA_E_ARG;
   if (cfg->nspec_dry < 1 || cfg->nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
   /* secondary ice (mo_salsa_secondary_ice.f90:6-40): rime splintering (mo_salsa_SIP_RS.f90)
-     in its two modes; drop fracturing and ice-ice breakup are not restated */
+     in its two modes and drop fracturing (mo_salsa_SIP_DF.f90) in modes 1-3; Phillips'
+     full drop-fracturing scheme (mode 4) and ice-ice breakup are not restated */
   if (cfg->lssecice.sw && cfg->level == 5 &&
-      (cfg->lssipdropfrac.sw || cfg->lssipicecollbreak.sw ||
-       (cfg->lssiprimespln.sw && cfg->lssiprimespln.mode != 1 && cfg->lssiprimespln.mode != 2)))
+      (cfg->lssipicecollbreak.sw ||
+       (cfg->lssiprimespln.sw && cfg->lssiprimespln.mode != 1 && cfg->lssiprimespln.mode != 2) ||
+       (cfg->lssipdropfrac.sw && (cfg->lssipdropfrac.mode < 1 || cfg->lssipdropfrac.mode > 3))))
     return SALSA_E_UNSUPPORTED;
   /* nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
      nj3 outside 1-3 STOPs once a cell nucleates (:600-602) */
@@ -2869,6 +3000,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
   }
   /* subprocess switches; define_salsa switches them off at level 4 (:631-633) */
   if (!lvl4 && g->lssiprimespln.sw && time >= g->lssiprimespln.delay) c->st_siprs = 1;
+  if (!lvl4 && g->lssipdropfrac.sw && time >= g->lssipdropfrac.delay) c->st_sipdf = 1;
   if (g->lsfreeRH.sw && time > g->lsfreeRH.delay) c->st_freeRH = 1;
   if (g->lsFreeTheta.sw && time > g->lsFreeTheta.delay) c->st_freeTheta = 1;
   c->lcgupdt = (c->st_coag && g->lscoag.mode == 2 && (fmod(time, g->cgintvl) < tstep || istp <= 1));

@@ -1,4 +1,4 @@
-"""States for the secondary-ice (rime splintering) oracle tests.
+"""States for the secondary-ice (rime splintering, drop fracturing) oracle tests.
 
 A block of the 256x256x128 workload (cloud droplets and drops in 30 % of the cells,
 T 240-275 K) with ice seeded in the cloudy cells.  The ice bins take the reference's
@@ -11,7 +11,7 @@ from uclales_salsa_gb300.inputs import make_inputs, PI6
 from uclales_salsa_gb300.layout import build_layout
 
 
-def sip_state(mode, splinter=True, coag_only=True, seed=7, X=6, Y=6, Z=8):
+def sip_state(mode, splinter=True, coag_only=True, seed=7, X=6, Y=6, Z=8, scheme="lssiprimespln"):
     inp = make_inputs("grid256x256x128", "cpu", X=X, Y=Y, Z=Z)
     cfg = inp.cfg
     cfg.ice_nbins, cfg.ice_dlo, cfg.ice_vol_ratio = 7, 20e-6, 8.0
@@ -38,6 +38,7 @@ def sip_state(mode, splinter=True, coag_only=True, seed=7, X=6, Y=6, Z=8):
         for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
             sw.sw = 0
     cfg.lssecice.sw = int(splinter)
-    cfg.lssiprimespln.sw = int(splinter)
-    cfg.lssiprimespln.mode = mode
+    sw = getattr(cfg, scheme)
+    sw.sw = int(splinter)
+    sw.mode = mode
     return inp

@@ -1,5 +1,6 @@
-"""Rime splintering (mo_salsa_SIP_RS.f90, through mo_salsa_secondary_ice.f90) in the
-oracle: the properties of the reference's scheme.  Secondary ice is not built on the
+"""Rime splintering (mo_salsa_SIP_RS.f90) and drop fracturing (mo_salsa_SIP_DF.f90),
+through mo_salsa_secondary_ice.f90, in the oracle: the properties of the reference's
+schemes.  Secondary ice is not built on the
 GPU (salsa_gb300_init refuses lssecice); these tests pin the oracle's restatement."""
 import pytest
 import torch
@@ -60,3 +61,24 @@ def test_hallett_mossop_counts_rime_mass_and_mossop_counts_drops():
     d1 = _step(sip_state(1))[0]["nice"].sum(0) - a["nice"].sum(0)
     d2 = _step(sip_state(2))[0]["nice"].sum(0) - a["nice"].sum(0)
     assert float(d1.sum()) > 100 * float(d2.sum()) > 0
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_drop_fracturing_conserves_ice_volume_and_adds_small_crystals(mode):
+    """Frozen drops above 100 um shatter into fragments spread over the ice bins below
+    their size: ice volume per species conserved, crystals added, small bins gain."""
+    kw = dict(scheme="lssipdropfrac")
+    a, T = _step(sip_state(mode, splinter=False, **kw))
+    b, _ = _step(sip_state(mode, **kw))
+    lay = sip_state(mode, **kw).layout
+    nw1, nic = lay.nwet + 1, lay.nice
+    ma = a["mice"].view(nw1, nic, *a["mice"].shape[1:]).sum(1)
+    mb = b["mice"].view(nw1, nic, *b["mice"].shape[1:]).sum(1)
+    scale = ma.abs().amax(0).clamp(min=1e-30)
+    assert float(((mb - ma).abs() / scale).max()) < 1e-12
+    dn = b["nice"].sum(0) - a["nice"].sum(0)
+    assert int((dn > 0).sum()) > 5
+    assert float((b["nice"][0] - a["nice"][0]).max()) > 0
+    out = (T < 248.15) | (T > 271.15)             # the scheme's range (:56)
+    assert int(out.sum()) > 0
+    assert torch.equal(a["nice"][:, out], b["nice"][:, out])
