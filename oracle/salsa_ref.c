@@ -109,7 +109,8 @@ struct salsa_ref_ctx {
   /* sticky switch states (mo_salsa_driver.f90:445-474) */
   int st_coag, st_cnd, st_auto, st_activ, st_icenucl, st_icemelt, st_secice, st_freeRH,
       st_freeTheta, lcgupdt;
-  int st_siprs, st_sipdf;   /* lssiprimespln, lssipdropfrac states (lssub, mo_salsa_driver.f90:458-461) */
+  int st_siprs, st_sipdf, st_sipib;   /* lssiprimespln, lssipdropfrac, lssipicecollbreak states
+                                          (lssub, mo_salsa_driver.f90:458-461) */
   long long counters[5];
   Section carry[MAXB];
   int carry_valid;
@@ -132,6 +133,7 @@ typedef struct {
      number and mass of drops frozen onto each ice bin; cleared per cell */
   double nfrzn_rs[MAXB * MAXB], mfrzn_rs[MAXB * MAXB];
   double nfrzn_df[MAXB * MAXB], mfrzn_df[MAXB * MAXB];   /* drop fracturing's (mo_salsa_SIP_DF.f90:15) */
+  double nii_ibr[MAXB * MAXB], mii_ibr[MAXB * MAXB];     /* ice-ice breakup's (mo_salsa_SIP_IIBR.f90:15), (nice, nice) */
   Rate rate[R_N];
   int lcharge, level;
   /* status flags */
@@ -553,6 +555,12 @@ static void accumulateSink(Cell *w, int nbcoll, int itrgt, int istr, int iend, c
     double sum = 0.;
     for (int l = 0; l < c->nice; l++) sum += KIDX(zcc, nbcoll, itrgt, l) * coll[l].numc;
     const double fix_coag = fmaxd(1. - sum, 0.1);
+    /* ice-ice breakup (:881-896): collisions of the smaller target with larger crystals */
+    if (c->st_sipib && trgtphase == 4)
+      for (int ll = istr; ll <= iend; ll++)
+        if (w->ice[itrgt].dnsp < coll[ll].dnsp && w->ice[itrgt].numc > w->ice[itrgt].nlim && coll[ll].numc > coll[ll].nlim)
+          w->nii_ibr[ll * c->nice + itrgt] += Eagg[ll] * KIDX(zcc, nbcoll, ll, itrgt) * coll[ll].numc *
+                                               w->ice[itrgt].numc * fix_coag;
     /* drop fracturing (:899-944): drops larger than the collecting crystal (mode 4 would
        count the others too); the drop bin's own numbers are tested twice, as written */
     if (c->st_sipdf && (trgtphase == 3 || trgtphase == 2)) {
@@ -747,6 +755,16 @@ static void accumulateSourceIce(Cell *w, int nbtrgt, int nspec, int itrgt, int i
     double k = KIDX(zcc, nbtrgt, ll, itrgt);
     for (int s = 0; s < nspec; s++) source[s] += Eagg[ll] * k * coll[ll].volc[s];
   }
+  /* :1429-1447 ice-ice breakup: ice mass collected from the smaller bins; the target's
+     diameters are updated first, for every smaller bin */
+  if (c->st_secice && c->st_sipib)
+    for (int ll = istr; ll <= iend; ll++) {
+      updateDiameter(c, &w->ice[itrgt], 1, T_ALL);
+      if (w->ice[itrgt].dnsp > coll[ll].dnsp && w->ice[itrgt].numc > w->ice[itrgt].nlim && coll[ll].numc > coll[ll].nlim)
+        w->mii_ibr[itrgt * c->nice + ll] +=
+            Eagg[ll] * KIDX(zcc, nbtrgt, itrgt, ll) *
+            (coll[ll].volc[nspec - 2] * c->rhoic + coll[ll].volc[nspec - 1] * c->rhori) * coll[itrgt].numc;
+    }
 }
 
 /* :1457-1584 accumulatePrecipFormation (cloud-cloud; zcc symmetric, (ncld,ncld)) */
@@ -1118,6 +1136,8 @@ static void cell_clear(Cell *w, const salsa_ref_ctx_t *c) {
   memset(w->mfrzn_rs, 0, sizeof(double) * p * i);
   memset(w->nfrzn_df, 0, sizeof(double) * p * i);
   memset(w->mfrzn_df, 0, sizeof(double) * p * i);
+  memset(w->nii_ibr, 0, sizeof(double) * i * i);
+  memset(w->mii_ibr, 0, sizeof(double) * i * i);
 }
 
 /* mo_salsa_dynamics.f90:92-202 coagulation */
@@ -2742,6 +2762,101 @@ static void dropfracturing(Cell *w, double ptemp, double ptstep) {
   }
 }
 
+/* mo_salsa_SIP_IIBR.f90:262-291 imf_sullivan (mode 1), imf_sotiropoulou (mode 2):
+   fragments per collision, at most 100 */
+static double iibr_imf(int mode, double T, double dmin) {
+  const double fbr = 280., Tmin = 252., D0 = 0.02;
+  double imf;
+  if (mode == 1) imf = T < Tmin ? 0. : fmaxd(0., fbr * pow(T - Tmin, 1.2) * exp(-(T - Tmin) / 5.));
+  else imf = T <= Tmin ? 0. : fmaxd(0., fbr * pow(T - Tmin, 1.2) * exp(-(T - Tmin) / 5.) * dmin / D0);
+  return fmind(imf, 100.0);
+}
+
+/* mo_salsa_SIP_IIBR.f90:23-258 iceicecollbreak (per cell): each pair (smaller bb, larger cc)
+   breaks the smaller crystal into fragments spread over the bins below it as d^-3 */
+static void iceicecollbreak(Cell *w, double ptemp, double ptstep) {
+  const salsa_ref_ctx_t *c = w->c;
+  const int nice = c->nice, nspec = c->nused, mode = c->cfg.lssipicecollbreak.mode;
+  const double tmin = 248.15, tmax = 270.15;
+  Section *ice = w->ice;
+  double icediams[MAXB], icebw[MAXB];
+  for (int bb = 0; bb < nice; bb++) {
+    icediams[bb] = ice[bb].dmid;
+    icebw[bb] = pow(ice[bb].vhilim / PI6, 1. / 3) - pow(ice[bb].vlolim / PI6, 1. / 3);
+  }
+  for (int e = 0; e < nice * nice; e++) {
+    w->mii_ibr[e] = w->mii_ibr[e] * ptstep;
+    w->nii_ibr[e] = w->nii_ibr[e] * ptstep;
+  }
+  double fragvolc[MAXB][NSP], sinkvolc[MAXB][NSP], fragnumc[MAXB], sinknumc[MAXB];
+  double fragv_loc[MAXB][NSP], fragn_loc[MAXB], sinkv[NSP], dNb[MAXB], dVb[MAXB];
+  memset(fragvolc, 0, sizeof fragvolc); memset(sinkvolc, 0, sizeof sinkvolc);
+  memset(fragnumc, 0, sizeof fragnumc); memset(sinknumc, 0, sizeof sinknumc);
+  for (int bb = 0; bb < nice; bb++) {
+    memset(fragv_loc, 0, sizeof fragv_loc); memset(fragn_loc, 0, sizeof fragn_loc);
+    for (int cc = bb; cc < nice; cc++) {
+      const double nii = w->nii_ibr[cc * nice + bb], mii = w->mii_ibr[cc * nice + bb];
+      double vb = 0., vc = 0.;
+      for (int s = 0; s < NSP; s++) { vb += ice[bb].volc[s]; vc += ice[cc].volc[s]; }
+      if (ptemp < tmin || ptemp > tmax || nii < 1.e-12 || mii < 1.e-15 || vb < 1.e-15 || ice[bb].numc < ice[bb].nlim ||
+          vc < 1.e-15 || ice[cc].numc < ice[cc].nlim)
+        continue;
+      updateDiameter(c, &ice[bb], 1, T_ALL);
+      const double v_i = mii / nii / ice[bb].rhomean;
+      const double dinsphmin = pow(v_i / PI6, 1. / 3.);
+      int npmax = 0;
+      for (int k = 0; k < nice; k++) npmax += icediams[k] <= dinsphmin;
+      npmax = npmax - 1;
+      if (npmax <= 2) continue;
+      const double dN = iibr_imf(mode, ptemp, dinsphmin) * nii;
+      for (int k = 0; k < nice; k++) dNb[k] = dVb[k] = 0.;
+      double Nnorm = 0.;
+      for (int k = 0; k < npmax; k++) dNb[k] = 1. / cube(icediams[k]);
+      for (int k = 0; k < npmax; k++) Nnorm += dNb[k] * icebw[k];
+      for (int k = 0; k < npmax; k++) dNb[k] = dN * dNb[k] * icebw[k] / Nnorm;
+      for (int k = 0; k < npmax; k++) dVb[k] = dNb[k] * PI6 * cube(icediams[k]);
+      double sv = 0., sdv = 0.;
+      for (int s = 0; s < nspec; s++) sv += ice[bb].volc[s];
+      for (int k = 0; k < npmax; k++) sdv += dVb[k];
+      for (int k = 0; k < npmax; k++) {
+        fragn_loc[k] = fragn_loc[k] + dNb[k];
+        for (int s = 0; s < nspec; s++) fragv_loc[k][s] = fragv_loc[k][s] + ice[bb].volc[s] * (dVb[k] / sv);
+      }
+      for (int s = 0; s < nspec; s++) sinkv[s] = ice[bb].volc[s] * sdv / sv;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = sinkvolc[bb][s] + sinkv[s];
+      double ss = 0.;
+      for (int s = 0; s < nspec; s++) ss += sinkv[s];
+      sinknumc[bb] = sinknumc[bb] + ss / v_i;
+    }
+    for (int k = 0; k < nice; k++) {                        /* :187-188, before the safeguard */
+      fragnumc[k] = fragnumc[k] + fragn_loc[k];
+      for (int s = 0; s < NSP; s++) fragvolc[k][s] = fragvolc[k][s] + fragv_loc[k][s];
+    }
+    if (ice[bb].numc < sinknumc[bb]) {
+      sinknumc[bb] = ice[bb].numc;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = ice[bb].volc[s];
+    }
+    double ssk = 0., sv = 0.;
+    for (int s = 0; s < nspec; s++) { ssk += sinkvolc[bb][s]; sv += ice[bb].volc[s]; }
+    if (ssk > sv) {
+      const double frconst = 0.99 * sv / ssk;
+      for (int s = 0; s < nspec; s++) sinkvolc[bb][s] = sinkvolc[bb][s] * frconst;
+      sinknumc[bb] = sinknumc[bb] * frconst;
+      sinknumc[bb] = fmind(sinknumc[bb], 0.99 * ice[bb].numc);
+    }
+  }
+  for (int bb = 0; bb < nice; bb++) {
+    ice[bb].numc = ice[bb].numc + fragnumc[bb];
+    ice[bb].numc = ice[bb].numc - sinknumc[bb];
+    ice[bb].numc = fmaxd(0., ice[bb].numc);
+    for (int s = 0; s < nspec; s++) {
+      ice[bb].volc[s] = ice[bb].volc[s] + fragvolc[bb][s];
+      ice[bb].volc[s] = ice[bb].volc[s] - sinkvolc[bb][s];
+      ice[bb].volc[s] = fmaxd(0., ice[bb].volc[s]);
+    }
+  }
+}
+
 /* ======================================================================
  * mo_salsa.f90:45-153 salsa
  * ====================================================================== */
@@ -2753,6 +2868,7 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
   if (c->st_secice) {                                                   /* :98-99 */
     if (c->st_siprs) rimesplintering(w, ptemp, ptstep);
     if (c->st_sipdf) dropfracturing(w, ptemp, ptstep);
+    if (c->st_sipib) iceicecollbreak(w, ptemp, ptstep);
   }
   if (c->st_cnd) {
     /* condensation :276-342.  nucleation (mo_salsa_nucleation.f90:72-625) only returns the
@@ -2815,10 +2931,11 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (cfg->nbin[0] < 1 || cfg->nbin[1] < 4 || cfg->prc_nbins < 1 || cfg->ice_nbins < 1) return SALSA_E_ARG;
   if (cfg->nspec_dry < 1 || cfg->nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
   /* secondary ice (mo_salsa_secondary_ice.f90:6-40): rime splintering (mo_salsa_SIP_RS.f90)
-     in its two modes and drop fracturing (mo_salsa_SIP_DF.f90) in modes 1-3; Phillips'
-     full drop-fracturing scheme (mode 4) and ice-ice breakup are not restated */
+     in its two modes, drop fracturing (mo_salsa_SIP_DF.f90) in modes 1-3 and ice-ice
+     breakup (mo_salsa_SIP_IIBR.f90) in modes 1-2; Phillips' schemes (drop fracturing
+     mode 4, breakup mode 3) are not restated */
   if (cfg->lssecice.sw && cfg->level == 5 &&
-      (cfg->lssipicecollbreak.sw ||
+      ((cfg->lssipicecollbreak.sw && cfg->lssipicecollbreak.mode != 1 && cfg->lssipicecollbreak.mode != 2) ||
        (cfg->lssiprimespln.sw && cfg->lssiprimespln.mode != 1 && cfg->lssiprimespln.mode != 2) ||
        (cfg->lssipdropfrac.sw && (cfg->lssipdropfrac.mode < 1 || cfg->lssipdropfrac.mode > 3))))
     return SALSA_E_UNSUPPORTED;
@@ -3001,6 +3118,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
   /* subprocess switches; define_salsa switches them off at level 4 (:631-633) */
   if (!lvl4 && g->lssiprimespln.sw && time >= g->lssiprimespln.delay) c->st_siprs = 1;
   if (!lvl4 && g->lssipdropfrac.sw && time >= g->lssipdropfrac.delay) c->st_sipdf = 1;
+  if (!lvl4 && g->lssipicecollbreak.sw && time >= g->lssipicecollbreak.delay) c->st_sipib = 1;
   if (g->lsfreeRH.sw && time > g->lsfreeRH.delay) c->st_freeRH = 1;
   if (g->lsFreeTheta.sw && time > g->lsFreeTheta.delay) c->st_freeTheta = 1;
   c->lcgupdt = (c->st_coag && g->lscoag.mode == 2 && (fmod(time, g->cgintvl) < tstep || istp <= 1));

@@ -1,6 +1,6 @@
-"""Rime splintering (mo_salsa_SIP_RS.f90) and drop fracturing (mo_salsa_SIP_DF.f90),
-through mo_salsa_secondary_ice.f90, in the oracle: the properties of the reference's
-schemes.  Secondary ice is not built on the
+"""Rime splintering (mo_salsa_SIP_RS.f90), drop fracturing (mo_salsa_SIP_DF.f90) and
+ice-ice collisional breakup (mo_salsa_SIP_IIBR.f90), through mo_salsa_secondary_ice.f90,
+in the oracle: the properties of the reference's schemes.  Secondary ice is not built on the
 GPU (salsa_gb300_init refuses lssecice); these tests pin the oracle's restatement."""
 import pytest
 import torch
@@ -80,5 +80,26 @@ def test_drop_fracturing_conserves_ice_volume_and_adds_small_crystals(mode):
     assert int((dn > 0).sum()) > 5
     assert float((b["nice"][0] - a["nice"][0]).max()) > 0
     out = (T < 248.15) | (T > 271.15)             # the scheme's range (:56)
+    assert int(out.sum()) > 0
+    assert torch.equal(a["nice"][:, out], b["nice"][:, out])
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_ice_ice_breakup_conserves_ice_volume_and_adds_fragments(mode):
+    """Collisions of a crystal with larger ones break it into fragments spread over the
+    bins below its size (Sullivan; Sotiropoulou): volume conserved, crystals added, and
+    nothing outside 248.15-270.15 K."""
+    kw = dict(scheme="lssipicecollbreak")
+    a, T = _step(sip_state(mode, splinter=False, **kw))
+    b, _ = _step(sip_state(mode, **kw))
+    lay = sip_state(mode, **kw).layout
+    nw1, nic = lay.nwet + 1, lay.nice
+    ma = a["mice"].view(nw1, nic, *a["mice"].shape[1:]).sum(1)
+    mb = b["mice"].view(nw1, nic, *b["mice"].shape[1:]).sum(1)
+    scale = ma.abs().amax(0).clamp(min=1e-30)
+    assert float(((mb - ma).abs() / scale).max()) < 1e-12
+    dn = b["nice"].sum(0) - a["nice"].sum(0)
+    assert int((dn > 0).sum()) > 5
+    out = (T < 248.15) | (T > 270.15)
     assert int(out.sum()) > 0
     assert torch.equal(a["nice"][:, out], b["nice"][:, out])
