@@ -40,7 +40,8 @@ def only(*keep):
     return f
 
 
-@pytest.mark.parametrize("tag", ["grid16x16x40_sub", "grid256x256x128_sub", "grid384x384x160_sub"])
+@pytest.mark.parametrize("tag", ["grid16x16x40_sub", "grid256x256x128_sub", "grid384x384x160_sub",
+                                 "secondary_ice_sub"])
 def test_golden_fixtures(tag):
     """The oracle reproduces its committed outputs (tests/golden/make_golden.py)."""
     import golden.make_golden as mg
