@@ -358,3 +358,62 @@ def test_unsupported_and_bad_configs():
         assert lib().salsa_ref_create(C.byref(cfg), C.byref(h)) == code
         if code == 0:
             lib().salsa_ref_destroy(h)
+
+
+def test_two_bin_coagulation_matches_the_closed_form():
+    """The semi-implicit coagulation update (coag_aero + applyCoag,
+    mo_salsa_coagulation_processes.f90:24-215, 539-559) for a cell with two populated
+    aerosol bins a < b, written out: the smaller bin first, N_a' = N_a / (1 + dt (K_ab N_b
+    + K_aa N_a / 2)), V_a' = V_a / (1 + dt K_ab N_b); then the larger bin, whose source
+    uses the updated V_a': V_b' = V_b + dt K_ab V_a' N_b, N_b' = N_b / (1 + dt K_bb N_b / 2).
+    The kernels come from the oracle's coagc (independently pinned above)."""
+    cfg = workload_config(4)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgcc", "lscgca", "lscgpc", "lscgpa", "lscgpp", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    inp = make_inputs("grid16x16x40", "cpu", X=1, Y=1, Z=1)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    a, b = lay.in2a + 1, lay.in2a + 5
+    T, P, dt = 285.0, 95.0e3, inp.dt
+    na, nb_ = 5.e13, 1.e13                        # /m3: enough for the update to take a good share
+    da, db = lay.dmid[a], lay.dmid[b]
+    f = inp.fields
+    f["temp"][..., 1] = T
+    f["press"][..., 1] = P
+    dn = float(f["dn"][2, 2, 1])
+    nw = lay.nwet
+    iw = nw - 1
+    f["naero"].zero_()
+    f["maero"].zero_()
+    m = f["maero"].view(nw, lay.nbins, *f["naero"].shape[1:])
+    rhow = 1000.0
+    for k, n, d in ((a, na, da), (b, nb_, db)):
+        f["naero"][k, 2, 2, 1] = n / dn
+        m[iw, k, 2, 2, 1] = n * PI6 * d ** 3 * rhow / dn
+    for k in ("ncloud", "mcloud", "nprecp", "mprecp"):
+        f[k].zero_()
+    fields = {k: v.clone() for k, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0, nthreads=1)
+    assert rc == 0
+    h = Oracle(cfg).h
+    kab = lib().salsa_ref_coagc_pair(h, a, b, na, da, nb_, db, T, P)
+    kaa = lib().salsa_ref_coagc_pair(h, a, a, na, da, na, da, T, P)
+    kbb = lib().salsa_ref_coagc_pair(h, b, b, nb_, db, nb_, db, T, P)
+    va, vb = na * PI6 * da ** 3, nb_ * PI6 * db ** 3
+    na1 = na / (1. + dt * (kab * nb_ + 0.5 * kaa * na))
+    va1 = va / (1. + dt * kab * nb_)
+    nb1 = nb_ / (1. + dt * 0.5 * kbb * nb_)
+    vb1 = vb + dt * kab * va1 * nb_
+    new_n = (f["naero"] + out["naerot"] * dt)[:, 2, 2, 1] * dn
+    new_v = (f["maero"] + out["maerot"] * dt).view(nw, lay.nbins, *f["naero"].shape[1:])[iw, :, 2, 2, 1] * dn / rhow
+    # the changes themselves agree to 1e-10
+    for got, want, old in ((float(new_n[a]), na1, na), (float(new_v[a]), va1, va), (float(new_n[b]), nb1, nb_),
+                           (float(new_v[b]), vb1, vb)):
+        assert got - old == pytest.approx(want - old, rel=1e-10)
+    assert na1 < 0.9 * na and vb1 - vb > 1e-5 * vb               # the update takes a good share
+    others = [k for k in range(lay.nbins) if k not in (a, b)]
+    assert float(new_n[others].abs().max()) == 0
