@@ -16,13 +16,19 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def test_reference_arm_under_torchrun_two_ranks():
+def _launch():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",
            "--workload", "grid16x16x40", "--cpu-sample-cells", "2048"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
-    r = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    return subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    r = _launch()
+    if r.returncode != 0 and "address already in use" in r.stderr.lower():
+        r = _launch()       # the free port was taken between the probe and the rendezvous
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1, r.stdout

@@ -1,9 +1,8 @@
-"""The multi-rank layout on CPU with two gloo ranks.  Cells are independent within a
+"""The multi-rank layout on CPU with two gloo ranks (file rendezvous).  Cells are independent within a
 step, so ranks that each run their own y-slab (with its halo rows) reproduce a
 single-process run over the whole block; the only collective is the max of the
 ranks' timers, as in bench.py under torchrun."""
 import os
-import socket
 import time
 
 import torch
@@ -24,12 +23,12 @@ def _slab(t, y0, y1):
     return t[..., y0:y1 + 4, :, :].contiguous()
 
 
-def _rank(rank, world, port, q):
+def _rank(rank, world, store, q):
     import sys
     sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     from oracle_ref import Oracle
-    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # a file rendezvous: no port to pick, so no race with other processes for one
+    dist.init_process_group("gloo", init_method="file://" + store, rank=rank, world_size=world)
     inp = _case()
     y0, y1 = rank * (Y // world), (rank + 1) * (Y // world)
     inp.fields = {k: _slab(v, y0, y1) for k, v in inp.fields.items()}
@@ -44,7 +43,7 @@ def _rank(rank, world, port, q):
     dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_reproduce_the_single_run():
+def test_two_gloo_ranks_reproduce_the_single_run(tmp_path):
     import sys
     sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     from oracle_ref import Oracle
@@ -53,12 +52,10 @@ def test_two_gloo_ranks_reproduce_the_single_run():
     f = {k: v.clone() for k, v in inp.fields.items()}
     rc, _ = Oracle(inp.cfg).run(inp, f, out, time=1.0, nthreads=1)
     assert rc == 0
-    with socket.socket() as s:
-        s.bind(("127.0.0.1", 0))
-        port = s.getsockname()[1]
+    store = str(tmp_path / "rendezvous")
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, 2, store, q)) for r in range(2)]
     for p in procs:
         p.start()
     res = sorted(q.get(timeout=300) for _ in procs)
