@@ -77,3 +77,24 @@ def test_null_arguments_are_rejected():
     assert lib.salsa_gb300_init(None, C.byref(h)) == capi.SALSA_E_ARG
     st = capi.Status()
     assert lib.salsa_gb300_run(None, 42, 20, 20, 6, 1.0, 1.0, 1, 4, 0, 0, None, C.byref(st)) == capi.SALSA_E_ARG
+
+
+def test_secondary_ice_is_refused_before_any_device_call():
+    """The step's secondary-ice form is compiled but not yet enabled: salsa_gb300_init
+    answers SALSA_E_UNSUPPORTED for lssecice (for every scheme and mode) before it
+    touches a device, and a configuration without it gets past that check."""
+    lib = api.library()
+    h = C.c_void_p()
+    for scheme, modes in (("lssiprimespln", (1, 2, 3)), ("lssipdropfrac", (1, 2, 3, 4)),
+                          ("lssipicecollbreak", (1, 2, 3))):
+        for mode in modes:
+            cfg = reference_defaults(level=5)
+            cfg.lssecice.sw = 1
+            sw = getattr(cfg, scheme)
+            sw.sw, sw.mode = 1, mode
+            assert lib.salsa_gb300_init(C.byref(cfg), C.byref(h)) == capi.SALSA_E_UNSUPPORTED, (scheme, mode)
+    cfg = reference_defaults(level=5)
+    rc = lib.salsa_gb300_init(C.byref(cfg), C.byref(h))
+    assert rc != capi.SALSA_E_UNSUPPORTED
+    if rc == capi.SALSA_OK:
+        lib.salsa_gb300_finalize(h)

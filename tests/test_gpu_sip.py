@@ -1,0 +1,65 @@
+"""GPU parity of the step's secondary-ice form (rime splintering, drop fracturing,
+ice-ice breakup) against the oracle, with the step's parity criterion.
+
+The secondary-ice form is compiled and wired in, but salsa_gb300_init refuses lssecice
+until this test has passed on a GB300: while it does, the test skips.
+"""
+import pytest
+
+from uclales_salsa_gb300 import capi
+from uclales_salsa_gb300.api import SalsaError
+from sip_cases import sip_state
+from test_gpu_parity import oracle_run, gpu_run, envelope, check, VIOL_FRAC, FRAC_WITHIN
+
+pytestmark = pytest.mark.gpu
+
+SCHEMES = [("lssiprimespln", 1), ("lssiprimespln", 2), ("lssipdropfrac", 1), ("lssipdropfrac", 2),
+           ("lssipdropfrac", 3), ("lssipicecollbreak", 1), ("lssipicecollbreak", 2)]
+
+
+def _gpu_or_skip(inp):
+    try:
+        return gpu_run(inp)
+    except SalsaError as e:
+        if e.code == capi.SALSA_E_UNSUPPORTED:
+            pytest.skip("salsa_gb300_init refuses lssecice: the GPU form has not been enabled")
+        raise
+
+
+def _parity(inp, rtol, eps):
+    _, gpu = _gpu_or_skip(inp)
+    _, ref = oracle_run(inp)
+    env = envelope(inp, ref, eps)
+    rep = check(inp, gpu, ref, env, rtol)
+    print(rep)
+    for k, r in rep.items():
+        assert r["violations"] <= VIOL_FRAC * r["n"], (k, r)
+        assert r["frac_within"] >= FRAC_WITHIN, (k, r)
+    return ref
+
+
+@pytest.mark.parametrize("scheme,mode", SCHEMES)
+def test_secondary_ice_fp64_parity(scheme, mode):
+    """Coagulation and one scheme: the GPU step matches the oracle, and the scheme
+    changes the ice numbers by far more than the tolerance (the test sees it)."""
+    inp = sip_state(mode, scheme=scheme)
+    ref = _parity(inp, 1e-10, 2.2e-16)
+    _, off = oracle_run(sip_state(mode, splinter=False, scheme=scheme))
+    d = (ref["nicet"] - off["nicet"]).abs().max()
+    assert float(d) > 1e-6 * float(ref["nicet"].abs().max())
+
+
+def test_secondary_ice_all_processes_fp64_parity():
+    """All processes with the three schemes on (the secondary_ice_sub fixture's setup)."""
+    inp = sip_state(1, coag_only=False)
+    for sw in (inp.cfg.lssipdropfrac, inp.cfg.lssipicecollbreak):
+        sw.sw, sw.mode = 1, 1
+    _parity(inp, 1e-10, 2.2e-16)
+
+
+def test_secondary_ice_mixed_error_bound():
+    inp = sip_state(1, coag_only=False)
+    for sw in (inp.cfg.lssipdropfrac, inp.cfg.lssipicecollbreak):
+        sw.sw, sw.mode = 1, 1
+    inp.cfg.precision = 1
+    _parity(inp, 1e-6, 1e-7)

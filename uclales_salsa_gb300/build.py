@@ -1,7 +1,7 @@
 """Build the CUDA library libsalsa_gb300.so in-tree for sm_103a.
 
-The four kernel forms (FP64 / FP32-mixed x with / without diagnostics) are
-separate translation units so they compile in parallel.
+The kernel forms (FP64 / FP32-mixed x with / without diagnostics, and the two
+secondary-ice forms) are separate translation units so they compile in parallel.
 """
 import os
 import shutil
@@ -15,8 +15,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsalsa_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
-UNITS = ["salsa_k_d0.cu", "salsa_k_d1.cu", "salsa_k_f0.cu", "salsa_k_f1.cu", "salsa_chain.cu", "salsa_post.cu",
-         "salsa_sedim.cu", "salsa_capi.cu"]
+UNITS = ["salsa_k_d0.cu", "salsa_k_d1.cu", "salsa_k_f0.cu", "salsa_k_f1.cu", "salsa_k_ds.cu", "salsa_k_fs.cu",
+         "salsa_chain.cu", "salsa_post.cu", "salsa_sedim.cu", "salsa_capi.cu"]
 # Units compiled without multiply-add contraction, so that their arithmetic rounds
 # like the reference's x86-64 SSE2 build: the post-step constraints, which match the
 # oracle bit for bit.  The step kernels (both forms), the gradient harness (whose

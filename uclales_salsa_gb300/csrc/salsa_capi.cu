@@ -29,7 +29,17 @@ int blocks_per_sm_d0(const DevParams &);
 int blocks_per_sm_d1(const DevParams &);
 int blocks_per_sm_f0(const DevParams &);
 int blocks_per_sm_f1(const DevParams &);
+cudaError_t launch_ds(const DevParams &, cudaStream_t, int);
+cudaError_t launch_fs(const DevParams &, cudaStream_t, int);
+int blocks_per_sm_ds(const DevParams &);
+int blocks_per_sm_fs(const DevParams &);
 }  // namespace salsa
+
+// Secondary ice production on the GPU: the step's secondary-ice form (salsa_k_ds.cu,
+// salsa_k_fs.cu) is compiled and wired in, but has not been compared with the oracle on
+// a GPU yet.  Until it has, salsa_gb300_init refuses a configuration that switches
+// lssecice on.
+static const bool kSecondaryIceChecked = false;
 
 using salsa::DevParams;
 using salsa::Row;
@@ -138,6 +148,7 @@ struct salsa_handle {
   // sticky switch states (set_SALSA_runtime)
   int st[7] = {0, 0, 0, 0, 0, 0, 0};
   int st_freeRH = 0, st_freeTheta = 0;
+  int st_sip[3] = {0, 0, 0};    // lssiprimespln, lssipdropfrac, lssipicecollbreak
   // staging buffers for host-pointer calls
   void *stage = nullptr;
   size_t stage_bytes = 0;
@@ -220,7 +231,15 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
   if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
   // processes outside this build (the init check mirrors the oracle's)
-  if (g.lssecice.sw) return SALSA_E_UNSUPPORTED;
+  if (g.lssecice.sw && !kSecondaryIceChecked) return SALSA_E_UNSUPPORTED;
+  // the schemes' modes the oracle restates: Phillips' full forms (drop fracturing mode 4,
+  // breakup mode 3) are not built
+  if (g.lssecice.sw) {
+    const salsa_switch_t &rs = g.lssiprimespln, &df = g.lssipdropfrac, &ib = g.lssipicecollbreak;
+    if (rs.sw && (rs.mode < 1 || rs.mode > 2)) return SALSA_E_UNSUPPORTED;
+    if (df.sw && (df.mode < 1 || df.mode > 3)) return SALSA_E_UNSUPPORTED;
+    if (ib.sw && (ib.mode < 1 || ib.mode > 2)) return SALSA_E_UNSUPPORTED;
+  }
   if (g.lscoag.mode == 2 && !(g.cgintvl > 0.)) return SALSA_E_ARG;
   // nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
   // nj3 outside 1-3 STOPs once a cell nucleates (:600-602)
@@ -510,6 +529,18 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
     // the kernel triangle; after the coagulation the ice nucleation keeps 8 doubles per liquid bin there
     size_t kd = std::max((tri_n * kt_bytes + 7) / 8, (size_t)8 * B.nliquid);
     size_t n = ((B.nraw + 1) & ~1) + nbp + SALSA_NSV * nbp + 7 * nbp + 13 * nbp + 336 + 64 + kd;
+    if (g.lssecice.sw && g.level == 5) {
+      // the secondary-ice tallies and the schemes' scratch after the kernel triangle
+      n = (n + 1) & ~(size_t)1;
+      B.sip_off = (int)n;
+      n += 4 * (size_t)nprc * nice + 2 * (size_t)nice * nice + 7 * (size_t)nice + 3 * (size_t)nice * SALSA_NSV + SALSA_NSV;
+      int spl = 0;   // mo_salsa_SIP_RS.f90:72: ice bins whose lower limit is below the 10 um splinters
+      for (int bb = 0; bb < nice; bb++) spl += std::pow(t.vlo[B.nliquid + bb] / PI6, 1. / 3.) < 10.e-6;
+      B.sip_splbin = spl < 1 ? 1 : spl;
+      B.sip_rs_mode = g.lssiprimespln.mode;
+      B.sip_df_mode = g.lssipdropfrac.mode;
+      B.sip_ib_mode = g.lssipicecollbreak.mode;
+    }
     B.ws_doubles = (int)((n + 1) & ~(size_t)1);
   }
   size_t smem = sizeof(double) * ((size_t)B.tab_doubles + (size_t)SALSA_CPG * B.ws_doubles);
@@ -641,6 +672,9 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
     if (level == 4 && i >= 4) sw = 0;   // define_salsa :615-635
     if (sw && time >= ms[i]->delay) h->st[i] = 1;
   }
+  const salsa_switch_t *sips[3] = {&g.lssiprimespln, &g.lssipdropfrac, &g.lssipicecollbreak};
+  for (int i = 0; i < 3; i++)
+    if (level == 5 && sips[i]->sw && time >= sips[i]->delay) h->st_sip[i] = 1;
   if (g.lsfreeRH.sw && time > g.lsfreeRH.delay) h->st_freeRH = 1;
   if (g.lsFreeTheta.sw && time > g.lsFreeTheta.delay) h->st_freeTheta = 1;
   (void)istp;
@@ -656,6 +690,8 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   P.st_coag = h->st[0]; P.st_cnd = h->st[1]; P.st_auto = h->st[2]; P.st_activ = h->st[3];
   P.st_icenucl = h->st[4]; P.st_icemelt = h->st[5];
   P.st_freeRH = h->st_freeRH; P.st_freeTheta = h->st_freeTheta;
+  P.st_secice = h->st[6] && h->base.sip_off > 0;
+  P.st_siprs = h->st_sip[0]; P.st_sipdf = h->st_sip[1]; P.st_sipib = h->st_sip[2];
   P.coag_mode = g.lscoag.mode; P.auto_mode = g.lsauto.mode; P.activ_mode = g.lsactiv.mode;
   P.icenucl_mode = (level == 4) ? 1 : g.lsicenucl.mode;
   P.lscgaa = g.lscgaa; P.lscgcc = g.lscgcc; P.lscgca = g.lscgca; P.lscgpc = g.lscgpc; P.lscgpa = g.lscgpa;
@@ -748,8 +784,10 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   };
   // order pre-pass and step kernel over the cells of Q, on stream s
   auto launch = [&](DevParams &Q, int *order) -> int {
-    int bps = prec == 0 ? (dg ? salsa::blocks_per_sm_d1(Q) : salsa::blocks_per_sm_d0(Q))
-                        : (dg ? salsa::blocks_per_sm_f1(Q) : salsa::blocks_per_sm_f0(Q));
+    const bool sip = Q.st_secice != 0;
+    int bps = sip ? (prec == 0 ? salsa::blocks_per_sm_ds(Q) : salsa::blocks_per_sm_fs(Q))
+                  : prec == 0 ? (dg ? salsa::blocks_per_sm_d1(Q) : salsa::blocks_per_sm_d0(Q))
+                              : (dg ? salsa::blocks_per_sm_f1(Q) : salsa::blocks_per_sm_f0(Q));
     if (bps <= 0) return SALSA_E_CUDA;
     long long grid = (long long)bps * h->nsm * 8;
     if (grid > Q.ngroups) grid = Q.ngroups;
@@ -765,8 +803,9 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
       if (cudaGetLastError() != cudaSuccess) return SALSA_E_CUDA;
       launches++;
     }
-    cudaError_t e = prec == 0 ? (dg ? salsa::launch_d1(Q, s, (int)grid) : salsa::launch_d0(Q, s, (int)grid))
-                              : (dg ? salsa::launch_f1(Q, s, (int)grid) : salsa::launch_f0(Q, s, (int)grid));
+    cudaError_t e = sip ? (prec == 0 ? salsa::launch_ds(Q, s, (int)grid) : salsa::launch_fs(Q, s, (int)grid))
+                    : prec == 0 ? (dg ? salsa::launch_d1(Q, s, (int)grid) : salsa::launch_d0(Q, s, (int)grid))
+                                : (dg ? salsa::launch_f1(Q, s, (int)grid) : salsa::launch_f0(Q, s, (int)grid));
     if (e != cudaSuccess) return SALSA_E_CUDA;
     launches++;
     return SALSA_OK;

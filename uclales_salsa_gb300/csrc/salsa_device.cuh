@@ -130,6 +130,11 @@ struct DevParams {
   unsigned long long *status;
   const int *order;         // processing order of the cells (clear cells first), or null
   unsigned long long *stage_clocks;   // per-stage clock sums (instrumented builds only)
+  // secondary ice (mo_salsa_secondary_ice.f90): states of lssecice and the three schemes,
+  // the schemes' modes, the first splinter bin (1-based, mo_salsa_SIP_RS.f90:72) and the
+  // offset of the tally region inside each warp's workspace (doubles)
+  int st_secice, st_siprs, st_sipdf, st_sipib;
+  int sip_rs_mode, sip_df_mode, sip_ib_mode, sip_splbin, sip_off;
 };
 
 // block table layout (per bin, padded to nb_pad): offsets in units of nb_pad

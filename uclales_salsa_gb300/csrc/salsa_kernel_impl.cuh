@@ -538,6 +538,392 @@ struct TAcc {
   }
 };
 
+// ----------------------------------------------------------------------------------------
+// Secondary ice (mo_salsa_secondary_ice.f90:6-40).  Only the SIP instantiations of the
+// step compile this code.  Coagulation tallies the collisions the three schemes read,
+// at the point of its Gauss-Seidel sweep where the reference does; the schemes then
+// run on lane 0 after coagulation.  The per-cell tallies and the schemes' scratch sit
+// at the end of the warp's workspace (P.sip_off doubles after its start); n = nice,
+// p = nprc, V = SALSA_NSV:
+//   nfrzn_rs, mfrzn_rs, nfrzn_df, mfrzn_df  p x n each (precipitation or cloud row, ice bin)
+//   nii_ibr, mii_ibr                        n x n each
+//   scratch                                 7 n + 3 n V + V
+// ----------------------------------------------------------------------------------------
+#define SIP_DLLIQ_RS 24.0e-6   // mo_salsa_SIP_RS.f90:17: smallest drop that splinters on riming
+#define SIP_DLLIQ_DF 100.e-6   // mo_salsa_SIP_DF.f90:18: smallest drop that fractures on freezing
+
+struct SipT {
+  double *nrs, *mrs, *ndf, *mdf, *nii, *mii, *scr;
+};
+__device__ __forceinline__ SipT sip_tallies(const DevParams &P, double *wsbase) {
+  const int pn = P.nprc * P.nice, nn = P.nice * P.nice;
+  double *t = wsbase + P.sip_off;
+  return {t, t + pn, t + 2 * pn, t + 3 * pn, t + 4 * pn, t + 4 * pn + nn, t + 4 * pn + 2 * nn};
+}
+__host__ __device__ __forceinline__ int sip_doubles(int nprc, int nice) {
+  return 4 * nprc * nice + 2 * nice * nice + 7 * nice + 3 * nice * SALSA_NSV + SALSA_NSV;
+}
+
+template <typename KT>
+__device__ void sip_clear(const DevParams &P, const WS<KT> &w, int lane) {
+  double *t = w.raw + P.sip_off;
+  const int n = 4 * P.nprc * P.nice + 2 * P.nice * P.nice;
+  for (int e = lane; e < n; e += 32) t[e] = 0.;
+  __syncwarp();
+}
+
+// accumulateSink's secondary-ice block (coagulation_processes.f90:863-944) for the liquid
+// target tg (a cloud or precipitation bin) and its ice collectors: the frozen-drop
+// numbers of drop fracturing (drops larger than the crystal) and rime splintering
+// (drops not larger), in row `row` (the precipitation bin, or 0 for every cloud bin).
+// tnlim is the target's number limit.  Lane 0.
+template <typename KT>
+__device__ void sip_drop_numbers(const DevParams &P, const WS<KT> &w, int tg, int row, double tnlim) {
+  const int I0 = P.nliquid, nice = P.nice;
+  const SipT s = sip_tallies(P, w.raw);
+  double sum = 0.;
+  for (int l = 0; l < nice; l++) sum += (double)kget(w, tg, I0 + l) * w.numc[I0 + l];
+  const double fix = fmax(1. - sum, 0.1);
+  const double Dt = w.dwet[tg], Nt = w.numc[tg];
+  for (int ll = 0; ll < nice; ll++) {
+    const int g = I0 + ll;
+    const double Nl = w.numc[g], Dl = w.dwet[g];
+    const double r = (double)kget(w, tg, g) * Nl * Nt * fix;
+    if (P.st_sipdf && Nl > K_PRLIM && Dl < Dt && Dt > SIP_DLLIQ_DF && Nt > tnlim) s.ndf[row * nice + ll] += r;
+    if (P.st_siprs && Dl >= Dt && Dt > SIP_DLLIQ_RS && Nt > tnlim && Nl > K_PRLIM) s.nrs[row * nice + ll] += r;
+  }
+}
+
+// accumulateSink's ice-ice breakup block (:881-896) for ice target kk: collisions with the
+// larger crystals kk+1..nice-1, with the aggregation efficiency of the pair.  Lane 0.
+template <typename KT>
+__device__ void sip_iibr_numbers(const DevParams &P, const WS<KT> &w, int kk, double rf_t) {
+  const int I0 = P.nliquid, nice = P.nice, tg = I0 + kk;
+  const SipT s = sip_tallies(P, w.raw);
+  double sum = 0.;
+  for (int l = 0; l < nice; l++) sum += (double)kget(w, tg, I0 + l) * w.numc[I0 + l];
+  const double fix = fmax(1. - sum, 0.1);
+  for (int ll = kk + 1; ll < nice; ll++) {
+    const int g = I0 + ll;
+    if (w.dnsp[tg] < w.dnsp[g] && w.numc[tg] > K_PRLIM && w.numc[g] > K_PRLIM) {
+      const double rf = fmax(rimefrac(P, w.numc[g], w.v(P.iwa, g), w.v(P.irim, g), 4), rf_t);
+      const double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
+      s.nii[ll * nice + kk] += E * (double)kget(w, g, tg) * w.numc[g] * w.numc[tg] * fix;
+    }
+  }
+}
+
+// accumulateSourcePhaseChange's secondary-ice block (:1285-1378) for ice target kk and the
+// liquid collectors c0 + istr..iend of a category with nb bins (cloud or precipitation):
+// the ice target's diameters are updated (:1291-1308), then the frozen-drop masses are
+// tallied; drops from cloud bins use the kernel of cloud bin 1 (ix = 1), as the
+// reference writes it.  Lane 0.
+template <typename KT>
+__device__ void sip_drop_masses(const DevParams &P, const WS<KT> &w, const double *dmid, int kk, int c0, int nb,
+                                int istr, int iend, bool precip) {
+  const int nice = P.nice, iwa = P.iwa, tg = P.nliquid + kk;
+  const SipT s = sip_tallies(P, w.raw);
+  double sum = 0.;
+  for (int l = 0; l < nb; l++) sum += (double)kget(w, c0 + l, tg) * w.numc[c0 + l];
+  const double fix = fmax(1. - sum, 0.1);
+  updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, tg);
+  const double Dt = w.dnsp[tg], Nt = w.numc[tg];
+  const double lnlim = precip ? K_PRLIM : K_NLIM;
+  for (int ll = istr; ll <= iend; ll++) {
+    const int g = c0 + ll, ix = precip ? ll : 0;
+    const double Dl = w.dwet[g];
+    const double r = (double)kget(w, c0 + ix, tg) * w.v(iwa, g) * Nt * K_RHOWA * fix;
+    if (P.st_sipdf && Dt < Dl && Dl > SIP_DLLIQ_DF && Nt > K_PRLIM && w.numc[g] > lnlim) s.mdf[ix * nice + kk] += r;
+    if (P.st_siprs && Dl >= SIP_DLLIQ_RS && Dl < Dt) s.mrs[ix * nice + kk] += r;
+  }
+}
+
+// accumulateSourceIce's ice-ice breakup block (:1429-1447) for ice target kk: the ice and
+// rime mass collected from the smaller crystals 0..kk-1.  Lane 0.
+template <typename KT>
+__device__ void sip_iibr_masses(const DevParams &P, const WS<KT> &w, const double *dmid, int kk, double rf_t) {
+  const int I0 = P.nliquid, nice = P.nice, tg = I0 + kk;
+  const SipT s = sip_tallies(P, w.raw);
+  updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, w.NB, tg);
+  for (int ll = 0; ll < kk; ll++) {
+    const int g = I0 + ll;
+    if (w.dnsp[tg] > w.dnsp[g] && w.numc[tg] > K_PRLIM && w.numc[g] > K_PRLIM) {
+      const double rf = fmax(rimefrac(P, w.numc[g], w.v(P.iwa, g), w.v(P.irim, g), 4), rf_t);
+      const double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
+      s.mii[kk * nice + ll] +=
+          E * (double)kget(w, tg, g) * (w.v(P.iwa, g) * K_RHOIC + w.v(P.irim, g) * K_RHORI) * w.numc[tg];
+    }
+  }
+}
+
+// The schemes' common end (mo_salsa_SIP_RS.f90:152-201, _DF.f90:183-237,
+// _IIBR.f90:195-250): per source bin, the sink is capped at the bin's content and scaled
+// to 99 % of its volume; then fragments are added and sinks removed.
+__device__ void sip_cap_sink(const DevParams &P, const double *numc, const double *volc, int NB, int g, double &sinkn,
+                             double *sinkv) {
+  const int nspec = P.nused;
+  if (numc[g] < sinkn) {
+    sinkn = numc[g];
+    for (int s = 0; s < nspec; s++) sinkv[s] = volc[s * NB + g];
+  }
+  double ssk = 0., sv = 0.;
+  for (int s = 0; s < nspec; s++) { ssk += sinkv[s]; sv += volc[s * NB + g]; }
+  if (ssk > sv) {
+    const double frconst = 0.99 * sv / ssk;
+    for (int s = 0; s < nspec; s++) sinkv[s] = sinkv[s] * frconst;
+    sinkn = sinkn * frconst;
+    sinkn = fmin(sinkn, 0.99 * numc[g]);
+  }
+}
+__device__ void sip_apply(const DevParams &P, double *numc, double *volc, int NB, const double *fragn,
+                          const double *fragv, const double *sinkn, const double *sinkv) {
+  const int I0 = P.nliquid, nspec = P.nused;
+  for (int bb = 0; bb < P.nice; bb++) {
+    const int g = I0 + bb;
+    double n = numc[g] + fragn[bb];
+    n = n - sinkn[bb];
+    numc[g] = fmax(0., n);
+    for (int s = 0; s < nspec; s++) {
+      double v = volc[s * NB + g] + fragv[bb * SALSA_NSV + s];
+      v = v - sinkv[bb * SALSA_NSV + s];
+      volc[s * NB + g] = fmax(0., v);
+    }
+  }
+}
+
+// Scratch of the schemes (inside the tally region).
+struct SipScr {
+  double *fragn, *sinkn, *fragn_loc, *dNb, *dVb, *diams, *bw, *fragv, *sinkv, *fragv_loc, *sv1;
+};
+__device__ __forceinline__ SipScr sip_scratch(const DevParams &P, const SipT &t) {
+  const int n = P.nice, V = SALSA_NSV;
+  double *p = t.scr;
+  SipScr q;
+  q.fragn = p; q.sinkn = p + n; q.fragn_loc = p + 2 * n; q.dNb = p + 3 * n; q.dVb = p + 4 * n;
+  q.diams = p + 5 * n; q.bw = p + 6 * n;
+  q.fragv = p + 7 * n; q.sinkv = q.fragv + n * V; q.fragv_loc = q.sinkv + n * V; q.sv1 = q.fragv_loc + n * V;
+  for (int e = 0; e < 7 * n + 3 * n * V + V; e++) p[e] = 0.;
+  return q;
+}
+// ice bin centres and widths in diameter (DF :82-88, IIBR :75-81)
+__device__ void sip_bin_geometry(const DevParams &P, const double *tb, SipScr &q) {
+  const int I0 = P.nliquid;
+  for (int bb = 0; bb < P.nice; bb++) {
+    q.diams[bb] = tb[TAB_DMID * P.nb_pad + I0 + bb];
+    q.bw[bb] = pow(tb[TAB_VHI * P.nb_pad + I0 + bb] / K_PI6, 1. / 3) - pow(tb[TAB_VLO * P.nb_pad + I0 + bb] / K_PI6, 1. / 3);
+  }
+}
+// Fragments dN spread over the ice bins 0..npmax-1 as d^-3 in number (DF :131-146, IIBR
+// :141-156): adds the fragment numbers and volumes (the source bin's composition);
+// returns the fragments' total volume sdv, and sv, the source bin g's.
+__device__ double sip_spread(const DevParams &P, const double *volc, int NB, int g, double dN, int npmax, SipScr &q,
+                             double &sv) {
+  const int nspec = P.nused;
+  for (int k = 0; k < P.nice; k++) q.dNb[k] = q.dVb[k] = 0.;
+  double Nnorm = 0.;
+  for (int k = 0; k < npmax; k++) q.dNb[k] = 1. / cube(q.diams[k]);
+  for (int k = 0; k < npmax; k++) Nnorm += q.dNb[k] * q.bw[k];
+  for (int k = 0; k < npmax; k++) q.dNb[k] = dN * q.dNb[k] * q.bw[k] / Nnorm;
+  for (int k = 0; k < npmax; k++) q.dVb[k] = q.dNb[k] * K_PI6 * cube(q.diams[k]);
+  double sdv = 0.;
+  sv = 0.;
+  for (int s = 0; s < nspec; s++) sv += volc[s * NB + g];
+  for (int k = 0; k < npmax; k++) sdv += q.dVb[k];
+  for (int k = 0; k < npmax; k++) {
+    q.fragn_loc[k] = q.fragn_loc[k] + q.dNb[k];
+    for (int s = 0; s < nspec; s++)
+      q.fragv_loc[k * SALSA_NSV + s] = q.fragv_loc[k * SALSA_NSV + s] + volc[s * NB + g] * (q.dVb[k] / sv);
+  }
+  return sdv;
+}
+// the per-source-bin fragments join the totals before the sink safeguard (DF :175-176,
+// IIBR :187-188)
+__device__ void sip_fold_local(const DevParams &P, SipScr &q) {
+  for (int k = 0; k < P.nice; k++) {
+    q.fragn[k] = q.fragn[k] + q.fragn_loc[k];
+    for (int s = 0; s < SALSA_NSV; s++) q.fragv[k * SALSA_NSV + s] = q.fragv[k * SALSA_NSV + s] + q.fragv_loc[k * SALSA_NSV + s];
+    q.fragn_loc[k] = 0.;
+    for (int s = 0; s < SALSA_NSV; s++) q.fragv_loc[k * SALSA_NSV + s] = 0.;
+  }
+}
+
+// mo_salsa_SIP_RS.f90:28-215 rimesplintering (Hallett-Mossop per kg of rime, mode 1;
+// Mossop per frozen drop, mode 2; dltemp_rs = 5: no temperature shape).  Lane 0.
+template <typename KT>
+__device__ void sip_rimesplintering(const DevParams &P, const WS<KT> &w, double T, double dt) {
+  const int nprc = P.nprc, nice = P.nice, nspec = P.nused, I0 = P.nliquid, NB = w.NB;
+  const SipT t = sip_tallies(P, w.raw);
+  SipScr q = sip_scratch(P, t);
+  const double v_i = 3.405365461487051e-16;   // a 10 um hexagonal column of bulk ice
+  const int splbin = P.sip_splbin;
+  for (int e = 0; e < nprc * nice; e++) {
+    t.mrs[e] = t.mrs[e] * dt;
+    t.nrs[e] = t.nrs[e] * dt;
+  }
+  for (int bb = 0; bb < nice; bb++) {
+    const int g = I0 + bb;
+    double vall = 0.;
+    for (int s = 0; s < nspec; s++) vall += w.v(s, g);
+    double *sinkv = q.sinkv + bb * SALSA_NSV;
+    for (int cc = 0; cc < nprc; cc++) {
+      const double nf = t.nrs[cc * nice + bb], mf = t.mrs[cc * nice + bb];
+      if (T < 238.15 || T > 273.15 || nf < 1.e-12 || vall < 1.e-15 || w.numc[g] < K_PRLIM || bb + 1 < splbin + 2)
+        continue;
+      const double ddmean = pow(mf / nf / K_RHOWA / K_PI6, 1. / 3.);
+      if (ddmean < SIP_DLLIQ_RS) continue;
+      const double dN = P.sip_rs_mode == 1 ? 3.5E8 * mf : 4.0E-3 * nf;
+      const double dV = dN * v_i;
+      q.fragn[splbin - 1] = q.fragn[splbin - 1] + dN;
+      double sv = 0.;
+      for (int s = 0; s < nspec; s++) sv += w.v(s, g);
+      const double f = fmin(dV / sv, 1.);
+      double ss = 0.;
+      for (int s = 0; s < nspec; s++) {
+        q.fragv[(splbin - 1) * SALSA_NSV + s] = q.fragv[(splbin - 1) * SALSA_NSV + s] + w.v(s, g) * f;
+        const double sk = w.v(s, g) * f;
+        sinkv[s] = sinkv[s] + sk;
+        ss += sk;
+      }
+      q.sinkn[bb] = q.sinkn[bb] + ss / (K_PI6 * pow(ddmean, 3.0));
+    }
+    sip_cap_sink(P, w.numc, w.volc, NB, g, q.sinkn[bb], sinkv);
+  }
+  sip_apply(P, w.numc, w.volc, NB, q.fragn, q.fragv, q.sinkn, q.sinkv);
+}
+
+// mo_salsa_SIP_DF.f90:370-398 fragments per frozen drop: Lawson (mode 1), Sullivan
+// (mode 2), Phillips' simple form (mode 3)
+__device__ double sip_df_fragments(int mode, double T, double nf, double ddmean) {
+  if (mode == 1) return nf * 2.5e-11 * pow(fmin(ddmean, 3.e-3) * 1.e6, 4.);
+  if (mode == 2) {
+    // f_gauss(T, 10, 258) / f_gauss(258, 10, 258)
+    const double a = sqrt(2. * K_PI_FULL) * 10.;
+    double b = (T - 258.) * (T - 258.);
+    b = b / (10. * 10.);
+    const double hT = ((1. / a) * exp(-0.5 * b)) / ((1. / a) * exp(-0.5 * 0.));
+    return nf * 0.2 * hT * 2.5e-11 * pow(fmin(ddmean, 3.e-3) * 1.e6, 4.);
+  }
+  const double t0 = -24. + 273.15, t1 = -20. + 273.15, t2 = -16. + 273.15, t3 = -10. + 273.15, t4 = -6. + 273.15;
+  double hT = 0.;
+  if (T >= t0 && T < t1) hT = (0.24 - 0.6) * ((T - t0) / 4.) + 0.6;
+  else if (T >= t1 && T < t2) hT = (2.6 - 0.24) * ((T - t2) / 4.) + 2.6;
+  else if (T >= t2 && T < t3) hT = (0.43 - 2.6) * ((T - t3) / 6.) + 0.43;
+  else if (T >= t3 && T < t4) hT = (0.35 - 0.43) * ((T - t4) / 4.) + 0.35;
+  return nf * ((4. / 9.) * 1.e4 * hT * ddmean);
+}
+
+// mo_salsa_SIP_DF.f90:29-260 dropfracturing.  Lane 0.
+template <typename KT>
+__device__ void sip_dropfracturing(const DevParams &P, const WS<KT> &w, const double *tb, double T, double dt) {
+  const int nprc = P.nprc, nice = P.nice, nspec = P.nused, I0 = P.nliquid, NB = w.NB;
+  const SipT t = sip_tallies(P, w.raw);
+  SipScr q = sip_scratch(P, t);
+  sip_bin_geometry(P, tb, q);
+  for (int e = 0; e < nprc * nice; e++) {
+    t.mdf[e] = t.mdf[e] * dt;
+    t.ndf[e] = t.ndf[e] * dt;
+  }
+  for (int bb = 0; bb < nice; bb++) {
+    const int g = I0 + bb;
+    double vall = 0.;
+    for (int s = 0; s < nspec; s++) vall += w.v(s, g);
+    double *sinkv = q.sinkv + bb * SALSA_NSV;
+    for (int cc = 0; cc < nprc; cc++) {
+      const double nf = t.ndf[cc * nice + bb], mf = t.mdf[cc * nice + bb];
+      if (T < 248.15 || T > 271.15 || nf < 1.e-12 || vall < 1.e-15 || w.numc[g] < K_PRLIM) continue;
+      const double ddmean = pow(mf / nf / K_RHOWA / K_PI6, 1. / 3.);
+      if (ddmean < SIP_DLLIQ_DF) continue;
+      int npmax = 0;
+      for (int k = 0; k < nice; k++) npmax += q.diams[k] <= ddmean;
+      npmax = npmax - 1 > 1 ? npmax - 1 : 1;
+      if (npmax <= 2) continue;
+      const double dN = sip_df_fragments(P.sip_df_mode, T, nf, ddmean);
+      double sv;
+      const double sdv = sip_spread(P, w.volc, NB, g, dN, npmax, q, sv);
+      double ss = 0.;
+      for (int s = 0; s < nspec; s++) {
+        const double sk = w.v(s, g) * sdv / sv;
+        sinkv[s] = sinkv[s] + sk;
+        ss += sk;
+      }
+      q.sinkn[bb] = q.sinkn[bb] + ss / (mf / nf / K_RHOWA);
+    }
+    sip_fold_local(P, q);
+    sip_cap_sink(P, w.numc, w.volc, NB, g, q.sinkn[bb], sinkv);
+  }
+  sip_apply(P, w.numc, w.volc, NB, q.fragn, q.fragv, q.sinkn, q.sinkv);
+}
+
+// mo_salsa_SIP_IIBR.f90:262-291 fragments per collision: Sullivan (mode 1), Sotiropoulou
+// (mode 2), at most 100
+__device__ double sip_iibr_imf(int mode, double T, double dmin) {
+  const double fbr = 280., Tmin = 252., D0 = 0.02;
+  double imf;
+  if (mode == 1) imf = T < Tmin ? 0. : fmax(0., fbr * pow(T - Tmin, 1.2) * exp(-(T - Tmin) / 5.));
+  else imf = T <= Tmin ? 0. : fmax(0., fbr * pow(T - Tmin, 1.2) * exp(-(T - Tmin) / 5.) * dmin / D0);
+  return fmin(imf, 100.0);
+}
+
+// mo_salsa_SIP_IIBR.f90:23-258 iceicecollbreak: each pair (smaller bb, larger cc) breaks
+// the smaller crystal; the source bin's diameters are updated first.  Lane 0.
+template <typename KT>
+__device__ void sip_iceicecollbreak(const DevParams &P, const WS<KT> &w, const double *tb, double T, double dt) {
+  const int nice = P.nice, nspec = P.nused, I0 = P.nliquid, NB = w.NB;
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const SipT t = sip_tallies(P, w.raw);
+  SipScr q = sip_scratch(P, t);
+  sip_bin_geometry(P, tb, q);
+  for (int e = 0; e < nice * nice; e++) {
+    t.mii[e] = t.mii[e] * dt;
+    t.nii[e] = t.nii[e] * dt;
+  }
+  for (int bb = 0; bb < nice; bb++) {
+    const int g = I0 + bb;
+    double *sinkv = q.sinkv + bb * SALSA_NSV;
+    for (int cc = bb; cc < nice; cc++) {
+      const int h = I0 + cc;
+      const double nii = t.nii[cc * nice + bb], mii = t.mii[cc * nice + bb];
+      double vb = 0., vc = 0.;
+      for (int s = 0; s < nspec; s++) { vb += w.v(s, g); vc += w.v(s, h); }
+      if (T < 248.15 || T > 270.15 || nii < 1.e-12 || mii < 1.e-15 || vb < 1.e-15 || w.numc[g] < K_PRLIM ||
+          vc < 1.e-15 || w.numc[h] < K_PRLIM)
+        continue;
+      updateDiameterAll(P, nullptr, w.numc, w.volc, w.dwet, w.ddry, w.dins, w.dnsp, dmid, NB, g);
+      const double v_i = mii / nii / w.rhomean[g];
+      const double dinsphmin = pow(v_i / K_PI6, 1. / 3.);
+      int npmax = 0;
+      for (int k = 0; k < nice; k++) npmax += q.diams[k] <= dinsphmin;
+      npmax = npmax - 1;
+      if (npmax <= 2) continue;
+      const double dN = sip_iibr_imf(P.sip_ib_mode, T, dinsphmin) * nii;
+      double sv;
+      const double sdv = sip_spread(P, w.volc, NB, g, dN, npmax, q, sv);
+      double ss = 0.;
+      for (int s = 0; s < nspec; s++) {
+        const double sk = w.v(s, g) * sdv / sv;
+        sinkv[s] = sinkv[s] + sk;
+        ss += sk;
+      }
+      q.sinkn[bb] = q.sinkn[bb] + ss / v_i;
+    }
+    sip_fold_local(P, q);
+    sip_cap_sink(P, w.numc, w.volc, NB, g, q.sinkn[bb], sinkv);
+  }
+  sip_apply(P, w.numc, w.volc, NB, q.fragn, q.fragv, q.sinkn, q.sinkv);
+}
+
+// secondary_ice (mo_salsa_secondary_ice.f90:6-40), after coagulation (mo_salsa.f90:98-99)
+template <typename KT>
+__device__ void secondary_ice(const DevParams &P, const WS<KT> &w, const double *tb, double T, double dt, int lane) {
+  __syncwarp();
+  if (lane == 0) {
+    if (P.st_siprs) sip_rimesplintering<KT>(P, w, T, dt);
+    if (P.st_sipdf) sip_dropfracturing<KT>(P, w, tb, T, dt);
+    if (P.st_sipib) sip_iceicecollbreak<KT>(P, w, tb, T, dt);
+  }
+  __syncwarp();
+}
+
 template <typename KT>
 __device__ __forceinline__ void source_range(const WS<KT> &w, int t, int g0, int istr, int iend, int nspec, TAcc &a,
                                              int lane) {
@@ -690,7 +1076,7 @@ __device__ void precip_formation(const DevParams &P, const WS<KT> &w, const doub
   }
 }
 
-template <typename KT>
+template <typename KT, bool SIP>
 __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb, double dt, bool diag, int lane) {
   const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, nprc = P.nprc;
   const bool autoc1 = P.st_auto && P.auto_mode == 1;
@@ -713,6 +1099,10 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
       int other = o_first + (kk - kfirst);
       int rel = kk - kfirst;
       list_sinks(w, L, tg, a, lane);
+      if constexpr (SIP) {
+        if (P.st_secice && P.lscgic && lane == 0) sip_drop_numbers<KT>(P, w, tg, 0, K_NLIM);
+        __syncwarp();
+      }
       if (P.lscgcc) {
         if (autoc1) {
           double n = w.numc[tg];
@@ -786,7 +1176,7 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
   }
 }
 
-template <typename KT>
+template <typename KT, bool SIP>
 __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb, double dt, bool diag, int lane) {
   const int nspec = P.nwet, C0 = P.nbins, P0 = P.nbins + P.ncld, nprc = P.nprc, iwa = P.iwa;
   const double *pbins = tb + TAB_PRECPBINS * P.nb_pad;
@@ -798,6 +1188,10 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
     a.zero();
     double num_slf = 0.;
     list_sinks(w, L, tg, a, lane);
+    if constexpr (SIP) {
+      if (P.st_secice && P.lscgip && lane == 0) sip_drop_numbers<KT>(P, w, tg, kk, K_PRLIM);
+      __syncwarp();
+    }
     if (P.lscgpp && kk == nprc - 1 && lane == 0) a.self += 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
     const double D = w.dwet[tg];
     if (P.lscgpa) {
@@ -873,11 +1267,11 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
   }
 }
 
-template <typename KT>
-__device__ void coag_ice(const DevParams &P, const WS<KT> &w, double dt, int lane) {
+template <typename KT, bool SIP>
+__device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, double dt, int lane) {
   const int nspec = P.nused, C0 = P.nbins, P0 = P.nbins + P.ncld, I0 = P.nliquid, nice = P.nice;
   const int iwa = P.iwa, irim = P.irim, ndry = P.ndry;
-  (void)C0; (void)P0;
+  (void)C0; (void)P0; (void)tb;
   for (int kk = 0; kk < nice; kk++) {
     int tg = I0 + kk;
     if (w.numc[tg] < K_PRLIM) continue;
@@ -896,6 +1290,19 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, double dt, int lan
         double E = P.Eiagg_max - fmax(rf_t, rf_t) * (P.Eiagg_max - P.Eiagg_min);
         a.self += E * 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
       }
+    }
+    if constexpr (SIP) {
+      // the secondary-ice tallies of this target, in the reference's order: breakup
+      // numbers (accumulateSink), frozen-drop masses (accumulateSourcePhaseChange),
+      // breakup masses (accumulateSourceIce)
+      if (P.st_secice && lane == 0) {
+        const double *dmid = tb + TAB_DMID * P.nb_pad;
+        if (P.lscgii && P.st_sipib) sip_iibr_numbers<KT>(P, w, kk, rf_t);
+        if (P.lscgic) sip_drop_masses<KT>(P, w, dmid, kk, C0, P.ncld, P.ica_cur, P.fcb_cur, false);
+        if (P.lscgip) sip_drop_masses<KT>(P, w, dmid, kk, P0, P.nprc, 0, P.nprc - 1, true);
+        if (P.lscgii && kk > 0 && P.st_sipib) sip_iibr_masses<KT>(P, w, dmid, kk, rf_t);
+      }
+      __syncwarp();
     }
     // accumulateSourcePhaseChange (:1244-1280)
     if (P.lscgia)
@@ -935,7 +1342,7 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, double dt, int lan
   }
 }
 
-template <typename KT>
+template <typename KT, bool SIP>
 __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *tb, double dt, double T, double pres,
                             bool diag, long long cell, int lane) {
   const double *dmid = tb + TAB_DMID * P.nb_pad;
@@ -973,10 +1380,10 @@ __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *t
   bool any_cloud = P.lscgcc || P.lscgca || P.lscgpc || P.lscgic;
   bool any_precp = P.lscgpp || P.lscgpa || P.lscgpc || P.lscgip;
   bool any_ice = P.lscgii || P.lscgia || P.lscgic || P.lscgip;
-  if (any_ice && T < 273.15) coag_ice<KT>(P, w, dt, lane);
-  if (any_precp) coag_precp<KT>(P, w, tb, dt, diag, lane);
+  if (any_ice && T < 273.15) coag_ice<KT, SIP>(P, w, tb, dt, lane);
+  if (any_precp) coag_precp<KT, SIP>(P, w, tb, dt, diag, lane);
   if (any_aero) coag_aero<KT>(P, w, tb, dt, lane);
-  if (any_cloud) coag_cloud<KT>(P, w, tb, dt, diag, lane);
+  if (any_cloud) coag_cloud<KT, SIP>(P, w, tb, dt, diag, lane);
   bool neg = false;
   for (int b = lane; b < P.ntotal; b += 32) {
     if (w.numc[b] < -1.e-6) neg = true;
@@ -2618,7 +3025,7 @@ __device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *
 #define STAGE_MARK(k) do { } while (0)
 #endif
 
-template <typename KT, bool DIAG>
+template <typename KT, bool DIAG, bool SIP>
 __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, long long cell, int lane) {
 #ifdef SALSA_STAGE_TIMERS
   long long t_stage = clock64();
@@ -2663,13 +3070,19 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   }
   for (int i = lane; i < M_PF; i += 32) w.misc[i] = 0.;
   __syncwarp();
+  if constexpr (SIP) {
+    if (P.st_secice) sip_clear<KT>(P, w, lane);
+  }
   if (P.initialize) equilibration<KT>(P, w, tb, 0.3, T, true, lane);
   // gases in #/m3 (mo_salsa_driver.f90:285-290)
   if (P.raw_gas >= 0 && lane < 5) w.misc[M_GAS + lane] = raw[P.raw_gas + lane] * dn;
   STAGE_MARK(0);
 
   // ---- salsa() ----
-  if (P.st_coag) coagulation<KT>(P, w, tb, dt, T, pres, DIAG, cell, lane);
+  if (P.st_coag) coagulation<KT, SIP>(P, w, tb, dt, T, pres, DIAG, cell, lane);
+  if constexpr (SIP) {
+    if (P.st_secice) secondary_ice<KT>(P, w, tb, T, dt, lane);
+  }
   STAGE_MARK(1);
   if (P.st_cnd) {
     // condensation (mo_salsa_dynamics.f90:276-342): nucleation returns only the 3 nm
@@ -2782,7 +3195,7 @@ __device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
 }
 
 
-template <typename KT, bool DIAG>
+template <typename KT, bool DIAG, bool SIP>
 __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevParams P) {
   extern __shared__ double smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -2809,7 +3222,7 @@ __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevP
       }
     __syncthreads();
     long long q = g * SALSA_CPG + warp;
-    if (q < P.ncells) cell_step<KT, DIAG>(P, w, tb, cell_at(P, q), lane);
+    if (q < P.ncells) cell_step<KT, DIAG, SIP>(P, w, tb, cell_at(P, q), lane);
     __syncthreads();
     // write the group's output rows
     if (okc)
@@ -2833,23 +3246,25 @@ inline size_t smem_bytes(const DevParams &P) {
   return sizeof(double) * ((size_t)P.tab_doubles + (size_t)SALSA_CPG * P.ws_doubles);
 }
 
-template <typename KT, bool DIAG>
+template <typename KT, bool DIAG, bool SIP = false>
 cudaError_t launch_t(const DevParams &P, cudaStream_t st, int grid) {
   size_t sm = smem_bytes(P);
-  cudaError_t e = cudaFuncSetAttribute(salsa_step_kernel<KT, DIAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e =
+      cudaFuncSetAttribute(salsa_step_kernel<KT, DIAG, SIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  salsa_step_kernel<KT, DIAG><<<grid, SALSA_THREADS, sm, st>>>(P);
+  salsa_step_kernel<KT, DIAG, SIP><<<grid, SALSA_THREADS, sm, st>>>(P);
   return cudaGetLastError();
 }
 
-template <typename KT, bool DIAG>
+template <typename KT, bool DIAG, bool SIP = false>
 int blocks_per_sm_t(const DevParams &P) {
   size_t sm = smem_bytes(P);
-  if (cudaFuncSetAttribute(salsa_step_kernel<KT, DIAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+  if (cudaFuncSetAttribute(salsa_step_kernel<KT, DIAG, SIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
       cudaSuccess)
     return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, salsa_step_kernel<KT, DIAG>, SALSA_THREADS, sm) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, salsa_step_kernel<KT, DIAG, SIP>, SALSA_THREADS, sm) !=
+      cudaSuccess)
     return 0;
   return nb;
 }
