@@ -56,6 +56,9 @@ enum {
   SALSA_DIAG_ICEDEP,       /* s_n_icedep     (level 5) */
   SALSA_DIAG_ICEIMM,       /* s_n_iceimm     (level 5) */
   SALSA_DIAG_CONDI,        /* s_m_condi      (level 5) */
+  SALSA_DIAG_SIPDRFR,      /* s_n_sipdrfr    (level 5, lssecice; :412-416) */
+  SALSA_DIAG_SIPRMSPL,     /* s_n_siprmspl   (level 5, lssecice) */
+  SALSA_DIAG_SIPIIBR,      /* s_n_sipiibr    (level 5, lssecice) */
   SALSA_NDIAG
 };
 
@@ -131,6 +134,10 @@ typedef struct {
   double *diag[SALSA_NDIAG];                      /* (nzp,nxp,nyp) out */
   /* GB300 extension: per-cell hygroscopicity override (NULL = species tables) */
   const double *kappa;
+  /* secondary-ice tracers (level 5 with lssecice, required then): crystals produced by
+   * drop fracturing, rime splintering and ice-ice breakup, per ice bin, #/kg, updated
+   * in place (Prog sipdrfr, siprmspl, sipiibr; mo_salsa_driver.f90:259-261, 346-348) */
+  double *sipdrfr, *siprmspl, *sipiibr;           /* (...,nice) */
 } salsa_fields_t;
 
 /* Per-call status.  The reference STOPs or prints in these situations; the

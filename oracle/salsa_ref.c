@@ -81,12 +81,14 @@ typedef struct {
   int phase;
   double nlim, dlim;
   double INdef, chargeTime, chargeTimeMax, chargeCollEnh;
+  double sip[3];   /* SIP_drfr, SIP_rmspl, SIP_iibr (:42-44): crystals from each scheme */
 } Section;
 
 /* Rate (classProcessRates.f90:37-41) */
 typedef struct { double volc[NSP]; double numc; } Rate;
 enum { R_AUTOC = 0, R_AUTOC50, R_AUTOC80, R_ACCR, R_ACCR50, R_ACCR80, R_ACCOLL, R_APCOLL,
-       R_AICOLL, R_ACTIV, R_ICEHOM, R_ICEIMM, R_ICEDEP, R_CONDA, R_CONDC, R_CONDP, R_CONDI, R_N };
+       R_AICOLL, R_ACTIV, R_ICEHOM, R_ICEIMM, R_ICEDEP, R_CONDA, R_CONDC, R_CONDP, R_CONDI,
+       R_SIPDRFR, R_SIPRMSPL, R_SIPIIBR, R_N };
 
 typedef struct { double alpha, beta, gamma, sigma; } Shape;   /* mo_ice_shape.f90:33-35 */
 
@@ -2286,6 +2288,7 @@ static void ice_melt(Cell *w, double ptemp) {
     P->volc[iwa] = P->volc[iwa] + maxfrac * liqvol;
     I->volc[iwa] = (1. - maxfrac) * I->volc[iwa];
     I->volc[irim] = (1. - maxfrac) * I->volc[irim];
+    for (int k = 0; k < 3; k++) I->sip[k] = (1. - maxfrac) * I->sip[k];   /* :453-456 */
   }
 }
 
@@ -2635,6 +2638,8 @@ static void rimesplintering(Cell *w, double ptemp, double ptstep) {
       double ss = 0.;
       for (int s = 0; s < nspec; s++) ss += sinkv[s];
       sinknumc[bb] = sinknumc[bb] + ss / (PI6 * pow(ddmean, 3.0));
+      ice[splbin - 1].sip[1] = ice[splbin - 1].sip[1] + dN;   /* :134-136 */
+      rate_acc_n(&w->rate[R_SIPRMSPL], dN / ptstep);
     }
     if (ice[bb].numc < sinknumc[bb]) {                       /* :152-158 */
       sinknumc[bb] = ice[bb].numc;
@@ -2732,6 +2737,10 @@ static void dropfracturing(Cell *w, double ptemp, double ptstep) {
       double ss = 0.;
       for (int s = 0; s < nspec; s++) ss += sinkv[s];
       sinknumc[bb] = sinknumc[bb] + ss / v_i;
+      double sdn = 0.;                                      /* :165-167 */
+      for (int k = 0; k < npmax; k++) ice[k].sip[0] = ice[k].sip[0] + dNb[k];
+      for (int k = 0; k < nice; k++) sdn += dNb[k];
+      rate_acc_n(&w->rate[R_SIPDRFR], sdn / ptstep);
     }
     for (int k = 0; k < nice; k++) {                        /* :175-176, before the safeguard */
       fragnumc[k] = fragnumc[k] + fragn_loc[k];
@@ -2827,6 +2836,10 @@ static void iceicecollbreak(Cell *w, double ptemp, double ptstep) {
       double ss = 0.;
       for (int s = 0; s < nspec; s++) ss += sinkv[s];
       sinknumc[bb] = sinknumc[bb] + ss / v_i;
+      double sdn = 0.;                                      /* :187-189 */
+      for (int k = 0; k < npmax; k++) ice[k].sip[2] = ice[k].sip[2] + dNb[k];
+      for (int k = 0; k < nice; k++) sdn += dNb[k];
+      rate_acc_n(&w->rate[R_SIPIIBR], sdn / ptstep);
     }
     for (int k = 0; k < nice; k++) {                        /* :187-188, before the safeguard */
       fragnumc[k] = fragnumc[k] + fragn_loc[k];
@@ -3102,6 +3115,7 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
     return SALSA_E_ARG;
   if (level == 5 && (!f->rsi || !f->nice || !f->mice || !f->nicet || !f->micet)) return SALSA_E_ARG;
   if (level == 5 && g->ice_theta_dist && !f->indef) return SALSA_E_ARG;
+  if (level == 5 && g->lssecice.sw && (!f->sipdrfr || !f->siprmspl || !f->sipiibr)) return SALSA_E_ARG;
   if (lcharge && !f->chargeTime) return SALSA_E_ARG;
   if (g->lscndgas && (!f->gaero || !f->gaerot)) return SALSA_E_ARG;
   if (g->lsactiv.sw && g->lsactiv.mode == 2 && !f->wp) return SALSA_E_ARG;
@@ -3207,6 +3221,11 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
           for (int nc = 0; nc < nwet; nc++)
             s->volc[nc] = min_[icat][p + plane * (nc * cat_nb + nbloc)] * dn / c->rhoice[nc];
           s->volc[irim] = min_[icat][p + plane * (irim * cat_nb + nbloc)] * dn / c->rhori;
+          if (g->lssecice.sw) {                                            /* :258-262 */
+            s->sip[0] = f->sipdrfr[p + plane * nbloc] * dn;
+            s->sip[1] = f->siprmspl[p + plane * nbloc] * dn;
+            s->sip[2] = f->sipiibr[p + plane * nbloc] * dn;
+          }
         }
         s->numc = nin[icat][p + plane * nbloc] * dn;
         updateRhomean(cc, s);
@@ -3245,6 +3264,11 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
           }
           long long str = p + plane * (irim * cat_nb + nbloc);
           mten[icat][str] = mten[icat][str] + ((s->volc[irim] * c->rhori / dn) - min_[icat][str]) / tstep;
+          if (g->lssecice.sw) {                                            /* :345-349 */
+            f->sipdrfr[p + plane * nbloc] = s->sip[0] / dn;
+            f->siprmspl[p + plane * nbloc] = s->sip[1] / dn;
+            f->sipiibr[p + plane * nbloc] = s->sip[2] / dn;
+          }
         }
         nten[icat][p + plane * nbloc] = nten[icat][p + plane * nbloc] + ((s->numc / dn) - nin[icat][p + plane * nbloc]) / tstep;
         if (!isfinite(s->numc)) s_nan++;
@@ -3283,7 +3307,10 @@ int salsa_ref_run(salsa_ref_ctx_t *c, int nzp, int nxp, int nyp, int ns, double 
         d[SALSA_DIAG_ICEDEP] = R[R_ICEDEP].numc / dn;
         d[SALSA_DIAG_ICEIMM] = R[R_ICEIMM].numc / dn;
         d[SALSA_DIAG_CONDI] = (R[R_CONDI].volc[iwa] * c->rhoic + R[R_CONDI].volc[irim] * c->rhori) / dn;
-        int nd = (level == 5) ? SALSA_NDIAG : SALSA_DIAG_AICOLL;
+        d[SALSA_DIAG_SIPDRFR] = R[R_SIPDRFR].numc / dn;                     /* :412-416 */
+        d[SALSA_DIAG_SIPRMSPL] = R[R_SIPRMSPL].numc / dn;
+        d[SALSA_DIAG_SIPIIBR] = R[R_SIPIIBR].numc / dn;
+        int nd = (level == 5) ? (g->lssecice.sw ? SALSA_NDIAG : SALSA_DIAG_CONDI + 1) : SALSA_DIAG_AICOLL;
         for (int i = 0; i < nd; i++) if (f->diag[i]) f->diag[i][p] = d[i];
       }
       if (carry_over) { memcpy(c->carry, w->all, sizeof(Section) * c->ntotal); c->carry_valid = 1; }

@@ -54,6 +54,9 @@ def main(tags):
         arrays = {f"out_{k}": v.numpy() for k, v in out.items()}
         if "indef" in fields:
             arrays["indef_after"] = fields["indef"].numpy()
+        for k in ("sipdrfr", "siprmspl", "sipiibr"):
+            if k in fields:
+                arrays[f"{k}_after"] = fields[k].numpy()
         np.savez_compressed(os.path.join(HERE, f"{tag}.npz"), **arrays)
         print("wrote", tag, sorted(arrays))
 

@@ -34,6 +34,10 @@ def sip_state(mode, splinter=True, coag_only=True, seed=7, X=6, Y=6, Z=8, scheme
             mi[k, j] = n * 1.e-3 * v / nd * rhoi[k] / dn
         mi[nd, j] = n * 0.5 * v * rhoi[nd] / dn           # pristine ice
         mi[nd + 1, j] = n * 0.5 * v * rhoi[nd + 1] / dn   # rime
+    # the secondary-ice tracers (#/kg per ice bin), seeded so that their passage through
+    # the step (x dn on the way in, / dn on the way out, melting) shows
+    for name in ("sipdrfr", "siprmspl", "sipiibr"):
+        f[name] = f["nice"] * 0.1 * torch.rand(f["nice"].shape, generator=g, dtype=torch.float64)
     if coag_only:
         for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
             sw.sw = 0

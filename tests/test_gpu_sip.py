@@ -27,14 +27,21 @@ def _gpu_or_skip(inp):
 
 
 def _parity(inp, rtol, eps):
-    _, gpu = _gpu_or_skip(inp)
-    _, ref = oracle_run(inp)
+    fg, gpu = _gpu_or_skip(inp)
+    fr, ref = oracle_run(inp)
     env = envelope(inp, ref, eps)
     rep = check(inp, gpu, ref, env, rtol)
     print(rep)
     for k, r in rep.items():
         assert r["violations"] <= VIOL_FRAC * r["n"], (k, r)
         assert r["frac_within"] >= FRAC_WITHIN, (k, r)
+    # the tracers (updated in place) and the three rate diagnostics, relative to each
+    # field's largest value
+    pairs = [(fg[k].cpu(), fr[k]) for k in ("sipdrfr", "siprmspl", "sipiibr")]
+    pairs += [(gpu["diag"][i], ref["diag"][i]) for i in (17, 18, 19)]
+    for a, b in pairs:
+        scale = float(b.abs().max())    # zero for the rates of schemes that are off
+        assert float((a - b).abs().max()) <= 1e-6 * scale
     return ref
 
 

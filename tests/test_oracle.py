@@ -55,6 +55,10 @@ def test_golden_fixtures(tag):
         # bitwise on the generating platform; other libm builds may move ulp-sensitive bins
         frac = float((diff <= 1e-12 * np.maximum(np.abs(b), 1e-300)).mean())
         assert frac > 0.995, (k, frac)
+    for k in ("sipdrfr", "siprmspl", "sipiibr"):    # the secondary-ice tracers, updated in place
+        if f"{k}_after" in ref.files:
+            a, b = f[k].numpy(), ref[f"{k}_after"]
+            assert float((np.abs(a - b) <= 1e-12 * np.maximum(np.abs(b), 1e-300)).mean()) > 0.995, k
 
 
 def test_layout_matches_reference_construction():

@@ -103,3 +103,25 @@ def test_ice_ice_breakup_conserves_ice_volume_and_adds_fragments(mode):
     out = (T < 248.15) | (T > 270.15)
     assert int(out.sum()) > 0
     assert torch.equal(a["nice"][:, out], b["nice"][:, out])
+
+
+@pytest.mark.parametrize("scheme,mode,tracer,rate", [("lssiprimespln", 1, "siprmspl", 18),
+                                                      ("lssipdropfrac", 1, "sipdrfr", 17),
+                                                      ("lssipicecollbreak", 1, "sipiibr", 19)])
+def test_tracers_gain_what_the_rates_report(scheme, mode, tracer, rate):
+    """Each scheme adds its fragments to its tracer (per ice bin, mo_salsa_SIP_*.f90) and
+    to its rate diagnostic (per second, run_SALSA :412-416): summed over the ice bins,
+    the tracer's gain is the rate times the time step."""
+    inp = sip_state(mode, scheme=scheme)
+    before = inp.fields[tracer].clone()
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(inp.cfg).run(inp, f, out, time=1.0)
+    assert rc == 0
+    gain = (f[tracer] - before).sum(0)
+    expect = out["diag"][rate] * inp.dt
+    assert float(expect.max()) > 0
+    assert float((gain - expect).abs().max()) <= 1e-12 * float(expect.abs().max())
+    others = [t for t in ("sipdrfr", "siprmspl", "sipiibr") if t != tracer]
+    for t in others:                          # the other schemes are off: their tracers pass through
+        assert float((f[t] - inp.fields[t]).abs().max()) <= 1e-15 * float(inp.fields[t].abs().max())

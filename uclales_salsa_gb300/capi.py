@@ -14,9 +14,11 @@ DIAG_NAMES = [
     "s_m_autoc", "s_m_autoc80", "s_m_autoc50", "s_m_accr", "s_m_accr80", "s_m_accr50",
     "s_m_ACcoll_dry", "s_m_APcoll_dry", "s_n_activ", "s_m_conda", "s_m_condc", "s_m_condp",
     "s_m_AIcoll_dry", "s_n_icehom", "s_n_icedep", "s_n_iceimm", "s_m_condi",
+    "s_n_sipdrfr", "s_n_siprmspl", "s_n_sipiibr",
 ]
 NDIAG = len(DIAG_NAMES)
 NDIAG_LEVEL4 = 12
+NDIAG_LEVEL5 = 17          # without the secondary-ice rates (lssecice off)
 
 SALSA_OK, SALSA_E_ARG, SALSA_E_UNSUPPORTED, SALSA_E_CUDA, SALSA_E_NUMERIC, SALSA_E_NODEV = range(6)
 ERROR_NAMES = {0: "ok", 1: "bad argument", 2: "unsupported configuration", 3: "CUDA error",
@@ -96,6 +98,7 @@ class Fields(C.Structure):
         ("pa_vactd", _PD),
         ("diag", _PD * NDIAG),
         ("kappa", _PD),
+        ("sipdrfr", _PD), ("siprmspl", _PD), ("sipiibr", _PD),
     ]
 
 
@@ -161,7 +164,7 @@ class Status(C.Structure):
 FIELD_INPUTS = ["press", "temp", "rsl", "rsi", "dn", "rp", "wp", "naero", "ncloud", "nprecp", "nice",
                 "maero", "mcloud", "mprecp", "mice", "gaero", "kappa"]
 FIELD_INOUT = ["rpt", "naerot", "ncloudt", "nprecpt", "nicet", "maerot", "mcloudt", "mprecpt", "micet",
-               "indef", "chargeTime", "gaerot", "pa_nactd", "pa_vactd"]
+               "indef", "chargeTime", "gaerot", "pa_nactd", "pa_vactd", "sipdrfr", "siprmspl", "sipiibr"]
 
 
 def ptr_of(addr):

@@ -406,8 +406,17 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   for (int s = 0; s < B.nwet; s++)
     for (int k = 0; k < ncld; k++) add(-1, salsa::FO_VACT, s * ncld + k, salsa::ROW_OUT);
   B.raw_diag = (int)rows.size();
-  int ndiag = (g.level == 5) ? SALSA_NDIAG : SALSA_DIAG_AICOLL;
+  // the secondary-ice rates follow the level-5 diagnostics when lssecice is on
+  const bool sipsw = g.level == 5 && g.lssecice.sw;
+  int ndiag = (g.level == 5) ? (sipsw ? SALSA_NDIAG : SALSA_DIAG_CONDI + 1) : SALSA_DIAG_AICOLL;
   for (int i = 0; i < ndiag; i++) add(-1, salsa::FO_DIAG0 + i, 0, salsa::ROW_OUT);
+  // the secondary-ice tracers, per ice bin, in and out in place (mo_salsa_driver.f90:259-261, 346-348)
+  B.raw_sip = -1;
+  if (sipsw) {
+    B.raw_sip = (int)rows.size();
+    for (int k = 0; k < 3; k++)
+      for (int b = 0; b < nice; b++) add(salsa::FI_SIPDRFR + k, salsa::FO_SIPDRFR + k, b, salsa::ROW_INOUT);
+  }
   B.nrows = (int)rows.size();
   B.nraw = B.nrows;
 
@@ -533,7 +542,8 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
       // the secondary-ice tallies and the schemes' scratch after the kernel triangle
       n = (n + 1) & ~(size_t)1;
       B.sip_off = (int)n;
-      n += 4 * (size_t)nprc * nice + 2 * (size_t)nice * nice + 7 * (size_t)nice + 3 * (size_t)nice * SALSA_NSV + SALSA_NSV;
+      n += 4 * (size_t)nprc * nice + 2 * (size_t)nice * nice + 7 * (size_t)nice + 3 * (size_t)nice * SALSA_NSV +
+           4 * (size_t)nice + 4;
       int spl = 0;   // mo_salsa_SIP_RS.f90:72: ice bins whose lower limit is below the 10 um splinters
       for (int bb = 0; bb < nice; bb++) spl += std::pow(t.vlo[B.nliquid + bb] / PI6, 1. / 3.) < 10.e-6;
       B.sip_splbin = spl < 1 ? 1 : spl;
@@ -661,6 +671,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   if (level == 5 && (!f->rsi || !f->nice || !f->mice || !f->nicet || !f->micet)) return SALSA_E_ARG;
   if (level == 5 && g.ice_theta_dist && !f->indef) return SALSA_E_ARG;
   if (lcharge && !f->chargeTime) return SALSA_E_ARG;
+  if (level == 5 && g.lssecice.sw && (!f->sipdrfr || !f->siprmspl || !f->sipiibr)) return SALSA_E_ARG;
   if (g.lscndgas && (!f->gaero || !f->gaerot)) return SALSA_E_ARG;
   if (g.lsactiv.sw && g.lsactiv.mode == 2 && !f->wp) return SALSA_E_ARG;
   if (cudaSetDevice(h->device) != cudaSuccess) return SALSA_E_NODEV;
@@ -756,8 +767,12 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   fio(f->pa_nactd, nb[1], salsa::FO_NACT, 0);
   fio(f->pa_vactd, (long long)nw * nb[1], salsa::FO_VACT, 0);
   fio(g.lscndgas ? f->gaerot : nullptr, 5, salsa::FO_GAEROT, 1);
-  int ndiag = (level == 5) ? SALSA_NDIAG : SALSA_DIAG_AICOLL;
+  const bool sipsw = level == 5 && g.lssecice.sw;
+  int ndiag = (level == 5) ? (sipsw ? SALSA_NDIAG : SALSA_DIAG_CONDI + 1) : SALSA_DIAG_AICOLL;
   for (int i = 0; i < ndiag; i++) fio(g.diagnostics ? f->diag[i] : nullptr, 1, salsa::FO_DIAG0 + i, 0);
+  fio(sipsw ? f->sipdrfr : nullptr, nb[3], salsa::FO_SIPDRFR, 1);
+  fio(sipsw ? f->siprmspl : nullptr, nb[3], salsa::FO_SIPRMSPL, 1);
+  fio(sipsw ? f->sipiibr : nullptr, nb[3], salsa::FO_SIPIIBR, 1);
 
   int side = -1;
   for (auto &x : fl) {
@@ -780,6 +795,7 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
       Q.fout[x.fo] = dp;
       if (x.fo == salsa::FO_INDEF) Q.fin[salsa::FI_INDEF] = dp;
       if (x.fo == salsa::FO_CHARGE) Q.fin[salsa::FI_CHARGE] = dp;
+      if (x.fo >= salsa::FO_SIPDRFR && x.fo <= salsa::FO_SIPIIBR) Q.fin[salsa::FI_SIPDRFR + (x.fo - salsa::FO_SIPDRFR)] = dp;
     }
   };
   // order pre-pass and step kernel over the cells of Q, on stream s

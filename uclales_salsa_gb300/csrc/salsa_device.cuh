@@ -53,12 +53,13 @@ namespace salsa {
 enum {
   FI_PRESS = 0, FI_TEMP, FI_RSL, FI_RSI, FI_RP, FI_DN, FI_WP, FI_KAPPA,
   FI_NAERO, FI_NCLOUD, FI_NPRECP, FI_NICE, FI_MAERO, FI_MCLOUD, FI_MPRECP, FI_MICE,
-  FI_INDEF, FI_CHARGE, FI_GAERO, FI_N
+  FI_INDEF, FI_CHARGE, FI_GAERO, FI_SIPDRFR, FI_SIPRMSPL, FI_SIPIIBR, FI_N
 };
 // output field ids (index into DevParams::fout)
 enum {
   FO_RPT = 0, FO_NAEROT, FO_NCLOUDT, FO_NPRECPT, FO_NICET, FO_MAEROT, FO_MCLOUDT, FO_MPRECPT, FO_MICET,
-  FO_INDEF, FO_CHARGE, FO_NACT, FO_VACT, FO_GAEROT, FO_DIAG0, FO_N = FO_DIAG0 + 17
+  FO_INDEF, FO_CHARGE, FO_NACT, FO_VACT, FO_GAEROT, FO_SIPDRFR, FO_SIPRMSPL, FO_SIPIIBR, FO_DIAG0,
+  FO_N = FO_DIAG0 + 20   // the diagnostics of the header's enum, the secondary-ice rates last
 };
 // row modes
 enum { ROW_IN = 0, ROW_TEND = 1, ROW_INOUT = 2, ROW_OUT = 3 };
@@ -135,6 +136,7 @@ struct DevParams {
   // offset of the tally region inside each warp's workspace (doubles)
   int st_secice, st_siprs, st_sipdf, st_sipib;
   int sip_rs_mode, sip_df_mode, sip_ib_mode, sip_splbin, sip_off;
+  int raw_sip;   // first of the 3 x nice tracer rows (sipdrfr, siprmspl, sipiibr), or -1
 };
 
 // block table layout (per bin, padded to nb_pad): offsets in units of nb_pad

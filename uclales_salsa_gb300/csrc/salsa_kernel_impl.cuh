@@ -547,28 +547,33 @@ struct TAcc {
 // p = nprc, V = SALSA_NSV:
 //   nfrzn_rs, mfrzn_rs, nfrzn_df, mfrzn_df  p x n each (precipitation or cloud row, ice bin)
 //   nii_ibr, mii_ibr                        n x n each
-//   scratch                                 7 n + 3 n V + V
+//   scratch                                 7 n + 3 n V
+//   tracers SIP_drfr, SIP_rmspl, SIP_iibr   3 n (per m3 of air during the step)
+//   the schemes' rates, melting flags       4, n
 // ----------------------------------------------------------------------------------------
 #define SIP_DLLIQ_RS 24.0e-6   // mo_salsa_SIP_RS.f90:17: smallest drop that splinters on riming
 #define SIP_DLLIQ_DF 100.e-6   // mo_salsa_SIP_DF.f90:18: smallest drop that fractures on freezing
+#define SALSA_DIAG_SIPDRFR_SLOT 17   // diagnostic slot of s_n_sipdrfr (then s_n_siprmspl, s_n_sipiibr)
 
 struct SipT {
-  double *nrs, *mrs, *ndf, *mdf, *nii, *mii, *scr;
+  double *nrs, *mrs, *ndf, *mdf, *nii, *mii, *scr, *tr, *rate, *melt;
 };
 __device__ __forceinline__ SipT sip_tallies(const DevParams &P, double *wsbase) {
-  const int pn = P.nprc * P.nice, nn = P.nice * P.nice;
+  const int n = P.nice, pn = P.nprc * n, nn = n * n;
   double *t = wsbase + P.sip_off;
-  return {t, t + pn, t + 2 * pn, t + 3 * pn, t + 4 * pn, t + 4 * pn + nn, t + 4 * pn + 2 * nn};
-}
-__host__ __device__ __forceinline__ int sip_doubles(int nprc, int nice) {
-  return 4 * nprc * nice + 2 * nice * nice + 7 * nice + 3 * nice * SALSA_NSV + SALSA_NSV;
+  double *scr = t + 4 * pn + 2 * nn, *tr = scr + 7 * n + 3 * n * SALSA_NSV;
+  return {t, t + pn, t + 2 * pn, t + 3 * pn, t + 4 * pn, t + 4 * pn + nn, scr, tr, tr + 3 * n, tr + 3 * n + 4};
 }
 
+// zero tallies and rates; the tracers from their rows, per m3 of air (mo_salsa_driver.f90:258-262)
 template <typename KT>
-__device__ void sip_clear(const DevParams &P, const WS<KT> &w, int lane) {
+__device__ void sip_clear(const DevParams &P, const WS<KT> &w, double dn, int lane) {
   double *t = w.raw + P.sip_off;
   const int n = 4 * P.nprc * P.nice + 2 * P.nice * P.nice;
   for (int e = lane; e < n; e += 32) t[e] = 0.;
+  const SipT s = sip_tallies(P, w.raw);
+  for (int e = lane; e < 3 * P.nice; e += 32) s.tr[e] = w.raw[P.raw_sip + e] * dn;
+  if (lane < 4) s.rate[lane] = 0.;
   __syncwarp();
 }
 
@@ -693,7 +698,7 @@ __device__ void sip_apply(const DevParams &P, double *numc, double *volc, int NB
 
 // Scratch of the schemes (inside the tally region).
 struct SipScr {
-  double *fragn, *sinkn, *fragn_loc, *dNb, *dVb, *diams, *bw, *fragv, *sinkv, *fragv_loc, *sv1;
+  double *fragn, *sinkn, *fragn_loc, *dNb, *dVb, *diams, *bw, *fragv, *sinkv, *fragv_loc;
 };
 __device__ __forceinline__ SipScr sip_scratch(const DevParams &P, const SipT &t) {
   const int n = P.nice, V = SALSA_NSV;
@@ -701,8 +706,8 @@ __device__ __forceinline__ SipScr sip_scratch(const DevParams &P, const SipT &t)
   SipScr q;
   q.fragn = p; q.sinkn = p + n; q.fragn_loc = p + 2 * n; q.dNb = p + 3 * n; q.dVb = p + 4 * n;
   q.diams = p + 5 * n; q.bw = p + 6 * n;
-  q.fragv = p + 7 * n; q.sinkv = q.fragv + n * V; q.fragv_loc = q.sinkv + n * V; q.sv1 = q.fragv_loc + n * V;
-  for (int e = 0; e < 7 * n + 3 * n * V + V; e++) p[e] = 0.;
+  q.fragv = p + 7 * n; q.sinkv = q.fragv + n * V; q.fragv_loc = q.sinkv + n * V;
+  for (int e = 0; e < 7 * n + 3 * n * V; e++) p[e] = 0.;
   return q;
 }
 // ice bin centres and widths in diameter (DF :82-88, IIBR :75-81)
@@ -785,6 +790,8 @@ __device__ void sip_rimesplintering(const DevParams &P, const WS<KT> &w, double 
         ss += sk;
       }
       q.sinkn[bb] = q.sinkn[bb] + ss / (K_PI6 * pow(ddmean, 3.0));
+      t.tr[nice + splbin - 1] = t.tr[nice + splbin - 1] + dN;   // :134-136
+      t.rate[1] += dN / dt;
     }
     sip_cap_sink(P, w.numc, w.volc, NB, g, q.sinkn[bb], sinkv);
   }
@@ -847,6 +854,10 @@ __device__ void sip_dropfracturing(const DevParams &P, const WS<KT> &w, const do
         ss += sk;
       }
       q.sinkn[bb] = q.sinkn[bb] + ss / (mf / nf / K_RHOWA);
+      double sdn = 0.;                                           // :165-167
+      for (int k = 0; k < npmax; k++) t.tr[k] = t.tr[k] + q.dNb[k];
+      for (int k = 0; k < nice; k++) sdn += q.dNb[k];
+      t.rate[0] += sdn / dt;
     }
     sip_fold_local(P, q);
     sip_cap_sink(P, w.numc, w.volc, NB, g, q.sinkn[bb], sinkv);
@@ -905,6 +916,10 @@ __device__ void sip_iceicecollbreak(const DevParams &P, const WS<KT> &w, const d
         ss += sk;
       }
       q.sinkn[bb] = q.sinkn[bb] + ss / v_i;
+      double sdn = 0.;                                           // :187-189
+      for (int k = 0; k < npmax; k++) t.tr[2 * nice + k] = t.tr[2 * nice + k] + q.dNb[k];
+      for (int k = 0; k < nice; k++) sdn += q.dNb[k];
+      t.rate[2] += sdn / dt;
     }
     sip_fold_local(P, q);
     sip_cap_sink(P, w.numc, w.volc, NB, g, q.sinkn[bb], sinkv);
@@ -3071,7 +3086,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   for (int i = lane; i < M_PF; i += 32) w.misc[i] = 0.;
   __syncwarp();
   if constexpr (SIP) {
-    if (P.st_secice) sip_clear<KT>(P, w, lane);
+    if (P.st_secice) sip_clear<KT>(P, w, dn, lane);
   }
   if (P.initialize) equilibration<KT>(P, w, tb, 0.3, T, true, lane);
   // gases in #/m3 (mo_salsa_driver.f90:285-290)
@@ -3101,7 +3116,23 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
     if (P.ice_theta_dist) ice_nucl_SE<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
     else ice_nucl_classic<KT>(P, w, tb, T, rv, rs, rsi, dt, kappa, DIAG, lane);
   }
+  if constexpr (SIP) {
+    // ice_melt's bins (numbers not below prlim) before it runs: their tracers melt with them
+    if (P.st_secice && P.st_icemelt) {
+      const SipT s = sip_tallies(P, w.raw);
+      for (int k = lane; k < P.nice; k += 32) s.melt[k] = w.numc[P.nliquid + k] < K_PRLIM ? 0. : 1.;
+      __syncwarp();
+    }
+  }
   if (P.st_icemelt) ice_melt<KT>(P, w, tb, T, lane);
+  if constexpr (SIP) {
+    if (P.st_secice && P.st_icemelt && T >= 273.15) {   // mo_salsa_cloud_ice.f90:453-456
+      const SipT s = sip_tallies(P, w.raw);
+      for (int e = lane; e < 3 * P.nice; e += 32)
+        if (s.melt[e % P.nice] != 0.) s.tr[e] = (1. - 0.999) * s.tr[e];
+      __syncwarp();
+    }
+  }
   STAGE_MARK(4);
   if (P.lsdistupdate) distr_update<KT>(P, w, tb, lane);
   STAGE_MARK(5);
@@ -3132,6 +3163,13 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   if (!(P.st_activ && P.activ_mode == 2))
     for (int i = lane; i < P.ncld * (1 + nwet); i += 32) raw[P.raw_nact + i] = 0.;
   if (lane == 0) raw[RW_RV] = (rv - rv_old) / dt;
+  if constexpr (SIP) {
+    if (P.st_secice) {   // :345-349 and :412-416
+      const SipT s = sip_tallies(P, w.raw);
+      for (int e = lane; e < 3 * P.nice; e += 32) raw[P.raw_sip + e] = s.tr[e] / dn;
+      if (P.raw_diag >= 0 && lane < 3) raw[P.raw_diag + SALSA_DIAG_SIPDRFR_SLOT + lane] = s.rate[lane] / dn;
+    }
+  }
   if (P.raw_gas >= 0 && lane < 5)   // :369-384
     raw[P.raw_gas + lane] = ((w.misc[M_GAS + lane] / dn) - raw[P.raw_gas + lane]) / dt;
   if (DIAG && P.raw_diag >= 0 && lane == 0) {

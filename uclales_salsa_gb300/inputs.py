@@ -295,7 +295,7 @@ def make_outputs(inp, device=None, with_diag=True):
         out["nicet"] = z(lay.nice)
         out["micet"] = z((lay.nwet + 1) * lay.nice)
     if with_diag:
-        nd = 17 if inp.level == 5 else 12
+        nd = (20 if inp.cfg.lssecice.sw else 17) if inp.level == 5 else 12
         out["diag"] = z(nd)
     if inp.cfg.lscndgas:
         out["gaerot"] = z(5)
