@@ -568,10 +568,15 @@ static void accumulateSink(Cell *w, int nbcoll, int itrgt, int istr, int iend, c
     if (c->st_sipdf && (trgtphase == 3 || trgtphase == 2)) {
       const Section *t = trgtphase == 3 ? &w->precp[itrgt] : &w->cloud[itrgt];
       const int row = trgtphase == 3 ? itrgt : 0;
-      for (int ll = istr; ll <= iend; ll++)
+      for (int ll = istr; ll <= iend; ll++) {
         if (coll[ll].numc > coll[ll].nlim && coll[ll].dwet < t->dwet && t->dwet > DLLIQ_DF && t->numc > t->nlim &&
             coll[ll].numc > coll[ll].nlim)
           w->nfrzn_df[row * c->nice + ll] += Eagg[ll] * KIDX(zcc, nbcoll, itrgt, ll) * coll[ll].numc * t->numc * fix_coag;
+        /* :916-921, :936-941: Phillips' full scheme also counts drops collected by larger crystals */
+        if (g->lssipdropfrac.mode == 4 && coll[ll].numc > coll[ll].nlim && coll[ll].dwet >= t->dwet &&
+            t->dwet > DLLIQ_DF && t->numc > t->nlim)
+          w->nfrzn_df[row * c->nice + ll] += Eagg[ll] * KIDX(zcc, nbcoll, itrgt, ll) * coll[ll].numc * t->numc * fix_coag;
+      }
     }
     if (c->st_siprs && (trgtphase == 3 || trgtphase == 2)) {
       const Section *t = trgtphase == 3 ? &w->precp[itrgt] : &w->cloud[itrgt];
@@ -725,6 +730,13 @@ static void accumulateSourcePhaseChange(Cell *w, int nbtrgt, int iice, int iwa, 
         if (ph != 2 && ph != 3) continue;
         if (w->ice[itrgt].dnsp < coll[ll].dwet && coll[ll].dwet > DLLIQ_DF && w->ice[itrgt].numc > w->ice[itrgt].nlim &&
             coll[ll].numc > coll[ll].nlim) {
+          const int ix = ph == 3 ? ll : 0;
+          w->mfrzn_df[ix * c->nice + itrgt] +=
+              KIDX(zcc, nbtrgt, ix, itrgt) * coll[ll].volc[iwa] * w->ice[itrgt].numc * rhocoll * fix_coag;
+        }
+        /* :1331-1343: Phillips' full scheme, drops collected by more massive crystals */
+        if (c->cfg.lssipdropfrac.mode == 4 && w->ice[itrgt].dnsp >= coll[ll].dwet && coll[ll].dwet > DLLIQ_DF &&
+            coll[ll].numc > coll[ll].nlim && w->ice[itrgt].numc > w->ice[itrgt].nlim) {
           const int ix = ph == 3 ? ll : 0;
           w->mfrzn_df[ix * c->nice + itrgt] +=
               KIDX(zcc, nbtrgt, ix, itrgt) * coll[ll].volc[iwa] * w->ice[itrgt].numc * rhocoll * fix_coag;
@@ -2684,9 +2696,66 @@ static double df_fragments(int mode, double T, double nfrzn, double ddmean) {
   return nfrzn * ((4. / 9.) * 1.e4 * hT * ddmean);
 }
 
+/* mo_salsa_SIP_DF.f90:534-608: Phillips et al. (2018) fits in x = log10 of the drop
+   diameter in mm, limited to 0.06-1.6 mm (beta: 0 below 0.4 mm, upper limit only) */
+static double ph_x(double d) { return log10(fmaxd(fmind(d * 1.e3, 1.6), 0.06)); }
+static double ph_cubic(double x, double c1, double c2, double c3, double c4) {
+  return (c1 * cube(x)) + (c2 * sq(x)) + (c3 * x) + c4;
+}
+static double ph_beta(double d) {
+  if (d < 0.4e-3) return 0.;
+  const double x = log10(fmind(d * 1.e3, 1.6));
+  return (-0.1839 * sq(x)) + (-0.2017 * x) + -0.0512;
+}
+/* :431-451 fragments per frozen drop, mode 1 (drop heavier than the crystal), eq. 1 */
+static double df_phillips_mode1_total(double d, double T) {
+  const double tc = T - 273.15, x = ph_x(d);
+  const double T0 = ph_cubic(x, -1.3999, -5.3285, -3.9847, -15.0332);
+  const double zeta = pow(10., ph_cubic(x, 2.4268, 3.3274, 2.0783, 1.2927));
+  const double eta = pow(10., ph_cubic(x, 0.1242, -0.2316, -0.9874, -0.0827));
+  return ph_beta(d) * tc + (zeta * sq(eta)) / (sq(tc - T0) + sq(eta));
+}
+/* :479-532 mode 2 (crystal heavier than the drop), eq. 7: from the collision's kinetic
+   energy over the drop's surface energy */
+static double df_phillips_mode2(const salsa_ref_ctx_t *c, double p, double T, double d, double disph, double dinsph,
+                                double mrim, double mpri, double ncice, double rhoip) {
+  const double rhoa = p / (RD * T);
+  const double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+  const double mfp = (1.656e-10 * T + 1.828e-8) * PSTAND / p;
+  double knud = 2. * mfp / dinsph;
+  double beta = 1. + knud * (1.142 + 0.558 * exp(-0.999 / knud));
+  Shape ish;
+  getShapeCoefficients(c, &ish, mpri, mrim, ncice);
+  const double vti = terminal_vel(disph, rhoip, rhoa, visc, beta, 4, &ish, dinsph);
+  knud = 2. * mfp / d;
+  beta = 1. + knud * (1.142 + 0.558 * exp(-0.999 / knud));
+  const double vtd = terminal_vel(d, c->rhowa, rhoa, visc, beta, 3, &ish, d);
+  const double mip = (mrim + mpri) / ncice, mdp = c->rhowa * PI6 * cube(d);
+  const double K0 = 0.5 * (mip * mdp / (mdp + mip)) * sq(vtd - vti);
+  const double DE = K0 / (SURFW0 * PI * sq(d));
+  const double fT = -4200. * (T - 273.15) / 3.3e5;   /* cwa, alf (mo_submctl.f90:268, 281) */
+  return 3. * fmind(4. * fT, 1.) * (1. - fT) * fmaxd(DE - 0.2, 0.);
+}
+/* :313-372 df_phillips_full_total: the regime by the masses of drop and crystal */
+static double df_phillips_full_total(const salsa_ref_ctx_t *c, double p, double T, double d, const Section *ice,
+                                     double nf) {
+  const int nspec = c->nused;
+  double sv = 0.;
+  for (int s = 0; s < nspec - 1; s++) sv += ice->volc[s];
+  const double mrim = ice->volc[nspec - 1] * c->rhori, mpri = sv * c->rhoic, ncice = ice->numc;
+  const double mip = (mrim + mpri) / ncice, mdp = c->rhowa * PI6 * cube(d);
+  if (mdp > mip) {
+    if (d < 50.e-6 && T > 267.15) return 0.;
+    return fmind(df_phillips_mode1_total(d, T), 100.) * nf;
+  }
+  if (d < 150.e-6) return 0.;
+  const double rhoip = (mrim * c->rhori + mpri * c->rhoic) / (mrim + mpri);
+  return fmind(df_phillips_mode2(c, p, T, d, ice->dwet, ice->dnsp, mrim, mpri, ncice, rhoip), 100.) * nf;
+}
+
 /* mo_salsa_SIP_DF.f90:29-260 dropfracturing (per cell): the fragments of each frozen
    drop size go to the ice bins below it with a d^-3 number distribution */
-static void dropfracturing(Cell *w, double ptemp, double ptstep) {
+static void dropfracturing(Cell *w, double ppres, double ptemp, double ptstep) {
   const salsa_ref_ctx_t *c = w->c;
   const int nprc = c->nprc, nice = c->nice, nspec = c->nused, mode = c->cfg.lssipdropfrac.mode;
   const double tmin = 248.15, tmax = 271.15;
@@ -2717,7 +2786,8 @@ static void dropfracturing(Cell *w, double ptemp, double ptstep) {
       for (int k = 0; k < nice; k++) npmax += icediams[k] <= ddmean;
       npmax = npmax - 1 > 1 ? npmax - 1 : 1;
       if (npmax <= 2) continue;
-      const double dN = df_fragments(mode, ptemp, nf, ddmean);
+      const double dN = mode == 4 ? df_phillips_full_total(c, ppres, ptemp, ddmean, &ice[bb], nf)
+                                  : df_fragments(mode, ptemp, nf, ddmean);
       for (int k = 0; k < nice; k++) dNb[k] = dVb[k] = 0.;
       double Nnorm = 0.;
       for (int k = 0; k < npmax; k++) dNb[k] = 1. / cube(icediams[k]);
@@ -2880,7 +2950,7 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
   if (c->st_coag) coagulation(w, ptstep, ptemp, ppres);
   if (c->st_secice) {                                                   /* :98-99 */
     if (c->st_siprs) rimesplintering(w, ptemp, ptstep);
-    if (c->st_sipdf) dropfracturing(w, ptemp, ptstep);
+    if (c->st_sipdf) dropfracturing(w, ppres, ptemp, ptstep);
     if (c->st_sipib) iceicecollbreak(w, ptemp, ptstep);
   }
   if (c->st_cnd) {
@@ -2950,7 +3020,7 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
   if (cfg->lssecice.sw && cfg->level == 5 &&
       ((cfg->lssipicecollbreak.sw && cfg->lssipicecollbreak.mode != 1 && cfg->lssipicecollbreak.mode != 2) ||
        (cfg->lssiprimespln.sw && cfg->lssiprimespln.mode != 1 && cfg->lssiprimespln.mode != 2) ||
-       (cfg->lssipdropfrac.sw && (cfg->lssipdropfrac.mode < 1 || cfg->lssipdropfrac.mode > 3))))
+       (cfg->lssipdropfrac.sw && (cfg->lssipdropfrac.mode < 1 || cfg->lssipdropfrac.mode > 4))))
     return SALSA_E_UNSUPPORTED;
   /* nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);
      nj3 outside 1-3 STOPs once a cell nucleates (:600-602) */

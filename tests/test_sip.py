@@ -63,7 +63,7 @@ def test_hallett_mossop_counts_rime_mass_and_mossop_counts_drops():
     assert float(d1.sum()) > 100 * float(d2.sum()) > 0
 
 
-@pytest.mark.parametrize("mode", [1, 2, 3])
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
 def test_drop_fracturing_conserves_ice_volume_and_adds_small_crystals(mode):
     """Frozen drops above 100 um shatter into fragments spread over the ice bins below
     their size: ice volume per species conserved, crystals added, small bins gain."""
