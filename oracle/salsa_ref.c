@@ -2851,9 +2851,68 @@ static double iibr_imf(int mode, double T, double dmin) {
   return fmind(imf, 100.0);
 }
 
+/* mo_salsa_SIP_IIBR.f90:588-607 mip and :552-585 getvelocity: mean crystal mass of an ice
+   bin, and its fall speed with the bin's shape coefficients and rime-weighted density */
+static void iibr_masses(const salsa_ref_ctx_t *c, const Section *s, double *mrim, double *mpri) {
+  double v = 0.;
+  for (int k = 0; k <= c->iwa; k++) v += s->volc[k];
+  *mrim = s->volc[c->irim] * c->rhori;
+  *mpri = v * c->rhoic;
+}
+static double iibr_mip(const salsa_ref_ctx_t *c, const Section *s) {
+  double mrim, mpri;
+  iibr_masses(c, s, &mrim, &mpri);
+  return (mrim + mpri) / s->numc;
+}
+static double iibr_velocity(const salsa_ref_ctx_t *c, const Section *s, double visc, double rhoa, double mfp) {
+  const double knud = 2. * mfp / s->dnsp;
+  const double beta = 1. + knud * (1.142 + 0.558 * exp(-0.999 / knud));
+  double mrim, mpri;
+  iibr_masses(c, s, &mrim, &mpri);
+  const double rhoip = (mrim * c->rhori + mpri * c->rhoic) / (mrim + mpri);
+  Shape sh;
+  getShapeCoefficients(c, &sh, mpri, mrim, s->numc);
+  return terminal_vel(s->dwet, rhoip, rhoa, visc, beta, 4, &sh, s->dnsp);
+}
+/* :505-548 kinetic_collision_energy of two ice bins */
+static double iibr_k0(const salsa_ref_ctx_t *c, double p, double T, const Section *a, const Section *b) {
+  const double rhoa = p / (RD * T);
+  const double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+  const double mfp = (1.656e-10 * T + 1.828e-8) * PSTAND / p;
+  const double v1 = iibr_velocity(c, a, visc, rhoa, mfp), m1 = iibr_mip(c, a);
+  const double v2 = iibr_velocity(c, b, visc, rhoa, mfp), m2 = iibr_mip(c, b);
+  return (m1 * m2 / (m1 + m2)) * (1.7 * sq(v1 - v2) + 0.3 * v1 * v2);
+}
+/* :323-401 imf_phillips_mod: Phillips et al. (2017) breakup with the corrections of
+   Sotiropoulou et al. (2020); asperity parameters by the rime fraction of `small`, the
+   supersaturation over ice ssi and the distance from -15 C */
+static double imf_phillips_mod(const salsa_ref_ctx_t *c, double p, double T, const Section *large,
+                               const Section *small, double disphmin, double ssi) {
+  const double T0 = 258.15;
+  double mrim, mpri;
+  iibr_masses(c, small, &mrim, &mpri);
+  const double rimfrac = mrim / (mrim + mpri);
+  double a0, C, g, Nmax;
+  if (rimfrac > 0.5) {
+    a0 = exp(14.74 * ssi + 14.28);
+    C = exp(20.15 * ssi + 13.78);
+    g = ssi + 0.55;
+    Nmax = 600.;
+  } else {
+    a0 = 4.75E7;
+    C = 1.0E08;
+    g = 0.78;
+    Nmax = 500.;
+  }
+  const double Am = a0 / 3. + fmaxd(2. / 3. * a0 - 1. / 9. * a0 * fabs(T - T0), 0.);
+  const double alpha = PI * sq(disphmin);
+  const double K0 = iibr_k0(c, p, T, large, small);
+  return fmind(alpha * Am * (1 - exp(-pow(C * K0 / alpha / Am, g))), Nmax);
+}
+
 /* mo_salsa_SIP_IIBR.f90:23-258 iceicecollbreak (per cell): each pair (smaller bb, larger cc)
    breaks the smaller crystal into fragments spread over the bins below it as d^-3 */
-static void iceicecollbreak(Cell *w, double ptemp, double ptstep) {
+static void iceicecollbreak(Cell *w, double ppres, double ptemp, double ptstep, double prv, double prsi) {
   const salsa_ref_ctx_t *c = w->c;
   const int nice = c->nice, nspec = c->nused, mode = c->cfg.lssipicecollbreak.mode;
   const double tmin = 248.15, tmax = 270.15;
@@ -2887,7 +2946,14 @@ static void iceicecollbreak(Cell *w, double ptemp, double ptstep) {
       for (int k = 0; k < nice; k++) npmax += icediams[k] <= dinsphmin;
       npmax = npmax - 1;
       if (npmax <= 2) continue;
-      const double dN = iibr_imf(mode, ptemp, dinsphmin) * nii;
+      double dN;
+      if (mode == 3) {   /* :148-155: bb passes as the larger crystal, as the reference writes it */
+        const double disphmin = pow((mii / nii / ice[bb].rhomean) / PI6, 1. / 3.);
+        const double ssi = fmaxd(0., prv / prsi - 1.0);
+        dN = fmind(imf_phillips_mod(c, ppres, ptemp, &ice[bb], &ice[cc], disphmin, ssi), 600.0) * nii;
+      } else {
+        dN = iibr_imf(mode, ptemp, dinsphmin) * nii;
+      }
       for (int k = 0; k < nice; k++) dNb[k] = dVb[k] = 0.;
       double Nnorm = 0.;
       for (int k = 0; k < npmax; k++) dNb[k] = 1. / cube(icediams[k]);
@@ -2951,7 +3017,7 @@ static void salsa_cell(Cell *w, double ppres, double *prv, double prs, double pr
   if (c->st_secice) {                                                   /* :98-99 */
     if (c->st_siprs) rimesplintering(w, ptemp, ptstep);
     if (c->st_sipdf) dropfracturing(w, ppres, ptemp, ptstep);
-    if (c->st_sipib) iceicecollbreak(w, ptemp, ptstep);
+    if (c->st_sipib) iceicecollbreak(w, ppres, ptemp, ptstep, *prv, prsi);
   }
   if (c->st_cnd) {
     /* condensation :276-342.  nucleation (mo_salsa_nucleation.f90:72-625) only returns the
@@ -3018,7 +3084,7 @@ int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out) {
      breakup (mo_salsa_SIP_IIBR.f90) in modes 1-2; Phillips' schemes (drop fracturing
      mode 4, breakup mode 3) are not restated */
   if (cfg->lssecice.sw && cfg->level == 5 &&
-      ((cfg->lssipicecollbreak.sw && cfg->lssipicecollbreak.mode != 1 && cfg->lssipicecollbreak.mode != 2) ||
+      ((cfg->lssipicecollbreak.sw && (cfg->lssipicecollbreak.mode < 1 || cfg->lssipicecollbreak.mode > 3)) ||
        (cfg->lssiprimespln.sw && cfg->lssiprimespln.mode != 1 && cfg->lssiprimespln.mode != 2) ||
        (cfg->lssipdropfrac.sw && (cfg->lssipdropfrac.mode < 1 || cfg->lssipdropfrac.mode > 4))))
     return SALSA_E_UNSUPPORTED;

@@ -348,11 +348,10 @@ def test_unsupported_and_bad_configs():
             c.lssecice.sw = 1
             getattr(c, sub).sw, getattr(c, sub).mode = 1, mode
         return m
-    # secondary ice: rime splintering (modes 1, 2), drop fracturing (modes 1-4, Phillips'
-    # full scheme included) and ice-ice breakup (modes 1, 2) are restated; Phillips'
-    # breakup (mode 3) is not
+    # secondary ice: rime splintering (modes 1, 2), drop fracturing (modes 1-4) and ice-ice
+    # breakup (modes 1-3), Phillips' schemes included, are restated
     for mod, code in ((lambda c: setattr(c, "nsnucl", 4), 2), (sip("lssipdropfrac", 5), 2), (sip("lssipdropfrac", 4), 0),
-                      (sip("lssipdropfrac", 2), 0), (sip("lssipicecollbreak", 3), 2), (sip("lssipicecollbreak", 2), 0),
+                      (sip("lssipdropfrac", 2), 0), (sip("lssipicecollbreak", 4), 2), (sip("lssipicecollbreak", 3), 0), (sip("lssipicecollbreak", 2), 0),
                       (sip("lssiprimespln", 3), 2),
                       (sip("lssiprimespln", 1), 0),
                       (lambda c: setattr(c, "nspec_dry", 0), 1), (lambda c: c.set_species(["SO4", "XX"]), 1)):

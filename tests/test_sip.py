@@ -84,7 +84,7 @@ def test_drop_fracturing_conserves_ice_volume_and_adds_small_crystals(mode):
     assert torch.equal(a["nice"][:, out], b["nice"][:, out])
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_ice_ice_breakup_conserves_ice_volume_and_adds_fragments(mode):
     """Collisions of a crystal with larger ones break it into fragments spread over the
     bins below its size (Sullivan; Sotiropoulou): volume conserved, crystals added, and
