@@ -1,13 +1,8 @@
 """GPU parity of the step's secondary-ice form (rime splintering, drop fracturing,
 ice-ice breakup) against the oracle, with the step's parity criterion.
-
-The secondary-ice form is compiled and wired in, but salsa_gb300_init refuses lssecice
-until this test has passed on a GB300: while it does, the test skips.
 """
 import pytest
 
-from uclales_salsa_gb300 import capi
-from uclales_salsa_gb300.api import SalsaError
 from sip_cases import sip_state
 from test_gpu_parity import oracle_run, gpu_run, envelope, check, VIOL_FRAC, FRAC_WITHIN
 
@@ -17,17 +12,8 @@ SCHEMES = [("lssiprimespln", 1), ("lssiprimespln", 2), ("lssipdropfrac", 1), ("l
            ("lssipdropfrac", 3), ("lssipicecollbreak", 1), ("lssipicecollbreak", 2)]
 
 
-def _gpu_or_skip(inp):
-    try:
-        return gpu_run(inp)
-    except SalsaError as e:
-        if e.code == capi.SALSA_E_UNSUPPORTED:
-            pytest.skip("salsa_gb300_init refuses lssecice: the GPU form has not been enabled")
-        raise
-
-
 def _parity(inp, rtol, eps):
-    fg, gpu = _gpu_or_skip(inp)
+    fg, gpu = gpu_run(inp)
     fr, ref = oracle_run(inp)
     env = envelope(inp, ref, eps)
     rep = check(inp, gpu, ref, env, rtol)

@@ -35,12 +35,6 @@ int blocks_per_sm_ds(const DevParams &);
 int blocks_per_sm_fs(const DevParams &);
 }  // namespace salsa
 
-// Secondary ice production on the GPU: the step's secondary-ice form (salsa_k_ds.cu,
-// salsa_k_fs.cu) is compiled and wired in, but has not been compared with the oracle on
-// a GPU yet.  Until it has, salsa_gb300_init refuses a configuration that switches
-// lssecice on.
-static const bool kSecondaryIceChecked = false;
-
 using salsa::DevParams;
 using salsa::Row;
 
@@ -230,10 +224,8 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   if (g.nspec_dry < 1 || g.nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
   if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
   if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
-  // processes outside this build (the init check mirrors the oracle's)
-  if (g.lssecice.sw && !kSecondaryIceChecked) return SALSA_E_UNSUPPORTED;
-  // the schemes' modes the oracle restates: Phillips' full forms (drop fracturing mode 4,
-  // breakup mode 3) are not built
+  // processes outside this build: Phillips' full secondary-ice forms (drop fracturing
+  // mode 4, breakup mode 3) are restated in the oracle but not in the step kernel
   if (g.lssecice.sw) {
     const salsa_switch_t &rs = g.lssiprimespln, &df = g.lssipdropfrac, &ib = g.lssipicecollbreak;
     if (rs.sw && (rs.mode < 1 || rs.mode > 2)) return SALSA_E_UNSUPPORTED;
