@@ -2,26 +2,29 @@
 
 A step is one SALSA call over every interior cell of the workload
 (run_SALSA, src/src_salsa/mo_salsa_driver.f90:112-435).  Default workload: the
-256x256x128 grid (8,388,608 cells) with 30 % cloudy cells, level 5, dt = 1 s.
+384x384x160 grid (23,592,960 cells), level 5, dt = 1 s, 10 % cloudy cells in
+convective columns with ice, the other 90 % clear at RH 40-85 %.  Its fields (about
+158 GB) stay resident on the device; the steps read them in place (the IN deficit,
+the only input a step rewrites, is put back before the error and end-to-end legs).
 
   value  -- FP64 (parity) form, cell-steps/s, inputs resident in HBM, CUDA events on
             the launch stream around exactly K steps (after W warm-up steps).
-  mixed  -- the FP32-mixed form on the same inputs.
-  e2e    -- FP64 form through the C-ABI with pinned HOST buffers: the host->device
+  mixed  -- the FP32-mixed form on the same inputs, and its per-field error against
+            the FP64 form over every interior cell (one step of each from one state).
+  e2e    -- FP64 form through the C-ABI with page-locked HOST buffers: the host->device
             copy of every array and the device->host copy of the results are inside
             the timed region (the C-ABI moves them in y-slabs that overlap the
-            computation).
+            computation).  The buffers are one exactly sized allocation registered with
+            the driver; the leg is skipped, with a note, when the host lacks the memory.
   roofline -- algorithmic bytes per cell-step (8 * (3S + T + G + I + A + D)) over the
             measured HBM copy bandwidth; the step is FP64-pipe bound, so the fraction is
             small and the ncu FP64 pipe figures are in profiles/.
   cpu_baseline -- the FP64 CPU oracle (a C restatement of the reference path; the
-            Fortran cannot be built here) on a bounded sample, all host threads.
+            Fortran cannot be built here) on a bounded sample, all host threads, and on
+            a smaller sample with one thread; the CPU model from lscpu.
+  post_step -- tend_constrain2, SALSA_diagnostics and sedim_SALSA over the grid.
   adjoint -- forward and adjoint time of the gradient harness (65,536 warm cells, 60
             coagulation + condensation steps of 0.5 s, checkpoints every step).
-
---workload grid384x384x160 (23.6 M cells) holds about 158 GB of fields on the device;
-run it with --in-place (the steps read the workload's own fields instead of a copy)
-and --no-e2e (the end-to-end leg would pin as much host memory again).
 
 --impl reference times that CPU implementation alone on bounded samples of the same
 workload.  With torchrun, every rank runs the workload on its own GPU (independent
@@ -30,6 +33,7 @@ over the slowest rank's time.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -102,6 +106,64 @@ def field_bytes(d):
     return sum(v.numel() * v.element_size() for v in d.values())
 
 
+def host_buffers(sources):
+    """Host copies of `sources` (name -> tensor to copy, or torch.Size of a zeroed array) in
+    one exactly sized host allocation registered with the CUDA driver (page-locked).
+    torch's pinned allocator rounds every block up to a power of two, which would take up
+    to twice the host memory for the largest workload."""
+    import torch
+    total = sum(math.prod(v.shape) for v in sources.values())
+    buf = torch.zeros(total, dtype=torch.float64)
+    rc = torch._C._cudart.cudaHostRegister(buf.data_ptr(), total * 8, 0)
+    if int(rc) != 0:
+        raise RuntimeError(f"cudaHostRegister failed ({rc})")
+    out, off = {}, 0
+    for k, v in sources.items():
+        n = math.prod(v.shape)
+        view = buf[off:off + n].view(v.shape)
+        if isinstance(v, torch.Tensor):
+            view.copy_(v)
+        out[k] = view
+        off += n
+    return buf, out
+
+
+def mem_available_bytes():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def form_errors(inp, fields, out_a, out_b, tol=1e-6):
+    """Per-field relative error of the new state x = old + tendency * dt of form b against
+    form a, over every interior cell, on the device: max, RMS and the fraction within tol.
+    The scale of a bin value is max(|x_a|, |old|, floor) with the parity tests' floors."""
+    import torch
+    from parity import STATE_OF, floor_of, interior
+    res = {}
+    for name, st in STATE_OF.items():
+        if name not in out_a or name not in out_b:
+            continue
+        n, s2, mx, over = 0, 0.0, 0.0, 0
+        for b in range(out_a[name].shape[0] if out_a[name].dim() == 4 else 1):
+            pick = (lambda t: t[b]) if out_a[name].dim() == 4 else (lambda t: t)
+            I = lambda t: interior(pick(t), inp.nzp, inp.nxp, inp.nyp)
+            old = I(fields[st])
+            xa, xb = old + I(out_a[name]) * inp.dt, old + I(out_b[name]) * inp.dt
+            scale = torch.maximum(xa.abs(), old.abs()).clamp(min=floor_of(name))
+            rel = (xb - xa).abs() / scale
+            n += rel.numel()
+            s2 += float((rel * rel).sum())
+            mx = max(mx, float(rel.max()))
+            over += int((rel > tol).sum())
+        res[name] = {"max": mx, "rms": (s2 / n) ** 0.5, "frac_within_1e-6": 1.0 - over / n}
+    return res
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as tdist
@@ -118,17 +180,30 @@ def run_gb300(args):
             tdist.barrier()
         torch.cuda.synchronize()
 
+    def tmax(x):
+        t = torch.tensor([x], device=dev)
+        if world > 1:
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+
     inp = make_inputs(args.workload, dev, precision=0, diagnostics=1)
     ncell = inp.ncells
     level = inp.level
+    fields = inp.fields           # the steps read the workload's fields; only the IN deficit changes
+    indef0 = fields["indef"].clone() if "indef" in fields else None
+
+    def restore():
+        if indef0 is not None:
+            fields["indef"].copy_(indef0)
+
     results = {}
     stream = torch.cuda.Stream(device=dev)
+    outs = make_outputs(inp)
     for form in (0, 1):
         inp.cfg.precision = form
         step = SalsaStep(inp.cfg)
-        fields = inp.fields if args.in_place else {k: v.clone() for k, v in inp.fields.items()}
-        outs = make_outputs(inp)
-        for _ in range(args.warmup):
+        warm = args.warmup if form == 0 else min(args.warmup, 3)
+        for _ in range(warm):
             step.run(inp, fields, outs, time=1.0, stream=stream)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -149,53 +224,82 @@ def run_gb300(args):
         if sampler:
             sampler.__exit__()
             results["clocks"] = sampler.summary()
-        if form == 0 and not args.no_post and not args.in_place:   # the post step changes the fields
-            results["post"] = post_bench(step, inp, fields, outs, stream, peak_gbs())
-        ms = e0.elapsed_time(e1)
-        t = torch.tensor([ms], device=dev)
-        if world > 1:
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        results[form] = dict(ms_total=float(t.item()), kernel_ms=sum(kms) / len(kms), launches=nlaunch)
+        results[form] = dict(ms_total=tmax(e0.elapsed_time(e1)), kernel_ms=sum(kms) / len(kms), launches=nlaunch,
+                             warmup=warm)
         step.close()
-        del fields, outs
+    del outs
+    torch.cuda.empty_cache()
+
+    # mixed form against the FP64 form: one step of each from the same state
+    errors = None
+    if not args.no_errors:
+        res = {}
+        for form in (0, 1):
+            inp.cfg.precision = form
+            restore()
+            o = make_outputs(inp, with_diag=False)
+            step = SalsaStep(inp.cfg)
+            step.run(inp, fields, o, time=1.0, stream=stream)
+            torch.cuda.synchronize()
+            step.close()
+            res[form] = o
+        restore()
+        errors = form_errors(inp, fields, res[0], res[1])
+        del res
         torch.cuda.empty_cache()
+    inp.cfg.precision = 0
 
     # bytes a step moves across the boundary: the C-ABI copies the interior y rows
     # (nyp - 4 of nyp) of every array it uses in, outputs included (so that their
     # values outside the interior cells come back unchanged), and of the tendencies,
     # outputs and IN deficit back out
-    inp.cfg.precision = 0
     outs_meta = make_outputs(inp, device="meta")
     rows = (inp.nyp - 4) / inp.nyp
-    inputs_b = sum(v.numel() * 8 for k, v in inp.fields.items() if k in (
+    inputs_b = sum(v.numel() * 8 for k, v in fields.items() if k in (
         "press", "temp", "rsl", "rsi", "rp", "dn", "wp", "naero", "ncloud", "nprecp", "nice", "maero", "mcloud",
         "mprecp", "mice", "indef"))
-    indef_b = inp.fields["indef"].numel() * 8 if "indef" in inp.fields else 0
+    indef_b = fields["indef"].numel() * 8 if "indef" in fields else 0
     h2d = int(round((inputs_b + field_bytes(outs_meta)) * rows))
     d2h = int(round((field_bytes(outs_meta) + indef_b) * rows))
-    e2e_s = None
+    e2e_s, e2e_note, e2e_warm = None, None, min(args.warmup, 3)
     if not args.no_e2e:
-        # end to end through the C-ABI with pinned host buffers (FP64 form)
-        def pinned(v):
-            return torch.empty(v.shape, dtype=v.dtype, pin_memory=True).copy_(v)
+        # end to end through the C-ABI with page-locked host buffers (FP64 form)
+        need = field_bytes(fields) + field_bytes(outs_meta)
+        avail = mem_available_bytes()
+        if avail < need + 24 * 2 ** 30:
+            e2e_note = f"skipped: {need / 1e9:.0f} GB of host buffers, {avail / 1e9:.0f} GB available"
+        else:
+            restore()
+            src = dict(fields)
+            src.update({"out_" + k: v.shape for k, v in outs_meta.items()})
+            buf, host = host_buffers(src)
+            host_in = {k: v for k, v in host.items() if not k.startswith("out_")}
+            host_out = {k[4:]: v for k, v in host.items() if k.startswith("out_")}
+            del src
+            step = SalsaStep(inp.cfg)
+            for _ in range(e2e_warm):
+                step.run(inp, host_in, host_out, time=1.0)   # the first call allocates the staging slots
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                step.run(inp, host_in, host_out, time=1.0)
+            barrier()
+            e2e_s = tmax(time.perf_counter() - t0)
+            step.close()
+            torch._C._cudart.cudaHostUnregister(buf.data_ptr())
+            del host_in, host_out, host, buf
+    else:
+        e2e_note = "not measured (--no-e2e)"
 
-        host_in = {k: pinned(v) for k, v in inp.fields.items()}
-        host_out = {k: pinned(v) for k, v in make_outputs(inp, device="cpu").items()}
-        del inp.fields
-        torch.cuda.empty_cache()
+    post = None
+    if not args.no_post:
         step = SalsaStep(inp.cfg)
-        step.run(inp, host_in, host_out, time=1.0)        # allocates the staging buffers once
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            step.run(inp, host_in, host_out, time=1.0)
-        barrier()
-        e2e_s = time.perf_counter() - t0
-        te = torch.tensor([e2e_s], device=dev)
-        if world > 1:
-            tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
-        e2e_s = float(te.item())
+        outs = make_outputs(inp)
+        step.run(inp, fields, outs, time=1.0, stream=stream)
+        post = post_bench(step, inp, fields, outs, stream, peak_gbs())   # changes the fields (last use)
         step.close()
+        del outs
+        torch.cuda.empty_cache()
 
     r0 = results[0]
     value = world * ncell * args.steps / (r0["ms_total"] / 1e3)
@@ -204,17 +308,17 @@ def run_gb300(args):
     bytes_cell = 8 * ALG_DOUBLES[level]
     peak, peak_src = peak_gbs()
     achieved = bytes_cell * ncell / (r0["kernel_ms"] / 1e3) / 1e9
-    # DRAM bytes per cell from one ncu capture of the same kernel on a 131072-cell block of
-    # this workload (dram__bytes_read.sum + dram__bytes_write.sum / cells), scaled to the
-    # cells of one launch; the FP64 pipe figure is that capture's sm__pipe_fp64_cycles_active.
-    traffic, fp64_pipe = None, None
-    tp = os.path.join(ROOT, "profiles", "salsa_step_kernel_grid256.json")
+    # DRAM bytes per cell and FP64-pipe activity from the committed ncu capture of the step
+    # kernel on a block of this workload, scaled to the cells of one launch (ncu cannot run
+    # inside the timed region)
+    traffic, fp64_pipe, tsrc = None, None, None
+    tp = os.path.join(ROOT, "profiles", "salsa_step_kernel.json")
     if os.path.exists(tp):
         try:
-            prof = json.load(open(tp))
-            if prof["workload"] == args.workload:
-                traffic = prof["dram_bytes_per_cell"]["fp64"] * ncell
-                fp64_pipe = prof["fp64_pipe_active_pct"]["fp64"]
+            prof = json.load(open(tp))[args.workload]
+            traffic = prof["dram_bytes_per_cell"]["fp64"] * ncell
+            fp64_pipe = prof["fp64_pipe_active_pct"]
+            tsrc = prof["source"]
         except Exception:
             traffic = None
     line = {
@@ -225,18 +329,24 @@ def run_gb300(args):
         "config": {"workload": args.workload, "cells": ncell, "level": level, "dt_s": inp.dt,
                    "l2": "inputs larger than L2 (%.1f GB per step)" % ((h2d + d2h) / 1e9)},
         "mixed": {"value": mixed, "unit": "cell-steps/s", "ms_per_step": results[1]["ms_total"] / args.steps,
-                  "speedup_vs_fp64": mixed / value, "dtype": "f32 kernels + f64 state"},
-        "e2e": ({"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-                if e2e is not None else {"value": None, "note": "not measured (--no-e2e)"}),
+                  "warmup": results[1]["warmup"], "speedup_vs_fp64": mixed / value,
+                  "dtype": "f32 collision kernels, mass-transfer coefficients and pair sums + f64 state",
+                  "errors_vs_fp64": errors,
+                  "errors_note": "one step of each form from the same state, every interior cell; relative to "
+                                 "max(|x_fp64|, |x_old|, floor) of the new state x = old + tendency * dt"},
+        "e2e": ({"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                 "warmup": e2e_warm, "host_buffers": "page-locked (cudaHostRegister), one allocation"}
+                if e2e is not None else {"value": None, "note": e2e_note}),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_cell": bytes_cell,
+                     "traffic": traffic, "traffic_source": tsrc, "peak_source": peak_src,
+                     "algorithmic_bytes_per_cell": bytes_cell,
                      "note": "the step is bound by the FP64 pipe, not HBM",
                      "fp64_pipe_active_pct_ncu": fp64_pipe},
         "gpu_launches": r0["launches"],
         "clocks": results.get("clocks"),
     }
-    if "post" in results:
-        line["post_step"] = results["post"]
+    if post:
+        line["post_step"] = post
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = chain_bench(dev)
     if rank == 0 and not args.no_cpu_baseline:
@@ -325,21 +435,42 @@ def oracle_sample(workload, cells):
     return make_inputs(workload, "cpu", X=side, Y=side, Z=Z)
 
 
-def cpu_baseline(workload, cells):
-    import torch
+def cpu_model():
+    """The host CPU's model name (lscpu), e.g. Neoverse-V2 on the GB300 hosts."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return None
+
+
+def cpu_baseline(workload, cells, single_core_cells=32768):
+    """The FP64 oracle on a sample of the workload with every host thread, and on a
+    smaller sample with one thread."""
     from uclales_salsa_gb300.inputs import make_outputs
     from oracle_ref import Oracle
-    inp = oracle_sample(workload, cells)
-    o = Oracle(inp.cfg)
-    f = {k: v.clone() for k, v in inp.fields.items()}
-    out = make_outputs(inp)
-    t0 = time.perf_counter()
-    o.run(inp, f, out, time=1.0)
-    dt = time.perf_counter() - t0
-    ncores = os.cpu_count()
-    return {"value": inp.ncells / dt, "unit": "cell-steps/s", "cores": ncores, "kind": "port",
+    res = {}
+    for n, threads in ((cells, 0), (single_core_cells, 1)):
+        inp = oracle_sample(workload, n)
+        o = Oracle(inp.cfg)
+        f = {k: v.clone() for k, v in inp.fields.items()}
+        out = make_outputs(inp)
+        t0 = time.perf_counter()
+        o.run(inp, f, out, time=1.0, nthreads=threads)
+        res[threads] = (inp, time.perf_counter() - t0)
+        del f, out
+    inp, dt = res[0]
+    inp1, dt1 = res[1]
+    return {"value": inp.ncells / dt, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": f"{inp.ncells} cells ({inp.nxp - 4}x{inp.nyp - 4}x{inp.nzp - 2}) of {workload}, FP64 oracle, "
-                      f"{dt:.1f} s"}
+                      f"{dt:.1f} s",
+            "single_core": {"value": inp1.ncells / dt1, "unit": "cell-steps/s",
+                            "sample": f"{inp1.ncells} cells ({inp1.nxp - 4}x{inp1.nyp - 4}x{inp1.nzp - 2}), "
+                                      f"{dt1:.1f} s"}}
 
 
 def run_reference(args):
@@ -367,7 +498,7 @@ def run_reference(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, run_SALSA layout)",
             "config": {"workload": args.workload, "cells_per_step": inp.ncells},
             "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": sample},
+                             "cpu_model": cpu_model(), "sample": sample},
             "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -378,12 +509,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="grid256x256x128")
+    ap.add_argument("--workload", default="grid384x384x160")
     ap.add_argument("--cpu-sample-cells", type=int, default=3145728)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-post", action="store_true", help="skip the tend_constrain2 / SALSA_diagnostics timing")
-    ap.add_argument("--in-place", action="store_true", help="steps read the workload's fields, not a copy")
+    ap.add_argument("--no-errors", action="store_true", help="skip the mixed-vs-FP64 error block")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg through host buffers")
     args = ap.parse_args()
     if args.impl == "reference":

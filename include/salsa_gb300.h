@@ -198,9 +198,11 @@ int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns,
  * 2,097,152 interior cells (larger grids return SALSA_E_ARG).  Every GPU that loads
  * the library holds that array until the process exits.  The array keeps the last
  * call's contents; each call clears the status counters on its stream and rewrites
- * the whole order list.  The first call on a handle looks up the array's device
- * address on the handle's device (cudaGetSymbolAddress); make that first call before
- * any stream capture.  All calls on one device share the array: calls that overlap
+ * the whole order list.  salsa_gb300_init, not the first call, loads the step's
+ * kernel modules on the handle's device (the array is part of one of them: with lazy
+ * module loading a module's device memory is taken when it loads) and looks up the
+ * array's device address there (cudaGetSymbolAddress); so create the handle before
+ * the caller's pool takes the free memory.  All calls on one device share the array: calls that overlap
  * on the GPU (other streams, other handles on that device) race on it, so the
  * caller must serialise them. */
 #define SALSA_NOALLOC_MAXCELLS 2097152

@@ -3235,6 +3235,13 @@ void salsa_ref_counters(const salsa_ref_ctx_t *c, long long out[5]) {
   for (int i = 0; i < 5; i++) out[i] = c->counters[i];
 }
 
+/* The sticky process states set_SALSA_runtime keeps (mo_salsa_driver.f90:445-474). */
+void salsa_ref_states(const salsa_ref_ctx_t *c, int out[12]) {
+  const int v[12] = {c->st_coag, c->st_cnd, c->st_auto, c->st_activ, c->st_icenucl, c->st_icemelt,
+                     c->st_secice, c->st_siprs, c->st_sipdf, c->st_sipib, c->st_freeRH, c->st_freeTheta};
+  for (int i = 0; i < 12; i++) out[i] = v[i];
+}
+
 /* ======================================================================
  * mo_salsa_driver.f90:112-435 run_SALSA (+ set_SALSA_runtime :445-474)
  * ====================================================================== */

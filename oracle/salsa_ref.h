@@ -59,6 +59,11 @@ int salsa_ref_layout(const salsa_ref_ctx_t *ctx, int *nbins, int *ncld, int *npr
  * [4] condensation substeps. */
 void salsa_ref_counters(const salsa_ref_ctx_t *ctx, long long out[5]);
 
+/* Process states after the last run (set_SALSA_runtime): lscoag, lscnd, lsauto,
+ * lsactiv, lsicenucl, lsicemelt, lssecice, the three secondary-ice schemes,
+ * lsfreeRH, lsFreeTheta. */
+void salsa_ref_states(const salsa_ref_ctx_t *ctx, int out[12]);
+
 /* Single-function probes used by the closed-form tests. */
 double salsa_ref_terminal_vel(double diam, double rhop, double rhoa, double visc,
                               double beta, int flag);

@@ -34,6 +34,7 @@ def lib():
         L.salsa_ref_run.restype = C.c_int
         L.salsa_ref_layout.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 5 + [C.POINTER(C.c_double)]
         L.salsa_ref_counters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong * 5)]
+        L.salsa_ref_states.argtypes = [C.c_void_p, C.POINTER(C.c_int * 12)]
         L.salsa_ref_terminal_vel.argtypes = [C.c_double] * 5 + [C.c_int]
         L.salsa_ref_terminal_vel.restype = C.c_double
         L.salsa_ref_coagc_pair.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 6
@@ -89,6 +90,14 @@ class Oracle:
         a = (C.c_longlong * 5)()
         lib().salsa_ref_counters(self.h, C.byref(a))
         return list(a)
+
+    def states(self):
+        """Process states of set_SALSA_runtime, in the order of salsa_ref_states."""
+        a = (C.c_int * 12)()
+        lib().salsa_ref_states(self.h, C.byref(a))
+        names = ("lscoag", "lscnd", "lsauto", "lsactiv", "lsicenucl", "lsicemelt", "lssecice", "lssiprimespln",
+                 "lssipdropfrac", "lssipicecollbreak", "lsfreeRH", "lsFreeTheta")
+        return dict(zip(names, list(a)))
 
     def __del__(self):
         if getattr(self, "h", None):

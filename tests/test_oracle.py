@@ -420,3 +420,41 @@ def test_two_bin_coagulation_matches_the_closed_form():
     assert na1 < 0.9 * na and vb1 - vb > 1e-5 * vb               # the update takes a good share
     others = [k for k in range(lay.nbins) if k not in (a, b)]
     assert float(new_n[others].abs().max()) == 0
+
+
+def test_switch_delays_are_sticky_and_follow_the_reference_comparisons():
+    """set_SALSA_runtime (mo_salsa_driver.f90:453-466): a master switch takes effect once
+    time >= delay and then stays on, also for a later call at an earlier time; lsfreeRH
+    compares with time > delay.  A delayed coagulation therefore gives the step without
+    coagulation before its delay, and the step with it from then on."""
+    inp = make_inputs("grid16x16x40", "cpu", X=4, Y=4, Z=6)
+
+    def step(o, time):
+        f = {k: v.clone() for k, v in inp.fields.items()}
+        out = make_outputs(inp)
+        rc, _ = o.run(inp, f, out, time=time)
+        assert rc == 0
+        return out
+
+    def same(a, b):
+        return all(torch.equal(a[k], b[k]) for k in a)
+
+    inp.cfg.lscoag.sw = 0
+    no_coag = step(Oracle(inp.cfg), 1.0)
+    inp.cfg.lscoag.sw, inp.cfg.lscoag.delay = 1, 0.0
+    with_coag = step(Oracle(inp.cfg), 1.0)
+    assert not same(no_coag, with_coag)
+    inp.cfg.lscoag.delay = 5.0
+    o = Oracle(inp.cfg)
+    assert same(step(o, 1.0), no_coag)           # time < delay: off
+    assert same(step(o, 4.999), no_coag)
+    assert same(step(o, 5.0), with_coag)         # time == delay: on
+    assert same(step(o, 2.0), with_coag)         # sticky
+    # lsfreeRH (rhlim unconstrained once its state is on) uses a strict comparison
+    inp.cfg.lscoag.delay = 0.0
+    inp.cfg.lsfreeRH.sw, inp.cfg.lsfreeRH.delay = 1, 3.0
+    o = Oracle(inp.cfg)
+    step(o, 3.0)                                 # time == delay: still constrained
+    assert o.states()["lsfreeRH"] == 0
+    step(o, 3.5)
+    assert o.states()["lsfreeRH"] == 1 and o.states()["lscoag"] == 1

@@ -42,8 +42,8 @@ using salsa::Row;
 // memory (their own pool holds it, or cudaMalloc's device-wide synchronisation would
 // stall their time loop): the cell-order list and the status counters live in module
 // memory.  SALSA_NOALLOC_MAXCELLS (header) bounds the interior cells of one call.
-// Host code must not take these names as device addresses: it looks the addresses up
-// with cudaGetSymbolAddress on the handle's device.
+// Host code must not take these names as device addresses: salsa_gb300_init looks the
+// addresses up with cudaGetSymbolAddress on the handle's device.
 static __device__ __align__(256) int g_na_order[SALSA_NOALLOC_MAXCELLS];
 static __device__ __align__(256) unsigned long long g_na_status[salsa::ST_N];
 
@@ -580,6 +580,26 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   B.iceShapeGamma = g.iceShapeGamma; B.iceShapeSigma = g.iceShapeSigma;
   B.level = g.level;
   h->base = B;
+  // Load, on the handle's device, every module a step of this handle can launch, and
+  // resolve the module scratch of salsa_gb300_run_noalloc: under lazy module loading a
+  // module (and its static device arrays) is loaded on first use, and for callers of
+  // the no-alloc step that first use must not come after their pool has taken the
+  // free memory.
+  {
+    void *po = nullptr, *ps = nullptr;
+    cudaFuncAttributes fa;
+    const bool sip = g.lssecice.sw && g.level == 5;
+    const int bps = sip ? (g.precision == 0 ? salsa::blocks_per_sm_ds(B) : salsa::blocks_per_sm_fs(B))
+                        : (g.precision == 0 ? (g.diagnostics ? salsa::blocks_per_sm_d1(B) : salsa::blocks_per_sm_d0(B))
+                                            : (g.diagnostics ? salsa::blocks_per_sm_f1(B) : salsa::blocks_per_sm_f0(B)));
+    if (bps <= 0 || cudaFuncGetAttributes(&fa, salsa_order_kernel) != cudaSuccess ||
+        cudaGetSymbolAddress(&po, g_na_order) != cudaSuccess || cudaGetSymbolAddress(&ps, g_na_status) != cudaSuccess) {
+      salsa_gb300_finalize(h);
+      return SALSA_E_CUDA;
+    }
+    h->na_order = static_cast<int *>(po);
+    h->na_status = static_cast<unsigned long long *>(ps);
+  }
   h->lolim_diam.resize(ntotal);
   for (int b = 0; b < ntotal; b++) h->lolim_diam[b] = std::pow(t.vlo[b] / PI6, 1. / 3.);
   *out = h;
@@ -983,16 +1003,7 @@ extern "C" int salsa_gb300_run_async(salsa_handle_t *h, int nzp, int nxp, int ny
 extern "C" int salsa_gb300_run_noalloc(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
                                        double time, int istp, int level, int lcharge, int initialize,
                                        const salsa_fields_t *f, void *stream, int sync, salsa_status_t *st) {
-  if (!h) return SALSA_E_ARG;
-  if (!h->na_order || !h->na_status) {
-    // first call on this handle: resolve the module scratch of the handle's device
-    if (cudaSetDevice(h->device) != cudaSuccess) return SALSA_E_NODEV;
-    void *po = nullptr, *ps = nullptr;
-    if (cudaGetSymbolAddress(&po, g_na_order) != cudaSuccess || cudaGetSymbolAddress(&ps, g_na_status) != cudaSuccess)
-      return SALSA_E_CUDA;
-    h->na_order = static_cast<int *>(po);
-    h->na_status = static_cast<unsigned long long *>(ps);
-  }
+  if (!h || !h->na_order || !h->na_status) return SALSA_E_ARG;   // both resolved by salsa_gb300_init
   return run_impl(h, nzp, nxp, nyp, ns, tstep, time, istp, level, lcharge, initialize, f, (cudaStream_t)stream, sync,
                   st, 0, 1);
 }
