@@ -112,15 +112,16 @@ def host_buffers(sources):
     torch's pinned allocator rounds every block up to a power of two, which would take up
     to twice the host memory for the largest workload."""
     import torch
-    total = sum(math.prod(v.shape) for v in sources.values())
+    shape = {k: (v.shape if isinstance(v, torch.Tensor) else torch.Size(v)) for k, v in sources.items()}
+    total = sum(math.prod(x) for x in shape.values())
     buf = torch.zeros(total, dtype=torch.float64)
     rc = torch._C._cudart.cudaHostRegister(buf.data_ptr(), total * 8, 0)
     if int(rc) != 0:
         raise RuntimeError(f"cudaHostRegister failed ({rc})")
     out, off = {}, 0
     for k, v in sources.items():
-        n = math.prod(v.shape)
-        view = buf[off:off + n].view(v.shape)
+        n = math.prod(shape[k])
+        view = buf[off:off + n].view(shape[k])
         if isinstance(v, torch.Tensor):
             view.copy_(v)
         out[k] = view

@@ -320,6 +320,14 @@ typedef struct {
 /* nstate of the handle's layout (0 when the handle is not level 4). */
 int salsa_gb300_chain_state_size(const salsa_handle_t *h);
 
+/* Device memory in bytes that a forward + adjoint pair with checkpoint spacing
+ * ckpt_every takes beyond its input and output arrays: the checkpoints, the per-cell
+ * tape of one step, the states of one checkpoint segment (ckpt_every > 1) and the
+ * work counters (-1 for a bad argument or a handle that is not level 4).  No
+ * counterpart in the reference: it lets the caller choose the spacing that fits. */
+long long salsa_gb300_chain_adjoint_bytes(const salsa_handle_t *h, int ncell, int nsub, double dt,
+                                          int ckpt_every);
+
 /* xN = chain(x0).  ckpt (NULL or [ceil(nsub/ckpt_every)][ncell][nstate]) receives
  * the states entering steps 0, ckpt_every, 2 ckpt_every, ... in SALSA units (#/m3,
  * m3/m3), the form in which the adjoint restarts from them. */

@@ -22,6 +22,36 @@
 #endif
 #include "salsa_ref.h"
 
+/* ---- rounding perturbation of the library functions (test infrastructure) ----
+ * Two correct FP64 implementations of this path differ in how their exp, log, pow and
+ * cube roots round (glibc here, CUDA's functions on the GPU): by about one ulp.  The
+ * parity tests measure the oracle's own response to that difference: with a mode set,
+ * every result of those functions moves by one ulp, up (+1), down (-1), or in a
+ * direction taken from the bits of the argument (modes 2 and above, one pattern each).  sqrt rounds correctly on both
+ * sides and is left alone.  Mode 0 (the default) leaves every result as it is. */
+static int g_libm_pert = 0;
+void salsa_ref_set_libm_perturbation(int mode) { g_libm_pert = mode; }
+static inline double pert_ulp(double r, double x) {
+  if (!g_libm_pert || !isfinite(r) || r == 0.) return r;
+  int up = g_libm_pert > 0;
+  if (g_libm_pert >= 2) {
+    unsigned long long b;
+    memcpy(&b, &x, sizeof b);
+    b += 0x9e3779b97f4a7c15ULL * (unsigned long long)g_libm_pert;   /* one direction pattern per mode */
+    b ^= b >> 29;
+    b *= 0xbf58476d1ce4e5b9ULL;
+    b ^= b >> 32;
+    up = (int)(b & 1u);
+  }
+  return nextafter(r, up ? INFINITY : -INFINITY);
+}
+#define exp(x) pert_ulp(exp(x), (x))
+#define log(x) pert_ulp(log(x), (x))
+#define log10(x) pert_ulp(log10(x), (x))
+#define pow(x, y) pert_ulp(pow((x), (y)), (x) + (y))
+#define erf(x) pert_ulp(erf(x), (x))
+#define cos(x) pert_ulp(cos(x), (x))
+
 /* ---- constants: src/src_shared/mo_submctl.f90:253-338 (truncated as written) ---- */
 #define AVOG   6.0221e+23
 #define BOLTZ  1.3807e-23

@@ -183,3 +183,67 @@ def test_autograd_function_returns_the_adjoint():
     _, ck = ch.forward(x, th, k, s, 4, inp.dt)
     xb, kb, sb = ch.adjoint(ck, 1, th, k, s, 4, inp.dt, yb)
     assert torch.equal(gx, xb) and torch.equal(gk, kb) and torch.equal(gs, sb)
+
+
+def test_sixty_step_chain_against_central_differences():
+    """The gradient workload's chain length (60 steps of 0.5 s) on 256 cells: the
+    tangent-linear model against central differences (h = 1e-6 relative), and the
+    adjoint against the tangent-linear model (dot-product test).  Cells whose difference
+    quotients at h and 2h agree to 1e-7 are the reliable ones; the test prints their
+    share and the agreement reached on them and on all cells."""
+    inp, x, th, k, s = chain_case(256, seed=21)
+    ch = SalsaChain(inp.cfg)
+    g = torch.Generator(device="cuda").manual_seed(17)
+    ux = x * torch.randn(x.shape, generator=g, device="cuda", dtype=torch.float64)
+    uk = k * torch.randn(k.shape, generator=g, device="cuda", dtype=torch.float64)
+    us = s * torch.randn(s.shape, generator=g, device="cuda", dtype=torch.float64)
+    nsub = 60
+    xN, dxN = ch.tlm(x, th, k, s, nsub, inp.dt, ux, uk, us)
+    cs = cloud_slice(inp)
+    fd = _fd(ch, x, th, k, s, nsub, inp.dt, ux, uk, us)[:, cs]
+    fd2 = _fd(ch, x, th, k, s, nsub, inp.dt, ux, uk, us, h=2 * H)[:, cs]
+    ok = _reliable(fd, fd2)
+    err = (dxN[:, cs] - fd).norm(dim=1) / fd.norm(dim=1).clamp(min=1e-300)
+    share = float(ok.double().mean())
+    within_ok = float((err[ok] < 1e-6).double().mean())
+    within_all = float((err < 1e-6).double().mean())
+    print(f"60 steps: reliable cells {100 * share:.1f} %; TLM within 1e-6 of FD: {100 * within_ok:.1f} % of the "
+          f"reliable cells, {100 * within_all:.1f} % of all; median error on reliable cells "
+          f"{float(err[ok].median()):.2e}")
+    assert share > 0.3
+    assert float(err[ok].median()) < 1e-7
+    assert within_ok > 0.9
+    # adjoint against the tangent-linear model over the same 60 steps
+    yb = torch.zeros_like(xN)
+    yb[:, cs] = torch.randn((x.shape[0], cs.numel()), generator=g, device="cuda", dtype=torch.float64) / \
+        xN[:, cs].abs().clamp(min=1e-30)
+    _, ck = ch.forward(x, th, k, s, nsub, inp.dt, ckpt_every=1)
+    xb, kb, sb = ch.adjoint(ck, 1, th, k, s, nsub, inp.dt, yb)
+    lhs = (yb * dxN).sum(1)
+    rhs = (xb * ux).sum(1) + kb * uk + sb * us
+    rel = (lhs - rhs).abs() / torch.maximum(lhs.abs(), rhs.abs()).clamp(min=1e-300)
+    print("60 steps: dot product test median", float(rel.median()), "max", float(rel.max()))
+    assert float(rel.median()) < 1e-10
+
+
+def test_checkpoint_spacing_follows_the_memory_budget():
+    """ckpt_every=None picks the spacing from the memory budget: every step when the
+    chain fits, a wider spacing (recomputing the steps in between) when it does not;
+    the adjoint is the same either way."""
+    inp, x, th, k, s = chain_case(128)
+    ch = SalsaChain(inp.cfg)
+    nsub = 12
+    ncell = x.shape[0]
+    b1 = ch.adjoint_bytes(ncell, nsub, inp.dt, 1)
+    assert ch.auto_ckpt_every(ncell, nsub, inp.dt, budget=b1) == 1
+    tight = min(ch.adjoint_bytes(ncell, nsub, inp.dt, e) for e in range(2, nsub + 1))
+    every = ch.auto_ckpt_every(ncell, nsub, inp.dt, budget=tight)
+    assert every > 1 and ch.adjoint_bytes(ncell, nsub, inp.dt, every) <= tight < b1
+    g = torch.Generator(device="cuda").manual_seed(5)
+    yb = torch.randn(x.shape, generator=g, device="cuda", dtype=torch.float64) / x.abs().clamp(min=1e-30)
+    _, ck1 = ch.forward(x, th, k, s, nsub, inp.dt, ckpt_every=1)
+    ref = ch.adjoint(ck1, 1, th, k, s, nsub, inp.dt, yb)
+    _, cke = ch.forward(x, th, k, s, nsub, inp.dt, ckpt_every=every)
+    got = ch.adjoint(cke, None, th, k, s, nsub, inp.dt, yb)
+    for a, b in zip(ref, got):
+        assert torch.equal(a, b)

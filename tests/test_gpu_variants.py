@@ -17,7 +17,7 @@ import torch
 from uclales_salsa_gb300.inputs import make_inputs, make_outputs
 from uclales_salsa_gb300.api import SalsaStep
 from oracle_ref import Oracle
-from test_gpu_parity import check, VIOL_FRAC, FRAC_WITHIN, PERTURBED
+from test_gpu_parity import check, assert_fp64, VIOL_FRAC, FRAC_WITHIN, PERTURBED, LIBM_MODES
 from parity import FLOOR, interior
 
 pytestmark = pytest.mark.gpu
@@ -92,12 +92,12 @@ def check_activation(inp, gpu, ref, env, rtol):
     return rep
 
 
-def _oracle(inp, fields, kw, pf=None, eps=0.0):
+def _oracle(inp, fields, kw, pf=None, eps=0.0, libm=0, variant="plain"):
     f = {k: v.clone() for k, v in fields.items()}
     if pf:
         f[pf] = f[pf] * (1 + eps)
     out = make_outputs(inp)
-    rc, st = Oracle(inp.cfg).run(inp, f, out, time=1.0, **kw)
+    rc, st = Oracle(inp.cfg, variant=variant).run(inp, f, out, time=1.0, libm=libm, **kw)
     assert rc == 0, st.as_dict()
     return out
 
@@ -110,11 +110,12 @@ def test_variant_parity(name, wl, kw, mod, call):
     inp.fields = fields
     ref = _oracle(inp, fields, call)
     env = {k: torch.zeros_like(v) for k, v in ref.items()}
-    for pf in PERTURBED:
-        for sgn in (1.0, -1.0):
-            o = _oracle(inp, fields, call, pf, sgn * 2.2e-16)
-            for k in env:
-                env[k] = torch.maximum(env[k], (o[k] - ref[k]).abs())
+    runs = [dict(pf=pf, eps=sgn * 2.2e-16) for pf in PERTURBED if pf in fields for sgn in (1.0, -1.0)]
+    runs += [dict(libm=m) for m in LIBM_MODES] + [dict(variant="contract")]
+    for r in runs:
+        o = _oracle(inp, fields, call, **r)
+        for k in env:
+            env[k] = torch.maximum(env[k], (o[k] - ref[k]).abs())
     f = {k: v.clone().cuda() for k, v in fields.items()}
     out = {k: v.cuda() for k, v in make_outputs(inp).items()}
     step = SalsaStep(inp.cfg)
@@ -126,9 +127,7 @@ def test_variant_parity(name, wl, kw, mod, call):
     rep = check(inp, gpu, ref, env, 1e-10)
     rep.update(check_activation(inp, gpu, ref, env, 1e-10))
     print(name, rep)
-    for k, r in rep.items():
-        assert r["violations"] <= VIOL_FRAC * r["n"], (name, k, r)
-        assert r["frac_within"] >= FRAC_WITHIN, (name, k, r)
+    assert_fp64(rep)
 
 
 @pytest.mark.parametrize("host", [False, True])

@@ -65,6 +65,7 @@ def library():
 EXPORTED = ["salsa_gb300_default_config", "salsa_gb300_init", "salsa_gb300_run", "salsa_gb300_run_async",
             "salsa_gb300_layout", "salsa_gb300_last_launches", "salsa_gb300_last_kernel_ms",
             "salsa_gb300_finalize", "salsa_gb300_version", "salsa_gb300_run_noalloc", "salsa_gb300_chain_state_size",
+            "salsa_gb300_chain_adjoint_bytes",
             "salsa_gb300_chain_forward", "salsa_gb300_chain_tlm", "salsa_gb300_chain_adjoint",
             "salsa_gb300_tend_constrain", "salsa_gb300_diagnostics", "salsa_gb300_sedimentation"]
 

@@ -52,6 +52,8 @@ def _lib():
     if not hasattr(L, "_chain_ready"):
         L.salsa_gb300_chain_state_size.argtypes = [C.c_void_p]
         L.salsa_gb300_chain_state_size.restype = C.c_int
+        L.salsa_gb300_chain_adjoint_bytes.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.salsa_gb300_chain_adjoint_bytes.restype = C.c_longlong
         L.salsa_gb300_chain_forward.argtypes = [C.c_void_p, C.POINTER(ChainDesc), _PD, _PD, _PD, C.c_int, C.c_void_p]
         L.salsa_gb300_chain_tlm.argtypes = [C.c_void_p, C.POINTER(ChainDesc), _PD, _PD, _PD, _PD, _PD, _PD,
                                             C.c_void_p]
@@ -85,9 +87,33 @@ class SalsaChain:
         if rc != SALSA_OK:
             raise api.SalsaError(rc, f"{what}: {ERROR_NAMES.get(rc, rc)}")
 
+    def adjoint_bytes(self, ncell, nsub, dt, ckpt_every):
+        """Device memory of a forward + adjoint pair beyond its arrays (C-ABI query)."""
+        b = self.L.salsa_gb300_chain_adjoint_bytes(self.step.h, int(ncell), int(nsub), float(dt), int(ckpt_every))
+        if b < 0:
+            raise api.SalsaError(1, "salsa_gb300_chain_adjoint_bytes")
+        return b
+
+    def auto_ckpt_every(self, ncell, nsub, dt, budget=None, fraction=0.5):
+        """Checkpoint spacing for a forward + adjoint pair: every step while that fits,
+        otherwise the smallest spacing whose memory fits (each step past a checkpoint is
+        recomputed once in the adjoint).  The budget defaults to `fraction` of the free
+        device memory."""
+        if budget is None:
+            budget = fraction * torch.cuda.mem_get_info()[0]
+        for k in range(1, nsub + 1):
+            if self.adjoint_bytes(ncell, nsub, dt, k) <= budget:
+                return k
+        raise api.SalsaError(3, f"the chain's adjoint needs more than {budget / 2**30:.1f} GiB at any spacing")
+
     def forward(self, x0, thermo, kappa, ssat, nsub, dt, ckpt_every=1, keep_checkpoints=True):
-        """Returns (xN, checkpoints or None)."""
+        """Returns (xN, checkpoints or None).  ckpt_every=None chooses the spacing from
+        the free device memory (auto_ckpt_every); the checkpoints tensor then has
+        ceil(nsub / spacing) rows, and the spacing is `self.last_ckpt_every`."""
         ncell = kappa.numel()
+        if ckpt_every is None:
+            ckpt_every = self.auto_ckpt_every(ncell, nsub, dt)
+        self.last_ckpt_every = ckpt_every
         xN = torch.empty_like(x0)
         ck = None
         if keep_checkpoints:
@@ -110,6 +136,8 @@ class SalsaChain:
         return xN, dxN
 
     def adjoint(self, ck, ckpt_every, thermo, kappa, ssat, nsub, dt, xbarN):
+        if ckpt_every is None:
+            ckpt_every = self.last_ckpt_every     # the spacing of the last forward's checkpoints
         xbar0 = torch.empty_like(xbarN)
         kbar = torch.empty_like(kappa)
         sbar = torch.empty_like(ssat)
@@ -128,7 +156,7 @@ class _ChainFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x0, kappa, ssat, chain, thermo, nsub, dt, ckpt_every):
         xN, ck = chain.forward(x0, thermo, kappa, ssat, nsub, dt, ckpt_every)
-        ctx.chain, ctx.thermo, ctx.nsub, ctx.dt, ctx.every = chain, thermo, nsub, dt, ckpt_every
+        ctx.chain, ctx.thermo, ctx.nsub, ctx.dt, ctx.every = chain, thermo, nsub, dt, chain.last_ckpt_every
         ctx.save_for_backward(ck, kappa, ssat)
         return xN
 
@@ -139,8 +167,11 @@ class _ChainFn(torch.autograd.Function):
         return x0b, kb, sb, None, None, None, None, None
 
 
-def chain_apply(chain, x0, kappa, ssat, thermo, nsub, dt, ckpt_every=1):
-    """xN = chain(x0; kappa, ssat) as a differentiable torch operation."""
+def chain_apply(chain, x0, kappa, ssat, thermo, nsub, dt, ckpt_every=None):
+    """xN = chain(x0; kappa, ssat) as a differentiable torch operation.  By default the
+    checkpoint spacing follows the free device memory (SalsaChain.auto_ckpt_every):
+    every step while the chain fits, recomputation between checkpoints once it
+    outgrows the memory."""
     return _ChainFn.apply(x0, kappa, ssat, chain, thermo, nsub, dt, ckpt_every)
 
 

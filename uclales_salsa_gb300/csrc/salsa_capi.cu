@@ -264,6 +264,8 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
     B.rhoice[j] = (k == 7) ? 917. : ALLRHO[k];
     B.MM[j] = ALLMM[k];
     B.diss[j] = ALLDISS[k];
+    B.irholiq[j] = 1. / B.rholiq[j];
+    B.irhoice[j] = 1. / B.rhoice[j];
   }
   for (int j = 0; j < B.nused; j++)
     for (int k = 0; k < 9; k++) if (used[k] && allInd[k] == j) {
@@ -710,6 +712,10 @@ int run_impl(salsa_handle_t *h, int nzp, int nxp, int nyp, int ns, double tstep,
   P.ngroups = (P.ncells + SALSA_CPG - 1) / SALSA_CPG;
   P.level = level; P.lcharge = lcharge; P.initialize = initialize;
   P.dt = tstep;
+  {
+    int ex = 0;
+    P.inv_dt = std::frexp(tstep, &ex) == 0.5 ? 1. / tstep : 0.;   // exact reciprocal of a power of two
+  }
   P.st_coag = h->st[0]; P.st_cnd = h->st[1]; P.st_auto = h->st[2]; P.st_activ = h->st[3];
   P.st_icenucl = h->st[4]; P.st_icemelt = h->st[5];
   P.st_freeRH = h->st_freeRH; P.st_freeTheta = h->st_freeTheta;

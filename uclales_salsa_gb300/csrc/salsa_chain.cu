@@ -181,7 +181,7 @@ __device__ __forceinline__ R liquid_dwet(const DevParams &P, const CW<R> &w, con
   if (val(w.n[b]) > nlim_of(ph)) {
     R vs = R(0.);
     for (int s = 0; s < P.nwet; s++) vs += w.V(s, b);
-    dw = g_cbrt(vs / w.n[b] / K_PI6);
+    dw = g_cbrt(vs * (R(1.) / (w.n[b] * K_PI6)));   // as the step kernel's updateDiameterAll
   } else {
     dw = R(dmid[b]);
   }
@@ -799,8 +799,8 @@ __device__ void chain_load(const DevParams &P, const CW<R> &w, const double *x, 
       if (dx) set_tangent(w.n[e], dx[e] * dn);
     } else {
       const int s = (e - NL) / NL, b = (e - NL) - s * NL;
-      w.V(s, b) = R(x[e] * dn / P.rholiq[s]);
-      if (dx) set_tangent(w.V(s, b), dx[e] * dn / P.rholiq[s]);
+      w.V(s, b) = R(x[e] * dn * P.irholiq[s]);   // as the step kernel's unpacking
+      if (dx) set_tangent(w.V(s, b), dx[e] * dn * P.irholiq[s]);
     }
   }
   __syncwarp();
@@ -1521,6 +1521,21 @@ int salsa_gb300_chain_state_size(const salsa_handle_t *h) {
   int dev, nsm;
   if (!salsa::handle_params(h, &P, &s, &dev, &nsm)) return 0;
   return salsa::handle_config(h)->level == 4 ? P.nliquid * (1 + P.nwet) : 0;
+}
+
+long long salsa_gb300_chain_adjoint_bytes(const salsa_handle_t *h, int ncell, int nsub, double dt,
+                                          int ckpt_every) {
+  DevParams P;
+  cudaStream_t s;
+  int dev, nsm;
+  if (!salsa::handle_params(h, &P, &s, &dev, &nsm) || salsa::handle_config(h)->level != 4) return -1;
+  if (ncell <= 0 || nsub <= 0 || ckpt_every <= 0 || !(dt > 0.)) return -1;
+  const long long ns = (long long)P.nliquid * (1 + P.nwet);
+  const salsa::TapeLayout tl = salsa::tape_layout(P.nliquid, P.nwet, P.fn1a - P.in1a + 1, salsa::tape_maxit(dt));
+  const long long nseg = (nsub + ckpt_every - 1) / ckpt_every;
+  long long d = nseg * ncell * ns + (long long)ncell * tl.total;   // checkpoints, tape
+  if (ckpt_every > 1) d += (long long)ckpt_every * ncell * ns;      // states of one segment
+  return d * (long long)sizeof(double) + (nseg + 2LL * nsub) * (long long)sizeof(unsigned) + 64;
 }
 
 int salsa_gb300_chain_forward(salsa_handle_t *h, const salsa_chain_t *c, const double *x0, double *xN, double *ckpt,

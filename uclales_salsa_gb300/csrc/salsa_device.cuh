@@ -91,6 +91,7 @@ struct DevParams {
   long long ncells, plane, ngroups;
   int level, lcharge, initialize;
   double dt;
+  double inv_dt;   // 1/dt when dt is a power of two (the product then equals the quotient), else 0
   // layout
   int nbins, ncld, nprc, nice, ntotal, nliquid, nused, ndry, nwet, iwa, irim, nb_pad;
   int in1a, fn1a, in2a, fn2a, in2b, fn2b;
@@ -98,6 +99,7 @@ struct DevParams {
   int nsoluble, ninsoluble, ind_soluble[5], ind_insoluble[2];
   int ix_so4, ix_oc, ix_bc, ix_du, ix_ss, ix_no, ix_nh;
   double rholiq[9], rhoice[9], MM[9], diss[9];
+  double irholiq[9], irhoice[9];   // reciprocal densities (the unit conversions multiply)
   int cnt80, cnt50;
   // effective switches for this call
   int st_coag, st_cnd, st_auto, st_activ, st_icenucl, st_icemelt, st_freeRH, st_freeTheta;

@@ -24,6 +24,7 @@
 #pragma once
 #include "salsa_device.cuh"
 #include <cstdio>
+#include <type_traits>
 
 namespace salsa {
 namespace {   // internal linkage: every instantiation unit carries its own copy
@@ -37,8 +38,20 @@ struct WS {
   KT *K;
   int *pbuf;
   int NB;
+  // float copies of numc and volc that the mixed form's coagulation update sums from
+  // (in the scratch rows, valid from shadow_all to the end of the update)
+  float *nf, *vf;
   __device__ __forceinline__ double &v(int s, int b) const { return volc[s * NB + b]; }
   __device__ __forceinline__ double *sc(int k) const { return scr + k * NB; }
+  // partner values in the kernel type: the state itself (FP64 form) or its float copy
+  __device__ __forceinline__ KT nk(int b) const {
+    if constexpr (sizeof(KT) == 4) return nf[b];
+    else return numc[b];
+  }
+  __device__ __forceinline__ KT vk(int s, int b) const {
+    if constexpr (sizeof(KT) == 4) return vf[s * NB + b];
+    else return volc[s * NB + b];
+  }
 };
 
 // misc slots (doubles)
@@ -85,9 +98,11 @@ __device__ void updateDiameterAll(const DevParams &P, const WS<double> *, double
     for (int s = 0; s < P.nused; s++) vs += volc[s * NB + b];
     for (int s = 0; s < P.ndry; s++) vd += volc[s * NB + b];
     for (int k = 0; k < P.ninsoluble; k++) vi += volc[P.ind_insoluble[k] * NB + b];
-    dw = cbrt(vs / n / K_PI6);
-    dd = cbrt(vd / n / K_PI6);
-    di = cbrt(vi / n / K_PI6);
+    // (v / numc / pi6)^(1/3) with one division for the three diameters
+    const double q = 1. / (n * K_PI6);
+    dw = cbrt(vs * q);
+    dd = cbrt(vd * q);
+    di = cbrt(vi * q);
   } else {
     dw = dd = di = dmid[b];
   }
@@ -326,14 +341,19 @@ __device__ __forceinline__ void load_props(const KT *S, int NB, int b, BinProps<
   o.schm = S[8 * NB + b];
 }
 
-// Per-bin properties are evaluated in FP64 in both forms and stored in the kernel type:
-// the float forms of exp/pow in the terminal velocities (Beard; Khvorostyanov-Curry for
-// ice) amplify the rounding of their exponents by |log(base)| to ~1e-5.
+// Per-bin properties are evaluated in the kernel type: FP64 in the FP64 form, float in
+// the mixed form (its pair kernels are float too) except for ice bins.
 template <typename KT>
 __device__ __forceinline__ void store_props(KT *S, int NB, int b, const BinProps<double> &o) {
   S[0 * NB + b] = (KT)o.diam; S[1 * NB + b] = (KT)o.mass; S[2 * NB + b] = (KT)o.beta; S[3 * NB + b] = (KT)o.dfpart;
   S[4 * NB + b] = (KT)o.mtvel; S[5 * NB + b] = (KT)o.omega; S[6 * NB + b] = (KT)o.termv; S[7 * NB + b] = (KT)o.reyn;
   S[8 * NB + b] = (KT)o.schm;
+}
+template <typename KT>
+__device__ __forceinline__ void store_props_kt(KT *S, int NB, int b, const BinProps<KT> &o) {
+  S[0 * NB + b] = o.diam; S[1 * NB + b] = o.mass; S[2 * NB + b] = o.beta; S[3 * NB + b] = o.dfpart;
+  S[4 * NB + b] = o.mtvel; S[5 * NB + b] = o.omega; S[6 * NB + b] = o.termv; S[7 * NB + b] = o.reyn;
+  S[8 * NB + b] = o.schm;
 }
 template <typename KT>
 __device__ __forceinline__ void to_kt(const BinProps<double> &d, BinProps<KT> &o) {
@@ -361,10 +381,22 @@ __device__ void eval_pairs(const DevParams &P, const WS<KT> &w, const CoagCell<K
       const double *SH = shape_rows(w);
       Shape<double> sh;
       sh.alpha = SH[0 * NB + i]; sh.beta = SH[1 * NB + i]; sh.gamma = SH[2 * NB + i]; sh.sigma = SH[3 * NB + i];
-      const double dj = w.dwet[j], mj = w.rhomean[j] * K_PI6 * cube(w.dwet[j]);
-      BinProps<double> ad;
-      bin_props<double>(cd, phase_of(P, i), 1.1 * dj, w.dwet[i], 1.33 * mj, w.rhomean[i], sh, ad);
-      to_kt<KT>(ad, a);
+      bool done = false;
+      if constexpr (sizeof(KT) == 4) {
+        if (phase_of(P, i) < 4) {
+          const float dj = (float)w.dwet[j], mj = (float)w.rhomean[j] * (float)K_PI6 * cube(dj);
+          Shape<float> shf;
+          shf.alpha = (float)sh.alpha; shf.beta = (float)sh.beta; shf.gamma = (float)sh.gamma; shf.sigma = (float)sh.sigma;
+          bin_props<float>(cc, phase_of(P, i), 1.1f * dj, (float)w.dwet[i], 1.33f * mj, (float)w.rhomean[i], shf, a);
+          done = true;
+        }
+      }
+      if (!done) {
+        const double dj = w.dwet[j], mj = w.rhomean[j] * K_PI6 * cube(w.dwet[j]);
+        BinProps<double> ad;
+        bin_props<double>(cd, phase_of(P, i), 1.1 * dj, w.dwet[i], 1.33 * mj, w.rhomean[i], sh, ad);
+        to_kt<KT>(ad, a);
+      }
     } else {
       load_props<KT>(S, NB, i, a);
     }
@@ -427,10 +459,28 @@ __device__ void build_kernels(const DevParams &P, const WS<KT> &w, const double 
       sh.alpha = sh.beta = sh.gamma = sh.sigma = 0.;
     }
     double diam = w.dwet[b];   // dnsp == dwet after a limited "all" update
-    double mass = w.rhomean[b] * K_PI6 * cube(w.dwet[b]);
-    BinProps<double> o;
-    bin_props<double>(cd, ph, diam, w.dwet[b], mass, w.rhomean[b], sh, o);
-    store_props<KT>(S, NB, b, o);
+    bool done = false;
+    if constexpr (sizeof(KT) == 4) {
+      if (ph < 4) {
+        // the mixed form evaluates the per-bin properties of the liquid bins in float as
+        // well; ice keeps FP64 (the Khvorostyanov-Curry fall speed carries float rounding
+        // of its exponents into ice-drop speed differences, which cancel)
+        const float df = (float)diam;
+        const float mass = (float)w.rhomean[b] * (float)K_PI6 * cube(df);
+        Shape<float> shf;
+        shf.alpha = (float)sh.alpha; shf.beta = (float)sh.beta; shf.gamma = (float)sh.gamma; shf.sigma = (float)sh.sigma;
+        BinProps<float> o;
+        bin_props<float>(cc, ph, df, df, mass, (float)w.rhomean[b], shf, o);
+        store_props_kt<KT>(S, NB, b, o);
+        done = true;
+      }
+    }
+    if (!done) {
+      double mass = w.rhomean[b] * K_PI6 * cube(w.dwet[b]);
+      BinProps<double> o;
+      bin_props<double>(cd, ph, diam, w.dwet[b], mass, w.rhomean[b], sh, o);
+      store_props<KT>(S, NB, b, o);
+    }
     SH[0 * NB + b] = sh.alpha; SH[1 * NB + b] = sh.beta; SH[2 * NB + b] = sh.gamma; SH[3 * NB + b] = sh.sigma;
   }
   __syncwarp();
@@ -503,40 +553,155 @@ __device__ __forceinline__ void warp_sum8(double (&v)[8], int lane) {
   for (int i = 0; i < 8; i++) v[i] = __shfl_sync(F, c, ((i >> 2) << 4) | (((i >> 1) & 1) << 3) | ((i & 1) << 2));
 }
 
-struct TAcc {
-  double sink, self;
-  double src[SALSA_NSV];
-  double dg[7];   // 0 autoc(abs) 1 autoc80 2 autoc50 3 accr 4 accr80 5 accr50 6 coll mass
+// Compensated (Kahan) float accumulator of the mixed form's partner sums: the running
+// sum and the correction of its rounding.  After the warp reduction it holds the total.
+struct KahanF {
+  float s, c;
+  __device__ __forceinline__ KahanF &operator=(float x) { s = x; c = 0.f; return *this; }
+  __device__ __forceinline__ KahanF &operator+=(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+    return *this;
+  }
+  __device__ __forceinline__ operator double() const { return (double)s; }
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// warp_sum8 for compensated float sums: every exchange adds the high parts exactly
+// (two_sum) and carries the low parts, so the totals keep float accuracy whatever the
+// cancellation between lanes; every lane receives the eight totals (high + low).
+__device__ __forceinline__ void warp_sum8_comp(float (&hi)[8], float (&lo)[8], int lane) {
+  const unsigned F = 0xffffffffu;
+  const bool h = lane & 16, g = lane & 8, f = lane & 4;
+  float ah[4], al[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float sh = h ? hi[i] : hi[i + 4], kh = h ? hi[i + 4] : hi[i];
+    const float sl = h ? lo[i] : lo[i + 4], kl = h ? lo[i + 4] : lo[i];
+    const float rh = __shfl_xor_sync(F, sh, 16), rl = __shfl_xor_sync(F, sl, 16);
+    float e;
+    two_sum(kh, rh, ah[i], e);
+    al[i] = kl + rl + e;
+  }
+  float bh[2], bl[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const float sh = g ? ah[i] : ah[i + 2], kh = g ? ah[i + 2] : ah[i];
+    const float sl = g ? al[i] : al[i + 2], kl = g ? al[i + 2] : al[i];
+    const float rh = __shfl_xor_sync(F, sh, 8), rl = __shfl_xor_sync(F, sl, 8);
+    float e;
+    two_sum(kh, rh, bh[i], e);
+    bl[i] = kl + rl + e;
+  }
+  float ch, cl;
+  {
+    const float sh = f ? bh[0] : bh[1], kh = f ? bh[1] : bh[0];
+    const float sl = f ? bl[0] : bl[1], kl = f ? bl[1] : bl[0];
+    const float rh = __shfl_xor_sync(F, sh, 4), rl = __shfl_xor_sync(F, sl, 4);
+    float e;
+    two_sum(kh, rh, ch, e);
+    cl = kl + rl + e;
+  }
+#pragma unroll
+  for (int o = 2; o > 0; o >>= 1) {
+    const float rh = __shfl_xor_sync(F, ch, o), rl = __shfl_xor_sync(F, cl, o);
+    float sh, e;
+    two_sum(ch, rh, sh, e);
+    ch = sh;
+    cl = cl + rl + e;
+  }
+  const float c = ch + cl;
+#pragma unroll
+  for (int i = 0; i < 8; i++) hi[i] = __shfl_sync(F, c, ((i >> 2) << 4) | (((i >> 1) & 1) << 3) | ((i & 1) << 2));
+}
+
+// Partner sums of one target bin: FP64 in the FP64 form; compensated float sums in the
+// mixed form, from float kernels and float copies of the partner state.
+template <typename KT>
+struct TAccT {
+  using A = typename std::conditional<sizeof(KT) == 4, KahanF, double>::type;
+  A sink, self;
+  A src[SALSA_NSV];
+  A dg[7];   // 0 autoc(abs) 1 autoc80 2 autoc50 3 accr 4 accr80 5 accr50 6 coll mass
   __device__ __forceinline__ void zero() {
-    sink = self = 0.;
+    sink = (KT)0; self = (KT)0;
 #pragma unroll
-    for (int s = 0; s < SALSA_NSV; s++) src[s] = 0.;
+    for (int s = 0; s < SALSA_NSV; s++) src[s] = (KT)0;
 #pragma unroll
-    for (int d = 0; d < 7; d++) dg[d] = 0.;
+    for (int d = 0; d < 7; d++) dg[d] = (KT)0;
   }
   __device__ __forceinline__ void reduce(bool diag, int lane) {
-    double v[8];
+    if constexpr (sizeof(KT) == 4) {
+      float h[8], l[8];
 #pragma unroll
-    for (int s = 0; s < 7; s++) v[s] = src[s];
-    v[7] = sink;
-    warp_sum8(v, lane);
+      for (int s = 0; s < 7; s++) { h[s] = src[s].s; l[s] = -src[s].c; }
+      h[7] = sink.s; l[7] = -sink.c;
+      warp_sum8_comp(h, l, lane);
 #pragma unroll
-    for (int s = 0; s < 7; s++) src[s] = v[s];
-    sink = v[7];
-    if (diag) {
-      double u[8];
-      u[0] = self;
+      for (int s = 0; s < 7; s++) src[s] = h[s];
+      sink = h[7];
+      if (diag) {
+        h[0] = self.s; l[0] = -self.c;
 #pragma unroll
-      for (int d = 0; d < 7; d++) u[d + 1] = dg[d];
-      warp_sum8(u, lane);
-      self = u[0];
+        for (int d = 0; d < 7; d++) { h[d + 1] = dg[d].s; l[d + 1] = -dg[d].c; }
+        warp_sum8_comp(h, l, lane);
+        self = h[0];
 #pragma unroll
-      for (int d = 0; d < 7; d++) dg[d] = u[d + 1];
+        for (int d = 0; d < 7; d++) dg[d] = h[d + 1];
+      } else {
+        self = __shfl_sync(0xffffffffu, self.s - self.c, 0);   // self terms are accumulated on lane 0 only
+      }
     } else {
-      self = __shfl_sync(0xffffffffu, self, 0);   // self terms are accumulated on lane 0 only
+      double v[8];
+#pragma unroll
+      for (int s = 0; s < 7; s++) v[s] = src[s];
+      v[7] = sink;
+      warp_sum8(v, lane);
+#pragma unroll
+      for (int s = 0; s < 7; s++) src[s] = v[s];
+      sink = v[7];
+      if (diag) {
+        double u[8];
+        u[0] = self;
+#pragma unroll
+        for (int d = 0; d < 7; d++) u[d + 1] = dg[d];
+        warp_sum8(u, lane);
+        self = u[0];
+#pragma unroll
+        for (int d = 0; d < 7; d++) dg[d] = u[d + 1];
+      } else {
+        self = __shfl_sync(0xffffffffu, self, 0);   // self terms are accumulated on lane 0 only
+      }
     }
   }
 };
+
+// float copies of the partner state for the mixed form's coagulation update: every bin
+// before the sweep, then each bin again whenever the sweep changes it
+template <typename KT>
+__device__ __forceinline__ void shadow_all(const DevParams &P, const WS<KT> &w, int lane) {
+  if constexpr (sizeof(KT) == 4) {
+    const int NB = w.NB, n = P.ntotal;
+    for (int b = lane; b < n; b += 32) w.nf[b] = (float)w.numc[b];
+    for (int e = lane; e < P.nused * NB; e += 32) w.vf[e] = (float)w.volc[e];
+    __syncwarp();
+  }
+}
+template <typename KT>
+__device__ __forceinline__ void shadow_bin(const DevParams &P, const WS<KT> &w, int b, int lane) {
+  if constexpr (sizeof(KT) == 4) {
+    if (lane < P.nused) w.vf[lane * w.NB + b] = (float)w.v(lane, b);
+    else if (lane == P.nused) w.nf[b] = (float)w.numc[b];
+    __syncwarp();
+  }
+}
 
 // ----------------------------------------------------------------------------------------
 // Secondary ice (mo_salsa_secondary_ice.f90:6-40).  Only the SIP instantiations of the
@@ -940,14 +1105,14 @@ __device__ void secondary_ice(const DevParams &P, const WS<KT> &w, const double 
 }
 
 template <typename KT>
-__device__ __forceinline__ void source_range(const WS<KT> &w, int t, int g0, int istr, int iend, int nspec, TAcc &a,
-                                             int lane) {
+__device__ __forceinline__ void source_range(const WS<KT> &w, int t, int g0, int istr, int iend, int nspec,
+                                             TAccT<KT> &a, int lane) {
   for (int ll = istr + lane; ll <= iend; ll += 32) {
     int g = g0 + ll;
-    double k = (double)kget(w, g, t);
+    const KT k = kget(w, g, t);
 #pragma unroll
     for (int s = 0; s < SALSA_NSV; s++)
-      if (s < nspec) a.src[s] += k * w.v(s, g);
+      if (s < nspec) a.src[s] += k * w.vk(s, g);
   }
 }
 
@@ -959,43 +1124,47 @@ __device__ __forceinline__ const int16_t *partner_lists(const DevParams &P, cons
 }
 
 template <typename KT>
-__device__ __forceinline__ void list_sinks(const WS<KT> &w, const int16_t *L, int t, TAcc &a, int lane) {
+__device__ __forceinline__ void list_sinks(const WS<KT> &w, const int16_t *L, int t, TAccT<KT> &a, int lane) {
   const int off = L[4 * t], n = L[4 * t + 1];
   for (int e = lane; e < n; e += 32) {
     const int g = L[off + e];
-    a.sink += (double)kget(w, t, g) * w.numc[g];
+    a.sink += kget(w, t, g) * w.nk(g);
   }
 }
 
 template <typename KT>
-__device__ __forceinline__ void list_sources(const WS<KT> &w, const int16_t *L, int t, int nspec, TAcc &a, int lane) {
+__device__ __forceinline__ void list_sources(const WS<KT> &w, const int16_t *L, int t, int nspec, TAccT<KT> &a,
+                                             int lane) {
   const int off = L[4 * t + 2], n = L[4 * t + 3];
   for (int e = lane; e < n; e += 32) {
     const int g = L[off + e];
-    const double k = (double)kget(w, g, t);
+    const KT k = kget(w, g, t);
 #pragma unroll
     for (int s = 0; s < SALSA_NSV; s++)
-      if (s < nspec) a.src[s] += k * w.v(s, g);
+      if (s < nspec) a.src[s] += k * w.vk(s, g);
   }
 }
 
 // applyCoag (:539-559): lanes 0..nspec-1 update the volumes and lane nspec the number,
 // all in one division.
 template <typename KT>
-__device__ __forceinline__ void apply_coag(const WS<KT> &w, int t, int nspec, double dt, const TAcc &a, int lane) {
+__device__ __forceinline__ void apply_coag(const DevParams &P, const WS<KT> &w, int t, int nspec, double dt,
+                                           const TAccT<KT> &a, int lane) {
   double my = 0.;
 #pragma unroll
   for (int s = 0; s < SALSA_NSV; s++)
     if (lane == s) my = a.src[s];
   const double n = w.numc[t];
+  const double sink = a.sink, self = a.self;
   const bool vol = lane < nspec;
   const double num = vol ? w.v(lane, t) + dt * my * n : n;
-  const double den = vol ? 1. + dt * a.sink : 1. + dt * (a.sink + a.self);
+  const double den = vol ? 1. + dt * sink : 1. + dt * (sink + self);
   const double q = num / den;
   __syncwarp();
   if (vol) w.v(lane, t) = q;
   else if (lane == nspec) w.numc[t] = q;
   __syncwarp();
+  shadow_bin<KT>(P, w, t, lane);
 }
 
 template <typename KT>
@@ -1004,13 +1173,13 @@ __device__ void coag_aero(const DevParams &P, const WS<KT> &w, const double *tb,
   const int16_t *L = partner_lists(P, tb);
   for (int kk = P.in1a; kk <= P.fn2b; kk++) {
     if (w.numc[kk] < K_NLIM) continue;
-    TAcc a;
+    TAccT<KT> a;
     a.zero();
-    if (P.lscgaa && lane == 0) a.self = 0.5 * (double)kget(w, kk, kk) * w.numc[kk];
+    if (P.lscgaa && lane == 0) a.self = (KT)0.5 * kget(w, kk, kk) * w.nk(kk);
     list_sinks(w, L, kk, a, lane);
     list_sources(w, L, kk, nspec, a, lane);
     a.reduce(false, lane);
-    apply_coag(w, kk, nspec, dt, a, lane);
+    apply_coag(P, w, kk, nspec, dt, a, lane);
   }
 }
 
@@ -1019,7 +1188,7 @@ __device__ void coag_aero(const DevParams &P, const WS<KT> &w, const double *tb,
 // summed per precipitation bin in partner order, which keeps the result deterministic.
 template <typename KT>
 __device__ void precip_formation(const DevParams &P, const WS<KT> &w, const double *tb, int t, int istr, int iend,
-                                 double fix, bool selfcoll, TAcc &a, bool diag, int lane) {
+                                 double fix, bool selfcoll, TAccT<KT> &a, bool diag, int lane) {
   const int C0 = P.nbins, nspec = P.nwet, nprc = P.nprc, iwa = P.iwa;
   const double *pbins = tb + TAB_PRECPBINS * P.nb_pad;
   double *pf = w.misc + M_PF;                // [0..6] volsink, then vol_prc[nprc][7], num_prc[nprc], INFnum[nprc]
@@ -1045,24 +1214,24 @@ __device__ void precip_formation(const DevParams &P, const WS<KT> &w, const doub
           for (int s = 0; s < nspec; s++) sl[1 + s] = w.v(s, lg) * nt * klt * fix;
           dnum = (0.5 * klt * nl * nt) * fix;
           sl[9] = w.indef[lg] * dnum;
-          a.self += 0.5 * klt * nt;
+          a.self += (KT)(0.5 * klt * nt);
         } else {
           for (int s = 0; s < nspec; s++) sl[1 + s] = (w.v(s, lg) * nt + w.v(s, tg) * nl) * klt * fix;
           dnum = (klt * nl * nt) * fix;
           sl[9] = 0.5 * (w.indef[lg] + w.indef[tg]) * dnum;
-          a.sink += (double)kget(w, tg, lg) * nl;
+          a.sink += (KT)((double)kget(w, tg, lg) * nl);
         }
         dvw = sl[1 + iwa];
         if (diag) {
-          a.dg[0] += dvw;
-          if (D_new > 50.e-6) a.dg[2] += dvw;
-          if (D_new > 80.e-6) a.dg[1] += dvw;
+          a.dg[0] += (KT)dvw;
+          if (D_new > 50.e-6) a.dg[2] += (KT)dvw;
+          if (D_new > 80.e-6) a.dg[1] += (KT)dvw;
         }
       } else {
         sl[0] = -1.;
-        if (selfcoll) a.self += 0.5 * (double)kget(w, tg, lg) * nl;
+        if (selfcoll) a.self += (KT)(0.5 * (double)kget(w, tg, lg) * nl);
         else
-          for (int s = 0; s < nspec; s++) a.src[s] += klt * w.v(s, lg);
+          for (int s = 0; s < nspec; s++) a.src[s] += (KT)(klt * w.v(s, lg));
       }
       sl[8] = dnum;
     }
@@ -1105,7 +1274,7 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
     for (int kk = kfirst; kk <= klast; kk++) {
       int tg = C0 + kk;
       if (w.numc[tg] < K_NLIM) continue;
-      TAcc a;
+      TAccT<KT> a;
       a.zero();
       if (autoc1) {
         for (int e = lane; e < 7 + nprc * 9; e += 32) pf[e] = 0.;
@@ -1124,21 +1293,21 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
           double fix = fmax(1. - dt * (0.5 * (double)kget(w, tg, tg) * (n * n) / n), 0.1);
           precip_formation(P, w, tb, kk, kk, kk, fix, true, a, diag, lane);
         } else if (lane == 0) {
-          a.self += 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
+          a.self += (KT)0.5 * kget(w, tg, tg) * w.nk(tg);
         }
       }
       if (P.lscgca) {
         int iaa = P.ica_par + rel, iab = P.icb_par + rel;
-        double cm = 0.;
+        KT cm = 0;
         for (int ll = P.in1a + lane; ll <= iaa; ll += 32) {
-          double k = (double)kget(w, ll, tg);
-          for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, ll);
-          if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.v(s, ll) * P.rholiq[s];
+          const KT k = kget(w, ll, tg);
+          for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, ll);
+          if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.vk(s, ll) * (KT)P.rholiq[s];
         }
         for (int ll = P.in2b + lane; ll <= iab; ll += 32) {
-          double k = (double)kget(w, ll, tg);
-          for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, ll);
-          if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.v(s, ll) * P.rholiq[s];
+          const KT k = kget(w, ll, tg);
+          for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, ll);
+          if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.vk(s, ll) * (KT)P.rholiq[s];
         }
         a.dg[6] += cm;
       }
@@ -1167,7 +1336,7 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
         w.misc[M_DIAG + DG_AUTOC80] += a.dg[1];
         w.misc[M_DIAG + DG_AUTOC50] += a.dg[2];
       }
-      apply_coag(w, tg, nspec, dt, a, lane);
+      apply_coag(P, w, tg, nspec, dt, a, lane);
       if (autoc1) {
         // applyCoagPrecipFormation (:654-702)
         const double *vol_prc = pf + 7, *num_prc = pf + 7 + 7 * nprc, *inf_num = num_prc + nprc;
@@ -1186,6 +1355,8 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
           if (n > K_PRLIM) w.indef[g] = (w.indef[g] * (n - dt * nrate) + inf * dt * nrate) / n;
         }
         __syncwarp();
+        shadow_bin<KT>(P, w, tg, lane);
+        for (int cc = 0; cc < nprc; cc++) shadow_bin<KT>(P, w, P0 + cc, lane);
       }
     }
   }
@@ -1199,7 +1370,7 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
   for (int kk = 0; kk < nprc; kk++) {
     int tg = P0 + kk;
     if (w.numc[tg] < K_PRLIM) continue;
-    TAcc a;
+    TAccT<KT> a;
     a.zero();
     double num_slf = 0.;
     list_sinks(w, L, tg, a, lane);
@@ -1207,14 +1378,14 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
       if (P.st_secice && P.lscgip && lane == 0) sip_drop_numbers<KT>(P, w, tg, kk, K_PRLIM);
       __syncwarp();
     }
-    if (P.lscgpp && kk == nprc - 1 && lane == 0) a.self += 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
+    if (P.lscgpp && kk == nprc - 1 && lane == 0) a.self += (KT)0.5 * kget(w, tg, tg) * w.nk(tg);
     const double D = w.dwet[tg];
     if (P.lscgpa) {
-      double cm = 0.;
+      KT cm = 0;
       for (int ll = P.in1a + lane; ll <= P.fn2b; ll += 32) {
-        double k = (double)kget(w, ll, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, ll);
-        if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.v(s, ll) * P.rholiq[s];
+        const KT k = kget(w, ll, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, ll);
+        if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.vk(s, ll) * (KT)P.rholiq[s];
       }
       a.dg[6] += cm;
     }
@@ -1222,10 +1393,10 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
       // source from cloud; accretion and autoconversion diagnostics (:1086-1215, coll phase 2)
       for (int ll = lane; ll < P.ncld; ll += 32) {
         int g = C0 + ll;
-        double k = (double)kget(w, g, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, g);
+        const KT k = kget(w, g, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, g);
         if (diag) {
-          double kw = k * w.v(iwa, g);
+          const KT kw = k * w.vk(iwa, g);
           a.dg[3] += kw;
           double dd = cube(D) + cube(w.dwet[g]);
           if (D > 0. && D < 80.e-6 && dd > cube(80.e-6)) a.dg[1] += kw;
@@ -1239,10 +1410,10 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
       int ex80 = min(kk - 1, P.cnt80 - 1), ex50 = min(kk - 1, P.cnt50 - 1);
       for (int ll = lane; ll <= kk - 1; ll += 32) {
         int g = P0 + ll;
-        double k = (double)kget(w, g, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += k * w.v(s, g);
+        const KT k = kget(w, g, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, g);
         if (diag) {
-          double kw = k * w.v(iwa, g);
+          const KT kw = k * w.vk(iwa, g);
           double dd = cube(D) + cube(w.dwet[g]);
           if (ll <= ex80 && D > 0. && D < 80.e-6 && dd > cube(80.e-6)) a.dg[1] += kw;
           if (ll <= ex50 && D > 0. && D < 50.e-6 && dd > cube(50.e-6)) a.dg[2] += kw;
@@ -1266,7 +1437,7 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
     double nold = w.numc[tg];
     double vs_my = (lane < nspec) ? w.v(lane, tg) * nold * kself : 0.;
     num_slf = 0.5 * kself * nold * nold;
-    apply_coag(w, tg, nspec, dt, a, lane);
+    apply_coag(P, w, tg, nspec, dt, a, lane);
     if (P.lscgpp && kk < nprc - 1) {
       // applyCoagPrecp (:584-599): self-coagulation products go to the next bin
       if (lane < nspec) {
@@ -1278,6 +1449,8 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
         w.numc[tg] = w.numc[tg] - dt * num_slf;
       }
       __syncwarp();
+      shadow_bin<KT>(P, w, tg, lane);
+      shadow_bin<KT>(P, w, tg + 1, lane);
     }
   }
 }
@@ -1290,7 +1463,7 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, 
   for (int kk = 0; kk < nice; kk++) {
     int tg = I0 + kk;
     if (w.numc[tg] < K_PRLIM) continue;
-    TAcc a;
+    TAccT<KT> a;
     a.zero();
     double rf_t = rimefrac(P, w.numc[tg], w.v(iwa, tg), w.v(irim, tg), 4);
     if (P.lscgii) {
@@ -1299,11 +1472,11 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, 
         int g = I0 + ll;
         double rf = fmax(rimefrac(P, w.numc[g], w.v(iwa, g), w.v(irim, g), 4), rf_t);
         double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
-        a.sink += E * 1.0 * (double)kget(w, tg, g) * w.numc[g];
+        a.sink += (KT)E * (KT)1.0 * kget(w, tg, g) * w.nk(g);
       }
       if (lane == 0) {
         double E = P.Eiagg_max - fmax(rf_t, rf_t) * (P.Eiagg_max - P.Eiagg_min);
-        a.self += E * 0.5 * (double)kget(w, tg, tg) * w.numc[tg];
+        a.self += (KT)E * (KT)0.5 * kget(w, tg, tg) * w.nk(tg);
       }
     }
     if constexpr (SIP) {
@@ -1322,23 +1495,23 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, 
     // accumulateSourcePhaseChange (:1244-1280)
     if (P.lscgia)
       for (int ll = P.in1a + lane; ll <= P.fn2b; ll += 32) {
-        double k = (double)kget(w, ll, tg);
-        for (int s = 0; s < ndry; s++) a.src[s] += k * w.v(s, ll);
-        a.src[iwa] += k * w.v(iwa, ll) * K_RHOWA / K_RHOIC;
+        const KT k = kget(w, ll, tg);
+        for (int s = 0; s < ndry; s++) a.src[s] += k * w.vk(s, ll);
+        a.src[iwa] += k * w.vk(iwa, ll) * (KT)K_RHOWA / (KT)K_RHOIC;
       }
     if (P.lscgic)
       for (int ll = lane; ll < P.ncld; ll += 32) {
         int g = C0 + ll;
-        double k = (double)kget(w, g, tg);
-        for (int s = 0; s < ndry; s++) a.src[s] += k * w.v(s, g);
-        a.src[irim] += k * w.v(iwa, g) * K_RHOWA / K_RHORI;
+        const KT k = kget(w, g, tg);
+        for (int s = 0; s < ndry; s++) a.src[s] += k * w.vk(s, g);
+        a.src[irim] += k * w.vk(iwa, g) * (KT)K_RHOWA / (KT)K_RHORI;
       }
     if (P.lscgip)
       for (int ll = lane; ll < P.nprc; ll += 32) {
         int g = P0 + ll;
-        double k = (double)kget(w, g, tg);
-        for (int s = 0; s < ndry; s++) a.src[s] += k * w.v(s, g);
-        a.src[irim] += k * w.v(iwa, g) * K_RHOWA / K_RHORI;
+        const KT k = kget(w, g, tg);
+        for (int s = 0; s < ndry; s++) a.src[s] += k * w.vk(s, g);
+        a.src[irim] += k * w.vk(iwa, g) * (KT)K_RHOWA / (KT)K_RHORI;
       }
     // accumulateSourceIce (:1385-1427)
     if (P.lscgii && kk > 0)
@@ -1346,12 +1519,12 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, 
         int g = I0 + ll;
         double rf = fmax(rimefrac(P, w.numc[g], w.v(iwa, g), w.v(irim, g), 4), rf_t);
         double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
-        double k = (double)kget(w, g, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += E * k * w.v(s, g);
+        const KT k = kget(w, g, tg);
+        for (int s = 0; s < nspec; s++) a.src[s] += (KT)E * k * w.vk(s, g);
       }
     a.reduce(false, lane);
     // applyCoagIce (:605-651): every species slot with the same semi-implicit form
-    apply_coag(w, tg, nspec, dt, a, lane);
+    apply_coag(P, w, tg, nspec, dt, a, lane);
     if (lane == 0) w.rhomean[tg] = rhomean_of(P, 4, w.numc[tg], w.v(iwa, tg), w.v(irim, tg));
     __syncwarp();
   }
@@ -1395,6 +1568,7 @@ __device__ void coagulation(const DevParams &P, const WS<KT> &w, const double *t
   bool any_cloud = P.lscgcc || P.lscgca || P.lscgpc || P.lscgic;
   bool any_precp = P.lscgpp || P.lscgpa || P.lscgpc || P.lscgip;
   bool any_ice = P.lscgii || P.lscgia || P.lscgic || P.lscgip;
+  shadow_all<KT>(P, w, lane);
   if (any_ice && T < 273.15) coag_ice<KT, SIP>(P, w, tb, dt, lane);
   if (any_precp) coag_precp<KT, SIP>(P, w, tb, dt, diag, lane);
   if (any_aero) coag_aero<KT>(P, w, tb, dt, lane);
@@ -1517,6 +1691,73 @@ __device__ __forceinline__ void eq_step(EqJob &j, double ckt) {
   j.count++;
 }
 
+// ---- the mixed form's water-uptake iteration in FP32 ----
+// The ZSR molality polynomials in aw (mo_salsa_properties.f90:202-227, 311-341) cancel
+// to a few parts in 1e4 of their terms as aw -> 1, so the float iteration evaluates them
+// in u = 1 - aw with the Taylor-shifted coefficients below, and carries
+// em = 1 - 1/zke = -expm1(-c/dwet), so that u = (1 - zrh) + zrh em keeps its relative
+// accuracy.  The callers clamp zrh to <= 0.98, so u >= 0.02 and the shifted polynomials
+// do not cancel.  Regime 2 (tolerance 1e-12) then takes two FP64 passes from the float
+// result; regime 1a (tolerance 1e-2) ends in float.
+#define ZSR_D0(a0, a1, a2, a3, a4) ((a0) + (a1) + (a2) + (a3) + (a4))
+#define ZSR_D1(a0, a1, a2, a3, a4) (-((a1) + 2. * (a2) + 3. * (a3) + 4. * (a4)))
+#define ZSR_D2(a0, a1, a2, a3, a4) ((a2) + 3. * (a3) + 6. * (a4))
+#define ZSR_D3(a0, a1, a2, a3, a4) (-((a3) + 4. * (a4)))
+#define ZSR_D4(a0, a1, a2, a3, a4) (a4)
+#define ZSR_SHIFTED(u, ...)                                                                          \
+  fmaf(fmaf(fmaf(fmaf((float)ZSR_D4(__VA_ARGS__), u, (float)ZSR_D3(__VA_ARGS__)), u,                 \
+                 (float)ZSR_D2(__VA_ARGS__)), u, (float)ZSR_D1(__VA_ARGS__)), u, (float)ZSR_D0(__VA_ARGS__))
+// bm1 (sulphate, :211-212) and bm5 (sea salt, :318-319) in u = 1 - aw
+__device__ __forceinline__ float zsr1_u(float u) {
+  return ZSR_SHIFTED(u, +1.1065495e+2, -3.6759197e+2, +5.0462934e+2, -3.1543839e+2, +6.770824e+1);
+}
+__device__ __forceinline__ float zsr5_u(float u) {
+  return ZSR_SHIFTED(u, +5.875248e+1, -1.8781997e+2, +2.7211377e+2, -1.8458287e+2, +4.153689e+1);
+}
+
+struct EqJobF {
+  int kk, count;
+  bool r2;
+  float tol, zrh, omrh, em, zdwet, zdold, zlwc;
+  float q0, q1, q4, p56, pc, rinv;
+};
+
+template <typename KT>
+__device__ __forceinline__ void eq_load_f(const DevParams &P, const WS<KT> &w, int b, EqJobF &j) {
+  j.kk = b;
+  j.count = 0;
+  const float numc = (float)w.numc[b], in = 1.f / numc;
+  float zv[7];
+  for (int i = 0; i < 7; i++) zv[i] = (float)zvolc_of(P, w, i, b);
+  const float zcore = j.r2 ? (zv[0] + zv[1] + zv[2] + zv[3] + zv[4]) * in : (zv[0] + zv[1]) * in;
+  const float rhosu_msu = (float)(1830. / 98.08e-3), rhooc_moc = (float)(1400. / 150.e-3),
+              rhoss_mss = (float)(2165. / 58.44e-3), ipi6 = (float)(1. / K_PI6);
+  j.q0 = zv[0] * rhosu_msu;
+  j.q1 = (float)K_EPSOC * zv[1] * rhooc_moc;
+  j.q4 = zv[4] * rhoss_mss;
+  j.p56 = (zv[5] + zv[6]) * in * ipi6;
+  j.pc = zcore * ipi6;
+  j.rinv = in * (float)(1. / (K_RHOWA * K_PI6));
+  j.zdwet = (float)w.dwet[b];
+  j.zdold = 1.f;
+  j.zlwc = 0.f;
+}
+
+__device__ __forceinline__ void eq_step_f(EqJobF &j, float ckt) {
+  j.zdold = fmaxf(j.zdwet, 1.e-20f);
+  const float u = fmaf(j.zrh, j.em, j.omrh);   // 1 - zrh / zke
+  const float zaw = 1.f - u;
+  const float bm1 = zsr1_u(u);
+  const float bm2 = u / (zaw * (float)K_MWA);   // 1/(aw M) - 1/M
+  const float bm5 = j.r2 ? zsr5_u(u) : 1.f;
+  const float q4 = j.r2 ? j.q4 : 0.f;
+  const float zlwc = fmaf(q4, bm1 * bm2, fmaf(j.q1, bm1 * bm5, j.q0 * (bm2 * bm5))) / (bm1 * bm2 * bm5);
+  j.zlwc = zlwc;
+  j.zdwet = cbrtf(fmaf(zlwc, j.rinv, j.p56) + j.pc);
+  j.em = -expm1f(-(ckt / j.zdwet));
+  j.count++;
+}
+
 // next regime-1a bin after b with numc > nlim; empty bins take dmid when initialising
 template <typename KT>
 __device__ __forceinline__ int eq_next_1a(const DevParams &P, const WS<KT> &w, const double *dmid, int b, bool init) {
@@ -1534,7 +1775,64 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
   int nonconv = 0;
   const int n2 = init ? P.fn2b - P.in2a + 1 : 0;
   const double ckt = 2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T);
-  if (n2 <= 31) {
+  if (n2 <= 31 && sizeof(KT) == 4) {
+    // the mixed form: lane 31 runs the regime-1a chain, lanes 0..n2-1 the regime-2 bins,
+    // all in float; then the regime-2 lanes take two FP64 passes from the float result
+    EqJobF j;
+    j.kk = -1;
+    const float cktf = (float)ckt;
+    if (lane == 31) {
+      const double zrh = fmin(fmax(prh, 0.05), 0.98);
+      j.r2 = false; j.tol = 1.e-2f; j.zrh = (float)zrh; j.omrh = (float)(1. - zrh); j.em = (float)(1. - 1. / 1.001);
+      int k = eq_next_1a(P, w, dmid, P.in1a - 1, init);
+      if (k >= 0) eq_load_f(P, w, k, j);
+    } else if (lane < n2) {
+      int k = P.in2a + lane;
+      if (w.numc[k] > K_NLIM) {
+        const double zrh = fmin(fmax(prh, 0.37), 0.98);
+        j.r2 = true; j.tol = 1.e-6f; j.zrh = (float)zrh; j.omrh = (float)(1. - zrh); j.em = (float)(1. - 1. / 1.02);
+        eq_load_f(P, w, k, j);
+      } else {
+        w.dwet[k] = dmid[k];
+      }
+    }
+    int r2k = -1;   // the regime-2 bin a lane polishes
+    while (__any_sync(0xffffffffu, j.kk >= 0)) {
+      if (j.kk >= 0) {
+        bool go = fabsf(j.zdwet - j.zdold) > j.tol * j.zdold;
+        if (go) {
+          eq_step_f(j, cktf);
+          if (j.count > 100) { nonconv = 1; go = false; }
+        }
+        if (!go) {
+          if (j.r2) {
+            r2k = j.kk;
+            j.kk = -1;
+          } else {
+            w.v(P.iwa, j.kk) = (double)j.zlwc * (1. / K_RHOWA);
+            if (init) w.dwet[j.kk] = (double)j.zdwet;
+            int k = eq_next_1a(P, w, dmid, j.kk, init);
+            if (k >= 0) eq_load_f(P, w, k, j);
+            else j.kk = -1;
+          }
+        }
+      }
+    }
+    if (__any_sync(0xffffffffu, r2k >= 0)) {
+      EqJob d;
+      if (r2k >= 0) {
+        d.r2 = true; d.tol = 1.e-12; d.zrh = fmin(fmax(prh, 0.37), 0.98);
+        eq_load(P, w, r2k, d);
+        d.zdwet = (double)j.zdwet;
+        d.izke = exp(-(ckt / d.zdwet));
+        eq_step(d, ckt);
+        eq_step(d, ckt);
+        w.v(P.iwa, r2k) = d.zlwc / K_RHOWA;
+        w.dwet[r2k] = d.zdwet;
+      }
+    }
+    __syncwarp();
+  } else if (n2 <= 31) {
     // lane 31: the regime-1a chain in bin order; lanes 0..n2-1: regime-2 bins
     EqJob j;
     j.kk = -1;
@@ -3075,8 +3373,8 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
     const int icat = (ncat == 4 && r >= P.raw_mbase[3]) ? 3 : (r >= P.raw_mbase[2] ? 2 : (r >= P.raw_mbase[1] ? 1 : 0));
     const int loc = r - P.raw_mbase[icat], nbc = bnum[icat];
     const int sp = loc / nbc, b = bstart[icat] + (loc - sp * nbc);
-    const double rho = icat < 3 ? P.rholiq[sp] : (sp < nwet ? P.rhoice[sp] : K_RHORI);
-    w.v(sp, b) = raw[r] * dn / rho;
+    const double irho = icat < 3 ? P.irholiq[sp] : (sp < nwet ? P.irhoice[sp] : 1. / K_RHORI);
+    w.v(sp, b) = raw[r] * dn * irho;
   }
   __syncwarp();
   for (int b = lane; b < P.ntotal; b += 32) {
@@ -3138,14 +3436,18 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   STAGE_MARK(5);
 
   // ---- tendencies and outputs (mo_salsa_driver.f90:310-419) into the raw slots ----
+  // (x / dn - old) / dt: one division for 1/dn per cell, and the quotient by dt as a
+  // product when dt is a power of two (then it is the same number)
   bool bad = false;
+  const double idn = 1. / dn;
   for (int e = lane; e < nmrow; e += 32) {
     const int r = m0 + e;
     const int icat = (ncat == 4 && r >= P.raw_mbase[3]) ? 3 : (r >= P.raw_mbase[2] ? 2 : (r >= P.raw_mbase[1] ? 1 : 0));
     const int loc = r - P.raw_mbase[icat], nbc = bnum[icat];
     const int sp = loc / nbc, b = bstart[icat] + (loc - sp * nbc);
     const double rho = icat < 3 ? P.rholiq[sp] : (sp < nwet ? P.rhoice[sp] : K_RHORI);
-    raw[r] = ((w.v(sp, b) * rho / dn) - raw[r]) / dt;
+    const double d = (w.v(sp, b) * rho * idn) - raw[r];
+    raw[r] = P.inv_dt != 0. ? d * P.inv_dt : d / dt;
   }
   for (int b = lane; b < P.ntotal; b += 32) {
     int icat = phase_of(P, b) - 1;
@@ -3155,7 +3457,8 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
       if (P.raw_charge >= 0) raw[P.raw_charge + b] = w.ctime[b];
     }
     double *on = raw + P.raw_num + b;
-    *on = ((w.numc[b] / dn) - *on) / dt;
+    const double d = (w.numc[b] * idn) - *on;
+    *on = P.inv_dt != 0. ? d * P.inv_dt : d / dt;
     bad |= !isfinite(w.numc[b]);
   }
   // interstitial activation leaves the activated-droplet outputs at zero (:879, local pactd);
@@ -3226,6 +3529,8 @@ __device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
   w.indef = p; p += NB;
   w.ctime = p; p += NB;
   w.scr = p; p += SALSA_NSCR * NB;
+  w.nf = reinterpret_cast<float *>(w.scr);   // NB floats, then SALSA_NSV * NB floats (4 scratch rows)
+  w.vf = w.nf + NB;
   w.misc = p; p += SALSA_MISC_DOUBLES;
   w.pbuf = reinterpret_cast<int *>(p); p += 64;   // 128 ints: bin lists (<= 96) and pair batches (<= 63)
   w.K = reinterpret_cast<KT *>(p);

@@ -44,6 +44,8 @@ struct ClampArgs {
   double dtlt;
   double rdt;           // 1 / dtlt when dtlt is a power of two (the quotient is then a product), else 0
   int be_dt;            // biased exponent of dtlt
+  unsigned long long cm;   // significand of |-1 + 1e-8| with its leading bit
+  int ce;                  // biased exponent of |-1 + 1e-8|
   double *indef;
   long long nindef;
 };
@@ -58,11 +60,34 @@ __device__ __forceinline__ bool gt_bits(long long b, long long bc) { return b > 
 __device__ __forceinline__ bool lt_bits(long long b, long long bc) { return (b & ABS_MASK) < bc; }
 __device__ __forceinline__ bool le0_bits(long long b) { return (b & ABS_MASK) == 0; }
 
+// |(-1 + 1e-8) p| / dtlt for p > 0 normal and dtlt = 2^(1023 - dk) a power of two, as the
+// bit pattern of a positive double, from the integer product of the significands rounded
+// to nearest even: the bits of the FP64 product and power-of-two quotient whenever the
+// result is normal, which is then exact.  Returns -1 where it would not be normal.
+__device__ __forceinline__ long long mag_lo_bits(long long bp, unsigned long long cm, int ce, int dk) {
+  const unsigned long long mp = ((unsigned long long)bp & 0x000fffffffffffffULL) | (1ULL << 52);
+  const unsigned long long hi = __umul64hi(mp, cm), lo = mp * cm;   // product in [2^104, 2^106)
+  const int ep = bexp(bp);
+  unsigned long long m, r, half;
+  int e;
+  if (hi >> 41) { m = (hi << 11) | (lo >> 53); r = lo & ((1ULL << 53) - 1); half = 1ULL << 52; e = ep + ce - 1022; }
+  else { m = (hi << 12) | (lo >> 52); r = lo & ((1ULL << 52) - 1); half = 1ULL << 51; e = ep + ce - 1023; }
+  if (r > half || (r == half && (m & 1ULL))) {
+    m++;
+    if (m >> 53) { m >>= 1; e++; }
+  }
+  e += dk;
+  if (e <= 0 || e >= 2047) return -1;
+  return ((long long)e << 52) | (long long)(m & 0x000fffffffffffffULL);
+}
+
 // t = MAX((-1 + 1e-8) * p / dtlt, t).  For p = +-0 the limit is the zero of the other
 // sign (a finite positive dtlt).  The limit is < 0 for a normal p > 0, so a tendency with
 // its sign bit clear never moves; for t < 0 the exponents settle |t| < |lo| whenever
-// |t| dtlt < p / 4; the rest compute lo in FP64.
-__device__ __forceinline__ void clamp_tendency(double p, double t, double *tp, double dtlt, double rdt, int be_dt) {
+// |t| dtlt < p / 4.  The rest form lo: with a power-of-two dtlt from the integer product
+// (mag_lo_bits) and compare magnitudes as integers (both negative), otherwise in FP64.
+__device__ __forceinline__ void clamp_tendency(double p, double t, double *tp, double dtlt, double rdt, int be_dt,
+                                               unsigned long long cm, int ce) {
   const long long bp = bits_of(p), bt = bits_of(t);
   if ((bp & ABS_MASK) == 0) {          // p = +-0: lo is the zero of the other sign
     if (neg_bits(bt)) *tp = bp == 0 ? -0. : 0.;
@@ -71,6 +96,14 @@ __device__ __forceinline__ void clamp_tendency(double p, double t, double *tp, d
   if (bp >= 0 && bexp(bp) != 0 && bexp(bp) != 0x7ff) {
     if (bt >= 0) return;
     if (bexp(bt) + be_dt + 3 - 1023 <= bexp(bp)) return;
+    if (rdt != 0. && (bt & ABS_MASK) <= INF_BITS) {
+      const long long ml = mag_lo_bits(bp, cm, ce, 1023 - be_dt);
+      if (ml >= 0) {
+        // lo = -|lo| > t  <=>  |lo| < |t| (t < 0, not NaN)
+        if (ml < (bt & ABS_MASK)) *tp = __longlong_as_double(ml | (long long)0x8000000000000000ULL);
+        return;
+      }
+    }
   }
   const double q = (-1. + 1.e-8) * p;
   const double lo = rdt != 0. ? q * rdt : q / dtlt;   // the same rounding of the same quotient
@@ -97,16 +130,20 @@ __global__ void __launch_bounds__(256) tend_constrain_kernel(const ClampArgs A) 
 #pragma unroll
       for (int u = 0; u < B; u++) {
         const long long e = e0 + u * stride;
-        if (e < n) clamp_tendency(vp[u], vt[u], t + e, A.dtlt, A.rdt, A.be_dt);
+        if (e < n) clamp_tendency(vp[u], vt[u], t + e, A.dtlt, A.rdt, A.be_dt, A.cm, A.ce);
       }
     }
   }
-  if (A.indef)
+  // the IN deficit to [0, 1] (MIN(MAX(v, 0), 1)), decided on the bits: NaN and v < 0
+  // become 0, v > 1 becomes 1; -0 and values inside stay as they are
+  if (A.indef) {
+    const long long ONE = 0x3ff0000000000000LL;
     for (long long e = i0; e < A.nindef; e += stride) {
-      const double v = A.indef[e];
-      const double c = fmin(fmax(v, 0.), 1.);
-      if (c != v) A.indef[e] = c;
+      const long long b = bits_of(A.indef[e]), m = b & ABS_MASK;
+      if (m > INF_BITS || neg_bits(b)) A.indef[e] = 0.;
+      else if (b > ONE) A.indef[e] = 1.;
     }
+  }
 }
 
 // util.f90:1005-1024 calc_correlation, as written (sxy keeps the last product only)
@@ -393,6 +430,14 @@ int salsa_gb300_tend_constrain(salsa_handle_t *h, int nzp, int nxp, int nyp, dou
   // a normal power of two with a normal reciprocal: mantissa zero
   const bool pow2 = (bdt & 0x000fffffffffffffLL) == 0 && A.be_dt > 1 && A.be_dt < 2045;
   A.rdt = pow2 ? 1. / dtlt : 0.;
+  {
+    const double c = -1. + 1.e-8;   // the factor of the limit, as tend_constrain2 writes it
+    const double cabs = -c;
+    long long bc;
+    memcpy(&bc, &cabs, sizeof bc);
+    A.cm = ((unsigned long long)bc & 0x000fffffffffffffULL) | (1ULL << 52);
+    A.ce = (int)((bc >> 52) & 0x7ff);
+  }
   A.indef = (g->ice_theta_dist && g->level > 4) ? f->indef : nullptr;
   A.nindef = (long long)P.nliquid * plane;
   if (!salsa::device_ptrs({vp[0], vp[1], vp[2], vp[3], vp[4], vp[5], vp[6], vp[7], vp[8], vt[0], vt[1], vt[2], vt[3],

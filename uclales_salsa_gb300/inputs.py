@@ -122,8 +122,12 @@ def _cloud_mask(spec, gen, X, Y, Z, device):
     return m.reshape(-1)
 
 
-def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnostics=1, seed=None, gases=False):
+def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnostics=1, seed=None, gases=False,
+                overrides=None):
     """Build the fields of workload `name` (optionally with a smaller interior).
+
+    overrides: entries of the workload's description to replace (e.g. cloudy=0.0 for
+    clear cells only, or cloudy=1.0 with pattern="random" for cloudy cells only).
 
     gases: seeded condensing-vapour concentrations in gaero (H2SO4 and non-volatile
     organics 1e5-1e7 /cm3, semi-volatile organics 1e6-1e8 /cm3, HNO3 and NH3 1e8-1e9
@@ -133,6 +137,8 @@ def make_inputs(name, device="cpu", X=None, Y=None, Z=None, precision=0, diagnos
         spec["X"], spec["Y"], spec["Z"] = X, Y, Z
     if seed is not None:
         spec["seed"] = seed
+    if overrides:
+        spec.update(overrides)
     X, Y, Z = spec["X"], spec["Y"], spec["Z"]
     level = spec["level"]
     cfg = workload_config(level, precision=precision, diagnostics=diagnostics)

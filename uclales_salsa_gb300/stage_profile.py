@@ -8,7 +8,7 @@ chain65536 workload, --steps steps) and prints the stage clocks of the forward c
 of the adjoint's taped recompute and of its reverse sweep.  The instrumented library
 is separate from the product build.
 
-    python -m uclales_salsa_gb300.stage_profile [--X 96 --Y 96 --Z 32]
+    python -m uclales_salsa_gb300.stage_profile [--X 96 --Y 96 --Z 32] [--classes]
     python -m uclales_salsa_gb300.stage_profile --chain [--cells 16384 --steps 10]
 """
 import argparse
@@ -92,6 +92,8 @@ def main():
     ap.add_argument("--chain", action="store_true")
     ap.add_argument("--cells", type=int, default=16384)
     ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--classes", action="store_true",
+                    help="also profile grid384x384x160 with clear cells only and with cloudy cells only")
     a = ap.parse_args()
     lib = build_instrumented()
     B.LIB = lib
@@ -103,9 +105,12 @@ def main():
         return
     import torch
     from .inputs import make_inputs, make_outputs
-    for wl in ("grid256x256x128", "grid384x384x160"):
+    cases = [("grid256x256x128", None), ("grid384x384x160", None)]
+    if a.classes:
+        cases += [("grid384x384x160", dict(cloudy=0.0)), ("grid384x384x160", dict(cloudy=1.0, pattern="random"))]
+    for wl, ov in cases:
         for prec in (0, 1):
-            inp = make_inputs(wl, "cuda", precision=prec, diagnostics=0, X=a.X, Y=a.Y, Z=a.Z)
+            inp = make_inputs(wl, "cuda", precision=prec, diagnostics=0, X=a.X, Y=a.Y, Z=a.Z, overrides=ov)
             s = api.SalsaStep(inp.cfg)
             outs = make_outputs(inp, with_diag=False)
             arr = (C.c_ulonglong * 16)()
@@ -116,7 +121,7 @@ def main():
             s.run(inp, f, outs)
             L.salsa_gb300_stage_clocks(s.h, arr)
             tot = sum(arr[i] for i in range(7))
-            print(wl, "precision", prec, "cells", inp.ncells, "kernel ms", round(s.last_kernel_ms(), 2))
+            print(wl, ov or "", "precision", prec, "cells", inp.ncells, "kernel ms", round(s.last_kernel_ms(), 2))
             for i, n in enumerate(STAGES):
                 if n != "-":
                     print(f"   {n:16s} {100.0 * arr[i] / tot:6.2f} %   ({arr[i] / inp.ncells:.0f} warp-clk/cell)")
