@@ -24,11 +24,12 @@
 
 /* ---- rounding perturbation of the library functions (test infrastructure) ----
  * Two correct FP64 implementations of this path differ in how their exp, log, pow and
- * cube roots round (glibc here, CUDA's functions on the GPU): by about one ulp.  The
+ * cube roots round (glibc here, CUDA's functions on the GPU): by one or two ulps.  The
  * parity tests measure the oracle's own response to that difference: with a mode set,
- * every result of those functions moves by one ulp, up (+1), down (-1), or in a
- * direction taken from the bits of the argument (modes 2 and above, one pattern each).  sqrt rounds correctly on both
- * sides and is left alone.  Mode 0 (the default) leaves every result as it is. */
+ * every result of those functions moves by two ulps, up (+1), down (-1), or in a
+ * direction taken from the bits of the argument (modes 2 and above, one pattern each).
+ * sqrt rounds correctly on both sides and is left alone.  Mode 0 (the default) leaves
+ * every result as it is. */
 static int g_libm_pert = 0;
 void salsa_ref_set_libm_perturbation(int mode) { g_libm_pert = mode; }
 static inline double pert_ulp(double r, double x) {
@@ -43,7 +44,9 @@ static inline double pert_ulp(double r, double x) {
     b ^= b >> 32;
     up = (int)(b & 1u);
   }
-  return nextafter(r, up ? INFINITY : -INFINITY);
+  /* two ulps: the documented bound of CUDA's pow (exp, log and cbrt are within one) */
+  const double dir = up ? INFINITY : -INFINITY;
+  return nextafter(nextafter(r, dir), dir);
 }
 #define exp(x) pert_ulp(exp(x), (x))
 #define log(x) pert_ulp(log(x), (x))

@@ -30,7 +30,7 @@ typedef struct salsa_ref_ctx salsa_ref_ctx_t;
 int salsa_ref_create(const salsa_config_t *cfg, salsa_ref_ctx_t **out);
 
 /* Test infrastructure: move every exp/log/log10/pow/erf/cos result of the following runs
- * by one ulp, up (1), down (-1) or in a direction from the argument's bits (2 and above,
+ * by two ulps, up (1), down (-1) or in a direction from the argument's bits (2 and above,
  * one pattern per mode); 0 turns it off.  The parity tests take the oracle's response as part of their envelope. */
 void salsa_ref_set_libm_perturbation(int mode);
 void salsa_ref_destroy(salsa_ref_ctx_t *ctx);

@@ -79,21 +79,21 @@ def test_null_arguments_are_rejected():
     assert lib.salsa_gb300_run(None, 42, 20, 20, 6, 1.0, 1.0, 1, 4, 0, 0, None, C.byref(st)) == capi.SALSA_E_ARG
 
 
-def test_secondary_ice_modes_outside_the_step_are_refused_before_any_device_call():
-    """salsa_gb300_init answers SALSA_E_UNSUPPORTED, before it touches a device, for
-    the secondary-ice modes the step kernel does not hold (rime splintering outside
-    modes 1-2, drop fracturing mode 4, ice-ice breakup mode 3); the modes it holds get
-    past that check."""
+def test_secondary_ice_modes_outside_the_reference_are_refused_before_any_device_call():
+    """salsa_gb300_init answers SALSA_E_UNSUPPORTED, before it touches a device, for the
+    secondary-ice modes the reference does not define (rime splintering outside 1-2, drop
+    fracturing outside 1-4, ice-ice breakup outside 1-3); every mode it defines gets past
+    that check."""
     lib = api.library()
     h = C.c_void_p()
-    for scheme, modes in (("lssiprimespln", (3,)), ("lssipdropfrac", (4,)), ("lssipicecollbreak", (3,))):
+    for scheme, modes in (("lssiprimespln", (0, 3)), ("lssipdropfrac", (0, 5)), ("lssipicecollbreak", (0, 4))):
         for mode in modes:
             cfg = reference_defaults(level=5)
             cfg.lssecice.sw = 1
             sw = getattr(cfg, scheme)
             sw.sw, sw.mode = 1, mode
             assert lib.salsa_gb300_init(C.byref(cfg), C.byref(h)) == capi.SALSA_E_UNSUPPORTED, (scheme, mode)
-    for scheme, modes in (("lssiprimespln", (1, 2)), ("lssipdropfrac", (1, 2, 3)), ("lssipicecollbreak", (1, 2))):
+    for scheme, modes in (("lssiprimespln", (1, 2)), ("lssipdropfrac", (1, 2, 3, 4)), ("lssipicecollbreak", (1, 2, 3))):
         for mode in modes:
             cfg = reference_defaults(level=5)
             cfg.lssecice.sw = 1
@@ -103,6 +103,11 @@ def test_secondary_ice_modes_outside_the_step_are_refused_before_any_device_call
             assert rc != capi.SALSA_E_UNSUPPORTED, (scheme, mode)
             if rc == capi.SALSA_OK:
                 lib.salsa_gb300_finalize(h)
+    cfg = reference_defaults(level=5)
+    rc = lib.salsa_gb300_init(C.byref(cfg), C.byref(h))
+    assert rc != capi.SALSA_E_UNSUPPORTED
+    if rc == capi.SALSA_OK:
+        lib.salsa_gb300_finalize(h)
     cfg = reference_defaults(level=5)
     rc = lib.salsa_gb300_init(C.byref(cfg), C.byref(h))
     assert rc != capi.SALSA_E_UNSUPPORTED

@@ -9,7 +9,8 @@ from test_gpu_parity import oracle_run, gpu_run, envelope, check, VIOL_FRAC, FRA
 pytestmark = pytest.mark.gpu
 
 SCHEMES = [("lssiprimespln", 1), ("lssiprimespln", 2), ("lssipdropfrac", 1), ("lssipdropfrac", 2),
-           ("lssipdropfrac", 3), ("lssipicecollbreak", 1), ("lssipicecollbreak", 2)]
+           ("lssipdropfrac", 3), ("lssipdropfrac", 4), ("lssipicecollbreak", 1), ("lssipicecollbreak", 2),
+           ("lssipicecollbreak", 3)]
 
 
 def _parity(inp, rtol, eps):

@@ -39,7 +39,9 @@ def _rank(rank, world, store, q):
     rc, _ = Oracle(inp.cfg).run(inp, f, out, time=1.0, nthreads=1)
     t = torch.tensor([time.perf_counter() - t0])
     dist.all_reduce(t, op=dist.ReduceOp.MAX)       # the slowest rank's time
-    q.put((rank, rc, float(t), {k: v[..., 2:-2, :, :].clone() for k, v in out.items() if k != "diag"}))
+    # numpy arrays travel by value: a torch tensor would travel as a file descriptor that
+    # this process must still serve when the parent unpickles it
+    q.put((rank, rc, float(t), {k: v[..., 2:-2, :, :].numpy().copy() for k, v in out.items() if k != "diag"}))
     dist.destroy_process_group()
 
 
@@ -67,5 +69,5 @@ def test_two_gloo_ranks_reproduce_the_single_run(tmp_path):
     for k, full in out.items():
         if k == "diag":
             continue
-        both = torch.cat([res[0][3][k], res[1][3][k]], dim=-3)
+        both = torch.cat([torch.from_numpy(res[0][3][k]), torch.from_numpy(res[1][3][k])], dim=-3)
         assert torch.equal(both, full[..., 2:-2, :, :]), k

@@ -224,13 +224,13 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
   if (g.nspec_dry < 1 || g.nspec_dry > SALSA_MAXSPEC) return SALSA_E_ARG;
   if (g.nspec_dry > 5) return SALSA_E_UNSUPPORTED;   // SALSA_NSV volume slots per bin
   if (g.precision != 0 && g.precision != 1) return SALSA_E_ARG;
-  // processes outside this build: Phillips' full secondary-ice forms (drop fracturing
-  // mode 4, breakup mode 3) are restated in the oracle but not in the step kernel
+  // the secondary-ice modes of the reference: rime splintering 1-2, drop fracturing 1-4,
+  // ice-ice breakup 1-3
   if (g.lssecice.sw) {
     const salsa_switch_t &rs = g.lssiprimespln, &df = g.lssipdropfrac, &ib = g.lssipicecollbreak;
     if (rs.sw && (rs.mode < 1 || rs.mode > 2)) return SALSA_E_UNSUPPORTED;
-    if (df.sw && (df.mode < 1 || df.mode > 3)) return SALSA_E_UNSUPPORTED;
-    if (ib.sw && (ib.mode < 1 || ib.mode > 2)) return SALSA_E_UNSUPPORTED;
+    if (df.sw && (df.mode < 1 || df.mode > 4)) return SALSA_E_UNSUPPORTED;
+    if (ib.sw && (ib.mode < 1 || ib.mode > 3)) return SALSA_E_UNSUPPORTED;
   }
   if (g.lscoag.mode == 2 && !(g.cgintvl > 0.)) return SALSA_E_ARG;
   // nucleation: the ternary scheme STOPs in the reference (mo_salsa_nucleation.f90:236-238);

@@ -203,15 +203,15 @@ __device__ __forceinline__ CoagCell<R> chain_coagcell(double T, double pres, con
 
 template <typename R>
 __device__ __forceinline__ void chain_store_props(R *S, int NL, int b, const BinProps<R> &o) {
-  S[0 * NL + b] = o.diam; S[1 * NL + b] = o.mass; S[2 * NL + b] = o.beta; S[3 * NL + b] = o.dfpart;
-  S[4 * NL + b] = o.mtvel; S[5 * NL + b] = o.omega; S[6 * NL + b] = o.termv; S[7 * NL + b] = o.reyn;
-  S[8 * NL + b] = o.schm;
+  const R *po = &o.diam;
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k * NL + b] = po[k];
 }
 template <typename R>
 __device__ __forceinline__ void chain_load_props(const R *S, int NL, int b, BinProps<R> &o) {
-  o.diam = S[0 * NL + b]; o.mass = S[1 * NL + b]; o.beta = S[2 * NL + b]; o.dfpart = S[3 * NL + b];
-  o.mtvel = S[4 * NL + b]; o.omega = S[5 * NL + b]; o.termv = S[6 * NL + b]; o.reyn = S[7 * NL + b];
-  o.schm = S[8 * NL + b];
+  R *po = &o.diam;
+#pragma unroll
+  for (int k = 0; k < 9; k++) po[k] = S[k * NL + b];
 }
 
 // Populated bins (number at or above the bin's limit), compacted into pbuf in bin order;

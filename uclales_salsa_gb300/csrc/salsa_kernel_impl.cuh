@@ -41,6 +41,10 @@ struct WS {
   // float copies of numc and volc that the mixed form's coagulation update sums from
   // (in the scratch rows, valid from shadow_all to the end of the update)
   float *nf, *vf;
+  // warp pairing of the FP64 water uptake: 0 alone, 1 the warp that runs both cells,
+  // 2 the warp whose cell it runs; the named barrier of the pair; the partner's workspace
+  int role, bar;
+  double *pbase;
   __device__ __forceinline__ double &v(int s, int b) const { return volc[s * NB + b]; }
   __device__ __forceinline__ double *sc(int k) const { return scr + k * NB; }
   // partner values in the kernel type: the state itself (FP64 form) or its float copy
@@ -59,6 +63,7 @@ enum {
   M_DIAG = 0,              // 17 diagnostic accumulators
   M_FLAGS = 17,            // F_* per-cell condition counters
   M_RV = 24,               // water vapour mixing ratio of the cell
+  M_EQ = 25,               // a paired cell's water-uptake inputs: relative humidity, T, init flag
   M_PF = 32,               // precipitation-formation accumulators (7 + 9 * nprc, nprc <= 23)
   M_PFSLOT = M_PF + 216,   // 8 partner slots * 10
   M_GAS = M_PFSLOT + 80,   // the cell's five gases [#/m3] (gas condensation only)
@@ -252,24 +257,43 @@ __device__ T terminal_vel(T diam, T rhop, T rhoa, T visc, T beta, int flag, cons
 template <typename T>
 struct CoagCell { T T_, visc, mfp, zrhoa, vkin, shearA, turbB; };
 
-// per-bin collision properties (the particle-dependent part of coagc :263-364)
+// Per-bin collision properties (the particle-dependent part of coagc :263-364), in the
+// form the pair evaluation uses: the squared mean thermal velocity, and the per-bin
+// factors of the convective Brownian term and of the collision efficiency, so that a pair
+// takes no cube root and one division less.  Nine values (the gradient harness stores
+// and differentiates them as a row each).
 template <typename T>
-struct BinProps { T diam, mass, beta, dfpart, mtvel, omega, termv, reyn, schm; };
+struct BinProps { T diam, fre, cschm, dfpart, mtvel2, omega, termv, reyn, ire; };
+// fre = Re^(1/3) for Re <= 1, else Re^(1/2) (:350-355); cschm = Sc^(1/3); ire = 1/(60 + Re)
 
 template <typename T>
 __device__ void bin_props(const CoagCell<T> &cc, int ph, T diam, T dsph, T mass, T rhomean, const Shape<T> &sh,
                           BinProps<T> &o) {
   o.diam = diam;
-  o.mass = mass;
   T knud = (T)2. * cc.mfp / diam;
-  o.beta = (T)1. + knud * ((T)1.142 + (T)0.558 * t_exp((T)-0.999 / knud));
-  o.dfpart = o.beta * (T)K_BOLTZ * cc.T_ / ((T)3. * (T)K_PI * cc.visc * diam);
-  o.mtvel = t_sqrt(((T)8. * (T)K_BOLTZ * cc.T_) / ((T)K_PI * mass));
-  o.omega = (T)8. * o.dfpart / ((T)K_PI * o.mtvel);
-  if (ph < 4) o.termv = terminal_vel<T>(diam, rhomean, cc.zrhoa, cc.visc, o.beta, ph, sh, (T)0);
-  else o.termv = terminal_vel<T>(dsph, rhomean, cc.zrhoa, cc.visc, o.beta, ph, sh, diam);
+  const T beta = (T)1. + knud * ((T)1.142 + (T)0.558 * t_exp((T)-0.999 / knud));
+  o.dfpart = beta * (T)K_BOLTZ * cc.T_ / ((T)3. * (T)K_PI * cc.visc * diam);
+  const T mtvel = t_sqrt(((T)8. * (T)K_BOLTZ * cc.T_) / ((T)K_PI * mass));
+  o.mtvel2 = sq(mtvel);
+  o.omega = (T)8. * o.dfpart / ((T)K_PI * mtvel);
+  if constexpr (is_f32<T>::value) {
+    // the fall speed stays FP64 in the mixed form: collision kernels of pairs with close
+    // fall speeds take their difference, which would magnify float rounding of the Beard
+    // exponent (exp of up to ~10) into the kernel
+    Shape<double> shd;
+    shd.alpha = sh.alpha; shd.beta = sh.beta; shd.gamma = sh.gamma; shd.sigma = sh.sigma;
+    const double vd = ph < 4 ? terminal_vel<double>(diam, rhomean, cc.zrhoa, cc.visc, beta, ph, shd, 0.)
+                             : terminal_vel<double>(dsph, rhomean, cc.zrhoa, cc.visc, beta, ph, shd, diam);
+    o.termv = (T)vd;
+  } else {
+    if (ph < 4) o.termv = terminal_vel<T>(diam, rhomean, cc.zrhoa, cc.visc, beta, ph, sh, (T)0);
+    else o.termv = terminal_vel<T>(dsph, rhomean, cc.zrhoa, cc.visc, beta, ph, sh, diam);
+  }
   o.reyn = diam * o.termv / cc.vkin;
-  o.schm = cc.vkin / o.dfpart;
+  const T schm = cc.vkin / o.dfpart;
+  o.fre = o.reyn <= (T)1. ? t_cbrt(o.reyn) : t_sqrt(o.reyn);
+  o.cschm = t_cbrt(schm);
+  o.ire = (T)1. / ((T)60. + o.reyn);
 }
 
 // ((m+w)^3 - (m^2+w^2)^(3/2)) / (3 m w) - m without cancellation (float form of :305-313):
@@ -290,7 +314,7 @@ template <typename T>
 __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinProps<T> &b) {
   T mdiam = (T)0.5 * (a.diam + b.diam);
   T flux1 = (T)4. * (T)K_PI * mdiam * (a.dfpart + b.dfpart);
-  T flux2 = (T)K_PI * t_sqrt(sq(a.mtvel) + sq(b.mtvel)) * sq(mdiam);
+  T flux2 = (T)K_PI * t_sqrt(a.mtvel2 + b.mtvel2) * sq(mdiam);
   T tva1, tva2;
   if (!is_f32<T>::value) {
     T m2 = sq(mdiam);
@@ -316,9 +340,8 @@ __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinPro
   } else {
     zbrown = flux1 / (mdiam / (mdiam + fmdist) + flux1 / flux2);
   }
-  T zbrconv;
-  if (L.reyn <= (T)1.) zbrconv = (T)0.45 * zbrown * t_cbrt(L.reyn * S.schm);
-  else zbrconv = (T)0.45 * zbrown * t_sqrt(L.reyn) * t_cbrt(S.schm);
+  // Re <= 1: (Re Sc)^(1/3), else Re^(1/2) Sc^(1/3), from the per-bin factors
+  const T zbrconv = (T)0.45 * zbrown * L.fre * S.cschm;
   T hd = (T)0.5 * (a.diam + b.diam);
   T ztshear = cc.shearA * cube(hd);
   T zturb = cc.turbB * sq(hd) * dv;
@@ -328,7 +351,7 @@ __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinPro
     zev = (T)0.75 * t_log((T)2. * stok) / (stok - (T)1.214);
     zev = (T)1. / sq((T)1. + zev);
   }
-  T zecoll = ((T)60. * zev + zea * L.reyn) / ((T)60. + L.reyn);
+  T zecoll = ((T)60. * zev + zea * L.reyn) * L.ire;
   T zgrav = zecoll * (T)K_PI * sq(mdiam);
   zgrav = zgrav * dv;
   return zbrown + zbrconv + t_sqrt(sq(zgrav) + sq(ztshear) + sq(zturb));
@@ -336,29 +359,31 @@ __device__ T coag_pair(const CoagCell<T> &cc, const BinProps<T> &a, const BinPro
 
 template <typename KT>
 __device__ __forceinline__ void load_props(const KT *S, int NB, int b, BinProps<KT> &o) {
-  o.diam = S[0 * NB + b]; o.mass = S[1 * NB + b]; o.beta = S[2 * NB + b]; o.dfpart = S[3 * NB + b];
-  o.mtvel = S[4 * NB + b]; o.omega = S[5 * NB + b]; o.termv = S[6 * NB + b]; o.reyn = S[7 * NB + b];
-  o.schm = S[8 * NB + b];
+  KT *po = &o.diam;
+#pragma unroll
+  for (int k = 0; k < 9; k++) po[k] = S[k * NB + b];
 }
 
 // Per-bin properties are evaluated in the kernel type: FP64 in the FP64 form, float in
 // the mixed form (its pair kernels are float too) except for ice bins.
 template <typename KT>
 __device__ __forceinline__ void store_props(KT *S, int NB, int b, const BinProps<double> &o) {
-  S[0 * NB + b] = (KT)o.diam; S[1 * NB + b] = (KT)o.mass; S[2 * NB + b] = (KT)o.beta; S[3 * NB + b] = (KT)o.dfpart;
-  S[4 * NB + b] = (KT)o.mtvel; S[5 * NB + b] = (KT)o.omega; S[6 * NB + b] = (KT)o.termv; S[7 * NB + b] = (KT)o.reyn;
-  S[8 * NB + b] = (KT)o.schm;
+  const double *po = &o.diam;
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k * NB + b] = (KT)po[k];
 }
 template <typename KT>
 __device__ __forceinline__ void store_props_kt(KT *S, int NB, int b, const BinProps<KT> &o) {
-  S[0 * NB + b] = o.diam; S[1 * NB + b] = o.mass; S[2 * NB + b] = o.beta; S[3 * NB + b] = o.dfpart;
-  S[4 * NB + b] = o.mtvel; S[5 * NB + b] = o.omega; S[6 * NB + b] = o.termv; S[7 * NB + b] = o.reyn;
-  S[8 * NB + b] = o.schm;
+  const KT *po = &o.diam;
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k * NB + b] = po[k];
 }
 template <typename KT>
 __device__ __forceinline__ void to_kt(const BinProps<double> &d, BinProps<KT> &o) {
-  o.diam = (KT)d.diam; o.mass = (KT)d.mass; o.beta = (KT)d.beta; o.dfpart = (KT)d.dfpart; o.mtvel = (KT)d.mtvel;
-  o.omega = (KT)d.omega; o.termv = (KT)d.termv; o.reyn = (KT)d.reyn; o.schm = (KT)d.schm;
+  const double *pd = &d.diam;
+  KT *po = &o.diam;
+#pragma unroll
+  for (int k = 0; k < 9; k++) po[k] = (KT)pd[k];
 }
 // FP64 shape coefficients of bin b: they share the memory of S rows 9-12 in the FP64
 // form and sit behind the float rows in the mixed form.
@@ -414,7 +439,7 @@ __device__ void eval_pairs(const DevParams &P, const WS<KT> &w, const CoagCell<K
 // ----------------------------------------------------------------------------------------
 // Collision kernels for all enabled bin pairs: mo_salsa_coagulation_kernels.f90:24-180
 // (buildKernelSelf/buildKernel: pairs whose partner has numc < nlim are zero).
-// Scratch: 0 diam 1 mass 2 beta 3 dfpart 4 mtvel 5 omega 6 termv 7 reyn 8 schm, then
+// Scratch: the nine BinProps rows (diam fre cschm dfpart mtvel2 omega termv reyn ire), then
 // the FP64 shape coefficients (shape_rows).
 // ----------------------------------------------------------------------------------------
 template <typename KT>
@@ -760,6 +785,9 @@ __device__ void sip_drop_numbers(const DevParams &P, const WS<KT> &w, int tg, in
     const double Nl = w.numc[g], Dl = w.dwet[g];
     const double r = (double)kget(w, tg, g) * Nl * Nt * fix;
     if (P.st_sipdf && Nl > K_PRLIM && Dl < Dt && Dt > SIP_DLLIQ_DF && Nt > tnlim) s.ndf[row * nice + ll] += r;
+    // :916-921, :936-941: Phillips' full scheme also counts drops collected by larger crystals
+    if (P.st_sipdf && P.sip_df_mode == 4 && Nl > K_PRLIM && Dl >= Dt && Dt > SIP_DLLIQ_DF && Nt > tnlim)
+      s.ndf[row * nice + ll] += r;
     if (P.st_siprs && Dl >= Dt && Dt > SIP_DLLIQ_RS && Nt > tnlim && Nl > K_PRLIM) s.nrs[row * nice + ll] += r;
   }
 }
@@ -804,6 +832,9 @@ __device__ void sip_drop_masses(const DevParams &P, const WS<KT> &w, const doubl
     const double Dl = w.dwet[g];
     const double r = (double)kget(w, c0 + ix, tg) * w.v(iwa, g) * Nt * K_RHOWA * fix;
     if (P.st_sipdf && Dt < Dl && Dl > SIP_DLLIQ_DF && Nt > K_PRLIM && w.numc[g] > lnlim) s.mdf[ix * nice + kk] += r;
+    // :1331-1343: Phillips' full scheme, drops collected by more massive crystals
+    if (P.st_sipdf && P.sip_df_mode == 4 && Dt >= Dl && Dl > SIP_DLLIQ_DF && w.numc[g] > lnlim && Nt > K_PRLIM)
+      s.mdf[ix * nice + kk] += r;
     if (P.st_siprs && Dl >= SIP_DLLIQ_RS && Dl < Dt) s.mrs[ix * nice + kk] += r;
   }
 }
@@ -985,8 +1016,65 @@ __device__ double sip_df_fragments(int mode, double T, double nf, double ddmean)
 }
 
 // mo_salsa_SIP_DF.f90:29-260 dropfracturing.  Lane 0.
+// Phillips et al. (2018) drop fracturing (mode 4, mo_salsa_SIP_DF.f90:313-608).  Fits in
+// x = log10 of the drop diameter in mm, limited to 0.06-1.6 mm (beta: 0 below 0.4 mm).
+__device__ __forceinline__ double sip_ph_cubic(double x, double c1, double c2, double c3, double c4) {
+  return (c1 * cube(x)) + (c2 * sq(x)) + (c3 * x) + c4;
+}
+// :431-451 fragments per frozen drop when the drop is heavier than the crystal (eq. 1)
+__device__ double sip_df_phillips_mode1(double d, double T) {
+  const double tc = T - 273.15, x = log10(fmax(fmin(d * 1.e3, 1.6), 0.06));
+  const double T0 = sip_ph_cubic(x, -1.3999, -5.3285, -3.9847, -15.0332);
+  const double zeta = pow(10., sip_ph_cubic(x, 2.4268, 3.3274, 2.0783, 1.2927));
+  const double eta = pow(10., sip_ph_cubic(x, 0.1242, -0.2316, -0.9874, -0.0827));
+  double beta = 0.;
+  if (!(d < 0.4e-3)) {
+    const double xb = log10(fmin(d * 1.e3, 1.6));
+    beta = (-0.1839 * sq(xb)) + (-0.2017 * xb) + -0.0512;
+  }
+  return beta * tc + (zeta * sq(eta)) / (sq(tc - T0) + sq(eta));
+}
+// :479-532 the crystal heavier than the drop (eq. 7): the collision's kinetic energy over
+// the drop's surface energy
+__device__ double sip_df_phillips_mode2(const DevParams &P, double p, double T, double d, double disph, double dinsph,
+                                        double mrim, double mpri, double ncice, double rhoip) {
+  const double rhoa = p / (K_RD * T);
+  const double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+  const double mfp = (1.656e-10 * T + 1.828e-8) * K_PSTAND / p;
+  double knud = 2. * mfp / dinsph;
+  double beta = 1. + knud * (1.142 + 0.558 * exp(-0.999 / knud));
+  Shape<double> ish;
+  shape_coeffs<double>(P, ish, mpri, mrim, ncice);
+  const double vti = terminal_vel<double>(disph, rhoip, rhoa, visc, beta, 4, ish, dinsph);
+  knud = 2. * mfp / d;
+  beta = 1. + knud * (1.142 + 0.558 * exp(-0.999 / knud));
+  const double vtd = terminal_vel<double>(d, K_RHOWA, rhoa, visc, beta, 3, ish, d);
+  const double mip = (mrim + mpri) / ncice, mdp = K_RHOWA * K_PI6 * cube(d);
+  const double K0 = 0.5 * (mip * mdp / (mdp + mip)) * sq(vtd - vti);
+  const double DE = K0 / (K_SURFW0 * K_PI * sq(d));
+  const double fT = -4200. * (T - 273.15) / 3.3e5;   // cwa, alf (mo_submctl.f90:268, 281)
+  return 3. * fmin(4. * fT, 1.) * (1. - fT) * fmax(DE - 0.2, 0.);
+}
+// :313-372 the regime by the masses of drop and crystal (ice bin g)
 template <typename KT>
-__device__ void sip_dropfracturing(const DevParams &P, const WS<KT> &w, const double *tb, double T, double dt) {
+__device__ double sip_df_phillips_full(const DevParams &P, const WS<KT> &w, double p, double T, double d, int g,
+                                       double nf) {
+  double sv = 0.;
+  for (int s = 0; s < P.nused - 1; s++) sv += w.v(s, g);
+  const double mrim = w.v(P.nused - 1, g) * K_RHORI, mpri = sv * K_RHOIC, ncice = w.numc[g];
+  const double mip = (mrim + mpri) / ncice, mdp = K_RHOWA * K_PI6 * cube(d);
+  if (mdp > mip) {
+    if (d < 50.e-6 && T > 267.15) return 0.;
+    return fmin(sip_df_phillips_mode1(d, T), 100.) * nf;
+  }
+  if (d < 150.e-6) return 0.;
+  const double rhoip = (mrim * K_RHORI + mpri * K_RHOIC) / (mrim + mpri);
+  return fmin(sip_df_phillips_mode2(P, p, T, d, w.dwet[g], w.dnsp[g], mrim, mpri, ncice, rhoip), 100.) * nf;
+}
+
+template <typename KT>
+__device__ void sip_dropfracturing(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
+                                   double dt) {
   const int nprc = P.nprc, nice = P.nice, nspec = P.nused, I0 = P.nliquid, NB = w.NB;
   const SipT t = sip_tallies(P, w.raw);
   SipScr q = sip_scratch(P, t);
@@ -1009,7 +1097,8 @@ __device__ void sip_dropfracturing(const DevParams &P, const WS<KT> &w, const do
       for (int k = 0; k < nice; k++) npmax += q.diams[k] <= ddmean;
       npmax = npmax - 1 > 1 ? npmax - 1 : 1;
       if (npmax <= 2) continue;
-      const double dN = sip_df_fragments(P.sip_df_mode, T, nf, ddmean);
+      const double dN = P.sip_df_mode == 4 ? sip_df_phillips_full<KT>(P, w, pres, T, ddmean, g, nf)
+                                           : sip_df_fragments(P.sip_df_mode, T, nf, ddmean);
       double sv;
       const double sdv = sip_spread(P, w.volc, NB, g, dN, npmax, q, sv);
       double ss = 0.;
@@ -1042,8 +1131,67 @@ __device__ double sip_iibr_imf(int mode, double T, double dmin) {
 
 // mo_salsa_SIP_IIBR.f90:23-258 iceicecollbreak: each pair (smaller bb, larger cc) breaks
 // the smaller crystal; the source bin's diameters are updated first.  Lane 0.
+// mo_salsa_SIP_IIBR.f90:588-607 mip and :552-585 getvelocity: mean crystal mass of ice
+// bin g, and its fall speed with the bin's shape coefficients and rime-weighted density
 template <typename KT>
-__device__ void sip_iceicecollbreak(const DevParams &P, const WS<KT> &w, const double *tb, double T, double dt) {
+__device__ __forceinline__ void sip_iibr_masses(const DevParams &P, const WS<KT> &w, int g, double &mrim, double &mpri) {
+  double v = 0.;
+  for (int k = 0; k <= P.iwa; k++) v += w.v(k, g);
+  mrim = w.v(P.irim, g) * K_RHORI;
+  mpri = v * K_RHOIC;
+}
+template <typename KT>
+__device__ double sip_iibr_velocity(const DevParams &P, const WS<KT> &w, int g, double visc, double rhoa, double mfp) {
+  const double knud = 2. * mfp / w.dnsp[g];
+  const double beta = 1. + knud * (1.142 + 0.558 * exp(-0.999 / knud));
+  double mrim, mpri;
+  sip_iibr_masses(P, w, g, mrim, mpri);
+  const double rhoip = (mrim * K_RHORI + mpri * K_RHOIC) / (mrim + mpri);
+  Shape<double> sh;
+  shape_coeffs<double>(P, sh, mpri, mrim, w.numc[g]);
+  return terminal_vel<double>(w.dwet[g], rhoip, rhoa, visc, beta, 4, sh, w.dnsp[g]);
+}
+// :323-401 imf_phillips_mod: Phillips et al. (2017) breakup with the corrections of
+// Sotiropoulou et al. (2020); asperity parameters by the rime fraction of bin `small`, the
+// supersaturation over ice ssi and the distance from -15 C; the collision's kinetic energy
+// from both bins' fall speeds (:505-548)
+template <typename KT>
+__device__ double sip_imf_phillips(const DevParams &P, const WS<KT> &w, double p, double T, int large, int small,
+                                   double disphmin, double ssi) {
+  const double T0 = 258.15;
+  double mrim, mpri;
+  sip_iibr_masses(P, w, small, mrim, mpri);
+  const double rimfrac = mrim / (mrim + mpri);
+  double a0, C, gg, Nmax;
+  if (rimfrac > 0.5) {
+    a0 = exp(14.74 * ssi + 14.28);
+    C = exp(20.15 * ssi + 13.78);
+    gg = ssi + 0.55;
+    Nmax = 600.;
+  } else {
+    a0 = 4.75E7;
+    C = 1.0E08;
+    gg = 0.78;
+    Nmax = 500.;
+  }
+  const double Am = a0 / 3. + fmax(2. / 3. * a0 - 1. / 9. * a0 * fabs(T - T0), 0.);
+  const double alpha = K_PI * sq(disphmin);
+  const double rhoa = p / (K_RD * T);
+  const double visc = (7.44523e-3 * sqrt(cube(T))) / (5093. * (T + 110.4));
+  const double mfp = (1.656e-10 * T + 1.828e-8) * K_PSTAND / p;
+  const double v1 = sip_iibr_velocity(P, w, large, visc, rhoa, mfp);
+  double mr1, mp1;
+  sip_iibr_masses(P, w, large, mr1, mp1);
+  const double m1 = (mr1 + mp1) / w.numc[large];
+  const double v2 = sip_iibr_velocity(P, w, small, visc, rhoa, mfp);
+  const double m2 = (mrim + mpri) / w.numc[small];
+  const double K0 = (m1 * m2 / (m1 + m2)) * (1.7 * sq(v1 - v2) + 0.3 * v1 * v2);
+  return fmin(alpha * Am * (1 - exp(-pow(C * K0 / alpha / Am, gg))), Nmax);
+}
+
+template <typename KT>
+__device__ void sip_iceicecollbreak(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
+                                    double rv, double rsi, double dt) {
   const int nice = P.nice, nspec = P.nused, I0 = P.nliquid, NB = w.NB;
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   const SipT t = sip_tallies(P, w.raw);
@@ -1071,7 +1219,14 @@ __device__ void sip_iceicecollbreak(const DevParams &P, const WS<KT> &w, const d
       for (int k = 0; k < nice; k++) npmax += q.diams[k] <= dinsphmin;
       npmax = npmax - 1;
       if (npmax <= 2) continue;
-      const double dN = sip_iibr_imf(P.sip_ib_mode, T, dinsphmin) * nii;
+      double dN;
+      if (P.sip_ib_mode == 3) {   // :148-155: bb passes as the larger crystal, as the reference writes it
+        const double disphmin = pow((mii / nii / w.rhomean[g]) / K_PI6, 1. / 3.);
+        const double ssi = fmax(0., rv / rsi - 1.0);
+        dN = fmin(sip_imf_phillips<KT>(P, w, pres, T, g, h, disphmin, ssi), 600.0) * nii;
+      } else {
+        dN = sip_iibr_imf(P.sip_ib_mode, T, dinsphmin) * nii;
+      }
       double sv;
       const double sdv = sip_spread(P, w.volc, NB, g, dN, npmax, q, sv);
       double ss = 0.;
@@ -1094,12 +1249,13 @@ __device__ void sip_iceicecollbreak(const DevParams &P, const WS<KT> &w, const d
 
 // secondary_ice (mo_salsa_secondary_ice.f90:6-40), after coagulation (mo_salsa.f90:98-99)
 template <typename KT>
-__device__ void secondary_ice(const DevParams &P, const WS<KT> &w, const double *tb, double T, double dt, int lane) {
+__device__ void secondary_ice(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres, double rv,
+                              double rsi, double dt, int lane) {
   __syncwarp();
   if (lane == 0) {
     if (P.st_siprs) sip_rimesplintering<KT>(P, w, T, dt);
-    if (P.st_sipdf) sip_dropfracturing<KT>(P, w, tb, T, dt);
-    if (P.st_sipib) sip_iceicecollbreak<KT>(P, w, tb, T, dt);
+    if (P.st_sipdf) sip_dropfracturing<KT>(P, w, tb, T, pres, dt);
+    if (P.st_sipib) sip_iceicecollbreak<KT>(P, w, tb, T, pres, rv, rsi, dt);
   }
   __syncwarp();
 }
@@ -1769,7 +1925,74 @@ __device__ __forceinline__ int eq_next_1a(const DevParams &P, const WS<KT> &w, c
 }
 
 template <typename KT>
-__device__ void equilibration(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
+__device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base);
+
+// named barrier of the two warps of a pair (64 threads): barrier 1 for warps 0-1, 2 for
+// warps 2-3 (immediate ids, so that the block reserves three barriers); barrier 0 is the
+// block's
+__device__ __forceinline__ void pair_sync(int id) {
+  if (id == 1) asm volatile("bar.sync 1, 64;" ::: "memory");
+  else asm volatile("bar.sync 2, 64;" ::: "memory");
+}
+
+// The FP64 water uptake of two cells in one warp: lanes 0-15 take the cell of workspace
+// wa, lanes 16-31 that of wb; in each half lanes 0..n2-1 run the regime-2 bins and lane
+// 15 the regime-1a chain.  The regime-1a chain is sequential (zke carries from bin to
+// bin) and sets the number of passes, so two cells per warp halve the FP64 instructions
+// of this stage.  Each lane's arithmetic is the one-cell form's (the same passes in the
+// same order), so the results are those of equilibration() alone.
+template <typename KT>
+__device__ void equilibration_pair(const DevParams &P, const WS<KT> &wa, const WS<KT> &wb, const double *tb,
+                                   double prh_a, double T_a, bool init_a, double prh_b, double T_b, bool init_b,
+                                   int lane) {
+  const double *dmid = tb + TAB_DMID * P.nb_pad;
+  const bool hi = lane >= 16;
+  const WS<KT> w = hi ? wb : wa;
+  const double prh = hi ? prh_b : prh_a, T = hi ? T_b : T_a;
+  const bool init = hi ? init_b : init_a;
+  const int sub = lane & 15;
+  const int n2 = init ? P.fn2b - P.in2a + 1 : 0;
+  const double ckt = 2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T);
+  int nonconv = 0;
+  EqJob j;
+  j.kk = -1;
+  if (sub == 15) {
+    j.r2 = false; j.tol = 1.e-2; j.zrh = fmin(fmax(prh, 0.05), 0.98); j.izke = 1. / 1.001;
+    int k = eq_next_1a(P, w, dmid, P.in1a - 1, init);
+    if (k >= 0) eq_load(P, w, k, j);
+  } else if (sub < n2) {
+    int k = P.in2a + sub;
+    if (w.numc[k] > K_NLIM) {
+      j.r2 = true; j.tol = 1.e-12; j.zrh = fmin(fmax(prh, 0.37), 0.98); j.izke = 1. / 1.02;
+      eq_load(P, w, k, j);
+    } else {
+      w.dwet[k] = dmid[k];
+    }
+  }
+  while (__any_sync(0xffffffffu, j.kk >= 0)) {
+    if (j.kk >= 0) {
+      bool go = fabs(j.zdwet - j.zdold) > j.tol * j.zdold;
+      if (go) {
+        eq_step(j, ckt);
+        if (j.count > 100) { nonconv = 1; go = false; }
+      }
+      if (!go) {
+        w.v(P.iwa, j.kk) = j.zlwc / K_RHOWA;
+        if (init) w.dwet[j.kk] = j.zdwet;
+        int k = j.r2 ? -1 : eq_next_1a(P, w, dmid, j.kk, init);
+        if (k >= 0) eq_load(P, w, k, j);
+        else j.kk = -1;
+      }
+    }
+  }
+  const unsigned nb = __ballot_sync(0xffffffffu, nonconv);
+  if (lane == 0 && (nb & 0xffffu)) wa.misc[M_FLAGS + F_EQUIL] = 1.;
+  if (lane == 16 && (nb >> 16)) wb.misc[M_FLAGS + F_EQUIL] = 1.;
+  __syncwarp();
+}
+
+template <typename KT>
+__device__ void equilibration_solo(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
                               int lane) {
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   int nonconv = 0;
@@ -1899,6 +2122,33 @@ __device__ void equilibration(const DevParams &P, const WS<KT> &w, const double 
   }
   if (warp_any(nonconv) && lane == 0) w.misc[M_FLAGS + F_EQUIL] = 1.;
   __syncwarp();
+}
+
+// The water uptake of the cell of w.  In the FP64 form the two warps of a pair meet at
+// their named barrier (every cell takes the same sequence of calls), the first runs both
+// cells (equilibration_pair) from the inputs the second left in its misc slots, and the
+// second waits at the barrier again until its cell is done.
+template <typename KT>
+__device__ void equilibration(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
+                              int lane) {
+  if (sizeof(KT) != 8 || w.role == 0 || P.fn2b - P.in2a + 1 > 15) {
+    equilibration_solo<KT>(P, w, tb, prh, T, init, lane);
+    return;
+  }
+  if (w.role == 2) {
+    if (lane == 0) {
+      w.misc[M_EQ] = prh;
+      w.misc[M_EQ + 1] = T;
+      w.misc[M_EQ + 2] = init ? 1. : 0.;
+    }
+    pair_sync(w.bar);
+    pair_sync(w.bar);
+    return;
+  }
+  pair_sync(w.bar);
+  const WS<KT> wb = make_ws<KT>(P, w.pbase);
+  equilibration_pair<KT>(P, w, wb, tb, prh, T, init, wb.misc[M_EQ], wb.misc[M_EQ + 1], wb.misc[M_EQ + 2] != 0., lane);
+  pair_sync(w.bar);
 }
 
 // ----------------------------------------------------------------------------------------
@@ -3394,7 +3644,7 @@ __device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb,
   // ---- salsa() ----
   if (P.st_coag) coagulation<KT, SIP>(P, w, tb, dt, T, pres, DIAG, cell, lane);
   if constexpr (SIP) {
-    if (P.st_secice) secondary_ice<KT>(P, w, tb, T, dt, lane);
+    if (P.st_secice) secondary_ice<KT>(P, w, tb, T, pres, rv, rsi, dt, lane);
   }
   STAGE_MARK(1);
   if (P.st_cnd) {
@@ -3531,6 +3781,9 @@ __device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
   w.scr = p; p += SALSA_NSCR * NB;
   w.nf = reinterpret_cast<float *>(w.scr);   // NB floats, then SALSA_NSV * NB floats (4 scratch rows)
   w.vf = w.nf + NB;
+  w.role = 0;
+  w.bar = 0;
+  w.pbase = nullptr;
   w.misc = p; p += SALSA_MISC_DOUBLES;
   w.pbuf = reinterpret_cast<int *>(p); p += 64;   // 128 ints: bin lists (<= 96) and pair batches (<= 63)
   w.K = reinterpret_cast<KT *>(p);
@@ -3565,6 +3818,15 @@ __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevP
       }
     __syncthreads();
     long long q = g * SALSA_CPG + warp;
+    // warps 2i and 2i+1 pair up for the FP64 water uptake when both hold a cell
+    static_assert(SALSA_CPG == 4, "the pairs' named barriers are 1 and 2");
+    {
+      const int mate = warp ^ 1;
+      const bool both = mate < SALSA_CPG && g * SALSA_CPG + (warp | 1) < P.ncells;
+      w.role = both ? ((warp & 1) ? 2 : 1) : 0;
+      w.bar = 1 + (warp >> 1);
+      w.pbase = wsbase + (size_t)mate * P.ws_doubles;
+    }
     if (q < P.ncells) cell_step<KT, DIAG, SIP>(P, w, tb, cell_at(P, q), lane);
     __syncthreads();
     // write the group's output rows
