@@ -41,10 +41,6 @@ struct WS {
   // float copies of numc and volc that the mixed form's coagulation update sums from
   // (in the scratch rows, valid from shadow_all to the end of the update)
   float *nf, *vf;
-  // warp pairing of the FP64 water uptake: 0 alone, 1 the warp that runs both cells,
-  // 2 the warp whose cell it runs; the named barrier of the pair; the partner's workspace
-  int role, bar;
-  double *pbase;
   __device__ __forceinline__ double &v(int s, int b) const { return volc[s * NB + b]; }
   __device__ __forceinline__ double *sc(int k) const { return scr + k * NB; }
   // partner values in the kernel type: the state itself (FP64 form) or its float copy
@@ -63,7 +59,6 @@ enum {
   M_DIAG = 0,              // 17 diagnostic accumulators
   M_FLAGS = 17,            // F_* per-cell condition counters
   M_RV = 24,               // water vapour mixing ratio of the cell
-  M_EQ = 25,               // a paired cell's water-uptake inputs: relative humidity, T, init flag
   M_PF = 32,               // precipitation-formation accumulators (7 + 9 * nprc, nprc <= 23)
   M_PFSLOT = M_PF + 216,   // 8 partner slots * 10
   M_GAS = M_PFSLOT + 80,   // the cell's five gases [#/m3] (gas condensation only)
@@ -1925,74 +1920,7 @@ __device__ __forceinline__ int eq_next_1a(const DevParams &P, const WS<KT> &w, c
 }
 
 template <typename KT>
-__device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base);
-
-// named barrier of the two warps of a pair (64 threads): barrier 1 for warps 0-1, 2 for
-// warps 2-3 (immediate ids, so that the block reserves three barriers); barrier 0 is the
-// block's
-__device__ __forceinline__ void pair_sync(int id) {
-  if (id == 1) asm volatile("bar.sync 1, 64;" ::: "memory");
-  else asm volatile("bar.sync 2, 64;" ::: "memory");
-}
-
-// The FP64 water uptake of two cells in one warp: lanes 0-15 take the cell of workspace
-// wa, lanes 16-31 that of wb; in each half lanes 0..n2-1 run the regime-2 bins and lane
-// 15 the regime-1a chain.  The regime-1a chain is sequential (zke carries from bin to
-// bin) and sets the number of passes, so two cells per warp halve the FP64 instructions
-// of this stage.  Each lane's arithmetic is the one-cell form's (the same passes in the
-// same order), so the results are those of equilibration() alone.
-template <typename KT>
-__device__ void equilibration_pair(const DevParams &P, const WS<KT> &wa, const WS<KT> &wb, const double *tb,
-                                   double prh_a, double T_a, bool init_a, double prh_b, double T_b, bool init_b,
-                                   int lane) {
-  const double *dmid = tb + TAB_DMID * P.nb_pad;
-  const bool hi = lane >= 16;
-  const WS<KT> w = hi ? wb : wa;
-  const double prh = hi ? prh_b : prh_a, T = hi ? T_b : T_a;
-  const bool init = hi ? init_b : init_a;
-  const int sub = lane & 15;
-  const int n2 = init ? P.fn2b - P.in2a + 1 : 0;
-  const double ckt = 2. * K_SURFW0 * K_MVWA / (K_BOLTZ * T);
-  int nonconv = 0;
-  EqJob j;
-  j.kk = -1;
-  if (sub == 15) {
-    j.r2 = false; j.tol = 1.e-2; j.zrh = fmin(fmax(prh, 0.05), 0.98); j.izke = 1. / 1.001;
-    int k = eq_next_1a(P, w, dmid, P.in1a - 1, init);
-    if (k >= 0) eq_load(P, w, k, j);
-  } else if (sub < n2) {
-    int k = P.in2a + sub;
-    if (w.numc[k] > K_NLIM) {
-      j.r2 = true; j.tol = 1.e-12; j.zrh = fmin(fmax(prh, 0.37), 0.98); j.izke = 1. / 1.02;
-      eq_load(P, w, k, j);
-    } else {
-      w.dwet[k] = dmid[k];
-    }
-  }
-  while (__any_sync(0xffffffffu, j.kk >= 0)) {
-    if (j.kk >= 0) {
-      bool go = fabs(j.zdwet - j.zdold) > j.tol * j.zdold;
-      if (go) {
-        eq_step(j, ckt);
-        if (j.count > 100) { nonconv = 1; go = false; }
-      }
-      if (!go) {
-        w.v(P.iwa, j.kk) = j.zlwc / K_RHOWA;
-        if (init) w.dwet[j.kk] = j.zdwet;
-        int k = j.r2 ? -1 : eq_next_1a(P, w, dmid, j.kk, init);
-        if (k >= 0) eq_load(P, w, k, j);
-        else j.kk = -1;
-      }
-    }
-  }
-  const unsigned nb = __ballot_sync(0xffffffffu, nonconv);
-  if (lane == 0 && (nb & 0xffffu)) wa.misc[M_FLAGS + F_EQUIL] = 1.;
-  if (lane == 16 && (nb >> 16)) wb.misc[M_FLAGS + F_EQUIL] = 1.;
-  __syncwarp();
-}
-
-template <typename KT>
-__device__ void equilibration_solo(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
+__device__ void equilibration(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
                               int lane) {
   const double *dmid = tb + TAB_DMID * P.nb_pad;
   int nonconv = 0;
@@ -2122,33 +2050,6 @@ __device__ void equilibration_solo(const DevParams &P, const WS<KT> &w, const do
   }
   if (warp_any(nonconv) && lane == 0) w.misc[M_FLAGS + F_EQUIL] = 1.;
   __syncwarp();
-}
-
-// The water uptake of the cell of w.  In the FP64 form the two warps of a pair meet at
-// their named barrier (every cell takes the same sequence of calls), the first runs both
-// cells (equilibration_pair) from the inputs the second left in its misc slots, and the
-// second waits at the barrier again until its cell is done.
-template <typename KT>
-__device__ void equilibration(const DevParams &P, const WS<KT> &w, const double *tb, double prh, double T, bool init,
-                              int lane) {
-  if (sizeof(KT) != 8 || w.role == 0 || P.fn2b - P.in2a + 1 > 15) {
-    equilibration_solo<KT>(P, w, tb, prh, T, init, lane);
-    return;
-  }
-  if (w.role == 2) {
-    if (lane == 0) {
-      w.misc[M_EQ] = prh;
-      w.misc[M_EQ + 1] = T;
-      w.misc[M_EQ + 2] = init ? 1. : 0.;
-    }
-    pair_sync(w.bar);
-    pair_sync(w.bar);
-    return;
-  }
-  pair_sync(w.bar);
-  const WS<KT> wb = make_ws<KT>(P, w.pbase);
-  equilibration_pair<KT>(P, w, wb, tb, prh, T, init, wb.misc[M_EQ], wb.misc[M_EQ + 1], wb.misc[M_EQ + 2] != 0., lane);
-  pair_sync(w.bar);
 }
 
 // ----------------------------------------------------------------------------------------
@@ -3781,9 +3682,6 @@ __device__ __forceinline__ WS<KT> make_ws(const DevParams &P, double *base) {
   w.scr = p; p += SALSA_NSCR * NB;
   w.nf = reinterpret_cast<float *>(w.scr);   // NB floats, then SALSA_NSV * NB floats (4 scratch rows)
   w.vf = w.nf + NB;
-  w.role = 0;
-  w.bar = 0;
-  w.pbase = nullptr;
   w.misc = p; p += SALSA_MISC_DOUBLES;
   w.pbuf = reinterpret_cast<int *>(p); p += 64;   // 128 ints: bin lists (<= 96) and pair batches (<= 63)
   w.K = reinterpret_cast<KT *>(p);
@@ -3818,15 +3716,6 @@ __global__ void __launch_bounds__(SALSA_THREADS, 2) salsa_step_kernel(const DevP
       }
     __syncthreads();
     long long q = g * SALSA_CPG + warp;
-    // warps 2i and 2i+1 pair up for the FP64 water uptake when both hold a cell
-    static_assert(SALSA_CPG == 4, "the pairs' named barriers are 1 and 2");
-    {
-      const int mate = warp ^ 1;
-      const bool both = mate < SALSA_CPG && g * SALSA_CPG + (warp | 1) < P.ncells;
-      w.role = both ? ((warp & 1) ? 2 : 1) : 0;
-      w.bar = 1 + (warp >> 1);
-      w.pbase = wsbase + (size_t)mate * P.ws_doubles;
-    }
     if (q < P.ncells) cell_step<KT, DIAG, SIP>(P, w, tb, cell_at(P, q), lane);
     __syncthreads();
     // write the group's output rows
