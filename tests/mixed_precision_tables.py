@@ -42,13 +42,16 @@ def sub_block(inp, X, Y, Z):
     return s
 
 
-def advance_gpu(inp, fields, steps, stream):
+def advance_gpu(inp, fields, steps):
+    """Every step: zero the tendencies, one synchronous SALSA call, add the tendencies
+    (torch's stream and the library's are ordered by the synchronisations)."""
     step = SalsaStep(inp.cfg)
     out = make_outputs(inp, with_diag=False)
     for k in range(steps):
         for v in out.values():
             v.zero_()
-        rc, st = step.run(inp, fields, out, time=float(k + 1), istp=k + 1, stream=stream)
+        torch.cuda.synchronize()
+        rc, st = step.run(inp, fields, out, time=float(k + 1), istp=k + 1)
         assert rc in (0, 4), st.as_dict()
         for t, f in PROG.items():
             if t in out:
@@ -133,12 +136,11 @@ def main():
     X, Y, Z = a.sub
     inp = make_inputs(a.workload, "cuda", precision=0, diagnostics=0)
     init = {k: v.clone() for k, v in inp.fields.items()}
-    stream = torch.cuda.Stream()
     res, secs = {}, {}
     for prec in (0, 1):
         inp.cfg.precision = prec
         t0 = time.perf_counter()
-        res[prec] = advance_gpu(inp, {k: v.clone() for k, v in init.items()}, a.steps, stream)
+        res[prec] = advance_gpu(inp, {k: v.clone() for k, v in init.items()}, a.steps)
         secs[prec] = time.perf_counter() - t0
     inp.cfg.precision = 0
     sub = sub_block(inp, X, Y, Z)

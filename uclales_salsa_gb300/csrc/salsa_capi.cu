@@ -554,7 +554,10 @@ int salsa_gb300_init(const salsa_config_t *cfg, salsa_handle_t **out) {
             cudaMalloc(&h->d_pairs, (pairs.size() + 1) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&h->d_status, salsa::ST_N * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMallocHost(&h->h_status, salsa::ST_N * sizeof(unsigned long long)) == cudaSuccess &&
-            cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            // a blocking stream: the synchronous entries then start after the work the
+            // caller queued on the legacy default stream (e.g. the copies that filled the
+            // fields), as a synchronous call should
+            cudaStreamCreate(&h->stream) == cudaSuccess &&
             cudaEventCreate(&h->ev0) == cudaSuccess && cudaEventCreate(&h->ev1) == cudaSuccess;
   if (ok)
     ok = cudaMemcpy(h->d_tables, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
