@@ -650,6 +650,13 @@ struct TAccT {
   A sink, self;
   A src[SALSA_NSV];
   A dg[7];   // 0 autoc(abs) 1 autoc80 2 autoc50 3 accr 4 accr80 5 accr50 6 coll mass
+  // src[s0] += x for a species index known only at run time, with every index of src
+  // constant after unrolling, so that the accumulator stays in registers
+  __device__ __forceinline__ void add_at(int s0, KT x) {
+#pragma unroll
+    for (int s = 0; s < SALSA_NSV; s++)
+      if (s == s0) src[s] += x;
+  }
   __device__ __forceinline__ void zero() {
     sink = (KT)0; self = (KT)0;
 #pragma unroll
@@ -1381,8 +1388,11 @@ __device__ void precip_formation(const DevParams &P, const WS<KT> &w, const doub
       } else {
         sl[0] = -1.;
         if (selfcoll) a.self += (KT)(0.5 * (double)kget(w, tg, lg) * nl);
-        else
-          for (int s = 0; s < nspec; s++) a.src[s] += (KT)(klt * w.v(s, lg));
+        else {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < nspec) a.src[s] += (KT)(klt * w.v(s, lg));
+        }
       }
       sl[8] = dnum;
     }
@@ -1452,12 +1462,20 @@ __device__ void coag_cloud(const DevParams &P, const WS<KT> &w, const double *tb
         KT cm = 0;
         for (int ll = P.in1a + lane; ll <= iaa; ll += 32) {
           const KT k = kget(w, ll, tg);
-          for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, ll);
+          {
+#pragma unroll
+            for (int s = 0; s < SALSA_NSV; s++)
+              if (s < nspec) a.src[s] += k * w.vk(s, ll);
+          }
           if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.vk(s, ll) * (KT)P.rholiq[s];
         }
         for (int ll = P.in2b + lane; ll <= iab; ll += 32) {
           const KT k = kget(w, ll, tg);
-          for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, ll);
+          {
+#pragma unroll
+            for (int s = 0; s < SALSA_NSV; s++)
+              if (s < nspec) a.src[s] += k * w.vk(s, ll);
+          }
           if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.vk(s, ll) * (KT)P.rholiq[s];
         }
         a.dg[6] += cm;
@@ -1535,7 +1553,11 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
       KT cm = 0;
       for (int ll = P.in1a + lane; ll <= P.fn2b; ll += 32) {
         const KT k = kget(w, ll, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, ll);
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < nspec) a.src[s] += k * w.vk(s, ll);
+        }
         if (diag) for (int s = 0; s < P.ndry; s++) cm += k * w.vk(s, ll) * (KT)P.rholiq[s];
       }
       a.dg[6] += cm;
@@ -1545,7 +1567,11 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
       for (int ll = lane; ll < P.ncld; ll += 32) {
         int g = C0 + ll;
         const KT k = kget(w, g, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, g);
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < nspec) a.src[s] += k * w.vk(s, g);
+        }
         if (diag) {
           const KT kw = k * w.vk(iwa, g);
           a.dg[3] += kw;
@@ -1562,7 +1588,11 @@ __device__ void coag_precp(const DevParams &P, const WS<KT> &w, const double *tb
       for (int ll = lane; ll <= kk - 1; ll += 32) {
         int g = P0 + ll;
         const KT k = kget(w, g, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += k * w.vk(s, g);
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < nspec) a.src[s] += k * w.vk(s, g);
+        }
         if (diag) {
           const KT kw = k * w.vk(iwa, g);
           double dd = cube(D) + cube(w.dwet[g]);
@@ -1647,22 +1677,34 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, 
     if (P.lscgia)
       for (int ll = P.in1a + lane; ll <= P.fn2b; ll += 32) {
         const KT k = kget(w, ll, tg);
-        for (int s = 0; s < ndry; s++) a.src[s] += k * w.vk(s, ll);
-        a.src[iwa] += k * w.vk(iwa, ll) * (KT)K_RHOWA / (KT)K_RHOIC;
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < ndry) a.src[s] += k * w.vk(s, ll);
+        }
+        a.add_at(iwa, k * w.vk(iwa, ll) * (KT)K_RHOWA / (KT)K_RHOIC);
       }
     if (P.lscgic)
       for (int ll = lane; ll < P.ncld; ll += 32) {
         int g = C0 + ll;
         const KT k = kget(w, g, tg);
-        for (int s = 0; s < ndry; s++) a.src[s] += k * w.vk(s, g);
-        a.src[irim] += k * w.vk(iwa, g) * (KT)K_RHOWA / (KT)K_RHORI;
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < ndry) a.src[s] += k * w.vk(s, g);
+        }
+        a.add_at(irim, k * w.vk(iwa, g) * (KT)K_RHOWA / (KT)K_RHORI);
       }
     if (P.lscgip)
       for (int ll = lane; ll < P.nprc; ll += 32) {
         int g = P0 + ll;
         const KT k = kget(w, g, tg);
-        for (int s = 0; s < ndry; s++) a.src[s] += k * w.vk(s, g);
-        a.src[irim] += k * w.vk(iwa, g) * (KT)K_RHOWA / (KT)K_RHORI;
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < ndry) a.src[s] += k * w.vk(s, g);
+        }
+        a.add_at(irim, k * w.vk(iwa, g) * (KT)K_RHOWA / (KT)K_RHORI);
       }
     // accumulateSourceIce (:1385-1427)
     if (P.lscgii && kk > 0)
@@ -1671,7 +1713,11 @@ __device__ void coag_ice(const DevParams &P, const WS<KT> &w, const double *tb, 
         double rf = fmax(rimefrac(P, w.numc[g], w.v(iwa, g), w.v(irim, g), 4), rf_t);
         double E = P.Eiagg_max - rf * (P.Eiagg_max - P.Eiagg_min);
         const KT k = kget(w, g, tg);
-        for (int s = 0; s < nspec; s++) a.src[s] += (KT)E * k * w.vk(s, g);
+        {
+#pragma unroll
+          for (int s = 0; s < SALSA_NSV; s++)
+            if (s < nspec) a.src[s] += (KT)E * k * w.vk(s, g);
+        }
       }
     a.reduce(false, lane);
     // applyCoagIce (:605-651): every species slot with the same semi-implicit form
@@ -2082,10 +2128,9 @@ __device__ __forceinline__ double acth2o_w(double znw, double zns) { return fmax
 // the 3 nm clusters from nucleation, only multiplies that zero.  Collision rates go to
 // scratch row 0, the non-volatile organic increments of the aerosol bins to row 1.
 // ----------------------------------------------------------------------------------------
-// Kept out of line: the step's other paths do not carry its registers.
 template <typename KT>
-__device__ __noinline__ void condgas(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
-                                     double dt, double *gas, double zxsa, int lane) {
+__device__ __forceinline__ void condgas(const DevParams &P, const WS<KT> &w, const double *tb, double T, double pres,
+                                        double dt, double *gas, double zxsa, int lane) {
   double zg[5];
   for (int i = 0; i < 5; i++) zg[i] = gas[i];
   const double *dmid = tb + TAB_DMID * P.nb_pad;
@@ -2435,10 +2480,9 @@ __device__ __forceinline__ double intgV(double k, double c, double lo, double hi
 // activated-droplet outputs (raw rows, per kg of air).  One lane per aerosol bin, then
 // one lane per cloud bin; sums run in bin order on every lane.
 // ----------------------------------------------------------------------------------------
-// Kept out of line: the step's other paths do not carry its registers.
 template <typename KT>
-__device__ __noinline__ void act_cloudbase(const DevParams &P, const WS<KT> &w, const double *tb, double pres,
-                                           double T, double wvel, double dn, double *raw, int lane) {
+__device__ __forceinline__ void act_cloudbase(const DevParams &P, const WS<KT> &w, const double *tb, double pres,
+                                              double T, double wvel, double dn, double *raw, int lane) {
   const int in1a = P.in1a, fn2a = P.fn2a, in2b = P.in2b, fn2b = P.fn2b, ndry = P.ndry, nwet = P.nwet;
   const int iwa = P.iwa, ncld = P.ncld;
   const double *dmid = tb + TAB_DMID * P.nb_pad, *vlo = tb + TAB_VLO * P.nb_pad, *vhi = tb + TAB_VHI * P.nb_pad;
@@ -3477,6 +3521,9 @@ __device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *
 // One cell: the body of the run_SALSA cell loop (mo_salsa_driver.f90:185-419) around
 // salsa() (mo_salsa.f90:89-149).  Every cell starts from the post-initialisation module
 // state (bin templates), i.e. each cell sees allSALSA as the reference's first cell does.
+// Inlined into the kernel with everything it calls: a call would pass the workspace
+// descriptor by reference through the stack, and the callee would reload its pointers
+// from local memory (the mixed form ran 10-14 % slower that way).
 // ----------------------------------------------------------------------------------------
 #ifdef SALSA_STAGE_TIMERS
 #define STAGE_MARK(k)                                                              \
@@ -3490,7 +3537,8 @@ __device__ void distr_update(const DevParams &P, const WS<KT> &w, const double *
 #endif
 
 template <typename KT, bool DIAG, bool SIP>
-__device__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, long long cell, int lane) {
+__device__ __forceinline__ void cell_step(const DevParams &P, const WS<KT> &w, const double *tb, long long cell,
+                                          int lane) {
 #ifdef SALSA_STAGE_TIMERS
   long long t_stage = clock64();
 #endif

@@ -217,7 +217,9 @@ __device__ __forceinline__ void clamp_neg(double *a, long long p, long long pl, 
 }
 
 // ---- SALSA_diagnostics (:52-370) ----
-__global__ void __launch_bounds__(128) diagnostics_kernel(const PostArgs A) {
+// at most 64 registers (8 blocks of 128 threads per SM): a point's passes over its bins
+// are dependent loads, so the kernel is bound by latency and gains from warps in flight
+__global__ void __launch_bounds__(128, 8) diagnostics_kernel(const PostArgs A) {
   const long long pl = A.plane;
   const salsa_post_fields_t &f = A.f;
   double *na = f.naero, *nc = f.ncloud, *np = f.nprecp, *ni = f.nice;
