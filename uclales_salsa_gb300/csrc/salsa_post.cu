@@ -43,6 +43,7 @@ struct ClampArgs {
   long long n[9];
   double dtlt;
   double rdt;           // 1 / dtlt when dtlt is a power of two (the quotient is then a product), else 0
+  int pow2;             // dtlt is a power of two
   int be_dt;            // biased exponent of dtlt
   unsigned long long cm;   // significand of |-1 + 1e-8| with its leading bit
   int ce;                  // biased exponent of |-1 + 1e-8|
@@ -81,33 +82,33 @@ __device__ __forceinline__ long long mag_lo_bits(long long bp, unsigned long lon
   return ((long long)e << 52) | (long long)(m & 0x000fffffffffffffULL);
 }
 
-// t = MAX((-1 + 1e-8) * p / dtlt, t).  For p = +-0 the limit is the zero of the other
-// sign (a finite positive dtlt).  The limit is < 0 for a normal p > 0, so a tendency with
-// its sign bit clear never moves; for t < 0 the exponents settle |t| < |lo| whenever
-// |t| dtlt < p / 4.  The rest form lo: with a power-of-two dtlt from the integer product
-// (mag_lo_bits) and compare magnitudes as integers (both negative), otherwise in FP64.
-__device__ __forceinline__ void clamp_tendency(double p, double t, double *tp, double dtlt, double rdt, int be_dt,
-                                               unsigned long long cm, int ce) {
-  const long long bp = bits_of(p), bt = bits_of(t);
+// t = MAX((-1 + 1e-8) * p / dtlt, t), from the bit patterns bp, bt of p and t (the
+// values are loaded as integers, so no FP64 compare is formed for the decisions taken on
+// bits).  For p = +-0 the limit is the zero of the other sign (a finite positive dtlt).
+// The limit is < 0 for a normal p > 0, so a tendency with its sign bit clear never moves;
+// for t < 0 the exponents settle |t| < |lo| whenever |t| dtlt < p / 4.  The rest form lo:
+// with a power-of-two dtlt from the integer product (mag_lo_bits) and compare magnitudes
+// as integers (both negative), otherwise in FP64.
+__device__ __forceinline__ void clamp_tendency(long long bp, long long bt, long long *tp, const ClampArgs &A) {
   if ((bp & ABS_MASK) == 0) {          // p = +-0: lo is the zero of the other sign
-    if (neg_bits(bt)) *tp = bp == 0 ? -0. : 0.;
+    if (neg_bits(bt)) *tp = bp == 0 ? (long long)0x8000000000000000ULL : 0LL;
     return;
   }
   if (bp >= 0 && bexp(bp) != 0 && bexp(bp) != 0x7ff) {
     if (bt >= 0) return;
-    if (bexp(bt) + be_dt + 3 - 1023 <= bexp(bp)) return;
-    if (rdt != 0. && (bt & ABS_MASK) <= INF_BITS) {
-      const long long ml = mag_lo_bits(bp, cm, ce, 1023 - be_dt);
+    if (bexp(bt) + A.be_dt + 3 - 1023 <= bexp(bp)) return;
+    if (A.pow2 && (bt & ABS_MASK) <= INF_BITS) {
+      const long long ml = mag_lo_bits(bp, A.cm, A.ce, 1023 - A.be_dt);
       if (ml >= 0) {
         // lo = -|lo| > t  <=>  |lo| < |t| (t < 0, not NaN)
-        if (ml < (bt & ABS_MASK)) *tp = __longlong_as_double(ml | (long long)0x8000000000000000ULL);
+        if (ml < (bt & ABS_MASK)) *tp = ml | (long long)0x8000000000000000ULL;
         return;
       }
     }
   }
-  const double q = (-1. + 1.e-8) * p;
-  const double lo = rdt != 0. ? q * rdt : q / dtlt;   // the same rounding of the same quotient
-  if (lo > t) *tp = lo;
+  const double q = (-1. + 1.e-8) * __longlong_as_double(bp);
+  const double lo = A.pow2 ? q * A.rdt : q / A.dtlt;   // the same rounding of the same quotient
+  if (lo > __longlong_as_double(bt)) *tp = __double_as_longlong(lo);
 }
 
 __global__ void __launch_bounds__(256) tend_constrain_kernel(const ClampArgs A) {
@@ -115,22 +116,22 @@ __global__ void __launch_bounds__(256) tend_constrain_kernel(const ClampArgs A) 
   const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int B = 4;   // elements per thread and pass, loaded before any store
   for (int a = 0; a < 9; a++) {
-    const double *__restrict__ p = A.p[a];
-    double *__restrict__ t = A.t[a];
+    const long long *__restrict__ p = reinterpret_cast<const long long *>(A.p[a]);
+    long long *__restrict__ t = reinterpret_cast<long long *>(A.t[a]);
     if (!p || !t) continue;
     const long long n = A.n[a];
     for (long long e0 = i0; e0 < n; e0 += B * stride) {
-      double vp[B], vt[B];
+      long long vp[B], vt[B];
 #pragma unroll
       for (int u = 0; u < B; u++) {
         const long long e = e0 + u * stride;
-        vp[u] = e < n ? __ldg(p + e) : 0.;
-        vt[u] = e < n ? t[e] : 0.;
+        vp[u] = e < n ? __ldg(p + e) : 0LL;
+        vt[u] = e < n ? t[e] : 0LL;
       }
 #pragma unroll
       for (int u = 0; u < B; u++) {
         const long long e = e0 + u * stride;
-        if (e < n) clamp_tendency(vp[u], vt[u], t + e, A.dtlt, A.rdt, A.be_dt, A.cm, A.ce);
+        if (e < n) clamp_tendency(vp[u], vt[u], t + e, A);
       }
     }
   }
@@ -138,10 +139,11 @@ __global__ void __launch_bounds__(256) tend_constrain_kernel(const ClampArgs A) 
   // become 0, v > 1 becomes 1; -0 and values inside stay as they are
   if (A.indef) {
     const long long ONE = 0x3ff0000000000000LL;
+    long long *in = reinterpret_cast<long long *>(A.indef);
     for (long long e = i0; e < A.nindef; e += stride) {
-      const long long b = bits_of(A.indef[e]), m = b & ABS_MASK;
-      if (m > INF_BITS || neg_bits(b)) A.indef[e] = 0.;
-      else if (b > ONE) A.indef[e] = 1.;
+      const long long b = in[e], m = b & ABS_MASK;
+      if (m > INF_BITS || neg_bits(b)) in[e] = 0LL;
+      else if (b > ONE) in[e] = ONE;
     }
   }
 }
@@ -432,6 +434,7 @@ int salsa_gb300_tend_constrain(salsa_handle_t *h, int nzp, int nxp, int nyp, dou
   // a normal power of two with a normal reciprocal: mantissa zero
   const bool pow2 = (bdt & 0x000fffffffffffffLL) == 0 && A.be_dt > 1 && A.be_dt < 2045;
   A.rdt = pow2 ? 1. / dtlt : 0.;
+  A.pow2 = pow2 ? 1 : 0;
   {
     const double c = -1. + 1.e-8;   // the factor of the limit, as tend_constrain2 writes it
     const double cabs = -c;
