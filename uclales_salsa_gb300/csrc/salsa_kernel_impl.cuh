@@ -16,9 +16,8 @@
 //     lane-parallel and reduced with warp shuffles.
 //   * KT is the arithmetic type of the collision kernels and of the condensation
 //     mass-transfer coefficients: double for the parity form, float for the mixed
-//     form (the partner sums accumulate the float kernel values in double, which is
-//     tighter than compensated float sums; denominators, the water budget and all
-//     state updates stay double).
+//     form (whose partner sums are compensated float sums; denominators, the water
+//     budget and all state updates stay double).
 //   * a pre-pass orders the cells so that the cells of one block share a class
 //     (all-clear or cloudy); a block's cells are then not always neighbours.
 #pragma once
