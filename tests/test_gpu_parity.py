@@ -37,6 +37,8 @@ LIBM_MODES = (1, -1, 2, 3, 4, 5)
 CASES = [("grid16x16x40", {}), ("grid256x256x128", dict(X=8, Y=8, Z=16)), ("grid384x384x160", dict(X=16, Y=16, Z=12))]
 # 131,072-cell blocks of the two large workloads
 LARGE = [("grid256x256x128", dict(X=64, Y=64, Z=32)), ("grid384x384x160", dict(X=64, Y=64, Z=32))]
+# a cell count that is not a multiple of the cells one block stages, and a single cell
+RAGGED = [("grid256x256x128", dict(X=5, Y=3, Z=7)), ("grid384x384x160", dict(X=1, Y=1, Z=1))]
 
 
 def oracle_run(inp, fields=None, scale=None, pert_eps=0.0, pert_field=None, libm=0, variant="plain"):
@@ -144,6 +146,21 @@ def test_fp64_parity_large_block(name, kw):
         print(f"{name} {k:8s} max rel {r['max_rel']:.3e}  within 1e-10 {100 * r['frac_within']:.4f} %  "
               f"beyond the bound {r['violations']} of {r['n']}")
     assert_fp64(rep)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name,kw", RAGGED)
+def test_ragged_and_single_cell_blocks(name, kw, precision):
+    """105 interior cells (the last block stages a partial group) and a single cell:
+    every bin value within the bound of its form."""
+    inp = make_inputs(name, "cpu", precision=precision, **kw)
+    _, ref = oracle_run(inp)
+    _, gpu = gpu_run(inp)
+    eps, rtol = (2.2e-16, 1e-10) if precision == 0 else (1e-7, 1e-6)
+    rep = check(inp, gpu, ref, envelope(inp, ref, eps), rtol)
+    print(name, precision, rep)
+    for k, r in rep.items():
+        assert r["violations"] == 0, (k, r)
 
 
 @pytest.mark.parametrize("name,kw", CASES)
