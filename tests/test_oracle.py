@@ -7,7 +7,7 @@ import pytest
 import torch
 
 from uclales_salsa_gb300.inputs import make_inputs, make_outputs
-from uclales_salsa_gb300.layout import build_layout, lolim_diameters, PI6
+from uclales_salsa_gb300.layout import build_layout, lolim_diameters, PI6, ALLRHO as ALL_RHO
 from uclales_salsa_gb300.config import workload_config
 from oracle_ref import Oracle, lib
 from parity import state_errors, interior
@@ -87,11 +87,47 @@ def test_terminal_velocity_stokes_regime():
     visc, rhoa = 1.8e-5, 1.2
     for d in (1e-7, 1e-6, 1e-5):
         v = lib().salsa_ref_terminal_vel(d, 1000., rhoa, visc, 1.1, 2)
-        assert v == pytest.approx(d * d * (1000. - rhoa) * 9.81 * 1.1 / (18. * visc), rel=1e-14)
+        assert v == pytest.approx(d * d * (1000. - rhoa) * 9.81 * 1.1 / (18. * visc), rel=1e-14, abs=0.)
     # Beard and raindrop regimes increase monotonically across the 19 um and 1.07 mm limits
     vs = [lib().salsa_ref_terminal_vel(d, 1000., rhoa, visc, 1.0, 3) for d in (15e-6, 25e-6, 1e-4, 1e-3, 2e-3)]
     assert all(b > a for a, b in zip(vs, vs[1:]))
     assert vs[-1] <= 9.2
+
+
+def terminal_vel_numpy(d, rhop, rhoa, visc, beta):
+    """Independent restatement of the liquid regimes of terminal_vel
+    (src/src_shared/mo_particle_external_properties.f90:43-100): Stokes with the
+    Cunningham factor below 19 um, Beard's Davies-number fit up to 1.07 mm, the Bond-number
+    fit above, capped at 9.2 m/s."""
+    grav, surfw0 = 9.81, 0.073
+    if d <= 19e-6:
+        return d ** 2 * (rhop - rhoa) * grav * beta / (18. * visc)
+    if d < 1.07e-3:
+        nda = 4. / 3. * d ** 3. * grav * (rhop - rhoa) * rhoa / visc ** 2.
+        x = math.log(nda)
+        y = (-0.318657e1 + 0.992696 * x - 0.153193e-2 * x ** 2 - 0.987059e-3 * x ** 3
+             - 0.578878e-3 * x ** 4 + 0.855176e-4 * x ** 5 - 0.327815e-5 * x ** 6)
+        return visc / rhoa / d * (beta * math.exp(y))
+    npn = surfw0 ** 3. * rhoa ** 2. / (visc ** 4. * (rhop - rhoa) * grav)
+    bo = 4. / 3. * (rhop - rhoa) * grav / surfw0 * d ** 2.
+    x3 = math.log(bo * npn ** (1. / 6.))
+    y3 = (-0.500015e1 + 0.523778e1 * x3 - 0.204914e1 * x3 ** 2 + 0.475294 * x3 ** 3
+          - 0.542819e-1 * x3 ** 4 + 0.238449e-2 * x3 ** 5)
+    return min(visc / rhoa / d * (npn ** (1. / 6.) * math.exp(y3)), 9.2)
+
+
+def test_terminal_velocity_matches_independent_restatement():
+    """Every liquid regime of the oracle's terminal_vel against the restatement above,
+    across the 19 um and 1.07 mm limits and the 9.2 m/s cap, for cloud and precipitation
+    flags and a range of air states."""
+    rng = np.random.default_rng(7)
+    diams = np.concatenate([np.geomspace(2e-7, 6e-3, 400), [19e-6, 19.0001e-6, 1.07e-3, 1.0699e-3, 1.0701e-3]])
+    for d in diams:
+        rhoa, visc = rng.uniform(0.4, 1.3), rng.uniform(1.5e-5, 1.9e-5)
+        beta = 1. + rng.uniform(0., 0.3)
+        for flag in (2, 3):
+            v = lib().salsa_ref_terminal_vel(float(d), 1000., rhoa, visc, beta, flag)
+            assert v == pytest.approx(terminal_vel_numpy(float(d), 1000., rhoa, visc, beta), rel=1e-13, abs=0.)
 
 
 def coagc_numpy(d1, m1, rho1, d2, m2, rho2, T, P, eddy=0.001):
@@ -140,7 +176,91 @@ def test_coagc_matches_independent_restatement():
         if lay.phase[b2] == 3 and d2 > 19e-6:
             continue
         kn = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
-        assert k == pytest.approx(kn, rel=1e-12), (b1, b2)
+        assert k == pytest.approx(kn, rel=1e-12, abs=0.), (b1, b2)
+
+
+def equilibration_numpy(numc, zvolc, dmid, T, prh, in1a, fn1a, in2a, fn2b, nlim=1.):
+    """Independent restatement of the initialisation call of equilibration
+    (src/src_salsa/mo_salsa_properties.f90:73-380) for one cell: the aerosol water
+    content [kg/m3] of every bin, regime 1a (SO4 and OC, Kelvin factor carried from bin
+    to bin, tolerance 1e-2) and regime 2 (SO4, OC, BC, DU, SS, tolerance 1e-12), each
+    iteration starting from the bin's mid diameter.  zvolc[b] = volumes of SO4, OC, BC,
+    DU, SS [m3/m3]."""
+    pi6, boltz, surfw0, epsoc = 0.5235988, 1.3807e-23, 0.073, 0.15
+    mwa, rhowa, avog = 18.016e-3, 1000., 6.0221e+23
+    mvwa = mwa / avog / rhowa
+    rhosu, msu, rhooc, moc, rhoss, mss = 1830., 98.08e-3, 1400., 150.e-3, 2165., 58.44e-3
+    out = {}
+
+    def bm_su(aw):
+        return 1.1065495e+2 - 3.6759197e+2 * aw + 5.0462934e+2 * aw ** 2 - 3.1543839e+2 * aw ** 3 + 6.770824e+1 * aw ** 4
+
+    def bm_oc(aw):
+        return 1. / (aw * mwa) - 1. / mwa
+
+    def bm_ss(aw):
+        return 5.875248e+1 - 1.8781997e+2 * aw + 2.7211377e+2 * aw ** 2 - 1.8458287e+2 * aw ** 3 + 4.153689e+1 * aw ** 4
+
+    zke = 1.001
+    for kk in range(in1a, fn1a + 1):
+        if numc[kk] > nlim:
+            v = zvolc[kk]
+            zcore = v[0] / numc[kk] + v[1] / numc[kk]
+            zrh = min(max(prh, 0.05), 0.98)
+            zdwet, zdold, lwc = dmid[kk], 1., 0.
+            while abs(zdwet / zdold - 1.) > 1.e-2:
+                zdold = max(zdwet, 1.e-20)
+                aw = zrh / zke
+                lwc = v[0] * (rhosu / msu) / bm_su(aw) + epsoc * v[1] * (rhooc / moc) / bm_oc(aw)
+                zdwet = (lwc / numc[kk] / rhowa / pi6 + zcore / pi6) ** (1. / 3.)
+                zke = math.exp(2. * surfw0 * mvwa / (boltz * T * zdwet))
+            out[kk] = lwc
+    for kk in range(in2a, fn2b + 1):
+        if numc[kk] > nlim:
+            v = zvolc[kk]
+            zcore = sum(x / numc[kk] for x in v[:5])
+            zrh = min(max(prh, 0.37), 0.98)
+            zke, zdwet, zdold, lwc = 1.02, dmid[kk], 1., 0.
+            while abs(zdwet / zdold - 1.) > 1.e-12:
+                zdold = max(zdwet, 1.e-20)
+                aw = zrh / zke
+                lwc = (v[0] * (rhosu / msu) / bm_su(aw) + epsoc * (v[1] * (rhooc / moc)) / bm_oc(aw)
+                       + v[4] * (rhoss / mss) / bm_ss(aw))
+                zdwet = (lwc / numc[kk] / rhowa / pi6 + zcore / pi6) ** (1. / 3.)
+                zke = math.exp(2. * surfw0 * mvwa / (boltz * T * zdwet))
+            out[kk] = lwc
+    return out
+
+
+def test_initial_water_uptake_matches_independent_restatement():
+    """With every process off, an initialising call leaves the aerosol water of the
+    equilibration's initialisation call (relative humidity 0.3); the oracle's water of
+    every populated bin of every cell matches the restatement above."""
+    inp = make_inputs("grid16x16x40", "cpu", X=4, Y=4, Z=4)
+    only()(inp.cfg)
+    lay, dt = inp.layout, inp.dt
+    f = {k: v.clone() for k, v in inp.fields.items()}
+    out = make_outputs(inp)
+    rc, st = Oracle(inp.cfg).run(inp, f, out, time=1.0, initialize=1)
+    assert rc == 0
+    nzp, nxp, nyp = inp.nzp, inp.nxp, inp.nyp
+    I = lambda t: interior(t, nzp, nxp, nyp)
+    nb, iw = lay.nbins, lay.nwet - 1
+    dn, T = I(inp.fields["dn"]), I(inp.fields["temp"])
+    na, ma, mt = I(inp.fields["naero"]), I(inp.fields["maero"]), I(out["maerot"])
+    rho = [ALL_RHO[s] for s in lay.species]
+    checked = 0
+    for c in range(dn.numel()):
+        d = float(dn.flatten()[c])
+        numc = [float(na[b].flatten()[c]) * d for b in range(nb)]
+        zvolc = [[float(ma[s * nb + b].flatten()[c]) * d / rho[s] for s in range(5)] for b in range(nb)]
+        ref = equilibration_numpy(numc, zvolc, lay.dmid, float(T.flatten()[c]), 0.3,
+                                  lay.in1a, lay.fn1a, lay.in2a, lay.fn2b)
+        for b, lwc in ref.items():
+            w = float(ma[iw * nb + b].flatten()[c] + mt[iw * nb + b].flatten()[c] * dt)
+            assert w == pytest.approx(lwc / d, rel=1e-10, abs=0.), (c, b)
+            checked += 1
+    assert checked > 100
 
 
 def test_condensation_conserves_water():
@@ -416,7 +536,7 @@ def test_two_bin_coagulation_matches_the_closed_form():
     # the changes themselves agree to 1e-10
     for got, want, old in ((float(new_n[a]), na1, na), (float(new_v[a]), va1, va), (float(new_n[b]), nb1, nb_),
                            (float(new_v[b]), vb1, vb)):
-        assert got - old == pytest.approx(want - old, rel=1e-10)
+        assert got - old == pytest.approx(want - old, rel=1e-10, abs=0.)
     assert na1 < 0.9 * na and vb1 - vb > 1e-5 * vb               # the update takes a good share
     others = [k for k in range(lay.nbins) if k not in (a, b)]
     assert float(new_n[others].abs().max()) == 0
