@@ -2048,6 +2048,16 @@ static double J_hf(const salsa_ref_ctx_t *c, double Tk, double Sw) {
          exp(-(crit_energy + act_energy) / (BOLTZ * Tk));
 }
 
+/* single-function probe of the nucleation rates for the closed-form tests: kind 1 J_imm,
+   2 J_dep (theta, Tk, Din, S), 3 J_hf (Tk, S) */
+double salsa_ref_nucleation_rate(const salsa_ref_ctx_t *c, int kind, double theta, double Tk, double Din,
+                                 double S) {
+  if (kind == 1) return J_imm(c, theta, Tk, Din, S);
+  if (kind == 2) return J_dep(c, theta, Tk, Din, S);
+  if (kind == 3) return J_hf(c, Tk, S);
+  return 0.;
+}
+
 static const double GL_X[10] = {-0.973908239224106, -0.865060566454542, -0.679410688379483, -0.433395397408358,
                                 -0.148874339007507, 0.148874339007507,  0.433395397408358,  0.679410688379483,
                                 0.865060566454542,  0.973908239224106};

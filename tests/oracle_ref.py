@@ -39,6 +39,8 @@ def lib(variant="plain"):
         L.salsa_ref_states.argtypes = [C.c_void_p, C.POINTER(C.c_int * 12)]
         L.salsa_ref_terminal_vel.argtypes = [C.c_double] * 5 + [C.c_int]
         L.salsa_ref_terminal_vel.restype = C.c_double
+        L.salsa_ref_nucleation_rate.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 4
+        L.salsa_ref_nucleation_rate.restype = C.c_double
         L.salsa_ref_coagc_pair.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 6
         L.salsa_ref_coagc_pair.restype = C.c_double
         L.salsa_ref_tend_constrain.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,

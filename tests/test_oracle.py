@@ -263,6 +263,87 @@ def test_initial_water_uptake_matches_independent_restatement():
     assert checked > 100
 
 
+def het_sf_numpy(x, mis):
+    """mo_salsa_cloud_ice_SE.f90:375-390 het_sf, restated.  Integer powers are products,
+    as the Fortran compiles them: the large-x form cancels, so their rounding shows."""
+    sq, cube = (lambda v: v * v), (lambda v: v * v * v)
+    if x > 100.:
+        return (cube(mis) - 3 * mis + 2) / 4
+    fii = math.sqrt(1. - 2. * mis * x + sq(x))
+    fpsi = (x - mis) / fii
+    return 0.5 * (1. + cube((1. - mis * x) / fii) + (2. - 3. * fpsi + cube(fpsi)) * cube(x) + 3. * mis * (fpsi - 1.) * sq(x))
+
+
+def nucleation_rate_numpy(kind, theta, tk, din, s):
+    """Independent restatement of J_imm (kind 1), J_dep (2) and J_hf (3) of
+    mo_salsa_cloud_ice_SE.f90:210-371 with the constants of mo_submctl.f90 and
+    classSpecies.f90 (water 18.016e-3 kg/mol, ice 917 kg/m3)."""
+    rg, avog, boltz, planck, pi = 8.314, 6.0221e+23, 1.3807e-23, 6.626070040e-34, 3.1415927
+    mwa, rhoic, rhowa, t0 = 18.016e-3, 917., 1000., 273.15
+    tc = tk - t0
+    if kind == 1:
+        if din < 1e-10:
+            return 0.
+        act = rg * tk * (347. / (tk - 177.) - math.log(4.14 / 349.)) / avog
+        sig = 28.e-3 + 0.25e-3 * tc
+        lefm = (79.7 + 0.708 * tc - 2.5e-3 * (tc * tc)) * 4.1868e3
+        gg = rg * tk / mwa / lefm
+        if (t0 / tk) * s ** gg < 1.0001:
+            return 0.
+        dg = 4. * sig / (900. * lefm * math.log((t0 / tk) * s ** gg))
+        if dg <= 1e-10:
+            return 0.
+        cth = math.cos(theta * pi / 180.)
+        crit = (pi / 3.) * sig * (dg * dg) * het_sf_numpy(din / dg, cth)
+        return (boltz * tk / planck) * 1.e19 * pi * (din * din) * math.exp(-(act + crit) / (boltz * tk))
+    if kind == 2:
+        if din < 1e-10 or s < 1.0001:
+            return 0.
+        sig = ((76.1 - 0.155 * tc) + (28.5 + 0.25 * tc)) * 1.e-3
+        dg = 4. * sig / (rg * rhoic / mwa * tk * math.log(s))
+        if dg <= 1e-10:
+            return 0.
+        cth = math.cos(theta * pi / 180.)
+        crit = (pi / 3.) * sig * (dg * dg) * het_sf_numpy(din / dg, cth)
+        return 0.25 * 1.e30 * (din * din) * math.exp(-crit / (boltz * tk))
+    act = 0.694e-19 * (1. + 0.027 * (tc + 30.))
+    lefm = (79.7 + 0.708 * tc - 2.5e-3 * (tc * tc)) * 4.1868e3
+    gg = rg * tk / lefm / mwa
+    if (t0 / tk) * s ** gg < 1.0001:
+        return 0.
+    sig = 28.e-3 + 0.25e-3 * tc
+    dg = 4. * sig / (rhoic * lefm * math.log((t0 / tk) * s ** gg))
+    if dg <= 1e-10:
+        return 0.
+    crit = (pi / 3.) * sig * (dg * dg)
+    return (2.0 * 5.85e16 * (rhowa * boltz * tk / rhoic / planck) * math.sqrt(sig / boltz / tk)
+            * math.exp(-(crit + act) / (boltz * tk)))
+
+
+def test_nucleation_rates_match_independent_restatement():
+    """The oracle's immersion, deposition and homogeneous freezing rates (probe
+    salsa_ref_nucleation_rate) against the restatement above over contact angles, sizes,
+    temperatures and saturation ratios: non-zero rates to 1e-9 relative (the exponent
+    reaches a few hundred, which scales its rounding), zero rates together."""
+    cfg = workload_config(5)
+    o = Oracle(cfg)
+    rng = np.random.default_rng(11)
+    nonzero = 0
+    for _ in range(4000):
+        kind = int(rng.integers(1, 4))
+        theta, tk = rng.uniform(5., 180.), rng.uniform(200., 272.)
+        din = 10 ** rng.uniform(-9., -5.)
+        s = rng.uniform(0.9, 1.6)
+        got = lib().salsa_ref_nucleation_rate(o.h, kind, theta, tk, din, s)
+        want = nucleation_rate_numpy(kind, theta, tk, din, s)
+        if want == 0. or got == 0.:
+            assert got == want, (kind, theta, tk, din, s, got, want)
+        else:
+            nonzero += 1
+            assert got == pytest.approx(want, rel=1e-9, abs=0.), (kind, theta, tk, din, s)
+    assert nonzero > 500
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
