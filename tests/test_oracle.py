@@ -623,6 +623,68 @@ def test_two_bin_coagulation_matches_the_closed_form():
     assert float(new_n[others].abs().max()) == 0
 
 
+def test_ice_collecting_aerosol_matches_the_closed_form_and_creates_mass():
+    """The reference's coagulation visits ice first (mo_salsa_dynamics.f90:92-202): with
+    only ice-aerosol collection on, the ice bin gains dt K N_i V_a (accumulateSourcePhase
+    Change + applyCoagIce, mo_salsa_coagulation_processes.f90:476-535, 605-651, 1244-1280)
+    from the aerosol volume before the aerosol update, which then loses
+    V_a x / (1 + x), x = dt K N_i (applyCoag :539-559).  The oracle follows both formulas,
+    and the pair gains V_a x^2 / (1 + x) of mass: the reference's scheme is not
+    conservative when x is not small, which the species totals of long runs show."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgcc", "lscgca", "lscgpc", "lscgpa", "lscgpp", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    cfg.lscgia = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=1, Y=1, Z=1)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    a, i = lay.in2b + 4, lay.nice - 1                 # a coarse aerosol bin, the largest ice bin
+    gi = lay.nbins + lay.ncld + lay.nprc + i
+    T, P, dt = 255.0, 80.0e3, inp.dt
+    da, di = lay.dmid[a], lay.dmid[gi]
+    na = 1.e11
+    h = Oracle(cfg).h
+    k = lib().salsa_ref_coagc_pair(h, a, gi, na, da, 1.e6, di, T, P)
+    ni = 0.8 / (dt * k)                               # x = 0.8
+    k = lib().salsa_ref_coagc_pair(h, a, gi, na, da, ni, di, T, P)
+    x = dt * k * ni
+    f = inp.fields
+    f["temp"][..., 1] = T
+    f["press"][..., 1] = P
+    dn = float(f["dn"][2, 2, 1])
+    nw, iw = lay.nwet, lay.nwet - 1
+    for key in ("naero", "maero", "ncloud", "mcloud", "nprecp", "mprecp", "nice", "mice"):
+        f[key].zero_()
+    rhow, rhoi = 1000., 917.
+    f["naero"][a, 2, 2, 1] = na / dn
+    f["maero"].view(nw, lay.nbins, *f["naero"].shape[1:])[iw, a, 2, 2, 1] = na * PI6 * da ** 3 * rhow / dn
+    f["nice"][i, 2, 2, 1] = ni / dn
+    f["mice"].view(nw + 1, lay.nice, *f["naero"].shape[1:])[iw, i, 2, 2, 1] = ni * PI6 * di ** 3 * rhoi / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0, nthreads=1)
+    assert rc == 0
+    va, vi = na * PI6 * da ** 3, ni * PI6 * di ** 3
+    va1 = va / (1. + x)
+    vi1 = vi + x * va * rhow / rhoi
+    sh = f["naero"].shape[1:]
+    # the changes, from the tendencies (the ice bin holds far more volume than it gains)
+    dva = float(out["maerot"].view(nw, lay.nbins, *sh)[iw, a, 2, 2, 1]) * dt * dn / rhow
+    dvi = float(out["micet"].view(nw + 1, lay.nice, *sh)[iw, i, 2, 2, 1]) * dt * dn / rhoi
+    dna = float(out["naerot"][a, 2, 2, 1]) * dt * dn
+    dni = float(out["nicet"][i, 2, 2, 1]) * dt * dn
+    assert dva == pytest.approx(va1 - va, rel=1e-10, abs=0.)
+    assert dvi == pytest.approx(vi1 - vi, rel=1e-10, abs=0.)
+    assert dna == pytest.approx(na / (1. + x) - na, rel=1e-10, abs=0.)
+    assert dni == 0.
+    gained = dva * rhow + dvi * rhoi
+    assert gained == pytest.approx(rhow * va * x * x / (1. + x), rel=1e-9, abs=0.)
+    assert gained > 0.3 * rhow * va
+
+
 def test_switch_delays_are_sticky_and_follow_the_reference_comparisons():
     """set_SALSA_runtime (mo_salsa_driver.f90:453-466): a master switch takes effect once
     time >= delay and then stays on, also for a later call at an earlier time; lsfreeRH
