@@ -2100,6 +2100,30 @@ static void low_theta(Cell *w, double *th00, double thmean, double thstd) {
   }
 }
 
+/* single-function probe of the contact-angle quadrature for the closed-form tests: the
+   frozen fraction of one liquid bin (the cloud bins' first) with insoluble diameter dins,
+   from gauss_legendre with mode 1 (immersion) or 2 (deposition) */
+double salsa_ref_freezing_fraction(const salsa_ref_ctx_t *c, int mode, double Tk, double S, double th00, double thm,
+                                   double ths, double dins, double tstep) {
+  Cell *w = (Cell *)malloc(sizeof(Cell));
+  if (!w) return -1.;
+  cell_clear(w, c);
+  w->c = c;
+  memcpy(w->all, c->tmpl, sizeof(Section) * c->ntotal);
+  w->liquid = &w->all[0];
+  double Seq[MAXB], th[MAXB], frac[MAXB];
+  int mask[MAXB];
+  for (int k = 0; k < c->nliquid; k++) { Seq[k] = S; th[k] = th00; mask[k] = 0; frac[k] = 0.; }
+  const int kk = c->nbins;   /* first cloud bin */
+  w->liquid[kk].numc = 1.e6;
+  w->liquid[kk].ddry = dins;
+  mask[kk] = 1;
+  gauss_legendre(w, Tk, Seq, th, thm, ths, tstep, mask, mode, frac);
+  const double r = frac[kk];
+  free(w);
+  return r;
+}
+
 /* :542-555 getIceBin */
 static int getIceBin(const Cell *w, double ldwet) {
   const salsa_ref_ctx_t *c = w->c;

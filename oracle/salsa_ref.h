@@ -77,6 +77,9 @@ double salsa_ref_coagc_pair(const salsa_ref_ctx_t *ctx, int b1, int b2,
                             double dwet2, double temp, double pres);
 double salsa_ref_nucleation_rate(const salsa_ref_ctx_t *ctx, int kind, double theta,
                                  double Tk, double Din, double S);
+double salsa_ref_freezing_fraction(const salsa_ref_ctx_t *ctx, int mode, double Tk, double S,
+                                   double th00, double thm, double ths, double dins,
+                                   double tstep);
 
 #ifdef __cplusplus
 }

@@ -344,6 +344,52 @@ def test_nucleation_rates_match_independent_restatement():
     assert nonzero > 500
 
 
+GL_NODES = [-0.973908239224106, -0.865060566454542, -0.679410688379483, -0.433395397408358, -0.148874339007507,
+            0.148874339007507, 0.433395397408358, 0.679410688379483, 0.865060566454542, 0.973908239224106]
+GL_WEIGHTS = [0.066667031481273176, 0.14945422671662059, 0.21908574324601154, 0.26926671836765848,
+              0.29552422471242434, 0.29552422471242434, 0.26926671836765848, 0.21908574324601154,
+              0.14945422671662059, 0.066667031481273176]
+
+
+def freezing_fraction_numpy(mode, tk, s, th00, thm, ths, dins, tstep):
+    """gauss_legendre (mo_salsa_cloud_ice_SE.f90:131-206) for one bin: the frozen
+    fraction over contact angles th00..180 with the Gaussian weight f_gauss
+    (math_functions.f90:36-45, which takes the full-precision pi), restated."""
+    if tk > 273.15:
+        return 0.
+    thmax, thmin, acc = 180., th00, 0.
+    for x, w in zip(GL_NODES, GL_WEIGHTS):
+        th1 = 0.5 * (thmax - thmin) * x + 0.5 * (thmax + thmin)
+        j = nucleation_rate_numpy(mode, th1, tk, dins, s)
+        if th1 > thmin:
+            ftheta = (1. / (math.sqrt(2. * math.pi) * ths)) * math.exp(-0.5 * ((th1 - thm) ** 2 / ths ** 2))
+        else:
+            ftheta = 0.
+        acc = acc + ftheta * w * (1. - math.exp(-j * tstep))
+    return 0.5 * (thmax - thmin) * acc
+
+
+def test_freezing_fraction_matches_independent_restatement():
+    """The oracle's contact-angle quadrature (probe salsa_ref_freezing_fraction) against
+    the restatement above, immersion and deposition, over 2,000 random states."""
+    o = Oracle(workload_config(5))
+    rng = np.random.default_rng(5)
+    nonzero = 0
+    for _ in range(2000):
+        mode = int(rng.integers(1, 3))
+        tk, s = rng.uniform(215., 275.), rng.uniform(0.95, 1.5)
+        th00, thm, ths = rng.uniform(0., 120.), rng.uniform(60., 160.), rng.uniform(5., 30.)
+        dins, tstep = 10 ** rng.uniform(-8., -5.), rng.choice([0.5, 1., 2.])
+        got = lib().salsa_ref_freezing_fraction(o.h, mode, tk, s, th00, thm, ths, dins, tstep)
+        want = freezing_fraction_numpy(mode, tk, s, th00, thm, ths, dins, tstep)
+        if want == 0. or got == 0.:
+            assert got == want, (mode, tk, s, th00, thm, ths, dins, tstep, got, want)
+        else:
+            nonzero += 1
+            assert got == pytest.approx(want, rel=1e-9, abs=0.), (mode, tk, s, th00, thm, ths, dins, tstep)
+    assert nonzero > 300
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
