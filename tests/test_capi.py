@@ -10,7 +10,7 @@ import pytest
 
 from uclales_salsa_gb300 import api, capi
 from uclales_salsa_gb300.chain import ChainDesc
-from uclales_salsa_gb300.config import reference_defaults
+from uclales_salsa_gb300.config import reference_defaults, workload_config
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "salsa_gb300.h")
@@ -95,7 +95,10 @@ def test_secondary_ice_modes_outside_the_reference_are_refused_before_any_device
             assert lib.salsa_gb300_init(C.byref(cfg), C.byref(h)) == capi.SALSA_E_UNSUPPORTED, (scheme, mode)
     for scheme, modes in (("lssiprimespln", (1, 2)), ("lssipdropfrac", (1, 2, 3, 4)), ("lssipicecollbreak", (1, 2, 3))):
         for mode in modes:
-            cfg = reference_defaults(level=5)
+            # the 7-bin precipitation and ice layout of the workloads: on a GPU, init goes on
+            # to size the shared memory, which the secondary-ice form with the 20-bin
+            # default layout exceeds (also SALSA_E_UNSUPPORTED)
+            cfg = workload_config(5)
             cfg.lssecice.sw = 1
             sw = getattr(cfg, scheme)
             sw.sw, sw.mode = 1, mode
