@@ -1967,6 +1967,22 @@ static double calcSweq(Cell *w, const Section *part, double T) {
   return (znw / (EPSR + zns + znw)) * kel;
 }
 
+/* single-function probe of calcSweq for the closed-form tests: the equilibrium
+   saturation ratio of liquid bin b holding numc particles with the volume
+   concentrations volc[0..nwet-1] (dry species, then water) at temperature T */
+double salsa_ref_sweq(const salsa_ref_ctx_t *c, int b, double numc, const double *volc, double T) {
+  Cell *w = (Cell *)malloc(sizeof(Cell));
+  if (!w) return -1.;
+  cell_clear(w, c);
+  w->c = c;
+  Section s = c->tmpl[b];
+  s.numc = numc;
+  for (int i = 0; i < NSP; i++) s.volc[i] = i < c->nwet ? volc[i] : 0.;
+  const double r = calcSweq(w, &s, T);
+  free(w);
+  return r;
+}
+
 /* math_functions.f90:494-510 erfm1 */
 static double erfm1(double x) {
   const double a = 0.140012;

@@ -80,6 +80,8 @@ double salsa_ref_nucleation_rate(const salsa_ref_ctx_t *ctx, int kind, double th
 double salsa_ref_freezing_fraction(const salsa_ref_ctx_t *ctx, int mode, double Tk, double S,
                                    double th00, double thm, double ths, double dins,
                                    double tstep);
+double salsa_ref_sweq(const salsa_ref_ctx_t *ctx, int b, double numc, const double *volc,
+                      double T);
 
 #ifdef __cplusplus
 }

@@ -43,6 +43,8 @@ def lib(variant="plain"):
         L.salsa_ref_nucleation_rate.restype = C.c_double
         L.salsa_ref_freezing_fraction.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 7
         L.salsa_ref_freezing_fraction.restype = C.c_double
+        L.salsa_ref_sweq.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.c_double]
+        L.salsa_ref_sweq.restype = C.c_double
         L.salsa_ref_coagc_pair.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 6
         L.salsa_ref_coagc_pair.restype = C.c_double
         L.salsa_ref_tend_constrain.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,

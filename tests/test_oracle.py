@@ -1,4 +1,5 @@
 """CPU tests of the oracle (the FP64 restatement of run_SALSA used as parity checker)."""
+import ctypes as C
 import math
 import os
 
@@ -393,6 +394,49 @@ def test_freezing_fraction_matches_independent_restatement():
             nonzero += 1
             assert got == pytest.approx(want, rel=1e-9, abs=0.), (mode, tk, s, th00, thm, ths, dins, tstep)
     assert nonzero > 300
+
+
+def sweq_numpy(numc, volc, T, species):
+    """calcSweq (src/src_shared/mo_particle_external_properties.f90:208-253) for a liquid
+    particle, restated: Raoult's term with the dissociating species and the Kelvin term
+    of the wet diameter; volc = dry species in order, then water."""
+    diss = {"SO4": 3., "OC": 1., "BC": 0., "DU": 0., "SS": 2., "NO": 1., "NH": 1.}
+    rho = {"SO4": 1830., "OC": 1400., "BC": 2000., "DU": 2650., "SS": 2165., "NO": 1479., "NH": 1530.}
+    mm = {"SO4": 98.08e-3, "OC": 150.e-3, "BC": 12.e-3, "DU": 100.e-3, "SS": 58.44e-3, "NO": 62.01e-3, "NH": 18.04e-3}
+    rg, surfw0, mwa, rhowa, eps = 8.314, 0.073, 18.016e-3, 1000., np.finfo(float).eps
+    dwet = (sum(volc) / numc / 0.5235988) ** (1. / 3.)
+    znw = volc[-1] * rhowa / mwa
+    zns = sum(diss[sp] * v * rho[sp] / mm[sp] for sp, v in zip(species, volc))
+    zvs = sum(min(1., diss[sp]) * v for sp, v in zip(species, volc))
+    zvtot = sum(volc[:-1])
+    kel = math.exp(4. * surfw0 * mwa / (rg * T * rhowa * dwet))
+    if volc[-1] > 1.e-28 * numc or zvs > 1.e-28 * numc:
+        return (znw / (zns + znw)) * kel
+    if zvtot - zvs > 1.e-28 * numc:
+        return kel
+    return (znw / (eps + zns + znw)) * kel
+
+
+def test_equilibrium_saturation_ratio_matches_independent_restatement():
+    """The oracle's calcSweq (probe salsa_ref_sweq) against the restatement above for
+    random compositions of cloud and aerosol particles, dry insoluble ones included."""
+    cfg = workload_config(5)
+    o = Oracle(cfg)
+    lay = build_layout(cfg)
+    rng = np.random.default_rng(3)
+    for _ in range(2000):
+        b = int(rng.integers(0, lay.nbins + lay.ncld))
+        numc = 10 ** rng.uniform(3., 9.)
+        d = 10 ** rng.uniform(-8., -4.5)
+        frac = rng.dirichlet(np.ones(lay.nwet))
+        if rng.uniform() < 0.2:
+            frac = np.zeros(lay.nwet)
+            frac[int(rng.choice([2, 3]))] = 1.        # a dry insoluble particle (BC or DU)
+        volc = (numc * 0.5235988 * d ** 3 * frac).tolist()
+        T = rng.uniform(230., 300.)
+        got = lib().salsa_ref_sweq(o.h, b, numc, (C.c_double * lay.nwet)(*volc), T)
+        want = sweq_numpy(numc, volc, T, lay.species)
+        assert got == pytest.approx(want, rel=1e-13, abs=0.), (b, numc, volc, T)
 
 
 def test_condensation_conserves_water():
