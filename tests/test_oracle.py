@@ -439,6 +439,93 @@ def test_equilibrium_saturation_ratio_matches_independent_restatement():
         assert got == pytest.approx(want, rel=1e-13, abs=0.), (b, numc, volc, T)
 
 
+def autoconv2_numpy(numc, volc, prc_numc, prc_volc, dt, ndry, iwa, nlim=1., prlim=1.e-6):
+    """autoconv2 (src/src_salsa/mo_salsa_cloud.f90:1401-1477) with cumlognorm
+    (src/src_shared/math_functions.f90:64-76), restated: from the largest cloud bin down,
+    the part of a lognormal drop population (sigma 1.2) above 50 um moves to the first
+    precipitation bin.  numc[c], volc[c][s] of the cloud bins; returns the new values."""
+    numc, volc = list(numc), [list(v) for v in volc]
+    pn, pv = prc_numc, list(prc_volc)
+    zd0, sigmag, max_rate = 50.e-6, 1.2, 1.0e10
+
+    def cumlognorm(dg, sg, dpart):
+        return 0.5 + 0.5 * math.erf((math.log(dpart) - math.log(dg)) / (math.sqrt(2.) * math.log(sg)))
+    for cc in range(len(numc) - 1, -1, -1):
+        tot = 0.
+        ntot, vtot = numc[cc], sum(volc[cc])
+        if ntot > nlim and vtot > 0.:
+            dvg = (vtot / ntot / 0.5235988) ** (1. / 3.) * math.exp((3. * math.log(sigmag) ** 2) / 2.)
+            dg = dvg * math.exp(-3. * math.log(sigmag) ** 2)
+            vrem = vtot * (1. - cumlognorm(dvg, sigmag, zd0))
+            nrem = ntot * (1. - cumlognorm(dg, sigmag, zd0))
+            if vrem > 0. and nrem > prlim:
+                for ss in range(ndry):
+                    pv[ss] = pv[ss] + volc[cc][ss] * (nrem / ntot)
+                    volc[cc][ss] = volc[cc][ss] * (1. - (nrem / ntot))
+                pv[iwa] = pv[iwa] + volc[cc][iwa] * (vrem / vtot)
+                volc[cc][iwa] = volc[cc][iwa] * (1. - (vrem / vtot))
+                pn = pn + nrem
+                numc[cc] = numc[cc] - nrem
+                tot = tot + nrem
+                if tot > max_rate * dt:
+                    break
+    return numc, volc, pn, pv
+
+
+def test_autoconversion_matches_independent_restatement():
+    """lsauto mode 2 alone: the oracle's cloud and first precipitation bins after one
+    step against the restatement above, for drop populations around the 50 um limit."""
+    cfg = workload_config(4)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsactiv):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    cfg.lsauto.sw, cfg.lsauto.mode = 1, 2
+    inp = make_inputs("grid16x16x40", "cpu", X=2, Y=2, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nd, iw, nc, npr = lay.nwet, lay.ndry, lay.nwet - 1, lay.ncld, lay.nprc
+    f = inp.fields
+    rng = np.random.default_rng(9)
+    for key in ("ncloud", "mcloud", "nprecp", "mprecp"):
+        f[key].zero_()
+    sh = f["ncloud"].shape[1:]
+    mc = f["mcloud"].view(nw, nc, *sh)
+    rho = [ALL_RHO[sp] for sp in lay.species] + [1000.]
+    cells = [(j, i, k) for j in (2, 3) for i in (2, 3) for k in (1, 2)]
+    for (j, i, k) in cells:
+        dn = float(f["dn"][j, i, k])
+        for cc in range(nc):
+            n = 10 ** rng.uniform(6., 8.)
+            d = 10 ** rng.uniform(math.log10(15e-6), math.log10(60e-6))
+            f["ncloud"][cc, j, i, k] = n / dn
+            v = n * PI6 * d ** 3
+            for sp in range(nd):
+                mc[sp, cc, j, i, k] = 1e-3 * v * rng.uniform(0.1, 1.) * rho[sp] / dn
+            mc[iw, cc, j, i, k] = v * rho[iw] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    moved = 0
+    for (j, i, k) in cells:
+        dn = float(f["dn"][j, i, k])
+        numc = [float(f["ncloud"][cc, j, i, k]) * dn for cc in range(nc)]
+        volc = [[float(mc[sp, cc, j, i, k]) * dn / rho[sp] for sp in range(nw)] for cc in range(nc)]
+        n1, v1, pn, pv = autoconv2_numpy(numc, volc, 0., [0.] * nw, dt, nd, iw)
+        moved += pn > 0.
+        got_n = [float(f["ncloud"][cc, j, i, k] + out["ncloudt"][cc, j, i, k] * dt) * dn for cc in range(nc)]
+        got_pn = float(out["nprecpt"][0, j, i, k]) * dt * dn
+        assert got_pn == pytest.approx(pn, rel=1e-10, abs=0.)
+        for cc in range(nc):
+            assert got_n[cc] == pytest.approx(n1[cc], rel=1e-10, abs=0.), cc
+        mp = out["mprecpt"].view(nw, npr, *sh)
+        for sp in range(nw):
+            got = float(mp[sp, 0, j, i, k]) * dt * dn / rho[sp]
+            assert got == pytest.approx(pv[sp], rel=1e-10, abs=0.), sp
+    assert moved == len(cells)
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
