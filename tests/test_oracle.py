@@ -526,6 +526,90 @@ def test_autoconversion_matches_independent_restatement():
     assert moved == len(cells)
 
 
+def ice_melt_numpy(inum, ivol, pnum, pvol, vlo_prc, ndry, iwa, irim, nlim=1.e-6):
+    """ice_melt (src/src_salsa/mo_salsa_cloud_ice.f90:393-439) with getPrecipBin
+    (:463-477), updateDiameter("wet") and updateRhomean (classSection.f90:91-195),
+    restated for T >= 273.15: 99.9 % of every populated ice bin moves to the
+    precipitation bin of its melted volume.  ivol[k] = dry species, pristine ice, rime;
+    pvol[b] = dry species, water."""
+    rhowa, rhoic, rhori, maxfrac = 1000., 917., 400., 0.999
+    inum, ivol, pnum, pvol = list(inum), [list(v) for v in ivol], list(pnum), [list(v) for v in pvol]
+    for kk in range(len(inum)):
+        if inum[kk] < nlim:
+            continue
+        dwet = (sum(ivol[kk]) / inum[kk] / 0.5235988) ** (1. / 3.)
+        mp, mr = rhoic * ivol[kk][iwa], rhori * ivol[kk][irim]
+        rhomean = min((mp * rhoic + mr * rhori) / max(mp + mr, 7.e-25), rhoic)
+        vol = 0.5235988 * dwet ** 3 * rhomean / rhowa
+        bb = min(max(1, sum(1 for v in vlo_prc if v < vol)), len(pnum)) - 1
+        for ss in range(ndry):
+            pvol[bb][ss] += maxfrac * ivol[kk][ss]
+            ivol[kk][ss] = (1. - maxfrac) * ivol[kk][ss]
+        liq = (ivol[kk][iwa] * rhoic + ivol[kk][irim] * rhori) / rhowa
+        pnum[bb] += maxfrac * inum[kk]
+        inum[kk] = (1. - maxfrac) * inum[kk]
+        pvol[bb][iwa] += maxfrac * liq
+        ivol[kk][iwa] = (1. - maxfrac) * ivol[kk][iwa]
+        ivol[kk][irim] = (1. - maxfrac) * ivol[kk][irim]
+    return inum, ivol, pnum, pvol
+
+
+def test_ice_melting_matches_independent_restatement():
+    """lsicemelt alone above freezing: the oracle's ice and precipitation bins after one
+    step against the restatement above, for rimed and pristine ice of every size."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    inp = make_inputs("grid256x256x128", "cpu", X=2, Y=2, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nd, nprc, nice = lay.nwet, lay.ndry, lay.nprc, lay.nice
+    iwa, irim = nw - 1, nw
+    f = inp.fields
+    rng = np.random.default_rng(13)
+    for key in ("naero", "maero", "ncloud", "mcloud", "nprecp", "mprecp", "nice", "mice"):
+        f[key].zero_()
+    sh = f["nice"].shape[1:]
+    mi = f["mice"].view(nw + 1, nice, *sh)
+    rho_i = lay.rhoice()
+    rho_l = lay.rholiq()
+    cells = [(j, i, k) for j in (2, 3) for i in (2, 3) for k in (1, 2)]
+    for (j, i, k) in cells:
+        f["temp"][j, i, k] = rng.uniform(273.2, 280.)
+        dn = float(f["dn"][j, i, k])
+        for kk in range(nice):
+            n = 10 ** rng.uniform(2., 6.)
+            d = 10 ** rng.uniform(-5.5, -3.)
+            v = n * 0.5235988 * d ** 3
+            f["nice"][kk, j, i, k] = n / dn
+            for sp in range(nd):
+                mi[sp, kk, j, i, k] = 1e-3 * v * rng.uniform(0.1, 1.) * rho_i[sp] / dn
+            rime = rng.uniform(0., 0.6)
+            mi[iwa, kk, j, i, k] = (1. - rime) * v * rho_i[iwa] / dn
+            mi[irim, kk, j, i, k] = rime * v * rho_i[irim] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    vlo_prc = lay.vlolim[lay.nbins + lay.ncld:lay.nliquid]
+    mp = out["mprecpt"].view(nw, nprc, *sh)
+    for (j, i, k) in cells:
+        dn = float(f["dn"][j, i, k])
+        inum = [float(f["nice"][kk, j, i, k]) * dn for kk in range(nice)]
+        ivol = [[float(mi[sp, kk, j, i, k]) * dn / rho_i[sp] for sp in range(nw + 1)] for kk in range(nice)]
+        n1, v1, pn, pv = ice_melt_numpy(inum, ivol, [0.] * nprc, [[0.] * nw for _ in range(nprc)], vlo_prc,
+                                        nd, iwa, irim)
+        for b in range(nprc):
+            got_n = float(out["nprecpt"][b, j, i, k]) * dt * dn
+            assert got_n == pytest.approx(pn[b], rel=1e-12, abs=0.), b
+            for sp in range(nw):
+                got = float(mp[sp, b, j, i, k]) * dt * dn / rho_l[sp]
+                assert got == pytest.approx(pv[b][sp], rel=1e-12, abs=0.), (b, sp)
+        assert sum(1 for x in pn if x > 0.) >= 2        # the melted ice spreads over several bins
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
