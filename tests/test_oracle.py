@@ -610,6 +610,152 @@ def test_ice_melting_matches_independent_restatement():
         assert sum(1 for x in pn if x > 0.) >= 2        # the melted ice spreads over several bins
 
 
+def ice_nucleation_numpy(T, rv, rs, rsi, dt, num, vol, indef, lay, cfg):
+    """ice_nucl_driver + iceNucleation (src/src_salsa/mo_salsa_cloud_ice_SE.f90:28-127,
+    421-555) for one cell, restated with low_theta (:394-417), erfm1
+    (math_functions.f90:14-30), the diameters of classSection.f90:91-166 and the rates and
+    quadrature restated above.  num[k], vol[k][s] of the liquid bins (aerosol, cloud,
+    precipitation; species then water); returns them with the new ice bins and IN
+    deficits."""
+    pi6, nw, nd = 0.5235988, lay.nwet, lay.ndry
+    iwa, irim = nw - 1, nw
+    rhowa, rhoic, rhori = 1000., 917., 400.
+    ins = [lay.species.index("BC"), lay.species.index("DU")]
+    idu = lay.species.index("DU")
+    nl = lay.nliquid
+    phase = [1] * lay.nbins + [2] * lay.ncld + [3] * lay.nprc
+    nlim = [1.] * (lay.nbins + lay.ncld) + [1.e-6] * lay.nprc
+    dlim = [30.e-6] * lay.nbins + [100.e-6] * lay.ncld + [5.e-3] * lay.nprc
+    num, vol, indef = list(num), [list(v) for v in vol], list(indef)
+    ice_num, ice_vol = [0.] * lay.nice, [[0.] * (nw + 1) for _ in range(lay.nice)]
+
+    def erfm1(x):
+        a = 0.140012
+        sgn = -1. if x < 0. else 1.
+        t1 = math.log(max(1.e-20, 1. - x ** 2))
+        t2 = 2. / (math.pi * a)
+        return sgn * math.sqrt(math.sqrt((t2 + 0.5 * t1) ** 2 - t1 / a) - (t2 + 0.5 * t1))
+
+    def low_theta(f, thm, ths):
+        th = min(max(thm + math.sqrt(2.) * ths * erfm1(2. * f - 1.), 0.), 180.)
+        return th if cfg.lsFreeTheta.sw else max(cfg.initMinTheta, th)
+
+    seq, dwet, ddry, dins = [0.] * nl, [0.] * nl, [0.] * nl, [0.] * nl
+    for k in range(nl):
+        if num[k] >= nlim[k]:
+            seq[k] = sweq_numpy(num[k], vol[k], T, lay.species)
+        if num[k] > nlim[k]:
+            dwet[k] = (sum(vol[k]) / num[k] / pi6) ** (1. / 3.)
+            ddry[k] = (sum(vol[k][:nd]) / num[k] / pi6) ** (1. / 3.)
+            dins[k] = (sum(vol[k][s] for s in ins) / num[k] / pi6) ** (1. / 3.)
+        else:
+            dwet[k] = ddry[k] = dins[k] = lay.dmid[k]
+        dwet[k], ddry[k], dins[k] = min(dwet[k], dlim[k]), min(ddry[k], dlim[k]), min(dins[k], dlim[k])
+    si = rv / rsi
+    f_hom, f_imm, f_dep = [0.] * nl, [0.] * nl, [0.] * nl
+    for k in range(nl):
+        if dwet[k] - ddry[k] > 1e-10 and T < 237.9 and cfg.lsicehom:
+            j = nucleation_rate_numpy(3, 0., T, 0., seq[k])
+            f_hom[k] = 1. - math.exp(-j * pi6 * (dwet[k] ** 3 - ddry[k] ** 3) * dt)
+        active = T <= 273.15 and num[k] >= nlim[k]
+        if cfg.lsiceimm and phase[k] in (2, 3) and dins[k] > 1e-10 and active:
+            f_imm[k] = freezing_fraction_numpy(1, T, seq[k], low_theta(indef[k], cfg.mean_theta_imm,
+                                               cfg.sigma_theta_imm), cfg.mean_theta_imm, cfg.sigma_theta_imm,
+                                               ddry[k], dt)
+        if (cfg.lsicedep and phase[k] == 1 and rv / rs < 1. and dwet[k] - dins[k] < 1e-10 and dins[k] > 1e-10
+                and active):
+            f_dep[k] = freezing_fraction_numpy(2, T, si, low_theta(indef[k], cfg.mean_theta_dep,
+                                               cfg.sigma_theta_dep), cfg.mean_theta_dep, cfg.sigma_theta_dep,
+                                               ddry[k], dt)
+    vlo_ice = lay.vlolim[nl:]
+    for k in range(nl):
+        frac = max(0., min(0.99, f_imm[k] + f_hom[k] + f_dep[k] - (f_imm[k] + f_dep[k]) * f_hom[k]))
+        if num[k] < nlim[k] or sum(vol[k][s] for s in ins) < pi6 * (1.e-8) ** 3:
+            continue
+        v = pi6 * dwet[k] ** 3 * rhowa / rhoic
+        bb = min(max(1, sum(1 for x in vlo_ice if x < v)), lay.nice) - 1
+        dry = sum(vol[k][:nd])
+        vtot = frac * dry
+        fdu = vol[k][idu] / dry
+        if fdu <= 0.1:
+            frac2, ncur0 = frac * fdu, num[k] * fdu
+        else:
+            frac2, ncur0 = frac, num[k]
+        nnew = frac2 * num[k]
+        f1 = (nnew + (ncur0 - nnew) * indef[k]) / ncur0
+        indef[k] = min(max(f1, 0.), 1. - 1.e-20)
+        if fdu <= 0.1:
+            ice_vol[bb][idu] = max(0., ice_vol[bb][idu] + vtot * fdu)
+            vol[k][idu] = max(0., vol[k][idu] - vtot * fdu)
+        else:
+            for ss in range(nd):
+                ice_vol[bb][ss] = max(0., ice_vol[bb][ss] + vol[k][ss] * frac2)
+                vol[k][ss] = max(0., vol[k][ss] * (1. - frac2))
+        if phase[k] in (1, 2):
+            ice_vol[bb][iwa] = max(0., ice_vol[bb][iwa] + vol[k][iwa] * frac2 * rhowa / rhoic)
+        else:
+            ice_vol[bb][irim] = max(0., ice_vol[bb][irim] + vol[k][iwa] * frac2 * rhowa / rhori)
+        vol[k][iwa] = max(0., vol[k][iwa] * (1. - frac2))
+        ice_num[bb] = max(0., ice_num[bb] + num[k] * frac2)
+        num[k] = max(0., num[k] * (1. - frac2))
+    return num, vol, ice_num, ice_vol, indef
+
+
+def test_ice_nucleation_matches_independent_restatement():
+    """lsicenucl alone (immersion, deposition and homogeneous freezing all on): the
+    oracle's ice bins, liquid numbers and IN deficits after one step against the
+    restatement above, on 32 cells of grid256x256x128."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    cfg.lsicehom = cfg.lsicedep = cfg.lsiceimm = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=4, Y=4, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nl, nice = lay.nwet, lay.nliquid, lay.nice
+    f = inp.fields
+    rng = np.random.default_rng(21)
+    f["temp"][...] = torch.from_numpy(rng.uniform(225., 272., size=f["temp"].shape))
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["nice"].shape[1:]
+    cats = [("naero", "maero", lay.nbins), ("ncloud", "mcloud", lay.ncld), ("nprecp", "mprecp", lay.nprc)]
+    rho = lay.rholiq()
+    froze = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num, vol = [], []
+                for nk, mk, nb in cats:
+                    mv = f[mk].view(nw, nb, *sh)
+                    for b in range(nb):
+                        num.append(float(f[nk][b, j, i, k]) * dn)
+                        vol.append([float(mv[s, b, j, i, k]) * dn / rho[s] for s in range(nw)])
+                indef = [float(f["indef"][b, j, i, k]) for b in range(nl)]
+                T, rv = float(f["temp"][j, i, k]), float(f["rp"][j, i, k])
+                n1, v1, inum, ivol, ind1 = ice_nucleation_numpy(T, rv, float(f["rsl"][j, i, k]),
+                                                                float(f["rsi"][j, i, k]), dt, num, vol, indef,
+                                                                lay, cfg)
+                froze += sum(1 for x in inum if x > 0.)
+                for b in range(nice):
+                    got = float(out["nicet"][b, j, i, k]) * dt * dn
+                    assert got == pytest.approx(inum[b], rel=1e-8, abs=0.), (j, i, k, b)
+                for b in range(nl):
+                    assert float(fields["indef"][b, j, i, k]) == pytest.approx(ind1[b], rel=1e-8, abs=1e-300), b
+                q = 0
+                for nk, mk, nb in cats:
+                    for b in range(nb):
+                        got = float(f[nk][b, j, i, k] + out[nk + "t"][b, j, i, k] * dt) * dn
+                        assert got == pytest.approx(n1[q], rel=1e-8, abs=0.), (nk, b)
+                        q += 1
+    assert froze > 10
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
