@@ -185,7 +185,7 @@ def test_coagc_matches_independent_restatement():
         assert k == pytest.approx(kn, rel=1e-12, abs=0.), (b1, b2)
 
 
-def equilibration_numpy(numc, zvolc, dmid, T, prh, in1a, fn1a, in2a, fn2b, nlim=1.):
+def equilibration_numpy(numc, zvolc, dmid, T, prh, in1a, fn1a, in2a, fn2b, nlim=1., init=True):
     """Independent restatement of the initialisation call of equilibration
     (src/src_salsa/mo_salsa_properties.f90:73-380) for one cell: the aerosol water
     content [kg/m3] of every bin, regime 1a (SO4 and OC, Kelvin factor carried from bin
@@ -222,7 +222,7 @@ def equilibration_numpy(numc, zvolc, dmid, T, prh, in1a, fn1a, in2a, fn2b, nlim=
                 zke = math.exp(2. * surfw0 * mvwa / (boltz * T * zdwet))
             out[kk] = lwc
     for kk in range(in2a, fn2b + 1):
-        if numc[kk] > nlim:
+        if init and numc[kk] > nlim:
             v = zvolc[kk]
             zcore = sum(x / numc[kk] for x in v[:5])
             zrh = min(max(prh, 0.37), 0.98)
@@ -754,6 +754,152 @@ def test_ice_nucleation_matches_independent_restatement():
                         assert got == pytest.approx(n1[q], rel=1e-8, abs=0.), (nk, b)
                         q += 1
     assert froze > 10
+
+
+def acth2o_numpy(vol, species, pcw=None):
+    """acth2o (mo_salsa_dynamics.f90:1127-1157): water activity of a liquid particle."""
+    diss = {"SO4": 3., "OC": 1., "BC": 0., "DU": 0., "SS": 2.}
+    rho = {"SO4": 1830., "OC": 1400., "BC": 2000., "DU": 2650., "SS": 2165.}
+    mm = {"SO4": 98.08e-3, "OC": 150.e-3, "BC": 12.e-3, "DU": 100.e-3, "SS": 58.44e-3}
+    zns = 0.
+    for sp, v in zip(species, vol):
+        zns = zns + diss[sp] * v * rho[sp] / mm[sp]
+    znw = pcw if pcw is not None else vol[-1] * 1000. / 18.016e-3
+    return max(0.1, znw / max(np.finfo(float).eps, (znw + zns)))
+
+
+def gpparth2o_numpy(T, P, rv, rs, dt, num, vol, lay, cl=True, ae=True):
+    """gpparth2o (src/src_salsa/mo_salsa_dynamics.f90:691-1125) for one cell without
+    ice, restated: the aerosol water of equilibration, then the mass-transfer
+    coefficients of the populated bins and the explicit substeps (0.02 s, +-10 %
+    limiter) of the water vapour budget.  num[k], vol[k][s] of the liquid bins;
+    returns the new volumes and the new water vapour mixing ratio."""
+    pi, rg, avog, mair, mwa, rhowa, surfw0, alv = 3.1415927, 8.314, 6.0221e+23, 28.97e-3, 18.016e-3, 1000., 0.073, 2.5e6
+    nb, nc, npr, nl, nd = lay.nbins, lay.ncld, lay.nprc, lay.nliquid, lay.ndry
+    iwa = lay.nwet - 1
+    nlim = [1.] * (nb + nc) + [1.e-6] * npr
+    dlim = [30.e-6] * nb + [100.e-6] * nc + [5.e-3] * npr
+    vol = [list(v) for v in vol]
+    zrh = rv / rs
+    aelwc1 = sum(vol[k][iwa] for k in range(lay.in1a, lay.fn2b + 1)) * rhowa
+    zv = [[v[0], v[1], v[2], v[3], v[4]] for v in vol[:nb]]
+    for init in ((False, True) if (zrh < 0.98 or not ae) else (False,)):
+        w = equilibration_numpy(num[:nb], zv, lay.dmid, T, zrh, lay.in1a, lay.fn1a, lay.in2a, lay.fn2b, init=init)
+        for k, lwc in w.items():
+            vol[k][iwa] = lwc / rhowa
+    aelwc2 = sum(vol[k][iwa] for k in range(lay.in1a, lay.fn2b + 1)) * rhowa
+    rv = rv - (aelwc2 - aelwc1) / (P * mair / (rg * T))
+    any_c = any(num[k] > 1. for k in range(nb, nb + nc))
+    any_p = any(num[k] > 1.e-6 for k in range(nb + nc, nl))
+    any_a = any(num[k] > 1. for k in range(nb))
+    if not ((any_c or (any_p and cl)) or (any_a and zrh > 0.98 and ae)):
+        return vol, rv
+    rhoair = mair * P / (rg * T)
+    zdfh2o = (5. / (16. * avog * rhoair * 1.e-3 * (3.11e-8) ** 2)) * \
+        math.sqrt(rg * 1.e7 * T * mair * 1.e3 * (mwa + mair) * 1.e3 / (2. * pi * mwa * 1.e3))
+    zdfh2o = zdfh2o * 1.e-4
+    zmfph2o = 3. * zdfh2o * math.sqrt(pi * mwa / (8. * rg * T))
+    zthcond = 0.023807 + 7.1128e-5 * (T - 273.16)
+    dwet = [min((sum(vol[k]) / num[k] / 0.5235988) ** (1. / 3.) if num[k] > nlim[k] else lay.dmid[k], dlim[k])
+            for k in range(nl)]
+    kel, surf, mt, wsat = [1.] * nl, [0.] * nl, [0.] * nl, [0.] * nl
+    for k in range(nl):
+        on = num[k] > nlim[k] and ((k >= nb and cl) or (k < nb and zrh > 0.98 and ae))
+        if not on:
+            continue
+        zact = acth2o_numpy(vol[k], lay.species)
+        kel[k] = math.exp(4. * surfw0 * mwa / (rg * T * rhowa * dwet[k]))
+        surf[k] = rs * rhoair / mwa
+        wsat[k] = zact * kel[k]
+        zknud = 2. * zmfph2o / dwet[k]
+        zbeta = (zknud + 1.) / (0.377 * zknud + 1. + 4. / (3.) * (zknud + zknud ** 2))
+        h1 = num[k] * 2. * pi * dwet[k] * zdfh2o * zbeta
+        h2 = mwa * zdfh2o * alv * wsat[k] * surf[k] / (zthcond * T)
+        h3 = ((alv * mwa) / (rg * T)) - 1.
+        mt[k] = h1 / (h2 * h3 + 1.)
+    zcwc = rv * rhoair / mwa
+    cw = [vol[k][iwa] * rhowa / mwa for k in range(nl)]
+    zcwtot = zcwc + sum(cw[:nb]) + sum(cw[nb:nb + nc]) + sum(cw[nb + nc:])
+    groups = [range(lay.in2a, nb), range(nb, nb + nc), range(nb + nc, nl)]
+    ttot = 0.
+    zcwint = 0.
+    while ttot < dt:
+        adt = 2.e-2
+        terms = [sum(mt[k] * wsat[k] * surf[k] for k in g) for g in groups]
+        h1 = zcwc + adt * (terms[0] + terms[1] + terms[2] + 0.)
+        h2 = 1. + adt * (sum(mt[k] for k in groups[0]) + sum(mt[k] for k in groups[1]) +
+                         sum(mt[k] for k in groups[2]) + 0.)
+        zcwint = min(h1 / h2, zcwtot)
+        new = list(cw)
+        active = [any(num[k] > 1. for k in range(nb)) and zrh > 0.98, any_c, any_p]
+        for g, on in zip(groups, active):
+            if not on:
+                continue
+            for k in g:
+                d = min(max(adt * mt[k] * (zcwint - wsat[k] * surf[k]), -1.e-1 * cw[k]), 1.e-1 * cw[k])
+                new[k] = cw[k] + d
+                wsat[k] = acth2o_numpy(vol[k], lay.species, new[k]) * kel[k]
+        for k in list(groups[0]) + list(groups[1]) + list(groups[2]):
+            new[k] = max(new[k], 0.)
+        zcwint = zcwtot - sum(new[:nb]) - sum(new[nb:nb + nc]) - sum(new[nb + nc:]) - 0.
+        cw = new
+        zcwc = zcwint
+        ttot = ttot + adt
+    rv = zcwint * mwa / rhoair
+    for k in range(nl):
+        vol[k][iwa] = max(0., cw[k] * mwa / rhowa)
+    return vol, rv
+
+
+def test_condensation_matches_independent_restatement():
+    """lscnd alone: the oracle's water in every liquid bin and its vapour after one step
+    against the restatement above, on the clear and cloudy cells of a 128-cell block of
+    grid256x256x128."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nl = lay.nwet, lay.nliquid
+    iwa = nw - 1
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["naero"].shape[1:]
+    cats = [("naero", "maero", lay.nbins), ("ncloud", "mcloud", lay.ncld), ("nprecp", "mprecp", lay.nprc)]
+    rho = lay.rholiq()
+    cloudy = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num, vol = [], []
+                for nk, mk, nb in cats:
+                    mv = f[mk].view(nw, nb, *sh)
+                    for b in range(nb):
+                        num.append(float(f[nk][b, j, i, k]) * dn)
+                        vol.append([float(mv[s, b, j, i, k]) * dn / rho[s] for s in range(nw)])
+                cloudy += any(num[b] > 1. for b in range(lay.nbins, lay.nbins + lay.ncld))
+                rv = float(f["rp"][j, i, k])
+                v1, rv1 = gpparth2o_numpy(float(f["temp"][j, i, k]), float(f["press"][j, i, k]), rv,
+                                          float(f["rsl"][j, i, k]), dt, num, vol, lay)
+                assert float(out["rpt"][j, i, k]) * dt == pytest.approx(rv1 - rv, rel=1e-9, abs=0.), (j, i, k)
+                q = 0
+                for nk, mk, nb in cats:
+                    tv = out[mk + "t"].view(nw, nb, *sh)
+                    for b in range(nb):
+                        got = float(tv[iwa, b, j, i, k]) * dt * dn / rho[iwa]
+                        want = v1[q][iwa] - vol[q][iwa]
+                        # changes below the rounding of the bin's water are noise in both
+                        assert got == pytest.approx(want, rel=1e-9, abs=1e-14 * vol[q][iwa] + 1e-30), \
+                            (j, i, k, nk, b)
+                        q += 1
+    assert cloudy >= 10
 
 
 def test_condensation_conserves_water():
