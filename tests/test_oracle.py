@@ -1002,6 +1002,101 @@ def test_aerosol_coagulation_matches_independent_restatement():
     assert changed > 20
 
 
+def distr_update_aero_numpy(num, vol, lay, nd):
+    """The aerosol part of distr_update (src/src_salsa/mo_salsa_update.f90:21-140),
+    restated: from bin fn2b-1 down to in1a, particles below their bin's lower volume
+    limit move down (2b's first bin to 1a's last), particles above the bin middle
+    move their excess up; repeated while the last bin checked is outside its limits."""
+    nlim, pi6 = 1., 0.5235988
+    num, vol = list(num), [list(v) for v in vol]
+    in1a, fn1a, fn2a, in2b, fn2b = lay.in1a, lay.fn1a, lay.fn2a, lay.in2b, lay.fn2b
+    within, count = False, 0
+    while not within:
+        within = True
+        for kk in range(fn2b - 1, in1a - 1, -1):
+            if num[kk] > nlim:
+                if kk == fn2a:
+                    continue
+                zvpart = sum(vol[kk][:nd]) / num[kk]
+                if lay.vlolim[kk] > zvpart and kk == in1a:
+                    continue
+                if lay.vlolim[kk] > zvpart:
+                    mm = fn1a if kk == in2b else kk - 1
+                    num[mm] = num[mm] + num[kk]
+                    num[kk] = 0.
+                    vol[mm] = [x + y for x, y in zip(vol[mm], vol[kk])]
+                    vol[kk] = [0.] * len(vol[kk])
+                    continue
+                if zvpart <= pi6 * (lay.dmid[kk] * lay.dmid[kk] * lay.dmid[kk]):
+                    continue
+                vrat = lay.vhilim[kk] / lay.vlolim[kk]
+                vilo = 2. * zvpart / (1. + vrat)
+                vihi = vrat * vilo
+                vexc = 0.5 * (vihi + lay.vhilim[kk])
+                nfrac = min(1., (vihi - lay.vhilim[kk]) / (vihi - vilo))
+                mm = kk + 1
+                dry = sum(vol[kk][:nd])
+                moved = [nfrac * num[kk] * vexc * v / dry for v in vol[kk]]
+                vol[mm] = [x + m for x, m in zip(vol[mm], moved)]
+                vol[kk] = [x - nfrac * num[kk] * vexc * x / dry for x in vol[kk]]
+                num[mm] = num[mm] + nfrac * num[kk]
+                num[kk] = num[kk] * (1. - nfrac)
+            if num[kk] > nlim:
+                zvpart = sum(vol[kk][:nd]) / num[kk]
+                within = lay.vlolim[kk] < zvpart < lay.vhilim[kk]
+        count += 1
+        assert count <= 100
+    return num, vol
+
+
+def test_aerosol_redistribution_matches_independent_restatement():
+    """lsdistupdate alone, with aerosol particles pushed out of their bins (dry volumes
+    scaled by 0.05 to 30, so some move over several bins): the oracle's aerosol numbers
+    and volumes after one step
+    against the restatement above.  Unscaled bins hold particles at exactly the bin's
+    middle volume, where the move up is decided on a rounding: the absolute tolerance,
+    1e-11 of the bin, takes the ulp-sized transfers that this leaves."""
+    cfg = workload_config(4)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto, cfg.lsactiv):
+        sw.sw = 0
+    cfg.lsdistupdate = 1
+    inp = make_inputs("grid16x16x40", "cpu", X=3, Y=3, Z=3)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nd = lay.nwet, lay.nbins, lay.ndry
+    f = inp.fields
+    sh = f["naero"].shape[1:]
+    mv = f["maero"].view(nw, nb, *sh)
+    rng = np.random.default_rng(31)
+    scale = torch.from_numpy(rng.choice([0.05, 0.3, 0.6, 1., 1.5, 2.5, 4., 30.], size=(nb,) + tuple(sh)))
+    scale[lay.in2b, 2, 2, :] = 0.05                     # 2b's first bin below its limit: it moves to 1a
+    mv[:nd] *= scale.unsqueeze(0)
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    rho = lay.rholiq()
+    tv = out["maerot"].view(nw, nb, *sh)
+    moved = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num = [float(f["naero"][b, j, i, k]) * dn for b in range(nb)]
+                vol = [[float(mv[s_, b, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for b in range(nb)]
+                n1, v1 = distr_update_aero_numpy(num, vol, lay, nd)
+                for b in range(nb):
+                    got = float(out["naerot"][b, j, i, k]) * dt * dn
+                    assert got == pytest.approx(n1[b] - num[b], rel=1e-10, abs=1e-11 * num[b] + 1e-300), b
+                    moved += abs(n1[b] - num[b]) > 1e-6 * max(num[b], 1.)
+                    for s_ in range(nw):
+                        got = float(tv[s_, b, j, i, k]) * dt * dn / rho[s_]
+                        assert got == pytest.approx(v1[b][s_] - vol[b][s_], rel=1e-10,
+                                                    abs=1e-11 * vol[b][s_] + 1e-300), (b, s_)
+    assert moved > 50
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
