@@ -1097,6 +1097,151 @@ def test_aerosol_redistribution_matches_independent_restatement():
     assert moved > 50
 
 
+def act_interst_numpy(num, vol, cnum, cvol, T, S, lay):
+    """actInterst (src/src_salsa/mo_salsa_cloud.f90:859-1195) with intgN / intgV
+    (:1381-1398) for one cell, restated: in each aerosol bin parallel to a cloud bin,
+    the part of a piecewise-linear number distribution whose wet size exceeds the
+    critical size of the supersaturation activates into that cloud bin.  num[k],
+    vol[k][s] of the aerosol bins, cnum / cvol of the cloud bins."""
+    pi6, mwa, surfw0, rg, rhowa, nlim, thvol = 0.5235988, 18.016e-3, 0.073, 8.314, 1000., 1., 1.e-28
+    sq, cube = (lambda x: x * x), (lambda x: x * x * x)
+    num, vol, cnum, cvol = list(num), [list(v) for v in vol], list(cnum), [list(v) for v in cvol]
+    if S <= 1.000:
+        return num, vol, cnum, cvol
+    nd, nw = lay.ndry, lay.nwet
+    sol = [i for i, sp in enumerate(lay.species) if sp in ("SO4", "OC", "SS", "NO", "NH")]
+    ins = [i for i, sp in enumerate(lay.species) if sp in ("BC", "DU")]
+    vmidb = [pi6 * (lay.dmid[k] * lay.dmid[k] * lay.dmid[k]) for k in range(lay.nbins)]
+    rlo = [lay.vlolim[k] / vmidb[k] for k in range(lay.nbins)]
+    rhi = [lay.vhilim[k] / vmidb[k] for k in range(lay.nbins)]
+
+    def intg_n(kk, cc, lo, hi):
+        return 0.5 * kk * max(sq(hi) - sq(lo), 0.) + cc * max(hi - lo, 0.)
+
+    def intg_v(kk, cc, lo, hi):
+        return (1. / 3.) * kk * max(cube(hi) - cube(lo), 0.) + 0.5 * cc * max(sq(hi) - sq(lo), 0.)
+    zkelvin = 4. * mwa * surfw0 / (rg * rhowa * T)
+    zdcstar = 2. * zkelvin / (3. * (S - 1.))
+    zvcstar = pi6 * cube(zdcstar)
+    act = []
+    for cb in range(lay.ncld):
+        ab = lay.in2a + cb
+        pn, pv = 0., [0.] * nw
+        vsol = sum(vol[ab][i] for i in sol)
+        if num[ab] < nlim or vsol < num[ab] * thvol or vol[ab][nw - 1] < num[ab] * thvol:
+            act.append((pn, pv))
+            continue
+        nmid = num[ab]
+        vwmid = sum(vol[ab][:nw]) / nmid
+        vmid = sum(vol[ab][:nd]) / nmid
+        vlo, vhi = vmid * rlo[ab], vmid * rhi[ab]
+        if ab in (lay.in1a, lay.in2b):
+            nim1, vim1, vlom1, vhim1 = nlim, vlo / 2., 0., vlo
+            vwim1 = vim1
+        else:
+            nim1 = num[ab - 1]
+            if nim1 > nlim:
+                vim1, vwim1 = sum(vol[ab - 1][:nd]) / nim1, sum(vol[ab - 1][:nw]) / nim1
+            else:
+                vim1 = vwim1 = pi6 * cube(lay.dmid[ab - 1])
+            vlom1, vhim1 = vim1 * rlo[ab - 1], vim1 * rhi[ab - 1]
+        if ab in (lay.fn2a, lay.fn2b):
+            nip1, vip1, vlop1, vhip1 = nlim, vhi + 0.5 * (vhi - vlo), vhi, vhi + (vhi - vlo)
+            vwip1 = vip1
+        else:
+            nip1 = num[ab + 1]
+            if nip1 > nlim:
+                vip1, vwip1 = sum(vol[ab + 1][:nd]) / nip1, sum(vol[ab + 1][:nw]) / nip1
+            else:
+                vip1 = vwip1 = pi6 * cube(lay.dmid[ab + 1])
+            vlop1, vhip1 = vip1 * rlo[ab + 1], vip1 * rhi[ab + 1]
+        vip1, vim1 = max(vhi, vip1), min(vlo, vim1)
+        zs1 = (vwmid - max(vwim1, 0.)) / (vmid - vim1)
+        zs2 = (max(vwip1, 0.) - vwmid) / (vip1 - vmid)
+        v01, v02 = vwmid - zs1 * vmid, vwmid - zs2 * vmid
+        vwlo, vwhi = max(v01 + zs1 * vlo, vlo), max(v02 + zs2 * vhi, vhi)
+        if zvcstar < vwlo and zvcstar < vwmid and zvcstar < vwhi:
+            vint1, vint2, rng_ = vlo, vhi, [True] * 4
+        elif zvcstar > vwlo and zvcstar > vwmid and zvcstar > vwhi:
+            vint1, vint2, rng_ = 999., 999., [False] * 4
+        else:
+            vcut = (zvcstar - v01) / zs1
+            vint1 = vlo if (vcut < vlo or vcut > vmid) else vcut
+            vcut = (zvcstar - v02) / zs2
+            vint2 = vmid if (vcut < vmid or vcut > vhi) else vcut
+            rng_ = [vwlo > zvcstar, vwmid > zvcstar, vwmid > zvcstar, vwhi > zvcstar]
+        dnim1, dnip1, dnmid = nim1 / (vhim1 - vlom1), nip1 / (vhip1 - vlop1), nmid / (vhi - vlo)
+        zs1 = (dnmid - dnim1) / (vmid - vim1)
+        zs2 = (dnip1 - dnmid) / (vip1 - vmid)
+        n01, n02 = dnmid - zs1 * vmid, dnmid - zs2 * vmid
+        nnorm = intg_n(zs1, n01, vlo, vmid) + intg_n(zs2, n02, vmid, vhi)
+        vnorm = intg_v(zs1, n01, vlo, vmid) + intg_v(zs2, n02, vmid, vhi)
+        nact, actvol = 0., 0.
+        for on, kk, cc, lo, hi in ((rng_[0], zs1, n01, vlo, vint1), (rng_[1], zs1, n01, vint1, vmid),
+                                   (rng_[2], zs2, n02, vmid, vint2), (rng_[3], zs2, n02, vint2, vhi)):
+            if on:
+                nact = nact + (nmid / nnorm) * intg_n(kk, cc, lo, hi)
+                actvol = actvol + (nmid * vmid / vnorm) * intg_v(kk, cc, lo, hi)
+        vact = [actvol * (vol[ab][s_] / (vmid * nmid)) for s_ in range(nw)]
+        act.append((min(nact, nmid), [min(x, y) for x, y in zip(vact, vol[ab][:nw])]))
+    for cb in range(lay.ncld):
+        ab = lay.in2a + cb
+        pn, pv = act[cb]
+        num[ab] = max(0., num[ab] - pn)
+        cnum[cb] = cnum[cb] + pn
+        for s_ in range(nw):
+            vol[ab][s_] = max(0., vol[ab][s_] - pv[s_])
+            cvol[cb][s_] = cvol[cb][s_] + pv[s_]
+    return num, vol, cnum, cvol
+
+
+def test_activation_matches_independent_restatement():
+    """lsactiv mode 1 alone: the oracle's aerosol and cloud bins after one step against
+    the restatement above, on the supersaturated cells of grid16x16x40 blocks."""
+    cfg = workload_config(4)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    cfg.lsactiv.sw, cfg.lsactiv.mode = 1, 1
+    inp = make_inputs("grid16x16x40", "cpu", X=4, Y=4, Z=4)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc = lay.nwet, lay.nbins, lay.ncld
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["naero"].shape[1:]
+    rho = lay.rholiq()
+    ma, mc = f["maero"].view(nw, nb, *sh), f["mcloud"].view(nw, nc, *sh)
+    ta, tc = out["maerot"].view(nw, nb, *sh), out["mcloudt"].view(nw, nc, *sh)
+    activated = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num = [float(f["naero"][b, j, i, k]) * dn for b in range(nb)]
+                vol = [[float(ma[s_, b, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for b in range(nb)]
+                cnum = [float(f["ncloud"][b, j, i, k]) * dn for b in range(nc)]
+                cvol = [[float(mc[s_, b, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for b in range(nc)]
+                S = float(f["rp"][j, i, k]) / float(f["rsl"][j, i, k])
+                n1, v1, c1, cv1 = act_interst_numpy(num, vol, cnum, cvol, float(f["temp"][j, i, k]), S, lay)
+                for b in range(nc):
+                    got = float(out["ncloudt"][b, j, i, k]) * dt * dn
+                    assert got == pytest.approx(c1[b] - cnum[b], rel=1e-10, abs=1e-14 * cnum[b] + 1e-300), b
+                    activated += c1[b] > cnum[b]
+                    for s_ in range(nw):
+                        got = float(tc[s_, b, j, i, k]) * dt * dn / rho[s_]
+                        assert got == pytest.approx(cv1[b][s_] - cvol[b][s_], rel=1e-10,
+                                                    abs=1e-14 * cvol[b][s_] + 1e-300), (b, s_)
+                for b in range(nb):
+                    got = float(out["naerot"][b, j, i, k]) * dt * dn
+                    assert got == pytest.approx(n1[b] - num[b], rel=1e-10, abs=1e-14 * num[b] + 1e-300), b
+    assert activated > 20
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
