@@ -107,7 +107,7 @@ def terminal_vel_numpy(d, rhop, rhoa, visc, beta):
     fit above, capped at 9.2 m/s."""
     grav, surfw0 = 9.81, 0.073
     if d <= 19e-6:
-        return d ** 2 * (rhop - rhoa) * grav * beta / (18. * visc)
+        return d * d * (rhop - rhoa) * grav * beta / (18. * visc)
     if d < 1.07e-3:
         nda = 4. / 3. * d ** 3. * grav * (rhop - rhoa) * rhoa / visc ** 2.
         x = math.log(nda)
@@ -154,7 +154,7 @@ def coagc_numpy(d1, m1, rho1, d2, m2, rho2, T, P, eddy=0.001):
     fm = math.sqrt(tva[0] ** 2 + tva[1] ** 2)
     rhoa = P / (rd * T)
     vkin = visc / rhoa
-    tv = [d * d * (r - rhoa) * grav * b / (18 * visc) for d, r, b in zip(diam, (rho1, rho2), beta)]
+    tv = [terminal_vel_numpy(d, r, rhoa, visc, b) for d, r, b in zip(diam, (rho1, rho2), beta)]
     lrg, sml = (0, 1) if d1 >= d2 else (1, 0)
     re = [d * v / vkin for d, v in zip(diam, tv)]
     sc = [vkin / f for f in df]
@@ -179,8 +179,6 @@ def test_coagc_matches_independent_restatement():
         k = lib().salsa_ref_coagc_pair(o.h, b1, b2, 1e6, d1, 1e6, d2, T, P)
         m1 = 1000. * PI6 * d1 ** 3
         m2 = 1000. * PI6 * d2 ** 3
-        if lay.phase[b2] == 3 and d2 > 19e-6:
-            continue
         kn = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
         assert k == pytest.approx(kn, rel=1e-12, abs=0.), (b1, b2)
 
@@ -1240,6 +1238,105 @@ def test_activation_matches_independent_restatement():
                     got = float(out["naerot"][b, j, i, k]) * dt * dn
                     assert got == pytest.approx(n1[b] - num[b], rel=1e-10, abs=1e-14 * num[b] + 1e-300), b
     assert activated > 20
+
+
+def coag_cloud_numpy(num, vol, lay, T, P, dt):
+    """Cloud self-collection (lscgcc alone, autoconversion off): buildKernelSelf over the
+    cloud bins (dlim 100 um; coagc's offset for equal mid diameters, the parallel a and
+    b bins included) and coag_cloud + applyCoag (mo_salsa_coagulation_processes.f90:
+    221-470, 539-559), restated: the a targets, then the b targets, each with the partner
+    ranges of the reference.  num[c], vol[c][s] of the cloud bins."""
+    nc, pi6, nlim = lay.ncld, 0.5235988, 1.
+    c0 = lay.nbins
+    num, vol = list(num), [list(v) for v in vol]
+    dmid = [lay.dmid[c0 + c] for c in range(nc)]
+    d = [min((sum(vol[c]) / num[c] / pi6) ** (1. / 3.), 100.e-6) if num[c] > nlim else dmid[c] for c in range(nc)]
+    K = [[0.] * nc for _ in range(nc)]
+    for mm in range(nc):
+        if num[mm] < nlim:
+            continue
+        for nn in range(mm, nc):
+            if num[nn] < nlim:
+                continue
+            d1, m1 = d[mm], 1000. * pi6 * d[mm] ** 3
+            d2, m2 = d[nn], 1000. * pi6 * d[nn] ** 3
+            if abs(dmid[mm] - dmid[nn]) / dmid[mm] < 1.e-2:
+                d1, m1 = 1.1 * d2, 1.33 * m2
+            K[mm][nn] = K[nn][mm] = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
+    ia, fa = 0, nc // 2 - 1
+    ib, fb = nc // 2, nc - 1
+
+    def update(kk, sinks, sources):
+        if num[kk] < nlim:
+            return
+        sink, self_ = 0., 0.5 * K[kk][kk] * num[kk]
+        for lo, hi in sinks:
+            for ll in range(lo, hi + 1):
+                sink = sink + K[kk][ll] * num[ll]
+        src = [0.] * len(vol[kk])
+        for lo, hi in sources:
+            for ll in range(lo, hi + 1):
+                for s_ in range(len(src)):
+                    src[s_] = src[s_] + K[ll][kk] * vol[ll][s_]
+        n = num[kk]
+        vol[kk] = [(vol[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(len(src))]
+        num[kk] = n / (1. + dt * (sink + self_))
+
+    for kk in range(ia, fa + 1):
+        xb = ib + (kk - ia)
+        update(kk, [(kk + 1, fa), (xb, fb)] if kk < fa else [], [(ia, kk - 1), (ib, xb)] if kk > ia else [])
+    for kk in range(ib, fb + 1):
+        xa = ia + (kk - ib)
+        update(kk, [(kk + 1, fb), (xa, fa)] if kk < fb else [], [(ib, kk - 1), (ia, xa)] if kk > ib else [])
+    num = [max(0., x) for x in num]
+    vol = [[max(0., x) for x in v] for v in vol]
+    return num, vol
+
+
+def test_cloud_coagulation_matches_independent_restatement():
+    """lscoag with cloud self-collection alone (autoconversion off): the oracle's cloud
+    numbers and volumes after one step against the restatement above, on the cloudy
+    cells of a grid256x256x128 block (droplets across the Stokes and Beard fall-speed
+    regimes)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgca", "lscgpc", "lscgpa", "lscgpp", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    cfg.lscgcc = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nc = lay.nwet, lay.ncld
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho = lay.rholiq()
+    mc, tc = f["mcloud"].view(nw, nc, *sh), out["mcloudt"].view(nw, nc, *sh)
+    cloudy = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num = [float(f["ncloud"][c, j, i, k]) * dn for c in range(nc)]
+                if not any(x > 1. for x in num):
+                    continue
+                cloudy += 1
+                vol = [[float(mc[s_, c, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for c in range(nc)]
+                n1, v1 = coag_cloud_numpy(num, vol, lay, float(f["temp"][j, i, k]), float(f["press"][j, i, k]), dt)
+                for c in range(nc):
+                    got = float(out["ncloudt"][c, j, i, k]) * dt * dn
+                    assert got == pytest.approx(n1[c] - num[c], rel=1e-9, abs=1e-14 * num[c] + 1e-300), c
+                    for s_ in range(nw):
+                        got = float(tc[s_, c, j, i, k]) * dt * dn / rho[s_]
+                        assert got == pytest.approx(v1[c][s_] - vol[c][s_], rel=1e-9,
+                                                    abs=1e-14 * vol[c][s_] + 1e-300), (c, s_)
+    assert cloudy >= 10
 
 
 def test_condensation_conserves_water():
