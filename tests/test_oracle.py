@@ -1339,6 +1339,105 @@ def test_cloud_coagulation_matches_independent_restatement():
     assert cloudy >= 10
 
 
+def coag_precp_numpy(num, vol, lay, T, P, dt):
+    """Precipitation self-collection (lscgpp alone): buildKernelSelf over the
+    precipitation bins (dlim 5 mm, prlim 1e-6), coag_precp with precipSelfCoag and
+    applyCoagPrecp (mo_salsa_coagulation_processes.f90:472-560, 563-603, 1588-1611),
+    restated: the self-collisions of a bin move to the next bin, the last bin keeps
+    them as a number sink."""
+    npr, pi6, nlim = lay.nprc, 0.5235988, 1.e-6
+    p0 = lay.nbins + lay.ncld
+    num, vol = list(num), [list(v) for v in vol]
+    dmid = [lay.dmid[p0 + c] for c in range(npr)]
+    d = [min((sum(vol[c]) / num[c] / pi6) ** (1. / 3.), 5.e-3) if num[c] > nlim else dmid[c] for c in range(npr)]
+    K = [[0.] * npr for _ in range(npr)]
+    for mm in range(npr):
+        if num[mm] < nlim:
+            continue
+        for nn in range(mm, npr):
+            if num[nn] < nlim:
+                continue
+            d1, m1 = d[mm], 1000. * pi6 * d[mm] ** 3
+            d2, m2 = d[nn], 1000. * pi6 * d[nn] ** 3
+            if abs(dmid[mm] - dmid[nn]) / dmid[mm] < 1.e-2:
+                d1, m1 = 1.1 * d2, 1.33 * m2
+            K[mm][nn] = K[nn][mm] = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
+    ns = len(vol[0])
+    for kk in range(npr):
+        if num[kk] < nlim:
+            continue
+        sink, self_, nslf, vslf = 0., 0., 0., [0.] * ns
+        if kk < npr - 1:
+            for ll in range(kk + 1, npr):
+                sink = sink + K[kk][ll] * num[ll]
+            vslf = [vol[kk][s_] * num[kk] * K[kk][kk] for s_ in range(ns)]
+            nslf = 0.5 * K[kk][kk] * num[kk] * num[kk]
+        else:
+            self_ = 0.5 * K[kk][kk] * num[kk]
+        src = [0.] * ns
+        for ll in range(kk):
+            for s_ in range(ns):
+                src[s_] = src[s_] + K[ll][kk] * vol[ll][s_]
+        n = num[kk]
+        vol[kk] = [(vol[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(ns)]
+        num[kk] = n / (1. + dt * (sink + self_))
+        if kk < npr - 1:
+            vol[kk + 1] = [vol[kk + 1][s_] + dt * vslf[s_] for s_ in range(ns)]
+            num[kk + 1] = num[kk + 1] + dt * nslf
+            vol[kk] = [vol[kk][s_] - dt * vslf[s_] for s_ in range(ns)]
+            num[kk] = num[kk] - dt * nslf
+    num = [max(0., x) for x in num]
+    vol = [[max(0., x) for x in v] for v in vol]
+    return num, vol
+
+
+def test_precipitation_coagulation_matches_independent_restatement():
+    """lscoag with precipitation self-collection alone: the oracle's precipitation
+    numbers and volumes after one step against the restatement above, for drops in
+    every fall-speed regime (the number of drops raised so that collisions count)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgca", "lscgcc", "lscgpc", "lscgpa", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    cfg.lscgpp = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, npr = lay.nwet, lay.nprc
+    f = inp.fields
+    f["nprecp"] *= 1.e3
+    f["mprecp"] *= 1.e3
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["nprecp"].shape[1:]
+    rho = lay.rholiq()
+    mp, tp = f["mprecp"].view(nw, npr, *sh), out["mprecpt"].view(nw, npr, *sh)
+    rainy = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num = [float(f["nprecp"][c, j, i, k]) * dn for c in range(npr)]
+                if not any(x > 1.e-6 for x in num):
+                    continue
+                rainy += 1
+                vol = [[float(mp[s_, c, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for c in range(npr)]
+                n1, v1 = coag_precp_numpy(num, vol, lay, float(f["temp"][j, i, k]), float(f["press"][j, i, k]), dt)
+                for c in range(npr):
+                    got = float(out["nprecpt"][c, j, i, k]) * dt * dn
+                    assert got == pytest.approx(n1[c] - num[c], rel=1e-9, abs=1e-14 * num[c] + 1e-300), c
+                    for s_ in range(nw):
+                        got = float(tp[s_, c, j, i, k]) * dt * dn / rho[s_]
+                        assert got == pytest.approx(v1[c][s_] - vol[c][s_], rel=1e-9,
+                                                    abs=1e-14 * vol[c][s_] + 1e-300), (c, s_)
+    assert rainy >= 10
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
