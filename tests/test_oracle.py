@@ -1438,6 +1438,150 @@ def test_precipitation_coagulation_matches_independent_restatement():
     assert rainy >= 10
 
 
+def coag_cloud_autoconv_numpy(num, vol, pnum, pvol, lay, T, P, dt):
+    """Cloud self-collection with autoconversion by collisions (lscgcc with lsauto
+    mode 1): coag_cloud with accumulatePrecipFormation and applyCoagPrecipFormation
+    (mo_salsa_coagulation_processes.f90:221-470, 654-702, 1457-1584), restated: a
+    collision whose coalesced drop exceeds the first precipitation bin's lower diameter
+    moves to the precipitation bin of that size, with the reference's limiter fix_coag;
+    the other collisions are ordinary coagulation."""
+    nc, npr, pi6, nlim = lay.ncld, lay.nprc, 0.5235988, 1.
+    c0, p0 = lay.nbins, lay.nbins + lay.ncld
+    num, vol, pnum, pvol = list(num), [list(v) for v in vol], list(pnum), [list(v) for v in pvol]
+    ns = len(vol[0])
+    dmid = [lay.dmid[c0 + c] for c in range(nc)]
+    d = [min((sum(vol[c]) / num[c] / pi6) ** (1. / 3.), 100.e-6) if num[c] > nlim else dmid[c] for c in range(nc)]
+    pbins = [(lay.vlolim[p0 + c] / pi6) ** (1. / 3.) for c in range(npr)]
+    K = [[0.] * nc for _ in range(nc)]
+    for mm in range(nc):
+        if num[mm] < nlim:
+            continue
+        for nn in range(mm, nc):
+            if num[nn] < nlim:
+                continue
+            d1, m1 = d[mm], 1000. * pi6 * d[mm] ** 3
+            d2, m2 = d[nn], 1000. * pi6 * d[nn] ** 3
+            if abs(dmid[mm] - dmid[nn]) / dmid[mm] < 1.e-2:
+                d1, m1 = 1.1 * d2, 1.33 * m2
+            K[mm][nn] = K[nn][mm] = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
+    ia, fa, ib, fb = 0, nc // 2 - 1, nc // 2, nc - 1
+
+    def formation(t, lo, hi, fix, acc):
+        selfc = (t == lo and t == hi)
+        for ll in range(lo, hi + 1):
+            dn_ = (d[t] * d[t] * d[t] + d[ll] * d[ll] * d[ll]) ** (1. / 3.)
+            tp = sum(1 for x in pbins if dn_ > x) - 1
+            if dn_ > pbins[0]:
+                if selfc:
+                    dv = [vol[ll][s_] * num[t] * K[ll][t] * fix for s_ in range(ns)]
+                    dnum = (0.5 * K[ll][t] * num[ll] * num[t]) * fix
+                    acc["vslf"] = [x + vol[ll][s_] * num[t] * K[ll][t] * fix for s_, x in enumerate(acc["vslf"])]
+                    acc["self"] += 0.5 * K[ll][t] * num[t]
+                else:
+                    dv = [(vol[ll][s_] * num[t] + vol[t][s_] * num[ll]) * K[ll][t] * fix for s_ in range(ns)]
+                    dnum = (K[ll][t] * num[ll] * num[t]) * fix
+                    acc["sink"] += K[t][ll] * num[ll]
+                acc["vprc"][tp] = [x + y for x, y in zip(acc["vprc"][tp], dv)]
+                acc["nprc"][tp] += dnum
+            elif selfc:
+                acc["self"] += 0.5 * K[t][ll] * num[ll]
+            else:
+                acc["src"] = [x + K[ll][t] * vol[ll][s_] for s_, x in enumerate(acc["src"])]
+
+    def update(kk, own_lo, own_hi, oth_lo, oth_hi, par):
+        if num[kk] < nlim:
+            return
+        acc = dict(sink=0., self=0., src=[0.] * ns, vslf=[0.] * ns, vprc=[[0.] * ns for _ in range(npr)],
+                   nprc=[0.] * npr)
+        if kk < own_hi:
+            for ll in range(kk + 1, own_hi + 1):
+                acc["sink"] += K[kk][ll] * num[ll]
+            for ll in range(par, oth_hi + 1):
+                acc["sink"] += K[kk][ll] * num[ll]
+        fix = max(1. - dt * (0.5 * K[kk][kk] * num[kk] ** 2 / (num[kk])), 0.1)
+        formation(kk, kk, kk, fix, acc)
+        if kk > own_lo:
+            fix = max(1. - dt * sum(K[kk][l] * num[l] for l in range(own_lo, own_hi + 1)), 0.1)
+            formation(kk, own_lo, kk - 1, fix, acc)
+            fix = max(1. - dt * sum(K[kk][l] * num[l] for l in range(oth_lo, oth_hi + 1)), 0.1)
+            formation(kk, oth_lo, par, fix, acc)
+        n = num[kk]
+        vol[kk] = [(vol[kk][s_] + dt * acc["src"][s_] * n) / (1. + dt * acc["sink"]) for s_ in range(ns)]
+        num[kk] = n / (1. + dt * (acc["sink"] + acc["self"]))
+        vol[kk] = [vol[kk][s_] - dt * acc["vslf"][s_] for s_ in range(ns)]
+        for cc in range(npr):
+            pvol[cc] = [pvol[cc][s_] + dt * acc["vprc"][cc][s_] for s_ in range(ns)]
+            pnum[cc] = pnum[cc] + dt * acc["nprc"][cc]
+
+    for kk in range(ia, fa + 1):
+        update(kk, ia, fa, ib, fb, ib + (kk - ia))
+    for kk in range(ib, fb + 1):
+        update(kk, ib, fb, ia, fa, ia + (kk - ib))
+    num = [max(0., x) for x in num]
+    vol = [[max(0., x) for x in v] for v in vol]
+    return num, vol, pnum, pvol
+
+
+def test_autoconversion_by_collisions_matches_independent_restatement():
+    """lscgcc with lsauto mode 1: the oracle's cloud and precipitation bins after one
+    step against the restatement above, on the cloudy cells of a grid256x256x128 block
+    with large drops (the number of the largest cloud drops raised so that
+    precipitation forms)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsauto.sw, cfg.lsauto.mode = 1, 1
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgca", "lscgpc", "lscgpa", "lscgpp", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    cfg.lscgcc = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nc, npr = lay.nwet, lay.ncld, lay.nprc
+    f = inp.fields
+    f["ncloud"] *= 30.
+    f["mcloud"] *= 30.
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho = lay.rholiq()
+    mc, tc = f["mcloud"].view(nw, nc, *sh), out["mcloudt"].view(nw, nc, *sh)
+    mp, tp = f["mprecp"].view(nw, npr, *sh), out["mprecpt"].view(nw, npr, *sh)
+    formed = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num = [float(f["ncloud"][c, j, i, k]) * dn for c in range(nc)]
+                if not any(x > 1. for x in num):
+                    continue
+                vol = [[float(mc[s_, c, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for c in range(nc)]
+                pnum = [float(f["nprecp"][c, j, i, k]) * dn for c in range(npr)]
+                pvol = [[float(mp[s_, c, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for c in range(npr)]
+                n1, v1, pn1, pv1 = coag_cloud_autoconv_numpy(num, vol, pnum, pvol, lay, float(f["temp"][j, i, k]),
+                                                             float(f["press"][j, i, k]), dt)
+                formed += sum(1 for a_, b_ in zip(pn1, pnum) if a_ > b_)
+                for c in range(nc):
+                    got = float(out["ncloudt"][c, j, i, k]) * dt * dn
+                    assert got == pytest.approx(n1[c] - num[c], rel=1e-9, abs=1e-14 * num[c] + 1e-300), c
+                    for s_ in range(nw):
+                        got = float(tc[s_, c, j, i, k]) * dt * dn / rho[s_]
+                        assert got == pytest.approx(v1[c][s_] - vol[c][s_], rel=1e-9,
+                                                    abs=1e-14 * vol[c][s_] + 1e-300), (c, s_)
+                for c in range(npr):
+                    got = float(out["nprecpt"][c, j, i, k]) * dt * dn
+                    assert got == pytest.approx(pn1[c] - pnum[c], rel=1e-9, abs=1e-14 * pnum[c] + 1e-300), c
+                    for s_ in range(nw):
+                        got = float(tp[s_, c, j, i, k]) * dt * dn / rho[s_]
+                        assert got == pytest.approx(pv1[c][s_] - pvol[c][s_], rel=1e-9,
+                                                    abs=1e-14 * pvol[c][s_] + 1e-300), ("p", c, s_)
+    assert formed >= 10
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
