@@ -1582,6 +1582,136 @@ def test_autoconversion_by_collisions_matches_independent_restatement():
     assert formed >= 10
 
 
+def coag_aero_cloud_numpy(anum, avol, cnum, cvol, lay, T, P, dt):
+    """Collisions of aerosol with cloud drops alone (lscgca): buildKernel(aero, cloud)
+    and the aerosol-cloud parts of coag_aero and coag_cloud with accumulateSink /
+    accumulateSource and their reversed forms (mo_salsa_coagulation_processes.f90:
+    24-470, 1023-1045, 1219-1242), restated: every aerosol target first, against the
+    cloud state before the step, then every cloud target against the updated aerosol."""
+    nb, nc, pi6, nlim = lay.nbins, lay.ncld, 0.5235988, 1.
+    c0 = lay.nbins
+    anum, avol, cnum, cvol = list(anum), [list(v) for v in avol], list(cnum), [list(v) for v in cvol]
+    ns = len(avol[0])
+    admid, cdmid = lay.dmid[:nb], [lay.dmid[c0 + c] for c in range(nc)]
+    da = [min((sum(avol[k]) / anum[k] / pi6) ** (1. / 3.), 30.e-6) if anum[k] > nlim else admid[k] for k in range(nb)]
+    dc = [min((sum(cvol[c]) / cnum[c] / pi6) ** (1. / 3.), 100.e-6) if cnum[c] > nlim else cdmid[c] for c in range(nc)]
+    K = [[0.] * nc for _ in range(nb)]
+    for mm in range(nb):
+        if anum[mm] < nlim:
+            continue
+        for nn in range(nc):
+            if cnum[nn] < nlim:
+                continue
+            d1, m1 = da[mm], 1000. * pi6 * da[mm] ** 3
+            d2, m2 = dc[nn], 1000. * pi6 * dc[nn] ** 3
+            if abs(admid[mm] - cdmid[nn]) / admid[mm] < 1.e-2:
+                d1, m1 = 1.1 * d2, 1.33 * m2
+            K[mm][nn] = coagc_numpy(d1, m1, 1000., d2, m2, 1000., T, P)
+    ica, fca, icb, fcb = 0, nc // 2 - 1, nc // 2, nc - 1
+    ipa, ipb = lay.in2a, lay.in2b
+
+    def apply(n, v, sink, src):
+        return [(v[s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(ns)], n / (1. + dt * sink)
+
+    for kk in range(lay.in1a, lay.fn2b + 1):
+        if anum[kk] < nlim:
+            continue
+        par = ipb if kk >= lay.in2b else ipa
+        if kk >= lay.in2b:
+            xa, xb = ica + max(kk - par, 0), icb + max(kk - par, 0)
+        elif kk >= lay.in2a:
+            xa, xb = ica + max(kk - par, 0), icb + max(kk - par, 0)
+        else:
+            xa = ica + max(kk - ipa, 0)
+            xb = icb + (xa - ica)
+        sink = 0.
+        for lo, hi in ((xa, fca), (xb, fcb)):
+            for ll in range(lo, hi + 1):
+                sink = sink + K[kk][ll] * cnum[ll]
+        if kk >= lay.in2b:
+            sb = icb + (kk - ipb) - 1
+            sa = ica + (sb - icb)
+        else:
+            sa = ica + (kk - ipa) - 1
+            sb = icb + (sa - ica)
+        src = [0.] * ns
+        for lo, hi, ok in ((ica, sa, sa >= ica), (icb, sb, sb >= icb)):
+            if ok:
+                for ll in range(lo, hi + 1):
+                    src = [x + K[kk][ll] * cvol[ll][s_] for s_, x in enumerate(src)]
+        avol[kk], anum[kk] = apply(anum[kk], avol[kk], sink, src)
+    for kk in range(nc):
+        if cnum[kk] < nlim:
+            continue
+        off = kk - ica if kk <= fca else kk - icb
+        last = fca if kk <= fca else fcb
+        sink = 0.
+        if kk < last:
+            for lo, hi in ((ipa + off + 1, lay.fn2a), (ipb + off + 1, lay.fn2b)):
+                for ll in range(lo, hi + 1):
+                    sink = sink + K[ll][kk] * anum[ll]
+        src = [0.] * ns
+        for lo, hi in ((lay.in1a, ipa + off), (lay.in2b, ipb + off)):
+            for ll in range(lo, hi + 1):
+                src = [x + K[ll][kk] * avol[ll][s_] for s_, x in enumerate(src)]
+        cvol[kk], cnum[kk] = apply(cnum[kk], cvol[kk], sink, src)
+    return ([max(0., x) for x in anum], [[max(0., x) for x in v] for v in avol],
+            [max(0., x) for x in cnum], [[max(0., x) for x in v] for v in cvol])
+
+
+def test_aerosol_cloud_coagulation_matches_independent_restatement():
+    """lscoag with aerosol-cloud collisions alone: the oracle's aerosol and cloud bins
+    after one step against the restatement above, on the cloudy cells of a
+    grid256x256x128 block (drop numbers raised so that scavenging counts)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgcc", "lscgpc", "lscgpa", "lscgpp", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    cfg.lscgca = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc = lay.nwet, lay.nbins, lay.ncld
+    f = inp.fields
+    f["ncloud"] *= 100.
+    f["mcloud"] *= 100.
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho = lay.rholiq()
+    ma, ta = f["maero"].view(nw, nb, *sh), out["maerot"].view(nw, nb, *sh)
+    mc, tc = f["mcloud"].view(nw, nc, *sh), out["mcloudt"].view(nw, nc, *sh)
+    cloudy = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                cnum = [float(f["ncloud"][c, j, i, k]) * dn for c in range(nc)]
+                if not any(x > 1. for x in cnum):
+                    continue
+                cloudy += 1
+                cvol = [[float(mc[s_, c, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for c in range(nc)]
+                anum = [float(f["naero"][b, j, i, k]) * dn for b in range(nb)]
+                avol = [[float(ma[s_, b, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for b in range(nb)]
+                a1, av1, c1, cv1 = coag_aero_cloud_numpy(anum, avol, cnum, cvol, lay, float(f["temp"][j, i, k]),
+                                                         float(f["press"][j, i, k]), dt)
+                for tag, n0, n1, v0, v1, tn, tv, nbn in (("a", anum, a1, avol, av1, out["naerot"], ta, nb),
+                                                         ("c", cnum, c1, cvol, cv1, out["ncloudt"], tc, nc)):
+                    for b in range(nbn):
+                        got = float(tn[b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * n0[b] + 1e-300), (tag, b)
+                        for s_ in range(nw):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rho[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * v0[b][s_] + 1e-300), (tag, b, s_)
+    assert cloudy >= 10
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
