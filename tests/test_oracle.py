@@ -1712,6 +1712,117 @@ def test_aerosol_cloud_coagulation_matches_independent_restatement():
     assert cloudy >= 10
 
 
+def accretion_numpy(anum, avol, cnum, cvol, pnum, pvol, lay, T, P, dt):
+    """Precipitation collecting aerosol and cloud alone (lscgpa, lscgpc): buildKernel
+    for (aerosol, precipitation) and (cloud, precipitation), then the precipitation
+    targets (coag_precp, sources from every aerosol and cloud bin as they stand before
+    their own update), the aerosol targets and the cloud targets (sinks against the
+    precipitation numbers), restated from mo_salsa_coagulation_processes.f90:24-560."""
+    nb, nc, npr, pi6 = lay.nbins, lay.ncld, lay.nprc, 0.5235988
+    c0, p0 = lay.nbins, lay.nbins + lay.ncld
+    anum, avol, cnum, cvol = list(anum), [list(v) for v in avol], list(cnum), [list(v) for v in cvol]
+    pnum, pvol = list(pnum), [list(v) for v in pvol]
+    ns = len(avol[0])
+
+    def diam(n, v, dmid, dlim, nlim):
+        return min((sum(v) / n / pi6) ** (1. / 3.), dlim) if n > nlim else dmid
+    da = [diam(anum[k], avol[k], lay.dmid[k], 30.e-6, 1.) for k in range(nb)]
+    dc = [diam(cnum[k], cvol[k], lay.dmid[c0 + k], 100.e-6, 1.) for k in range(nc)]
+    dp = [diam(pnum[k], pvol[k], lay.dmid[p0 + k], 5.e-3, 1.e-6) for k in range(npr)]
+
+    def kernels(n1, d1_, dm1, nl1, n2, d2_, dm2, nl2):
+        K = [[0.] * len(n2) for _ in range(len(n1))]
+        for mm in range(len(n1)):
+            if n1[mm] < nl1:
+                continue
+            for nn in range(len(n2)):
+                if n2[nn] < nl2:
+                    continue
+                a1, m1 = d1_[mm], 1000. * pi6 * d1_[mm] ** 3
+                a2, m2 = d2_[nn], 1000. * pi6 * d2_[nn] ** 3
+                if abs(dm1[mm] - dm2[nn]) / dm1[mm] < 1.e-2:
+                    a1, m1 = 1.1 * a2, 1.33 * m2
+                K[mm][nn] = coagc_numpy(a1, m1, 1000., a2, m2, 1000., T, P)
+        return K
+    Kap = kernels(anum, da, lay.dmid[:nb], 1., pnum, dp, lay.dmid[p0:p0 + npr], 1.e-6)
+    Kcp = kernels(cnum, dc, lay.dmid[c0:c0 + nc], 1., pnum, dp, lay.dmid[p0:p0 + npr], 1.e-6)
+    for kk in range(npr):
+        if pnum[kk] < 1.e-6:
+            continue
+        src = [0.] * ns
+        for ll in range(nb):
+            src = [x + Kap[ll][kk] * avol[ll][s_] for s_, x in enumerate(src)]
+        for ll in range(nc):
+            src = [x + Kcp[ll][kk] * cvol[ll][s_] for s_, x in enumerate(src)]
+        n = pnum[kk]
+        pvol[kk] = [(pvol[kk][s_] + dt * src[s_] * n) / (1. + dt * 0.) for s_ in range(ns)]
+        pnum[kk] = n / (1. + dt * (0. + 0.))
+    for nums, vols, Kxp in ((anum, avol, Kap), (cnum, cvol, Kcp)):
+        for kk in range(len(nums)):
+            if nums[kk] < 1.:
+                continue
+            sink = 0.
+            for ll in range(npr):
+                sink = sink + Kxp[kk][ll] * pnum[ll]
+            n = nums[kk]
+            vols[kk] = [vols[kk][s_] / (1. + dt * sink) for s_ in range(ns)]
+            nums[kk] = n / (1. + dt * sink)
+    return anum, avol, cnum, cvol, pnum, pvol
+
+
+def test_accretion_matches_independent_restatement():
+    """lscoag with precipitation collecting aerosol and cloud alone: the oracle's
+    aerosol, cloud and precipitation bins after one step against the restatement
+    above, on the cloudy cells of a grid256x256x128 block (drop numbers raised)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgca", "lscgcc", "lscgpp", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 0)
+    cfg.lscgpa = cfg.lscgpc = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc, npr = lay.nwet, lay.nbins, lay.ncld, lay.nprc
+    f = inp.fields
+    f["nprecp"] *= 1.e3
+    f["mprecp"] *= 1.e3
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho = lay.rholiq()
+    cats = [("naero", "maero", nb), ("ncloud", "mcloud", nc), ("nprecp", "mprecp", npr)]
+    rainy = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                state = []
+                for nk, mk, nbn in cats:
+                    mv = f[mk].view(nw, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rho[s_] for s_ in range(nw)] for b in range(nbn)])
+                if not any(x > 1.e-6 for x in state[4]):
+                    continue
+                rainy += 1
+                new = accretion_numpy(*state, lay, float(f["temp"][j, i, k]), float(f["press"][j, i, k]), dt)
+                for q, (nk, mk, nbn) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nw, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * n0[b] + 1e-300), (nk, b)
+                        for s_ in range(nw):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rho[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * v0[b][s_] + 1e-300), (mk, b, s_)
+    assert rainy >= 10
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
