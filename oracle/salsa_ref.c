@@ -529,6 +529,31 @@ double salsa_ref_coagc_pair(const salsa_ref_ctx_t *c, int b1, int b2, double num
   return coagc(c, &s1, &s2, temp, pres, 0);
 }
 
+/* single-function probe of coagc for two bins given their number concentrations and
+   the volume concentrations of all c->nused species (dry, water, then rime for ice),
+   with the diameters and mean densities updated as buildKernel updates them */
+double salsa_ref_coagc_sections(const salsa_ref_ctx_t *c, int b1, double numc1, const double *volc1, int b2,
+                                double numc2, const double *volc2, double temp, double pres) {
+  Section s1 = c->tmpl[b1], s2 = c->tmpl[b2];
+  s1.numc = numc1; s2.numc = numc2;
+  for (int i = 0; i < NSP; i++) {
+    s1.volc[i] = i < c->nused ? volc1[i] : 0.;
+    s2.volc[i] = i < c->nused ? volc2[i] : 0.;
+  }
+  updateDiameter(c, &s1, 1, T_ALL); updateRhomean(c, &s1);
+  updateDiameter(c, &s2, 1, T_ALL); updateRhomean(c, &s2);
+  return coagc(c, &s1, &s2, temp, pres, 0);
+}
+
+/* single-function probe of getShapeCoefficients and getDiameter for primary ice mass
+   mpri, rime mass mrim and number numc: out = alpha, beta, gamma, sigma, diameter */
+void salsa_ref_ice_shape(const salsa_ref_ctx_t *c, double mpri, double mrim, double numc, double out[5]) {
+  Shape s;
+  getShapeCoefficients(c, &s, mpri, mrim, numc);
+  out[0] = s.alpha; out[1] = s.beta; out[2] = s.gamma; out[3] = s.sigma;
+  out[4] = getDiameter(c, mpri, mrim, numc);
+}
+
 /* ======================================================================
  * Coagulation processes: mo_salsa_coagulation_processes.f90
  * Kernel access helpers follow the dummy-argument shapes of the reference:

@@ -75,6 +75,11 @@ double salsa_ref_terminal_vel(double diam, double rhop, double rhoa, double visc
 double salsa_ref_coagc_pair(const salsa_ref_ctx_t *ctx, int b1, int b2,
                             double numc1, double dwet1, double numc2,
                             double dwet2, double temp, double pres);
+double salsa_ref_coagc_sections(const salsa_ref_ctx_t *ctx, int b1, double numc1,
+                                const double *volc1, int b2, double numc2,
+                                const double *volc2, double temp, double pres);
+void salsa_ref_ice_shape(const salsa_ref_ctx_t *ctx, double mpri, double mrim, double numc,
+                         double out[5]);
 double salsa_ref_nucleation_rate(const salsa_ref_ctx_t *ctx, int kind, double theta,
                                  double Tk, double Din, double S);
 double salsa_ref_freezing_fraction(const salsa_ref_ctx_t *ctx, int mode, double Tk, double S,

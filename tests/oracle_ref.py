@@ -47,6 +47,10 @@ def lib(variant="plain"):
         L.salsa_ref_sweq.restype = C.c_double
         L.salsa_ref_coagc_pair.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 6
         L.salsa_ref_coagc_pair.restype = C.c_double
+        L.salsa_ref_coagc_sections.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.c_int,
+                                               C.c_double, C.POINTER(C.c_double), C.c_double, C.c_double]
+        L.salsa_ref_coagc_sections.restype = C.c_double
+        L.salsa_ref_ice_shape.argtypes = [C.c_void_p] + [C.c_double] * 3 + [C.POINTER(C.c_double * 5)]
         L.salsa_ref_tend_constrain.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                                C.POINTER(PostFields)]
         L.salsa_ref_tend_constrain.restype = C.c_int

@@ -183,6 +183,199 @@ def test_coagc_matches_independent_restatement():
         assert k == pytest.approx(kn, rel=1e-12, abs=0.), (b1, b2)
 
 
+RHO_IC, RHO_RI = 917., 400.
+ICE_A, ICE_B, ICE_G, ICE_S = 15.56999e-3, 2.02, 0.55, 1.97
+
+
+def ice_shape_numpy(mpri, mrim, numc):
+    """Independent restatement of getShapeCoefficients and getDiameter
+    (src/src_shared/mo_ice_shape.f90:46-91, 104-141, 145-191) for the default
+    Khvorostyanov-Curry crystal coefficients: returns (alpha, beta, gamma, sigma), the
+    maximum dimension and the regime (0 spherical ice, 1 dense non-spherical, 2 graupel,
+    3 partially rimed).  The rime fraction is clipped to [1e-4, 0.9999] and the bulk
+    density is rime-weighted, so the regime limits move with the rime fraction."""
+    pi, pi6 = 3.1415927, 0.5235988
+    sph = (pi6 * RHO_IC, 3., pi / 4., 2.)
+    if numc < 1.e-6:
+        return sph, 1.e-9, -1
+    m = (mpri + mrim) / numc                              # mass of one particle
+    fr = max(min(mrim / (m * numc), 0.9999), 0.0001)
+    rho_b = fr * RHO_RI + (1. - fr) * RHO_IC
+    # m = alpha D^beta meets the spheres of density rhoic, rho_b, rho_b/(1-fr)
+    d_th = (pi6 * RHO_IC / ICE_A) ** (1. / (ICE_B - 3.))
+    d_gr = (ICE_A / (pi6 * rho_b)) ** (1. / (3. - ICE_B))
+    d_cr = (ICE_A / (1. - fr) / (pi6 * rho_b)) ** (1. / (3. - ICE_B))
+    m_th = RHO_IC * pi6 * d_th * d_th * d_th
+    m_gr = rho_b * pi6 * d_gr * d_gr * d_gr
+    m_cr = rho_b * pi6 * d_cr * d_cr * d_cr
+    if m < m_th:
+        return sph, (m / (pi6 * RHO_IC)) ** (1. / 3.), 0
+    if m < m_gr:
+        return (ICE_A, ICE_B, ICE_G, ICE_S), (m / ICE_A) ** (1. / ICE_B), 1
+    if m < m_cr:
+        return sph, (m / (pi6 * rho_b)) ** (1. / 3.), 2
+    coeffs = sph if m == m_cr else (ICE_A / (1. - fr), ICE_B, ICE_G * (1. - fr) + pi / 4. * fr,
+                                    ICE_S * (1. - fr) + 2. * fr)
+    return coeffs, (m * (1. - fr) / ICE_A) ** (1. / ICE_B), 3
+
+
+def ice_terminal_vel_numpy(dsph, dmax, rhop, rhoa, visc, shape):
+    """Independent restatement of the ice branch of terminal_vel
+    (src/src_shared/mo_particle_external_properties.f90:88-96, 103-158): the power law
+    V = A_v D^B_v of Khvorostyanov and Curry (2002) eqs. 2.12-2.13 and 2.23-2.25, with the
+    Best number X formed from the spherical-equivalent volume and the area gamma D^sigma
+    of the maximum dimension D."""
+    grav, c1, delta0 = 9.81, 0.0902, 9.06
+    alpha, beta, gamma, sigma = shape
+    vb = 0.5235988 * dsph * dsph * dsph
+    area = gamma * dmax ** sigma
+    x = 2. * vb * (rhop - rhoa) * grav * dmax * dmax / (area * rhoa * visc * visc)
+    s = math.sqrt(1. + c1 * math.sqrt(x))
+    b_re = 0.5 * c1 * math.sqrt(x) / ((s - 1.) * s)
+    a_re = 0.25 * delta0 * delta0 * (s - 1.) * (s - 1.) / x ** b_re
+    a_v = a_re * visc ** (1. - 2. * b_re) * (2. * alpha * grav / (rhoa * gamma)) ** b_re
+    b_v = b_re * (beta - sigma + 2.) - 1.
+    return a_v * dmax ** b_v
+
+
+def particle_numpy(lay, b, numc, volc):
+    """The properties coagc reads from a bin after buildKernel's updateDiameter(limit)
+    and updateRhomean (src/src_salsa/classSection.f90:91-195): kernel diameter,
+    spherical diameter, mean density and, for ice, the shape coefficients from the
+    primary (all species but rime, at ice density) and rime masses."""
+    pi6 = 0.5235988
+    phase = lay.phase[b]
+    dlim = {1: 30.e-6, 2: 100.e-6, 3: 5.e-3, 4: 10.e-3}[phase]
+    nlim = 1.0 if phase < 3 else 1.e-6
+    dwet = (sum(volc) / numc / pi6) ** (1. / 3.) if numc > nlim else lay.dmid[b]
+    dwet = min(dwet, dlim)
+    p = dict(dmid=lay.dmid[b], d=dwet, dsph=dwet, rho=1000., shape=None)
+    if phase == 4:
+        mp, mr = RHO_IC * volc[-2], RHO_RI * volc[-1]      # water (ice) and rime
+        p["rho"] = min((mp * RHO_IC + mr * RHO_RI) / max(mp + mr, 7.e-25), RHO_IC) if numc > nlim else RHO_IC
+        p["shape"] = ice_shape_numpy(sum(volc[:-1]) * RHO_IC, volc[-1] * RHO_RI, numc)[0]
+    p["m"] = p["rho"] * pi6 * dwet * dwet * dwet
+    return p
+
+
+def coagc_particles_numpy(p1, p2, T, P, eddy=0.001):
+    """Independent restatement of mo_salsa_coagulation_kernels.f90:263-407 for any two
+    categories (no charge): the liquid restatement above with the ice fall speed and the
+    offset a pair of equal bins gets (kernel diameter 1.1x, mass 1.33x the partner's,
+    the spherical diameter of the first particle kept for its fall speed).  Returns the
+    kernel, the Stokes number and the larger particle's Reynolds number."""
+    pi, boltz, grav, rd, pstand = 3.1415927, 1.3807e-23, 9.81, 287.04, 1.01325e5
+    d = [p1["d"], p2["d"]]
+    mp = [p1["m"], p2["m"]]
+    if abs(p1["dmid"] - p2["dmid"]) / p1["dmid"] < 1.e-2:
+        d[0], mp[0] = 1.1 * d[1], 1.33 * mp[1]
+    visc = (7.44523e-3 * math.sqrt(T * T * T)) / (5093. * (T + 110.4))
+    mfp = (1.656e-10 * T + 1.828e-8) * pstand / P
+    knud = [2 * mfp / x for x in d]
+    beta = [1 + k * (1.142 + 0.558 * math.exp(-0.999 / k)) for k in knud]
+    df = [b * boltz * T / (3 * pi * visc * x) for b, x in zip(beta, d)]
+    mt = [math.sqrt(8 * boltz * T / (pi * m)) for m in mp]
+    om = [8 * f / (pi * v) for f, v in zip(df, mt)]
+    md = 0.5 * (d[0] + d[1])
+    f1 = 4 * pi * md * (df[0] + df[1])
+    f2 = pi * math.sqrt(mt[0] ** 2 + mt[1] ** 2) * md ** 2
+    tva = [((md + o) ** 3 - (md ** 2 + o ** 2) * math.sqrt(md ** 2 + o ** 2)) / (3 * md * o) - md for o in om]
+    fm = math.sqrt(tva[0] ** 2 + tva[1] ** 2)
+    rhoa = P / (rd * T)
+    vkin = visc / rhoa
+    tv = []
+    for p, x, b in zip((p1, p2), d, beta):
+        if p["shape"] is None:
+            tv.append(terminal_vel_numpy(x, p["rho"], rhoa, visc, b))
+        else:
+            tv.append(ice_terminal_vel_numpy(p["dsph"], x, p["rho"], rhoa, visc, p["shape"]))
+    lrg, sml = (0, 1) if d[0] >= d[1] else (1, 0)
+    re = [x * v / vkin for x, v in zip(d, tv)]
+    sc = [vkin / f for f in df]
+    dv = abs(tv[0] - tv[1])
+    stok = 2 * tv[sml] * dv / (d[lrg] * grav)
+    zb = f1 / (md / (md + fm) + f1 / f2)
+    zc = 0.45 * zb * (re[lrg] * sc[sml]) ** (1 / 3) if re[lrg] <= 1 else 0.45 * zb * math.sqrt(re[lrg]) * sc[sml] ** (1 / 3)
+    ts = math.sqrt(8 * pi * eddy / (15 * vkin)) * md ** 3
+    ti = pi * eddy ** 0.75 / (grav * math.sqrt(math.sqrt(vkin))) * md ** 2 * dv
+    zea = stok ** 2 / (stok + 0.5) ** 2
+    zev = (1 + 0.75 * math.log(2 * stok) / (stok - 1.214)) ** -2 if stok > 1.214 else 0.
+    ze = (60 * zev + zea * re[lrg]) / (60 + re[lrg])
+    zg = ze * pi * md ** 2 * dv
+    return zb + zc + math.sqrt(zg ** 2 + ts ** 2 + ti ** 2), stok, re[lrg]
+
+
+def test_ice_shape_matches_independent_restatement():
+    """The oracle's getShapeCoefficients and getDiameter against the restatement above,
+    over four decades of particle mass on both sides of every regime limit, rime
+    fractions from none to all (clipped to [1e-4, 0.9999]) and a number below the 1e-6
+    floor; every regime is visited."""
+    o = Oracle(workload_config(5))
+    out = (C.c_double * 5)()
+    seen = set()
+    for m in np.geomspace(1.e-14, 1.e-6, 241):
+        for fr in (0., 1.e-5, 0.02, 0.3, 0.7, 0.95, 1.):
+            for numc in (1.e3, 5.e-7):
+                mpri, mrim = numc * m * (1. - fr), numc * m * fr
+                lib().salsa_ref_ice_shape(o.h, mpri, mrim, numc, C.byref(out))
+                shape, dmax, regime = ice_shape_numpy(mpri, mrim, numc)
+                seen.add(regime)
+                assert list(out)[:4] == pytest.approx(list(shape), rel=1e-15, abs=0.), (m, fr, regime)
+                assert out[4] == pytest.approx(dmax, rel=1e-13, abs=0.), (m, fr, regime)
+    assert seen == {-1, 0, 1, 2, 3}
+
+
+def test_ice_collision_kernel_matches_independent_restatement():
+    """coagc for every pair that involves ice (ice with aerosol, cloud, precipitation and
+    ice, equal bins included, both argument orders) against the restatement above:
+    unrimed and rimed crystals from 5 um to 3 mm with some dry material inside, in cold
+    air of several densities.  The cases reach spherical, non-spherical, graupel and
+    rimed crystals, Stokes numbers on both sides of 1.214 and Reynolds numbers on both
+    sides of 1."""
+    cfg = workload_config(5)
+    o = Oracle(cfg)
+    lay = build_layout(cfg)
+    nu = lay.nwet + 1                                     # dry species, water, rime
+    ice0 = lay.nbins + lay.ncld + lay.nprc
+    rng = np.random.default_rng(11)
+
+    def volumes(b, numc, d, fr, dry):
+        v = [0.] * nu
+        total = numc * 0.5235988 * d * d * d
+        v[0] = total * dry
+        v[nu - 1] = total * fr if lay.phase[b] == 4 else 0.
+        v[nu - 2] = total - v[0] - v[nu - 1]
+        return v
+
+    def logu(lo, hi):
+        return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+    partners = [(lay.in2a + 2, 0.1e-6, 3.e-6, 0.9), (lay.nbins + 3, 5.e-6, 60.e-6, 1.e-4),
+                (lay.nbins + lay.ncld + 2, 80.e-6, 2.e-3, 1.e-4)]
+    partners += [(ice0 + j, 5.e-6, 3.e-3, 1.e-3) for j in range(lay.nice)]
+    regimes, stokes, reyn, n = set(), set(), set(), 0
+    for gi in range(ice0, ice0 + lay.nice):
+        for b, dlo, dhi, dry in partners:
+            for _ in range(6):
+                T, P = float(rng.uniform(235., 272.)), float(rng.uniform(50.e3, 100.e3))
+                fr = float(rng.choice([0., 0.1, 0.5, 0.9]))
+                ni, nb_ = float(10. ** rng.uniform(2., 6.)), float(10. ** rng.uniform(2., 8.))
+                vi = volumes(gi, ni, logu(5.e-6, 3.e-3), fr, 1.e-3)
+                vb = volumes(b, nb_, logu(dlo, dhi), float(rng.choice([0., 0.3])), dry)
+                regimes.add(ice_shape_numpy(sum(vi[:-1]) * RHO_IC, vi[-1] * RHO_RI, ni)[2])
+                for (b1, n1, v1), (b2, n2, v2) in (((gi, ni, vi), (b, nb_, vb)), ((b, nb_, vb), (gi, ni, vi))):
+                    k = lib().salsa_ref_coagc_sections(o.h, b1, n1, (C.c_double * nu)(*v1), b2, n2,
+                                                       (C.c_double * nu)(*v2), T, P)
+                    kn, stok, re_lrg = coagc_particles_numpy(particle_numpy(lay, b1, n1, v1),
+                                                             particle_numpy(lay, b2, n2, v2), T, P)
+                    assert k == pytest.approx(kn, rel=1e-12, abs=0.), (b1, b2, v1, v2, T, P)
+                    stokes.add(stok > 1.214)
+                    reyn.add(re_lrg > 1.)
+                    n += 1
+    assert n == 2 * lay.nice * len(partners) * 6
+    assert regimes == {0, 1, 2, 3} and stokes == {False, True} and reyn == {False, True}, (regimes, stokes, reyn)
+
+
 def equilibration_numpy(numc, zvolc, dmid, T, prh, in1a, fn1a, in2a, fn2b, nlim=1., init=True):
     """Independent restatement of the initialisation call of equilibration
     (src/src_salsa/mo_salsa_properties.f90:73-380) for one cell: the aerosol water
