@@ -2016,6 +2016,170 @@ def test_accretion_matches_independent_restatement():
     assert rainy >= 10
 
 
+def coag_ice_numpy(anum, avol, cnum, cvol, pnum, pvol, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05):
+    """Collisions that involve ice alone (lscgia, lscgic, lscgip, lscgii), restated from
+    mo_salsa_dynamics.f90:150-170 and mo_salsa_coagulation_processes.f90:24-535,
+    539-651, 707-770, 1244-1270, 1385-1430: buildKernel for aerosol, cloud and
+    precipitation with ice and buildKernelSelf for ice; below 273.15 K the ice targets
+    first, in ascending order, gaining the dry volume of collected aerosol, cloud and
+    precipitation as it stands before their own update, their water as pristine ice
+    (aerosol) or rime (cloud, precipitation) at the new density, and the whole volume of
+    the smaller ice bins already updated, with the aggregation efficiency Emax - f (Emax
+    - Emin) of the larger rime fraction f of the two bins; then the precipitation,
+    aerosol and cloud targets lose number and volume to the updated ice, at any
+    temperature."""
+    nb, nc, npr, ni = lay.nbins, lay.ncld, lay.nprc, lay.nice
+    c0, p0, i0 = nb, nb + nc, nb + nc + npr
+    cat = [(list(anum), [list(v) for v in avol], 0, nb), (list(cnum), [list(v) for v in cvol], c0, nc),
+           (list(pnum), [list(v) for v in pvol], p0, npr)]
+    inum, ivol = list(inum), [list(v) for v in ivol]
+    ndry = lay.ndry
+    iwa, irim = ndry, ndry + 1
+    nlim = {1: 1., 2: 1., 3: 1.e-6, 4: 1.e-6}
+
+    def volc(v):                                         # every section holds dry, water, rime
+        return list(v) + [0.] * (ndry + 2 - len(v))
+
+    def props(b, n, v):
+        return particle_numpy(lay, b, n, volc(v))
+
+    def rime_fraction(n, v):
+        if v[iwa] > 1.e-23 and v[irim] > 1.e-23 and n > 1.e-6:
+            return v[irim] * RHO_RI / (v[iwa] * RHO_IC + v[irim] * RHO_RI)
+        return 0.
+
+    pice = [props(i0 + j, inum[j], ivol[j]) for j in range(ni)]
+    K = []                                               # K[q][x][j]: bin x of category q with ice bin j
+    for nums, vols, b0, nbn in cat:
+        ph = lay.phase[b0]
+        K.append([[coagc_particles_numpy(props(b0 + x, nums[x], vols[x]), pice[j], T, P)[0]
+                   if nums[x] >= nlim[ph] and inum[j] >= 1.e-6 else 0. for j in range(ni)] for x in range(nbn)])
+    Kii = [[0.] * ni for _ in range(ni)]
+    for m in range(ni):
+        for n in range(m, ni):
+            if inum[m] >= 1.e-6 and inum[n] >= 1.e-6:
+                Kii[m][n] = Kii[n][m] = coagc_particles_numpy(pice[m], pice[n], T, P)[0]
+    if T < 273.15:
+        for kk in range(ni):
+            if inum[kk] < 1.e-6:
+                continue
+
+            def eagg(ll):
+                f = max(rime_fraction(inum[ll], ivol[ll]), rime_fraction(inum[kk], ivol[kk]))
+                return e_max - f * (e_max - e_min)
+            sink = 0.
+            for ll in range(kk + 1, ni):
+                sink = sink + eagg(ll) * Kii[kk][ll] * inum[ll]
+            sink_self = 0.5 * eagg(kk) * Kii[kk][kk] * inum[kk]
+            src = [0.] * (ndry + 2)
+            for q, (nums, vols, b0, nbn) in enumerate(cat):
+                into, rho = (iwa, RHO_IC) if q == 0 else (irim, RHO_RI)
+                for x in range(nbn):
+                    for s_ in range(ndry):
+                        src[s_] = src[s_] + K[q][x][kk] * vols[x][s_]
+                    src[into] = src[into] + K[q][x][kk] * vols[x][iwa] * 1000. / rho
+            for ll in range(kk):
+                e = eagg(ll)
+                for s_ in range(ndry + 2):
+                    src[s_] = src[s_] + e * Kii[ll][kk] * ivol[ll][s_]
+            n = inum[kk]
+            ivol[kk] = [(ivol[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(ndry + 2)]
+            inum[kk] = n / (1. + dt * (sink + sink_self))
+    out = []
+    for q in (2, 0, 1):                                  # precipitation, aerosol, cloud
+        nums, vols, b0, nbn = cat[q]
+        for x in range(nbn):
+            if nums[x] < nlim[lay.phase[b0]]:
+                continue
+            sink = 0.
+            for j in range(ni):
+                sink = sink + K[q][x][j] * inum[j]
+            vols[x] = [v / (1. + dt * sink) for v in vols[x]]
+            nums[x] = nums[x] / (1. + dt * sink)
+    for nums, vols, _, _ in cat:
+        out += [nums, vols]
+    return out + [inum, ivol]
+
+
+def test_ice_coagulation_matches_independent_restatement():
+    """lscoag with the four ice collisions alone (aerosol, cloud and precipitation
+    collected by ice, ice aggregation): every aerosol, cloud, precipitation and ice
+    bin of a grid256x256x128 block after one step against the restatement above.  The
+    block holds pristine and rimed crystals with some dry material, up to eight times
+    their bin's mid diameter, in cold cells and in cells above 273.15 K, where the
+    reference updates the liquid sinks and leaves the ice alone."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgca", "lscgcc", "lscgpp", "lscgpa", "lscgpc"):
+        setattr(cfg, name, 0)
+    cfg.lscgia = cfg.lscgic = cfg.lscgip = cfg.lscgii = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=6, Y=6, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc, npr, ni = lay.nwet, lay.nbins, lay.ncld, lay.nprc, lay.nice
+    i0 = nb + nc + npr
+    f = inp.fields
+    sh = f["ncloud"].shape[1:]
+    rng = np.random.default_rng(5)
+    mi = f["mice"].view(nw + 1, ni, *sh)
+    rhoi = lay.rhoice()
+    f["nprecp"] *= 1.e3
+    f["mprecp"] *= 1.e3
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                f["temp"][j, i, k] = float(rng.uniform(245., 272.)) if (i + j + k) % 5 else 275.
+                for b in range(ni):
+                    n = float(10. ** rng.uniform(3., 7.5))
+                    d = lay.dmid[i0 + b] * float(rng.uniform(1., 8.))
+                    fr = float(rng.choice([0., 0.2, 0.6]))
+                    v = n * PI6 * d ** 3
+                    f["nice"][b, j, i, k] = n / dn
+                    for s_ in range(nw + 1):
+                        share = 1.e-3 if s_ == 0 else (fr if s_ == nw else (1. - fr - 1.e-3 if s_ == nw - 1 else 0.))
+                        mi[s_, b, j, i, k] = v * share * rhoi[s_] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    rho = lay.rholiq()
+    cats = [("naero", "maero", nb, nw, rho), ("ncloud", "mcloud", nc, nw, rho), ("nprecp", "mprecp", npr, nw, rho),
+            ("nice", "mice", ni, nw + 1, rhoi)]
+    cold = warm = 0
+    agg = rime = 0.
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                T = float(f["temp"][j, i, k])
+                state = []
+                for nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)])
+                new = coag_ice_numpy(*state, lay, T, float(f["press"][j, i, k]), dt)
+                cold, warm = cold + (T < 273.15), warm + (T >= 273.15)
+                for q, (nk, mk, nbn, nsp, rh) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * n0[b] + 1e-300), (nk, b, T)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * v0[b][s_] + 1e-300), (mk, b, s_, T)
+                if T < 273.15:
+                    agg = max(agg, max(1. - a / b for a, b in zip(new[6], state[6])))
+                    rime = max(rime, max((a[-1] - b[-1]) / b[-1] for a, b in zip(new[7], state[7]) if b[-1] > 0.))
+    assert cold >= 40 and warm >= 10
+    assert agg > 1.e-3 and rime > 1.e-3, (agg, rime)       # aggregation and riming take a share
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
