@@ -959,12 +959,18 @@ def acth2o_numpy(vol, species, pcw=None):
     return max(0.1, znw / max(np.finfo(float).eps, (znw + zns)))
 
 
-def gpparth2o_numpy(T, P, rv, rs, dt, num, vol, lay, cl=True, ae=True):
-    """gpparth2o (src/src_salsa/mo_salsa_dynamics.f90:691-1125) for one cell without
-    ice, restated: the aerosol water of equilibration, then the mass-transfer
-    coefficients of the populated bins and the explicit substeps (0.02 s, +-10 %
-    limiter) of the water vapour budget.  num[k], vol[k][s] of the liquid bins;
-    returns the new volumes and the new water vapour mixing ratio."""
+def gpparth2o_numpy(T, P, rv, rs, dt, num, vol, lay, cl=True, ae=True, ice=None):
+    """gpparth2o (src/src_salsa/mo_salsa_dynamics.f90:691-1125) for one cell,
+    restated: the aerosol water of equilibration, then the mass-transfer coefficients
+    of the populated bins and the explicit substeps (0.02 s, +-10 % limiter) of the
+    water vapour budget.  num[k], vol[k][s] of the liquid bins; ice = (inum, ivol,
+    rsi) adds the ice bins (ivol[k] = dry species, ice, rime): below 273.15 K they take
+    vapour over ice with capacitance D/2 (D = the sphere of the whole particle, at most
+    10 mm), the Kelvin factor of ice's surface tension and the latent heat of
+    sublimation; pristine and rimed ice are one water budget during the substeps,
+    deposition goes to pristine ice and sublimation takes the same fraction of both.
+    Returns the new volumes, the new water vapour mixing ratio and, with ice, the new
+    ice volumes."""
     pi, rg, avog, mair, mwa, rhowa, surfw0, alv = 3.1415927, 8.314, 6.0221e+23, 28.97e-3, 18.016e-3, 1000., 0.073, 2.5e6
     nb, nc, npr, nl, nd = lay.nbins, lay.ncld, lay.nprc, lay.nliquid, lay.ndry
     iwa = lay.nwet - 1
@@ -983,8 +989,12 @@ def gpparth2o_numpy(T, P, rv, rs, dt, num, vol, lay, cl=True, ae=True):
     any_c = any(num[k] > 1. for k in range(nb, nb + nc))
     any_p = any(num[k] > 1.e-6 for k in range(nb + nc, nl))
     any_a = any(num[k] > 1. for k in range(nb))
-    if not ((any_c or (any_p and cl)) or (any_a and zrh > 0.98 and ae)):
-        return vol, rv
+    inum, ivol, rsi = ice if ice is not None else ([], [], 0.)
+    ivol = [list(v) for v in ivol]
+    ni, iic, irim = len(inum), lay.nwet - 1, lay.nwet
+    any_i = any(n > 1.e-6 for n in inum)
+    if not ((any_c or (any_p and cl)) or any_i or (any_a and zrh > 0.98 and ae)):
+        return (vol, rv) if ice is None else (vol, rv, ivol)
     rhoair = mair * P / (rg * T)
     zdfh2o = (5. / (16. * avog * rhoair * 1.e-3 * (3.11e-8) ** 2)) * \
         math.sqrt(rg * 1.e7 * T * mair * 1.e3 * (mwa + mair) * 1.e3 / (2. * pi * mwa * 1.e3))
@@ -1008,18 +1018,35 @@ def gpparth2o_numpy(T, P, rv, rs, dt, num, vol, lay, cl=True, ae=True):
         h2 = mwa * zdfh2o * alv * wsat[k] * surf[k] / (zthcond * T)
         h3 = ((alv * mwa) / (rg * T)) - 1.
         mt[k] = h1 / (h2 * h3 + 1.)
+    als, surfi0, rhoic, rhori = 2.834e6, 0.105, 917., 400.
+    kel_i, surf_i, mt_i = [1.] * ni, [0.] * ni, [0.] * ni
+    for k in range(ni):
+        if not (inum[k] > 1.e-6 and T < 273.15):
+            continue
+        d = min((sum(ivol[k]) / inum[k] / 0.5235988) ** (1. / 3.), 10.e-3)
+        kel_i[k] = math.exp(4. * surfi0 * mwa / (rg * T * rhowa * d))
+        surf_i[k] = rsi * rhoair / mwa
+        zknud = 2. * zmfph2o / d
+        zbeta = (zknud + 1.) / (0.377 * zknud + 1. + 4. / 3. * (zknud + zknud * zknud))
+        h1 = inum[k] * 4. * pi * (0.5 * d) * zdfh2o * zbeta
+        h2 = mwa * zdfh2o * als * kel_i[k] * surf_i[k] / (zthcond * T)
+        mt_i[k] = h1 / (h2 * ((als * mwa) / (rg * T) - 1.) + 1.)
+    wsat_i = list(kel_i)
+    org_ic = [v[iic] * rhoic / mwa for v in ivol]
+    org_ri = [v[irim] * rhori / mwa for v in ivol]
+    cw_i = [a + b for a, b in zip(org_ic, org_ri)]
     zcwc = rv * rhoair / mwa
     cw = [vol[k][iwa] * rhowa / mwa for k in range(nl)]
-    zcwtot = zcwc + sum(cw[:nb]) + sum(cw[nb:nb + nc]) + sum(cw[nb + nc:])
+    zcwtot = zcwc + sum(cw[:nb]) + sum(cw[nb:nb + nc]) + sum(cw[nb + nc:]) + sum(cw_i)
     groups = [range(lay.in2a, nb), range(nb, nb + nc), range(nb + nc, nl)]
     ttot = 0.
     zcwint = 0.
     while ttot < dt:
         adt = 2.e-2
         terms = [sum(mt[k] * wsat[k] * surf[k] for k in g) for g in groups]
-        h1 = zcwc + adt * (terms[0] + terms[1] + terms[2] + 0.)
+        h1 = zcwc + adt * (terms[0] + terms[1] + terms[2] + sum(m * w * s for m, w, s in zip(mt_i, wsat_i, surf_i)))
         h2 = 1. + adt * (sum(mt[k] for k in groups[0]) + sum(mt[k] for k in groups[1]) +
-                         sum(mt[k] for k in groups[2]) + 0.)
+                         sum(mt[k] for k in groups[2]) + sum(mt_i))
         zcwint = min(h1 / h2, zcwtot)
         new = list(cw)
         active = [any(num[k] > 1. for k in range(nb)) and zrh > 0.98, any_c, any_p]
@@ -1032,14 +1059,27 @@ def gpparth2o_numpy(T, P, rv, rs, dt, num, vol, lay, cl=True, ae=True):
                 wsat[k] = acth2o_numpy(vol[k], lay.species, new[k]) * kel[k]
         for k in list(groups[0]) + list(groups[1]) + list(groups[2]):
             new[k] = max(new[k], 0.)
-        zcwint = zcwtot - sum(new[:nb]) - sum(new[nb:nb + nc]) - sum(new[nb + nc:]) - 0.
+        if any_i:
+            new_i = [max(c + min(max(adt * m * (zcwint - w * s), -1.e-1 * c), 1.e-1 * c), 0.)
+                     for c, m, w, s in zip(cw_i, mt_i, wsat_i, surf_i)]
+            wsat_i = list(kel_i)
+            cw_i = new_i
+        zcwint = zcwtot - sum(new[:nb]) - sum(new[nb:nb + nc]) - sum(new[nb + nc:]) - sum(cw_i)
         cw = new
         zcwc = zcwint
         ttot = ttot + adt
     rv = zcwint * mwa / rhoair
     for k in range(nl):
         vol[k][iwa] = max(0., cw[k] * mwa / rhowa)
-    return vol, rv
+    for k in range(ni):
+        dv = cw_i[k] - (org_ic[k] + org_ri[k])
+        if dv > 0.:
+            ivol[k][iic] = ivol[k][iic] + dv * mwa / rhoic
+        elif dv < 0.:
+            fr = cw_i[k] / (org_ic[k] + org_ri[k]) - 1.
+            ivol[k][iic] = ivol[k][iic] + fr * org_ic[k] * mwa / rhoic
+            ivol[k][irim] = ivol[k][irim] + fr * org_ri[k] * mwa / rhori
+    return (vol, rv) if ice is None else (vol, rv, ivol)
 
 
 def test_condensation_matches_independent_restatement():
@@ -1091,6 +1131,86 @@ def test_condensation_matches_independent_restatement():
                             (j, i, k, nk, b)
                         q += 1
     assert cloudy >= 10
+
+
+def test_ice_deposition_matches_independent_restatement():
+    """lscnd alone with ice: the oracle's water in every liquid bin, the pristine ice
+    and rime of every ice bin and the vapour after one step against the restatement
+    above, on a 128-cell block of grid256x256x128 given pristine and rimed crystals
+    of every bin.  The block has cells where the ice grows, cells where it
+    sublimates and cells above 273.15 K, where the ice takes no vapour."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    inp = make_inputs("grid256x256x128", "cpu", X=8, Y=8, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, ni = lay.nwet, lay.nice
+    iwa = nw - 1
+    i0 = lay.nbins + lay.ncld + lay.nprc
+    f = inp.fields
+    sh = f["naero"].shape[1:]
+    rho, rhoi = lay.rholiq(), lay.rhoice()
+    mi = f["mice"].view(nw + 1, ni, *sh)
+    rng = np.random.default_rng(17)
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                # vapour between 0.8 and 1.15 of the saturation over ice
+                f["rp"][j, i, k] = float(f["rsi"][j, i, k]) * float(rng.uniform(0.8, 1.15))
+                for b in range(ni):
+                    n = float(10. ** rng.uniform(2., 5.))
+                    v = n * PI6 * (lay.dmid[i0 + b] * float(rng.uniform(1., 6.))) ** 3
+                    fr = float(rng.choice([0., 0.3]))
+                    f["nice"][b, j, i, k] = n / dn
+                    mi[0, b, j, i, k] = 1.e-3 * v * rhoi[0] / dn
+                    mi[nw - 1, b, j, i, k] = (1. - fr - 1.e-3) * v * rhoi[nw - 1] / dn
+                    mi[nw, b, j, i, k] = fr * v * rhoi[nw] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    cats = [("naero", "maero", lay.nbins), ("ncloud", "mcloud", lay.ncld), ("nprecp", "mprecp", lay.nprc)]
+    grow = shrink = warm = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                T = float(f["temp"][j, i, k])
+                num, vol = [], []
+                for nk, mk, nb in cats:
+                    mv = f[mk].view(nw, nb, *sh)
+                    for b in range(nb):
+                        num.append(float(f[nk][b, j, i, k]) * dn)
+                        vol.append([float(mv[s, b, j, i, k]) * dn / rho[s] for s in range(nw)])
+                inum = [float(f["nice"][b, j, i, k]) * dn for b in range(ni)]
+                ivol = [[float(mi[s, b, j, i, k]) * dn / rhoi[s] for s in range(nw + 1)] for b in range(ni)]
+                rv = float(f["rp"][j, i, k])
+                v1, rv1, iv1 = gpparth2o_numpy(T, float(f["press"][j, i, k]), rv, float(f["rsl"][j, i, k]), dt, num,
+                                               vol, lay, ice=(inum, ivol, float(f["rsi"][j, i, k])))
+                assert float(out["rpt"][j, i, k]) * dt == pytest.approx(rv1 - rv, rel=1e-9, abs=0.), (j, i, k)
+                q = 0
+                for nk, mk, nb in cats:
+                    tv = out[mk + "t"].view(nw, nb, *sh)
+                    for b in range(nb):
+                        got = float(tv[iwa, b, j, i, k]) * dt * dn / rho[iwa]
+                        assert got == pytest.approx(v1[q][iwa] - vol[q][iwa], rel=1e-9,
+                                                    abs=1e-14 * vol[q][iwa] + 1e-30), (j, i, k, nk, b)
+                        q += 1
+                tv = out["micet"].view(nw + 1, ni, *sh)
+                for b in range(ni):
+                    for s in (iwa, nw):
+                        got = float(tv[s, b, j, i, k]) * dt * dn / rhoi[s]
+                        assert got == pytest.approx(iv1[b][s] - ivol[b][s], rel=1e-9,
+                                                    abs=1e-14 * ivol[b][s] + 1e-30), (j, i, k, b, s)
+                d = sum(iv1[b][iwa] - ivol[b][iwa] for b in range(ni))
+                warm += T >= 273.15
+                grow += T < 273.15 and d > 0.
+                shrink += T < 273.15 and d < 0.
+    assert grow >= 10 and shrink >= 10 and warm >= 3, (grow, shrink, warm)
 
 
 def coag_aero_numpy(num, vol, lay, T, P, dt):
