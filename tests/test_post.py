@@ -1,10 +1,15 @@
 """tend_constrain2 and SALSA_diagnostics (src/src_LES/constrain_SALSA.f90) in the
 oracle: the properties the LES relies on after a SALSA step."""
+import math
+
+import numpy as np
+import pytest
 import torch
 
 from oracle_ref import Oracle
 from parity import interior
 from post_cases import post_state, TENDS
+from uclales_salsa_gb300.layout import lolim_diameters
 
 
 def test_tend_constrain_keeps_values_positive():
@@ -125,3 +130,231 @@ def test_integer_limit_equals_the_fp64_product():
         else:
             assert got == -1 or not normal, (p, dtlt)
     assert checked > 150000
+
+
+DISS = {"SO4": 3., "OC": 1., "BC": 0., "DU": 0., "SS": 2.}
+MMOL = {"SO4": 98.08e-3, "OC": 150.e-3, "BC": 12.e-3, "DU": 100.e-3, "SS": 58.44e-3}
+
+
+def correlation_numpy(x, y):
+    """calc_correlation (src/src_LES/util.f90:1005-1024) as the reference writes it:
+    the cross term keeps only the last product, and nearly constant vectors (variance
+    term below the FP64 epsilon) give 0."""
+    n = len(x)
+    sx, sy = sum(x), sum(y)
+    sx2, sy2 = sum(v * v for v in x), sum(v * v for v in y)
+    sxy = x[-1] * y[-1]
+    if sx2 * n - sx * sx < np.finfo(float).eps or sy2 * n - sy * sy < np.finfo(float).eps:
+        return 0.
+    return (sxy * n - sx * sy) / (math.sqrt(sx2 * n - sx * sx) * math.sqrt(sy2 * n - sy * sy))
+
+
+def diagnostics_numpy(inp, a, lscndgas):
+    """Independent restatement of SALSA_diagnostics with findDry4Wet
+    (src/src_LES/constrain_SALSA.f90:50-470) on numpy copies of the arrays: negatives
+    to zero everywhere; on the horizontal interior, every level, bins with number but
+    no mass emptied, then evaporated cloud droplets (below 0.7 of the critical diameter
+    or 13 um) to their parallel aerosol bin, drops (below 0.2 of it or 10 um) and dry or
+    small ice to the aerosol bin of matching dry size, the b bin taken as fn2a + (ba -
+    in2a) as the reference writes it and chosen by composition when both are
+    populated, and aerosol bins below 0.1 nm dry diameter removed, their sulphate and
+    organics to the gas phase; then the water mixing ratios at every point."""
+    lay = inp.layout
+    sp = lay.species
+    nb, nc, npr, ni, nd = lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.ndry
+    nsp = nd + 1
+    iwa, irim = nd, nd + 1
+    pi, pi6, rg, surfw0, mwa, rhowa, avog = 3.1415927, 0.5235988, 8.314, 0.073, 18.016e-3, 1000., 6.0221e+23
+    rhol, rhoi = lay.rholiq(), lay.rhoice()
+    aetot = lolim_diameters(lay)
+    r = {k: v.numpy().copy() for k, v in a.items()}
+    sh = r["naero"].shape[1:]
+    lvl5 = inp.level == 5
+    if not lvl5:
+        ni = 0
+    na, nc_, np_ = r["naero"], r["ncloud"], r["nprecp"]
+    ma = r["maero"].reshape(nsp, nb, *sh)
+    mc = r["mcloud"].reshape(nsp, nc, *sh)
+    mp = r["mprecp"].reshape(nsp, npr, *sh)
+    ni_ = r["nice"] if lvl5 else None
+    mi = r["mice"].reshape(nsp + 1, ni, *sh) if lvl5 else None
+    for arr in (na, nc_, np_, ni_, ma, mc, mp, mi):
+        if arr is not None:
+            np.maximum(arr, 0., out=arr)
+
+    def dry4wet(n, m, ib, q):
+        cd = sum(m[s][ib][q] / rhol[s] for s in range(nd)) / n[ib][q]
+        cd = (cd / pi6) ** (1. / 3.)
+        ba = min(max(lay.in2a + sum(cd > aetot[b] for b in range(lay.in2a, lay.fn2a + 1)) - 1, lay.in2a), lay.fn2a)
+        bb = lay.fn2a + (ba - lay.in2a)
+        if na[bb][q] <= 1.:
+            return ba
+        if na[ba][q] <= 1.:
+            return bb
+        y = [m[s][ib][q] for s in range(nd)]
+        ra = correlation_numpy([ma[s][ba][q] for s in range(nd)], y)
+        rb = correlation_numpy([ma[s][bb][q] for s in range(nd)], y)
+        return bb if ra < rb else ba
+
+    def move(n, m, nsrc, b, ba, q):
+        na[ba][q] = na[ba][q] + n[b][q]
+        n[b][q] = 0.
+        for s in range(nsrc):
+            ma[s][ba][q] = ma[s][ba][q] + m[s][b][q]
+            m[s][b][q] = 0.
+
+    def critical_diameter(m, b, n, T):
+        ns = sum(DISS[sp[s]] * m[s][b] / MMOL[sp[s]] for s in range(nd)) / n
+        zbb = 6. * mwa * ns / (pi * rhowa)
+        with np.errstate(divide="ignore"):
+            zaa = 4. * mwa * surfw0 / (rg * rhowa * T)
+        return float(np.sqrt(3. * zbb / zaa))
+
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(inp.nzp):
+                q = (j, i, k)
+                for n, m, nbn in ((na, ma, nb), (nc_, mc, nc)):
+                    for b in range(nbn):
+                        if n[b][q] > 0. and sum(m[s][b][q] for s in range(nsp)) <= 0.:
+                            n[b][q] = 0.
+                            for s in range(nsp):
+                                m[s][b][q] = 0.
+                for b in range(npr):
+                    if np_[b][q] > 0. and mp[iwa][b][q] <= 0.:
+                        np_[b][q] = 0.
+                        for s in range(nsp):
+                            mp[s][b][q] = 0.
+                for b in range(ni):
+                    if ni_[b][q] > 0. and mi[iwa][b][q] + mi[irim][b][q] < 1.e-25:
+                        ni_[b][q] = 0.
+                        for s in range(nsp + 1):
+                            mi[s][b][q] = 0.
+                T, rh = np.float64(r["temp"][q]), float(r["rh"][q])     # IEEE division at T = 0
+                rhi = float(r["rhi"][q]) if lvl5 else 1.
+                for b in range(nc):
+                    n = nc_[b][q]
+                    if n > 1. and rh < 0.999 and mc[iwa][b][q] < 1.e-5:
+                        cd = critical_diameter([[mc[s][bb][q] for bb in range(nc)] for s in range(nd)], b, n, T)
+                        d = (sum(mc[s][b][q] / rhol[s] for s in range(nsp)) / n / pi6) ** (1. / 3.)
+                        if d < min(0.7 * cd, 1.3e-5) or mc[iwa][b][q] < 1.e-25 * n:
+                            move(nc_, mc, nsp, b, lay.cloud_parallel(b), q)
+                for b in range(npr):
+                    n = np_[b][q]
+                    if n > 1.e-6 and rh < 0.999 and mp[iwa][b][q] < 1.e-6:
+                        cd = critical_diameter([[mp[s][bb][q] for bb in range(npr)] for s in range(nd)], b, n, T)
+                        d = (sum(mp[s][b][q] / rhol[s] for s in range(nsp)) / n / pi6) ** (1. / 3.)
+                        if d < min(0.2 * cd, 10.e-6) or mp[iwa][b][q] < 1.e-25 * n:
+                            move(np_, mp, nsp, b, dry4wet(np_, mp, b, q), q)
+                for b in range(ni):
+                    n = ni_[b][q]
+                    if n > 1.e-6 and rhi < 0.999 and mi[iwa][b][q] + mi[irim][b][q] < 1.e-15:
+                        d = (sum(mi[s][b][q] / rhoi[s] for s in range(nsp + 1)) / n / pi6) ** (1. / 3.)
+                        dry = sum(mi[s][b][q] for s in range(nd)) / sum(mi[s][b][q] for s in range(nsp + 1))
+                        if dry > 0.5 or d < 2.e-6:
+                            ba = dry4wet(ni_, mi, b, q)
+                            rime = mi[irim][b][q]
+                            move(ni_, mi, nsp, b, ba, q)
+                            ma[iwa][ba][q] = ma[iwa][ba][q] + rime
+                            mi[irim][b][q] = 0.
+                for b in range(nb):
+                    n = na[b][q]
+                    if n > 1. and sum(ma[s][b][q] / rhol[s] for s in range(nd)) / n < pi6 * 1.e-10 ** 3:
+                        if lscndgas:
+                            for name, g in (("SO4", 0), ("OC", 4)):
+                                if name in sp:
+                                    s = sp.index(name)
+                                    r["gaero"][g][q] = r["gaero"][g][q] + ma[s][b][q] / MMOL[name] * avog
+                        for s in range(nsp):
+                            ma[s][b][q] = 0.
+                        na[b][q] = 0.
+    r["rc"] = ma[iwa][lay.in1a:lay.fn2b + 1].sum(0) + mc[iwa].sum(0)
+    r["srp"] = mp[iwa].sum(0)
+    r["snrp"] = np_.sum(0)
+    r["rtot"] = r["rc"] + r["srp"] + r["rp"]
+    if lvl5:
+        r["ri"] = mi[iwa].sum(0)
+        r["riri"] = mi[irim].sum(0)
+        r["rtot"] = r["rtot"] + r["ri"] + r["riri"]
+    return r
+
+
+def test_diagnostics_match_independent_restatement():
+    """SALSA_diagnostics in the oracle against the restatement above on perturbed
+    post-step states of both workloads, every branch taken somewhere: each number
+    and mass array, the gas concentrations and the water mixing ratios (1e-14; the
+    bin moves themselves agree exactly)."""
+    moves = dict(ncloud=0, nprecp=0, nice=0, gaero=0)
+    for wl in ("grid16x16x40", "grid256x256x128"):
+        inp, a = post_state(wl, X=6, Y=6, Z=6)
+        want = diagnostics_numpy(inp, a, bool(inp.cfg.lscndgas))
+        before = {k: v.clone() for k, v in a.items()}
+        assert Oracle(inp.cfg).diagnostics(inp.nzp, inp.nxp, inp.nyp, a) == 0
+        for k, w in want.items():
+            got = a[k].numpy()
+            assert got == pytest.approx(w, rel=1e-14, abs=0.), (wl, k)
+        # count the moves: cloud, drops and ice to aerosol, tiny aerosol to gas
+        for k, lim in (("ncloud", 1.), ("nprecp", 1.e-6), ("nice", 1.e-6)):
+            if k in a:
+                moves[k] += int((before[k] > lim).sum() - (a[k] > lim).sum())
+        moves["gaero"] += int((a["gaero"] != before["gaero"]).sum())
+    assert min(moves.values()) > 0, moves
+
+
+def test_diagnostics_choose_the_aerosol_bin_by_composition():
+    """Evaporating drops and dry ice crystals into populated a and b aerosol bins of
+    random composition, so that findDry4Wet decides by calc_correlation (both
+    outcomes occur), the ice carrying rime that goes to the aerosol water: the oracle
+    against the restatement above.  calc_correlation returns 0 when a variance term
+    is below the FP64 epsilon, which mass mixing ratios of realistic aerosol (1e-9
+    kg/kg) always are, so the masses here are raised to 1e-6 kg/kg and more for the
+    composition to decide."""
+    inp, a = post_state("grid256x256x128", X=6, Y=6, Z=6)
+    lay = inp.layout
+    nd, nsp = lay.ndry, lay.nwet
+    rng = np.random.default_rng(23)
+    sh = a["naero"].shape[1:]
+    ma = a["maero"].view(nsp, lay.nbins, *sh)
+    mp = a["mprecp"].view(nsp, lay.nprc, *sh)
+    mi = a["mice"].view(nsp + 1, lay.nice, *sh)
+    rho = lay.rholiq()
+    aetot = lolim_diameters(lay)
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(inp.nzp):
+                a["rh"][j, i, k] = a["rhi"][j, i, k] = 0.9
+                big = (i + j + k) % 3 != 0           # else realistic masses: no composition choice
+                for b in range(lay.nbins):
+                    a["naero"][b, j, i, k] = 10. ** rng.uniform(2., 8.)
+                    for s in range(nd):
+                        ma[s, b, j, i, k] = float(rng.uniform(0., 1.)) * (1.e-5 if big else 1.e-9)
+                for m, n, nb, extra in ((mp, a["nprecp"], lay.nprc, ()), (mi, a["nice"], lay.nice, (nsp,))):
+                    for b in range(nb):
+                        n[b, j, i, k] = num = 10. ** rng.uniform(12., 14.) * (1. if big else 1.e-5)
+                        # dry diameter inside the 2a range, random composition
+                        d = float(np.exp(rng.uniform(np.log(aetot[lay.in2a]), np.log(1.5 * aetot[lay.fn2a]))))
+                        w = rng.uniform(0., 1., nd)
+                        v = num * 0.5235988 * d ** 3
+                        for s in range(nd):
+                            m[s, b, j, i, k] = v * w[s] / w.sum() * rho[s]
+                        m[nsp - 1, b, j, i, k] = 1.e-30 * num
+                        for s in extra:
+                            m[s, b, j, i, k] = 3.e-30 * num
+    calls = []
+
+    def corr(x, y):
+        r = correlation_numpy(x, y)
+        calls.append(r)
+        return r
+    g = dict(globals())
+    g["correlation_numpy"] = corr
+    restated = type(diagnostics_numpy)(diagnostics_numpy.__code__, g)
+    want = restated(inp, a, bool(inp.cfg.lscndgas))
+    before = {k: v.clone() for k, v in a.items()}
+    assert Oracle(inp.cfg).diagnostics(inp.nzp, inp.nxp, inp.nyp, a) == 0
+    for k, w in want.items():
+        assert a[k].numpy() == pytest.approx(w, rel=1e-14, abs=0.), k
+    pairs = list(zip(calls[0::2], calls[1::2]))
+    assert sum(ra < rb for ra, rb in pairs) > 20 and sum(ra > rb for ra, rb in pairs) > 20
+    assert sum(ra == rb == 0. for ra, rb in pairs) > 20
+    assert int((a["nice"] < before["nice"]).sum()) > 100 and int((a["nprecp"] < before["nprecp"]).sum()) > 100
