@@ -1332,6 +1332,140 @@ def test_aerosol_redistribution_matches_independent_restatement():
     assert moved > 50
 
 
+def distr_update_hydro_numpy(num, vol, lay, cat):
+    """The cloud, precipitation and ice parts of distr_update
+    (src/src_salsa/mo_salsa_update.f90:141-427), restated for one category: from the
+    last bin down, a bin whose particles lie outside its range hands the part of a
+    uniform number distribution over [V_lo, V_hi] (mean = the particle volume, V_hi /
+    V_lo = the bin's ratio) that lies beyond the limit to its neighbour, at most 99 % of
+    the volume.  Cloud droplets are placed by their dry volume and move past either
+    limit, except out of the a and b ranges; drops and ice are placed by their whole
+    volume, move down below 80 % of the way from the lower limit to the middle and up
+    above the middle (at most 99 % of the number), not out of the category.  Repeated
+    while the last populated bin checked lies outside its limits."""
+    pi6, nd, nw = 0.5235988, lay.ndry, lay.nwet
+    num, vol = list(num), [list(v) for v in vol]
+    b0 = {"cloud": lay.nbins, "precp": lay.nbins + lay.ncld, "ice": lay.nbins + lay.ncld + lay.nprc}[cat]
+    nbn = len(num)
+    lo = [lay.vlolim[b0 + k] for k in range(nbn)]
+    hi = [lay.vhilim[b0 + k] for k in range(nbn)]
+    vmid = [pi6 * (lay.dmid[b0 + k] * lay.dmid[b0 + k] * lay.dmid[b0 + k]) for k in range(nbn)]
+    half = lay.ncld // 2
+    nlim = 1. if cat == "cloud" else 1.e-6
+    nsum = nd if cat == "cloud" else (nw if cat == "precp" else nw + 1)
+
+    def populated(k):
+        if cat == "precp":
+            return num[k] > nlim
+        return num[k] > nlim and sum(vol[k][:nsum]) > 1.e-30
+
+    within, count = False, 0
+    while not within:
+        within = True
+        for kk in range(nbn - 1, -1, -1):
+            if (num[kk] > nlim and cat != "cloud") or (cat == "cloud" and populated(kk)):
+                zvpart = sum(vol[kk][:nsum]) / num[kk]
+                vrat = hi[kk] / lo[kk]
+                vilo = 2. * zvpart / (1. + vrat)
+                vihi = vrat * vilo
+                if cat == "cloud":
+                    down = zvpart < lo[kk] and kk not in (0, half)
+                    up = zvpart > hi[kk] and kk not in (half - 1, nbn - 1)
+                    cap_up = 1.
+                else:
+                    down = zvpart < vmid[kk] - 0.2 * (vmid[kk] - lo[kk]) and kk != 0
+                    up = zvpart > vmid[kk] and kk != nbn - 1
+                    cap_up = 0.99
+                if down:
+                    vexc = 0.5 * (vilo + lo[kk])
+                    nfrac = min(1., (lo[kk] - vilo) / (vihi - vilo))
+                    mm = kk - 1
+                elif up:
+                    vexc = 0.5 * (vihi + hi[kk])
+                    nfrac = min(cap_up, (vihi - hi[kk]) / (vihi - vilo))
+                    mm = kk + 1
+                else:
+                    continue
+                vfrac = min(0.99, nfrac * vexc / zvpart)
+                vol[mm] = [x + vfrac * y for x, y in zip(vol[mm], vol[kk])]
+                vol[kk] = [y - vfrac * y for y in vol[kk]]
+                num[mm] = num[mm] + nfrac * num[kk]
+                num[kk] = num[kk] - nfrac * num[kk]
+            if populated(kk):
+                zvpart = sum(vol[kk][:nsum]) / num[kk]
+                within = lo[kk] < zvpart < hi[kk]
+        count += 1
+        assert count <= 100
+    return num, vol
+
+
+def test_hydrometeor_redistribution_matches_independent_restatement():
+    """lsdistupdate alone at level 5, with the cloud droplets' dry volumes and the drops'
+    and crystals' volumes scaled by 0.05 to 30 (some move over several bins, some out
+    of the a or b range's end bins, where they stay): the oracle's cloud, precipitation
+    and ice numbers and volumes after one step against the restatement above (1e-10,
+    with 1e-11 of the bin for transfers decided on a rounding at the mid volume)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=6, Y=6, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nc, npr, ni, nd = lay.nwet, lay.ncld, lay.nprc, lay.nice, lay.ndry
+    i0 = lay.nbins + nc + npr
+    f = inp.fields
+    sh = f["ncloud"].shape[1:]
+    rng = np.random.default_rng(37)
+    choice = [0.05, 0.3, 0.6, 1., 1.5, 2.5, 4., 30.]
+    mc = f["mcloud"].view(nw, nc, *sh)
+    mp = f["mprecp"].view(nw, npr, *sh)
+    mi = f["mice"].view(nw + 1, ni, *sh)
+    mc[:nd] *= torch.from_numpy(rng.choice(choice, size=(nc,) + tuple(sh))).unsqueeze(0)
+    mp *= torch.from_numpy(rng.choice(choice, size=(npr,) + tuple(sh))).unsqueeze(0)
+    rhoi = lay.rhoice()
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                for b in range(ni):
+                    n = float(10. ** rng.uniform(2., 5.))
+                    v = n * PI6 * lay.dmid[i0 + b] ** 3 * float(rng.choice(choice))
+                    fr = float(rng.choice([0., 0.3]))
+                    f["nice"][b, j, i, k] = n / dn
+                    mi[0, b, j, i, k] = 1.e-3 * v * rhoi[0] / dn
+                    mi[nw - 1, b, j, i, k] = (1. - fr - 1.e-3) * v * rhoi[nw - 1] / dn
+                    mi[nw, b, j, i, k] = fr * v * rhoi[nw] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    rho = lay.rholiq()
+    cats = [("cloud", "ncloud", "mcloud", nc, nw, rho), ("precp", "nprecp", "mprecp", npr, nw, rho),
+            ("ice", "nice", "mice", ni, nw + 1, rhoi)]
+    moved = {c[0]: 0 for c in cats}
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                for cat, nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    num = [float(f[nk][b, j, i, k]) * dn for b in range(nbn)]
+                    vol = [[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)]
+                    n1, v1 = distr_update_hydro_numpy(num, vol, lay, cat)
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - num[b], rel=1e-10, abs=1e-11 * num[b] + 1e-300), (cat, b)
+                        moved[cat] += abs(n1[b] - num[b]) > 1e-6 * max(num[b], 1.e-6)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            assert got == pytest.approx(v1[b][s_] - vol[b][s_], rel=1e-10,
+                                                        abs=1e-11 * vol[b][s_] + 1e-300), (cat, b, s_)
+    assert min(moved.values()) > 30, moved
+
+
 def act_interst_numpy(num, vol, cnum, cvol, T, S, lay):
     """actInterst (src/src_salsa/mo_salsa_cloud.f90:859-1195) with intgN / intgV
     (:1381-1398) for one cell, restated: in each aerosol bin parallel to a cloud bin,
