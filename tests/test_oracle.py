@@ -2358,6 +2358,288 @@ def test_ice_coagulation_matches_independent_restatement():
     assert agg > 1.e-3 and rime > 1.e-3, (agg, rime)       # aggregation and riming take a share
 
 
+def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05, stats=None):
+    """The whole coagulation of one cell with all ten collision pairs on and
+    autoconversion by collisions (lsauto mode 1), restated from mo_salsa_dynamics.f90:
+    92-202, mo_salsa_coagulation_kernels.f90:24-420 and
+    mo_salsa_coagulation_processes.f90:24-1611: the kernels of every pair from the
+    state before the step; below 273.15 K the ice targets; then the precipitation,
+    aerosol and cloud targets in the reference's order, each against the categories
+    as they stand at that point (updated ones included) -- the Gauss-Seidel sweep the
+    restatements above follow one pair at a time.  Numbers and volumes per m3; ivol
+    holds the dry species, ice and rime.  stats, a dict, counts the collisions that
+    form precipitation under "formed"."""
+    nb, nc, npr, ni, nd = lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.ndry
+    c0, p0, i0 = nb, nb + nc, nb + nc + npr
+    ns, nsi, iwa, irim, pi6 = nd + 1, nd + 2, nd, nd + 1, 0.5235988
+    an, cn, pn, inum = list(an), list(cn), list(pn), list(inum)
+    av, cv, pv, ivol = ([list(v) for v in x] for x in (av, cv, pv, ivol))
+
+    def pad(v):
+        return list(v) + [0.] * (nsi - len(v))
+    pa = [particle_numpy(lay, k, an[k], pad(av[k])) for k in range(nb)]
+    pc = [particle_numpy(lay, c0 + k, cn[k], pad(cv[k])) for k in range(nc)]
+    pp = [particle_numpy(lay, p0 + k, pn[k], pad(pv[k])) for k in range(npr)]
+    pi_ = [particle_numpy(lay, i0 + k, inum[k], ivol[k]) for k in range(ni)]
+
+    def cross(p1, n1, l1, p2, n2, l2):
+        return [[coagc_particles_numpy(p1[x], p2[y], T, P)[0] if n1[x] >= l1 and n2[y] >= l2 else 0.
+                 for y in range(len(p2))] for x in range(len(p1))]
+
+    def selfk(p1, n1, l1):
+        K = [[0.] * len(p1) for _ in p1]
+        for m in range(len(p1)):
+            for n in range(m, len(p1)):
+                if n1[m] >= l1 and n1[n] >= l1:
+                    K[m][n] = K[n][m] = coagc_particles_numpy(p1[m], p1[n], T, P)[0]
+        return K
+    Kaa, Kcc, Kpp, Kii = selfk(pa, an, 1.), selfk(pc, cn, 1.), selfk(pp, pn, 1.e-6), selfk(pi_, inum, 1.e-6)
+    Kca, Kpa, Kia = cross(pa, an, 1., pc, cn, 1.), cross(pa, an, 1., pp, pn, 1.e-6), cross(pa, an, 1., pi_, inum, 1.e-6)
+    Kpc, Kic, Kip = cross(pc, cn, 1., pp, pn, 1.e-6), cross(pc, cn, 1., pi_, inum, 1.e-6), cross(pp, pn, 1.e-6, pi_, inum, 1.e-6)
+
+    def add(src, k, v, n=None):
+        for s_ in range(n if n is not None else len(v)):
+            src[s_] = src[s_] + k * v[s_]
+
+    # ice targets (coag_ice)
+    if T < 273.15:
+        def rf(n, v):
+            if v[iwa] > 1.e-23 and v[irim] > 1.e-23 and n > 1.e-6:
+                return v[irim] * RHO_RI / (v[iwa] * RHO_IC + v[irim] * RHO_RI)
+            return 0.
+        for kk in range(ni):
+            if inum[kk] < 1.e-6:
+                continue
+            eagg = [e_max - max(rf(inum[ll], ivol[ll]), rf(inum[kk], ivol[kk])) * (e_max - e_min) for ll in range(ni)]
+            sink = sum(eagg[ll] * Kii[kk][ll] * inum[ll] for ll in range(kk + 1, ni))
+            sink_self = 0.5 * eagg[kk] * Kii[kk][kk] * inum[kk]
+            src = [0.] * nsi
+            for x in range(nb):
+                add(src, Kia[x][kk], av[x], nd)
+                src[iwa] = src[iwa] + Kia[x][kk] * av[x][iwa] * 1000. / RHO_IC
+            for cat_v, Kx, nbn in ((cv, Kic, nc), (pv, Kip, npr)):
+                for x in range(nbn):
+                    add(src, Kx[x][kk], cat_v[x], nd)
+                    src[irim] = src[irim] + Kx[x][kk] * cat_v[x][iwa] * 1000. / RHO_RI
+            for ll in range(kk):
+                add(src, eagg[ll] * Kii[ll][kk], ivol[ll])
+            n = inum[kk]
+            ivol[kk] = [(ivol[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(nsi)]
+            inum[kk] = n / (1. + dt * (sink + sink_self))
+
+    # precipitation targets (coag_precp, precipSelfCoag, applyCoagPrecp)
+    for kk in range(npr):
+        if pn[kk] < 1.e-6:
+            continue
+        sink, self_, nslf, vslf = 0., 0., 0., [0.] * ns
+        if kk < npr - 1:
+            sink = sum(Kpp[kk][ll] * pn[ll] for ll in range(kk + 1, npr))
+            vslf = [pv[kk][s_] * pn[kk] * Kpp[kk][kk] for s_ in range(ns)]
+            nslf = 0.5 * Kpp[kk][kk] * pn[kk] * pn[kk]
+        else:
+            self_ = 0.5 * Kpp[kk][kk] * pn[kk]
+        sink = sink + sum(Kip[kk][j] * inum[j] for j in range(ni))
+        src = [0.] * ns
+        for x in range(nb):
+            add(src, Kpa[x][kk], av[x])
+        for x in range(nc):
+            add(src, Kpc[x][kk], cv[x])
+        for ll in range(kk):
+            add(src, Kpp[ll][kk], pv[ll])
+        n = pn[kk]
+        pv[kk] = [(pv[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(ns)]
+        pn[kk] = n / (1. + dt * (sink + self_))
+        if kk < npr - 1:
+            pv[kk + 1] = [pv[kk + 1][s_] + dt * vslf[s_] for s_ in range(ns)]
+            pn[kk + 1] = pn[kk + 1] + dt * nslf
+            pv[kk] = [pv[kk][s_] - dt * vslf[s_] for s_ in range(ns)]
+            pn[kk] = pn[kk] - dt * nslf
+
+    # aerosol targets (coag_aero)
+    ica, fca, icb, fcb = 0, nc // 2 - 1, nc // 2, nc - 1
+    in1a, fn1a, in2a, fn2a, in2b, fn2b = lay.in1a, lay.fn1a, lay.in2a, lay.fn2a, lay.in2b, lay.fn2b
+    for kk in range(nb):
+        if an[kk] < 1.:
+            continue
+        if kk <= fn1a:
+            a_sinks = [(kk + 1, fn2b)]
+            a_srcs = [(in1a, kk - 1)] if kk > in1a else []
+            xa = ica + max(kk - in2a, 0)
+            xb = icb + (xa - ica)
+            sa = ica + (kk - in2a) - 1
+            sb = icb + (sa - ica)
+        elif kk <= fn2a:
+            ib = in2b + (kk - in2a)
+            a_sinks = [(kk + 1, fn2a), (ib, fn2b)] if kk < fn2a else []
+            a_srcs = [(in1a, kk - 1), (in2b, ib)]
+            xa, xb = ica + max(kk - in2a, 0), icb + max(kk - in2a, 0)
+            sa = ica + (kk - in2a) - 1
+            sb = icb + (sa - ica)
+        else:
+            ia = in2a + (kk - in2b)
+            a_sinks = [(kk + 1, fn2b), (ia, fn2a)] if kk < fn2b else []
+            a_srcs = [(in2b, kk - 1), (in1a, ia)]
+            xa, xb = ica + max(kk - in2b, 0), icb + max(kk - in2b, 0)
+            sb = icb + (kk - in2b) - 1
+            sa = ica + (sb - icb)
+        sink, self_ = 0., 0.5 * Kaa[kk][kk] * an[kk]
+        for lo, hi in a_sinks:
+            sink = sink + sum(Kaa[kk][ll] * an[ll] for ll in range(lo, hi + 1))
+        for lo, hi in ((xa, fca), (xb, fcb)):
+            sink = sink + sum(Kca[kk][ll] * cn[ll] for ll in range(lo, hi + 1))
+        sink = sink + sum(Kpa[kk][p] * pn[p] for p in range(npr))
+        sink = sink + sum(Kia[kk][j] * inum[j] for j in range(ni))
+        src = [0.] * ns
+        for lo, hi in a_srcs:
+            for ll in range(lo, hi + 1):
+                add(src, Kaa[ll][kk], av[ll])
+        for lo, hi in ((ica, sa), (icb, sb)):
+            for ll in range(lo, hi + 1):
+                add(src, Kca[kk][ll], cv[ll])
+        n = an[kk]
+        av[kk] = [(av[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(ns)]
+        an[kk] = n / (1. + dt * (sink + self_))
+
+    # cloud targets (coag_cloud with accumulatePrecipFormation, applyCoagPrecipFormation)
+    d = [pc[k]["d"] for k in range(nc)]
+    pbins = [(lay.vlolim[p0 + k] / pi6) ** (1. / 3.) for k in range(npr)]
+
+    def formation(t, lo, hi, fix, acc):
+        selfc = (t == lo and t == hi)
+        for ll in range(lo, hi + 1):
+            dn_ = (d[t] * d[t] * d[t] + d[ll] * d[ll] * d[ll]) ** (1. / 3.)
+            tp = sum(1 for x in pbins if dn_ > x) - 1
+            if dn_ > pbins[0]:
+                if selfc:
+                    dv = [cv[ll][s_] * cn[t] * Kcc[ll][t] * fix for s_ in range(ns)]
+                    dnum = (0.5 * Kcc[ll][t] * cn[ll] * cn[t]) * fix
+                    acc["vslf"] = [x + cv[ll][s_] * cn[t] * Kcc[ll][t] * fix for s_, x in enumerate(acc["vslf"])]
+                    acc["self"] += 0.5 * Kcc[ll][t] * cn[t]
+                else:
+                    dv = [(cv[ll][s_] * cn[t] + cv[t][s_] * cn[ll]) * Kcc[ll][t] * fix for s_ in range(ns)]
+                    dnum = (Kcc[ll][t] * cn[ll] * cn[t]) * fix
+                    acc["sink"] += Kcc[t][ll] * cn[ll]
+                acc["vprc"][tp] = [x + y for x, y in zip(acc["vprc"][tp], dv)]
+                acc["nprc"][tp] += dnum
+                if stats is not None and dnum > 0.:
+                    stats["formed"] = stats.get("formed", 0) + 1
+            elif selfc:
+                acc["self"] += 0.5 * Kcc[t][ll] * cn[ll]
+            else:
+                acc["src"] = [x + Kcc[ll][t] * cv[ll][s_] for s_, x in enumerate(acc["src"])]
+
+    for kk in range(nc):
+        if cn[kk] < 1.:
+            continue
+        a_side = kk <= fca
+        own_lo, own_hi, oth_lo, oth_hi = (ica, fca, icb, fcb) if a_side else (icb, fcb, ica, fca)
+        off = kk - own_lo
+        par = oth_lo + off
+        acc = dict(sink=0., self=0., src=[0.] * ns, vslf=[0.] * ns, vprc=[[0.] * ns for _ in range(npr)],
+                   nprc=[0.] * npr)
+        if kk < own_hi:
+            for lo, hi in ((in2a + off + 1, fn2a), (in2b + off + 1, fn2b)):
+                acc["sink"] += sum(Kca[ll][kk] * an[ll] for ll in range(lo, hi + 1))
+            acc["sink"] += sum(Kcc[kk][ll] * cn[ll] for ll in range(kk + 1, own_hi + 1))
+            acc["sink"] += sum(Kcc[kk][ll] * cn[ll] for ll in range(par, oth_hi + 1))
+        fix = max(1. - dt * (0.5 * Kcc[kk][kk] * cn[kk] ** 2 / (cn[kk])), 0.1)
+        formation(kk, kk, kk, fix, acc)
+        acc["sink"] += sum(Kpc[kk][p] * pn[p] for p in range(npr))
+        acc["sink"] += sum(Kic[kk][j] * inum[j] for j in range(ni))
+        for lo, hi in ((in1a, in2a + off), (in2b, in2b + off)):
+            for ll in range(lo, hi + 1):
+                acc["src"] = [x + Kca[ll][kk] * av[ll][s_] for s_, x in enumerate(acc["src"])]
+        if kk > own_lo:
+            fix = max(1. - dt * sum(Kcc[kk][l] * cn[l] for l in range(own_lo, own_hi + 1)), 0.1)
+            formation(kk, own_lo, kk - 1, fix, acc)
+            fix = max(1. - dt * sum(Kcc[kk][l] * cn[l] for l in range(oth_lo, oth_hi + 1)), 0.1)
+            formation(kk, oth_lo, par, fix, acc)
+        n = cn[kk]
+        cv[kk] = [(cv[kk][s_] + dt * acc["src"][s_] * n) / (1. + dt * acc["sink"]) for s_ in range(ns)]
+        cn[kk] = n / (1. + dt * (acc["sink"] + acc["self"]))
+        cv[kk] = [cv[kk][s_] - dt * acc["vslf"][s_] for s_ in range(ns)]
+        for q in range(npr):
+            pv[q] = [pv[q][s_] + dt * acc["vprc"][q][s_] for s_ in range(ns)]
+            pn[q] = pn[q] + dt * acc["nprc"][q]
+    clip = lambda x: max(0., x)
+    return ([clip(x) for x in an], [[clip(x) for x in v] for v in av], [clip(x) for x in cn],
+            [[clip(x) for x in v] for v in cv], [clip(x) for x in pn], [[clip(x) for x in v] for v in pv],
+            [clip(x) for x in inum], [[clip(x) for x in v] for v in ivol])
+
+
+def test_full_coagulation_matches_independent_restatement():
+    """lscoag with all ten collision pairs and autoconversion by collisions, the
+    configuration of the workloads: every aerosol, cloud, precipitation and ice bin of
+    a grid256x256x128 block after one step against the restatement above.  The block
+    holds pristine and rimed crystals, raised drop numbers and cells on both sides of
+    273.15 K."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscnd, cfg.lsactiv, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsauto.sw, cfg.lsauto.mode = 1, 1
+    cfg.lsdistupdate = 0
+    for name in ("lscgaa", "lscgcc", "lscgca", "lscgpc", "lscgpa", "lscgpp", "lscgia", "lscgic", "lscgii", "lscgip"):
+        setattr(cfg, name, 1)
+    inp = make_inputs("grid256x256x128", "cpu", X=6, Y=6, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc, npr, ni = lay.nwet, lay.nbins, lay.ncld, lay.nprc, lay.nice
+    i0 = nb + nc + npr
+    f = inp.fields
+    sh = f["ncloud"].shape[1:]
+    rng = np.random.default_rng(41)
+    mi = f["mice"].view(nw + 1, ni, *sh)
+    rhoi = lay.rhoice()
+    f["ncloud"] *= 30.
+    f["mcloud"] *= 30.
+    f["nprecp"] *= 1.e3
+    f["mprecp"] *= 1.e3
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                f["temp"][j, i, k] = float(rng.uniform(245., 272.)) if (i + j + k) % 5 else 275.
+                for b in range(ni):
+                    n = float(10. ** rng.uniform(3., 7.))
+                    v = n * PI6 * (lay.dmid[i0 + b] * float(rng.uniform(1., 8.))) ** 3
+                    fr = float(rng.choice([0., 0.2, 0.6]))
+                    f["nice"][b, j, i, k] = n / dn
+                    mi[0, b, j, i, k] = 1.e-3 * v * rhoi[0] / dn
+                    mi[nw - 1, b, j, i, k] = (1. - fr - 1.e-3) * v * rhoi[nw - 1] / dn
+                    mi[nw, b, j, i, k] = fr * v * rhoi[nw] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    rho = lay.rholiq()
+    cats = [("naero", "maero", nb, nw, rho), ("ncloud", "mcloud", nc, nw, rho), ("nprecp", "mprecp", npr, nw, rho),
+            ("nice", "mice", ni, nw + 1, rhoi)]
+    stats = {}
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                state = []
+                for nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)])
+                new = coagulation_numpy(*state, lay, float(f["temp"][j, i, k]), float(f["press"][j, i, k]), dt,
+                                        stats=stats)
+                for q, (nk, mk, nbn, nsp, rh) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * n0[b] + 1e-300), (nk, b)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * v0[b][s_] + 1e-300), (mk, b, s_)
+    assert stats.get("formed", 0) >= 10, stats
+
+
 def test_condensation_conserves_water():
     """gpparth2o moves water between vapour and particles with zcwtot fixed (:975-978, 1039-1042)."""
     inp, f, out, rc, st, _ = run("grid16x16x40", only("lscnd"), X=6, Y=6, Z=10)
