@@ -2358,7 +2358,8 @@ def test_ice_coagulation_matches_independent_restatement():
     assert agg > 1.e-3 and rime > 1.e-3, (agg, rime)       # aggregation and riming take a share
 
 
-def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05, stats=None):
+def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05, stats=None,
+                      indef=None):
     """The whole coagulation of one cell with all ten collision pairs on and
     autoconversion by collisions (lsauto mode 1), restated from mo_salsa_dynamics.f90:
     92-202, mo_salsa_coagulation_kernels.f90:24-420 and
@@ -2368,7 +2369,9 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
     as they stand at that point (updated ones included) -- the Gauss-Seidel sweep the
     restatements above follow one pair at a time.  Numbers and volumes per m3; ivol
     holds the dry species, ice and rime.  stats, a dict, counts the collisions that
-    form precipitation under "formed"."""
+    form precipitation under "formed".  indef, the IN deficits of the liquid bins, is
+    updated in place for the drops that form (the number-weighted mean of the
+    colliding droplets', applyCoagPrecipFormation :690-697)."""
     nb, nc, npr, ni, nd = lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.ndry
     c0, p0, i0 = nb, nb + nc, nb + nc + npr
     ns, nsi, iwa, irim, pi6 = nd + 1, nd + 2, nd, nd + 1, 0.5235988
@@ -2521,6 +2524,9 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
                     acc["sink"] += Kcc[t][ll] * cn[ll]
                 acc["vprc"][tp] = [x + y for x, y in zip(acc["vprc"][tp], dv)]
                 acc["nprc"][tp] += dnum
+                if indef is not None and acc["nprc"][tp] > 0.:
+                    inf_ = indef[c0 + ll] if selfc else 0.5 * (indef[c0 + ll] + indef[c0 + t])
+                    acc["inf"][tp] = (acc["inf"][tp] * (acc["nprc"][tp] - dnum) + inf_ * dnum) / acc["nprc"][tp]
                 if stats is not None and dnum > 0.:
                     stats["formed"] = stats.get("formed", 0) + 1
             elif selfc:
@@ -2536,7 +2542,7 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
         off = kk - own_lo
         par = oth_lo + off
         acc = dict(sink=0., self=0., src=[0.] * ns, vslf=[0.] * ns, vprc=[[0.] * ns for _ in range(npr)],
-                   nprc=[0.] * npr)
+                   nprc=[0.] * npr, inf=[0.] * npr)
         if kk < own_hi:
             for lo, hi in ((in2a + off + 1, fn2a), (in2b + off + 1, fn2b)):
                 acc["sink"] += sum(Kca[ll][kk] * an[ll] for ll in range(lo, hi + 1))
@@ -2561,6 +2567,8 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
         for q in range(npr):
             pv[q] = [pv[q][s_] + dt * acc["vprc"][q][s_] for s_ in range(ns)]
             pn[q] = pn[q] + dt * acc["nprc"][q]
+            if indef is not None and pn[q] > 1.e-6:
+                indef[p0 + q] = (indef[p0 + q] * (pn[q] - dt * acc["nprc"][q]) + acc["inf"][q] * dt * acc["nprc"][q]) / pn[q]
     clip = lambda x: max(0., x)
     return ([clip(x) for x in an], [[clip(x) for x in v] for v in av], [clip(x) for x in cn],
             [[clip(x) for x in v] for v in cv], [clip(x) for x in pn], [[clip(x) for x in v] for v in pv],
@@ -2638,6 +2646,117 @@ def test_full_coagulation_matches_independent_restatement():
                             assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
                                                         abs=1e-14 * v0[b][s_] + 1e-300), (mk, b, s_)
     assert stats.get("formed", 0) >= 10, stats
+
+
+def salsa_step_numpy(state, indef, lay, cfg, T, P, rv, rs, rsi, dt):
+    """One whole SALSA step of one cell in the configuration of the workloads
+    (mo_salsa.f90:45-153): coagulation with autoconversion by collisions, water
+    condensation onto liquid and ice, interstitial activation (with the IN deficit of
+    the activated aerosol mixed into the droplets', mo_salsa_cloud.f90:1181-1185),
+    immersion freezing, melting above 273.15 K and the redistribution of every
+    category, each from the restatements above, in the reference's order and each on
+    the state the one before left.  state = (an, av, cn, cv, pn, pv, inum, ivol) per m3;
+    returns the new state, the water vapour mixing ratio and the IN deficits."""
+    nb, nc, npr, nd = lay.nbins, lay.ncld, lay.nprc, lay.ndry
+    indef = list(indef)
+    an, av, cn, cv, pn, pv, inum, ivol = coagulation_numpy(*state, lay, T, P, dt, indef=indef)
+    vol, rv, ivol = gpparth2o_numpy(T, P, rv, rs, dt, an + cn + pn, av + cv + pv, lay, ice=(inum, ivol, rsi))
+    av, cv, pv = vol[:nb], vol[nb:nb + nc], vol[nb + nc:]
+    n1, av, c1, cv = act_interst_numpy(an, av, cn, cv, T, rv / rs, lay)
+    for cb in range(nc):
+        if c1[cb] > 0.:
+            nact = c1[cb] - cn[cb]
+            indef[nb + cb] = (indef[nb + cb] * (c1[cb] - nact) + indef[lay.cloud_parallel(cb)] * nact) / c1[cb]
+    an, cn = n1, c1
+    num, vol, new_n, new_v, indef = ice_nucleation_numpy(T, rv, rs, rsi, dt, an + cn + pn, av + cv + pv, indef,
+                                                         lay, cfg)
+    an, cn, pn = num[:nb], num[nb:nb + nc], num[nb + nc:]
+    av, cv, pv = vol[:nb], vol[nb:nb + nc], vol[nb + nc:]
+    inum = [a + b for a, b in zip(inum, new_n)]
+    ivol = [[a + b for a, b in zip(x, y)] for x, y in zip(ivol, new_v)]
+    if T >= 273.15:
+        inum, ivol, pn, pv = ice_melt_numpy(inum, ivol, pn, pv, lay.vlolim[nb + nc:lay.nliquid], nd, nd, nd + 1)
+    an, av = distr_update_aero_numpy(an, av, lay, nd)
+    cn, cv = distr_update_hydro_numpy(cn, cv, lay, "cloud")
+    pn, pv = distr_update_hydro_numpy(pn, pv, lay, "precp")
+    inum, ivol = distr_update_hydro_numpy(inum, ivol, lay, "ice")
+    return (an, av, cn, cv, pn, pv, inum, ivol), rv, indef
+
+
+def test_whole_step_matches_the_restatements_in_sequence():
+    """One step of the workload configuration (every process of the workloads on,
+    lsauto mode 1, immersion freezing): the oracle's tendencies of every bin, its
+    water vapour and its IN deficits against the restatements above run in the
+    reference's order, on a grid256x256x128 block with ice seeded and cells on both
+    sides of 273.15 K (1e-8; the freezing rates reach exponents of a few hundred)."""
+    cfg = workload_config(5)
+    inp = make_inputs("grid256x256x128", "cpu", X=6, Y=6, Z=2)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc, npr, ni, nl = lay.nwet, lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.nliquid
+    i0 = nb + nc + npr
+    f = inp.fields
+    sh = f["ncloud"].shape[1:]
+    rng = np.random.default_rng(43)
+    mi = f["mice"].view(nw + 1, ni, *sh)
+    rhoi = lay.rhoice()
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                if (i + j + k) % 5 == 0:
+                    f["temp"][j, i, k] = 274.5
+                for b in range(ni):
+                    n = float(10. ** rng.uniform(2., 5.))
+                    v = n * PI6 * (lay.dmid[i0 + b] * float(rng.uniform(1., 3.))) ** 3
+                    fr = float(rng.choice([0., 0.2]))
+                    f["nice"][b, j, i, k] = n / dn
+                    mi[0, b, j, i, k] = 1.e-3 * v * rhoi[0] / dn
+                    mi[nw - 1, b, j, i, k] = (1. - fr - 1.e-3) * v * rhoi[nw - 1] / dn
+                    mi[nw, b, j, i, k] = fr * v * rhoi[nw] / dn
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    rho = lay.rholiq()
+    cats = [("naero", "maero", nb, nw, rho), ("ncloud", "mcloud", nc, nw, rho), ("nprecp", "mprecp", npr, nw, rho),
+            ("nice", "mice", ni, nw + 1, rhoi)]
+    cold = warm = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                T = float(f["temp"][j, i, k])
+                state = []
+                for nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)])
+                indef = [float(f["indef"][b, j, i, k]) for b in range(nl)]
+                rv = float(f["rp"][j, i, k])
+                new, rv1, ind1 = salsa_step_numpy(state, indef, lay, cfg, T, float(f["press"][j, i, k]), rv,
+                                                  float(f["rsl"][j, i, k]), float(f["rsi"][j, i, k]), dt)
+                cold, warm = cold + (T < 273.15), warm + (T >= 273.15)
+                assert float(out["rpt"][j, i, k]) * dt == pytest.approx(rv1 - rv, rel=1e-8, abs=0.), (j, i, k)
+                for b in range(nl):
+                    assert float(fields["indef"][b, j, i, k]) == pytest.approx(ind1[b], rel=1e-8, abs=1e-300), b
+                # a bin's change gathers moves from its neighbours and from other categories:
+                # differences down to 1e-12 of the category's largest bin are rounding
+                water = sum(v[-1] for q in range(3) for v in state[2 * q + 1]) + sum(v[-2] for v in state[7])
+                for q, (nk, mk, nbn, nsp, rh) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-8, abs=1e-12 * max(n0) + 1e-300), \
+                            (j, i, k, nk, b)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            scale = max(v[s_] for v in v0) + (water if s_ >= nw - 1 else 0.)
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-8,
+                                                        abs=1e-12 * scale + 1e-300), (j, i, k, mk, b, s_)
+    assert cold >= 40 and warm >= 10
 
 
 def test_condensation_conserves_water():
