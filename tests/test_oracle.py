@@ -2691,7 +2691,7 @@ def salsa_step_numpy(state, indef, lay, cfg, T, P, rv, rs, rsi, dt):
     return (an, av, cn, cv, pn, pv, inum, ivol), rv, indef
 
 
-@pytest.mark.parametrize("name,level", [("grid16x16x40", 4), ("grid256x256x128", 5)])
+@pytest.mark.parametrize("name,level", [("grid16x16x40", 4), ("grid256x256x128", 5), ("grid384x384x160", 5)])
 def test_whole_step_matches_the_restatements_in_sequence(name, level):
     """One step of each workload's configuration (every process of the workload on,
     lsauto mode 1; at level 5 immersion freezing and melting too): the oracle's
