@@ -2363,7 +2363,7 @@ def test_ice_coagulation_matches_independent_restatement():
 
 
 def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05, stats=None,
-                      indef=None):
+                      indef=None, rs=None):
     """The whole coagulation of one cell with all ten collision pairs on and
     autoconversion by collisions (lsauto mode 1), restated from mo_salsa_dynamics.f90:
     92-202, mo_salsa_coagulation_kernels.f90:24-420 and
@@ -2375,7 +2375,14 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
     holds the dry species, ice and rime.  stats, a dict, counts the collisions that
     form precipitation under "formed".  indef, the IN deficits of the liquid bins, is
     updated in place for the drops that form (the number-weighted mean of the
-    colliding droplets', applyCoagPrecipFormation :690-697)."""
+    colliding droplets', applyCoagPrecipFormation :690-697).  rs = {"n": [[0.] * ni
+    for each precipitation bin], "m": ...} gathers the rime-splintering tallies
+    (lssecice with lssiprimespln, :868-962, 1270-1372): the number of drops above 24
+    um that crystals at least as large collect (cloud droplets under the first
+    precipitation bin) and the mass of drops from 24 um up to the crystal's size that
+    each ice bin collects (cloud droplets under the first precipitation bin with the
+    first cloud bin's kernel, as the reference indexes it), each times the limiter
+    max(1 - sum K N, 0.1)."""
     nb, nc, npr, ni, nd = lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.ndry
     c0, p0, i0 = nb, nb + nc, nb + nc + npr
     ns, nsi, iwa, irim, pi6 = nd + 1, nd + 2, nd, nd + 1, 0.5235988
@@ -2430,6 +2437,15 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
                     src[irim] = src[irim] + Kx[x][kk] * cat_v[x][iwa] * 1000. / RHO_RI
             for ll in range(kk):
                 add(src, eagg[ll] * Kii[ll][kk], ivol[ll])
+            if rs is not None:
+                fix = max(1. - sum(Kic[c][kk] * cn[c] for c in range(nc)), 0.1)
+                for ll in range(nc):
+                    if 24.e-6 <= pc[ll]["d"] < pi_[kk]["d"]:
+                        rs["m"][0][kk] += Kic[0][kk] * cv[ll][nd] * inum[kk] * 1000. * fix
+                fix = max(1. - sum(Kip[p][kk] * pn[p] for p in range(npr)), 0.1)
+                for ll in range(npr):
+                    if 24.e-6 <= pp[ll]["d"] < pi_[kk]["d"]:
+                        rs["m"][ll][kk] += Kip[ll][kk] * pv[ll][nd] * inum[kk] * 1000. * fix
             n = inum[kk]
             ivol[kk] = [(ivol[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(nsi)]
             inum[kk] = n / (1. + dt * (sink + sink_self))
@@ -2446,6 +2462,11 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
         else:
             self_ = 0.5 * Kpp[kk][kk] * pn[kk]
         sink = sink + sum(Kip[kk][j] * inum[j] for j in range(ni))
+        if rs is not None:
+            fix = max(1. - sum(Kip[kk][j] * inum[j] for j in range(ni)), 0.1)
+            for ll in range(ni):
+                if (pi_[ll]["d"] >= pp[kk]["d"] > 24.e-6 and pn[kk] > 1.e-6 and inum[ll] > 1.e-6):
+                    rs["n"][kk][ll] += Kip[kk][ll] * inum[ll] * pn[kk] * fix
         src = [0.] * ns
         for x in range(nb):
             add(src, Kpa[x][kk], av[x])
@@ -2556,6 +2577,11 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
         formation(kk, kk, kk, fix, acc)
         acc["sink"] += sum(Kpc[kk][p] * pn[p] for p in range(npr))
         acc["sink"] += sum(Kic[kk][j] * inum[j] for j in range(ni))
+        if rs is not None:
+            fix = max(1. - sum(Kic[kk][j] * inum[j] for j in range(ni)), 0.1)
+            for ll in range(ni):
+                if pi_[ll]["d"] >= pc[kk]["d"] > 24.e-6 and cn[kk] > 1. and inum[ll] > 1.e-6:
+                    rs["n"][0][ll] += Kic[kk][ll] * inum[ll] * cn[kk] * fix
         for lo, hi in ((in1a, in2a + off), (in2b, in2b + off)):
             for ll in range(lo, hi + 1):
                 acc["src"] = [x + Kca[ll][kk] * av[ll][s_] for s_, x in enumerate(acc["src"])]
@@ -2773,6 +2799,112 @@ def test_whole_step_matches_the_restatements_in_sequence(name, level):
                             assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-8,
                                                         abs=1e-12 * scale + 1e-300), (j, i, k, mk, b, s_)
     assert (cold >= 40 and warm >= 10) if level == 5 else cold + warm >= 40
+
+
+def rime_splintering_numpy(inum, ivol, rs, lay, T, dt, mode, stats=None):
+    """rimesplintering with rs_halletmossop / rs_mossop at dltemp_rs = 5
+    (src/src_salsa/mo_salsa_SIP_RS.f90:28-252), restated for one cell after the
+    coagulation that gathered the tallies rs: between 238.15 and 273.15 K every ice bin
+    above the splinter bin's next one that rimed drops of mean diameter above 24 um
+    sheds 3.5e8 splinters per kg of rime (mode 1) or 4e-3 per drop (mode 2), of the
+    volume of a 3.4e-16 m3 column, into the bin of 10 um crystals; it loses their volume
+    and that volume in frozen drops' number, both capped to 99 % of the bin (the
+    reference scales the sinks only).  Returns the ice and the splinters per ice bin;
+    stats, a dict, counts the capped bins under "capped"."""
+    pi6, ni, npr = 0.5235988, lay.nice, lay.nprc
+    inum, ivol = list(inum), [list(v) for v in ivol]
+    nsp = len(ivol[0])
+    icebins = [(lay.vlolim[lay.nliquid + k] / pi6) ** (1. / 3.) for k in range(ni)]
+    splbin = max(sum(1 for x in icebins if x < 10.e-6), 1) - 1
+    frag_n, frag_v = [0.] * ni, [[0.] * nsp for _ in range(ni)]
+    sink_n, sink_v = [0.] * ni, [[0.] * nsp for _ in range(ni)]
+    for bb in range(ni):
+        for cc in range(npr):
+            nf, mf = rs["n"][cc][bb] * dt, rs["m"][cc][bb] * dt
+            if (T < 238.15 or T > 273.15 or nf < 1.e-12 or sum(ivol[bb]) < 1.e-15 or inum[bb] < 1.e-6
+                    or bb < splbin + 2):
+                continue
+            dd = (mf / nf / 1000. / pi6) ** (1. / 3.)
+            if dd < 24.e-6:
+                continue
+            dN = 3.5e8 * mf if mode == 1 else 4.0e-3 * nf
+            share = min(dN * 3.405365461487051e-16 / sum(ivol[bb]), 1.)
+            frag_n[splbin] += dN
+            for s_ in range(nsp):
+                frag_v[splbin][s_] += ivol[bb][s_] * share
+                sink_v[bb][s_] += ivol[bb][s_] * share
+            sink_n[bb] += sum(ivol[bb][s_] * share for s_ in range(nsp)) / (pi6 * dd ** 3.0)
+        if inum[bb] < sink_n[bb]:
+            sink_n[bb], sink_v[bb] = inum[bb], list(ivol[bb])
+        if sum(sink_v[bb]) > sum(ivol[bb]):
+            if stats is not None:
+                stats["capped"] = stats.get("capped", 0) + 1
+            f = 0.99 * sum(ivol[bb]) / sum(sink_v[bb])
+            sink_v[bb] = [x * f for x in sink_v[bb]]
+            sink_n[bb] = min(sink_n[bb] * f, 0.99 * inum[bb])
+    for bb in range(ni):
+        inum[bb] = max(0., inum[bb] + frag_n[bb] - sink_n[bb])
+        ivol[bb] = [max(0., ivol[bb][s_] + frag_v[bb][s_] - sink_v[bb][s_]) for s_ in range(nsp)]
+    return inum, ivol, frag_n
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_rime_splintering_matches_independent_restatement(mode):
+    """Coagulation (all pairs, autoconversion by collisions) with rime splintering, the
+    Hallett-Mossop (mode 1) or Mossop (mode 2) form: every ice bin and the splinter
+    tracer after one step against the coagulation restatement above, with its
+    rime-splintering tallies, followed by the restatement of rimesplintering (1e-9).
+    The block has crystals from 20 um up, doubling in diameter per bin, riming cloud
+    droplets and drops in cells between 240 and 275 K.  The caps on a bin's sinks are
+    not reached: the splinters' volume stays below 1e-5 of their bin's even with 30
+    times the droplets and drops, so states that reach them are not physical."""
+    from sip_cases import sip_state
+    inp = sip_state(mode)
+    cfg = inp.cfg
+    cfg.lsauto.sw, cfg.lsauto.mode = 1, 1
+    cfg.lsdistupdate = 0
+    lay = inp.layout
+    nw, nb, nc, npr, ni = lay.nwet, lay.nbins, lay.ncld, lay.nprc, lay.nice
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho, rhoi = lay.rholiq(), lay.rhoice()
+    cats = [("naero", "maero", nb, nw, rho), ("ncloud", "mcloud", nc, nw, rho), ("nprecp", "mprecp", npr, nw, rho),
+            ("nice", "mice", ni, nw + 1, rhoi)]
+    splinters, stats = 0, {}
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                T = float(f["temp"][j, i, k])
+                state = []
+                for nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)])
+                rs = {"n": [[0.] * ni for _ in range(npr)], "m": [[0.] * ni for _ in range(npr)]}
+                new = list(coagulation_numpy(*state, lay, T, float(f["press"][j, i, k]), dt, rs=rs))
+                new[6], new[7], frag = rime_splintering_numpy(new[6], new[7], rs, lay, T, dt, mode, stats)
+                splinters += sum(1 for x in frag if x > 0.)
+                for b in range(ni):
+                    got = float(fields["siprmspl"][b, j, i, k] - f["siprmspl"][b, j, i, k]) * dn
+                    assert got == pytest.approx(frag[b], rel=1e-9, abs=1e-14 * float(f["siprmspl"][b, j, i, k]) * dn
+                                                + 1e-300), (j, i, k, b)
+                for q, (nk, mk, nbn, nsp, rh) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * max(n0) + 1e-300), (nk, b)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * max(v[s_] for v in v0) + 1e-300), (mk, b, s_)
+    assert splinters >= 10 and not stats, (splinters, stats)
 
 
 def test_condensation_conserves_water():

@@ -1,7 +1,7 @@
 """Rime splintering (mo_salsa_SIP_RS.f90), drop fracturing (mo_salsa_SIP_DF.f90) and
 ice-ice collisional breakup (mo_salsa_SIP_IIBR.f90), through mo_salsa_secondary_ice.f90,
-in the oracle: the properties of the reference's schemes.  Secondary ice is not built on the
-GPU (salsa_gb300_init refuses lssecice); these tests pin the oracle's restatement."""
+in the oracle: the properties of the reference's schemes (budgets, temperature ranges and
+tracers).  tests/test_gpu_sip.py compares the GPU form with the oracle."""
 import pytest
 import torch
 
