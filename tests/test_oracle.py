@@ -2363,7 +2363,7 @@ def test_ice_coagulation_matches_independent_restatement():
 
 
 def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05, stats=None,
-                      indef=None, rs=None):
+                      indef=None, rs=None, df=None):
     """The whole coagulation of one cell with all ten collision pairs on and
     autoconversion by collisions (lsauto mode 1), restated from mo_salsa_dynamics.f90:
     92-202, mo_salsa_coagulation_kernels.f90:24-420 and
@@ -2382,7 +2382,10 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
     precipitation bin) and the mass of drops from 24 um up to the crystal's size that
     each ice bin collects (cloud droplets under the first precipitation bin with the
     first cloud bin's kernel, as the reference indexes it), each times the limiter
-    max(1 - sum K N, 0.1)."""
+    max(1 - sum K N, 0.1).  df = {"n": ..., "m": ..., "full": bool} gathers the
+    drop-fracturing tallies the same way (lssipdropfrac, :895-925, 1300-1343): drops
+    above 100 um collected by smaller crystals, and with Phillips' full scheme
+    ("full") by larger ones too."""
     nb, nc, npr, ni, nd = lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.ndry
     c0, p0, i0 = nb, nb + nc, nb + nc + npr
     ns, nsi, iwa, irim, pi6 = nd + 1, nd + 2, nd, nd + 1, 0.5235988
@@ -2446,6 +2449,15 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
                 for ll in range(npr):
                     if 24.e-6 <= pp[ll]["d"] < pi_[kk]["d"]:
                         rs["m"][ll][kk] += Kip[ll][kk] * pv[ll][nd] * inum[kk] * 1000. * fix
+            if df is not None:
+                for props, nums, vols, Kx, nbn, lim in ((pc, cn, cv, Kic, nc, 1.), (pp, pn, pv, Kip, npr, 1.e-6)):
+                    fix = max(1. - sum(Kx[x][kk] * nums[x] for x in range(nbn)), 0.1)
+                    for ll in range(nbn):
+                        ix = ll if nbn == npr else 0
+                        small = pi_[kk]["d"] < props[ll]["d"]
+                        if ((small or df["full"]) and props[ll]["d"] > 100.e-6 and inum[kk] > 1.e-6
+                                and nums[ll] > lim):
+                            df["m"][ix][kk] += Kx[ix][kk] * vols[ll][nd] * inum[kk] * 1000. * fix
             n = inum[kk]
             ivol[kk] = [(ivol[kk][s_] + dt * src[s_] * n) / (1. + dt * sink) for s_ in range(nsi)]
             inum[kk] = n / (1. + dt * (sink + sink_self))
@@ -2467,6 +2479,12 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
             for ll in range(ni):
                 if (pi_[ll]["d"] >= pp[kk]["d"] > 24.e-6 and pn[kk] > 1.e-6 and inum[ll] > 1.e-6):
                     rs["n"][kk][ll] += Kip[kk][ll] * inum[ll] * pn[kk] * fix
+        if df is not None:
+            fix = max(1. - sum(Kip[kk][j] * inum[j] for j in range(ni)), 0.1)
+            for ll in range(ni):
+                small = pi_[ll]["d"] < pp[kk]["d"]
+                if (small or df["full"]) and pp[kk]["d"] > 100.e-6 and pn[kk] > 1.e-6 and inum[ll] > 1.e-6:
+                    df["n"][kk][ll] += Kip[kk][ll] * inum[ll] * pn[kk] * fix
         src = [0.] * ns
         for x in range(nb):
             add(src, Kpa[x][kk], av[x])
@@ -2905,6 +2923,132 @@ def test_rime_splintering_matches_independent_restatement(mode):
                             assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
                                                         abs=1e-14 * max(v[s_] for v in v0) + 1e-300), (mk, b, s_)
     assert splinters >= 10 and not stats, (splinters, stats)
+
+
+def drop_fracturing_numpy(inum, ivol, df, lay, T, dt, mode):
+    """dropfracturing with df_lawson (mode 1), df_sullivan (mode 2) and
+    df_phillips_simple (mode 3) (src/src_salsa/mo_salsa_SIP_DF.f90:29-309), restated for
+    one cell after the coagulation that gathered the tallies df: between 248.15 and
+    271.15 K every ice bin that froze drops of mean diameter above 100 um sheds
+    fragments over the ice bins below the frozen drops' size (at least three of them),
+    in proportion to D^-3 times the bin width, each of its bin's mid-diameter volume;
+    it loses that volume in frozen drops' number.  The reference's scaling of the
+    fragments by the caps comes after they are counted and has no effect.  Returns the
+    ice and the fragments per ice bin."""
+    pi6, ni, npr = 0.5235988, lay.nice, lay.nprc
+    inum, ivol = list(inum), [list(v) for v in ivol]
+    nsp = len(ivol[0])
+    i0 = lay.nliquid
+    dmid = [lay.dmid[i0 + k] for k in range(ni)]
+    width = [(lay.vhilim[i0 + k] / pi6) ** (1. / 3) - (lay.vlolim[i0 + k] / pi6) ** (1. / 3) for k in range(ni)]
+    frag_n, frag_v = [0.] * ni, [[0.] * nsp for _ in range(ni)]
+    sink_n, sink_v = [0.] * ni, [[0.] * nsp for _ in range(ni)]
+    for bb in range(ni):
+        for cc in range(npr):
+            nf, mf = df["n"][cc][bb] * dt, df["m"][cc][bb] * dt
+            if T < 248.15 or T > 271.15 or nf < 1.e-12 or sum(ivol[bb]) < 1.e-15 or inum[bb] < 1.e-6:
+                continue
+            dd = (mf / nf / 1000. / pi6) ** (1. / 3.)
+            if dd < 100.e-6:
+                continue
+            npmax = max(sum(1 for x in dmid if x <= dd) - 1, 1)
+            if npmax <= 2:
+                continue
+            d6 = min(dd, 3.e-3) * 1.e6
+            if mode == 1:
+                dN = nf * 2.5e-11 * d6 ** 4.
+            elif mode == 2:
+                g = lambda x: 1. / (math.sqrt(2. * math.pi) * 10.) * math.exp(-0.5 * (x - 258.) ** 2 / 10. ** 2)
+                dN = nf * 0.2 * (g(T) / g(258.)) * 2.5e-11 * d6 ** 4.
+            else:
+                tl, hv = [x + 273.15 for x in (-24., -20., -16., -10., -6.)], [0.6, 0.24, 2.6, 0.43, 0.35]
+                hT = 0.
+                if tl[0] <= T < tl[1]:
+                    hT = (hv[1] - hv[0]) * ((T - tl[0]) / 4.) + hv[0]
+                elif tl[1] <= T < tl[2]:
+                    hT = (hv[2] - hv[1]) * ((T - tl[2]) / 4.) + hv[2]
+                elif tl[2] <= T < tl[3]:
+                    hT = (hv[3] - hv[2]) * ((T - tl[3]) / 6.) + hv[3]
+                elif tl[3] <= T < tl[4]:
+                    hT = (hv[4] - hv[3]) * ((T - tl[4]) / 4.) + hv[4]
+                dN = nf * ((4. / 9.) * 1.e4 * hT * dd)
+            w = [1. / (dmid[b] * dmid[b] * dmid[b]) for b in range(npmax)]
+            norm = sum(x * y for x, y in zip(w, width))
+            dNb = [dN * w[b] * width[b] / norm for b in range(npmax)]
+            dVb = [dNb[b] * pi6 * dmid[b] * dmid[b] * dmid[b] for b in range(npmax)]
+            vb = sum(ivol[bb])
+            for b in range(npmax):
+                frag_n[b] += dNb[b]
+                for s_ in range(nsp):
+                    frag_v[b][s_] += ivol[bb][s_] * (dVb[b] / vb)
+            sv = [ivol[bb][s_] * sum(dVb) / vb for s_ in range(nsp)]
+            sink_v[bb] = [x + y for x, y in zip(sink_v[bb], sv)]
+            sink_n[bb] += sum(sv) / (mf / nf / 1000.)
+        if inum[bb] < sink_n[bb]:
+            sink_n[bb], sink_v[bb] = inum[bb], list(ivol[bb])
+        if sum(sink_v[bb]) > sum(ivol[bb]):
+            f = 0.99 * sum(ivol[bb]) / sum(sink_v[bb])
+            sink_v[bb] = [x * f for x in sink_v[bb]]
+            sink_n[bb] = min(sink_n[bb] * f, 0.99 * inum[bb])
+    for bb in range(ni):
+        inum[bb] = max(0., inum[bb] + frag_n[bb] - sink_n[bb])
+        ivol[bb] = [max(0., ivol[bb][s_] + frag_v[bb][s_] - sink_v[bb][s_]) for s_ in range(nsp)]
+    return inum, ivol, frag_n
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_drop_fracturing_matches_independent_restatement(mode):
+    """Coagulation (all pairs, autoconversion by collisions) with drop fracturing in the
+    Lawson (1), Sullivan (2) and simple Phillips (3) forms: every bin and the fragment
+    tracer after one step against the coagulation restatement above, with its
+    drop-fracturing tallies, followed by the restatement of dropfracturing (1e-9)."""
+    from sip_cases import sip_state
+    inp = sip_state(mode, scheme="lssipdropfrac")
+    cfg = inp.cfg
+    cfg.lsauto.sw, cfg.lsauto.mode = 1, 1
+    cfg.lsdistupdate = 0
+    lay = inp.layout
+    nw, nb, nc, npr, ni = lay.nwet, lay.nbins, lay.ncld, lay.nprc, lay.nice
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho, rhoi = lay.rholiq(), lay.rhoice()
+    cats = [("naero", "maero", nb, nw, rho), ("ncloud", "mcloud", nc, nw, rho), ("nprecp", "mprecp", npr, nw, rho),
+            ("nice", "mice", ni, nw + 1, rhoi)]
+    fragmented = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                T = float(f["temp"][j, i, k])
+                state = []
+                for nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)])
+                df = {"n": [[0.] * ni for _ in range(npr)], "m": [[0.] * ni for _ in range(npr)], "full": False}
+                new = list(coagulation_numpy(*state, lay, T, float(f["press"][j, i, k]), dt, df=df))
+                new[6], new[7], frag = drop_fracturing_numpy(new[6], new[7], df, lay, T, dt, mode)
+                fragmented += any(x > 0. for x in frag)
+                for b in range(ni):
+                    got = float(fields["sipdrfr"][b, j, i, k] - f["sipdrfr"][b, j, i, k]) * dn
+                    assert got == pytest.approx(frag[b], rel=1e-9, abs=1e-14 * float(f["sipdrfr"][b, j, i, k]) * dn
+                                                + 1e-300), (j, i, k, b)
+                for q, (nk, mk, nbn, nsp, rh) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * max(n0) + 1e-300), (nk, b)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * max(v[s_] for v in v0) + 1e-300), (mk, b, s_)
+    assert fragmented >= 5, fragmented
 
 
 def test_condensation_conserves_water():
