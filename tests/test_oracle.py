@@ -2363,7 +2363,7 @@ def test_ice_coagulation_matches_independent_restatement():
 
 
 def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0.3, e_min=0.05, stats=None,
-                      indef=None, rs=None, df=None):
+                      indef=None, rs=None, df=None, ib=None):
     """The whole coagulation of one cell with all ten collision pairs on and
     autoconversion by collisions (lsauto mode 1), restated from mo_salsa_dynamics.f90:
     92-202, mo_salsa_coagulation_kernels.f90:24-420 and
@@ -2385,7 +2385,10 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
     max(1 - sum K N, 0.1).  df = {"n": ..., "m": ..., "full": bool} gathers the
     drop-fracturing tallies the same way (lssipdropfrac, :895-925, 1300-1343): drops
     above 100 um collected by smaller crystals, and with Phillips' full scheme
-    ("full") by larger ones too."""
+    ("full") by larger ones too.  ib = {"n": [[0.] * ni] * ni, "m": ...} gathers the
+    ice-ice breakup tallies (lssipicecollbreak, :878-894, 1425-1449), [larger][smaller]:
+    the collisions of a crystal with larger ones and the ice mass a crystal collects
+    from smaller ones."""
     nb, nc, npr, ni, nd = lay.nbins, lay.ncld, lay.nprc, lay.nice, lay.ndry
     c0, p0, i0 = nb, nb + nc, nb + nc + npr
     ns, nsi, iwa, irim, pi6 = nd + 1, nd + 2, nd, nd + 1, 0.5235988
@@ -2428,6 +2431,15 @@ def coagulation_numpy(an, av, cn, cv, pn, pv, inum, ivol, lay, T, P, dt, e_max=0
             if inum[kk] < 1.e-6:
                 continue
             eagg = [e_max - max(rf(inum[ll], ivol[ll]), rf(inum[kk], ivol[kk])) * (e_max - e_min) for ll in range(ni)]
+            if ib is not None:
+                fix = max(1. - sum(Kii[kk][j] * inum[j] for j in range(ni)), 0.1)
+                for ll in range(kk + 1, ni):
+                    if pi_[kk]["d"] < pi_[ll]["d"] and inum[kk] > 1.e-6 and inum[ll] > 1.e-6:
+                        ib["n"][ll][kk] += eagg[ll] * Kii[ll][kk] * inum[ll] * inum[kk] * fix
+                for ll in range(kk):
+                    if pi_[kk]["d"] > pi_[ll]["d"] and inum[kk] > 1.e-6 and inum[ll] > 1.e-6:
+                        ib["m"][kk][ll] += eagg[ll] * Kii[kk][ll] * (ivol[ll][iwa] * RHO_IC + ivol[ll][irim] * RHO_RI) \
+                            * inum[kk]
             sink = sum(eagg[ll] * Kii[kk][ll] * inum[ll] for ll in range(kk + 1, ni))
             sink_self = 0.5 * eagg[kk] * Kii[kk][kk] * inum[kk]
             src = [0.] * nsi
@@ -3049,6 +3061,122 @@ def test_drop_fracturing_matches_independent_restatement(mode):
                             assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
                                                         abs=1e-14 * max(v[s_] for v in v0) + 1e-300), (mk, b, s_)
     assert fragmented >= 5, fragmented
+
+
+def ice_breakup_numpy(inum, ivol, ib, lay, T, dt, mode):
+    """iceicecollbreak with imf_sullivan (mode 1) and imf_sotiropoulou (mode 2)
+    (src/src_salsa/mo_salsa_SIP_IIBR.f90:23-319), restated for one cell after the
+    coagulation that gathered the tallies ib: between 248.15 and 270.15 K each
+    crystal bin that collided with larger ones breaks into at most 100 fragments per
+    collision, spread like the drop fracturing's over the ice bins below the size of
+    the collected ice mass per collision (at least three); it loses their volume in
+    collided crystals' number.  Returns the ice and the fragments per ice bin."""
+    pi6, ni = 0.5235988, lay.nice
+    inum, ivol = list(inum), [list(v) for v in ivol]
+    nsp, iwa, irim = len(ivol[0]), len(ivol[0]) - 2, len(ivol[0]) - 1
+    i0 = lay.nliquid
+    dmid = [lay.dmid[i0 + k] for k in range(ni)]
+    width = [(lay.vhilim[i0 + k] / pi6) ** (1. / 3) - (lay.vlolim[i0 + k] / pi6) ** (1. / 3) for k in range(ni)]
+    frag_n, frag_v = [0.] * ni, [[0.] * nsp for _ in range(ni)]
+    sink_n, sink_v = [0.] * ni, [[0.] * nsp for _ in range(ni)]
+
+    def rhomean(b):
+        if inum[b] > 1.e-6:
+            mp, mr = RHO_IC * ivol[b][iwa], RHO_RI * ivol[b][irim]
+            return min((mp * RHO_IC + mr * RHO_RI) / max(mp + mr, 7.e-25), RHO_IC)
+        return RHO_IC
+    for bb in range(ni):
+        for cc in range(bb, ni):
+            nf, mf = ib["n"][cc][bb] * dt, ib["m"][cc][bb] * dt
+            if (T < 248.15 or T > 270.15 or nf < 1.e-12 or mf < 1.e-15 or sum(ivol[bb]) < 1.e-15
+                    or inum[bb] < 1.e-6 or sum(ivol[cc]) < 1.e-15 or inum[cc] < 1.e-6):
+                continue
+            v_i = mf / nf / rhomean(bb)
+            dmin = (v_i / pi6) ** (1. / 3.)
+            npmax = sum(1 for x in dmid if x <= dmin) - 1
+            if npmax <= 2:
+                continue
+            imf = 0. if T < 252. else max(0., 280. * (T - 252.) ** 1.2 * math.exp(-(T - 252.) / 5.))
+            if mode == 2:
+                imf = 0. if T <= 252. else max(0., 280. * (T - 252.) ** 1.2 * math.exp(-(T - 252.) / 5.) * dmin / 0.02)
+            dN = min(imf, 100.0) * nf
+            w = [1. / (dmid[b] * dmid[b] * dmid[b]) for b in range(npmax)]
+            norm = sum(x * y for x, y in zip(w, width))
+            dNb = [dN * w[b] * width[b] / norm for b in range(npmax)]
+            dVb = [dNb[b] * pi6 * dmid[b] * dmid[b] * dmid[b] for b in range(npmax)]
+            vb = sum(ivol[bb])
+            for b in range(npmax):
+                frag_n[b] += dNb[b]
+                for s_ in range(nsp):
+                    frag_v[b][s_] += ivol[bb][s_] * (dVb[b] / vb)
+            sv = [ivol[bb][s_] * sum(dVb) / vb for s_ in range(nsp)]
+            sink_v[bb] = [x + y for x, y in zip(sink_v[bb], sv)]
+            sink_n[bb] += sum(sv) / v_i
+        if inum[bb] < sink_n[bb]:
+            sink_n[bb], sink_v[bb] = inum[bb], list(ivol[bb])
+        if sum(sink_v[bb]) > sum(ivol[bb]):
+            f = 0.99 * sum(ivol[bb]) / sum(sink_v[bb])
+            sink_v[bb] = [x * f for x in sink_v[bb]]
+            sink_n[bb] = min(sink_n[bb] * f, 0.99 * inum[bb])
+    for bb in range(ni):
+        inum[bb] = max(0., inum[bb] + frag_n[bb] - sink_n[bb])
+        ivol[bb] = [max(0., ivol[bb][s_] + frag_v[bb][s_] - sink_v[bb][s_]) for s_ in range(nsp)]
+    return inum, ivol, frag_n
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_ice_breakup_matches_independent_restatement(mode):
+    """Coagulation (all pairs, autoconversion by collisions) with ice-ice collisional
+    breakup in the Sullivan (1) and Sotiropoulou (2) forms: every bin and the fragment
+    tracer after one step against the coagulation restatement above, with its breakup
+    tallies, followed by the restatement of iceicecollbreak (1e-9)."""
+    from sip_cases import sip_state
+    inp = sip_state(mode, scheme="lssipicecollbreak")
+    cfg = inp.cfg
+    cfg.lsauto.sw, cfg.lsauto.mode = 1, 1
+    cfg.lsdistupdate = 0
+    lay = inp.layout
+    nw, nb, nc, npr, ni = lay.nwet, lay.nbins, lay.ncld, lay.nprc, lay.nice
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["ncloud"].shape[1:]
+    rho, rhoi = lay.rholiq(), lay.rhoice()
+    cats = [("naero", "maero", nb, nw, rho), ("ncloud", "mcloud", nc, nw, rho), ("nprecp", "mprecp", npr, nw, rho),
+            ("nice", "mice", ni, nw + 1, rhoi)]
+    broke = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                T = float(f["temp"][j, i, k])
+                state = []
+                for nk, mk, nbn, nsp, rh in cats:
+                    mv = f[mk].view(nsp, nbn, *sh)
+                    state.append([float(f[nk][b, j, i, k]) * dn for b in range(nbn)])
+                    state.append([[float(mv[s_, b, j, i, k]) * dn / rh[s_] for s_ in range(nsp)] for b in range(nbn)])
+                ib = {"n": [[0.] * ni for _ in range(ni)], "m": [[0.] * ni for _ in range(ni)]}
+                new = list(coagulation_numpy(*state, lay, T, float(f["press"][j, i, k]), dt, ib=ib))
+                new[6], new[7], frag = ice_breakup_numpy(new[6], new[7], ib, lay, T, dt, mode)
+                broke += any(x > 0. for x in frag)
+                for b in range(ni):
+                    got = float(fields["sipiibr"][b, j, i, k] - f["sipiibr"][b, j, i, k]) * dn
+                    assert got == pytest.approx(frag[b], rel=1e-9, abs=1e-14 * float(f["sipiibr"][b, j, i, k]) * dn
+                                                + 1e-300), (j, i, k, b)
+                for q, (nk, mk, nbn, nsp, rh) in enumerate(cats):
+                    n0, v0, n1, v1 = state[2 * q], state[2 * q + 1], new[2 * q], new[2 * q + 1]
+                    tv = out[mk + "t"].view(nsp, nbn, *sh)
+                    for b in range(nbn):
+                        got = float(out[nk + "t"][b, j, i, k]) * dt * dn
+                        assert got == pytest.approx(n1[b] - n0[b], rel=1e-9, abs=1e-14 * max(n0) + 1e-300), (nk, b)
+                        for s_ in range(nsp):
+                            got = float(tv[s_, b, j, i, k]) * dt * dn / rh[s_]
+                            assert got == pytest.approx(v1[b][s_] - v0[b][s_], rel=1e-9,
+                                                        abs=1e-14 * max(v[s_] for v in v0) + 1e-300), (mk, b, s_)
+    assert broke >= 5, broke
 
 
 def test_condensation_conserves_water():
