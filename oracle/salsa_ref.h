@@ -10,10 +10,13 @@
  * Parity status: the reference is Fortran and no Fortran compiler exists in
  * this environment, and the reference ships no tests, golden vectors or
  * fixtures for this path.  The restatement is therefore "parity unpinned"
- * against the real Fortran; it is pinned instead by closed-form checks in
- * tests/ (flux-matching limits, semi-implicit single-pair update, Koehler
- * equilibrium, water conservation by construction) and by committed golden
- * vectors of its own outputs (tests/golden/).
+ * against the real Fortran; it is checked instead by second, independent numpy
+ * restatements of the Fortran in tests/ (every process of the step, composed
+ * into whole steps of the workload configurations, the secondary-ice schemes,
+ * sedimentation and the post-step diagnostics), by closed-form checks
+ * (flux-matching limits, semi-implicit single-pair update, Koehler equilibrium,
+ * water conservation by construction) and by committed golden vectors of its
+ * own outputs (tests/golden/).
  *
  * Interface: same structs as the product C-ABI (include/salsa_gb300.h).
  */
