@@ -871,6 +871,182 @@ def test_ice_nucleation_matches_independent_restatement():
     assert froze > 10
 
 
+def classic_ice_nucleation_numpy(T, rv, rs, rsi, dt, num, vol, lay, cfg):
+    """ice_nucl_driver with calc_Jhet, calc_Jdep, calc_Jhf, calc_het_sf, getIceBin and
+    iceNucleation of the classic scheme (ice_theta_dist off;
+    src/src_salsa/mo_salsa_cloud_ice.f90:26-316, 466-531) for one cell, restated: one
+    contact angle (cosine 0.5) for immersion and deposition freezing, homogeneous
+    freezing of the solution volume, the frozen fraction of each liquid bin moved to
+    the ice bin of its frozen volume.  num[k], vol[k][s] of the liquid bins; returns
+    them with the new ice."""
+    pi, pi6 = 3.1415927, 0.5235988
+    boltz, planck, rg, avog, mwa, rhowa = 1.3807e-23, 6.626070040e-34, 8.314, 6.0221e+23, 18.016e-3, 1000.
+    nw, nd = lay.nwet, lay.ndry
+    iwa, irim = nw - 1, nw
+    ins = [lay.species.index("BC"), lay.species.index("DU")]
+    nl = lay.nliquid
+    phase = [1] * lay.nbins + [2] * lay.ncld + [3] * lay.nprc
+    nlim = [1.] * (lay.nbins + lay.ncld) + [1.e-6] * lay.nprc
+    dlim = [30.e-6] * lay.nbins + [100.e-6] * lay.ncld + [5.e-3] * lay.nprc
+    num, vol = list(num), [list(v) for v in vol]
+    ice_num, ice_vol = [0.] * lay.nice, [[0.] * (nw + 1) for _ in range(lay.nice)]
+    mis = 0.5
+
+    def het_sf(x):
+        if x > 100.:
+            return (mis * mis * mis - 3 * mis + 2) / 4
+        fii = math.sqrt(1. - 2. * mis * x + x * x)
+        fpsi = (x - mis) / fii
+        a = (1. - mis * x) / fii
+        return 0.5 * (1. + a * a * a + (2. - 3. * fpsi + fpsi * fpsi * fpsi) * x * x * x + 3. * mis * (fpsi - 1.) * x * x)
+
+    def lefm(tc):
+        return (79.7 + 0.708 * tc - 2.5e-3 * tc * tc) * 4.1868e3
+
+    def j_het(rn, sw):
+        if rn < 1e-10:
+            return 0.
+        tc = T - 273.15
+        act = rg * T * (347. / (T - 177.) - math.log(4.14 / 349.)) / avog
+        lf = lefm(tc)
+        gg = rg * T / mwa / lf
+        if (273.15 / T) * sw ** gg < 1.0001:
+            return 0.
+        sig = 28.e-3 + 0.25e-3 * tc
+        r_g = 4. * sig / (900. * lf * math.log((273.15 / T) * sw ** gg) - 0.)
+        if r_g <= 1e-10:
+            return 0.
+        crit = (pi / 3.) * sig * r_g * r_g * het_sf(rn / r_g) - 0.
+        return boltz * T / planck * 1e32 * pi * rn * rn * math.exp((-act - crit) / (boltz * T))
+
+    def j_dep(rn, si):
+        if rn < 1e-10 or si < 1.0001:
+            return 0.
+        tc = T - 273.15
+        sig = ((76.1 - 0.155 * tc) + (28.5 + 0.25 * tc)) * 1e-3
+        r_g = 4. * sig / (rg * 900. / mwa * T * math.log(si) - 0.)
+        if r_g <= 1e-10:
+            return 0.
+        crit = (pi / 3.) * sig * r_g * r_g * het_sf(rn / r_g)
+        return (1. / 4.) * 1.e30 * rn * rn * math.exp((-0. - crit) / (boltz * T))
+
+    def j_hf(sw):
+        tc = T - 273.15
+        act = 0.694e-19 * (1. + 0.027 * (tc + 30.))
+        lf = lefm(tc)
+        gg = rg * T / lf / mwa
+        if (273.15 / T) * sw ** gg < 1.0001:
+            return 0.
+        sig = 28.e-3 + 0.25e-3 * tc
+        r_g = 2. * sig / (900. * lf * math.log((273.15 / T) * sw ** gg))
+        if r_g <= 1e-10:
+            return 0.
+        crit = 4. * pi / 3. * sig * r_g * r_g
+        return 2.0 * 5.85e16 * (rhowa * boltz * T / 900. / planck) * math.sqrt(sig / boltz / T) * \
+            math.exp((-crit - act) / (boltz * T))
+
+    vlo_ice = lay.vlolim[nl:]
+    for k in range(nl):
+        if T > 273.15 or num[k] < nlim[k]:
+            continue
+        if num[k] > nlim[k]:
+            dwet = (sum(vol[k]) / num[k] / pi6) ** (1. / 3.)
+            ddry = (sum(vol[k][:nd]) / num[k] / pi6) ** (1. / 3.)
+            dins = (sum(vol[k][s] for s in ins) / num[k] / pi6) ** (1. / 3.)
+        else:
+            dwet = ddry = dins = lay.dmid[k]
+        dwet, ddry, dins = min(dwet, dlim[k]), min(ddry, dlim[k]), min(dins, dlim[k])
+        sw = sweq_numpy(num[k], vol[k], T, lay.species)
+        f_imm = f_dep = f_hom = 0.
+        if dins > 1.e-10 and cfg.lsiceimm and phase[k] in (2, 3):
+            f_imm = 1. - math.exp(-j_het(dins, sw) * dt)
+        if dins > 1.e-10 and dwet - dins < 1.e-10 and rv / rs < 1.0 and phase[k] == 1 and cfg.lsicedep:
+            f_dep = 1. - math.exp(-j_dep(dins, rv / rsi) * dt)
+        if dwet - dins > 1.e-10 and T < 237.9 and cfg.lsicehom:
+            f_hom = 1. - math.exp(-j_hf(sw) * pi6 * (dwet ** 3 - dins ** 3) * dt)
+        frac = max(0., min(0.99, f_imm + f_hom + f_dep - (f_imm + f_dep) * f_hom))
+        v = pi6 * dwet ** 3 * rhowa / 917.
+        bb = min(max(1, sum(1 for x in vlo_ice if x < v)), lay.nice) - 1
+        for ss in range(nd):
+            ice_vol[bb][ss] = max(0., ice_vol[bb][ss] + vol[k][ss] * frac)
+            vol[k][ss] = max(0., vol[k][ss] * (1. - frac))
+        into, rho = (iwa, 917.) if phase[k] in (1, 2) else (irim, 400.)
+        ice_vol[bb][into] = max(0., ice_vol[bb][into] + vol[k][iwa] * frac * rhowa / rho)
+        vol[k][iwa] = max(0., vol[k][iwa] * (1. - frac))
+        ice_num[bb] = max(0., ice_num[bb] + num[k] * frac)
+        num[k] = max(0., num[k] * (1. - frac))
+    return num, vol, ice_num, ice_vol
+
+
+def test_classic_ice_nucleation_matches_independent_restatement():
+    """lsicenucl alone with the classic scheme (ice_theta_dist off; immersion, deposition
+    and homogeneous freezing on): the oracle's ice bins and liquid bins after one step
+    against the restatement above, on 32 cells of grid256x256x128 between 225 and
+    272 K, half of them cloudy and half with bare dust particles just below water
+    saturation (1e-8: the rates' exponents reach a few hundred).  The classic
+    deposition rate is nil there: with the contact angle's cosine of 0.5 its exponent
+    exceeds 1000 at ice saturation ratios up to 1.23."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto, cfg.lsactiv, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    cfg.ice_theta_dist = 0
+    cfg.lsicehom = cfg.lsicedep = cfg.lsiceimm = 1
+    inp = make_inputs("grid256x256x128", "cpu", X=4, Y=4, Z=2, overrides=dict(cloudy=0.5, pattern="random"))
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nl, nice = lay.nwet, lay.nliquid, lay.nice
+    f = inp.fields
+    rng = np.random.default_rng(53)
+    f["temp"][...] = torch.from_numpy(rng.uniform(225., 272., size=f["temp"].shape))
+    f["nice"].zero_()
+    f["mice"].zero_()
+    # bare dust in the 2b bins of half the columns, for deposition freezing
+    ma = f["maero"].view(nw, lay.nbins, *f["naero"].shape[1:])
+    idu = lay.species.index("DU")
+    for s in range(nw):
+        if s != idu:
+            ma[s, lay.in2b:, ::2] = 0.
+    f["rp"][::2] = 0.99 * f["rsl"][::2]                     # just below water saturation
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    dt = inp.dt
+    sh = f["nice"].shape[1:]
+    cats = [("naero", "maero", lay.nbins), ("ncloud", "mcloud", lay.ncld), ("nprecp", "mprecp", lay.nprc)]
+    rho, rhoi = lay.rholiq(), lay.rhoice()
+    ti = out["micet"].view(nw + 1, nice, *sh)
+    froze = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num, vol = [], []
+                for nk, mk, nb in cats:
+                    mv = f[mk].view(nw, nb, *sh)
+                    for b in range(nb):
+                        num.append(float(f[nk][b, j, i, k]) * dn)
+                        vol.append([float(mv[s, b, j, i, k]) * dn / rho[s] for s in range(nw)])
+                T, rv = float(f["temp"][j, i, k]), float(f["rp"][j, i, k])
+                n1, v1, inum, ivol = classic_ice_nucleation_numpy(T, rv, float(f["rsl"][j, i, k]),
+                                                                  float(f["rsi"][j, i, k]), dt, num, vol, lay, cfg)
+                froze += sum(1 for x in inum if x > 0.)
+                for b in range(nice):
+                    got = float(out["nicet"][b, j, i, k]) * dt * dn
+                    assert got == pytest.approx(inum[b], rel=1e-8, abs=0.), (j, i, k, b)
+                    for s in range(nw + 1):
+                        got = float(ti[s, b, j, i, k]) * dt * dn / rhoi[s]
+                        assert got == pytest.approx(ivol[b][s], rel=1e-8, abs=1e-300), (j, i, k, b, s)
+                q = 0
+                for nk, mk, nb in cats:
+                    for b in range(nb):
+                        got = float(f[nk][b, j, i, k] + out[nk + "t"][b, j, i, k] * dt) * dn
+                        assert got == pytest.approx(n1[q], rel=1e-8, abs=0.), (nk, b)
+                        q += 1
+    assert froze > 10, froze
+
+
 def acth2o_numpy(vol, species, pcw=None):
     """acth2o (mo_salsa_dynamics.f90:1127-1157): water activity of a liquid particle."""
     diss = {"SO4": 3., "OC": 1., "BC": 0., "DU": 0., "SS": 2.}
