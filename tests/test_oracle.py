@@ -1791,6 +1791,163 @@ def test_activation_matches_independent_restatement():
     assert activated > 20
 
 
+def act_cloudbase_numpy(num, vol, T, P, w, lay):
+    """ActCloudBase with getSolute and activate3 (src/src_salsa/mo_salsa_cloud.f90:
+    112-375, 1199-1398), restated for one cell: the maximum supersaturation of an
+    updraft w by Abdul-Razzak and Ghan, the critical diameters of every aerosol bin,
+    and the droplets that activate in each bin parallel to a cloud bin, from a
+    piecewise-linear number distribution cut at the critical volume of the first
+    partly activated 1a/2a bin.  Returns their numbers and species volumes (water at
+    the critical size, at most twice its volume below 3 um)."""
+    pi, pi6, eps = 3.1415927, 0.5235988, np.finfo(float).eps
+    mwa, rhowa, surfw0, rg, grav, cpa, mair = 18.016e-3, 1000., 0.073, 8.314, 9.81, 1005., 28.97e-3
+    diss = {"SO4": 3., "OC": 1., "BC": 0., "DU": 0., "SS": 2.}
+    mm = {"SO4": 98.08e-3, "OC": 150.e-3, "BC": 12.e-3, "DU": 100.e-3, "SS": 58.44e-3}
+    nb, nc, nd, nw = lay.nbins, lay.ncld, lay.ndry, lay.nwet
+    rho = lay.rholiq()
+    act_n, act_v = [0.] * nc, [[0.] * nw for _ in range(nc)]
+    if w <= 0.:
+        return act_n, act_v
+    ns = [sum(diss[lay.species[s]] * vol[k][s] * rho[s] / mm[lay.species[s]] for s in range(nd)) / num[k]
+          if num[k] > 1. else 0. for k in range(nb)]
+    bbr = 6. * mwa / (pi * rhowa)
+    aa = 4. * mwa * surfw0 / (rg * rhowa * T)
+    x = 4. * aa ** 3 / (27. * bbr)
+    scrit = [math.exp(math.sqrt(x / max(eps, n))) - 1. for n in ns]
+    ntot = sum(num[:nb])
+    sum1 = sum(n / s ** (2. / 3.) for n, s in zip(num[:nb], scrit))
+    if ntot < 1.:
+        return act_n, act_v
+    L = 2.501e6 - 2370. * (T - 273.15)
+    a1 = 1. - (373.15 / T)
+    ps = 101325. * math.exp(13.3185 * a1 - 1.976 * a1 ** 2 - 0.6445 * a1 ** 3 - 0.1299 * a1 ** 4)
+    alpha = grav * mwa * L / (cpa * rg * T ** 2) - grav * mair / (rg * T)
+    gamma = rg * T / (ps * mwa) + mwa * L ** 2 / (cpa * P * mair * T)
+    dv1 = 1.e-4 * (0.211 / (P / 101325.)) * ((T / 273.) ** 1.94)
+    ka1 = 1.e-3 * (4.39 + 0.071 * T)
+    gc = 1. / (rhowa * rg * T / (ps * dv1 * mwa) + L * rhowa / (ka1 * T) * (L * mwa / (T * rg) - 1.))
+    s_eff = math.sqrt((ntot / sum1) ** 3)
+    theta = (math.sqrt((alpha * w / gc) ** 3)) / (2. * pi * rhowa * gamma * ntot)
+    khi = (2. / 3.) * aa * math.sqrt(alpha * w / gc)
+    s_max = s_eff / math.sqrt(0.5 * math.sqrt((khi / theta) ** 3) + ((s_eff ** 2) / (theta + 3. * khi)) ** 0.75)
+    dcstar = 2. * aa / (3. * s_max)
+    frac, dcrit, dclo, dchi = [0.] * nb, [0.] * nb, [0.] * nb, [0.] * nb
+    for k in range(nb):
+        if num[k] < 1.:
+            continue
+        vm = pi6 * lay.dmid[k] ** 3
+        nshi, nslo = ns[k] * (lay.vhilim[k] / vm), ns[k] * (lay.vlolim[k] / vm)
+        sil = math.exp(math.sqrt(x / nshi)) - 1.
+        if s_max < sil:
+            continue
+        siu = math.exp(math.sqrt(x / nslo)) - 1.
+        frac[k] = min(1., math.log(s_max / sil) / math.log(siu / sil))
+        dclo[k] = 2. * math.sqrt(3. * nslo * bbr / aa)
+        dchi[k] = 2. * math.sqrt(3. * nshi * bbr / aa)
+        dcrit[k] = 2. * math.sqrt(3. * ns[k] * bbr / aa)
+    bca = next((k for k in range(lay.in1a, lay.fn2a + 1) if 0. < frac[k] < 1.), lay.fn2a)
+    if all(d < eps for d in dcrit):
+        return act_n, act_v
+
+    def intg_n(kk, cc, lo, hi):
+        return 0.5 * kk * max(hi ** 2 - lo ** 2, 0.) + cc * max(hi - lo, 0.)
+
+    def intg_v(kk, cc, lo, hi):
+        return (1. / 3.) * kk * max(hi ** 3 - lo ** 3, 0.) + 0.5 * cc * max(hi ** 2 - lo ** 2, 0.)
+
+    def vdry(k):
+        return sum(vol[k][:nd])
+    vmid = pi6 * lay.dmid[bca] ** 3 if num[bca] < 1. else vdry(bca) / max(1., num[bca])
+    vhi, vlo = lay.vhilim[bca], lay.vlolim[bca]
+    if dcstar >= dcrit[bca]:
+        h = (pi6 * dcstar ** 3 - pi6 * dcrit[bca] ** 3) / max(eps, pi6 * dchi[bca] ** 3 - pi6 * dcrit[bca] ** 3)
+        vcstar = vmid + h * (vhi - vmid)
+    else:
+        h = (pi6 * dcrit[bca] ** 3 - pi6 * dcstar ** 3) / max(eps, pi6 * dcrit[bca] ** 3 - pi6 * dclo[bca] ** 3)
+        vcstar = vmid - h * (vmid - vlo)
+    vcstar = min(max(vcstar, lay.vlolim[bca]), lay.vhilim[bca])
+    for cb in range(nc):
+        ab = lay.cloud_parallel(cb)
+        if num[ab] < 1.:
+            continue
+        nmid = max(num[ab], 1.)
+        vmid = vdry(ab) / nmid
+        vlo, vhi = lay.vlolim[ab], lay.vhilim[ab]
+        if ab in (lay.in1a, lay.in2b):
+            nim1, vim1, vlom1, vhim1 = 1., vlo / 2., 0., vlo
+        else:
+            nim1 = max(num[ab - 1], 1.)
+            vim1 = vdry(ab - 1) / nim1 if nim1 > 1. else pi6 * lay.dmid[ab - 1] ** 3
+            vlom1, vhim1 = lay.vlolim[ab - 1], lay.vhilim[ab - 1]
+        if ab in (lay.fn2a, lay.fn2b):
+            nip1, vip1, vlop1, vhip1 = 1., vhi + 0.5 * (vhi - vlo), vhi, vhi + (vhi - vlo)
+        else:
+            nip1 = max(num[ab + 1], 1.)
+            vip1 = vdry(ab + 1) / nip1 if nip1 > 1. else pi6 * lay.dmid[ab + 1] ** 3
+            vlop1, vhip1 = lay.vlolim[ab + 1], lay.vhilim[ab + 1]
+        vip1 = max(vlop1, min(vip1, vhip1))
+        vim1 = max(vlom1, min(vim1, vhim1))
+        dnim1, dnip1, dnmid = nim1 / (vhim1 - vlom1), nip1 / (vhip1 - vlop1), nmid / (vhi - vlo)
+        zs1 = (dnmid - dnim1) / (vmid - vim1)
+        zs2 = (dnip1 - dnmid) / (vip1 - vmid)
+        n01, n02 = dnmid - zs1 * vmid, dnip1 - zs2 * vip1
+        nnorm = intg_n(zs1, n01, vlo, vmid) + intg_n(zs2, n02, vmid, vhi)
+        vnorm = intg_v(zs1, n01, vlo, vmid) + intg_v(zs2, n02, vmid, vhi)
+        if vcstar < vmid:
+            vint = max(vcstar, vlo)
+            n = (nmid / nnorm) * (intg_n(zs1, n01, vint, vmid) + intg_n(zs2, n02, vmid, vhi))
+            av = (nmid * vmid / vnorm) * (intg_v(zs1, n01, vint, vmid) + intg_v(zs2, n02, vmid, vhi))
+        else:
+            vint = min(vcstar, vhi)
+            n = (nmid / nnorm) * intg_n(zs2, n02, vint, vhi)
+            av = (nmid * vmid / vnorm) * intg_v(zs2, n02, vint, vhi)
+        act_n[cb] = max(0., n)
+        act_v[cb] = [max(0., av * (vol[ab][s] / (vmid * nmid))) for s in range(nw)]
+        act_v[cb][nw - 1] = act_n[cb] * pi6 * (dcrit[ab] ** 3) * min(2., (3.e-6 / max(eps, dcrit[ab])) ** 2)
+    return act_n, act_v
+
+
+def test_cloud_base_activation_matches_independent_restatement():
+    """lsactiv mode 2 alone: the oracle's newly activated droplets (pa_nactd, pa_vactd)
+    after one step against the restatement above, on the updraft cells of a
+    grid384x384x160 block (1e-9)."""
+    cfg = workload_config(5)
+    for sw in (cfg.lscoag, cfg.lscnd, cfg.lsauto, cfg.lsicenucl, cfg.lsicemelt):
+        sw.sw = 0
+    cfg.lsdistupdate = 0
+    cfg.lsactiv.sw, cfg.lsactiv.mode = 1, 2
+    inp = make_inputs("grid384x384x160", "cpu", X=6, Y=6, Z=4)
+    inp.cfg = cfg
+    lay = build_layout(cfg)
+    nw, nb, nc = lay.nwet, lay.nbins, lay.ncld
+    f = inp.fields
+    fields = {key: v.clone() for key, v in f.items()}
+    out = make_outputs(inp)
+    rc, _ = Oracle(cfg).run(inp, fields, out, time=1.0)
+    assert rc == 0
+    sh = f["naero"].shape[1:]
+    rho = lay.rholiq()
+    ma = f["maero"].view(nw, nb, *sh)
+    pv = out["pa_vactd"].view(nw, nc, *sh)
+    up = 0
+    for j in range(2, inp.nyp - 2):
+        for i in range(2, inp.nxp - 2):
+            for k in range(1, inp.nzp - 1):
+                dn = float(f["dn"][j, i, k])
+                num = [float(f["naero"][b, j, i, k]) * dn for b in range(nb)]
+                vol = [[float(ma[s, b, j, i, k]) * dn / rho[s] for s in range(nw)] for b in range(nb)]
+                w = float(f["wp"][j, i, k])
+                an, av = act_cloudbase_numpy(num, vol, float(f["temp"][j, i, k]), float(f["press"][j, i, k]), w, lay)
+                up += w > 0. and sum(an) > 0.
+                for cb in range(nc):
+                    got = float(out["pa_nactd"][cb, j, i, k]) * dn
+                    assert got == pytest.approx(an[cb], rel=1e-9, abs=1e-300), (j, i, k, cb)
+                    for s in range(nw):
+                        got = float(pv[s, cb, j, i, k]) * dn / rho[s]
+                        assert got == pytest.approx(av[cb][s], rel=1e-9, abs=1e-300), (j, i, k, cb, s)
+    assert up >= 20, up
+
+
 def coag_cloud_numpy(num, vol, lay, T, P, dt):
     """Cloud self-collection (lscgcc alone, autoconversion off): buildKernelSelf over the
     cloud bins (dlim 100 um; coagc's offset for equal mid diameters, the parallel a and
